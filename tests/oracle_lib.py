@@ -1,0 +1,120 @@
+"""ctypes binding of the CPU oracle (oracle/_build/liboracle.so).
+
+Test infrastructure: the oracle restates zml's Zig loop nests in C and is the
+parity reference for every GPU routine.  Only tests, smoke() and bench.py's
+CPU-baseline leg load it.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
+
+_lib = None
+
+i32, f64, f32, vp = C.c_int, C.c_double, C.c_float, C.c_void_p
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
+        _lib = C.CDLL(LIB_PATH)
+        for pfx, T in (("zo_d_", f64), ("zo_s_", f32)):
+            sig = {
+                "gemm": (i32, [i32, i32, i32, i32, i32, i32, T, vp, i32, vp, i32, T, vp, i32]),
+                "trsm": (i32, [i32, i32, i32, i32, i32, i32, i32, T, vp, i32, vp, i32]),
+                "trmm": (i32, [i32, i32, i32, i32, i32, i32, i32, T, vp, i32, vp, i32]),
+                "syrk": (i32, [i32, i32, i32, i32, i32, T, vp, i32, T, vp, i32]),
+                "gemv": (i32, [i32, i32, i32, i32, T, vp, i32, vp, i32, T, vp, i32]),
+                "ger": (i32, [i32, i32, i32, T, vp, i32, vp, i32, vp, i32]),
+                "iamax": (i32, [i32, vp, i32]),
+                "scal": (i32, [i32, T, vp, i32]),
+                "nrm2": (T, [i32, vp, i32]),
+                "lamch": (T, [C.c_char]),
+                "laswp": (i32, [i32, i32, vp, i32, i32, i32, vp, i32]),
+                "getrf2": (i32, [i32, i32, i32, vp, i32, vp]),
+                "getrf": (i32, [i32, i32, i32, vp, i32, vp]),
+                "getrs": (i32, [i32, i32, i32, i32, vp, i32, vp, vp, i32]),
+                "gesv": (i32, [i32, i32, i32, vp, i32, vp, vp, i32]),
+                "potrf2": (i32, [i32, i32, i32, vp, i32]),
+                "potrf": (i32, [i32, i32, i32, vp, i32]),
+                "potrs": (i32, [i32, i32, i32, i32, vp, i32, vp, i32]),
+                "posv": (i32, [i32, i32, i32, i32, vp, i32, vp, i32]),
+                "geqr2": (i32, [i32, i32, i32, vp, i32, vp, vp]),
+                "geqrf": (i32, [i32, i32, i32, vp, i32, vp, vp, i32]),
+                "larft": (i32, [i32, i32, i32, i32, i32, vp, i32, vp, vp, i32]),
+                "larfg": (i32, [i32, vp, vp, i32, vp]),
+            }
+            for name, (res, args) in sig.items():
+                fn = getattr(_lib, pfx + name)
+                fn.restype, fn.argtypes = res, args
+        _lib.zo_set_trsm_as_written.argtypes = [i32]
+        _lib.zo_ilaenv.argtypes = [i32, C.c_char_p, i32, i32, i32, i32]
+        _lib.zo_ilaenv.restype = i32
+    return _lib
+
+
+def ptr(a):
+    return a.ctypes.data_as(vp) if a is not None else None
+
+
+def fn(name, dtype=np.float64):
+    return getattr(load(), ("zo_d_" if dtype == np.float64 else "zo_s_") + name)
+
+
+# ---- numpy-level conveniences (column-major, Fortran-ordered arrays) --------
+
+def getrf(a, order=102):
+    """LU of a copy of `a` (F-ordered for col-major); returns (lu, ipiv, info)."""
+    a = np.array(a, dtype=a.dtype, order="F" if order == 102 else "C", copy=True)
+    m, n = a.shape
+    lda = m if order == 102 else n
+    ipiv = np.zeros(min(m, n), dtype=np.int32)
+    info = fn("getrf", a.dtype)(order, m, n, ptr(a), max(1, lda), ptr(ipiv))
+    return a, ipiv, info
+
+
+def getrs(lu, ipiv, b, trans=111):
+    b = np.array(b, dtype=lu.dtype, order="F", copy=True)
+    if b.ndim == 1:
+        b = b.reshape(-1, 1, order="F")
+    n, nrhs = b.shape
+    r = fn("getrs", lu.dtype)(102, trans, n, nrhs, ptr(lu), max(1, n), ptr(ipiv), ptr(b), max(1, n))
+    assert r == 0
+    return b
+
+
+def potrf(a, uplo=122):
+    a = np.array(a, dtype=a.dtype, order="F", copy=True)
+    n = a.shape[0]
+    info = fn("potrf", a.dtype)(102, uplo, n, ptr(a), max(1, n))
+    return a, info
+
+
+def potrs(l, b, uplo=122):
+    b = np.array(b, dtype=l.dtype, order="F", copy=True)
+    if b.ndim == 1:
+        b = b.reshape(-1, 1, order="F")
+    n, nrhs = b.shape
+    r = fn("potrs", l.dtype)(102, uplo, n, nrhs, ptr(l), max(1, n), ptr(b), max(1, n))
+    assert r == 0
+    return b
+
+
+def geqrf(a):
+    a = np.array(a, dtype=a.dtype, order="F", copy=True)
+    m, n = a.shape
+    tau = np.zeros(max(1, min(m, n)), dtype=a.dtype)
+    q = np.zeros(1, dtype=a.dtype)
+    f = fn("geqrf", a.dtype)
+    assert f(102, m, n, ptr(a), max(1, m), ptr(tau), ptr(q), -1) == 0
+    lwork = max(1, int(q[0]))
+    work = np.zeros(lwork, dtype=a.dtype)
+    r = f(102, m, n, ptr(a), max(1, m), ptr(tau), ptr(work), lwork)
+    assert r == 0
+    return a, tau
