@@ -1,0 +1,90 @@
+/*
+ * clapack.h -- dense factor-and-solve of libzml_gb300 (GB300, sm_103a).
+ *
+ * The reference's include/clapack.h is an empty shell (clapack.h:1-12); the
+ * LAPACK C signatures zml itself uses are the LAPACKE ones it calls when
+ * built with -Dlink_lapacke (src/linalg/lapack.zig:1169, 1575, 2103, 3012,
+ * 3466, 3948, 5121).  This header declares exactly those, so zml's
+ * LAPACK dispatch (lapack.zig) can be pointed at this library, plus
+ * GPU extensions below.
+ *
+ * Conventions (LAPACKE): layout is LAPACK_ROW_MAJOR (101) or
+ * LAPACK_COL_MAJOR (102); the return value is 0, -(index of the first bad
+ * argument), or the positive LAPACK info (first zero pivot for getrf, first
+ * non-positive leading minor for potrf).  ipiv is 1-based.  Library failures
+ * return codes <= -1000; zml_gpu_last_error() describes them.
+ *
+ * Pointers may be host memory (staged to the GPU and back) or device /
+ * managed memory (used in place).  Calls are synchronous.
+ */
+#ifndef ZML_GB300_CLAPACK_H
+#define ZML_GB300_CLAPACK_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LAPACK_ROW_MAJOR 101
+#define LAPACK_COL_MAJOR 102
+
+#define ZML_GPU_ERR_CUDA (-1001)
+#define ZML_GPU_ERR_ALLOC (-1002)
+#define ZML_GPU_ERR_NODEVICE (-1003)
+#define ZML_GPU_ERR_TIMEOUT (-1004)
+#define ZML_GPU_ERR_INVALID (-1005)
+
+/* ---- LAPACKE-shaped drop-ins ------------------------------------------- */
+/* replaces zml.linalg.lapack.getrf (lapack.zig:1130; kernel lapack/getrf.zig:14) */
+int LAPACKE_dgetrf(int matrix_layout, int m, int n, double *a, int lda, int *ipiv);
+int LAPACKE_sgetrf(int matrix_layout, int m, int n, float *a, int lda, int *ipiv);
+/* replaces zml.linalg.lapack.getrs (lapack.zig:1517; kernel lapack/getrs.zig:13) */
+int LAPACKE_dgetrs(int matrix_layout, char trans, int n, int nrhs, const double *a, int lda,
+                   const int *ipiv, double *b, int ldb);
+int LAPACKE_sgetrs(int matrix_layout, char trans, int n, int nrhs, const float *a, int lda,
+                   const int *ipiv, float *b, int ldb);
+/* replaces zml.linalg.lapack.gesv (lapack.zig:2051; kernel lapack/gesv.zig:13) */
+int LAPACKE_dgesv(int matrix_layout, int n, int nrhs, double *a, int lda, int *ipiv, double *b,
+                  int ldb);
+int LAPACKE_sgesv(int matrix_layout, int n, int nrhs, float *a, int lda, int *ipiv, float *b,
+                  int ldb);
+/* replaces zml.linalg.lapack.potrf (lapack.zig:2975; kernel lapack/potrf.zig:17) */
+int LAPACKE_dpotrf(int matrix_layout, char uplo, int n, double *a, int lda);
+int LAPACKE_spotrf(int matrix_layout, char uplo, int n, float *a, int lda);
+/* replaces zml.linalg.lapack.potrs (lapack.zig:3412; kernel lapack/potrs.zig:15) */
+int LAPACKE_dpotrs(int matrix_layout, char uplo, int n, int nrhs, const double *a, int lda,
+                   double *b, int ldb);
+int LAPACKE_spotrs(int matrix_layout, char uplo, int n, int nrhs, const float *a, int lda,
+                   float *b, int ldb);
+/* replaces zml.linalg.lapack.posv (lapack.zig:3896; kernel lapack/posv.zig:15) */
+int LAPACKE_dposv(int matrix_layout, char uplo, int n, int nrhs, double *a, int lda, double *b,
+                  int ldb);
+int LAPACKE_sposv(int matrix_layout, char uplo, int n, int nrhs, float *a, int lda, float *b,
+                  int ldb);
+
+/* ---- GPU extensions: device pointers, column-major, stream ordered ------
+ * `stream` is a cudaStream_t (NULL = legacy default stream).  The call
+ * returns after the stream has drained (info is a host value). */
+/* device-pointer form of getrf (lapack/getrf.zig:14) */
+int zml_gpu_dgetrf(int m, int n, double *dA, int ldda, int *dipiv, int *info, void *stream);
+/* device-pointer form of getrs (lapack/getrs.zig:13) */
+int zml_gpu_dgetrs(char trans, int n, int nrhs, const double *dA, int ldda, const int *dipiv,
+                   double *dB, int lddb, void *stream);
+/* device-pointer form of potrf (lapack/potrf.zig:17) */
+int zml_gpu_dpotrf(char uplo, int n, double *dA, int ldda, int *info, void *stream);
+/* device-pointer form of potrs (lapack/potrs.zig:15) */
+int zml_gpu_dpotrs(char uplo, int n, int nrhs, const double *dA, int ldda, double *dB, int lddb,
+                   void *stream);
+/* device-pointer form of gemm (blas/gemm.zig:14), CBLAS transpose codes */
+int zml_gpu_dgemm(int transa, int transb, int m, int n, int k, double alpha, const double *dA,
+                  int ldda, const double *dB, int lddb, double beta, double *dC, int lddc,
+                  void *stream);
+
+/* Text of the last library error on this thread. */
+const char *zml_gpu_last_error(void);
+/* ABI version of this library. */
+int zml_gpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

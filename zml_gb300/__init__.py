@@ -1,0 +1,87 @@
+"""zml_gb300 -- GB300-native dense factor-and-solve behind zml's C ABI.
+
+The product is the shared library zml_gb300/lib/libzml_gb300.so, whose C
+entry points are declared in include/cblas.h and include/clapack.h.  This
+module is the Python-side loader used by the tests and the benchmark: it
+binds every declared entry point through ctypes and fails loudly when the
+library has not been built (there is no CPU fallback).
+"""
+import ctypes as C
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB_PATH = os.path.join(HERE, "lib", "libzml_gb300.so")
+INCLUDE = os.path.join(ROOT, "include")
+
+ROW_MAJOR, COL_MAJOR = 101, 102
+NO_TRANS, TRANS, CONJ_TRANS, CONJ_NO_TRANS = 111, 112, 113, 114
+UPPER, LOWER = 121, 122
+NON_UNIT, UNIT = 131, 132
+LEFT, RIGHT = 141, 142
+
+i32, f64, f32, vp, ch = C.c_int, C.c_double, C.c_float, C.c_void_p, C.c_char
+
+_SIGS = {}
+for p, T in (("d", f64), ("s", f32)):
+    _SIGS.update({
+        "cblas_%sgemm" % p: (None, [i32, i32, i32, i32, i32, i32, T, vp, i32, vp, i32, T, vp, i32]),
+        "cblas_%ssyrk" % p: (None, [i32, i32, i32, i32, i32, T, vp, i32, T, vp, i32]),
+        "cblas_%strsm" % p: (None, [i32, i32, i32, i32, i32, i32, i32, T, vp, i32, vp, i32]),
+        "LAPACKE_%sgetrf" % p: (i32, [i32, i32, i32, vp, i32, vp]),
+        "LAPACKE_%sgetrs" % p: (i32, [i32, ch, i32, i32, vp, i32, vp, vp, i32]),
+        "LAPACKE_%sgesv" % p: (i32, [i32, i32, i32, vp, i32, vp, vp, i32]),
+        "LAPACKE_%spotrf" % p: (i32, [i32, ch, i32, vp, i32]),
+        "LAPACKE_%spotrs" % p: (i32, [i32, ch, i32, i32, vp, i32, vp, i32]),
+        "LAPACKE_%sposv" % p: (i32, [i32, ch, i32, i32, vp, i32, vp, i32]),
+    })
+_SIGS.update({
+    "zml_gpu_dgetrf": (i32, [i32, i32, vp, i32, vp, vp, vp]),
+    "zml_gpu_dgetrs": (i32, [ch, i32, i32, vp, i32, vp, vp, i32, vp]),
+    "zml_gpu_dpotrf": (i32, [ch, i32, vp, i32, vp, vp]),
+    "zml_gpu_dpotrs": (i32, [ch, i32, i32, vp, i32, vp, i32, vp]),
+    "zml_gpu_dgemm": (i32, [i32, i32, i32, i32, i32, f64, vp, i32, vp, i32, f64, vp, i32, vp]),
+    "zml_gpu_last_error": (C.c_char_p, []),
+    "zml_gpu_version": (i32, []),
+})
+
+_lib = None
+
+
+class NotBuiltError(RuntimeError):
+    pass
+
+
+def declared_symbols():
+    """Every function name declared in include/*.h."""
+    names = []
+    for h in sorted(os.listdir(INCLUDE)):
+        if not h.endswith(".h"):
+            continue
+        txt = open(os.path.join(INCLUDE, h)).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w\s\*]*?\b(\w+)\s*\(", txt, flags=re.M):
+            name = m.group(1)
+            if name not in ("if", "defined") and not txt[m.start():m.end()].startswith("typedef"):
+                names.append(name)
+    return names
+
+
+def lib():
+    """The loaded library with argtypes set; raises NotBuiltError if absent."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise NotBuiltError("%s missing: run python -c 'import __graft_entry__ as g; g.build()'"
+                                % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype, f.argtypes = res, args
+        _lib = L
+    return _lib
+
+
+def last_error():
+    return lib().zml_gpu_last_error().decode()

@@ -1,0 +1,472 @@
+// capi.cu -- the C ABI of libzml_gb300 (include/cblas.h, include/clapack.h).
+//
+// cblas_* keep the reference prototypes (reference include/cblas.h:216-253,
+// implemented in src/cblas.zig:523-638) and its behaviour: row-major calls
+// are mapped to column-major by the index swaps of blas/gemm.zig:48-65,
+// trsm.zig:48-63 and syrk.zig:28-57; invalid arguments return silently
+// (cblas.zig forwards to zml.linalg.blas.d*, which swallows the error).
+//
+// LAPACKE_* take the LAPACKE signatures the reference itself calls when
+// linked against a system LAPACKE (lapack.zig:1169, 1575, 2103, 3012, 3466,
+// 3948, 5121) and return LAPACKE's info: 0, -(index of the bad argument), or
+// a positive numerical info.  Row-major matrices are transposed on the
+// device, factored column-major and transposed back (the logical matrix is
+// the same one zml factors with its row-major indexing).
+//
+// Every pointer may be host memory (staged through device workspaces) or
+// device / managed memory (used in place).  Calls are synchronous.
+#include <cstring>
+
+#include "common.cuh"
+#include "kernels.h"
+
+using namespace zg;
+
+namespace {
+
+cudaStream_t lib_stream() {
+  static thread_local cudaStream_t s = nullptr;
+  static thread_local int dev = -1;
+  int d = 0;
+  cudaGetDevice(&d);
+  if (!s || d != dev) {
+    cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    dev = d;
+  }
+  return s;
+}
+
+bool is_device_ptr(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// A column-major rows x cols operand that lives on the device for the call.
+template <typename T> struct Staged {
+  T *d = nullptr;
+  long ld = 0;
+  const T *host = nullptr;
+  long host_ld = 0;
+  int rows = 0, cols = 0;
+  bool staged = false;
+
+  int in(const T *p, long ldp, int r, int c, int slot, bool copy, cudaStream_t s) {
+    rows = r; cols = c; host = p; host_ld = ldp;
+    if (r <= 0 || c <= 0) return 0;
+    if (is_device_ptr(p)) {
+      d = const_cast<T *>(p);
+      ld = ldp;
+      return 0;
+    }
+    void *w;
+    ZG_TRY(workspace(s, slot, sizeof(T) * (size_t)r * c, &w));
+    d = (T *)w;
+    ld = r;
+    staged = true;
+    if (copy)
+      ZG_CUDA(cudaMemcpy2DAsync(d, sizeof(T) * r, p, sizeof(T) * ldp, sizeof(T) * r, c,
+                                cudaMemcpyHostToDevice, s));
+    return 0;
+  }
+  int out(cudaStream_t s) {
+    if (staged && rows > 0 && cols > 0)
+      ZG_CUDA(cudaMemcpy2DAsync(const_cast<T *>(host), sizeof(T) * host_ld, d, sizeof(T) * ld,
+                                sizeof(T) * rows, cols, cudaMemcpyDeviceToHost, s));
+    return 0;
+  }
+};
+
+template <typename T> struct Buf {  // small host-or-device vector
+  T *d = nullptr;
+  T *host = nullptr;
+  long n = 0;
+  bool staged = false;
+  int in(T *p, long cnt, int slot, bool copy, cudaStream_t s) {
+    host = p; n = cnt;
+    if (cnt <= 0) return 0;
+    if (is_device_ptr(p)) { d = p; return 0; }
+    void *w;
+    ZG_TRY(workspace(s, slot, sizeof(T) * cnt, &w));
+    d = (T *)w;
+    staged = true;
+    if (copy) ZG_CUDA(cudaMemcpyAsync(d, p, sizeof(T) * cnt, cudaMemcpyHostToDevice, s));
+    return 0;
+  }
+  int out(cudaStream_t s) {
+    if (staged && n > 0) ZG_CUDA(cudaMemcpyAsync(host, d, sizeof(T) * n, cudaMemcpyDeviceToHost, s));
+    return 0;
+  }
+};
+
+int sync(cudaStream_t s) {
+  ZG_CUDA(cudaStreamSynchronize(s));
+  return 0;
+}
+
+bool is_trans(int t) { return t == kNoTrans || t == kTrans || t == kConjTrans || t == kConjNoTrans; }
+int trans_invert(int t) {
+  switch (t) {
+    case kNoTrans: return kTrans;
+    case kTrans: return kNoTrans;
+    case kConjNoTrans: return kConjTrans;
+    default: return kConjNoTrans;
+  }
+}
+
+// ---- BLAS level 3 ----------------------------------------------------------
+
+template <typename T>
+int gemm_any(int order, int ta, int tb, int m, int n, int k, T alpha, const T *a, int lda,
+             const T *b, int ldb, T beta, T *c, int ldc) {
+  if (order != kRowMajor && order != kColMajor) return kErrInvalid;
+  if (!is_trans(ta) || !is_trans(tb)) return kErrInvalid;
+  if (order == kRowMajor) {  // gemm.zig:48-65
+    std::swap(ta, tb); std::swap(m, n); std::swap(a, b); std::swap(lda, ldb);
+  }
+  const bool nota = ta == kNoTrans || ta == kConjNoTrans;
+  const bool notb = tb == kNoTrans || tb == kConjNoTrans;
+  const int nrowa = nota ? m : k, ncola = nota ? k : m;
+  const int nrowb = notb ? k : n, ncolb = notb ? n : k;
+  if (m < 0 || n < 0 || k < 0 || lda < std::max(1, nrowa) || ldb < std::max(1, nrowb) ||
+      ldc < std::max(1, m))
+    return kErrInvalid;  // gemm.zig:101-102
+  if (m == 0 || n == 0 || ((alpha == T(0) || k == 0) && beta == T(1))) return 0;
+  cudaStream_t s = lib_stream();
+  Staged<T> A, B, C;
+  const bool use_ab = alpha != T(0) && k > 0;
+  if (use_ab) {
+    ZG_TRY(A.in(a, lda, nrowa, ncola, 0, true, s));
+    ZG_TRY(B.in(b, ldb, nrowb, ncolb, 1, true, s));
+  }
+  ZG_TRY(C.in(c, ldc, m, n, 2, beta != T(0), s));
+  ZG_TRY(gemm_simt<T>(ta, tb, m, n, use_ab ? k : 0, alpha, A.d, A.ld ? A.ld : 1, B.d,
+                      B.ld ? B.ld : 1, beta, C.d, C.ld, 0, s));
+  ZG_TRY(C.out(s));
+  return sync(s);
+}
+
+template <typename T>
+int syrk_any(int order, int uplo, int trans, int n, int k, T alpha, const T *a, int lda, T beta,
+             T *c, int ldc) {
+  if (order != kRowMajor && order != kColMajor) return kErrInvalid;
+  if (uplo != kUpper && uplo != kLower) return kErrInvalid;
+  if (!is_trans(trans)) return kErrInvalid;
+  if (order == kRowMajor) {  // syrk.zig:28-57
+    uplo = uplo == kUpper ? kLower : kUpper;
+    trans = trans_invert(trans);
+  }
+  const int nrowa = trans == kNoTrans ? n : k;
+  if (trans == kConjNoTrans || trans == kConjTrans || n < 0 || k < 0 ||
+      lda < std::max(1, nrowa) || ldc < std::max(1, n))
+    return kErrInvalid;  // syrk.zig:82-84
+  if (n == 0 || ((alpha == T(0) || k == 0) && beta == T(1))) return 0;
+  cudaStream_t s = lib_stream();
+  Staged<T> A, C;
+  const bool use_a = alpha != T(0) && k > 0;
+  if (use_a) ZG_TRY(A.in(a, lda, nrowa, trans == kNoTrans ? k : n, 0, true, s));
+  // C: the whole n x n square is staged so that the other triangle survives
+  ZG_TRY(C.in(c, ldc, n, n, 2, true, s));
+  if (use_a)
+    ZG_TRY(syrk_dev<T>(uplo, trans, n, k, alpha, A.d, A.ld, beta, C.d, C.ld, s));
+  else
+    ZG_TRY(gemm_simt<T>(kNoTrans, kNoTrans, n, n, 0, T(0), C.d, C.ld, C.d, C.ld, beta, C.d, C.ld,
+                        uplo == kLower ? 1 : 2, s));
+  ZG_TRY(C.out(s));
+  return sync(s);
+}
+
+template <typename T>
+int trsm_any(int order, int side, int uplo, int ta, int diag, int m, int n, T alpha, const T *a,
+             int lda, T *b, int ldb) {
+  if (order != kRowMajor && order != kColMajor) return kErrInvalid;
+  if ((side != kLeft && side != kRight) || (uplo != kUpper && uplo != kLower) || !is_trans(ta) ||
+      (diag != kUnit && diag != kNonUnit))
+    return kErrInvalid;
+  if (order == kRowMajor) {  // trsm.zig:48-63
+    side = side == kLeft ? kRight : kLeft;
+    uplo = uplo == kUpper ? kLower : kUpper;
+    std::swap(m, n);
+  }
+  const int nrowa = side == kLeft ? m : n;
+  if (m < 0 || n < 0 || lda < std::max(1, nrowa) || ldb < std::max(1, m)) return kErrInvalid;
+  if (m == 0 || n == 0) return 0;
+  cudaStream_t s = lib_stream();
+  Staged<T> A, B;
+  if (alpha != T(0)) ZG_TRY(A.in(a, lda, nrowa, nrowa, 0, true, s));
+  ZG_TRY(B.in(b, ldb, m, n, 1, alpha != T(0), s));
+  ZG_TRY(trsm_dev<T>(side, uplo, ta, diag, m, n, alpha, A.d, A.ld, B.d, B.ld, s));
+  ZG_TRY(B.out(s));
+  return sync(s);
+}
+
+// ---- LAPACK ------------------------------------------------------------------
+
+int lay_ok(int layout) { return layout == kRowMajor || layout == kColMajor; }
+
+// Brings a (possibly row-major) r x c matrix to a column-major device copy.
+template <typename T> struct ColMajor {
+  Staged<T> st;     // the caller's storage as it is
+  T *d = nullptr;   // column-major view
+  long ld = 0;
+  bool transposed = false;
+  int in(int layout, const T *p, int ldp, int r, int c, int slot, int tslot, bool copy,
+         cudaStream_t s) {
+    if (layout == kColMajor) {
+      ZG_TRY(st.in(p, ldp, r, c, slot, copy, s));
+      d = st.d;
+      ld = st.ld;
+      return 0;
+    }
+    // row-major r x c == column-major c x r with leading dimension ldp
+    ZG_TRY(st.in(p, ldp, c, r, slot, copy, s));
+    void *w;
+    ZG_TRY(workspace(s, tslot, sizeof(T) * (size_t)std::max(1, r) * std::max(1, c), &w));
+    d = (T *)w;
+    ld = std::max(1, r);
+    transposed = true;
+    if (copy) ZG_TRY(transpose_dev<T>(c, r, st.d, st.ld, d, ld, s));
+    return 0;
+  }
+  int out(cudaStream_t s) {
+    if (transposed) ZG_TRY(transpose_dev<T>(st.cols, st.rows, d, ld, st.d, st.ld, s));
+    return st.out(s);
+  }
+};
+
+char up(char c) { return (c >= 'a' && c <= 'z') ? (char)(c - 32) : c; }
+
+template <typename T> int getrf_any(int layout, int m, int n, T *a, int lda, int *ipiv) {
+  if (!lay_ok(layout)) return -1;
+  if (m < 0) return -2;
+  if (n < 0) return -3;
+  if (lda < std::max(1, layout == kColMajor ? m : n)) return -5;
+  if (m == 0 || n == 0) return 0;
+  cudaStream_t s = lib_stream();
+  ColMajor<T> A;
+  Buf<int> P;
+  ZG_TRY(A.in(layout, a, lda, m, n, 0, 1, true, s));
+  ZG_TRY(P.in(ipiv, std::min(m, n), 2, false, s));
+  int info = 0;
+  ZG_TRY(getrf_dev<T>(m, n, A.d, A.ld, P.d, &info, s));
+  ZG_TRY(A.out(s));
+  ZG_TRY(P.out(s));
+  ZG_TRY(sync(s));
+  return info;
+}
+
+template <typename T>
+int getrs_any(int layout, char trans, int n, int nrhs, const T *a, int lda, const int *ipiv, T *b,
+              int ldb) {
+  if (!lay_ok(layout)) return -1;
+  trans = up(trans);
+  if (trans != 'N' && trans != 'T' && trans != 'C') return -2;
+  if (n < 0) return -3;
+  if (nrhs < 0) return -4;
+  if (lda < std::max(1, n)) return -6;
+  if (ldb < std::max(1, layout == kColMajor ? n : nrhs)) return -9;
+  if (n == 0 || nrhs == 0) return 0;
+  cudaStream_t s = lib_stream();
+  ColMajor<T> A, B;
+  Buf<int> P;
+  ZG_TRY(A.in(layout, a, lda, n, n, 0, 1, true, s));
+  ZG_TRY(B.in(layout, b, ldb, n, nrhs, 2, 3, true, s));
+  ZG_TRY(P.in(const_cast<int *>(ipiv), n, 4, true, s));
+  ZG_TRY(getrs_dev<T>(trans == 'N' ? kNoTrans : kTrans, n, nrhs, A.d, A.ld, P.d, B.d, B.ld, s));
+  ZG_TRY(B.out(s));
+  ZG_TRY(sync(s));
+  return 0;
+}
+
+template <typename T>
+int gesv_any(int layout, int n, int nrhs, T *a, int lda, int *ipiv, T *b, int ldb) {
+  if (!lay_ok(layout)) return -1;
+  if (n < 0) return -2;
+  if (nrhs < 0) return -3;
+  if (lda < std::max(1, n)) return -5;
+  if (ldb < std::max(1, layout == kColMajor ? n : nrhs)) return -8;
+  if (n == 0 || nrhs == 0) return 0;
+  cudaStream_t s = lib_stream();
+  ColMajor<T> A, B;
+  Buf<int> P;
+  ZG_TRY(A.in(layout, a, lda, n, n, 0, 1, true, s));
+  ZG_TRY(B.in(layout, b, ldb, n, nrhs, 2, 3, true, s));
+  ZG_TRY(P.in(ipiv, n, 4, false, s));
+  int info = 0;
+  ZG_TRY(getrf_dev<T>(n, n, A.d, A.ld, P.d, &info, s));
+  if (info == 0) ZG_TRY(getrs_dev<T>(kNoTrans, n, nrhs, A.d, A.ld, P.d, B.d, B.ld, s));
+  ZG_TRY(A.out(s));
+  ZG_TRY(P.out(s));
+  if (info == 0) ZG_TRY(B.out(s));
+  ZG_TRY(sync(s));
+  return info;
+}
+
+template <typename T> int potrf_any(int layout, char uplo, int n, T *a, int lda) {
+  if (!lay_ok(layout)) return -1;
+  uplo = up(uplo);
+  if (uplo != 'U' && uplo != 'L') return -2;
+  if (n < 0) return -3;
+  if (lda < std::max(1, n)) return -5;
+  if (n == 0) return 0;
+  cudaStream_t s = lib_stream();
+  ColMajor<T> A;
+  ZG_TRY(A.in(layout, a, lda, n, n, 0, 1, true, s));
+  int info = 0;
+  ZG_TRY(potrf_dev<T>(uplo == 'L' ? kLower : kUpper, n, A.d, A.ld, &info, s));
+  ZG_TRY(A.out(s));
+  ZG_TRY(sync(s));
+  return info;
+}
+
+template <typename T>
+int potrs_any(int layout, char uplo, int n, int nrhs, const T *a, int lda, T *b, int ldb) {
+  if (!lay_ok(layout)) return -1;
+  uplo = up(uplo);
+  if (uplo != 'U' && uplo != 'L') return -2;
+  if (n < 0) return -3;
+  if (nrhs < 0) return -4;
+  if (lda < std::max(1, n)) return -6;
+  if (ldb < std::max(1, layout == kColMajor ? n : nrhs)) return -8;
+  if (n == 0 || nrhs == 0) return 0;
+  cudaStream_t s = lib_stream();
+  ColMajor<T> A, B;
+  ZG_TRY(A.in(layout, a, lda, n, n, 0, 1, true, s));
+  ZG_TRY(B.in(layout, b, ldb, n, nrhs, 2, 3, true, s));
+  ZG_TRY(potrs_dev<T>(uplo == 'L' ? kLower : kUpper, n, nrhs, A.d, A.ld, B.d, B.ld, s));
+  ZG_TRY(B.out(s));
+  ZG_TRY(sync(s));
+  return 0;
+}
+
+template <typename T>
+int posv_any(int layout, char uplo, int n, int nrhs, T *a, int lda, T *b, int ldb) {
+  if (!lay_ok(layout)) return -1;
+  uplo = up(uplo);
+  if (uplo != 'U' && uplo != 'L') return -2;
+  if (n < 0) return -3;
+  if (nrhs < 0) return -4;
+  if (lda < std::max(1, n)) return -6;
+  if (ldb < std::max(1, layout == kColMajor ? n : nrhs)) return -8;
+  if (n == 0 || nrhs == 0) return 0;
+  cudaStream_t s = lib_stream();
+  ColMajor<T> A, B;
+  ZG_TRY(A.in(layout, a, lda, n, n, 0, 1, true, s));
+  ZG_TRY(B.in(layout, b, ldb, n, nrhs, 2, 3, true, s));
+  const int ul = uplo == 'L' ? kLower : kUpper;
+  int info = 0;
+  ZG_TRY(potrf_dev<T>(ul, n, A.d, A.ld, &info, s));
+  if (info == 0) ZG_TRY(potrs_dev<T>(ul, n, nrhs, A.d, A.ld, B.d, B.ld, s));
+  ZG_TRY(A.out(s));
+  if (info == 0) ZG_TRY(B.out(s));
+  ZG_TRY(sync(s));
+  return info;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---- CBLAS (include/cblas.h) ----
+#define CBLAS_GEMM(P, T)                                                                          \
+  void cblas_##P##gemm(int order, int ta, int tb, int m, int n, int k, T alpha, const T *a,        \
+                       int lda, const T *b, int ldb, T beta, T *c, int ldc) {                      \
+    gemm_any<T>(order, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc);                      \
+  }                                                                                                \
+  void cblas_##P##syrk(int order, int uplo, int trans, int n, int k, T alpha, const T *a, int lda, \
+                       T beta, T *c, int ldc) {                                                    \
+    syrk_any<T>(order, uplo, trans, n, k, alpha, a, lda, beta, c, ldc);                            \
+  }                                                                                                \
+  void cblas_##P##trsm(int order, int side, int uplo, int ta, int diag, int m, int n, T alpha,     \
+                       const T *a, int lda, T *b, int ldb) {                                       \
+    trsm_any<T>(order, side, uplo, ta, diag, m, n, alpha, a, lda, b, ldb);                         \
+  }
+CBLAS_GEMM(d, double)
+CBLAS_GEMM(s, float)
+#undef CBLAS_GEMM
+
+// ---- LAPACKE-shaped (include/clapack.h) ----
+#define LAPACKE_FNS(P, T)                                                                        \
+  int LAPACKE_##P##getrf(int layout, int m, int n, T *a, int lda, int *ipiv) {                   \
+    return getrf_any<T>(layout, m, n, a, lda, ipiv);                                             \
+  }                                                                                               \
+  int LAPACKE_##P##getrs(int layout, char trans, int n, int nrhs, const T *a, int lda,           \
+                         const int *ipiv, T *b, int ldb) {                                       \
+    return getrs_any<T>(layout, trans, n, nrhs, a, lda, ipiv, b, ldb);                           \
+  }                                                                                               \
+  int LAPACKE_##P##gesv(int layout, int n, int nrhs, T *a, int lda, int *ipiv, T *b, int ldb) {  \
+    return gesv_any<T>(layout, n, nrhs, a, lda, ipiv, b, ldb);                                   \
+  }                                                                                               \
+  int LAPACKE_##P##potrf(int layout, char uplo, int n, T *a, int lda) {                          \
+    return potrf_any<T>(layout, uplo, n, a, lda);                                                \
+  }                                                                                               \
+  int LAPACKE_##P##potrs(int layout, char uplo, int n, int nrhs, const T *a, int lda, T *b,      \
+                         int ldb) {                                                              \
+    return potrs_any<T>(layout, uplo, n, nrhs, a, lda, b, ldb);                                  \
+  }                                                                                               \
+  int LAPACKE_##P##posv(int layout, char uplo, int n, int nrhs, T *a, int lda, T *b, int ldb) {  \
+    return posv_any<T>(layout, uplo, n, nrhs, a, lda, b, ldb);                                   \
+  }
+LAPACKE_FNS(d, double)
+LAPACKE_FNS(s, float)
+#undef LAPACKE_FNS
+
+// ---- device-pointer, stream-ordered extensions (column-major) ----
+int zml_gpu_dgetrf(int m, int n, double *dA, int ldda, int *dipiv, int *info, void *stream) {
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (ldda < std::max(1, m)) return -4;
+  int inf = 0;
+  int r = getrf_dev<double>(m, n, dA, ldda, dipiv, &inf, (cudaStream_t)stream);
+  if (info) *info = inf;
+  return r;
+}
+int zml_gpu_dgetrs(char trans, int n, int nrhs, const double *dA, int ldda, const int *dipiv,
+                   double *dB, int lddb, void *stream) {
+  trans = up(trans);
+  if (trans != 'N' && trans != 'T' && trans != 'C') return -1;
+  if (n < 0) return -2;
+  if (nrhs < 0) return -3;
+  if (ldda < std::max(1, n)) return -5;
+  if (lddb < std::max(1, n)) return -8;
+  return getrs_dev<double>(trans == 'N' ? kNoTrans : kTrans, n, nrhs, dA, ldda, dipiv, dB, lddb,
+                           (cudaStream_t)stream);
+}
+int zml_gpu_dpotrf(char uplo, int n, double *dA, int ldda, int *info, void *stream) {
+  uplo = up(uplo);
+  if (uplo != 'U' && uplo != 'L') return -1;
+  if (n < 0) return -2;
+  if (ldda < std::max(1, n)) return -4;
+  int inf = 0;
+  int r = potrf_dev<double>(uplo == 'L' ? kLower : kUpper, n, dA, ldda, &inf,
+                            (cudaStream_t)stream);
+  if (info) *info = inf;
+  return r;
+}
+int zml_gpu_dpotrs(char uplo, int n, int nrhs, const double *dA, int ldda, double *dB, int lddb,
+                   void *stream) {
+  uplo = up(uplo);
+  if (uplo != 'U' && uplo != 'L') return -1;
+  if (n < 0) return -2;
+  if (nrhs < 0) return -3;
+  if (ldda < std::max(1, n)) return -5;
+  if (lddb < std::max(1, n)) return -7;
+  return potrs_dev<double>(uplo == 'L' ? kLower : kUpper, n, nrhs, dA, ldda, dB, lddb,
+                           (cudaStream_t)stream);
+}
+int zml_gpu_dgemm(int ta, int tb, int m, int n, int k, double alpha, const double *dA, int ldda,
+                  const double *dB, int lddb, double beta, double *dC, int lddc, void *stream) {
+  if (!is_trans(ta) || !is_trans(tb)) return kErrInvalid;
+  return gemm_simt<double>(ta, tb, m, n, k, alpha, dA, ldda, dB, lddb, beta, dC, lddc, 0,
+                           (cudaStream_t)stream);
+}
+
+const char *zml_gpu_last_error(void) { return last_error(); }
+
+int zml_gpu_version(void) { return 1; }
+
+}  // extern "C"

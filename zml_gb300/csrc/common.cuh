@@ -1,0 +1,147 @@
+// common.cuh -- shared runtime pieces of the zml_gb300 CUDA library (sm_103a).
+//
+// Conventions used by every kernel file:
+//   * matrices are column-major with a leading dimension (the LAPACK layout
+//     zml's Zig kernels use after their row-major -> column-major swaps,
+//     linalg/blas/gemm.zig:48-65); row-major callers are transposed at the
+//     C-ABI boundary;
+//   * enum values are the CBLAS codes (reference include/cblas.h:11-38);
+//   * no kernel traps or asserts: every wait is bounded and reports through a
+//     device status word that the host reads after the launch.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <mutex>
+#include <string>
+
+namespace zg {
+
+enum : int {
+  kRowMajor = 101, kColMajor = 102,
+  kNoTrans = 111, kTrans = 112, kConjTrans = 113, kConjNoTrans = 114,
+  kUpper = 121, kLower = 122,
+  kNonUnit = 131, kUnit = 132,
+  kLeft = 141, kRight = 142,
+};
+
+// Library error codes (negative, below every LAPACK -(argument index)).
+enum : int {
+  kErrCuda = -1001,      // a CUDA runtime call failed (see zml_gpu_last_error)
+  kErrAlloc = -1002,     // device allocation failed
+  kErrNoDevice = -1003,  // no usable sm_103 device
+  kErrTimeout = -1004,   // a bounded device-side wait gave up
+  kErrInvalid = -1005,   // invalid argument to an extension entry point
+};
+
+// Status bits written by kernels into the per-call device status word.
+enum : unsigned { kStatusBarrierTimeout = 1u, kStatusQueueTimeout = 2u, kStatusMbarTimeout = 4u };
+
+void set_last_error(const char *fmt, ...);
+const char *last_error();
+
+#define ZG_CUDA(call)                                                                  \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess) {                                                           \
+      ::zg::set_last_error("%s:%d %s: %s", __FILE__, __LINE__, #call,                  \
+                           cudaGetErrorString(e_));                                    \
+      return ::zg::kErrCuda;                                                           \
+    }                                                                                  \
+  } while (0)
+
+#define ZG_TRY(expr)          \
+  do {                        \
+    int r_ = (expr);          \
+    if (r_ < 0) return r_;    \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Per-(device, stream) workspace.  Calls are stream ordered; two calls on the
+// same stream reuse the same buffers safely.  The buffer only grows.
+struct Workspace {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+};
+
+struct DeviceInfo {
+  int device = -1;
+  int num_sms = 0;
+  int cc_major = 0, cc_minor = 0;
+  size_t smem_optin = 0;
+};
+
+int device_info(DeviceInfo *out);  // for the current device
+
+// Returns a device buffer of at least `bytes` bound to `stream`.  `slot`
+// selects one of 8 independent buffers: 0-4 stage C-ABI operands, 5 is the
+// LU panel exchange, 6-7 belong to the mixed-precision and batched solvers.
+int workspace(cudaStream_t stream, int slot, size_t bytes, void **out);
+
+// Small per-stream control block: grid-barrier counters and a status word.
+struct Control {
+  unsigned int barrier[2];   // arrive counter, generation
+  unsigned int status;       // kStatus* bits
+  int info;                  // LAPACK info produced on the device
+  unsigned int queue;        // work-queue head for persistent kernels
+  unsigned int pad[3];
+};
+int control(cudaStream_t stream, Control **out);  // zeroed on the stream before return
+
+// Copies the device status word back and converts timeouts to kErrTimeout.
+int check_status(cudaStream_t stream, Control *ctl, int *info_out);
+
+// Bounded spin limit for device-side waits (~1 s at GB300 clocks).
+constexpr long long kSpinLimit = 1ll << 22;
+
+// ---------------------------------------------------------------------------
+// Device helpers
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid-wide barrier for a cooperative launch: every CTA arrives once per
+// phase; the last arrival bumps the generation.  The wait is bounded; on
+// timeout the status bit is set and the CTA carries on (its results are then
+// discarded by the host, which reports kErrTimeout).
+__device__ __forceinline__ void grid_barrier(Control *ctl, unsigned nblocks, unsigned &gen) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    unsigned arrived = atomicAdd(&ctl->barrier[0], 1u);
+    if (arrived == nblocks - 1) {
+      ctl->barrier[0] = 0;
+      __threadfence();
+      atomicAdd(&ctl->barrier[1], 1u);
+    } else {
+      long long spins = 0;
+      while (ld_acquire(&ctl->barrier[1]) == gen) {
+        if (++spins > kSpinLimit) {
+          atomicOr(&ctl->status, kStatusBarrierTimeout);
+          break;
+        }
+      }
+    }
+    __threadfence();
+  }
+  ++gen;
+  __syncthreads();
+}
+
+template <typename T> struct Real;
+template <> struct Real<double> {
+  static __device__ __forceinline__ double sfmin() { return 2.2250738585072014e-308; }
+};
+template <> struct Real<float> {
+  static __device__ __forceinline__ float sfmin() { return 1.17549435e-38f; }
+};
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace zg

@@ -1,0 +1,45 @@
+// kernels.h -- internal (C++) launchers shared between the kernel files and
+// the C ABI.  All pointers are device pointers; matrices are column-major.
+#pragma once
+#include "common.cuh"
+
+namespace zg {
+
+// gemm_simt.cu -- C <- alpha op(A) op(B) + beta C on CUDA cores; tri: 0 full,
+// 1 lower, 2 upper triangle of C (SYRK).
+template <typename T>
+int gemm_simt(int transa, int transb, int m, int n, int k, T alpha, const T *A, long lda,
+              const T *B, long ldb, T beta, T *C, long ldc, int tri, cudaStream_t s);
+template <typename T>
+int syrk_dev(int uplo, int trans, int n, int k, T alpha, const T *A, long lda, T beta, T *C,
+             long ldc, cudaStream_t s);
+
+// trsm.cu -- B <- alpha op(A)^-1 B (left) or alpha B op(A)^-1 (right).
+template <typename T>
+int trsm_dev(int side, int uplo, int transa, int diag, int m, int n, T alpha, const T *A, long lda,
+             T *B, long ldb, cudaStream_t s);
+template <typename T> int scale_dev(int m, int n, T alpha, T *B, long ldb, cudaStream_t s);
+template <typename T>
+int transpose_dev(int rows, int cols, const T *src, long lds, T *dst, long ldd, cudaStream_t s);
+
+// lu.cu
+template <typename T>
+int laswp_dev(int n, T *A, long lda, int k1, int k2, const int *ipiv, int incx, cudaStream_t s);
+// Partial-pivot LU of the m x nb panel at A (leading dim lda); writes
+// ipiv[0..nb) (1-based, relative to the panel's first row, plus ipiv_base)
+// and records the first zero pivot (1-based column + info_base) in ctl->info.
+template <typename T>
+int panel_lu(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *ctl, int info_base,
+             cudaStream_t s);
+template <typename T>
+int getrf_dev(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s);
+template <typename T>
+int getrs_dev(int trans, int n, int nrhs, const T *A, long lda, const int *ipiv, T *B, long ldb,
+              cudaStream_t s);
+
+// chol.cu
+template <typename T> int potrf_dev(int uplo, int n, T *A, long lda, int *info, cudaStream_t s);
+template <typename T>
+int potrs_dev(int uplo, int n, int nrhs, const T *A, long lda, T *B, long ldb, cudaStream_t s);
+
+}  // namespace zg

@@ -1,0 +1,282 @@
+// lu.cu -- LU with partial pivoting: getrf / getrs / laswp on the GPU.
+//
+// Replaces zml's lapack/getrf.zig:14-152 (blocked right-looking loop),
+// getrf2.zig:14-210 (panel), laswp.zig:12-96 and getrs.zig:13-142.
+//
+// The panel (m x nb, nb <= 64 for FP64, <= 128 for FP32) is factored by ONE
+// cooperative launch: every CTA keeps a contiguous slab of the panel's rows
+// in shared memory for the whole panel; per column it finds its local
+// pivot candidate, publishes (|value|, row, row contents) to a global
+// exchange slot, meets the other CTAs at one bounded grid barrier, and then
+// every CTA reduces the candidates identically, swaps, scales and applies
+// the rank-1 update to its own rows.  The pivot rule is zml's iamax
+// (blas/iamax.zig:29-38): the first maximum of |a(i,k)| over i >= k wins,
+// NaN never displaces the running maximum, so ties resolve to the lowest row.
+// The column is scaled by the reciprocal of the pivot when |pivot| >= sfmin,
+// else divided (getrf2.zig:65-87).
+#include <cooperative_groups.h>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace zg {
+
+// Comparison key of candidate row i for pivot column k (see header comment).
+template <typename T> __device__ __forceinline__ T pivot_key(T v, bool first) {
+  if (v != v) return first ? T(INFINITY) : T(-INFINITY);
+  return fabs(v);
+}
+
+template <typename T>
+__device__ __forceinline__ void better(T &bk, int &bi, T k2, int i2) {
+  if (k2 > bk || (k2 == bk && i2 < bi)) { bk = k2; bi = i2; }
+}
+
+template <typename T>
+__device__ void block_argmax(T &key, int &idx, T *sk, int *si) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    T k2 = __shfl_xor_sync(0xffffffffu, key, off);
+    int i2 = __shfl_xor_sync(0xffffffffu, idx, off);
+    better(key, idx, k2, i2);
+  }
+  if (lane == 0) { sk[warp] = key; si[warp] = idx; }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    key = lane < nw ? sk[lane] : T(-INFINITY);
+    idx = lane < nw ? si[lane] : 0x7fffffff;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      T k2 = __shfl_xor_sync(0xffffffffu, key, off);
+      int i2 = __shfl_xor_sync(0xffffffffu, idx, off);
+      better(key, idx, k2, i2);
+    }
+    if (lane == 0) { sk[0] = key; si[0] = idx; }
+  }
+  __syncthreads();
+  key = sk[0];
+  idx = si[0];
+  __syncthreads();
+}
+
+// Exchange layout (T words): for parity p in {0,1}:
+//   cand[p][b] : [key, row, v_0 .. v_{nb-1}]  (stride nb + 2), b < gridDim.x
+//   rowk[p]    : [v_0 .. v_{nb-1}]
+template <typename T>
+__global__ void __launch_bounds__(256) panel_lu_kernel(int m, int nb, T *__restrict__ A, long lda,
+                                                       int *__restrict__ ipiv, int ipiv_base,
+                                                       Control *ctl, int info_base, int R,
+                                                       T *__restrict__ xchg) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *S = reinterpret_cast<T *>(smem_raw);  // S[c * R + r], column-major slab
+  __shared__ T sk[32];
+  __shared__ int si[32];
+  __shared__ T urow[128];                  // pivot row of the current column
+  const int b = blockIdx.x, nblk = gridDim.x, tid = threadIdx.x;
+  const int r0 = b * R, rows = max(0, min(R, m - r0));
+  const int stride = nb + 2;
+  T *cand[2] = {xchg, xchg + (long)nblk * stride};
+  T *rowk[2] = {xchg + 2L * nblk * stride, xchg + 2L * nblk * stride + nb};
+  unsigned gen = 0;
+
+  for (int e = tid; e < rows * nb; e += blockDim.x) {
+    int r = e % rows, c = e / rows;
+    S[c * R + r] = A[(r0 + r) + (long)c * lda];
+  }
+  __syncthreads();
+
+  const int kmax = min(m, nb);
+  for (int k = 0; k < kmax; ++k) {
+    const int p = k & 1;
+    // 1. local candidate among rows i >= k
+    T key = T(-INFINITY);
+    int idx = 0x7fffffff;
+    for (int r = tid; r < rows; r += blockDim.x) {
+      const int gi = r0 + r;
+      if (gi < k) continue;
+      better(key, idx, pivot_key(S[k * R + r], gi == k), gi);
+    }
+    block_argmax(key, idx, sk, si);
+    T *my = cand[p] + (long)b * stride;
+    if (tid == 0) { my[0] = key; my[1] = idx == 0x7fffffff ? T(-1) : T(idx); }
+    if (idx != 0x7fffffff)
+      for (int c = tid; c < nb; c += blockDim.x) my[2 + c] = S[c * R + (idx - r0)];
+    if (k >= r0 && k < r0 + rows)
+      for (int c = tid; c < nb; c += blockDim.x) rowk[p][c] = S[c * R + (k - r0)];
+    // 2. meet every CTA
+    grid_barrier(ctl, nblk, gen);
+    // 3. global pivot: identical reduction in every CTA
+    key = T(-INFINITY);
+    idx = 0x7fffffff;
+    int win = 0;
+    for (int q = tid; q < nblk; q += blockDim.x) {
+      const T *cq = cand[p] + (long)q * stride;
+      const T kq = __ldcg(cq), rq = __ldcg(cq + 1);
+      better(key, idx, kq, rq < T(0) ? 0x7fffffff : (int)rq);
+    }
+    block_argmax(key, idx, sk, si);
+    // locate the slot that holds row idx
+    if (idx != 0x7fffffff) win = idx / R;
+    const T *prow = cand[p] + (long)win * stride + 2;
+    for (int c = tid; c < nb; c += blockDim.x) urow[c] = __ldcg(prow + c);
+    __syncthreads();
+    const T piv = urow[k];
+    if (b == 0 && tid == 0) {
+      ipiv[k] = idx + 1 + ipiv_base;
+      if (piv == T(0)) atomicCAS(&ctl->info, 0, k + 1 + info_base);
+    }
+    if (piv != T(0) && idx != k) {  // 4. swap rows k and idx
+      if (k >= r0 && k < r0 + rows)
+        for (int c = tid; c < nb; c += blockDim.x) S[c * R + (k - r0)] = urow[c];
+      if (idx >= r0 && idx < r0 + rows)
+        for (int c = tid; c < nb; c += blockDim.x) S[c * R + (idx - r0)] = __ldcg(rowk[p] + c);
+      __syncthreads();
+    }
+    // 5. scale the column below the pivot, 6. rank-1 update of the slab
+    const int rb = max(0, k + 1 - r0);  // first local row strictly below k
+    if (piv != T(0)) {
+      const bool recip = fabs(piv) >= Real<T>::sfmin();
+      const T rp = T(1) / piv;
+      for (int r = rb + tid; r < rows; r += blockDim.x)
+        S[k * R + r] = recip ? S[k * R + r] * rp : S[k * R + r] / piv;
+      __syncthreads();
+    }
+    const int nr = rows - rb, ncol = nb - k - 1;
+    if (nr > 0 && ncol > 0) {
+      for (int e = tid; e < nr * ncol; e += blockDim.x) {
+        const int r = rb + e % nr, c = k + 1 + e / nr;
+        S[c * R + r] -= S[k * R + r] * urow[c];
+      }
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < rows * nb; e += blockDim.x) {
+    int r = e % rows, c = e / rows;
+    A[(r0 + r) + (long)c * lda] = S[c * R + r];
+  }
+}
+
+template <typename T>
+int panel_lu(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *ctl, int info_base,
+             cudaStream_t s) {
+  if (m <= 0 || nb <= 0) return 0;
+  if (nb > 128) {
+    set_last_error("panel_lu: nb %d > 128", nb);
+    return kErrInvalid;
+  }
+  DeviceInfo di;
+  ZG_TRY(device_info(&di));
+  // rows per CTA: at least 8, at most what fits in shared memory
+  const size_t limit = di.smem_optin - 4096;
+  int nblk = min(di.num_sms, ceil_div(m, 8));
+  int R = ceil_div(m, nblk);
+  if ((size_t)R * nb * sizeof(T) > limit) {
+    set_last_error("panel_lu: panel %d x %d too tall for %d SMs", m, nb, di.num_sms);
+    return kErrInvalid;
+  }
+  nblk = ceil_div(m, R);
+  const size_t smem = (size_t)R * nb * sizeof(T);
+  void *xchg;
+  ZG_TRY(workspace(s, 5, sizeof(T) * (2L * nblk * (nb + 2) + 2L * nb), &xchg));
+  static bool attr_set[2] = {false, false};
+  const int ti = sizeof(T) == 8 ? 0 : 1;
+  if (!attr_set[ti]) {
+    ZG_CUDA(cudaFuncSetAttribute(panel_lu_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)limit));
+    attr_set[ti] = true;
+  }
+  // barrier counters are per launch
+  ZG_CUDA(cudaMemsetAsync(&ctl->barrier[0], 0, 2 * sizeof(unsigned), s));
+  T *xp = (T *)xchg;
+  void *args[] = {&m, &nb, &A, &lda, &ipiv, &ipiv_base, &ctl, &info_base, &R, &xp};
+  ZG_CUDA(cudaLaunchCooperativeKernel((void *)panel_lu_kernel<T>, dim3(nblk), dim3(256), args,
+                                      smem, s));
+  return 0;
+}
+
+// Row interchanges (laswp.zig): one thread per column applies the pivots
+// k1..k2 (1-based) in order, or in reverse for incx < 0.
+template <typename T>
+__global__ void laswp_kernel(int n, T *A, long lda, int k1, int k2, const int *__restrict__ ipiv,
+                             int incx) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  T *col = A + (long)j * lda;
+  if (incx > 0) {
+    for (int i = k1 - 1; i < k2; ++i) {
+      const int ip = ipiv[i] - 1;
+      if (ip != i) { T t = col[i]; col[i] = col[ip]; col[ip] = t; }
+    }
+  } else {
+    for (int i = k2 - 1; i >= k1 - 1; --i) {
+      const int ip = ipiv[i] - 1;
+      if (ip != i) { T t = col[i]; col[i] = col[ip]; col[ip] = t; }
+    }
+  }
+}
+
+template <typename T>
+int laswp_dev(int n, T *A, long lda, int k1, int k2, const int *ipiv, int incx, cudaStream_t s) {
+  if (n <= 0 || k2 < k1) return 0;
+  laswp_kernel<T><<<ceil_div(n, 128), 128, 0, s>>>(n, A, lda, k1, k2, ipiv, incx);
+  ZG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+template <typename T> static int lu_block() { return sizeof(T) == 8 ? 64 : 128; }
+
+template <typename T>
+int getrf_dev(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s) {
+  *info = 0;
+  if (m <= 0 || n <= 0) return 0;
+  Control *ctl;
+  ZG_TRY(control(s, &ctl));
+  const int nb = lu_block<T>();
+  const int mn = min(m, n);
+  for (int j = 0; j < mn; j += nb) {
+    const int jb = min(nb, mn - j);
+    T *Ajj = A + j + (long)j * lda;
+    ZG_TRY(panel_lu<T>(m - j, jb, Ajj, lda, ipiv + j, j, ctl, j, s));
+    ZG_TRY(laswp_dev<T>(j, A, lda, j + 1, j + jb, ipiv, 1, s));
+    if (j + jb < n) {
+      T *Aright = A + (long)(j + jb) * lda;
+      ZG_TRY(laswp_dev<T>(n - j - jb, Aright, lda, j + 1, j + jb, ipiv, 1, s));
+      ZG_TRY(trsm_dev<T>(kLeft, kLower, kNoTrans, kUnit, jb, n - j - jb, T(1), Ajj, lda,
+                         Aright + j, lda, s));
+      if (j + jb < m)
+        ZG_TRY(gemm_simt<T>(kNoTrans, kNoTrans, m - j - jb, n - j - jb, jb, T(-1), Ajj + jb, lda,
+                            Aright + j, lda, T(1), Aright + j + jb, lda, 0, s));
+    }
+  }
+  return check_status(s, ctl, info);
+}
+
+template <typename T>
+int getrs_dev(int trans, int n, int nrhs, const T *A, long lda, const int *ipiv, T *B, long ldb,
+              cudaStream_t s) {
+  if (n <= 0 || nrhs <= 0) return 0;
+  const bool nt = trans == kNoTrans || trans == kConjNoTrans;
+  if (nt) {
+    ZG_TRY(laswp_dev<T>(nrhs, B, ldb, 1, n, ipiv, 1, s));
+    ZG_TRY(trsm_dev<T>(kLeft, kLower, kNoTrans, kUnit, n, nrhs, T(1), A, lda, B, ldb, s));
+    ZG_TRY(trsm_dev<T>(kLeft, kUpper, kNoTrans, kNonUnit, n, nrhs, T(1), A, lda, B, ldb, s));
+  } else {
+    ZG_TRY(trsm_dev<T>(kLeft, kUpper, kTrans, kNonUnit, n, nrhs, T(1), A, lda, B, ldb, s));
+    ZG_TRY(trsm_dev<T>(kLeft, kLower, kTrans, kUnit, n, nrhs, T(1), A, lda, B, ldb, s));
+    ZG_TRY(laswp_dev<T>(nrhs, B, ldb, 1, n, ipiv, -1, s));
+  }
+  return 0;
+}
+
+#define INST(T)                                                                                 \
+  template int panel_lu<T>(int, int, T *, long, int *, int, Control *, int, cudaStream_t);      \
+  template int laswp_dev<T>(int, T *, long, int, int, const int *, int, cudaStream_t);          \
+  template int getrf_dev<T>(int, int, T *, long, int *, int *, cudaStream_t);                   \
+  template int getrs_dev<T>(int, int, int, const T *, long, const int *, T *, long, cudaStream_t);
+INST(double)
+INST(float)
+#undef INST
+
+}  // namespace zg

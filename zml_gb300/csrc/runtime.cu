@@ -1,0 +1,116 @@
+// runtime.cu -- error reporting, device query, per-stream workspaces.
+#include "common.cuh"
+
+#include <cstdarg>
+#include <map>
+#include <utility>
+#include <vector>
+
+namespace zg {
+
+static thread_local char g_last_error[512] = "";
+
+void set_last_error(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+  va_end(ap);
+}
+
+const char *last_error() { return g_last_error; }
+
+static std::mutex g_mu;
+static std::map<int, DeviceInfo> g_dev;
+
+int device_info(DeviceInfo *out) {
+  int dev = 0;
+  ZG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_dev.find(dev);
+  if (it == g_dev.end()) {
+    DeviceInfo d;
+    d.device = dev;
+    cudaDeviceProp p;
+    ZG_CUDA(cudaGetDeviceProperties(&p, dev));
+    d.num_sms = p.multiProcessorCount;
+    d.cc_major = p.major;
+    d.cc_minor = p.minor;
+    d.smem_optin = p.sharedMemPerBlockOptin;
+    it = g_dev.emplace(dev, d).first;
+  }
+  *out = it->second;
+  return 0;
+}
+
+struct StreamState {
+  Workspace ws[8];
+  Control *ctl = nullptr;
+};
+
+static std::map<std::pair<int, cudaStream_t>, StreamState> g_streams;
+
+static StreamState *state_for(cudaStream_t s, int *err) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    *err = kErrCuda;
+    return nullptr;
+  }
+  *err = 0;
+  return &g_streams[{dev, s}];
+}
+
+int workspace(cudaStream_t stream, int slot, size_t bytes, void **out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  int err;
+  StreamState *st = state_for(stream, &err);
+  if (!st) return err;
+  Workspace &w = st->ws[slot];
+  if (w.bytes < bytes) {
+    if (w.ptr) {
+      ZG_CUDA(cudaStreamSynchronize(stream));
+      cudaFree(w.ptr);
+      w.ptr = nullptr;
+      w.bytes = 0;
+    }
+    size_t want = bytes + (bytes >> 3) + 256;
+    if (cudaMalloc(&w.ptr, want) != cudaSuccess) {
+      cudaGetLastError();
+      set_last_error("workspace: cudaMalloc(%zu) failed", want);
+      return kErrAlloc;
+    }
+    w.bytes = want;
+  }
+  *out = w.ptr;
+  return 0;
+}
+
+int control(cudaStream_t stream, Control **out) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  int err;
+  StreamState *st = state_for(stream, &err);
+  if (!st) return err;
+  if (!st->ctl) {
+    if (cudaMalloc(&st->ctl, sizeof(Control)) != cudaSuccess) {
+      cudaGetLastError();
+      set_last_error("control: cudaMalloc failed");
+      return kErrAlloc;
+    }
+  }
+  ZG_CUDA(cudaMemsetAsync(st->ctl, 0, sizeof(Control), stream));
+  *out = st->ctl;
+  return 0;
+}
+
+int check_status(cudaStream_t stream, Control *ctl, int *info_out) {
+  Control h;
+  ZG_CUDA(cudaMemcpyAsync(&h, ctl, sizeof(Control), cudaMemcpyDeviceToHost, stream));
+  ZG_CUDA(cudaStreamSynchronize(stream));
+  if (h.status) {
+    set_last_error("device-side wait timed out (status 0x%x)", h.status);
+    return kErrTimeout;
+  }
+  if (info_out) *info_out = h.info;
+  return 0;
+}
+
+}  // namespace zg
