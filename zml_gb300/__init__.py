@@ -42,9 +42,29 @@ _SIGS.update({
     "zml_gpu_dpotrf": (i32, [ch, i32, vp, i32, vp, vp]),
     "zml_gpu_dpotrs": (i32, [ch, i32, i32, vp, i32, vp, i32, vp]),
     "zml_gpu_dgemm": (i32, [i32, i32, i32, i32, i32, f64, vp, i32, vp, i32, f64, vp, i32, vp]),
+    "zml_gpu_gemm_lowp": (i32, [i32, i32, i32, i32, f32, vp, i32, vp, i32, f32, vp, i32, vp]),
     "zml_gpu_last_error": (C.c_char_p, []),
     "zml_gpu_version": (i32, []),
 })
+
+
+
+class MpirResult(C.Structure):
+    _fields_ = [("info", C.c_int), ("iters", C.c_int), ("inner_iters", C.c_int),
+                ("converged", C.c_int), ("berr", C.c_double), ("factor_ms", C.c_double),
+                ("berr_history", C.c_double * 32)]
+
+
+_SIGS.update({
+    "zml_dgesv_mpir": (i32, [i32, i32, i32, vp, i32, vp, i32, vp, i32, i32, i32, f64, i32,
+                             C.POINTER(MpirResult)]),
+    "LAPACKE_dsgesv": (i32, [i32, i32, i32, vp, i32, vp, vp, i32, vp, i32, vp]),
+    "zml_gpu_dgesv_mpir": (i32, [i32, i32, vp, i32, vp, i32, vp, i32, i32, i32, f64, i32,
+                                 C.POINTER(MpirResult), vp]),
+})
+
+PREC_FP16, PREC_BF16, PREC_FP32 = 0, 1, 2
+REFINE_IR, REFINE_GMRES = 0, 1
 
 _lib = None
 

@@ -19,6 +19,8 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "kernels_mixed.h"
+#include "kernels_tc.h"
 
 using namespace zg;
 
@@ -140,10 +142,10 @@ int gemm_any(int order, int ta, int tb, int m, int n, int k, T alpha, const T *a
   Staged<T> A, B, C;
   const bool use_ab = alpha != T(0) && k > 0;
   if (use_ab) {
-    ZG_TRY(A.in(a, lda, nrowa, ncola, 0, true, s));
-    ZG_TRY(B.in(b, ldb, nrowb, ncolb, 1, true, s));
+    ZG_TRY(A.in(a, lda, nrowa, ncola, kSlotA, true, s));
+    ZG_TRY(B.in(b, ldb, nrowb, ncolb, kSlotB, true, s));
   }
-  ZG_TRY(C.in(c, ldc, m, n, 2, beta != T(0), s));
+  ZG_TRY(C.in(c, ldc, m, n, kSlotC, beta != T(0), s));
   ZG_TRY(gemm_simt<T>(ta, tb, m, n, use_ab ? k : 0, alpha, A.d, A.ld ? A.ld : 1, B.d,
                       B.ld ? B.ld : 1, beta, C.d, C.ld, 0, s));
   ZG_TRY(C.out(s));
@@ -168,9 +170,9 @@ int syrk_any(int order, int uplo, int trans, int n, int k, T alpha, const T *a, 
   cudaStream_t s = lib_stream();
   Staged<T> A, C;
   const bool use_a = alpha != T(0) && k > 0;
-  if (use_a) ZG_TRY(A.in(a, lda, nrowa, trans == kNoTrans ? k : n, 0, true, s));
+  if (use_a) ZG_TRY(A.in(a, lda, nrowa, trans == kNoTrans ? k : n, kSlotA, true, s));
   // C: the whole n x n square is staged so that the other triangle survives
-  ZG_TRY(C.in(c, ldc, n, n, 2, true, s));
+  ZG_TRY(C.in(c, ldc, n, n, kSlotC, true, s));
   if (use_a)
     ZG_TRY(syrk_dev<T>(uplo, trans, n, k, alpha, A.d, A.ld, beta, C.d, C.ld, s));
   else
@@ -197,8 +199,8 @@ int trsm_any(int order, int side, int uplo, int ta, int diag, int m, int n, T al
   if (m == 0 || n == 0) return 0;
   cudaStream_t s = lib_stream();
   Staged<T> A, B;
-  if (alpha != T(0)) ZG_TRY(A.in(a, lda, nrowa, nrowa, 0, true, s));
-  ZG_TRY(B.in(b, ldb, m, n, 1, alpha != T(0), s));
+  if (alpha != T(0)) ZG_TRY(A.in(a, lda, nrowa, nrowa, kSlotA, true, s));
+  ZG_TRY(B.in(b, ldb, m, n, kSlotB, alpha != T(0), s));
   ZG_TRY(trsm_dev<T>(side, uplo, ta, diag, m, n, alpha, A.d, A.ld, B.d, B.ld, s));
   ZG_TRY(B.out(s));
   return sync(s);
@@ -249,8 +251,8 @@ template <typename T> int getrf_any(int layout, int m, int n, T *a, int lda, int
   cudaStream_t s = lib_stream();
   ColMajor<T> A;
   Buf<int> P;
-  ZG_TRY(A.in(layout, a, lda, m, n, 0, 1, true, s));
-  ZG_TRY(P.in(ipiv, std::min(m, n), 2, false, s));
+  ZG_TRY(A.in(layout, a, lda, m, n, kSlotA, kSlotAT, true, s));
+  ZG_TRY(P.in(ipiv, std::min(m, n), kSlotPiv, false, s));
   int info = 0;
   ZG_TRY(getrf_dev<T>(m, n, A.d, A.ld, P.d, &info, s));
   ZG_TRY(A.out(s));
@@ -273,9 +275,9 @@ int getrs_any(int layout, char trans, int n, int nrhs, const T *a, int lda, cons
   cudaStream_t s = lib_stream();
   ColMajor<T> A, B;
   Buf<int> P;
-  ZG_TRY(A.in(layout, a, lda, n, n, 0, 1, true, s));
-  ZG_TRY(B.in(layout, b, ldb, n, nrhs, 2, 3, true, s));
-  ZG_TRY(P.in(const_cast<int *>(ipiv), n, 4, true, s));
+  ZG_TRY(A.in(layout, a, lda, n, n, kSlotA, kSlotAT, true, s));
+  ZG_TRY(B.in(layout, b, ldb, n, nrhs, kSlotB, kSlotBT, true, s));
+  ZG_TRY(P.in(const_cast<int *>(ipiv), n, kSlotPiv, true, s));
   ZG_TRY(getrs_dev<T>(trans == 'N' ? kNoTrans : kTrans, n, nrhs, A.d, A.ld, P.d, B.d, B.ld, s));
   ZG_TRY(B.out(s));
   ZG_TRY(sync(s));
@@ -293,9 +295,9 @@ int gesv_any(int layout, int n, int nrhs, T *a, int lda, int *ipiv, T *b, int ld
   cudaStream_t s = lib_stream();
   ColMajor<T> A, B;
   Buf<int> P;
-  ZG_TRY(A.in(layout, a, lda, n, n, 0, 1, true, s));
-  ZG_TRY(B.in(layout, b, ldb, n, nrhs, 2, 3, true, s));
-  ZG_TRY(P.in(ipiv, n, 4, false, s));
+  ZG_TRY(A.in(layout, a, lda, n, n, kSlotA, kSlotAT, true, s));
+  ZG_TRY(B.in(layout, b, ldb, n, nrhs, kSlotB, kSlotBT, true, s));
+  ZG_TRY(P.in(ipiv, n, kSlotPiv, false, s));
   int info = 0;
   ZG_TRY(getrf_dev<T>(n, n, A.d, A.ld, P.d, &info, s));
   if (info == 0) ZG_TRY(getrs_dev<T>(kNoTrans, n, nrhs, A.d, A.ld, P.d, B.d, B.ld, s));
@@ -315,7 +317,7 @@ template <typename T> int potrf_any(int layout, char uplo, int n, T *a, int lda)
   if (n == 0) return 0;
   cudaStream_t s = lib_stream();
   ColMajor<T> A;
-  ZG_TRY(A.in(layout, a, lda, n, n, 0, 1, true, s));
+  ZG_TRY(A.in(layout, a, lda, n, n, kSlotA, kSlotAT, true, s));
   int info = 0;
   ZG_TRY(potrf_dev<T>(uplo == 'L' ? kLower : kUpper, n, A.d, A.ld, &info, s));
   ZG_TRY(A.out(s));
@@ -335,8 +337,8 @@ int potrs_any(int layout, char uplo, int n, int nrhs, const T *a, int lda, T *b,
   if (n == 0 || nrhs == 0) return 0;
   cudaStream_t s = lib_stream();
   ColMajor<T> A, B;
-  ZG_TRY(A.in(layout, a, lda, n, n, 0, 1, true, s));
-  ZG_TRY(B.in(layout, b, ldb, n, nrhs, 2, 3, true, s));
+  ZG_TRY(A.in(layout, a, lda, n, n, kSlotA, kSlotAT, true, s));
+  ZG_TRY(B.in(layout, b, ldb, n, nrhs, kSlotB, kSlotBT, true, s));
   ZG_TRY(potrs_dev<T>(uplo == 'L' ? kLower : kUpper, n, nrhs, A.d, A.ld, B.d, B.ld, s));
   ZG_TRY(B.out(s));
   ZG_TRY(sync(s));
@@ -355,8 +357,8 @@ int posv_any(int layout, char uplo, int n, int nrhs, T *a, int lda, T *b, int ld
   if (n == 0 || nrhs == 0) return 0;
   cudaStream_t s = lib_stream();
   ColMajor<T> A, B;
-  ZG_TRY(A.in(layout, a, lda, n, n, 0, 1, true, s));
-  ZG_TRY(B.in(layout, b, ldb, n, nrhs, 2, 3, true, s));
+  ZG_TRY(A.in(layout, a, lda, n, n, kSlotA, kSlotAT, true, s));
+  ZG_TRY(B.in(layout, b, ldb, n, nrhs, kSlotB, kSlotBT, true, s));
   const int ul = uplo == 'L' ? kLower : kUpper;
   int info = 0;
   ZG_TRY(potrf_dev<T>(ul, n, A.d, A.ld, &info, s));
@@ -367,7 +369,29 @@ int posv_any(int layout, char uplo, int n, int nrhs, T *a, int lda, T *b, int ld
   return info;
 }
 
+int mpir_any(int layout, int n, int nrhs, const double *a, int lda, const double *b, int ldb,
+             double *x, int ldx, const MpirOpts &o, MpirResult *res) {
+  if (!lay_ok(layout)) return -1;
+  if (n < 0) return -2;
+  if (nrhs < 0) return -3;
+  if (lda < std::max(1, n)) return -5;
+  if (ldb < std::max(1, layout == kColMajor ? n : nrhs)) return -7;
+  if (ldx < std::max(1, layout == kColMajor ? n : nrhs)) return -9;
+  *res = MpirResult{};
+  if (n == 0 || nrhs == 0) return 0;
+  cudaStream_t s = lib_stream();
+  ColMajor<double> A, B, X;
+  ZG_TRY(A.in(layout, a, lda, n, n, kSlotA, kSlotAT, true, s));
+  ZG_TRY(B.in(layout, b, ldb, n, nrhs, kSlotB, kSlotBT, true, s));
+  ZG_TRY(X.in(layout, x, ldx, n, nrhs, kSlotX, kSlotXT, false, s));
+  ZG_TRY(gesv_mpir_dev(n, nrhs, A.d, A.ld, B.d, B.ld, X.d, X.ld, o, res, s));
+  ZG_TRY(X.out(s));
+  return sync(s);
+}
+
 }  // namespace
+
+static_assert(sizeof(MpirResult) == 4 * sizeof(int) + 34 * sizeof(double), "zml_mpir_result layout");
 
 extern "C" {
 
@@ -463,6 +487,88 @@ int zml_gpu_dgemm(int ta, int tb, int m, int n, int k, double alpha, const doubl
   if (!is_trans(ta) || !is_trans(tb)) return kErrInvalid;
   return gemm_simt<double>(ta, tb, m, n, k, alpha, dA, ldda, dB, lddb, beta, dC, lddc, 0,
                            (cudaStream_t)stream);
+}
+
+// C <- alpha A B^T + beta C with 16-bit K-major A (m x k), B (n x k) on the
+// tensor cores; prec 0 = fp16, 1 = bf16.
+int zml_gpu_gemm_lowp(int prec, int m, int n, int k, float alpha, const void *dA, int lda,
+                      const void *dB, int ldb, float beta, float *dC, int ldc, void *stream) {
+  if (prec != 0 && prec != 1) return -1;
+  if (m < 0) return -2;
+  if (n < 0) return -3;
+  if (k < 0) return -4;
+  if (lda < std::max(1, k) || lda % 8) return -7;
+  if (ldb < std::max(1, k) || ldb % 8) return -9;
+  if (ldc < std::max(1, m)) return -12;
+  cudaStream_t s = (cudaStream_t)stream;
+  Control *ctl;
+  ZG_TRY(control(s, &ctl));
+  ZG_TRY(gemm_tc(m, n, k, alpha, dA, lda, dB, ldb, beta, dC, ldc, prec, &ctl->status, s));
+  return check_status(s, ctl, nullptr);
+}
+
+// Mixed-precision solve of A X = B to FP64 backward error (host or device
+// pointers).  prec: 0 fp16, 1 bf16, 2 fp32 trailing updates; mode: 0 plain
+// IR, 1 GMRES-IR; tol 0 = refine until the backward error stagnates.
+int zml_dgesv_mpir(int layout, int n, int nrhs, const double *a, int lda, const double *b, int ldb,
+                   double *x, int ldx, int prec, int mode, double tol, int max_iter,
+                   MpirResult *res) {
+  if (prec < 0 || prec > 2) return -10;
+  if (mode != 0 && mode != 1) return -11;
+  MpirOpts o;
+  o.prec = prec;
+  o.mode = mode;
+  o.tol = tol;
+  o.max_iter = max_iter > 0 ? max_iter : 30;
+  MpirResult local;
+  return mpir_any(layout, n, nrhs, a, lda, b, ldb, x, ldx, o, res ? res : &local);
+}
+
+// LAPACK dsgesv semantics: FP32 factorization + FP64 iterative refinement;
+// if refinement does not reach FP64 accuracy within 30 steps the system is
+// re-solved with the FP64 LU (iter < 0), leaving that LU in a and ipiv.
+int LAPACKE_dsgesv(int layout, int n, int nrhs, double *a, int lda, int *ipiv, double *b, int ldb,
+                   double *x, int ldx, int *iter) {
+  MpirOpts o;
+  o.prec = kPrecFP32;
+  o.mode = kModeIR;
+  o.max_iter = 30;
+  MpirResult res;
+  int r = mpir_any(layout, n, nrhs, a, lda, b, ldb, x, ldx, o, &res);
+  if (r < 0) return r;
+  if (iter) *iter = res.iters;
+  if (res.info == 0 && res.converged) return 0;
+  // fallback: FP64 LU of a, solution into x (X <- B first; either may be
+  // host or device memory)
+  if (iter) *iter = -1;
+  if (layout == kColMajor) {
+    ZG_CUDA(cudaMemcpy2D(x, sizeof(double) * ldx, b, sizeof(double) * ldb, sizeof(double) * n,
+                         nrhs, cudaMemcpyDefault));
+  } else {
+    ZG_CUDA(cudaMemcpy2D(x, sizeof(double) * ldx, b, sizeof(double) * ldb,
+                         sizeof(double) * nrhs, n, cudaMemcpyDefault));
+  }
+  return gesv_any<double>(layout, n, nrhs, a, lda, ipiv, x, ldx);
+}
+
+int zml_gpu_dgesv_mpir(int n, int nrhs, const double *dA, int ldda, const double *dB, int lddb,
+                       double *dX, int lddx, int prec, int mode, double tol, int max_iter,
+                       MpirResult *res, void *stream) {
+  if (n < 0) return -1;
+  if (nrhs < 0) return -2;
+  if (ldda < std::max(1, n)) return -4;
+  if (lddb < std::max(1, n)) return -6;
+  if (lddx < std::max(1, n)) return -8;
+  if (prec < 0 || prec > 2) return -9;
+  if (mode != 0 && mode != 1) return -10;
+  MpirOpts o;
+  o.prec = prec;
+  o.mode = mode;
+  o.tol = tol;
+  o.max_iter = max_iter > 0 ? max_iter : 30;
+  MpirResult local;
+  return gesv_mpir_dev(n, nrhs, dA, ldda, dB, lddb, dX, lddx, o, res ? res : &local,
+                       (cudaStream_t)stream);
 }
 
 const char *zml_gpu_last_error(void) { return last_error(); }

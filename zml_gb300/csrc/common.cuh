@@ -77,9 +77,23 @@ struct DeviceInfo {
 
 int device_info(DeviceInfo *out);  // for the current device
 
-// Returns a device buffer of at least `bytes` bound to `stream`.  `slot`
-// selects one of 8 independent buffers: 0-4 stage C-ABI operands, 5 is the
-// LU panel exchange, 6-7 belong to the mixed-precision and batched solvers.
+// Workspace slots: every user owns its slot, so a nested routine never
+// reallocates a buffer its caller still holds.
+enum Slot : int {
+  kSlotA = 0, kSlotAT = 1,    // C ABI: staged / transposed first matrix
+  kSlotB = 2, kSlotBT = 3,    // C ABI: second matrix (B)
+  kSlotPiv = 4,               // C ABI: pivots
+  kSlotC = 5,                 // C ABI: third matrix (gemm/syrk C)
+  kSlotX = 6, kSlotXT = 7,    // C ABI: solution X
+  kSlotPanel = 8,             // LU panel candidate exchange
+  kSlotIRVec = 9,             // refinement vectors
+  kSlotLowLU = 10,            // low-precision factor copy, pivots, permutation
+  kSlotL16 = 11, kSlotU16 = 12,  // 16-bit L21 / U12 operands of the tensor-core update
+  kSlotBatch = 13,            // batched solver descriptors
+  kNumSlots = 16
+};
+
+// Returns a device buffer of at least `bytes` bound to `stream` in `slot`.
 int workspace(cudaStream_t stream, int slot, size_t bytes, void **out);
 
 // Small per-stream control block: grid-barrier counters and a status word.

@@ -1,0 +1,36 @@
+// kernels_mixed.h -- mixed-precision factorization and iterative refinement.
+#pragma once
+#include "common.cuh"
+
+namespace zg {
+
+enum : int { kPrecFP16 = 0, kPrecBF16 = 1, kPrecFP32 = 2 };
+enum : int { kModeIR = 0, kModeGMRES = 1 };
+
+struct MpirOpts {
+  int prec = kPrecBF16;     // factor precision of the trailing updates
+  int mode = kModeGMRES;    // refinement
+  double tol = 0;           // stop when berr <= tol; 0 = iterate to stagnation
+  int max_iter = 30;        // outer refinement steps
+  int gmres_restart = 50;   // inner GMRES iterations per outer step
+  double gmres_rtol = 1e-6; // inner relative tolerance (preconditioned residual)
+};
+
+struct MpirResult {
+  int info = 0;             // getrf info of the low-precision factorization
+  int iters = 0;            // outer refinement steps taken
+  int inner_iters = 0;      // total GMRES iterations
+  int converged = 0;        // berr reached FP64 level (or tol)
+  double berr = 0;          // final normwise backward error
+  double factor_ms = 0;     // device time of the factorization
+  double berr_history[32] = {0};
+};
+
+int d2s(int m, int n, const double *A, long lda, float *B, long ldb, cudaStream_t s);
+int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cudaStream_t s);
+// Solves A X = B (device pointers, column-major) to FP64 accuracy: one
+// low-precision factorization, then refinement of each right-hand side.
+int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, long ldb,
+                  double *X, long ldx, const MpirOpts &o, MpirResult *res, cudaStream_t s);
+
+}  // namespace zg

@@ -179,7 +179,7 @@ int panel_lu(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *c
   nblk = ceil_div(m, R);
   const size_t smem = (size_t)R * nb * sizeof(T);
   void *xchg;
-  ZG_TRY(workspace(s, 5, sizeof(T) * (2L * nblk * (nb + 2) + 2L * nb), &xchg));
+  ZG_TRY(workspace(s, kSlotPanel, sizeof(T) * (2L * nblk * (nb + 2) + 2L * nb), &xchg));
   static bool attr_set[2] = {false, false};
   const int ti = sizeof(T) == 8 ? 0 : 1;
   if (!attr_set[ti]) {

@@ -1,0 +1,581 @@
+// mixed.cu -- mixed-precision LU / Cholesky with FP64 iterative refinement.
+//
+// Factorization ("the low-precision getrf"): the matrix is held in FP32; the
+// blocked right-looking loop of lapack/getrf.zig:52-144 runs with NB = 256:
+// each 256-wide panel is factored in FP32 (cooperative panel kernel on two
+// 128-wide halves), the block row of U is solved in FP32, and the trailing
+// update A22 -= L21 U12 runs on the tcgen05 tensor cores with L21 and U12
+// rounded to BF16 (or FP16) and FP32 accumulation.
+//
+// Solve: plain iterative refinement (x += U^-1 L^-1 P r) or GMRES-IR
+// (restarted GMRES on the left-preconditioned system (LU)^-1 A d = (LU)^-1 r).
+// The residual r = b - A x, the update and the GMRES orthogonalisation are
+// FP64; the preconditioner applies the FP32 factors with FP64 accumulation.
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "kernels_mixed.h"
+#include "kernels_tc.h"
+
+namespace zg {
+
+// ---------------------------------------------------------------------------
+// Conversions
+__global__ void d2s_kernel(int m, int n, const double *A, long lda, float *B, long ldb) {
+  long total = (long)m * n;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total;
+       e += (long)gridDim.x * blockDim.x) {
+    int i = e % m, j = e / m;
+    B[i + (long)j * ldb] = (float)A[i + (long)j * lda];
+  }
+}
+
+template <typename H> __device__ __forceinline__ H to16(float v);
+template <> __device__ __forceinline__ __nv_bfloat16 to16(float v) { return __float2bfloat16_rn(v); }
+template <> __device__ __forceinline__ __half to16(float v) { return __float2half_rn(v); }
+
+// rows x k block of a column-major fp32 matrix -> row-major (K-major) 16-bit
+// with row stride ldo (transpose through shared memory).
+template <typename H>
+__global__ void to_kmajor_t_kernel(int rows, int k, const float *A, long lda, H *out, long ldo) {
+  __shared__ float t[32][33];
+  const int r0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  for (int c = threadIdx.y; c < 32; c += 8) {
+    int r = r0 + threadIdx.x, kk = k0 + c;
+    t[c][threadIdx.x] = (r < rows && kk < k) ? A[r + (long)kk * lda] : 0.f;
+  }
+  __syncthreads();
+  for (int c = threadIdx.y; c < 32; c += 8) {
+    int r = r0 + c, kk = k0 + threadIdx.x;
+    if (r < rows && kk < ldo) out[(long)r * ldo + kk] = to16<H>(kk < k ? t[threadIdx.x][c] : 0.f);
+  }
+}
+
+// k x cols block of a column-major fp32 matrix (k contiguous) -> 16-bit with
+// column stride ldo (already K-major).
+template <typename H>
+__global__ void to_kmajor_n_kernel(int k, int cols, const float *A, long lda, H *out, long ldo) {
+  long total = (long)ldo * cols;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total;
+       e += (long)gridDim.x * blockDim.x) {
+    int kk = e % ldo, c = e / ldo;
+    out[(long)c * ldo + kk] = to16<H>(kk < k ? A[kk + (long)c * lda] : 0.f);
+  }
+}
+
+static int grid1d(long total) { return (int)std::min<long>((total + 255) / 256, 152L * 16); }
+
+int d2s(int m, int n, const double *A, long lda, float *B, long ldb, cudaStream_t s) {
+  if (m <= 0 || n <= 0) return 0;
+  d2s_kernel<<<grid1d((long)m * n), 256, 0, s>>>(m, n, A, lda, B, ldb);
+  ZG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+static int to_kmajor_t(int prec, int rows, int k, const float *A, long lda, void *out, long ldo,
+                       cudaStream_t s) {
+  if (rows <= 0) return 0;
+  dim3 grid(ceil_div(rows, 32), ceil_div(ldo, 32)), blk(32, 8);
+  if (prec == kPrecBF16)
+    to_kmajor_t_kernel<__nv_bfloat16><<<grid, blk, 0, s>>>(rows, k, A, lda, (__nv_bfloat16 *)out, ldo);
+  else
+    to_kmajor_t_kernel<__half><<<grid, blk, 0, s>>>(rows, k, A, lda, (__half *)out, ldo);
+  ZG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+static int to_kmajor_n(int prec, int k, int cols, const float *A, long lda, void *out, long ldo,
+                       cudaStream_t s) {
+  if (cols <= 0) return 0;
+  if (prec == kPrecBF16)
+    to_kmajor_n_kernel<__nv_bfloat16><<<grid1d(ldo * cols), 256, 0, s>>>(k, cols, A, lda,
+                                                                         (__nv_bfloat16 *)out, ldo);
+  else
+    to_kmajor_n_kernel<__half><<<grid1d(ldo * cols), 256, 0, s>>>(k, cols, A, lda, (__half *)out, ldo);
+  ZG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Low-precision LU of an n x n FP32 matrix (partial pivoting, ipiv 1-based).
+int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cudaStream_t s) {
+  if (n <= 0) return 0;
+  constexpr int NB = 256, NBP = 128;
+  if (prec == kPrecFP32) {
+    int info = 0;
+    return getrf_dev<float>(n, n, A, lda, ipiv, &info, s) < 0 ? kErrCuda : 0;
+  }
+  void *wl, *wu;
+  ZG_TRY(workspace(s, kSlotL16, sizeof(uint16_t) * (size_t)n * NB, &wl));
+  ZG_TRY(workspace(s, kSlotU16, sizeof(uint16_t) * (size_t)n * NB, &wu));
+  for (int j = 0; j < n; j += NB) {
+    const int jb = std::min(NB, n - j);
+    // panel: two cooperative FP32 half-panels with an FP32 update between
+    for (int p = 0; p < jb; p += NBP) {
+      const int r = j + p, pb = std::min(NBP, jb - p);
+      ZG_TRY(panel_lu<float>(n - r, pb, A + r + (long)r * lda, lda, ipiv + r, r, ctl, r, s));
+      ZG_TRY(laswp_dev<float>(r - j, A + (long)j * lda, lda, r + 1, r + pb, ipiv, 1, s));
+      const int right = j + jb - r - pb;
+      if (right > 0) {
+        float *Ar = A + (long)(r + pb) * lda;
+        ZG_TRY(laswp_dev<float>(right, Ar, lda, r + 1, r + pb, ipiv, 1, s));
+        ZG_TRY(trsm_dev<float>(kLeft, kLower, kNoTrans, kUnit, pb, right, 1.f,
+                               A + r + (long)r * lda, lda, Ar + r, lda, s));
+        ZG_TRY(gemm_simt<float>(kNoTrans, kNoTrans, n - r - pb, right, pb, -1.f,
+                                A + (r + pb) + (long)r * lda, lda, Ar + r, lda, 1.f,
+                                Ar + r + pb, lda, 0, s));
+      }
+    }
+    ZG_TRY(laswp_dev<float>(j, A, lda, j + 1, j + jb, ipiv, 1, s));
+    const int rest = n - j - jb;
+    if (rest <= 0) break;
+    float *A12 = A + j + (long)(j + jb) * lda;
+    ZG_TRY(laswp_dev<float>(rest, A + (long)(j + jb) * lda, lda, j + 1, j + jb, ipiv, 1, s));
+    ZG_TRY(trsm_dev<float>(kLeft, kLower, kNoTrans, kUnit, jb, rest, 1.f, A + j + (long)j * lda,
+                           lda, A12, lda, s));
+    const long ldk = ((jb + 7) / 8) * 8;
+    ZG_TRY(to_kmajor_t(prec, rest, jb, A + (j + jb) + (long)j * lda, lda, wl, ldk, s));
+    ZG_TRY(to_kmajor_n(prec, jb, rest, A12, lda, wu, ldk, s));
+    ZG_TRY(gemm_tc(rest, rest, jb, -1.f, wl, ldk, wu, ldk, 1.f, A12 + jb, lda,
+                   prec == kPrecBF16 ? 1 : 0, &ctl->status, s));
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 residual r = b - A x (column-major A), deterministic two-pass GEMV.
+constexpr int kGemvRows = 256, kGemvCols = 512;
+
+__global__ void gemv_partial_kernel(int n, int ncols, const double *__restrict__ A, long lda,
+                                    const double *__restrict__ x, double *__restrict__ part) {
+  const int i = blockIdx.x * kGemvRows + threadIdx.x;
+  const int c0 = blockIdx.y * kGemvCols, c1 = min(ncols, c0 + kGemvCols);
+  __shared__ double xs[kGemvCols];
+  for (int c = c0 + threadIdx.x; c < c1; c += blockDim.x) xs[c - c0] = x[c];
+  __syncthreads();
+  if (i >= n) return;
+  double acc0 = 0, acc1 = 0;
+  const double *a = A + i + (long)c0 * lda;
+  int c = c0;
+  for (; c + 1 < c1; c += 2, a += 2 * lda) {
+    acc0 = fma(a[0], xs[c - c0], acc0);
+    acc1 = fma(a[lda], xs[c + 1 - c0], acc1);
+  }
+  if (c < c1) acc0 = fma(a[0], xs[c - c0], acc0);
+  part[(long)blockIdx.y * n + i] = acc0 + acc1;
+}
+
+__global__ void gemv_finish_kernel(int n, int nparts, const double *part, const double *b,
+                                   double *r) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double acc = 0;
+  for (int p = 0; p < nparts; ++p) acc += part[(long)p * n + i];
+  r[i] = b ? b[i] - acc : acc;
+}
+
+// y = A x  (b == nullptr)  or  y = b - A x
+int gemv_d(int n, const double *A, long lda, const double *x, const double *b, double *y,
+           double *part, cudaStream_t s) {
+  const int nparts = ceil_div(n, kGemvCols);
+  dim3 grid(ceil_div(n, kGemvRows), nparts);
+  gemv_partial_kernel<<<grid, kGemvRows, 0, s>>>(n, n, A, lda, x, part);
+  gemv_finish_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, nparts, part, b, y);
+  ZG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Triangular solves with the FP32 factors, FP64 vectors ("sync-free"): one CTA
+// per 64-row block, claimed in order through a ticket; a block accumulates
+// L(block, 0:block) x(0:block) as earlier blocks publish their pieces, then
+// solves its diagonal block and publishes.  Lower = unit lower (forward),
+// upper = non-unit upper (backward).
+constexpr int kTB = 64;
+
+__global__ void __launch_bounds__(256) trsv_lowp_kernel(int n, const float *__restrict__ A, long lda,
+                                                         double *x, unsigned *flags,
+                                                         unsigned *ticket, bool upper,
+                                                         unsigned *status) {
+  __shared__ unsigned sb;
+  __shared__ double part[4][kTB];
+  __shared__ double xb[kTB];
+  __shared__ float D[kTB][kTB + 1];
+  const int tid = threadIdx.x;
+  if (tid == 0) sb = atomicAdd(ticket, 1u);
+  __syncthreads();
+  const int nblk = (n + kTB - 1) / kTB;
+  const int t = sb;                                // order of processing
+  const int blk = upper ? nblk - 1 - t : t;        // block row handled
+  const int r0 = blk * kTB, rows = min(kTB, n - r0);
+  const int lr = tid % kTB, ph = tid / kTB;        // row in block, column phase
+  double acc = 0;
+  // off-diagonal blocks in dependency order
+  for (int q = 0; q < t; ++q) {
+    const int cb = upper ? nblk - 1 - q : q;       // block column, already solved
+    if (tid == 0) {
+      long spins = 0;
+      while (atomicAdd(&flags[cb], 0u) == 0u) {
+        if (++spins > kSpinLimit) { atomicOr(status, kStatusQueueTimeout); break; }
+      }
+      __threadfence();
+    }
+    __syncthreads();
+    const int c0 = cb * kTB, cols = min(kTB, n - c0);
+    if (lr < rows) {
+      const float *a = A + (r0 + lr) + (long)c0 * lda;
+      for (int c = ph; c < cols; c += 4) acc = fma((double)a[(long)c * lda], __ldcg(x + c0 + c), acc);
+    }
+  }
+  part[ph][lr] = acc;
+  // diagonal block into shared memory
+  for (int e = tid; e < kTB * kTB; e += 256) {
+    const int i = e % kTB, j = e / kTB;
+    D[i][j] = (i < rows && j < rows) ? A[(r0 + i) + (long)(r0 + j) * lda] : 0.f;
+  }
+  __syncthreads();
+  if (tid < kTB) {
+    double v = 0;
+    if (tid < rows) v = x[r0 + tid] - (part[0][tid] + part[1][tid] + part[2][tid] + part[3][tid]);
+    xb[tid] = v;
+  }
+  __syncthreads();
+  // substitution on the diagonal block
+  for (int st = 0; st < rows; ++st) {
+    const int k = upper ? rows - 1 - st : st;
+    if (upper && tid == k) xb[k] = xb[k] / (double)D[k][k];
+    __syncthreads();
+    const double xk = xb[k];
+    const bool upd = upper ? (tid < k) : (tid > k && tid < rows);
+    if (upd) xb[tid] -= (double)D[tid][k] * xk;
+    __syncthreads();
+  }
+  if (tid < rows) x[r0 + tid] = xb[tid];
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) atomicExch(&flags[blk], 1u);
+}
+
+// x <- op^-1 x with op = unit-lower L (upper=false) or non-unit upper U of
+// the FP32 LU factors in A.  flags/ticket: n/64 + 1 zeroed words (device).
+int trsv_lowp(int n, const float *A, long lda, double *x, bool upper, unsigned *work,
+              unsigned *status, cudaStream_t s) {
+  if (n <= 0) return 0;
+  const int nblk = ceil_div(n, kTB);
+  ZG_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned) * (nblk + 1), s));
+  trsv_lowp_kernel<<<nblk, 256, 0, s>>>(n, A, lda, x, work + 1, work, upper, status);
+  ZG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// d[i] = r[perm[i]]: the row interchanges of getrf as one gather (perm is the
+// composition of the ipiv swaps, built once per factorization).
+__global__ void gather_kernel(int n, const double *r, const int *perm, double *d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) d[i] = r[perm[i]];
+}
+
+int perm_from_ipiv(int n, const int *ipiv_dev, int *perm_dev, cudaStream_t s) {
+  std::vector<int> ip(n), pm(n);
+  ZG_CUDA(cudaMemcpyAsync(ip.data(), ipiv_dev, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  ZG_CUDA(cudaStreamSynchronize(s));
+  for (int i = 0; i < n; ++i) pm[i] = i;
+  for (int i = 0; i < n; ++i) {
+    const int p = ip[i] - 1;
+    if (p >= 0 && p < n && p != i) std::swap(pm[i], pm[p]);
+  }
+  ZG_CUDA(cudaMemcpyAsync(perm_dev, pm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  ZG_CUDA(cudaStreamSynchronize(s));
+  return 0;
+}
+
+// d = (LU)^-1 P r applied in FP64 with the FP32 factors.
+int lu_apply(int n, const float *LU, long lda, const int *perm, const double *r, double *d,
+             unsigned *work, unsigned *status, cudaStream_t s) {
+  gather_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, r, perm, d);
+  ZG_CUDA(cudaGetLastError());
+  ZG_TRY(trsv_lowp(n, LU, lda, d, false, work, status, s));
+  ZG_TRY(trsv_lowp(n, LU, lda, d, true, work, status, s));
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Small FP64 vector kernels (single block reductions are enough at n <= 64k).
+__global__ void absmax_kernel(int n, const double *x, double *out) {
+  __shared__ double sm[256];
+  double m = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, fabs(x[i]));
+  sm[threadIdx.x] = m;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + o]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sm[0];
+}
+
+// ||A||_inf: row sums of |A| (column-major), then the maximum.
+__global__ void rowabs_kernel(int n, const double *A, long lda, double *rs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double acc = 0;
+  for (int j = 0; j < n; ++j) acc += fabs(A[i + (long)j * lda]);
+  rs[i] = acc;
+}
+
+__global__ void axpy_kernel(int n, double a, const double *x, double *y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] += a * x[i];
+}
+
+// h[j] = V(:, j) . w for j < k   (V column-major, ldv)
+__global__ void gs_dots_kernel(int n, int k, const double *V, long ldv, const double *w,
+                               double *h) {
+  __shared__ double sm[256];
+  const int j = blockIdx.x;
+  double acc = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc = fma(V[i + (long)j * ldv], w[i], acc);
+  sm[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sm[threadIdx.x] += sm[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) h[j] = sm[0];
+}
+
+// w -= V(:, 0:k) h ; out <- optional copy
+__global__ void gs_update_kernel(int n, int k, const double *V, long ldv, const double *h,
+                                 double *w) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double acc = w[i];
+  for (int j = 0; j < k; ++j) acc -= V[i + (long)j * ldv] * h[j];
+  w[i] = acc;
+}
+
+__global__ void nrm2_kernel(int n, const double *x, double *out) {
+  __shared__ double sm[256];
+  double acc = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc = fma(x[i], x[i], acc);
+  sm[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) sm[threadIdx.x] += sm[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sqrt(sm[0]);
+}
+
+__global__ void scale_copy_kernel(int n, double a, const double *x, double *y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = a * x[i];
+}
+
+// x += V(:, 0:k) y
+__global__ void combine_kernel(int n, int k, const double *V, long ldv, const double *y,
+                               double *x) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double acc = 0;
+  for (int j = 0; j < k; ++j) acc = fma(V[i + (long)j * ldv], y[j], acc);
+  x[i] += acc;
+}
+
+// ---------------------------------------------------------------------------
+struct IRWork {
+  double *r, *d, *part, *scal, *V, *w, *h;
+  unsigned *tw;
+};
+
+static int host_scalar(const double *d, double *h, cudaStream_t s) {
+  ZG_CUDA(cudaMemcpyAsync(h, d, sizeof(double), cudaMemcpyDeviceToHost, s));
+  ZG_CUDA(cudaStreamSynchronize(s));
+  return 0;
+}
+
+// Normwise backward error of x for A x = b: ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf)
+static int berr_of(int n, const double *A, long lda, const double *b, const double *x, double anrm,
+                   double bnrm, IRWork &w, double *berr, cudaStream_t s) {
+  ZG_TRY(gemv_d(n, A, lda, x, b, w.r, w.part, s));
+  absmax_kernel<<<1, 256, 0, s>>>(n, w.r, w.scal);
+  absmax_kernel<<<1, 256, 0, s>>>(n, x, w.scal + 1);
+  ZG_CUDA(cudaGetLastError());
+  double h[2];
+  ZG_CUDA(cudaMemcpyAsync(h, w.scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  ZG_CUDA(cudaStreamSynchronize(s));
+  const double den = anrm * h[1] + bnrm;
+  *berr = den > 0 ? h[0] / den : h[0];
+  return 0;
+}
+
+// GMRES on (LU)^-1 A d = (LU)^-1 r with restart m; returns after `inner`
+// iterations or when the preconditioned residual fell by `rtol`.
+static int gmres_correction(int n, const double *A, long lda, const float *LU, long ldlu,
+                            const int *perm, IRWork &w, int m, double rtol, int *iters,
+                            Control *ctl, cudaStream_t s) {
+  const int b1 = ceil_div(n, 256);
+  double *V = w.V;  // n x (m+1)
+  // z = M^-1 r ; beta = ||z|| ; v0 = z / beta
+  ZG_TRY(lu_apply(n, LU, ldlu, perm, w.r, w.w, w.tw, &ctl->status, s));
+  nrm2_kernel<<<1, 256, 0, s>>>(n, w.w, w.scal);
+  double beta;
+  ZG_TRY(host_scalar(w.scal, &beta, s));
+  ZG_CUDA(cudaMemsetAsync(w.d, 0, sizeof(double) * n, s));
+  if (!(beta > 0) || !std::isfinite(beta)) return 0;
+  scale_copy_kernel<<<b1, 256, 0, s>>>(n, 1.0 / beta, w.w, V);
+  std::vector<double> H((m + 1) * m, 0.0), cs(m), sn(m), g(m + 1, 0.0);
+  g[0] = beta;
+  int k = 0;
+  std::vector<double> hcol(m + 1);
+  for (; k < m; ++k) {
+    // w = M^-1 A v_k
+    ZG_TRY(gemv_d(n, A, lda, V + (long)k * n, nullptr, w.d, w.part, s));
+    ZG_TRY(lu_apply(n, LU, ldlu, perm, w.d, w.w, w.tw, &ctl->status, s));
+    // classical Gram-Schmidt, twice
+    ZG_CUDA(cudaMemsetAsync(w.h, 0, sizeof(double) * 2 * (m + 1), s));
+    for (int pass = 0; pass < 2; ++pass) {
+      gs_dots_kernel<<<k + 1, 256, 0, s>>>(n, k + 1, V, n, w.w, w.h + pass * (m + 1));
+      gs_update_kernel<<<b1, 256, 0, s>>>(n, k + 1, V, n, w.h + pass * (m + 1), w.w);
+    }
+    nrm2_kernel<<<1, 256, 0, s>>>(n, w.w, w.scal);
+    ZG_CUDA(cudaGetLastError());
+    std::vector<double> hh(2 * (m + 1));
+    ZG_CUDA(cudaMemcpyAsync(hh.data(), w.h, sizeof(double) * 2 * (m + 1), cudaMemcpyDeviceToHost, s));
+    double hk1;
+    ZG_CUDA(cudaMemcpyAsync(&hk1, w.scal, sizeof(double), cudaMemcpyDeviceToHost, s));
+    ZG_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i <= k; ++i) hcol[i] = hh[i] + hh[(m + 1) + i];
+    hcol[k + 1] = hk1;
+    if (hk1 > 0 && k + 1 <= m)
+      scale_copy_kernel<<<b1, 256, 0, s>>>(n, 1.0 / hk1, w.w, V + (long)(k + 1) * n);
+    // Givens rotations on the new Hessenberg column
+    for (int i = 0; i < k; ++i) {
+      const double t = cs[i] * hcol[i] + sn[i] * hcol[i + 1];
+      hcol[i + 1] = -sn[i] * hcol[i] + cs[i] * hcol[i + 1];
+      hcol[i] = t;
+    }
+    const double rho = std::hypot(hcol[k], hcol[k + 1]);
+    cs[k] = rho > 0 ? hcol[k] / rho : 1.0;
+    sn[k] = rho > 0 ? hcol[k + 1] / rho : 0.0;
+    hcol[k] = rho;
+    hcol[k + 1] = 0;
+    g[k + 1] = -sn[k] * g[k];
+    g[k] = cs[k] * g[k];
+    for (int i = 0; i <= k; ++i) H[i + k * (m + 1)] = hcol[i];
+    ++*iters;
+    if (std::fabs(g[k + 1]) <= rtol * beta || !(hk1 > 0)) {
+      ++k;
+      break;
+    }
+  }
+  // back substitution H y = g, d = V y
+  std::vector<double> y(k, 0.0);
+  for (int i = k - 1; i >= 0; --i) {
+    double t = g[i];
+    for (int j = i + 1; j < k; ++j) t -= H[i + j * (m + 1)] * y[j];
+    y[i] = H[i + i * (m + 1)] != 0 ? t / H[i + i * (m + 1)] : 0.0;
+  }
+  ZG_CUDA(cudaMemcpyAsync(w.h, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
+  ZG_CUDA(cudaMemsetAsync(w.d, 0, sizeof(double) * n, s));
+  combine_kernel<<<b1, 256, 0, s>>>(n, k, V, n, w.h, w.d);
+  ZG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, long ldb,
+                  double *X, long ldx, const MpirOpts &o, MpirResult *res, cudaStream_t s) {
+  *res = MpirResult{};
+  if (n <= 0 || nrhs <= 0) return 0;
+  Control *ctl;
+  ZG_TRY(control(s, &ctl));
+  const int m = std::max(1, std::min(o.gmres_restart, 200));
+  // workspace: FP32 factor copy, ipiv, perm and FP64 vectors
+  void *wf, *wv;
+  const size_t nf = (size_t)n * n;
+  ZG_TRY(workspace(s, kSlotLowLU, sizeof(float) * nf + 2 * sizeof(int) * (size_t)n + 256, &wf));
+  float *LU = (float *)wf;
+  int *ipiv = (int *)((char *)wf + sizeof(float) * nf);
+  int *perm = ipiv + n;
+  const int nparts = ceil_div(n, kGemvCols);
+  const size_t nv = (size_t)n * (4 + nparts + (m + 1)) + 4 * (m + 2) + 64;
+  ZG_TRY(workspace(s, kSlotIRVec, sizeof(double) * nv + sizeof(unsigned) * (n / kTB + 8), &wv));
+  IRWork w;
+  double *p = (double *)wv;
+  w.r = p; p += n;
+  w.d = p; p += n;
+  w.w = p; p += n;
+  w.part = p; p += (size_t)n * nparts;
+  w.V = p; p += (size_t)n * (m + 1);
+  w.h = p; p += 2 * (m + 2);
+  w.scal = p; p += 8;
+  w.tw = (unsigned *)p;
+
+  // ||A||_inf
+  rowabs_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, A, lda, w.r);
+  absmax_kernel<<<1, 256, 0, s>>>(n, w.r, w.scal);
+  ZG_CUDA(cudaGetLastError());
+  double anrm;
+  ZG_TRY(host_scalar(w.scal, &anrm, s));
+
+  // factor in low precision
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, s);
+  ZG_TRY(d2s(n, n, A, lda, LU, n, s));
+  ZG_TRY(getrf_lowp(n, LU, n, ipiv, o.prec, ctl, s));
+  cudaEventRecord(e1, s);
+  int info = 0;
+  ZG_TRY(check_status(s, ctl, &info));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  res->factor_ms = ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  res->info = info;
+  if (info != 0) return 0;
+  ZG_TRY(perm_from_ipiv(n, ipiv, perm, s));
+
+  res->converged = 1;
+  for (int q = 0; q < nrhs; ++q) {
+    const double *b = B + (long)q * ldb;
+    double *x = X + (long)q * ldx;
+    absmax_kernel<<<1, 256, 0, s>>>(n, b, w.scal);
+    double bnrm;
+    ZG_TRY(host_scalar(w.scal, &bnrm, s));
+    // x0 = (LU)^-1 P b
+    ZG_TRY(lu_apply(n, LU, n, perm, b, x, w.tw, &ctl->status, s));
+    double berr = 0, prev = INFINITY;
+    ZG_TRY(berr_of(n, A, lda, b, x, anrm, bnrm, w, &berr, s));  // leaves r = b - A x
+    if (q == 0) res->berr_history[0] = berr;
+    int it = 0;
+    const double tol = o.tol > 0 ? o.tol : 0.0;
+    while (it < o.max_iter) {
+      if (berr <= tol) break;
+      if (tol == 0.0 && it > 0 && berr > 0.5 * prev) break;  // stagnated at its floor
+      prev = berr;
+      if (o.mode == kModeGMRES) {
+        ZG_TRY(gmres_correction(n, A, lda, LU, n, perm, w, m, o.gmres_rtol, &res->inner_iters, ctl, s));
+      } else {
+        ZG_TRY(lu_apply(n, LU, n, perm, w.r, w.d, w.tw, &ctl->status, s));
+      }
+      axpy_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, 1.0, w.d, x);
+      ZG_CUDA(cudaGetLastError());
+      ++it;
+      ZG_TRY(berr_of(n, A, lda, b, x, anrm, bnrm, w, &berr, s));
+      if (q == 0 && it < 32) res->berr_history[it] = berr;
+      if (!std::isfinite(berr) || berr > 1e3 * prev) break;  // diverged
+    }
+    res->iters = std::max(res->iters, it);
+    res->berr = std::max(res->berr, berr);
+    const bool ok = std::isfinite(berr) && (tol > 0 ? berr <= tol : berr <= 64 * 1.1102230246251565e-16);
+    if (!ok) res->converged = 0;
+  }
+  ZG_TRY(check_status(s, ctl, nullptr));
+  return 0;
+}
+
+}  // namespace zg

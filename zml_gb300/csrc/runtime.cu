@@ -43,7 +43,7 @@ int device_info(DeviceInfo *out) {
 }
 
 struct StreamState {
-  Workspace ws[8];
+  Workspace ws[kNumSlots];
   Control *ctl = nullptr;
 };
 
@@ -64,6 +64,10 @@ int workspace(cudaStream_t stream, int slot, size_t bytes, void **out) {
   int err;
   StreamState *st = state_for(stream, &err);
   if (!st) return err;
+  if (slot < 0 || slot >= kNumSlots) {
+    set_last_error("workspace: bad slot %d", slot);
+    return kErrInvalid;
+  }
   Workspace &w = st->ws[slot];
   if (w.bytes < bytes) {
     if (w.ptr) {
