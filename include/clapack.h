@@ -103,12 +103,13 @@ typedef struct zml_mpir_result {
 #define ZML_PREC_FP16 0
 #define ZML_PREC_BF16 1
 #define ZML_PREC_FP32 2
+#define ZML_PREC_BF16X3 3 /* hi+lo split, three BF16 products: ~16-bit updates */
 #define ZML_REFINE_IR 0
 #define ZML_REFINE_GMRES 1
 
 /* Solves A X = B (the problem of lapack/gesv.zig:13) to FP64 backward error:
- * LU with trailing updates in `prec` (tensor cores for fp16/bf16, FP32
- * panels), then plain IR or GMRES-IR with FP64 residuals.  A and B are not
+ * LU with trailing updates in `prec` (tensor cores for fp16/bf16/bf16x3,
+ * FP32 panels), then plain IR or GMRES-IR with FP64 residuals.  A and B are not
  * modified.  tol = 0 refines until the backward error stops improving.
  * Host or device pointers. */
 int zml_dgesv_mpir(int matrix_layout, int n, int nrhs, const double *a, int lda, const double *b,
@@ -122,6 +123,20 @@ int LAPACKE_dsgesv(int matrix_layout, int n, int nrhs, double *a, int lda, int *
 int zml_gpu_dgesv_mpir(int n, int nrhs, const double *dA, int ldda, const double *dB, int lddb,
                        double *dX, int lddx, int prec, int mode, double tol, int max_iter,
                        zml_mpir_result *res, void *stream);
+
+/* ---- instrumentation ------------------------------------------------------
+ * Kernel classes: 0 tensor-core GEMM, 1 CUDA-core GEMM/SYRK, 2 LU panel,
+ * 3 TRSM diagonal block, 4 row interchanges, 5 low-precision TRSV, 6 FP64
+ * GEMV / residual, 7 conversions, 8 Cholesky diagonal block, 9 vector ops,
+ * 10 batched solver, 11 QR, 12 selector MLP, 13 other. */
+/* Enables (1) or disables (0) CUDA-event timing of every launch, by class;
+ * enabling clears the accumulated figures. */
+void zml_gpu_profile(int enable);
+/* Launches, device ms, algorithmic flops and bytes of one class so far. */
+int zml_gpu_profile_read(int kernel_class, unsigned long long *launches, double *ms,
+                         double *flops, double *bytes);
+/* Kernels launched by this library in this process. */
+unsigned long long zml_gpu_launch_count(void);
 
 /* Text of the last library error on this thread. */
 const char *zml_gpu_last_error(void);

@@ -63,7 +63,29 @@ _SIGS.update({
                                  C.POINTER(MpirResult), vp]),
 })
 
-PREC_FP16, PREC_BF16, PREC_FP32 = 0, 1, 2
+_SIGS.update({
+    "zml_gpu_profile": (None, [i32]),
+    "zml_gpu_profile_read": (i32, [i32, C.POINTER(C.c_ulonglong), C.POINTER(C.c_double),
+                                   C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "zml_gpu_launch_count": (C.c_ulonglong, []),
+})
+
+KERNEL_CLASSES = ["gemm_tc", "gemm_simt", "panel", "trsm_diag", "laswp", "trsv", "gemv",
+                  "convert", "potf2", "vector", "batched", "qr", "mlp", "other"]
+
+
+def profile_read():
+    """{class: (launches, ms, flops, bytes)} accumulated since zml_gpu_profile(1)."""
+    out = {}
+    for t, name in enumerate(KERNEL_CLASSES):
+        n, ms, fl, by = C.c_ulonglong(), C.c_double(), C.c_double(), C.c_double()
+        lib().zml_gpu_profile_read(t, C.byref(n), C.byref(ms), C.byref(fl), C.byref(by))
+        if n.value:
+            out[name] = (n.value, ms.value, fl.value, by.value)
+    return out
+
+
+PREC_FP16, PREC_BF16, PREC_FP32, PREC_BF16X3 = 0, 1, 2, 3
 REFINE_IR, REFINE_GMRES = 0, 1
 
 _lib = None

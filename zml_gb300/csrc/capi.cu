@@ -513,7 +513,7 @@ int zml_gpu_gemm_lowp(int prec, int m, int n, int k, float alpha, const void *dA
 int zml_dgesv_mpir(int layout, int n, int nrhs, const double *a, int lda, const double *b, int ldb,
                    double *x, int ldx, int prec, int mode, double tol, int max_iter,
                    MpirResult *res) {
-  if (prec < 0 || prec > 2) return -10;
+  if (prec < 0 || prec > 3) return -10;
   if (mode != 0 && mode != 1) return -11;
   MpirOpts o;
   o.prec = prec;
@@ -559,7 +559,7 @@ int zml_gpu_dgesv_mpir(int n, int nrhs, const double *dA, int ldda, const double
   if (ldda < std::max(1, n)) return -4;
   if (lddb < std::max(1, n)) return -6;
   if (lddx < std::max(1, n)) return -8;
-  if (prec < 0 || prec > 2) return -9;
+  if (prec < 0 || prec > 3) return -9;
   if (mode != 0 && mode != 1) return -10;
   MpirOpts o;
   o.prec = prec;

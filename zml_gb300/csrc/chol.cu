@@ -73,7 +73,7 @@ template <typename T> int potrf_dev(int uplo, int n, T *A, long lda, int *info, 
   for (int j = 0; j < n; j += nb) {
     const int jb = min(nb, n - j);
     T *Ajj = A + j + (long)j * lda;
-    potf2_kernel<T><<<1, 256, 0, s>>>(jb, Ajj, lda, lower, ctl, j);
+    ZG_LAUNCH(kTagPotf2, 0, 0, s, potf2_kernel<T><<<1, 256, 0, s>>>(jb, Ajj, lda, lower, ctl, j));
     ZG_CUDA(cudaGetLastError());
     const int rest = n - j - jb;
     if (rest <= 0) break;

@@ -158,4 +158,28 @@ template <> struct Real<float> {
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+// ---------------------------------------------------------------------------
+// Launch accounting.  Every kernel launch goes through ZG_LAUNCH, which counts
+// it and, while profiling is enabled (zml_gpu_profile), brackets it with CUDA
+// events on its stream and files it under a kernel class with the launch's
+// algorithmic flops and bytes.
+enum ProfTag : int {
+  kTagGemmTC = 0, kTagGemmSimt, kTagPanel, kTagTrsmDiag, kTagLaswp, kTagTrsv, kTagGemv,
+  kTagConvert, kTagPotf2, kTagVector, kTagBatched, kTagQR, kTagMLP, kTagOther, kNumTags
+};
+extern unsigned long long g_launches;
+extern bool g_profiling;
+void prof_record(cudaStream_t s, int tag, double flops, double bytes, cudaEvent_t *begin);
+void prof_end(cudaStream_t s, cudaEvent_t begin, int tag, double flops, double bytes);
+
+#define ZG_LAUNCH(tag, flops, bytes, stream, ...)                                     \
+  do {                                                                                \
+    cudaEvent_t zg_ev0_ = nullptr;                                                    \
+    if (::zg::g_profiling) ::zg::prof_record((stream), (tag), 0, 0, &zg_ev0_);        \
+    __VA_ARGS__;                                                                      \
+    ++::zg::g_launches;                                                               \
+    if (::zg::g_profiling) ::zg::prof_end((stream), zg_ev0_, (tag), (flops), (bytes)); \
+    ZG_CUDA(cudaGetLastError());                                                      \
+  } while (0)
+
 }  // namespace zg

@@ -100,8 +100,8 @@ int gemm_simt(int transa, int transb, int m, int n, int k, T alpha, const T *A, 
     set_last_error("gemm: n too large for the grid");
     return kErrInvalid;
   }
-  gemm_simt_kernel<T, BM, BN, BK><<<grid, 256, 0, s>>>(transa, transb, m, n, k, alpha, A, lda, B,
-                                                       ldb, beta, C, ldc, tri);
+  ZG_LAUNCH(kTagGemmSimt, 2.0 * m * n * k, sizeof(T) * ((double)m * k + (double)k * n + 2.0 * m * n), s, gemm_simt_kernel<T, BM, BN, BK><<<grid, 256, 0, s>>>(transa, transb, m, n, k, alpha, A, lda, B,
+                                                       ldb, beta, C, ldc, tri));
   ZG_CUDA(cudaGetLastError());
   return 0;
 }

@@ -192,8 +192,8 @@ int launch(int M, int N, int K, float alpha, const void *A, long lda, const void
     attr = true;
   }
   dim3 grid(ceil_div(M, kBM), ceil_div(N, BN));
-  gemm_tc_kernel<BN, STAGES><<<grid, 256, Cfg::smem_bytes, s>>>(ta, tb, M, N, K, alpha, beta, C,
-                                                               ldc, ab_type, status);
+  ZG_LAUNCH(kTagGemmTC, 2.0 * M * N * K, 2.0 * ((double)M + N) * K + (beta != 0.f ? 8.0 : 4.0) * M * N, s, gemm_tc_kernel<BN, STAGES><<<grid, 256, Cfg::smem_bytes, s>>>(ta, tb, M, N, K, alpha, beta, C,
+                                                               ldc, ab_type, status));
   ZG_CUDA(cudaGetLastError());
   return 0;
 }

@@ -4,7 +4,9 @@
 
 namespace zg {
 
-enum : int { kPrecFP16 = 0, kPrecBF16 = 1, kPrecFP32 = 2 };
+// kPrecBF16x3: each 16-bit operand split hi + lo, three BF16 products
+// (hi*hi + hi*lo + lo*hi) accumulated in FP32 -- about 16 significant bits.
+enum : int { kPrecFP16 = 0, kPrecBF16 = 1, kPrecFP32 = 2, kPrecBF16x3 = 3 };
 enum : int { kModeIR = 0, kModeGMRES = 1 };
 
 struct MpirOpts {

@@ -191,8 +191,9 @@ int panel_lu(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *c
   ZG_CUDA(cudaMemsetAsync(&ctl->barrier[0], 0, 2 * sizeof(unsigned), s));
   T *xp = (T *)xchg;
   void *args[] = {&m, &nb, &A, &lda, &ipiv, &ipiv_base, &ctl, &info_base, &R, &xp};
-  ZG_CUDA(cudaLaunchCooperativeKernel((void *)panel_lu_kernel<T>, dim3(nblk), dim3(256), args,
-                                      smem, s));
+  ZG_LAUNCH(kTagPanel, 1.0 * m * nb * nb, 2.0 * sizeof(T) * m * nb, s,
+            ZG_CUDA(cudaLaunchCooperativeKernel((void *)panel_lu_kernel<T>, dim3(nblk), dim3(256),
+                                                args, smem, s)));
   return 0;
 }
 
@@ -220,7 +221,7 @@ __global__ void laswp_kernel(int n, T *A, long lda, int k1, int k2, const int *_
 template <typename T>
 int laswp_dev(int n, T *A, long lda, int k1, int k2, const int *ipiv, int incx, cudaStream_t s) {
   if (n <= 0 || k2 < k1) return 0;
-  laswp_kernel<T><<<ceil_div(n, 128), 128, 0, s>>>(n, A, lda, k1, k2, ipiv, incx);
+  ZG_LAUNCH(kTagLaswp, 0, 4.0 * sizeof(T) * n * (k2 - k1 + 1), s, laswp_kernel<T><<<ceil_div(n, 128), 128, 0, s>>>(n, A, lda, k1, k2, ipiv, incx));
   ZG_CUDA(cudaGetLastError());
   return 0;
 }

@@ -37,9 +37,12 @@ template <> __device__ __forceinline__ __nv_bfloat16 to16(float v) { return __fl
 template <> __device__ __forceinline__ __half to16(float v) { return __float2half_rn(v); }
 
 // rows x k block of a column-major fp32 matrix -> row-major (K-major) 16-bit
-// with row stride ldo (transpose through shared memory).
+// with row stride ldo (transpose through shared memory).  split: the row is
+// written three times, [hi | hi | lo] with hi = bf16(v), lo = bf16(v - hi),
+// each segment ldk wide (the A side of the three-product split GEMM).
 template <typename H>
-__global__ void to_kmajor_t_kernel(int rows, int k, const float *A, long lda, H *out, long ldo) {
+__global__ void to_kmajor_t_kernel(int rows, int k, const float *A, long lda, H *out, long ldo,
+                                   int ldk, bool split) {
   __shared__ float t[32][33];
   const int r0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
   for (int c = threadIdx.y; c < 32; c += 8) {
@@ -49,19 +52,35 @@ __global__ void to_kmajor_t_kernel(int rows, int k, const float *A, long lda, H 
   __syncthreads();
   for (int c = threadIdx.y; c < 32; c += 8) {
     int r = r0 + c, kk = k0 + threadIdx.x;
-    if (r < rows && kk < ldo) out[(long)r * ldo + kk] = to16<H>(kk < k ? t[threadIdx.x][c] : 0.f);
+    if (r >= rows || kk >= ldk) continue;
+    const float v = kk < k ? t[threadIdx.x][c] : 0.f;
+    const H hi = to16<H>(v);
+    H *o = out + (long)r * ldo + kk;
+    o[0] = hi;
+    if (split) {
+      o[ldk] = hi;
+      o[2 * ldk] = to16<H>(v - (float)hi);
+    }
   }
 }
 
 // k x cols block of a column-major fp32 matrix (k contiguous) -> 16-bit with
-// column stride ldo (already K-major).
+// column stride ldo (already K-major).  split: [hi | lo | hi] (the B side).
 template <typename H>
-__global__ void to_kmajor_n_kernel(int k, int cols, const float *A, long lda, H *out, long ldo) {
-  long total = (long)ldo * cols;
+__global__ void to_kmajor_n_kernel(int k, int cols, const float *A, long lda, H *out, long ldo,
+                                   int ldk, bool split) {
+  long total = (long)ldk * cols;
   for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total;
        e += (long)gridDim.x * blockDim.x) {
-    int kk = e % ldo, c = e / ldo;
-    out[(long)c * ldo + kk] = to16<H>(kk < k ? A[kk + (long)c * lda] : 0.f);
+    int kk = e % ldk, c = e / ldk;
+    const float v = kk < k ? A[kk + (long)c * lda] : 0.f;
+    const H hi = to16<H>(v);
+    H *o = out + (long)c * ldo + kk;
+    o[0] = hi;
+    if (split) {
+      o[ldk] = to16<H>(v - (float)hi);
+      o[2 * ldk] = hi;
+    }
   }
 }
 
@@ -69,32 +88,44 @@ static int grid1d(long total) { return (int)std::min<long>((total + 255) / 256, 
 
 int d2s(int m, int n, const double *A, long lda, float *B, long ldb, cudaStream_t s) {
   if (m <= 0 || n <= 0) return 0;
-  d2s_kernel<<<grid1d((long)m * n), 256, 0, s>>>(m, n, A, lda, B, ldb);
+  ZG_LAUNCH(kTagConvert, 0, 0, s, d2s_kernel<<<grid1d((long)m * n), 256, 0, s>>>(m, n, A, lda, B, ldb));
   ZG_CUDA(cudaGetLastError());
   return 0;
 }
 
-static int to_kmajor_t(int prec, int rows, int k, const float *A, long lda, void *out, long ldo,
+// ldk: segment width (>= k, multiple of 8); the operand row stride is ldk,
+// or 3 ldk for the split (bf16x3) form.
+static int to_kmajor_t(int prec, int rows, int k, const float *A, long lda, void *out, int ldk,
                        cudaStream_t s) {
   if (rows <= 0) return 0;
-  dim3 grid(ceil_div(rows, 32), ceil_div(ldo, 32)), blk(32, 8);
-  if (prec == kPrecBF16)
-    to_kmajor_t_kernel<__nv_bfloat16><<<grid, blk, 0, s>>>(rows, k, A, lda, (__nv_bfloat16 *)out, ldo);
+  const bool split = prec == kPrecBF16x3;
+  const long ldo = split ? 3L * ldk : ldk;
+  dim3 grid(ceil_div(rows, 32), ceil_div(ldk, 32)), blk(32, 8);
+  if (prec == kPrecFP16)
+    ZG_LAUNCH(kTagConvert, 0, 4.0 * rows * k + 2.0 * rows * ldo, s,
+              to_kmajor_t_kernel<__half><<<grid, blk, 0, s>>>(rows, k, A, lda, (__half *)out, ldo,
+                                                              ldk, false));
   else
-    to_kmajor_t_kernel<__half><<<grid, blk, 0, s>>>(rows, k, A, lda, (__half *)out, ldo);
-  ZG_CUDA(cudaGetLastError());
+    ZG_LAUNCH(kTagConvert, 0, 4.0 * rows * k + 2.0 * rows * ldo, s,
+              to_kmajor_t_kernel<__nv_bfloat16><<<grid, blk, 0, s>>>(
+                  rows, k, A, lda, (__nv_bfloat16 *)out, ldo, ldk, split));
   return 0;
 }
 
-static int to_kmajor_n(int prec, int k, int cols, const float *A, long lda, void *out, long ldo,
+static int to_kmajor_n(int prec, int k, int cols, const float *A, long lda, void *out, int ldk,
                        cudaStream_t s) {
   if (cols <= 0) return 0;
-  if (prec == kPrecBF16)
-    to_kmajor_n_kernel<__nv_bfloat16><<<grid1d(ldo * cols), 256, 0, s>>>(k, cols, A, lda,
-                                                                         (__nv_bfloat16 *)out, ldo);
+  const bool split = prec == kPrecBF16x3;
+  const long ldo = split ? 3L * ldk : ldk;
+  const int g = grid1d((long)ldk * cols);
+  if (prec == kPrecFP16)
+    ZG_LAUNCH(kTagConvert, 0, 4.0 * cols * k + 2.0 * cols * ldo, s,
+              to_kmajor_n_kernel<__half><<<g, 256, 0, s>>>(k, cols, A, lda, (__half *)out, ldo,
+                                                           ldk, false));
   else
-    to_kmajor_n_kernel<__half><<<grid1d(ldo * cols), 256, 0, s>>>(k, cols, A, lda, (__half *)out, ldo);
-  ZG_CUDA(cudaGetLastError());
+    ZG_LAUNCH(kTagConvert, 0, 4.0 * cols * k + 2.0 * cols * ldo, s,
+              to_kmajor_n_kernel<__nv_bfloat16><<<g, 256, 0, s>>>(
+                  k, cols, A, lda, (__nv_bfloat16 *)out, ldo, ldk, split));
   return 0;
 }
 
@@ -107,9 +138,10 @@ int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cud
     int info = 0;
     return getrf_dev<float>(n, n, A, lda, ipiv, &info, s) < 0 ? kErrCuda : 0;
   }
+  const int segs = prec == kPrecBF16x3 ? 3 : 1;
   void *wl, *wu;
-  ZG_TRY(workspace(s, kSlotL16, sizeof(uint16_t) * (size_t)n * NB, &wl));
-  ZG_TRY(workspace(s, kSlotU16, sizeof(uint16_t) * (size_t)n * NB, &wu));
+  ZG_TRY(workspace(s, kSlotL16, sizeof(uint16_t) * (size_t)n * NB * segs, &wl));
+  ZG_TRY(workspace(s, kSlotU16, sizeof(uint16_t) * (size_t)n * NB * segs, &wu));
   for (int j = 0; j < n; j += NB) {
     const int jb = std::min(NB, n - j);
     // panel: two cooperative FP32 half-panels with an FP32 update between
@@ -135,11 +167,13 @@ int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cud
     ZG_TRY(laswp_dev<float>(rest, A + (long)(j + jb) * lda, lda, j + 1, j + jb, ipiv, 1, s));
     ZG_TRY(trsm_dev<float>(kLeft, kLower, kNoTrans, kUnit, jb, rest, 1.f, A + j + (long)j * lda,
                            lda, A12, lda, s));
-    const long ldk = ((jb + 7) / 8) * 8;
+    // 16-bit operands: L21 (rest x jb) and U12^T (rest x jb), K-major
+    const int ldk = ((jb + 7) / 8) * 8;
     ZG_TRY(to_kmajor_t(prec, rest, jb, A + (j + jb) + (long)j * lda, lda, wl, ldk, s));
     ZG_TRY(to_kmajor_n(prec, jb, rest, A12, lda, wu, ldk, s));
-    ZG_TRY(gemm_tc(rest, rest, jb, -1.f, wl, ldk, wu, ldk, 1.f, A12 + jb, lda,
-                   prec == kPrecBF16 ? 1 : 0, &ctl->status, s));
+    const long ldo = (long)ldk * segs;
+    ZG_TRY(gemm_tc(rest, rest, (int)ldo, -1.f, wl, ldo, wu, ldo, 1.f, A12 + jb, lda,
+                   prec == kPrecFP16 ? 0 : 1, &ctl->status, s));
   }
   return 0;
 }
@@ -181,8 +215,8 @@ int gemv_d(int n, const double *A, long lda, const double *x, const double *b, d
            double *part, cudaStream_t s) {
   const int nparts = ceil_div(n, kGemvCols);
   dim3 grid(ceil_div(n, kGemvRows), nparts);
-  gemv_partial_kernel<<<grid, kGemvRows, 0, s>>>(n, n, A, lda, x, part);
-  gemv_finish_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, nparts, part, b, y);
+  ZG_LAUNCH(kTagGemv, 2.0 * n * n, 8.0 * n * n + 8.0 * n * (nparts + 1), s, gemv_partial_kernel<<<grid, kGemvRows, 0, s>>>(n, n, A, lda, x, part));
+  ZG_LAUNCH(kTagGemv, 0, 0, s, gemv_finish_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, nparts, part, b, y));
   ZG_CUDA(cudaGetLastError());
   return 0;
 }
@@ -265,7 +299,7 @@ int trsv_lowp(int n, const float *A, long lda, double *x, bool upper, unsigned *
   if (n <= 0) return 0;
   const int nblk = ceil_div(n, kTB);
   ZG_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned) * (nblk + 1), s));
-  trsv_lowp_kernel<<<nblk, 256, 0, s>>>(n, A, lda, x, work + 1, work, upper, status);
+  ZG_LAUNCH(kTagTrsv, 1.0 * n * n, 2.0 * n * n + 16.0 * n, s, trsv_lowp_kernel<<<nblk, 256, 0, s>>>(n, A, lda, x, work + 1, work, upper, status));
   ZG_CUDA(cudaGetLastError());
   return 0;
 }
@@ -294,7 +328,7 @@ int perm_from_ipiv(int n, const int *ipiv_dev, int *perm_dev, cudaStream_t s) {
 // d = (LU)^-1 P r applied in FP64 with the FP32 factors.
 int lu_apply(int n, const float *LU, long lda, const int *perm, const double *r, double *d,
              unsigned *work, unsigned *status, cudaStream_t s) {
-  gather_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, r, perm, d);
+  ZG_LAUNCH(kTagVector, 0, 0, s, gather_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, r, perm, d));
   ZG_CUDA(cudaGetLastError());
   ZG_TRY(trsv_lowp(n, LU, lda, d, false, work, status, s));
   ZG_TRY(trsv_lowp(n, LU, lda, d, true, work, status, s));
@@ -400,8 +434,8 @@ static int host_scalar(const double *d, double *h, cudaStream_t s) {
 static int berr_of(int n, const double *A, long lda, const double *b, const double *x, double anrm,
                    double bnrm, IRWork &w, double *berr, cudaStream_t s) {
   ZG_TRY(gemv_d(n, A, lda, x, b, w.r, w.part, s));
-  absmax_kernel<<<1, 256, 0, s>>>(n, w.r, w.scal);
-  absmax_kernel<<<1, 256, 0, s>>>(n, x, w.scal + 1);
+  ZG_LAUNCH(kTagVector, 0, 0, s, absmax_kernel<<<1, 256, 0, s>>>(n, w.r, w.scal));
+  ZG_LAUNCH(kTagVector, 0, 0, s, absmax_kernel<<<1, 256, 0, s>>>(n, x, w.scal + 1));
   ZG_CUDA(cudaGetLastError());
   double h[2];
   ZG_CUDA(cudaMemcpyAsync(h, w.scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -420,12 +454,12 @@ static int gmres_correction(int n, const double *A, long lda, const float *LU, l
   double *V = w.V;  // n x (m+1)
   // z = M^-1 r ; beta = ||z|| ; v0 = z / beta
   ZG_TRY(lu_apply(n, LU, ldlu, perm, w.r, w.w, w.tw, &ctl->status, s));
-  nrm2_kernel<<<1, 256, 0, s>>>(n, w.w, w.scal);
+  ZG_LAUNCH(kTagVector, 0, 0, s, nrm2_kernel<<<1, 256, 0, s>>>(n, w.w, w.scal));
   double beta;
   ZG_TRY(host_scalar(w.scal, &beta, s));
   ZG_CUDA(cudaMemsetAsync(w.d, 0, sizeof(double) * n, s));
   if (!(beta > 0) || !std::isfinite(beta)) return 0;
-  scale_copy_kernel<<<b1, 256, 0, s>>>(n, 1.0 / beta, w.w, V);
+  ZG_LAUNCH(kTagVector, 0, 0, s, scale_copy_kernel<<<b1, 256, 0, s>>>(n, 1.0 / beta, w.w, V));
   std::vector<double> H((m + 1) * m, 0.0), cs(m), sn(m), g(m + 1, 0.0);
   g[0] = beta;
   int k = 0;
@@ -437,10 +471,10 @@ static int gmres_correction(int n, const double *A, long lda, const float *LU, l
     // classical Gram-Schmidt, twice
     ZG_CUDA(cudaMemsetAsync(w.h, 0, sizeof(double) * 2 * (m + 1), s));
     for (int pass = 0; pass < 2; ++pass) {
-      gs_dots_kernel<<<k + 1, 256, 0, s>>>(n, k + 1, V, n, w.w, w.h + pass * (m + 1));
-      gs_update_kernel<<<b1, 256, 0, s>>>(n, k + 1, V, n, w.h + pass * (m + 1), w.w);
+      ZG_LAUNCH(kTagVector, 0, 0, s, gs_dots_kernel<<<k + 1, 256, 0, s>>>(n, k + 1, V, n, w.w, w.h + pass * (m + 1)));
+      ZG_LAUNCH(kTagVector, 0, 0, s, gs_update_kernel<<<b1, 256, 0, s>>>(n, k + 1, V, n, w.h + pass * (m + 1), w.w));
     }
-    nrm2_kernel<<<1, 256, 0, s>>>(n, w.w, w.scal);
+    ZG_LAUNCH(kTagVector, 0, 0, s, nrm2_kernel<<<1, 256, 0, s>>>(n, w.w, w.scal));
     ZG_CUDA(cudaGetLastError());
     std::vector<double> hh(2 * (m + 1));
     ZG_CUDA(cudaMemcpyAsync(hh.data(), w.h, sizeof(double) * 2 * (m + 1), cudaMemcpyDeviceToHost, s));
@@ -450,7 +484,7 @@ static int gmres_correction(int n, const double *A, long lda, const float *LU, l
     for (int i = 0; i <= k; ++i) hcol[i] = hh[i] + hh[(m + 1) + i];
     hcol[k + 1] = hk1;
     if (hk1 > 0 && k + 1 <= m)
-      scale_copy_kernel<<<b1, 256, 0, s>>>(n, 1.0 / hk1, w.w, V + (long)(k + 1) * n);
+      ZG_LAUNCH(kTagVector, 0, 0, s, scale_copy_kernel<<<b1, 256, 0, s>>>(n, 1.0 / hk1, w.w, V + (long)(k + 1) * n));
     // Givens rotations on the new Hessenberg column
     for (int i = 0; i < k; ++i) {
       const double t = cs[i] * hcol[i] + sn[i] * hcol[i + 1];
@@ -480,7 +514,7 @@ static int gmres_correction(int n, const double *A, long lda, const float *LU, l
   }
   ZG_CUDA(cudaMemcpyAsync(w.h, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
   ZG_CUDA(cudaMemsetAsync(w.d, 0, sizeof(double) * n, s));
-  combine_kernel<<<b1, 256, 0, s>>>(n, k, V, n, w.h, w.d);
+  ZG_LAUNCH(kTagVector, 0, 0, s, combine_kernel<<<b1, 256, 0, s>>>(n, k, V, n, w.h, w.d));
   ZG_CUDA(cudaGetLastError());
   return 0;
 }
@@ -514,8 +548,8 @@ int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, l
   w.tw = (unsigned *)p;
 
   // ||A||_inf
-  rowabs_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, A, lda, w.r);
-  absmax_kernel<<<1, 256, 0, s>>>(n, w.r, w.scal);
+  ZG_LAUNCH(kTagGemv, 0, 0, s, rowabs_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, A, lda, w.r));
+  ZG_LAUNCH(kTagVector, 0, 0, s, absmax_kernel<<<1, 256, 0, s>>>(n, w.r, w.scal));
   ZG_CUDA(cudaGetLastError());
   double anrm;
   ZG_TRY(host_scalar(w.scal, &anrm, s));
@@ -543,7 +577,7 @@ int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, l
   for (int q = 0; q < nrhs; ++q) {
     const double *b = B + (long)q * ldb;
     double *x = X + (long)q * ldx;
-    absmax_kernel<<<1, 256, 0, s>>>(n, b, w.scal);
+    ZG_LAUNCH(kTagVector, 0, 0, s, absmax_kernel<<<1, 256, 0, s>>>(n, b, w.scal));
     double bnrm;
     ZG_TRY(host_scalar(w.scal, &bnrm, s));
     // x0 = (LU)^-1 P b
@@ -562,7 +596,7 @@ int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, l
       } else {
         ZG_TRY(lu_apply(n, LU, n, perm, w.r, w.d, w.tw, &ctl->status, s));
       }
-      axpy_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, 1.0, w.d, x);
+      ZG_LAUNCH(kTagVector, 0, 0, s, axpy_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, 1.0, w.d, x));
       ZG_CUDA(cudaGetLastError());
       ++it;
       ZG_TRY(berr_of(n, A, lda, b, x, anrm, bnrm, w, &berr, s));

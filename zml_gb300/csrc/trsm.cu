@@ -83,7 +83,7 @@ template <typename T> int scale_dev(int m, int n, T alpha, T *B, long ldb, cudaS
   long total = (long)m * n;
   int blocks = (int)((total + 255) / 256);
   if (blocks > 152 * 32) blocks = 152 * 32;
-  scale_kernel<T><<<blocks, 256, 0, s>>>(m, n, alpha, B, ldb);
+  ZG_LAUNCH(kTagVector, 0, 0, s, scale_kernel<T><<<blocks, 256, 0, s>>>(m, n, alpha, B, ldb));
   ZG_CUDA(cudaGetLastError());
   return 0;
 }
@@ -108,7 +108,7 @@ template <typename T>
 int transpose_dev(int rows, int cols, const T *src, long lds, T *dst, long ldd, cudaStream_t s) {
   if (rows <= 0 || cols <= 0) return 0;
   dim3 grid(ceil_div(rows, 32), ceil_div(cols, 32)), block(32, 8);
-  transpose_kernel<T><<<grid, block, 0, s>>>(rows, cols, src, lds, dst, ldd);
+  ZG_LAUNCH(kTagConvert, 0, 0, s, transpose_kernel<T><<<grid, block, 0, s>>>(rows, cols, src, lds, dst, ldd));
   ZG_CUDA(cudaGetLastError());
   return 0;
 }
@@ -118,8 +118,8 @@ static int diag_solve(int nbk, int nrhs, const T *A, long lda, bool transA, bool
                       bool lower_eff, bool unit, T *B, long ldb, cudaStream_t s) {
   if (nbk <= 0 || nrhs <= 0) return 0;
   int grid = ceil_div(nrhs, kTrsmNC);
-  trsm_diag_kernel<T><<<grid, 256, 0, s>>>(nbk, nrhs, A, lda, transA, right, lower_eff, unit, B,
-                                           ldb);
+  ZG_LAUNCH(kTagTrsmDiag, 1.0 * nbk * nbk * nrhs, sizeof(T) * (1.0 * nbk * nbk + 2.0 * nbk * nrhs), s, trsm_diag_kernel<T><<<grid, 256, 0, s>>>(nbk, nrhs, A, lda, transA, right, lower_eff, unit, B,
+                                           ldb));
   ZG_CUDA(cudaGetLastError());
   return 0;
 }
