@@ -90,6 +90,7 @@ enum Slot : int {
   kSlotLowLU = 10,            // low-precision factor copy, pivots, permutation
   kSlotL16 = 11, kSlotU16 = 12,  // 16-bit L21 / U12 operands of the tensor-core update
   kSlotBatch = 13,            // batched solver descriptors
+  kSlotSwap = 14,             // composed row-interchange pairs
   kNumSlots = 16
 };
 

@@ -14,6 +14,7 @@
 // NaN never displaces the running maximum, so ties resolve to the lowest row.
 // The column is scaled by the reciprocal of the pivot when |pivot| >= sfmin,
 // else divided (getrf2.zig:65-87).
+#include <algorithm>
 #include <cooperative_groups.h>
 
 #include "common.cuh"
@@ -170,7 +171,11 @@ int panel_lu(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *c
   ZG_TRY(device_info(&di));
   // rows per CTA: at least 8, at most what fits in shared memory
   const size_t limit = di.smem_optin - 4096;
-  int nblk = min(di.num_sms, ceil_div(m, 8));
+  // FP32: 256-row slabs (fewer CTAs meet at each column's barrier; the rank-1
+  // work per CTA stays small on the FP32 pipes).  FP64: every SM, because
+  // the slab's rank-1 updates run at the low FP64 rate.
+  const int min_rows = sizeof(T) == 4 ? 256 : 8;
+  int nblk = min(di.num_sms, ceil_div(m, min_rows));
   int R = ceil_div(m, nblk);
   if ((size_t)R * nb * sizeof(T) > limit) {
     set_last_error("panel_lu: panel %d x %d too tall for %d SMs", m, nb, di.num_sms);
@@ -197,32 +202,103 @@ int panel_lu(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *c
   return 0;
 }
 
-// Row interchanges (laswp.zig): one thread per column applies the pivots
-// k1..k2 (1-based) in order, or in reverse for incx < 0.
-template <typename T>
-__global__ void laswp_kernel(int n, T *A, long lda, int k1, int k2, const int *__restrict__ ipiv,
-                             int incx) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n) return;
-  T *col = A + (long)j * lda;
-  if (incx > 0) {
-    for (int i = k1 - 1; i < k2; ++i) {
-      const int ip = ipiv[i] - 1;
-      if (ip != i) { T t = col[i]; col[i] = col[ip]; col[ip] = t; }
+// Row interchanges (laswp.zig:12-96).  The sequence of swaps k1..k2 (1-based,
+// forward for incx > 0, backward otherwise) is first composed by one warp
+// into a list of (destination row, source row) pairs -- at most 2 (k2-k1+1)
+// rows move -- and then every column gathers its moved rows and scatters
+// them in parallel, so no column walks a chain of dependent swaps.
+constexpr int kSwapMax = 256;  // pivots per composed chunk
+
+__global__ void laswp_prep_kernel(int k1, int k2, const int *__restrict__ ipiv, int incx,
+                                  int *pairs, int *npairs) {
+  __shared__ int seg[kSwapMax];      // content of rows base .. base+len-1
+  __shared__ int orow[kSwapMax];     // rows outside the segment that were touched
+  __shared__ int ocont[kSwapMax];    // and their contents
+  __shared__ int nout;
+  const int lane = threadIdx.x;
+  const int base = k1 - 1, len = k2 - k1 + 1;
+  for (int t = lane; t < len; t += 32) seg[t] = base + t;
+  if (lane == 0) nout = 0;
+  __syncwarp();
+  for (int s = 0; s < len; ++s) {
+    const int i = incx > 0 ? base + s : base + len - 1 - s;
+    const int p = ipiv[i] - 1;
+    if (p == i) continue;
+    if (p >= base && p < base + len) {
+      if (lane == 0) { int t = seg[i - base]; seg[i - base] = seg[p - base]; seg[p - base] = t; }
+    } else {
+      int found = -1;
+      for (int t0 = 0; t0 < nout; t0 += 32) {
+        const int t = t0 + lane;
+        const unsigned hit = __ballot_sync(0xffffffffu, t < nout && orow[t] == p);
+        if (hit) { found = t0 + __ffs(hit) - 1; break; }
+      }
+      if (lane == 0) {
+        if (found < 0) { found = nout; orow[found] = p; ocont[found] = p; nout = found + 1; }
+        int t = seg[i - base]; seg[i - base] = ocont[found]; ocont[found] = t;
+      }
     }
-  } else {
-    for (int i = k2 - 1; i >= k1 - 1; --i) {
-      const int ip = ipiv[i] - 1;
-      if (ip != i) { T t = col[i]; col[i] = col[ip]; col[ip] = t; }
-    }
+    __syncwarp();
   }
+  __syncwarp();
+  if (lane == 0) {
+    int np = 0;
+    for (int t = 0; t < len; ++t)
+      if (seg[t] != base + t) { pairs[2 * np] = base + t; pairs[2 * np + 1] = seg[t]; ++np; }
+    for (int t = 0; t < nout; ++t)
+      if (ocont[t] != orow[t]) { pairs[2 * np] = orow[t]; pairs[2 * np + 1] = ocont[t]; ++np; }
+    *npairs = np;
+  }
+}
+
+// 32 columns per CTA: all moved values of the 32 columns are staged in shared
+// memory (every read completes before any write), then scattered.
+template <typename T>
+__global__ void __launch_bounds__(256) laswp_apply_kernel(int n, T *A, long lda,
+                                                          const int *__restrict__ pairs,
+                                                          const int *__restrict__ npairs) {
+  extern __shared__ __align__(16) unsigned char lsw_raw[];
+  T *stage = reinterpret_cast<T *>(lsw_raw);  // stage[t * 32 + lane]
+  const int np = *npairs;
+  const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
+  const int c = blockIdx.x * 32 + lane;
+  T *col = A + (long)c * lda;
+  if (c < n)
+    for (int t = g; t < np; t += 8) stage[t * 32 + lane] = col[__ldg(pairs + 2 * t + 1)];
+  __syncthreads();
+  if (c < n)
+    for (int t = g; t < np; t += 8) col[__ldg(pairs + 2 * t)] = stage[t * 32 + lane];
 }
 
 template <typename T>
 int laswp_dev(int n, T *A, long lda, int k1, int k2, const int *ipiv, int incx, cudaStream_t s) {
   if (n <= 0 || k2 < k1) return 0;
-  ZG_LAUNCH(kTagLaswp, 0, 4.0 * sizeof(T) * n * (k2 - k1 + 1), s, laswp_kernel<T><<<ceil_div(n, 128), 128, 0, s>>>(n, A, lda, k1, k2, ipiv, incx));
-  ZG_CUDA(cudaGetLastError());
+  for (int q = 0;; ++q) {  // long pivot ranges in chunks, in application order
+    int lo, hi;
+    if (incx > 0) {
+      lo = k1 + q * kSwapMax;
+      if (lo > k2) break;
+      hi = std::min(k2, lo + kSwapMax - 1);
+    } else {
+      hi = k2 - q * kSwapMax;
+      if (hi < k1) break;
+      lo = std::max(k1, hi - kSwapMax + 1);
+    }
+    void *w;
+    ZG_TRY(workspace(s, kSlotSwap, sizeof(int) * (4 * kSwapMax + 8), &w));
+    int *pairs = (int *)w, *np = pairs + 4 * kSwapMax;
+    ZG_LAUNCH(kTagLaswp, 0, 0, s, laswp_prep_kernel<<<1, 32, 0, s>>>(lo, hi, ipiv, incx, pairs, np));
+    const size_t smem = sizeof(T) * 32 * 2 * (hi - lo + 1);
+    static bool attr = false;
+    if (!attr) {
+      ZG_CUDA(cudaFuncSetAttribute(laswp_apply_kernel<T>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(sizeof(T) * 32 * 2 * kSwapMax)));
+      attr = true;
+    }
+    ZG_LAUNCH(kTagLaswp, 0, 4.0 * sizeof(T) * n * (hi - lo + 1), s,
+              laswp_apply_kernel<T><<<ceil_div(n, 32), 256, smem, s>>>(n, A, lda, pairs, np));
+  }
   return 0;
 }
 

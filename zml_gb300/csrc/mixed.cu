@@ -222,85 +222,164 @@ int gemv_d(int n, const double *A, long lda, const double *x, const double *b, d
 }
 
 // ---------------------------------------------------------------------------
-// Triangular solves with the FP32 factors, FP64 vectors ("sync-free"): one CTA
-// per 64-row block, claimed in order through a ticket; a block accumulates
-// L(block, 0:block) x(0:block) as earlier blocks publish their pieces, then
-// solves its diagonal block and publishes.  Lower = unit lower (forward),
-// upper = non-unit upper (backward).
-constexpr int kTB = 64;
+// Triangular solves with the FP32 factors, FP64 vectors ("sync-free").
+//
+// The factor is cut into 128-row blocks.  One CTA per block row claims its
+// block in dependency order through a ticket, streams its off-diagonal tiles
+// L(blk, cb) (the load of the next tile is issued before waiting for the
+// flag of the current one, so the HBM stream overlaps the dependency chain),
+// accumulates L(blk, cb) x(cb) in FP64 as earlier blocks publish, and then
+// applies the FP64 inverse of its diagonal block (precomputed once per
+// factorization) and publishes x(blk).  lower = unit lower L (forward),
+// upper = non-unit upper U (backward).
+constexpr int kTB = 128;          // block rows
+constexpr int kTT = 512;          // threads: 128 rows x 4 column phases
+constexpr int kTC = kTB / 4;      // columns per phase and tile
 
-__global__ void __launch_bounds__(256) trsv_lowp_kernel(int n, const float *__restrict__ A, long lda,
-                                                         double *x, unsigned *flags,
-                                                         unsigned *ticket, bool upper,
-                                                         unsigned *status) {
+__device__ __forceinline__ void trsv_load_tile(float (&v)[kTC], const float *A, long lda, int row,
+                                               bool row_ok, int c0, int ph, int n) {
+#pragma unroll
+  for (int j = 0; j < kTC; ++j) {
+    const int c = c0 + ph + 4 * j;
+    v[j] = (row_ok && c < n) ? __ldcs(A + row + (long)c * lda) : 0.f;
+  }
+}
+
+__global__ void __launch_bounds__(kTT) trsv_lowp_kernel(int n, const float *__restrict__ A, long lda,
+                                                        const double *__restrict__ Dinv, double *x,
+                                                        unsigned *flags, unsigned *ticket,
+                                                        bool upper, unsigned *status) {
   __shared__ unsigned sb;
   __shared__ double part[4][kTB];
-  __shared__ double xb[kTB];
-  __shared__ float D[kTB][kTB + 1];
+  __shared__ double xs[kTB];
   const int tid = threadIdx.x;
   if (tid == 0) sb = atomicAdd(ticket, 1u);
   __syncthreads();
   const int nblk = (n + kTB - 1) / kTB;
-  const int t = sb;                                // order of processing
-  const int blk = upper ? nblk - 1 - t : t;        // block row handled
+  const int t = sb;
+  const int blk = upper ? nblk - 1 - t : t;
   const int r0 = blk * kTB, rows = min(kTB, n - r0);
-  const int lr = tid % kTB, ph = tid / kTB;        // row in block, column phase
+  const int lr = tid % kTB, ph = tid / kTB;
+  const int row = r0 + lr;
+  const bool row_ok = lr < rows;
   double acc = 0;
-  // off-diagonal blocks in dependency order
+  float cur[kTC], nxt[kTC];
+  if (t > 0) trsv_load_tile(cur, A, lda, row, row_ok, (upper ? nblk - 1 : 0) * kTB, ph, n);
   for (int q = 0; q < t; ++q) {
-    const int cb = upper ? nblk - 1 - q : q;       // block column, already solved
+    const int cb = upper ? nblk - 1 - q : q;
+    if (q + 1 < t)
+      trsv_load_tile(nxt, A, lda, row, row_ok, (upper ? nblk - 2 - q : q + 1) * kTB, ph, n);
     if (tid == 0) {
-      long spins = 0;
-      while (atomicAdd(&flags[cb], 0u) == 0u) {
+      long long spins = 0;
+      while (ld_acquire(&flags[cb]) == 0u) {
         if (++spins > kSpinLimit) { atomicOr(status, kStatusQueueTimeout); break; }
+        __nanosleep(20);
       }
-      __threadfence();
     }
     __syncthreads();
-    const int c0 = cb * kTB, cols = min(kTB, n - c0);
-    if (lr < rows) {
-      const float *a = A + (r0 + lr) + (long)c0 * lda;
-      for (int c = ph; c < cols; c += 4) acc = fma((double)a[(long)c * lda], __ldcg(x + c0 + c), acc);
-    }
+    const int c0 = cb * kTB;
+    if (tid < kTB) xs[tid] = (c0 + tid < n) ? __ldcg(x + c0 + tid) : 0.0;
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kTC; ++j) acc = fma((double)cur[j], xs[ph + 4 * j], acc);
+#pragma unroll
+    for (int j = 0; j < kTC; ++j) cur[j] = nxt[j];
   }
   part[ph][lr] = acc;
-  // diagonal block into shared memory
-  for (int e = tid; e < kTB * kTB; e += 256) {
-    const int i = e % kTB, j = e / kTB;
-    D[i][j] = (i < rows && j < rows) ? A[(r0 + i) + (long)(r0 + j) * lda] : 0.f;
-  }
   __syncthreads();
-  if (tid < kTB) {
-    double v = 0;
-    if (tid < rows) v = x[r0 + tid] - (part[0][tid] + part[1][tid] + part[2][tid] + part[3][tid]);
-    xb[tid] = v;
-  }
+  if (tid < kTB)
+    xs[tid] = row_ok ? x[row] - (part[0][tid] + part[1][tid] + part[2][tid] + part[3][tid]) : 0.0;
   __syncthreads();
-  // substitution on the diagonal block
-  for (int st = 0; st < rows; ++st) {
-    const int k = upper ? rows - 1 - st : st;
-    if (upper && tid == k) xb[k] = xb[k] / (double)D[k][k];
-    __syncthreads();
-    const double xk = xb[k];
-    const bool upd = upper ? (tid < k) : (tid > k && tid < rows);
-    if (upd) xb[tid] -= (double)D[tid][k] * xk;
-    __syncthreads();
-  }
-  if (tid < rows) x[r0 + tid] = xb[tid];
+  // x(blk) = inv(D) * rhs, D^-1 column-major in Dinv + blk * kTB^2
+  const double *Di = Dinv + (long)blk * kTB * kTB;
+  double y = 0;
+#pragma unroll 8
+  for (int j = ph; j < kTB; j += 4) y = fma(Di[lr + (long)j * kTB], xs[j], y);
+  part[ph][lr] = y;
+  __syncthreads();
+  if (tid < kTB && row_ok) x[row] = part[0][tid] + part[1][tid] + part[2][tid] + part[3][tid];
   __threadfence();
   __syncthreads();
   if (tid == 0) atomicExch(&flags[blk], 1u);
 }
 
+// FP64 inverses of the kTB x kTB diagonal blocks of the FP32 LU factors:
+// inv(L_bb) (unit lower) into Linv, inv(U_bb) into Uinv, each column-major
+// kTB x kTB per block (zero outside the triangle).  In-place triangular
+// inversion in shared memory, one CTA per block.
+__global__ void __launch_bounds__(512) invert_diag_kernel(int n, const float *__restrict__ A,
+                                                          long lda, double *Linv, double *Uinv) {
+  extern __shared__ double T[];  // T[i + j * kTB]
+  const int blk = blockIdx.x, upper = blockIdx.y;
+  const int r0 = blk * kTB, rows = min(kTB, n - r0);
+  const int tid = threadIdx.x;
+  for (int e = tid; e < kTB * kTB; e += blockDim.x) {
+    const int i = e % kTB, j = e / kTB;
+    double v = 0;
+    if (i < rows && j < rows) {
+      if (upper) v = i <= j ? (double)A[(r0 + i) + (long)(r0 + j) * lda] : 0.0;
+      else v = i > j ? (double)A[(r0 + i) + (long)(r0 + j) * lda] : (i == j ? 1.0 : 0.0);
+    } else if (i == j) {
+      v = 1.0;  // padding rows of the last block: identity
+    }
+    T[e] = v;
+  }
+  __syncthreads();
+  if (upper) {
+    // columns left to right: T(j,j) = 1/U(j,j); T(0:j, j) = -T(j,j) T(0:j,0:j) U(0:j, j)
+    for (int j = 0; j < kTB; ++j) {
+      const double djj = 1.0 / T[j + j * kTB];
+      double v = 0;
+      if (tid < j) {
+        for (int k = tid; k < j; ++k) v = fma(T[tid + k * kTB], T[k + j * kTB], v);
+      }
+      __syncthreads();
+      if (tid < j) T[tid + j * kTB] = -djj * v;
+      if (tid == j) T[j + j * kTB] = djj;
+      __syncthreads();
+    }
+  } else {
+    // columns right to left: T(j+1:, j) = -T(j+1:, j+1:) L(j+1:, j)
+    for (int j = kTB - 1; j >= 0; --j) {
+      double v = 0;
+      const int i = j + 1 + tid;
+      if (i < kTB) {
+        for (int k = j + 1; k <= i; ++k) v = fma(T[i + k * kTB], T[k + j * kTB], v);
+      }
+      __syncthreads();
+      if (i < kTB) T[i + j * kTB] = -v;
+      __syncthreads();
+    }
+  }
+  double *out = (upper ? Uinv : Linv) + (long)blk * kTB * kTB;
+  for (int e = tid; e < kTB * kTB; e += blockDim.x) out[e] = T[e];
+}
+
+int invert_diag_blocks(int n, const float *A, long lda, double *Linv, double *Uinv, cudaStream_t s) {
+  const int nblk = ceil_div(n, kTB);
+  const size_t smem = sizeof(double) * kTB * kTB;
+  static bool attr = false;
+  if (!attr) {
+    ZG_CUDA(cudaFuncSetAttribute(invert_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+    attr = true;
+  }
+  ZG_LAUNCH(kTagTrsv, 2.0 * nblk * kTB * kTB * kTB / 3, 8.0 * nblk * kTB * kTB * 3, s,
+            invert_diag_kernel<<<dim3(nblk, 2), 512, smem, s>>>(n, A, lda, Linv, Uinv));
+  return 0;
+}
+
 // x <- op^-1 x with op = unit-lower L (upper=false) or non-unit upper U of
-// the FP32 LU factors in A.  flags/ticket: n/64 + 1 zeroed words (device).
-int trsv_lowp(int n, const float *A, long lda, double *x, bool upper, unsigned *work,
-              unsigned *status, cudaStream_t s) {
+// the FP32 LU factors in A, Dinv their diagonal-block inverses.
+// work: n/128 + 1 unsigned words (device).
+int trsv_lowp(int n, const float *A, long lda, const double *Dinv, double *x, bool upper,
+              unsigned *work, unsigned *status, cudaStream_t s) {
   if (n <= 0) return 0;
   const int nblk = ceil_div(n, kTB);
   ZG_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned) * (nblk + 1), s));
-  ZG_LAUNCH(kTagTrsv, 1.0 * n * n, 2.0 * n * n + 16.0 * n, s, trsv_lowp_kernel<<<nblk, 256, 0, s>>>(n, A, lda, x, work + 1, work, upper, status));
-  ZG_CUDA(cudaGetLastError());
+  ZG_LAUNCH(kTagTrsv, 1.0 * n * n, 2.0 * n * n + 16.0 * n + 8.0 * nblk * kTB * kTB, s,
+            trsv_lowp_kernel<<<nblk, kTT, 0, s>>>(n, A, lda, Dinv, x, work + 1, work, upper,
+                                                   status));
   return 0;
 }
 
@@ -326,12 +405,22 @@ int perm_from_ipiv(int n, const int *ipiv_dev, int *perm_dev, cudaStream_t s) {
 }
 
 // d = (LU)^-1 P r applied in FP64 with the FP32 factors.
-int lu_apply(int n, const float *LU, long lda, const int *perm, const double *r, double *d,
-             unsigned *work, unsigned *status, cudaStream_t s) {
+struct LowLU {
+  const float *LU;
+  long lda;
+  const int *perm;
+  const double *Linv, *Uinv;
+};
+
+int lu_apply(int n, const LowLU &f, const double *r, double *d, unsigned *work, unsigned *status,
+             cudaStream_t s) {
+  const float *LU = f.LU;
+  const long lda = f.lda;
+  const int *perm = f.perm;
   ZG_LAUNCH(kTagVector, 0, 0, s, gather_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, r, perm, d));
   ZG_CUDA(cudaGetLastError());
-  ZG_TRY(trsv_lowp(n, LU, lda, d, false, work, status, s));
-  ZG_TRY(trsv_lowp(n, LU, lda, d, true, work, status, s));
+  ZG_TRY(trsv_lowp(n, LU, lda, f.Linv, d, false, work, status, s));
+  ZG_TRY(trsv_lowp(n, LU, lda, f.Uinv, d, true, work, status, s));
   return 0;
 }
 
@@ -447,13 +536,12 @@ static int berr_of(int n, const double *A, long lda, const double *b, const doub
 
 // GMRES on (LU)^-1 A d = (LU)^-1 r with restart m; returns after `inner`
 // iterations or when the preconditioned residual fell by `rtol`.
-static int gmres_correction(int n, const double *A, long lda, const float *LU, long ldlu,
-                            const int *perm, IRWork &w, int m, double rtol, int *iters,
-                            Control *ctl, cudaStream_t s) {
+static int gmres_correction(int n, const double *A, long lda, const LowLU &f, IRWork &w, int m,
+                            double rtol, int *iters, Control *ctl, cudaStream_t s) {
   const int b1 = ceil_div(n, 256);
   double *V = w.V;  // n x (m+1)
   // z = M^-1 r ; beta = ||z|| ; v0 = z / beta
-  ZG_TRY(lu_apply(n, LU, ldlu, perm, w.r, w.w, w.tw, &ctl->status, s));
+  ZG_TRY(lu_apply(n, f, w.r, w.w, w.tw, &ctl->status, s));
   ZG_LAUNCH(kTagVector, 0, 0, s, nrm2_kernel<<<1, 256, 0, s>>>(n, w.w, w.scal));
   double beta;
   ZG_TRY(host_scalar(w.scal, &beta, s));
@@ -467,7 +555,7 @@ static int gmres_correction(int n, const double *A, long lda, const float *LU, l
   for (; k < m; ++k) {
     // w = M^-1 A v_k
     ZG_TRY(gemv_d(n, A, lda, V + (long)k * n, nullptr, w.d, w.part, s));
-    ZG_TRY(lu_apply(n, LU, ldlu, perm, w.d, w.w, w.tw, &ctl->status, s));
+    ZG_TRY(lu_apply(n, f, w.d, w.w, w.tw, &ctl->status, s));
     // classical Gram-Schmidt, twice
     ZG_CUDA(cudaMemsetAsync(w.h, 0, sizeof(double) * 2 * (m + 1), s));
     for (int pass = 0; pass < 2; ++pass) {
@@ -529,10 +617,16 @@ int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, l
   // workspace: FP32 factor copy, ipiv, perm and FP64 vectors
   void *wf, *wv;
   const size_t nf = (size_t)n * n;
-  ZG_TRY(workspace(s, kSlotLowLU, sizeof(float) * nf + 2 * sizeof(int) * (size_t)n + 256, &wf));
+  const size_t ninv = (size_t)ceil_div(n, kTB) * kTB * kTB;
+  ZG_TRY(workspace(s, kSlotLowLU,
+                   sizeof(float) * nf + 2 * sizeof(double) * ninv + 2 * sizeof(int) * (size_t)n + 512,
+                   &wf));
   float *LU = (float *)wf;
-  int *ipiv = (int *)((char *)wf + sizeof(float) * nf);
+  double *Linv = (double *)(((uintptr_t)(LU + nf) + 255) & ~(uintptr_t)255);
+  double *Uinv = Linv + ninv;
+  int *ipiv = (int *)(Uinv + ninv);
   int *perm = ipiv + n;
+  const LowLU f{LU, (long)n, perm, Linv, Uinv};
   const int nparts = ceil_div(n, kGemvCols);
   const size_t nv = (size_t)n * (4 + nparts + (m + 1)) + 4 * (m + 2) + 64;
   ZG_TRY(workspace(s, kSlotIRVec, sizeof(double) * nv + sizeof(unsigned) * (n / kTB + 8), &wv));
@@ -572,6 +666,7 @@ int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, l
   res->info = info;
   if (info != 0) return 0;
   ZG_TRY(perm_from_ipiv(n, ipiv, perm, s));
+  ZG_TRY(invert_diag_blocks(n, LU, n, Linv, Uinv, s));
 
   res->converged = 1;
   for (int q = 0; q < nrhs; ++q) {
@@ -581,7 +676,7 @@ int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, l
     double bnrm;
     ZG_TRY(host_scalar(w.scal, &bnrm, s));
     // x0 = (LU)^-1 P b
-    ZG_TRY(lu_apply(n, LU, n, perm, b, x, w.tw, &ctl->status, s));
+    ZG_TRY(lu_apply(n, f, b, x, w.tw, &ctl->status, s));
     double berr = 0, prev = INFINITY;
     ZG_TRY(berr_of(n, A, lda, b, x, anrm, bnrm, w, &berr, s));  // leaves r = b - A x
     if (q == 0) res->berr_history[0] = berr;
@@ -592,9 +687,9 @@ int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, l
       if (tol == 0.0 && it > 0 && berr > 0.5 * prev) break;  // stagnated at its floor
       prev = berr;
       if (o.mode == kModeGMRES) {
-        ZG_TRY(gmres_correction(n, A, lda, LU, n, perm, w, m, o.gmres_rtol, &res->inner_iters, ctl, s));
+        ZG_TRY(gmres_correction(n, A, lda, f, w, m, o.gmres_rtol, &res->inner_iters, ctl, s));
       } else {
-        ZG_TRY(lu_apply(n, LU, n, perm, w.r, w.d, w.tw, &ctl->status, s));
+        ZG_TRY(lu_apply(n, f, w.r, w.d, w.tw, &ctl->status, s));
       }
       ZG_LAUNCH(kTagVector, 0, 0, s, axpy_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, 1.0, w.d, x));
       ZG_CUDA(cudaGetLastError());
