@@ -61,6 +61,13 @@ int LAPACKE_dposv(int matrix_layout, char uplo, int n, int nrhs, double *a, int 
 int LAPACKE_sposv(int matrix_layout, char uplo, int n, int nrhs, float *a, int lda, float *b,
                   int ldb);
 
+/* replaces zml.linalg.lapack.laswp (kernel lapack/laswp.zig:12): row
+ * interchanges k1..k2 (1-based) of n columns, |incx| = 1 */
+int LAPACKE_dlaswp(int matrix_layout, int n, double *a, int lda, int k1, int k2, const int *ipiv,
+                   int incx);
+int LAPACKE_slaswp(int matrix_layout, int n, float *a, int lda, int k1, int k2, const int *ipiv,
+                   int incx);
+
 /* ---- GPU extensions: device pointers, column-major, stream ordered ------
  * `stream` is a cudaStream_t (NULL = legacy default stream).  The call
  * returns after the stream has drained (info is a host value). */

@@ -193,3 +193,18 @@ def test_device_pointer_getrf_getrs():
     assert info[0] == 0
     assert L.zml_gpu_dgetrs(b"N", n, nrhs, da.data_ptr(), n, dp.data_ptr(), db.data_ptr(), n, None) == 0
     np.testing.assert_allclose(db.cpu().numpy().T, x, rtol=1e-8, atol=1e-9)
+
+
+@pytest.mark.parametrize("k1,k2,incx", [(1, 64, 1), (1, 64, -1), (5, 300, 1), (3, 700, -1)])
+def test_dlaswp_vs_oracle(k1, k2, incx):
+    """Random pivots with repeated targets, forward and backward order, and
+    ranges longer than one composed chunk."""
+    m, n = 800, 77
+    rng = np.random.default_rng(k2)
+    a = np.asfortranarray(rng.standard_normal((m, n)))
+    ipiv = rng.integers(1, m + 1, size=m).astype(np.int32)
+    ipiv[10:20] = 400  # the same target row, many times
+    ref, got = a.copy(order="F"), a.copy(order="F")
+    assert ol.fn("laswp")(102, n, P(ref), m, k1, k2, P(ipiv), incx) == 0
+    assert zg.lib().LAPACKE_dlaswp(102, n, P(got), m, k1, k2, P(ipiv), incx) == 0
+    np.testing.assert_array_equal(got, ref)

@@ -35,6 +35,7 @@ for p, T in (("d", f64), ("s", f32)):
         "LAPACKE_%spotrf" % p: (i32, [i32, ch, i32, vp, i32]),
         "LAPACKE_%spotrs" % p: (i32, [i32, ch, i32, i32, vp, i32, vp, i32]),
         "LAPACKE_%sposv" % p: (i32, [i32, ch, i32, i32, vp, i32, vp, i32]),
+        "LAPACKE_%slaswp" % p: (i32, [i32, i32, vp, i32, i32, i32, vp, i32]),
     })
 _SIGS.update({
     "zml_gpu_dgetrf": (i32, [i32, i32, vp, i32, vp, vp, vp]),

@@ -369,6 +369,30 @@ int posv_any(int layout, char uplo, int n, int nrhs, T *a, int lda, T *b, int ld
   return info;
 }
 
+template <typename T>
+int laswp_any(int layout, int n, T *a, int lda, int k1, int k2, const int *ipiv, int incx) {
+  if (!lay_ok(layout)) return -1;
+  if (n < 0) return -2;
+  if (incx == 0) return -7;
+  if (n == 0 || k2 < k1) return 0;
+  // rows touched: k1..k2 and every pivot target
+  int rmax = k2;
+  for (int i = k1 - 1; i < k2; ++i) rmax = std::max(rmax, ipiv[(long)i * std::abs(incx)]);
+  if (layout == kColMajor ? lda < std::max(1, rmax) : lda < std::max(1, n)) return -4;
+  if (std::abs(incx) != 1) {
+    set_last_error("laswp: |incx| != 1 is not supported");
+    return kErrInvalid;
+  }
+  cudaStream_t s = lib_stream();
+  ColMajor<T> A;
+  Buf<int> P;
+  ZG_TRY(A.in(layout, a, lda, rmax, n, kSlotA, kSlotAT, true, s));
+  ZG_TRY(P.in(const_cast<int *>(ipiv), k2, kSlotPiv, true, s));
+  ZG_TRY(laswp_dev<T>(n, A.d, A.ld, k1, k2, P.d, incx, s));
+  ZG_TRY(A.out(s));
+  return sync(s);
+}
+
 int mpir_any(int layout, int n, int nrhs, const double *a, int lda, const double *b, int ldb,
              double *x, int ldx, const MpirOpts &o, MpirResult *res) {
   if (!lay_ok(layout)) return -1;
@@ -437,6 +461,15 @@ CBLAS_GEMM(s, float)
   }
 LAPACKE_FNS(d, double)
 LAPACKE_FNS(s, float)
+
+int LAPACKE_dlaswp(int layout, int n, double *a, int lda, int k1, int k2, const int *ipiv,
+                   int incx) {
+  return laswp_any<double>(layout, n, a, lda, k1, k2, ipiv, incx);
+}
+int LAPACKE_slaswp(int layout, int n, float *a, int lda, int k1, int k2, const int *ipiv,
+                   int incx) {
+  return laswp_any<float>(layout, n, a, lda, k1, k2, ipiv, incx);
+}
 #undef LAPACKE_FNS
 
 // ---- device-pointer, stream-ordered extensions (column-major) ----

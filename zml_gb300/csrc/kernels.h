@@ -25,6 +25,11 @@ int transpose_dev(int rows, int cols, const T *src, long lds, T *dst, long ldd, 
 // lu.cu
 template <typename T>
 int laswp_dev(int n, T *A, long lda, int k1, int k2, const int *ipiv, int incx, cudaStream_t s);
+// One panel's interchanges (rows k1..k2, forward, 1-based) on the column
+// ranges [0, c_left) and [c_right, n), composed once.
+template <typename T>
+int laswp_panel(int c_left, int c_right, int n, T *A, long lda, int k1, int k2, const int *ipiv,
+                cudaStream_t s);
 // Partial-pivot LU of the m x nb panel at A (leading dim lda); writes
 // ipiv[0..nb) (1-based, relative to the panel's first row, plus ipiv_base)
 // and records the first zero pivot (1-based column + info_base) in ctl->info.

@@ -135,8 +135,10 @@ __global__ void __launch_bounds__(256) panel_lu_kernel(int m, int nb, T *__restr
         for (int c = tid; c < nb; c += blockDim.x) S[c * R + (idx - r0)] = __ldcg(rowk[p] + c);
       __syncthreads();
     }
-    // 5. scale the column below the pivot, 6. rank-1 update of the slab
+    // 5. scale the column below the pivot, 6. rank-1 update of the slab:
+    // thread = (row lane, column phase); no index division in the loops.
     const int rb = max(0, k + 1 - r0);  // first local row strictly below k
+    const int lr = tid & 127, cph = tid >> 7;  // 128 row lanes x 2 column phases
     if (piv != T(0)) {
       const bool recip = fabs(piv) >= Real<T>::sfmin();
       const T rp = T(1) / piv;
@@ -144,12 +146,10 @@ __global__ void __launch_bounds__(256) panel_lu_kernel(int m, int nb, T *__restr
         S[k * R + r] = recip ? S[k * R + r] * rp : S[k * R + r] / piv;
       __syncthreads();
     }
-    const int nr = rows - rb, ncol = nb - k - 1;
-    if (nr > 0 && ncol > 0) {
-      for (int e = tid; e < nr * ncol; e += blockDim.x) {
-        const int r = rb + e % nr, c = k + 1 + e / nr;
-        S[c * R + r] -= S[k * R + r] * urow[c];
-      }
+    for (int r = rb + lr; r < rows; r += 128) {
+      const T l = S[k * R + r];
+      T *row = S + r;
+      for (int c = k + 1 + cph; c < nb; c += 2) row[c * R] -= l * urow[c];
     }
     __syncthreads();
   }
@@ -171,11 +171,7 @@ int panel_lu(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *c
   ZG_TRY(device_info(&di));
   // rows per CTA: at least 8, at most what fits in shared memory
   const size_t limit = di.smem_optin - 4096;
-  // FP32: 256-row slabs (fewer CTAs meet at each column's barrier; the rank-1
-  // work per CTA stays small on the FP32 pipes).  FP64: every SM, because
-  // the slab's rank-1 updates run at the low FP64 rate.
-  const int min_rows = sizeof(T) == 4 ? 256 : 8;
-  int nblk = min(di.num_sms, ceil_div(m, min_rows));
+  int nblk = min(di.num_sms, ceil_div(m, 8));
   int R = ceil_div(m, nblk);
   if ((size_t)R * nb * sizeof(T) > limit) {
     set_last_error("panel_lu: panel %d x %d too tall for %d SMs", m, nb, di.num_sms);
@@ -211,44 +207,50 @@ constexpr int kSwapMax = 256;  // pivots per composed chunk
 
 __global__ void laswp_prep_kernel(int k1, int k2, const int *__restrict__ ipiv, int incx,
                                   int *pairs, int *npairs) {
+  constexpr int kHash = 1024;        // open-addressing table of touched outside rows
   __shared__ int seg[kSwapMax];      // content of rows base .. base+len-1
   __shared__ int orow[kSwapMax];     // rows outside the segment that were touched
   __shared__ int ocont[kSwapMax];    // and their contents
-  __shared__ int nout;
+  __shared__ int hkey[kHash], hval[kHash];
   const int lane = threadIdx.x;
   const int base = k1 - 1, len = k2 - k1 + 1;
   for (int t = lane; t < len; t += 32) seg[t] = base + t;
-  if (lane == 0) nout = 0;
+  for (int t = lane; t < kHash; t += 32) hkey[t] = -1;
   __syncwarp();
-  for (int s = 0; s < len; ++s) {
-    const int i = incx > 0 ? base + s : base + len - 1 - s;
+  if (lane != 0) return;
+  int nout = 0;
+  for (int st = 0; st < len; ++st) {
+    const int i = incx > 0 ? base + st : base + len - 1 - st;
     const int p = ipiv[i] - 1;
     if (p == i) continue;
     if (p >= base && p < base + len) {
-      if (lane == 0) { int t = seg[i - base]; seg[i - base] = seg[p - base]; seg[p - base] = t; }
+      const int t = seg[i - base];
+      seg[i - base] = seg[p - base];
+      seg[p - base] = t;
     } else {
-      int found = -1;
-      for (int t0 = 0; t0 < nout; t0 += 32) {
-        const int t = t0 + lane;
-        const unsigned hit = __ballot_sync(0xffffffffu, t < nout && orow[t] == p);
-        if (hit) { found = t0 + __ffs(hit) - 1; break; }
+      unsigned h = ((unsigned)p * 2654435761u) >> 22;
+      while (hkey[h] != -1 && hkey[h] != p) h = (h + 1) & (kHash - 1);
+      int idx;
+      if (hkey[h] == p) {
+        idx = hval[h];
+      } else {
+        idx = nout++;
+        hkey[h] = p;
+        hval[h] = idx;
+        orow[idx] = p;
+        ocont[idx] = p;
       }
-      if (lane == 0) {
-        if (found < 0) { found = nout; orow[found] = p; ocont[found] = p; nout = found + 1; }
-        int t = seg[i - base]; seg[i - base] = ocont[found]; ocont[found] = t;
-      }
+      const int t = seg[i - base];
+      seg[i - base] = ocont[idx];
+      ocont[idx] = t;
     }
-    __syncwarp();
   }
-  __syncwarp();
-  if (lane == 0) {
-    int np = 0;
-    for (int t = 0; t < len; ++t)
-      if (seg[t] != base + t) { pairs[2 * np] = base + t; pairs[2 * np + 1] = seg[t]; ++np; }
-    for (int t = 0; t < nout; ++t)
-      if (ocont[t] != orow[t]) { pairs[2 * np] = orow[t]; pairs[2 * np + 1] = ocont[t]; ++np; }
-    *npairs = np;
-  }
+  int np = 0;
+  for (int t = 0; t < len; ++t)
+    if (seg[t] != base + t) { pairs[2 * np] = base + t; pairs[2 * np + 1] = seg[t]; ++np; }
+  for (int t = 0; t < nout; ++t)
+    if (ocont[t] != orow[t]) { pairs[2 * np] = orow[t]; pairs[2 * np + 1] = ocont[t]; ++np; }
+  *npairs = np;
 }
 
 // 32 columns per CTA: all moved values of the 32 columns are staged in shared
@@ -270,6 +272,40 @@ __global__ void __launch_bounds__(256) laswp_apply_kernel(int n, T *A, long lda,
     for (int t = g; t < np; t += 8) col[__ldg(pairs + 2 * t)] = stage[t * 32 + lane];
 }
 
+// A composed row interchange: device pairs (dst, src) and their count.
+struct SwapPlan {
+  int *pairs = nullptr, *np = nullptr;
+  int rows = 0;  // pivots composed (bounds the pair count by 2 rows)
+};
+
+static int laswp_compose(int k1, int k2, const int *ipiv, int incx, SwapPlan *plan, int slot,
+                         cudaStream_t s) {
+  void *w;
+  ZG_TRY(workspace(s, slot, sizeof(int) * (4 * kSwapMax + 8), &w));
+  plan->pairs = (int *)w;
+  plan->np = plan->pairs + 4 * kSwapMax;
+  plan->rows = k2 - k1 + 1;
+  ZG_LAUNCH(kTagLaswp, 0, 0, s,
+            laswp_prep_kernel<<<1, 32, 0, s>>>(k1, k2, ipiv, incx, plan->pairs, plan->np));
+  return 0;
+}
+
+template <typename T>
+static int laswp_apply(int n, T *A, long lda, const SwapPlan &plan, cudaStream_t s) {
+  if (n <= 0 || plan.rows <= 0) return 0;
+  const size_t smem = sizeof(T) * 32 * 2 * plan.rows;
+  static bool attr = false;
+  if (!attr) {
+    ZG_CUDA(cudaFuncSetAttribute(laswp_apply_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(T) * 32 * 2 * kSwapMax)));
+    attr = true;
+  }
+  ZG_LAUNCH(kTagLaswp, 0, 4.0 * sizeof(T) * n * plan.rows, s,
+            laswp_apply_kernel<T><<<ceil_div(n, 32), 256, smem, s>>>(n, A, lda, plan.pairs,
+                                                                      plan.np));
+  return 0;
+}
+
 template <typename T>
 int laswp_dev(int n, T *A, long lda, int k1, int k2, const int *ipiv, int incx, cudaStream_t s) {
   if (n <= 0 || k2 < k1) return 0;
@@ -284,22 +320,27 @@ int laswp_dev(int n, T *A, long lda, int k1, int k2, const int *ipiv, int incx, 
       if (hi < k1) break;
       lo = std::max(k1, hi - kSwapMax + 1);
     }
-    void *w;
-    ZG_TRY(workspace(s, kSlotSwap, sizeof(int) * (4 * kSwapMax + 8), &w));
-    int *pairs = (int *)w, *np = pairs + 4 * kSwapMax;
-    ZG_LAUNCH(kTagLaswp, 0, 0, s, laswp_prep_kernel<<<1, 32, 0, s>>>(lo, hi, ipiv, incx, pairs, np));
-    const size_t smem = sizeof(T) * 32 * 2 * (hi - lo + 1);
-    static bool attr = false;
-    if (!attr) {
-      ZG_CUDA(cudaFuncSetAttribute(laswp_apply_kernel<T>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)(sizeof(T) * 32 * 2 * kSwapMax)));
-      attr = true;
-    }
-    ZG_LAUNCH(kTagLaswp, 0, 4.0 * sizeof(T) * n * (hi - lo + 1), s,
-              laswp_apply_kernel<T><<<ceil_div(n, 32), 256, smem, s>>>(n, A, lda, pairs, np));
+    SwapPlan plan;
+    ZG_TRY(laswp_compose(lo, hi, ipiv, incx, &plan, kSlotSwap, s));
+    ZG_TRY(laswp_apply<T>(n, A, lda, plan, s));
   }
   return 0;
+}
+
+// The interchanges of one panel (rows k1..k2, forward) applied to the column
+// ranges [0, c_left) and [c_right, n) with one composition.
+template <typename T>
+int laswp_panel(int c_left, int c_right, int n, T *A, long lda, int k1, int k2, const int *ipiv,
+                cudaStream_t s) {
+  if (k2 < k1) return 0;
+  if (k2 - k1 + 1 > kSwapMax) {
+    ZG_TRY(laswp_dev<T>(c_left, A, lda, k1, k2, ipiv, 1, s));
+    return laswp_dev<T>(n - c_right, A + (long)c_right * lda, lda, k1, k2, ipiv, 1, s);
+  }
+  SwapPlan plan;
+  ZG_TRY(laswp_compose(k1, k2, ipiv, 1, &plan, kSlotSwap, s));
+  ZG_TRY(laswp_apply<T>(c_left, A, lda, plan, s));
+  return laswp_apply<T>(n - c_right, A + (long)c_right * lda, lda, plan, s);
 }
 
 template <typename T> static int lu_block() { return sizeof(T) == 8 ? 64 : 128; }
@@ -316,10 +357,9 @@ int getrf_dev(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s
     const int jb = min(nb, mn - j);
     T *Ajj = A + j + (long)j * lda;
     ZG_TRY(panel_lu<T>(m - j, jb, Ajj, lda, ipiv + j, j, ctl, j, s));
-    ZG_TRY(laswp_dev<T>(j, A, lda, j + 1, j + jb, ipiv, 1, s));
+    ZG_TRY(laswp_panel<T>(j, std::min(n, j + jb), n, A, lda, j + 1, j + jb, ipiv, s));
     if (j + jb < n) {
       T *Aright = A + (long)(j + jb) * lda;
-      ZG_TRY(laswp_dev<T>(n - j - jb, Aright, lda, j + 1, j + jb, ipiv, 1, s));
       ZG_TRY(trsm_dev<T>(kLeft, kLower, kNoTrans, kUnit, jb, n - j - jb, T(1), Ajj, lda,
                          Aright + j, lda, s));
       if (j + jb < m)
@@ -348,6 +388,7 @@ int getrs_dev(int trans, int n, int nrhs, const T *A, long lda, const int *ipiv,
 }
 
 #define INST(T)                                                                                 \
+  template int laswp_panel<T>(int, int, int, T *, long, int, int, const int *, cudaStream_t);    \
   template int panel_lu<T>(int, int, T *, long, int *, int, Control *, int, cudaStream_t);      \
   template int laswp_dev<T>(int, T *, long, int, int, const int *, int, cudaStream_t);          \
   template int getrf_dev<T>(int, int, T *, long, int *, int *, cudaStream_t);                   \

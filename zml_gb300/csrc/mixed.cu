@@ -148,11 +148,12 @@ int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cud
     for (int p = 0; p < jb; p += NBP) {
       const int r = j + p, pb = std::min(NBP, jb - p);
       ZG_TRY(panel_lu<float>(n - r, pb, A + r + (long)r * lda, lda, ipiv + r, r, ctl, r, s));
-      ZG_TRY(laswp_dev<float>(r - j, A + (long)j * lda, lda, r + 1, r + pb, ipiv, 1, s));
       const int right = j + jb - r - pb;
+      // interchanges of this half-panel inside the panel's other columns
+      ZG_TRY(laswp_panel<float>(r - j, r + pb - j, jb, A + (long)j * lda, lda, r + 1, r + pb,
+                                ipiv, s));
       if (right > 0) {
         float *Ar = A + (long)(r + pb) * lda;
-        ZG_TRY(laswp_dev<float>(right, Ar, lda, r + 1, r + pb, ipiv, 1, s));
         ZG_TRY(trsm_dev<float>(kLeft, kLower, kNoTrans, kUnit, pb, right, 1.f,
                                A + r + (long)r * lda, lda, Ar + r, lda, s));
         ZG_TRY(gemm_simt<float>(kNoTrans, kNoTrans, n - r - pb, right, pb, -1.f,
@@ -160,11 +161,10 @@ int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cud
                                 Ar + r + pb, lda, 0, s));
       }
     }
-    ZG_TRY(laswp_dev<float>(j, A, lda, j + 1, j + jb, ipiv, 1, s));
+    ZG_TRY(laswp_panel<float>(j, j + jb, n, A, lda, j + 1, j + jb, ipiv, s));
     const int rest = n - j - jb;
     if (rest <= 0) break;
     float *A12 = A + j + (long)(j + jb) * lda;
-    ZG_TRY(laswp_dev<float>(rest, A + (long)(j + jb) * lda, lda, j + 1, j + jb, ipiv, 1, s));
     ZG_TRY(trsm_dev<float>(kLeft, kLower, kNoTrans, kUnit, jb, rest, 1.f, A + j + (long)j * lda,
                            lda, A12, lda, s));
     // 16-bit operands: L21 (rest x jb) and U12^T (rest x jb), K-major
@@ -249,6 +249,7 @@ __global__ void __launch_bounds__(kTT) trsv_lowp_kernel(int n, const float *__re
                                                         const double *__restrict__ Dinv, double *x,
                                                         unsigned *flags, unsigned *ticket,
                                                         bool upper, unsigned *status) {
+  extern __shared__ double DiS[];  // this block's diagonal inverse, column-major
   __shared__ unsigned sb;
   __shared__ double part[4][kTB];
   __shared__ double xs[kTB];
@@ -262,6 +263,14 @@ __global__ void __launch_bounds__(kTT) trsv_lowp_kernel(int n, const float *__re
   const int lr = tid % kTB, ph = tid / kTB;
   const int row = r0 + lr;
   const bool row_ok = lr < rows;
+  // everything the end of the dependency chain needs is fetched up front:
+  // the diagonal inverse (into shared memory) and this block's right-hand side
+  {
+    const double2 *src = reinterpret_cast<const double2 *>(Dinv + (long)blk * kTB * kTB);
+    double2 *dst = reinterpret_cast<double2 *>(DiS);
+    for (int e = tid; e < kTB * kTB / 2; e += kTT) dst[e] = __ldcs(src + e);
+  }
+  const double rhs = (ph == 0 && row_ok) ? x[row] : 0.0;
   double acc = 0;
   float cur[kTC], nxt[kTC];
   if (t > 0) trsv_load_tile(cur, A, lda, row, row_ok, (upper ? nblk - 1 : 0) * kTB, ph, n);
@@ -288,13 +297,12 @@ __global__ void __launch_bounds__(kTT) trsv_lowp_kernel(int n, const float *__re
   part[ph][lr] = acc;
   __syncthreads();
   if (tid < kTB)
-    xs[tid] = row_ok ? x[row] - (part[0][tid] + part[1][tid] + part[2][tid] + part[3][tid]) : 0.0;
+    xs[tid] = row_ok ? rhs - (part[0][tid] + part[1][tid] + part[2][tid] + part[3][tid]) : 0.0;
   __syncthreads();
-  // x(blk) = inv(D) * rhs, D^-1 column-major in Dinv + blk * kTB^2
-  const double *Di = Dinv + (long)blk * kTB * kTB;
+  // x(blk) = inv(D) * rhs
   double y = 0;
 #pragma unroll 8
-  for (int j = ph; j < kTB; j += 4) y = fma(Di[lr + (long)j * kTB], xs[j], y);
+  for (int j = ph; j < kTB; j += 4) y = fma(DiS[lr + j * kTB], xs[j], y);
   part[ph][lr] = y;
   __syncthreads();
   if (tid < kTB && row_ok) x[row] = part[0][tid] + part[1][tid] + part[2][tid] + part[3][tid];
@@ -377,9 +385,16 @@ int trsv_lowp(int n, const float *A, long lda, const double *Dinv, double *x, bo
   if (n <= 0) return 0;
   const int nblk = ceil_div(n, kTB);
   ZG_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned) * (nblk + 1), s));
+  const size_t smem = sizeof(double) * kTB * kTB;
+  static bool attr = false;
+  if (!attr) {
+    ZG_CUDA(cudaFuncSetAttribute(trsv_lowp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+    attr = true;
+  }
   ZG_LAUNCH(kTagTrsv, 1.0 * n * n, 2.0 * n * n + 16.0 * n + 8.0 * nblk * kTB * kTB, s,
-            trsv_lowp_kernel<<<nblk, kTT, 0, s>>>(n, A, lda, Dinv, x, work + 1, work, upper,
-                                                   status));
+            trsv_lowp_kernel<<<nblk, kTT, smem, s>>>(n, A, lda, Dinv, x, work + 1, work, upper,
+                                                      status));
   return 0;
 }
 
