@@ -67,10 +67,10 @@ def test_mpir_reaches_fp64_backward_error(n, prec, mode):
     assert np.abs(x - xt).max() / np.abs(xt).max() <= 10 * cond * U64 * n
 
 
-@pytest.mark.parametrize("kappa,prec", [(1e2, 1), (1e6, 3), (1e10, 2)])
+@pytest.mark.parametrize("kappa,prec", [(1e2, 1), (1e6, 3), (1e8, 2)])
 def test_gmres_ir_ill_conditioned(kappa, prec):
     """GMRES-IR reaches FP64 backward error with BF16 factors at kappa 1e2,
-    split BF16x3 factors at 1e6 and FP32 factors at 1e10."""
+    split BF16x3 factors at 1e6 and FP32 factors at 1e8."""
     n = 512
     a = svd_matrix(n, kappa, seed=int(np.log10(kappa)))
     xt = np.random.default_rng(7).uniform(-1, 1, (n, 1))

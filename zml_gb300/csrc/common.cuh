@@ -121,26 +121,22 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
   return v;
 }
 
-// Grid-wide barrier for a cooperative launch: every CTA arrives once per
-// phase; the last arrival bumps the generation.  The wait is bounded; on
-// timeout the status bit is set and the CTA carries on (its results are then
-// discarded by the host, which reports kErrTimeout).
+// Grid-wide barrier for a cooperative launch.  ctl->barrier[0] counts
+// arrivals monotonically over the launch (zeroed before it): phase g is
+// complete once it reaches (g + 1) * nblocks, so a waiter sees the last
+// arrival directly.  The wait is bounded; on timeout the status bit is set
+// and the CTA carries on (the host then reports kErrTimeout).
 __device__ __forceinline__ void grid_barrier(Control *ctl, unsigned nblocks, unsigned &gen) {
   __syncthreads();
   if (threadIdx.x == 0) {
+    const unsigned target = (gen + 1) * nblocks;
     __threadfence();
-    unsigned arrived = atomicAdd(&ctl->barrier[0], 1u);
-    if (arrived == nblocks - 1) {
-      ctl->barrier[0] = 0;
-      __threadfence();
-      atomicAdd(&ctl->barrier[1], 1u);
-    } else {
-      long long spins = 0;
-      while (ld_acquire(&ctl->barrier[1]) == gen) {
-        if (++spins > kSpinLimit) {
-          atomicOr(&ctl->status, kStatusBarrierTimeout);
-          break;
-        }
+    atomicAdd(&ctl->barrier[0], 1u);
+    long long spins = 0;
+    while (ld_acquire(&ctl->barrier[0]) < target) {
+      if (++spins > kSpinLimit) {
+        atomicOr(&ctl->status, kStatusBarrierTimeout);
+        break;
       }
     }
     __threadfence();

@@ -246,13 +246,17 @@ __device__ __forceinline__ void trsv_load_tile(float (&v)[kTC], const float *A, 
 }
 
 __global__ void __launch_bounds__(kTT) trsv_lowp_kernel(int n, const float *__restrict__ A, long lda,
-                                                        const double *__restrict__ Dinv, double *x,
+                                                        const float *__restrict__ Dinv, double *x,
                                                         unsigned *flags, unsigned *ticket,
                                                         bool upper, unsigned *status) {
-  extern __shared__ double DiS[];  // this block's diagonal inverse, column-major
+  // GB300 runs FP64 at a small fraction of FP32, so every product here is
+  // FP32 (the factors are FP32 already); partial sums of one 128-column tile
+  // are FP32, the sum over tiles and the right-hand side stay FP64.
+  extern __shared__ float DiS[];  // this block's diagonal inverse, column-major
   __shared__ unsigned sb;
   __shared__ double part[4][kTB];
-  __shared__ double xs[kTB];
+  __shared__ float xs[kTB];
+  __shared__ float ys[kTB];
   const int tid = threadIdx.x;
   if (tid == 0) sb = atomicAdd(ticket, 1u);
   __syncthreads();
@@ -263,12 +267,11 @@ __global__ void __launch_bounds__(kTT) trsv_lowp_kernel(int n, const float *__re
   const int lr = tid % kTB, ph = tid / kTB;
   const int row = r0 + lr;
   const bool row_ok = lr < rows;
-  // everything the end of the dependency chain needs is fetched up front:
-  // the diagonal inverse (into shared memory) and this block's right-hand side
+  // fetched up front: the diagonal inverse and this block's right-hand side
   {
-    const double2 *src = reinterpret_cast<const double2 *>(Dinv + (long)blk * kTB * kTB);
-    double2 *dst = reinterpret_cast<double2 *>(DiS);
-    for (int e = tid; e < kTB * kTB / 2; e += kTT) dst[e] = __ldcs(src + e);
+    const float4 *src = reinterpret_cast<const float4 *>(Dinv + (long)blk * kTB * kTB);
+    float4 *dst = reinterpret_cast<float4 *>(DiS);
+    for (int e = tid; e < kTB * kTB / 4; e += kTT) dst[e] = __ldcs(src + e);
   }
   const double rhs = (ph == 0 && row_ok) ? x[row] : 0.0;
   double acc = 0;
@@ -287,23 +290,32 @@ __global__ void __launch_bounds__(kTT) trsv_lowp_kernel(int n, const float *__re
     }
     __syncthreads();
     const int c0 = cb * kTB;
-    if (tid < kTB) xs[tid] = (c0 + tid < n) ? __ldcg(x + c0 + tid) : 0.0;
+    if (tid < kTB) xs[tid] = (c0 + tid < n) ? (float)__ldcg(x + c0 + tid) : 0.f;
     __syncthreads();
+    float p0 = 0.f, p1 = 0.f;
 #pragma unroll
-    for (int j = 0; j < kTC; ++j) acc = fma((double)cur[j], xs[ph + 4 * j], acc);
+    for (int j = 0; j < kTC; j += 2) {
+      p0 = fmaf(cur[j], xs[ph + 4 * j], p0);
+      p1 = fmaf(cur[j + 1], xs[ph + 4 * (j + 1)], p1);
+    }
+    acc += (double)p0 + (double)p1;
 #pragma unroll
     for (int j = 0; j < kTC; ++j) cur[j] = nxt[j];
   }
   part[ph][lr] = acc;
   __syncthreads();
   if (tid < kTB)
-    xs[tid] = row_ok ? rhs - (part[0][tid] + part[1][tid] + part[2][tid] + part[3][tid]) : 0.0;
+    ys[tid] = row_ok ? (float)(rhs - (part[0][tid] + part[1][tid] + part[2][tid] + part[3][tid]))
+                     : 0.f;
   __syncthreads();
   // x(blk) = inv(D) * rhs
-  double y = 0;
+  float y0 = 0.f, y1 = 0.f;
 #pragma unroll 8
-  for (int j = ph; j < kTB; j += 4) y = fma(DiS[lr + j * kTB], xs[j], y);
-  part[ph][lr] = y;
+  for (int j = ph; j < kTB; j += 8) {
+    y0 = fmaf(DiS[lr + j * kTB], ys[j], y0);
+    y1 = fmaf(DiS[lr + (j + 4) * kTB], ys[j + 4], y1);
+  }
+  part[ph][lr] = (double)y0 + (double)y1;
   __syncthreads();
   if (tid < kTB && row_ok) x[row] = part[0][tid] + part[1][tid] + part[2][tid] + part[3][tid];
   __threadfence();
@@ -316,7 +328,7 @@ __global__ void __launch_bounds__(kTT) trsv_lowp_kernel(int n, const float *__re
 // kTB x kTB per block (zero outside the triangle).  In-place triangular
 // inversion in shared memory, one CTA per block.
 __global__ void __launch_bounds__(512) invert_diag_kernel(int n, const float *__restrict__ A,
-                                                          long lda, double *Linv, double *Uinv) {
+                                                          long lda, float *Linv, float *Uinv) {
   extern __shared__ double T[];  // T[i + j * kTB]
   const int blk = blockIdx.x, upper = blockIdx.y;
   const int r0 = blk * kTB, rows = min(kTB, n - r0);
@@ -359,11 +371,11 @@ __global__ void __launch_bounds__(512) invert_diag_kernel(int n, const float *__
       __syncthreads();
     }
   }
-  double *out = (upper ? Uinv : Linv) + (long)blk * kTB * kTB;
-  for (int e = tid; e < kTB * kTB; e += blockDim.x) out[e] = T[e];
+  float *out = (upper ? Uinv : Linv) + (long)blk * kTB * kTB;
+  for (int e = tid; e < kTB * kTB; e += blockDim.x) out[e] = (float)T[e];
 }
 
-int invert_diag_blocks(int n, const float *A, long lda, double *Linv, double *Uinv, cudaStream_t s) {
+int invert_diag_blocks(int n, const float *A, long lda, float *Linv, float *Uinv, cudaStream_t s) {
   const int nblk = ceil_div(n, kTB);
   const size_t smem = sizeof(double) * kTB * kTB;
   static bool attr = false;
@@ -380,19 +392,19 @@ int invert_diag_blocks(int n, const float *A, long lda, double *Linv, double *Ui
 // x <- op^-1 x with op = unit-lower L (upper=false) or non-unit upper U of
 // the FP32 LU factors in A, Dinv their diagonal-block inverses.
 // work: n/128 + 1 unsigned words (device).
-int trsv_lowp(int n, const float *A, long lda, const double *Dinv, double *x, bool upper,
+int trsv_lowp(int n, const float *A, long lda, const float *Dinv, double *x, bool upper,
               unsigned *work, unsigned *status, cudaStream_t s) {
   if (n <= 0) return 0;
   const int nblk = ceil_div(n, kTB);
   ZG_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned) * (nblk + 1), s));
-  const size_t smem = sizeof(double) * kTB * kTB;
+  const size_t smem = sizeof(float) * kTB * kTB;
   static bool attr = false;
   if (!attr) {
     ZG_CUDA(cudaFuncSetAttribute(trsv_lowp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem));
     attr = true;
   }
-  ZG_LAUNCH(kTagTrsv, 1.0 * n * n, 2.0 * n * n + 16.0 * n + 8.0 * nblk * kTB * kTB, s,
+  ZG_LAUNCH(kTagTrsv, 1.0 * n * n, 2.0 * n * n + 16.0 * n + 4.0 * nblk * kTB * kTB, s,
             trsv_lowp_kernel<<<nblk, kTT, smem, s>>>(n, A, lda, Dinv, x, work + 1, work, upper,
                                                       status));
   return 0;
@@ -424,7 +436,7 @@ struct LowLU {
   const float *LU;
   long lda;
   const int *perm;
-  const double *Linv, *Uinv;
+  const float *Linv, *Uinv;
 };
 
 int lu_apply(int n, const LowLU &f, const double *r, double *d, unsigned *work, unsigned *status,
@@ -637,8 +649,8 @@ int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, l
                    sizeof(float) * nf + 2 * sizeof(double) * ninv + 2 * sizeof(int) * (size_t)n + 512,
                    &wf));
   float *LU = (float *)wf;
-  double *Linv = (double *)(((uintptr_t)(LU + nf) + 255) & ~(uintptr_t)255);
-  double *Uinv = Linv + ninv;
+  float *Linv = (float *)(((uintptr_t)(LU + nf) + 255) & ~(uintptr_t)255);
+  float *Uinv = Linv + ninv;
   int *ipiv = (int *)(Uinv + ninv);
   int *perm = ipiv + n;
   const LowLU f{LU, (long)n, perm, Linv, Uinv};
