@@ -102,6 +102,8 @@ typedef struct zml_mpir_result {
   int iters;             /* outer refinement steps (max over right-hand sides) */
   int inner_iters;       /* total GMRES iterations */
   int converged;         /* 1 if every right-hand side reached FP64 backward error */
+  int switched_f64;      /* 1 if the solves moved from FP32 to FP64 arithmetic */
+  int reserved;
   double berr;           /* largest final ||b - A x||inf / (||A||inf ||x||inf + ||b||inf) */
   double factor_ms;      /* device time of the factorization */
   double berr_history[32]; /* backward error per outer step, first right-hand side */

@@ -76,7 +76,8 @@ def test_gmres_ir_ill_conditioned(kappa, prec):
     xt = np.random.default_rng(7).uniform(-1, 1, (n, 1))
     b = np.asfortranarray(a @ xt)
     x, res = solve(a, b, prec, 1)
-    assert res.info == 0 and res.converged
+    assert res.info == 0 and res.converged, (res.berr, list(res.berr_history[:res.iters + 1]),
+                                              res.switched_f64)
     assert berr(a, x, b) <= 2 * fp64_berr(a, b) + U64
 
 

@@ -52,7 +52,8 @@ _SIGS.update({
 
 class MpirResult(C.Structure):
     _fields_ = [("info", C.c_int), ("iters", C.c_int), ("inner_iters", C.c_int),
-                ("converged", C.c_int), ("berr", C.c_double), ("factor_ms", C.c_double),
+                ("converged", C.c_int), ("switched_f64", C.c_int), ("reserved", C.c_int),
+                ("berr", C.c_double), ("factor_ms", C.c_double),
                 ("berr_history", C.c_double * 32)]
 
 

@@ -415,7 +415,7 @@ int mpir_any(int layout, int n, int nrhs, const double *a, int lda, const double
 
 }  // namespace
 
-static_assert(sizeof(MpirResult) == 4 * sizeof(int) + 34 * sizeof(double), "zml_mpir_result layout");
+static_assert(sizeof(MpirResult) == 6 * sizeof(int) + 34 * sizeof(double), "zml_mpir_result layout");
 
 extern "C" {
 

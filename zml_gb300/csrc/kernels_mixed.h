@@ -8,6 +8,8 @@ namespace zg {
 // (hi*hi + hi*lo + lo*hi) accumulated in FP32 -- about 16 significant bits.
 enum : int { kPrecFP16 = 0, kPrecBF16 = 1, kPrecFP32 = 2, kPrecBF16x3 = 3 };
 enum : int { kModeIR = 0, kModeGMRES = 1 };
+// Arithmetic of the preconditioner / correction solves with the FP32 factors.
+enum : int { kApplyAuto = 0, kApplyF32 = 1, kApplyF64 = 2 };
 
 struct MpirOpts {
   int prec = kPrecBF16;     // factor precision of the trailing updates
@@ -16,6 +18,7 @@ struct MpirOpts {
   int max_iter = 30;        // outer refinement steps
   int gmres_restart = 50;   // inner GMRES iterations per outer step
   double gmres_rtol = 1e-6; // inner relative tolerance (preconditioned residual)
+  int apply = kApplyAuto;   // FP32 first, FP64 once refinement stops improving
 };
 
 struct MpirResult {
@@ -23,6 +26,8 @@ struct MpirResult {
   int iters = 0;            // outer refinement steps taken
   int inner_iters = 0;      // total GMRES iterations
   int converged = 0;        // berr reached FP64 level (or tol)
+  int switched_f64 = 0;     // the solves moved to FP64 arithmetic
+  int reserved = 0;
   double berr = 0;          // final normwise backward error
   double factor_ms = 0;     // device time of the factorization
   double berr_history[32] = {0};

@@ -245,18 +245,22 @@ __device__ __forceinline__ void trsv_load_tile(float (&v)[kTC], const float *A, 
   }
 }
 
+// F = float: every product FP32 (GB300's FP64 rate is a small fraction of
+// FP32; right for well-conditioned factors).  F = double: products and the
+// diagonal inverse in FP64, for ill-conditioned factors where an FP32
+// triangular solve would not apply (LU)^-1.  Tile sums are accumulated in
+// FP64 in both forms; x stays FP64.
+template <typename F>
 __global__ void __launch_bounds__(kTT) trsv_lowp_kernel(int n, const float *__restrict__ A, long lda,
-                                                        const float *__restrict__ Dinv, double *x,
+                                                        const F *__restrict__ Dinv, double *x,
                                                         unsigned *flags, unsigned *ticket,
                                                         bool upper, unsigned *status) {
-  // GB300 runs FP64 at a small fraction of FP32, so every product here is
-  // FP32 (the factors are FP32 already); partial sums of one 128-column tile
-  // are FP32, the sum over tiles and the right-hand side stay FP64.
-  extern __shared__ float DiS[];  // this block's diagonal inverse, column-major
+  extern __shared__ __align__(16) unsigned char tsv_raw[];
+  F *DiS = reinterpret_cast<F *>(tsv_raw);  // this block's diagonal inverse, column-major
   __shared__ unsigned sb;
   __shared__ double part[4][kTB];
-  __shared__ float xs[kTB];
-  __shared__ float ys[kTB];
+  __shared__ F xs[kTB];
+  __shared__ F ys[kTB];
   const int tid = threadIdx.x;
   if (tid == 0) sb = atomicAdd(ticket, 1u);
   __syncthreads();
@@ -271,7 +275,8 @@ __global__ void __launch_bounds__(kTT) trsv_lowp_kernel(int n, const float *__re
   {
     const float4 *src = reinterpret_cast<const float4 *>(Dinv + (long)blk * kTB * kTB);
     float4 *dst = reinterpret_cast<float4 *>(DiS);
-    for (int e = tid; e < kTB * kTB / 4; e += kTT) dst[e] = __ldcs(src + e);
+    const int words = kTB * kTB * (int)sizeof(F) / 16;
+    for (int e = tid; e < words; e += kTT) dst[e] = __ldcs(src + e);
   }
   const double rhs = (ph == 0 && row_ok) ? x[row] : 0.0;
   double acc = 0;
@@ -290,13 +295,13 @@ __global__ void __launch_bounds__(kTT) trsv_lowp_kernel(int n, const float *__re
     }
     __syncthreads();
     const int c0 = cb * kTB;
-    if (tid < kTB) xs[tid] = (c0 + tid < n) ? (float)__ldcg(x + c0 + tid) : 0.f;
+    if (tid < kTB) xs[tid] = (c0 + tid < n) ? (F)__ldcg(x + c0 + tid) : F(0);
     __syncthreads();
-    float p0 = 0.f, p1 = 0.f;
+    F p0 = 0, p1 = 0;
 #pragma unroll
     for (int j = 0; j < kTC; j += 2) {
-      p0 = fmaf(cur[j], xs[ph + 4 * j], p0);
-      p1 = fmaf(cur[j + 1], xs[ph + 4 * (j + 1)], p1);
+      p0 = fma((F)cur[j], xs[ph + 4 * j], p0);
+      p1 = fma((F)cur[j + 1], xs[ph + 4 * (j + 1)], p1);
     }
     acc += (double)p0 + (double)p1;
 #pragma unroll
@@ -305,15 +310,14 @@ __global__ void __launch_bounds__(kTT) trsv_lowp_kernel(int n, const float *__re
   part[ph][lr] = acc;
   __syncthreads();
   if (tid < kTB)
-    ys[tid] = row_ok ? (float)(rhs - (part[0][tid] + part[1][tid] + part[2][tid] + part[3][tid]))
-                     : 0.f;
+    ys[tid] = row_ok ? (F)(rhs - (part[0][tid] + part[1][tid] + part[2][tid] + part[3][tid])) : F(0);
   __syncthreads();
   // x(blk) = inv(D) * rhs
-  float y0 = 0.f, y1 = 0.f;
+  F y0 = 0, y1 = 0;
 #pragma unroll 8
   for (int j = ph; j < kTB; j += 8) {
-    y0 = fmaf(DiS[lr + j * kTB], ys[j], y0);
-    y1 = fmaf(DiS[lr + (j + 4) * kTB], ys[j + 4], y1);
+    y0 = fma(DiS[lr + j * kTB], ys[j], y0);
+    y1 = fma(DiS[lr + (j + 4) * kTB], ys[j + 4], y1);
   }
   part[ph][lr] = (double)y0 + (double)y1;
   __syncthreads();
@@ -328,7 +332,8 @@ __global__ void __launch_bounds__(kTT) trsv_lowp_kernel(int n, const float *__re
 // kTB x kTB per block (zero outside the triangle).  In-place triangular
 // inversion in shared memory, one CTA per block.
 __global__ void __launch_bounds__(512) invert_diag_kernel(int n, const float *__restrict__ A,
-                                                          long lda, float *Linv, float *Uinv) {
+                                                          long lda, double *Linv, double *Uinv,
+                                                          float *Linv32, float *Uinv32) {
   extern __shared__ double T[];  // T[i + j * kTB]
   const int blk = blockIdx.x, upper = blockIdx.y;
   const int r0 = blk * kTB, rows = min(kTB, n - r0);
@@ -371,11 +376,16 @@ __global__ void __launch_bounds__(512) invert_diag_kernel(int n, const float *__
       __syncthreads();
     }
   }
-  float *out = (upper ? Uinv : Linv) + (long)blk * kTB * kTB;
-  for (int e = tid; e < kTB * kTB; e += blockDim.x) out[e] = (float)T[e];
+  double *out = (upper ? Uinv : Linv) + (long)blk * kTB * kTB;
+  float *out32 = (upper ? Uinv32 : Linv32) + (long)blk * kTB * kTB;
+  for (int e = tid; e < kTB * kTB; e += blockDim.x) {
+    out[e] = T[e];
+    out32[e] = (float)T[e];
+  }
 }
 
-int invert_diag_blocks(int n, const float *A, long lda, float *Linv, float *Uinv, cudaStream_t s) {
+int invert_diag_blocks(int n, const float *A, long lda, double *Linv, double *Uinv, float *Linv32,
+                       float *Uinv32, cudaStream_t s) {
   const int nblk = ceil_div(n, kTB);
   const size_t smem = sizeof(double) * kTB * kTB;
   static bool attr = false;
@@ -385,28 +395,30 @@ int invert_diag_blocks(int n, const float *A, long lda, float *Linv, float *Uinv
     attr = true;
   }
   ZG_LAUNCH(kTagTrsv, 2.0 * nblk * kTB * kTB * kTB / 3, 8.0 * nblk * kTB * kTB * 3, s,
-            invert_diag_kernel<<<dim3(nblk, 2), 512, smem, s>>>(n, A, lda, Linv, Uinv));
+            invert_diag_kernel<<<dim3(nblk, 2), 512, smem, s>>>(n, A, lda, Linv, Uinv, Linv32,
+                                                                Uinv32));
   return 0;
 }
 
 // x <- op^-1 x with op = unit-lower L (upper=false) or non-unit upper U of
-// the FP32 LU factors in A, Dinv their diagonal-block inverses.
-// work: n/128 + 1 unsigned words (device).
-int trsv_lowp(int n, const float *A, long lda, const float *Dinv, double *x, bool upper,
+// the FP32 LU factors in A, Dinv their diagonal-block inverses (FP32 or
+// FP64: the arithmetic of the solve).  work: n/128 + 1 unsigned words.
+template <typename F>
+int trsv_lowp(int n, const float *A, long lda, const F *Dinv, double *x, bool upper,
               unsigned *work, unsigned *status, cudaStream_t s) {
   if (n <= 0) return 0;
   const int nblk = ceil_div(n, kTB);
   ZG_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned) * (nblk + 1), s));
-  const size_t smem = sizeof(float) * kTB * kTB;
+  const size_t smem = sizeof(F) * kTB * kTB;
   static bool attr = false;
   if (!attr) {
-    ZG_CUDA(cudaFuncSetAttribute(trsv_lowp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    ZG_CUDA(cudaFuncSetAttribute(trsv_lowp_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem));
     attr = true;
   }
-  ZG_LAUNCH(kTagTrsv, 1.0 * n * n, 2.0 * n * n + 16.0 * n + 4.0 * nblk * kTB * kTB, s,
-            trsv_lowp_kernel<<<nblk, kTT, smem, s>>>(n, A, lda, Dinv, x, work + 1, work, upper,
-                                                      status));
+  ZG_LAUNCH(kTagTrsv, 1.0 * n * n, 2.0 * n * n + 16.0 * n + sizeof(F) * nblk * kTB * kTB, s,
+            trsv_lowp_kernel<F><<<nblk, kTT, smem, s>>>(n, A, lda, Dinv, x, work + 1, work, upper,
+                                                        status));
   return 0;
 }
 
@@ -436,7 +448,9 @@ struct LowLU {
   const float *LU;
   long lda;
   const int *perm;
-  const float *Linv, *Uinv;
+  const double *Linv, *Uinv;      // FP64 diagonal-block inverses
+  const float *Linv32, *Uinv32;   // their FP32 roundings
+  bool f64 = false;               // apply in FP64 arithmetic
 };
 
 int lu_apply(int n, const LowLU &f, const double *r, double *d, unsigned *work, unsigned *status,
@@ -446,8 +460,13 @@ int lu_apply(int n, const LowLU &f, const double *r, double *d, unsigned *work, 
   const int *perm = f.perm;
   ZG_LAUNCH(kTagVector, 0, 0, s, gather_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, r, perm, d));
   ZG_CUDA(cudaGetLastError());
-  ZG_TRY(trsv_lowp(n, LU, lda, f.Linv, d, false, work, status, s));
-  ZG_TRY(trsv_lowp(n, LU, lda, f.Uinv, d, true, work, status, s));
+  if (f.f64) {
+    ZG_TRY(trsv_lowp<double>(n, LU, lda, f.Linv, d, false, work, status, s));
+    ZG_TRY(trsv_lowp<double>(n, LU, lda, f.Uinv, d, true, work, status, s));
+  } else {
+    ZG_TRY(trsv_lowp<float>(n, LU, lda, f.Linv32, d, false, work, status, s));
+    ZG_TRY(trsv_lowp<float>(n, LU, lda, f.Uinv32, d, true, work, status, s));
+  }
   return 0;
 }
 
@@ -646,14 +665,16 @@ int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, l
   const size_t nf = (size_t)n * n;
   const size_t ninv = (size_t)ceil_div(n, kTB) * kTB * kTB;
   ZG_TRY(workspace(s, kSlotLowLU,
-                   sizeof(float) * nf + 2 * sizeof(double) * ninv + 2 * sizeof(int) * (size_t)n + 512,
+                   sizeof(float) * nf + 3 * sizeof(double) * ninv + 2 * sizeof(int) * (size_t)n + 512,
                    &wf));
   float *LU = (float *)wf;
-  float *Linv = (float *)(((uintptr_t)(LU + nf) + 255) & ~(uintptr_t)255);
-  float *Uinv = Linv + ninv;
-  int *ipiv = (int *)(Uinv + ninv);
+  double *Linv = (double *)(((uintptr_t)(LU + nf) + 255) & ~(uintptr_t)255);
+  double *Uinv = Linv + ninv;
+  float *Linv32 = (float *)(Uinv + ninv);
+  float *Uinv32 = Linv32 + ninv;
+  int *ipiv = (int *)(Uinv32 + ninv);
   int *perm = ipiv + n;
-  const LowLU f{LU, (long)n, perm, Linv, Uinv};
+  LowLU f{LU, (long)n, perm, Linv, Uinv, Linv32, Uinv32, o.apply == kApplyF64};
   const int nparts = ceil_div(n, kGemvCols);
   const size_t nv = (size_t)n * (4 + nparts + (m + 1)) + 4 * (m + 2) + 64;
   ZG_TRY(workspace(s, kSlotIRVec, sizeof(double) * nv + sizeof(unsigned) * (n / kTB + 8), &wv));
@@ -693,7 +714,7 @@ int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, l
   res->info = info;
   if (info != 0) return 0;
   ZG_TRY(perm_from_ipiv(n, ipiv, perm, s));
-  ZG_TRY(invert_diag_blocks(n, LU, n, Linv, Uinv, s));
+  ZG_TRY(invert_diag_blocks(n, LU, n, Linv, Uinv, Linv32, Uinv32, s));
 
   res->converged = 1;
   for (int q = 0; q < nrhs; ++q) {
@@ -711,19 +732,31 @@ int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, l
     const double tol = o.tol > 0 ? o.tol : 0.0;
     while (it < o.max_iter) {
       if (berr <= tol) break;
-      if (tol == 0.0 && it > 0 && berr > 0.5 * prev) break;  // stagnated at its floor
-      prev = berr;
+      if (tol == 0.0 && it > 0 && berr > 0.5 * prev) {
+        // no progress: with FP32 application, retry in FP64 arithmetic
+        // (ill-conditioned factors); otherwise the floor is reached
+        if (f.f64 || o.apply != kApplyAuto || berr < 1e3 * 1.1102230246251565e-16) break;
+        f.f64 = true;
+        res->switched_f64 = 1;
+      }
+      prev = std::min(prev, berr);
       if (o.mode == kModeGMRES) {
         ZG_TRY(gmres_correction(n, A, lda, f, w, m, o.gmres_rtol, &res->inner_iters, ctl, s));
       } else {
         ZG_TRY(lu_apply(n, f, w.r, w.d, w.tw, &ctl->status, s));
       }
       ZG_LAUNCH(kTagVector, 0, 0, s, axpy_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, 1.0, w.d, x));
-      ZG_CUDA(cudaGetLastError());
       ++it;
       ZG_TRY(berr_of(n, A, lda, b, x, anrm, bnrm, w, &berr, s));
       if (q == 0 && it < 32) res->berr_history[it] = berr;
-      if (!std::isfinite(berr) || berr > 1e3 * prev) break;  // diverged
+      if (!std::isfinite(berr) || berr > 1e3 * prev) {  // diverged
+        if (f.f64 || o.apply != kApplyAuto) break;
+        f.f64 = true;  // restart the refinement from the first solve in FP64
+        res->switched_f64 = 1;
+        ZG_TRY(lu_apply(n, f, b, x, w.tw, &ctl->status, s));
+        ZG_TRY(berr_of(n, A, lda, b, x, anrm, bnrm, w, &berr, s));
+        prev = INFINITY;
+      }
     }
     res->iters = std::max(res->iters, it);
     res->berr = std::max(res->berr, berr);
