@@ -32,6 +32,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "n=16384 Ax=b to FP64 backward err: IR-BF16 vs FP64 LU time; batched solves/s"
+
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) over the
+# algorithmic bytes of one launch, per kernel class, from ncu captures of the
+# n = 8192 case; the roofline's "traffic" scales a launch's algorithmic bytes
+# by it.  panel: the slab is read once, its write-back is still in L2 when the
+# kernel ends; gemm_tc: part of C is L2-resident; trsv: the factor streams once.
+TRAFFIC_RATIO = {"panel": 0.506, "gemm_tc": 0.761, "trsv": 1.006}
 UNIT = "solves/s"
 
 
@@ -329,13 +336,17 @@ def main():
         per = kms / cnt / 1e3
         if name in ("gemm_tc",):
             ach = kfl / cnt / per / 1e12
+            tr = TRAFFIC_RATIO.get(name)
             roof = {"kernel": name, "bound": "tensor", "achieved": ach, "peak": bf16,
-                    "unit": "TFLOP/s", "frac": ach / bf16, "traffic": None,
+                    "unit": "TFLOP/s", "frac": ach / bf16,
+                    "traffic": tr * kby / cnt if tr else None,
                     "peak_source": src, "launches": cnt, "avg_launch_ms": 1e3 * per}
         else:
             ach = kby / cnt / per / 1e9
+            tr = TRAFFIC_RATIO.get(name)
             roof = {"kernel": name, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
-                    "frac": ach / hbm, "traffic": None, "peak_source": src, "launches": cnt,
+                    "frac": ach / hbm, "traffic": tr * kby / cnt if tr else None,
+                    "peak_source": src, "launches": cnt,
                     "avg_launch_ms": 1e3 * per}
     cpu = None
     if world == 1:
