@@ -73,6 +73,20 @@ int LAPACKE_slaswp(int matrix_layout, int n, float *a, int lda, int k1, int k2, 
  * returns after the stream has drained (info is a host value). */
 /* device-pointer form of getrf (lapack/getrf.zig:14) */
 int zml_gpu_dgetrf(int m, int n, double *dA, int ldda, int *dipiv, int *info, void *stream);
+/* FP64 getrf on device memory that allocates nothing; no counterpart in the
+ * reference.  For callers that cannot allocate device memory at solve time:
+ * code being captured into a CUDA graph (cudaMalloc cannot be captured),
+ * hosts whose device memory belongs to another allocator, loops that must not
+ * allocate after start-up.  Same factorization, bit for bit, as
+ * zml_gpu_dgetrf.  Its scratch is one static device array of about 273 KB
+ * that every GPU loading the library holds until exit; the first call on a
+ * device resolves that array's address (make it before any stream capture).
+ * Every call shares the array: calls that overlap on the GPU race.  Limit: m
+ * at most what one 64-column panel holds in shared memory (about 446 rows per
+ * SM), on devices of at most 256 SMs; larger sizes return
+ * ZML_GPU_ERR_INVALID with a message in zml_gpu_last_error(). */
+int zml_gpu_dgetrf_noalloc(int m, int n, double *dA, int ldda, int *dipiv, int *info,
+                           void *stream);
 /* device-pointer form of getrs (lapack/getrs.zig:13) */
 int zml_gpu_dgetrs(char trans, int n, int nrhs, const double *dA, int ldda, const int *dipiv,
                    double *dB, int lddb, void *stream);

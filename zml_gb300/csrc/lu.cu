@@ -398,3 +398,159 @@ INST(float)
 #undef INST
 
 }  // namespace zg
+
+// ===========================================================================
+// LU without any allocation: zml_gpu_dgetrf_noalloc.
+//
+// Some callers cannot allocate device memory at solve time: code that is being
+// captured into a CUDA graph (cudaMalloc is not a capturable operation), hosts
+// whose device memory belongs to another allocator (a framework's caching
+// allocator, a fixed arena set up at start-up), and real-time loops that may
+// not allocate after initialisation.  This entry point gives them the FP64
+// getrf with every scratch buffer it needs -- the panel's control words, the
+// candidate-pivot exchange and the composed row-interchange pairs -- carved
+// from one static device array that every GPU loading the library holds
+// until the process exits.  The caller passes only the matrix, the pivot
+// vector and the info pointer.
+namespace zg {
+namespace {
+
+constexpr int kNaMaxCtas = 256;   // panel CTAs the exchange has room for (SMs per device)
+constexpr int kNaNb = 64;         // panel width of the FP64 factorization
+constexpr size_t kNaCtlBytes = 256;
+constexpr size_t kNaSwapBytes = sizeof(int) * (4 * kSwapMax + 8);
+constexpr size_t kNaSwapOff = kNaCtlBytes;
+constexpr size_t kNaXchgOff = (kNaSwapOff + kNaSwapBytes + 255) / 256 * 256;
+constexpr size_t kNaXchgWords = 2 * (size_t)kNaMaxCtas * (kNaNb + 2) + 2 * kNaNb;
+constexpr size_t kNaBytes = kNaXchgOff + sizeof(double) * kNaXchgWords;  // ~273 KB
+
+// The scratch.  Shared by every call on a device: calls that overlap on the
+// GPU (two streams, two host threads) race on it.  Its control words are
+// cleared at the start of every call; the rest needs no initial value.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+struct NaDevice {
+  unsigned char *scratch = nullptr;  // device address of g_noalloc_scratch
+  int sms = 0;
+  int smem_optin = 0;
+};
+constexpr int kNaMaxDevices = 64;
+NaDevice g_na_dev[kNaMaxDevices];
+std::mutex g_na_mu;
+
+// Once per device, with that device current: resolve the array's device
+// address (the host-side symbol is only a stand-in and must never be passed
+// to a kernel) and the launch limits.  Runs on the first call on a device.
+int noalloc_setup(NaDevice **out) {
+  int dev = 0;
+  ZG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNaMaxDevices) {
+    set_last_error("dgetrf_noalloc: device ordinal %d beyond %d", dev, kNaMaxDevices);
+    return kErrInvalid;
+  }
+  std::lock_guard<std::mutex> lk(g_na_mu);
+  NaDevice &d = g_na_dev[dev];
+  if (!d.scratch) {
+    void *p = nullptr;
+    ZG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    ZG_CUDA(cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev));
+    ZG_CUDA(cudaDeviceGetAttribute(&d.smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    ZG_CUDA(cudaFuncSetAttribute(panel_lu_kernel<double>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 d.smem_optin - 4096));
+    ZG_CUDA(cudaFuncSetAttribute(laswp_apply_kernel<double>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(double) * 32 * 2 * kSwapMax)));
+    d.scratch = (unsigned char *)p;
+  }
+  *out = &d;
+  return 0;
+}
+
+// Rows one panel launch can hold: every CTA keeps R rows x kNaNb columns in
+// shared memory, at most one CTA per SM.
+int noalloc_max_rows(const NaDevice &d) {
+  const int rmax = (d.smem_optin - 4096) / (kNaNb * (int)sizeof(double));
+  return std::min(d.sms, kNaMaxCtas) * rmax;
+}
+
+int na_panel(const NaDevice &d, int m, int nb, double *A, long lda, int *ipiv, int base,
+             Control *ctl, double *xchg, cudaStream_t s) {
+  int nblk = std::min(std::min(d.sms, kNaMaxCtas), ceil_div(m, 8));
+  int R = ceil_div(m, nblk);
+  nblk = ceil_div(m, R);
+  const size_t smem = (size_t)R * nb * sizeof(double);
+  ZG_CUDA(cudaMemsetAsync(&ctl->barrier[0], 0, 2 * sizeof(unsigned), s));
+  void *args[] = {&m, &nb, &A, &lda, &ipiv, &base, &ctl, &base, &R, &xchg};
+  ZG_LAUNCH(kTagPanel, 1.0 * m * nb * nb, 2.0 * sizeof(double) * m * nb, s,
+            ZG_CUDA(cudaLaunchCooperativeKernel((void *)panel_lu_kernel<double>, dim3(nblk),
+                                                dim3(256), args, smem, s)));
+  return 0;
+}
+
+int na_laswp(int n, double *A, long lda, int k1, int k2, const int *ipiv, int *pairs,
+             cudaStream_t s) {
+  if (n <= 0 || k2 < k1) return 0;
+  int *np = pairs + 4 * kSwapMax;
+  ZG_LAUNCH(kTagLaswp, 0, 0, s, laswp_prep_kernel<<<1, 32, 0, s>>>(k1, k2, ipiv, 1, pairs, np));
+  const size_t smem = sizeof(double) * 32 * 2 * (k2 - k1 + 1);
+  ZG_LAUNCH(kTagLaswp, 0, 4.0 * sizeof(double) * n * (k2 - k1 + 1), s,
+            laswp_apply_kernel<double><<<ceil_div(n, 32), 256, smem, s>>>(n, A, lda, pairs, np));
+  return 0;
+}
+
+}  // namespace
+}  // namespace zg
+
+using namespace zg;
+
+// FP64 getrf (partial pivoting, 1-based ipiv, LAPACK info) on device memory
+// with no allocation; same factorization, bit for bit, as zml_gpu_dgetrf.
+// Returns 0, -(bad argument index), or a library error (ZML_GPU_ERR_INVALID
+// with a message when m exceeds what one panel can hold on this device).
+extern "C" int zml_gpu_dgetrf_noalloc(int m, int n, double *dA, int ldda, int *dipiv, int *info,
+                                      void *stream) {
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (ldda < std::max(1, m)) return -4;
+  if (info) *info = 0;
+  if (m == 0 || n == 0) return 0;
+  NaDevice *d;
+  ZG_TRY(noalloc_setup(&d));
+  if (m > noalloc_max_rows(*d)) {
+    set_last_error("dgetrf_noalloc: m = %d exceeds the %d rows one panel holds on this device", m,
+                   noalloc_max_rows(*d));
+    return kErrInvalid;
+  }
+  if (d->sms > kNaMaxCtas) {
+    set_last_error("dgetrf_noalloc: %d SMs exceed the scratch's %d panel slots", d->sms,
+                   kNaMaxCtas);
+    return kErrInvalid;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  Control *ctl = reinterpret_cast<Control *>(d->scratch);
+  int *pairs = reinterpret_cast<int *>(d->scratch + kNaSwapOff);
+  double *xchg = reinterpret_cast<double *>(d->scratch + kNaXchgOff);
+  ZG_CUDA(cudaMemsetAsync(ctl, 0, sizeof(Control), s));  // counters, status, info start at zero
+  const long lda = ldda;
+  const int mn = std::min(m, n);
+  for (int j = 0; j < mn; j += kNaNb) {
+    const int jb = std::min(kNaNb, mn - j);
+    double *Ajj = dA + j + (long)j * lda;
+    ZG_TRY(na_panel(*d, m - j, jb, Ajj, lda, dipiv + j, j, ctl, xchg, s));
+    ZG_TRY(na_laswp(j, dA, lda, j + 1, j + jb, dipiv, pairs, s));
+    if (j + jb < n) {
+      double *Aright = dA + (long)(j + jb) * lda;
+      ZG_TRY(na_laswp(n - j - jb, Aright, lda, j + 1, j + jb, dipiv, pairs, s));
+      ZG_TRY(trsm_dev<double>(kLeft, kLower, kNoTrans, kUnit, jb, n - j - jb, 1.0, Ajj, lda,
+                              Aright + j, lda, s));
+      if (j + jb < m)
+        ZG_TRY(gemm_simt<double>(kNoTrans, kNoTrans, m - j - jb, n - j - jb, jb, -1.0, Ajj + jb,
+                                 lda, Aright + j, lda, 1.0, Aright + j + jb, lda, 0, s));
+    }
+  }
+  int inf = 0;
+  ZG_TRY(check_status(s, ctl, &inf));
+  if (info) *info = inf;
+  return 0;
+}
