@@ -61,6 +61,10 @@ int LAPACKE_dposv(int matrix_layout, char uplo, int n, int nrhs, double *a, int 
 int LAPACKE_sposv(int matrix_layout, char uplo, int n, int nrhs, float *a, int lda, float *b,
                   int ldb);
 
+/* replaces zml.linalg.lapack.geqrf (lapack.zig:5060; kernel lapack/geqrf.zig:18):
+ * R in the upper triangle, the Householder vectors below it, tau[min(m,n)] */
+int LAPACKE_dgeqrf(int matrix_layout, int m, int n, double *a, int lda, double *tau);
+int LAPACKE_sgeqrf(int matrix_layout, int m, int n, float *a, int lda, float *tau);
 /* replaces zml.linalg.lapack.laswp (kernel lapack/laswp.zig:12): row
  * interchanges k1..k2 (1-based) of n columns, |incx| = 1 */
 int LAPACKE_dlaswp(int matrix_layout, int n, double *a, int lda, int k1, int k2, const int *ipiv,
@@ -95,6 +99,8 @@ int zml_gpu_dpotrf(char uplo, int n, double *dA, int ldda, int *info, void *stre
 /* device-pointer form of potrs (lapack/potrs.zig:15) */
 int zml_gpu_dpotrs(char uplo, int n, int nrhs, const double *dA, int ldda, double *dB, int lddb,
                    void *stream);
+/* device-pointer form of geqrf (lapack/geqrf.zig:18) */
+int zml_gpu_dgeqrf(int m, int n, double *dA, int ldda, double *dtau, void *stream);
 /* device-pointer form of gemm (blas/gemm.zig:14), CBLAS transpose codes */
 int zml_gpu_dgemm(int transa, int transb, int m, int n, int k, double alpha, const double *dA,
                   int ldda, const double *dB, int lddb, double beta, double *dC, int lddc,

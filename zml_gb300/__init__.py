@@ -36,11 +36,13 @@ for p, T in (("d", f64), ("s", f32)):
         "LAPACKE_%spotrs" % p: (i32, [i32, ch, i32, i32, vp, i32, vp, i32]),
         "LAPACKE_%sposv" % p: (i32, [i32, ch, i32, i32, vp, i32, vp, i32]),
         "LAPACKE_%slaswp" % p: (i32, [i32, i32, vp, i32, i32, i32, vp, i32]),
+        "LAPACKE_%sgeqrf" % p: (i32, [i32, i32, i32, vp, i32, vp]),
     })
 _SIGS.update({
     "zml_gpu_dgetrf": (i32, [i32, i32, vp, i32, vp, vp, vp]),
     "zml_gpu_dgetrs": (i32, [ch, i32, i32, vp, i32, vp, vp, i32, vp]),
     "zml_gpu_dgetrf_noalloc": (i32, [i32, i32, vp, i32, vp, vp, vp]),
+    "zml_gpu_dgeqrf": (i32, [i32, i32, vp, i32, vp, vp]),
     "zml_gpu_dpotrf": (i32, [ch, i32, vp, i32, vp, vp]),
     "zml_gpu_dpotrs": (i32, [ch, i32, i32, vp, i32, vp, i32, vp]),
     "zml_gpu_dgemm": (i32, [i32, i32, i32, i32, i32, f64, vp, i32, vp, i32, f64, vp, i32, vp]),

@@ -369,6 +369,23 @@ int posv_any(int layout, char uplo, int n, int nrhs, T *a, int lda, T *b, int ld
   return info;
 }
 
+template <typename T> int geqrf_any(int layout, int m, int n, T *a, int lda, T *tau) {
+  if (!lay_ok(layout)) return -1;
+  if (m < 0) return -2;
+  if (n < 0) return -3;
+  if (lda < std::max(1, layout == kColMajor ? m : n)) return -5;
+  if (m == 0 || n == 0) return 0;
+  cudaStream_t s = lib_stream();
+  ColMajor<T> A;
+  Buf<T> Tau;
+  ZG_TRY(A.in(layout, a, lda, m, n, kSlotA, kSlotAT, true, s));
+  ZG_TRY(Tau.in(tau, std::min(m, n), kSlotPiv, false, s));
+  ZG_TRY(geqrf_dev<T>(m, n, A.d, A.ld, Tau.d, s));
+  ZG_TRY(A.out(s));
+  ZG_TRY(Tau.out(s));
+  return sync(s);
+}
+
 template <typename T>
 int laswp_any(int layout, int n, T *a, int lda, int k1, int k2, const int *ipiv, int incx) {
   if (!lay_ok(layout)) return -1;
@@ -461,6 +478,19 @@ CBLAS_GEMM(s, float)
   }
 LAPACKE_FNS(d, double)
 LAPACKE_FNS(s, float)
+
+int LAPACKE_dgeqrf(int layout, int m, int n, double *a, int lda, double *tau) {
+  return geqrf_any<double>(layout, m, n, a, lda, tau);
+}
+int LAPACKE_sgeqrf(int layout, int m, int n, float *a, int lda, float *tau) {
+  return geqrf_any<float>(layout, m, n, a, lda, tau);
+}
+int zml_gpu_dgeqrf(int m, int n, double *dA, int ldda, double *dtau, void *stream) {
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (ldda < std::max(1, m)) return -4;
+  return geqrf_dev<double>(m, n, dA, ldda, dtau, (cudaStream_t)stream);
+}
 
 int LAPACKE_dlaswp(int layout, int n, double *a, int lda, int k1, int k2, const int *ipiv,
                    int incx) {

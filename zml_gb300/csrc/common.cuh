@@ -91,6 +91,7 @@ enum Slot : int {
   kSlotL16 = 11, kSlotU16 = 12,  // 16-bit L21 / U12 operands of the tensor-core update
   kSlotBatch = 13,            // batched solver descriptors
   kSlotSwap = 14,             // composed row-interchange pairs
+  kSlotQR = 15,               // QR: V, T, W, split-K partials, panel exchange
   kNumSlots = 16
 };
 

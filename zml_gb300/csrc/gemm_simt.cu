@@ -9,17 +9,25 @@
 //
 // tri selects the SYRK form: 0 = full C, 1 = lower triangle (i >= j),
 // 2 = upper triangle (i <= j); tiles outside the triangle are skipped.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
 namespace zg {
 
+// gridDim.z > 1 splits K: CTA z covers l in [z*kchunk, (z+1)*kchunk) and
+// writes its partial product to C + z*cz (beta ignored, partials reduced by
+// splitk_reduce_kernel).
 template <typename T, int BM, int BN, int BK>
 __global__ void __launch_bounds__(256) gemm_simt_kernel(int transa, int transb, int m, int n, int k,
                                                         T alpha, const T *__restrict__ A, long lda,
                                                         const T *__restrict__ B, long ldb, T beta,
-                                                        T *__restrict__ C, long ldc, int tri) {
+                                                        T *__restrict__ C, long ldc, int tri,
+                                                        int kchunk, long cz) {
   const int i0 = blockIdx.x * BM, j0 = blockIdx.y * BN;
+  const int kbeg = blockIdx.z * kchunk, kend = min(k, kbeg + kchunk);
+  C += blockIdx.z * cz;
   if (tri == 1 && i0 + BM - 1 < j0) return;  // tile strictly above the diagonal
   if (tri == 2 && j0 + BN - 1 < i0) return;  // tile strictly below the diagonal
 
@@ -36,7 +44,7 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(int transa, int transb, 
   const bool ta = transa == kTrans || transa == kConjTrans;
   const bool tb = transb == kTrans || transb == kConjTrans;
 
-  for (int l0 = 0; l0 < k; l0 += BK) {
+  for (int l0 = kbeg; l0 < kend; l0 += BK) {
     // A tile: op(A)(i, l) for i in [i0, i0+BM), l in [l0, l0+BK)
     for (int e = tid; e < BM * BK; e += 256) {
       int ii, ll;
@@ -44,7 +52,7 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(int transa, int transb, 
       else     { ll = e % BK; ii = e / BK; }   // contiguous along l
       const int gi = i0 + ii, gl = l0 + ll;
       T v = 0;
-      if (gi < m && gl < k) v = ta ? A[gl + (long)gi * lda] : A[gi + (long)gl * lda];
+      if (gi < m && gl < kend) v = ta ? A[gl + (long)gi * lda] : A[gi + (long)gl * lda];
       As[ll][ii] = v;
     }
     // B tile: op(B)(l, j)
@@ -54,7 +62,7 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(int transa, int transb, 
       else     { jj = e % BN; ll = e / BN; }   // contiguous along j
       const int gj = j0 + jj, gl = l0 + ll;
       T v = 0;
-      if (gj < n && gl < k) v = tb ? B[gj + (long)gl * ldb] : B[gl + (long)gj * ldb];
+      if (gj < n && gl < kend) v = tb ? B[gj + (long)gl * ldb] : B[gl + (long)gj * ldb];
       Bs[ll][jj] = v;
     }
     __syncthreads();
@@ -83,7 +91,8 @@ __global__ void __launch_bounds__(256) gemm_simt_kernel(int transa, int transb, 
       if (tri == 1 && i < j) continue;
       if (tri == 2 && i > j) continue;
       T *p = C + i + (long)j * ldc;
-      *p = beta == T(0) ? alpha * acc[r][c] : alpha * acc[r][c] + beta * *p;
+      if (gridDim.z > 1) *p = acc[r][c];
+      else *p = beta == T(0) ? alpha * acc[r][c] : alpha * acc[r][c] + beta * *p;
     }
   }
 }
@@ -101,10 +110,55 @@ int gemm_simt(int transa, int transb, int m, int n, int k, T alpha, const T *A, 
     return kErrInvalid;
   }
   ZG_LAUNCH(kTagGemmSimt, 2.0 * m * n * k, sizeof(T) * ((double)m * k + (double)k * n + 2.0 * m * n), s, gemm_simt_kernel<T, BM, BN, BK><<<grid, 256, 0, s>>>(transa, transb, m, n, k, alpha, A, lda, B,
-                                                       ldb, beta, C, ldc, tri));
+                                                       ldb, beta, C, ldc, tri, k, 0));
   ZG_CUDA(cudaGetLastError());
   return 0;
 }
+
+// C = alpha * sum_z P_z + beta * C over `splits` partials P_z (m x n, ld m).
+template <typename T>
+__global__ void splitk_reduce_kernel(int m, int n, int splits, const T *__restrict__ P, T alpha,
+                                     T beta, T *__restrict__ C, long ldc) {
+  const long total = (long)m * n;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total;
+       e += (long)gridDim.x * blockDim.x) {
+    const int i = e % m, j = e / m;
+    T acc = 0;
+    for (int z = 0; z < splits; ++z) acc += P[(long)z * total + e];
+    T *p = C + i + (long)j * ldc;
+    *p = beta == T(0) ? alpha * acc : alpha * acc + beta * *p;
+  }
+}
+
+// GEMM with K split over `splits` CTA layers (for short-and-wide outputs with
+// a long K, e.g. W = V^T C of the block reflector); work: splits*m*n scratch.
+template <typename T>
+int gemm_simt_splitk(int transa, int transb, int m, int n, int k, T alpha, const T *A, long lda,
+                     const T *B, long ldb, T beta, T *C, long ldc, int splits, T *work,
+                     cudaStream_t s) {
+  if (m <= 0 || n <= 0) return 0;
+  if (splits <= 1 || k <= 0) return gemm_simt<T>(transa, transb, m, n, k, alpha, A, lda, B, ldb,
+                                                 beta, C, ldc, 0, s);
+  constexpr int BM = 64, BN = 64, BK = 16;
+  const int kchunk = ((ceil_div(k, splits) + BK - 1) / BK) * BK;
+  splits = ceil_div(k, kchunk);
+  dim3 grid(ceil_div(m, BM), ceil_div(n, BN), splits);
+  ZG_LAUNCH(kTagGemmSimt, 2.0 * m * n * k, sizeof(T) * ((double)m * k + (double)k * n + 2.0 * m * n * splits), s,
+            gemm_simt_kernel<T, BM, BN, BK><<<grid, 256, 0, s>>>(transa, transb, m, n, k, T(1), A,
+                                                                 lda, B, ldb, T(0), work, m, 0,
+                                                                 kchunk, (long)m * n));
+  const long total = (long)m * n;
+  ZG_LAUNCH(kTagGemmSimt, 0, sizeof(T) * total * (splits + 2), s,
+            splitk_reduce_kernel<T><<<(int)std::min<long>((total + 255) / 256, 152L * 8), 256, 0,
+                                      s>>>(m, n, splits, work, alpha, beta, C, ldc));
+  return 0;
+}
+template int gemm_simt_splitk<double>(int, int, int, int, int, double, const double *, long,
+                                      const double *, long, double, double *, long, int, double *,
+                                      cudaStream_t);
+template int gemm_simt_splitk<float>(int, int, int, int, int, float, const float *, long,
+                                     const float *, long, float, float *, long, int, float *,
+                                     cudaStream_t);
 
 template int gemm_simt<double>(int, int, int, int, int, double, const double *, long,
                                const double *, long, double, double *, long, int, cudaStream_t);

@@ -13,6 +13,14 @@ int gemm_simt(int transa, int transb, int m, int n, int k, T alpha, const T *A, 
 template <typename T>
 int syrk_dev(int uplo, int trans, int n, int k, T alpha, const T *A, long lda, T beta, T *C,
              long ldc, cudaStream_t s);
+// K split over `splits` CTA layers, partials in work (splits*m*n), then reduced.
+template <typename T>
+int gemm_simt_splitk(int transa, int transb, int m, int n, int k, T alpha, const T *A, long lda,
+                     const T *B, long ldb, T beta, T *C, long ldc, int splits, T *work,
+                     cudaStream_t s);
+
+// qr.cu -- Householder QR (geqrf) with the T factor of each panel.
+template <typename T> int geqrf_dev(int m, int n, T *A, long lda, T *tau, cudaStream_t s);
 
 // trsm.cu -- B <- alpha op(A)^-1 B (left) or alpha B op(A)^-1 (right).
 template <typename T>
