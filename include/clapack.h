@@ -153,6 +153,31 @@ int zml_gpu_dgesv_mpir(int n, int nrhs, const double *dA, int ldda, const double
                        double *dX, int lddx, int prec, int mode, double tol, int max_iter,
                        zml_mpir_result *res, void *stream);
 
+/* ---- batched small solves (no counterpart in the reference) -------------
+ * count systems A_i X_i = B_i, n_i in 1..256, packed back to back in device
+ * memory: A_i (n_i x n_i, ld n_i) at offset sum_{j<i} n_j^2, B_i and X_i
+ * (n_i x nrhs, ld n_i) at sum_{j<i} n_j nrhs, ipiv_i at sum_{j<i} n_j.
+ * spd[i] != 0: lower Cholesky (potrf + potrs of potrf.zig:17 / potrs.zig:15),
+ * else partial-pivot LU (getrf + getrs of getrf.zig:14 / getrs.zig:13).
+ * prec 0: FP64 (A overwritten by its factors); prec 1: FP32 factors + FP64
+ * iterative refinement (A untouched; iters[i] = refinement steps).
+ * info[i] as LAPACK.  The plan does the host work once; execute is one
+ * memset and one persistent launch (capturable); run_graph captures it in a
+ * CUDA graph on first use and replays it. */
+int zml_gpu_batched_plan_create(void **plan, int count, const int *n, const int *spd, int nrhs,
+                                int prec, int max_ir);
+int zml_gpu_batched_execute(void *plan, double *dA, const double *dB, double *dX, int *dipiv,
+                            int *dinfo, int *diters, void *stream);
+int zml_gpu_batched_run_graph(void *plan, double *dA, const double *dB, double *dX, int *dipiv,
+                              int *dinfo, int *diters, void *stream);
+void zml_gpu_batched_plan_destroy(void *plan);
+/* Per-size-class warp schedule (warps per matrix; class i holds n <= edges[i]):
+ * read (set = 0) or replace (set = 1).  Returns the number of classes. */
+int zml_gpu_batched_schedule(int prec, int *warps, int *edges, int cap, int set);
+/* Times every warp count for every class and keeps the fastest; chosen[i]
+ * and ms[i] (may be NULL) receive the result per class. */
+int zml_gpu_batched_autotune(int prec, int nrhs, int *chosen, double *ms, void *stream);
+
 /* ---- instrumentation ------------------------------------------------------
  * Kernel classes: 0 tensor-core GEMM, 1 CUDA-core GEMM/SYRK, 2 LU panel,
  * 3 TRSM diagonal block, 4 row interchanges, 5 low-precision TRSV, 6 FP64

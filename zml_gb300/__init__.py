@@ -90,6 +90,15 @@ def profile_read():
     return out
 
 
+_SIGS.update({
+    "zml_gpu_batched_plan_create": (i32, [C.POINTER(vp), i32, vp, vp, i32, i32, i32]),
+    "zml_gpu_batched_execute": (i32, [vp, vp, vp, vp, vp, vp, vp, vp]),
+    "zml_gpu_batched_run_graph": (i32, [vp, vp, vp, vp, vp, vp, vp, vp]),
+    "zml_gpu_batched_plan_destroy": (None, [vp]),
+    "zml_gpu_batched_schedule": (i32, [i32, vp, vp, i32, i32]),
+    "zml_gpu_batched_autotune": (i32, [i32, i32, vp, vp, vp]),
+})
+
 PREC_FP16, PREC_BF16, PREC_FP32, PREC_BF16X3 = 0, 1, 2, 3
 REFINE_IR, REFINE_GMRES = 0, 1
 

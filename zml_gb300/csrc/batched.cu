@@ -1,0 +1,602 @@
+// batched.cu -- thousands of small dense solves of uneven sizes in one launch.
+//
+// Each system is one of zml's small problems: general A (getrf + getrs,
+// lapack/getrf.zig:14 / getrs.zig:13) or SPD A (potrf + potrs, lower,
+// potrf.zig:17 / potrs.zig:15), with nrhs right-hand sides.
+//
+// One persistent launch: CTAs pull tasks from an atomic queue in descending
+// estimated cost (longest processing time first).  A task is up to 8/w
+// matrices of one size class that the CTA processes concurrently with w warps
+// each -- the per-size warp schedule, chosen by the autotuner -- and each
+// group of w warps synchronises on its own named barrier.  A group's factor
+// lives in its w/8 share of the CTA's shared memory when it fits, otherwise
+// in L2-resident global memory (FP64: in place in the caller's matrix).
+//
+// Precisions: FP64 (factor and solve in FP64; A is overwritten with the
+// factors like getrf/potrf), or FP32 factorization + FP64 iterative
+// refinement (A untouched; x += (LU)^-1 (b - A x) with the residual from the
+// FP64 A until ||r||inf <= 4 u ||A||inf ||x||inf or max_ir steps).
+//
+// A plan (zml_gpu_batched_plan_create) does the host work once -- sizes,
+// offsets, the task list -- so that executing it is a memset and one kernel
+// launch, which can be captured in a CUDA graph and replayed.
+#include <algorithm>
+#include <map>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "kernels_batched.h"
+
+namespace zg {
+
+namespace {
+
+constexpr int kSmemTotal = 200 * 1024;  // per CTA; a group of w warps owns w/8 of it
+
+__device__ __forceinline__ void group_sync(int gid, int nthreads) {
+  if (nthreads == 32)
+    __syncwarp();
+  else
+    asm volatile("bar.sync %0, %1;" ::"r"(gid + 1), "r"(nthreads) : "memory");
+}
+
+template <typename F> struct View {
+  F *p;
+  int ld;
+  __device__ __forceinline__ F &operator()(int i, int j) const { return p[i + (long)j * ld]; }
+};
+
+// argmax of |a(i,k)| over the group: first maximum wins (iamax.zig:29-38)
+template <typename F>
+__device__ void group_argmax(F &key, int &idx, int tid, int nt, int gid, float *sk, int *si) {
+  const int lane = tid & 31, w = tid >> 5, nw = nt >> 5;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const F k2 = __shfl_xor_sync(0xffffffffu, key, off);
+    const int i2 = __shfl_xor_sync(0xffffffffu, idx, off);
+    if (k2 > key || (k2 == key && i2 < idx)) { key = k2; idx = i2; }
+  }
+  if (nw == 1) return;
+  if (lane == 0) { reinterpret_cast<F *>(sk)[w] = key; si[w] = idx; }
+  group_sync(gid, nt);
+  key = reinterpret_cast<F *>(sk)[0];
+  idx = si[0];
+  for (int q = 1; q < nw; ++q) {
+    const F kq = reinterpret_cast<F *>(sk)[q];
+    if (kq > key || (kq == key && si[q] < idx)) { key = kq; idx = si[q]; }
+  }
+  group_sync(gid, nt);
+}
+
+template <typename F>
+__device__ int lu_inplace(View<F> M, int n, int *ipiv, int tid, int nt, int gid, float *sk,
+                          int *si) {
+  int info = 0;
+  for (int k = 0; k < n; ++k) {
+    F key = F(-1);
+    int idx = 0x7fffffff;
+    for (int i = k + tid; i < n; i += nt) {
+      const F v = M(i, k);
+      const F kv = v != v ? (i == k ? F(INFINITY) : F(-1)) : fabs(v);
+      if (kv > key || (kv == key && i < idx)) { key = kv; idx = i; }
+    }
+    group_argmax(key, idx, tid, nt, gid, sk, si);
+    const int p = idx == 0x7fffffff ? k : idx;
+    if (tid == 0) ipiv[k] = p + 1;
+    const F piv = M(p, k);
+    if (piv == F(0)) {
+      if (info == 0) info = k + 1;
+    } else {
+      if (p != k)
+        for (int j = tid; j < n; j += nt) {
+          const F t = M(k, j);
+          M(k, j) = M(p, j);
+          M(p, j) = t;
+        }
+      group_sync(gid, nt);
+      const F rp = F(1) / piv;
+      const bool recip = fabs(piv) >= Real<F>::sfmin();
+      for (int i = k + 1 + tid; i < n; i += nt) M(i, k) = recip ? M(i, k) * rp : M(i, k) / piv;
+    }
+    group_sync(gid, nt);
+    for (int i = k + 1 + tid; i < n; i += nt) {  // rank-1 update, one row per thread
+      const F lik = M(i, k);
+      for (int j = k + 1; j < n; ++j) M(i, j) -= lik * M(k, j);
+    }
+    group_sync(gid, nt);
+  }
+  return info;
+}
+
+template <typename F> __device__ int chol_inplace(View<F> M, int n, int tid, int nt, int gid) {
+  for (int k = 0; k < n; ++k) {
+    const F d = M(k, k);
+    if (!(d > F(0))) return k + 1;
+    const F s = sqrt(d);
+    const F r = F(1) / s;
+    group_sync(gid, nt);
+    if (tid == 0) M(k, k) = s;
+    for (int i = k + 1 + tid; i < n; i += nt) M(i, k) *= r;
+    group_sync(gid, nt);
+    for (int i = k + 1 + tid; i < n; i += nt) {  // trailing lower triangle, one row per thread
+      const F lik = M(i, k);
+      for (int j = k + 1; j <= i; ++j) M(i, j) -= lik * M(j, k);
+    }
+    group_sync(gid, nt);
+  }
+  return 0;
+}
+
+// X (n x nrhs, FP64, ld ldx) <- A^-1 X from the factors in M, FP64 arithmetic.
+template <typename F>
+__device__ void solve_inplace(View<F> M, int n, bool spd, const int *ipiv, double *X, int ldx,
+                              int nrhs, int tid, int nt, int gid) {
+  if (!spd) {
+    if (tid < nrhs)
+      for (int k = 0; k < n; ++k) {
+        const int p = ipiv[k] - 1;
+        if (p != k) {
+          const double t = X[k + tid * ldx];
+          X[k + tid * ldx] = X[p + tid * ldx];
+          X[p + tid * ldx] = t;
+        }
+      }
+    group_sync(gid, nt);
+  }
+  for (int k = 0; k < n; ++k) {  // forward: unit L (LU) or L (Cholesky)
+    if (spd && tid < nrhs) X[k + tid * ldx] /= (double)M(k, k);
+    group_sync(gid, nt);
+    for (int c = 0; c < nrhs; ++c) {
+      const double xk = X[k + c * ldx];
+      for (int i = k + 1 + tid; i < n; i += nt) X[i + c * ldx] -= (double)M(i, k) * xk;
+    }
+    group_sync(gid, nt);
+  }
+  for (int k = n - 1; k >= 0; --k) {  // backward: U (LU) or L^T (Cholesky)
+    if (tid < nrhs) X[k + tid * ldx] /= (double)M(k, k);
+    group_sync(gid, nt);
+    for (int c = 0; c < nrhs; ++c) {
+      const double xk = X[k + c * ldx];
+      for (int i = tid; i < k; i += nt)
+        X[i + c * ldx] -= (spd ? (double)M(k, i) : (double)M(i, k)) * xk;
+    }
+    group_sync(gid, nt);
+  }
+}
+
+// max over the group (for norms)
+__device__ double group_max(double v, int tid, int nt, int gid, double *red) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if (nt == 32) return v;
+  if ((tid & 31) == 0) red[tid >> 5] = v;
+  group_sync(gid, nt);
+  v = red[0];
+  for (int q = 1; q < (nt >> 5); ++q) v = fmax(v, red[q]);
+  group_sync(gid, nt);
+  return v;
+}
+
+}  // namespace
+
+template <typename F>
+__global__ void __launch_bounds__(256) batched_kernel(BatchArgs a, const BatchTask *__restrict__ tasks,
+                                                      int ntasks, unsigned *queue, F *gscratch,
+                                                      long gscratch_per_group, unsigned *status) {
+  extern __shared__ __align__(16) unsigned char bsm[];
+  __shared__ unsigned s_task;
+  __shared__ float sk[8][16];
+  __shared__ int si[8][8];
+  __shared__ double red[8][8];
+  const int tid = threadIdx.x;
+  for (;;) {
+    if (tid == 0) s_task = atomicAdd(queue, 1u);
+    __syncthreads();
+    const unsigned t = s_task;
+    __syncthreads();
+    if (t >= (unsigned)ntasks) break;
+    const BatchTask task = tasks[t];
+    const int w = task.warps, nt = 32 * w, groups = 8 / w;
+    const int gid = tid / nt, gt = tid % nt;
+    if (gid < groups && gid < task.count) {
+      const int mi = task.mat[gid];
+      const int n = a.n[mi];
+      const bool spd = a.spd[mi] != 0;
+      const int nrhs = a.nrhs;
+      double *Ag = a.A + a.a_off[mi];
+      const double *Bg = a.B + a.b_off[mi];
+      double *Xg = a.X + a.b_off[mi];
+      int *ipiv = a.ipiv + a.p_off[mi];
+      const int share = kSmemTotal / groups;
+      unsigned char *gsm = bsm + (long)gid * share;
+      const bool in_smem = (long)n * n * (long)sizeof(F) <= share;
+      F *fbuf;
+      if (in_smem)
+        fbuf = reinterpret_cast<F *>(gsm);
+      else if (sizeof(F) == sizeof(double))
+        fbuf = reinterpret_cast<F *>(Ag);  // FP64 factor in place, L2-resident
+      else
+        fbuf = gscratch + ((long)blockIdx.x * 8 + gid) * gscratch_per_group;
+      View<F> M{fbuf, n};
+      // ||A||inf of the input (refinement stopping test)
+      double anorm = 0;
+      if (sizeof(F) == sizeof(float)) {
+        for (int i = gt; i < n; i += nt) {
+          double rs = 0;
+          for (int j = 0; j < n; ++j) {
+            const double v = spd ? (i >= j ? Ag[i + (long)j * n] : Ag[j + (long)i * n]) : Ag[i + (long)j * n];
+            rs += fabs(v);
+          }
+          anorm = fmax(anorm, rs);
+        }
+        anorm = group_max(anorm, gt, nt, gid, red[gid]);
+      }
+      if (fbuf != reinterpret_cast<F *>(Ag))
+        for (int e = gt; e < n * n; e += nt) fbuf[e] = (F)Ag[e];
+      group_sync(gid, nt);
+      const int info = spd ? chol_inplace<F>(M, n, gt, nt, gid)
+                           : lu_inplace<F>(M, n, ipiv, gt, nt, gid, sk[gid], si[gid]);
+      int iters = 0;
+      if (info == 0) {
+        for (int e = gt; e < n * nrhs; e += nt) Xg[e] = Bg[e];
+        group_sync(gid, nt);
+        solve_inplace<F>(M, n, spd, ipiv, Xg, n, nrhs, gt, nt, gid);
+        if (sizeof(F) == sizeof(float)) {
+          double *R = a.R + a.b_off[mi];
+          for (iters = 0; iters < a.max_ir; ++iters) {
+            double rmax = 0, xmax = 0;
+            for (int e = gt; e < n * nrhs; e += nt) {
+              const int i = e % n, c = e / n;
+              double acc = Bg[i + (long)c * n];
+              for (int j = 0; j < n; ++j) {
+                const double v =
+                    spd ? (i >= j ? Ag[i + (long)j * n] : Ag[j + (long)i * n]) : Ag[i + (long)j * n];
+                acc -= v * Xg[j + (long)c * n];
+              }
+              R[e] = acc;
+              rmax = fmax(rmax, fabs(acc));
+              xmax = fmax(xmax, fabs(Xg[e]));
+            }
+            rmax = group_max(rmax, gt, nt, gid, red[gid]);
+            xmax = group_max(xmax, gt, nt, gid, red[gid]);
+            if (rmax <= 4.0 * 1.1102230246251565e-16 * anorm * xmax) break;
+            solve_inplace<F>(M, n, spd, ipiv, R, n, nrhs, gt, nt, gid);
+            for (int e = gt; e < n * nrhs; e += nt) Xg[e] += R[e];
+            group_sync(gid, nt);
+          }
+        }
+      }
+      if (gt == 0) {
+        a.info[mi] = info;
+        if (a.iters) a.iters[mi] = iters;
+      }
+      if (sizeof(F) == sizeof(double) && in_smem)  // FP64: A <- factors
+        for (int e = gt; e < n * n; e += nt) Ag[e] = (double)fbuf[e];
+    }
+    __syncthreads();
+  }
+  (void)status;
+}
+
+// ---------------------------------------------------------------------------
+// Host: size classes, schedules, plans, autotuning.
+
+namespace {
+
+constexpr int kEdges[] = {24, 32, 48, 64, 96, 128, 160, 192, 256, 1 << 30};
+constexpr int kClasses = sizeof(kEdges) / sizeof(int);
+int class_of(int n) {
+  int c = 0;
+  while (n > kEdges[c]) ++c;
+  return c;
+}
+// warps per matrix by class; [0] FP64, [1] FP32 + refinement
+int g_sched[2][kClasses] = {{1, 1, 1, 2, 4, 8, 8, 8, 8, 8}, {1, 1, 1, 2, 2, 4, 8, 8, 8, 8}};
+
+}  // namespace
+
+int batched_classes(int *edges, int cap) {
+  for (int c = 0; c < std::min(cap, kClasses); ++c) edges[c] = kEdges[c];
+  return kClasses;
+}
+
+int batched_schedule(int fp32, int *warps, int cap, bool set) {
+  for (int c = 0; c < std::min(cap, kClasses); ++c) {
+    if (set) {
+      if (warps[c] != 1 && warps[c] != 2 && warps[c] != 4 && warps[c] != 8) return kErrInvalid;
+      g_sched[fp32 ? 1 : 0][c] = warps[c];
+    } else {
+      warps[c] = g_sched[fp32 ? 1 : 0][c];
+    }
+  }
+  return kClasses;
+}
+
+int batched_plan_create(BatchPlan **out, int count, const int *n, const int *spd, int nrhs,
+                        int fp32, int max_ir) {
+  *out = nullptr;
+  if (count < 0 || nrhs < 1 || nrhs > 64) return kErrInvalid;
+  auto *p = new BatchPlan{};
+  p->count = count;
+  p->nrhs = nrhs;
+  p->fp32 = fp32;
+  p->max_ir = max_ir > 0 ? max_ir : 10;
+  std::vector<long> aoff(count), boff(count), poff(count);
+  long sa = 0, sb = 0, sp = 0;
+  int nmax = 0;
+  for (int i = 0; i < count; ++i) {
+    if (n[i] < 1) {
+      delete p;
+      set_last_error("batched plan: n[%d] = %d", i, n[i]);
+      return kErrInvalid;
+    }
+    aoff[i] = sa;
+    boff[i] = sb;
+    poff[i] = sp;
+    sa += (long)n[i] * n[i];
+    sb += (long)n[i] * nrhs;
+    sp += n[i];
+    nmax = std::max(nmax, n[i]);
+  }
+  p->a_elems = sa;
+  p->b_elems = sb;
+  p->p_elems = sp;
+  p->nmax = nmax;
+  // tasks: matrices sorted by n (descending), grouped per class by its warp count
+  std::vector<int> order(count);
+  for (int i = 0; i < count; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return n[x] > n[y]; });
+  std::vector<BatchTask> tasks;
+  std::vector<double> cost;
+  for (size_t q = 0; q < order.size();) {
+    const int c = class_of(n[order[q]]);
+    const int w = g_sched[fp32 ? 1 : 0][c];
+    BatchTask t{};
+    t.warps = w;
+    double cc = 0;
+    while (t.count < 8 / w && q < order.size() && class_of(n[order[q]]) == c) {
+      const double nn = n[order[q]];
+      cc = std::max(cc, nn * nn * nn / (2.0 + w));
+      t.mat[t.count++] = order[q++];
+    }
+    tasks.push_back(t);
+    cost.push_back(cc);
+  }
+  std::vector<int> ti(tasks.size());
+  for (size_t i = 0; i < ti.size(); ++i) ti[i] = (int)i;
+  std::stable_sort(ti.begin(), ti.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+  std::vector<BatchTask> sorted(tasks.size());
+  for (size_t i = 0; i < ti.size(); ++i) sorted[i] = tasks[ti[i]];
+  p->ntasks = (int)sorted.size();
+  DeviceInfo di;
+  int r = device_info(&di);
+  if (r < 0) { delete p; return r; }
+  p->grid = di.num_sms;
+  p->scratch_per_group = fp32 ? (long)nmax * nmax : 0;
+  // device buffers: descriptors, tasks, per-group FP32 scratch, residuals, queue
+  const size_t bytes = sizeof(int) * 2 * count + sizeof(long) * 3 * count +
+                       sizeof(BatchTask) * sorted.size() +
+                       sizeof(float) * (size_t)p->grid * 8 * p->scratch_per_group +
+                       (fp32 ? sizeof(double) * sb : 0) + 4096;
+  if (cudaMalloc(&p->dev, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    delete p;
+    set_last_error("batched plan: cudaMalloc(%zu) failed", bytes);
+    return kErrAlloc;
+  }
+  char *c = (char *)p->dev;
+  auto take = [&](size_t b) {
+    char *q = c;
+    c += (b + 255) / 256 * 256;
+    return (void *)q;
+  };
+  p->d_n = (int *)take(sizeof(int) * count);
+  p->d_spd = (int *)take(sizeof(int) * count);
+  p->d_aoff = (long *)take(sizeof(long) * count);
+  p->d_boff = (long *)take(sizeof(long) * count);
+  p->d_poff = (long *)take(sizeof(long) * count);
+  p->d_tasks = (BatchTask *)take(sizeof(BatchTask) * sorted.size());
+  p->d_scratch = (float *)take(sizeof(float) * (size_t)p->grid * 8 * p->scratch_per_group);
+  p->d_R = fp32 ? (double *)take(sizeof(double) * sb) : nullptr;
+  p->d_queue = (unsigned *)take(64);
+  std::vector<int> spdv(count);
+  for (int i = 0; i < count; ++i) spdv[i] = spd ? spd[i] : 0;
+  cudaMemcpy(p->d_n, n, sizeof(int) * count, cudaMemcpyHostToDevice);
+  cudaMemcpy(p->d_spd, spdv.data(), sizeof(int) * count, cudaMemcpyHostToDevice);
+  cudaMemcpy(p->d_aoff, aoff.data(), sizeof(long) * count, cudaMemcpyHostToDevice);
+  cudaMemcpy(p->d_boff, boff.data(), sizeof(long) * count, cudaMemcpyHostToDevice);
+  cudaMemcpy(p->d_poff, poff.data(), sizeof(long) * count, cudaMemcpyHostToDevice);
+  if (cudaMemcpy(p->d_tasks, sorted.data(), sizeof(BatchTask) * sorted.size(),
+                 cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(p->dev);
+    delete p;
+    set_last_error("batched plan: upload failed");
+    return kErrCuda;
+  }
+  double fl = 0;
+  for (int i = 0; i < count; ++i) {
+    const double nn = n[i];
+    fl += (spd && spd[i] ? nn * nn * nn / 3 : 2 * nn * nn * nn / 3) + 2.0 * nn * nn * nrhs;
+  }
+  p->flops = fl;
+  *out = p;
+  return 0;
+}
+
+void batched_plan_destroy(BatchPlan *p) {
+  if (!p) return;
+  if (p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
+  if (p->dev) cudaFree(p->dev);
+  delete p;
+}
+
+// Stream-ordered execution: a memset and one persistent launch (capturable).
+int batched_plan_execute(BatchPlan *p, double *A, const double *B, double *X, int *ipiv, int *info,
+                         int *iters, cudaStream_t s) {
+  BatchArgs a{};
+  a.n = p->d_n;
+  a.spd = p->d_spd;
+  a.a_off = p->d_aoff;
+  a.b_off = p->d_boff;
+  a.p_off = p->d_poff;
+  a.nrhs = p->nrhs;
+  a.max_ir = p->max_ir;
+  a.A = A;
+  a.B = B;
+  a.X = X;
+  a.R = p->d_R;
+  a.ipiv = ipiv;
+  a.info = info;
+  a.iters = iters;
+  ZG_CUDA(cudaMemsetAsync(p->d_queue, 0, sizeof(unsigned), s));
+  if (p->fp32) {
+    static bool attr = false;
+    if (!attr) {
+      ZG_CUDA(cudaFuncSetAttribute(batched_kernel<float>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTotal));
+      attr = true;
+    }
+    ZG_LAUNCH(kTagBatched, p->flops, 0, s,
+              batched_kernel<float><<<p->grid, 256, kSmemTotal, s>>>(
+                  a, p->d_tasks, p->ntasks, p->d_queue, p->d_scratch, p->scratch_per_group,
+                  nullptr));
+  } else {
+    static bool attr = false;
+    if (!attr) {
+      ZG_CUDA(cudaFuncSetAttribute(batched_kernel<double>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTotal));
+      attr = true;
+    }
+    ZG_LAUNCH(kTagBatched, p->flops, 0, s,
+              batched_kernel<double><<<p->grid, 256, kSmemTotal, s>>>(
+                  a, p->d_tasks, p->ntasks, p->d_queue, nullptr, 0, nullptr));
+  }
+  return 0;
+}
+
+// Captures the execution for these buffers in a CUDA graph once, then replays it.
+int batched_plan_run_graph(BatchPlan *p, double *A, const double *B, double *X, int *ipiv,
+                           int *info, int *iters, cudaStream_t s) {
+  const void *key[6] = {A, B, X, ipiv, info, iters};
+  bool same = p->graph_exec != nullptr;
+  for (int i = 0; i < 6 && same; ++i) same = p->graph_key[i] == key[i];
+  if (!same) {
+    if (p->graph_exec) {
+      cudaGraphExecDestroy(p->graph_exec);
+      p->graph_exec = nullptr;
+    }
+    cudaStream_t cs;
+    ZG_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    ZG_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    const int r = batched_plan_execute(p, A, B, X, ipiv, info, iters, cs);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(cs, &g);
+    cudaStreamDestroy(cs);
+    if (r < 0) return r;
+    ZG_CUDA(e);
+    ZG_CUDA(cudaGraphInstantiate(&p->graph_exec, g, 0));
+    cudaGraphDestroy(g);
+    for (int i = 0; i < 6; ++i) p->graph_key[i] = key[i];
+  }
+  ZG_CUDA(cudaGraphLaunch(p->graph_exec, s));
+  ++g_launches;
+  return 0;
+}
+
+}  // namespace zg
+
+namespace zg {
+
+namespace {
+// deterministic test matrices for the autotuner: general (hash-uniform) or
+// SPD (symmetrised, shifted by n on the diagonal)
+__global__ void fill_batch_kernel(int count, int n, double *A, double *B, int nrhs,
+                                  unsigned seed) {
+  const long per = (long)n * n;
+  const long total = per * count;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total;
+       e += (long)gridDim.x * blockDim.x) {
+    const int m = e / per;
+    const int r = (e % per) % n, c = (e % per) / n;
+    const int lo = min(r, c), hi = max(r, c);
+    const bool spd = m & 1;
+    unsigned h = seed ^ (unsigned)(m * 2654435761u) ^ (unsigned)((spd ? lo * 40503u + hi : r * 40503u + c) * 2246822519u);
+    h ^= h >> 15; h *= 2654435761u; h ^= h >> 13;
+    double v = (h & 0xffffff) / 16777216.0 - 0.5;
+    if (spd && r == c) v += n;
+    A[e] = v;
+  }
+  const long tb = (long)n * nrhs * count;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < tb;
+       e += (long)gridDim.x * blockDim.x)
+    B[e] = ((e * 2654435761u) & 0xffff) / 65536.0 - 0.5;
+}
+}  // namespace
+
+// Times every feasible warp count for every size class on a synthetic batch
+// of the class's largest n and keeps the fastest.  Writes the chosen warps
+// per class into `chosen` (if not null).
+int batched_autotune(int fp32, int nrhs, cudaStream_t s, int *chosen, double *ms_out) {
+  DeviceInfo di;
+  ZG_TRY(device_info(&di));
+  int saved[kClasses];
+  for (int c = 0; c < kClasses; ++c) saved[c] = g_sched[fp32 ? 1 : 0][c];
+  cudaEvent_t e0, e1;
+  ZG_CUDA(cudaEventCreate(&e0));
+  ZG_CUDA(cudaEventCreate(&e1));
+  int rc = 0;
+  for (int c = 0; c < kClasses && rc == 0; ++c) {
+    const int n = std::min(kEdges[c], 256);
+    // enough matrices for a few full waves of groups
+    const int count = std::max(2 * di.num_sms, std::min(8 * di.num_sms * 2, (int)(4e8 / ((double)n * n * n))));
+    std::vector<int> nv(count, n), sv(count);
+    for (int i = 0; i < count; ++i) sv[i] = i & 1;
+    double *dA = nullptr, *dA0 = nullptr, *dB = nullptr, *dX = nullptr;
+    int *dp = nullptr, *di2 = nullptr, *dit = nullptr;
+    const size_t na = (size_t)count * n * n, nb = (size_t)count * n * nrhs;
+    if (cudaMalloc(&dA, 8 * na) || cudaMalloc(&dA0, 8 * na) || cudaMalloc(&dB, 8 * nb) ||
+        cudaMalloc(&dX, 8 * nb) || cudaMalloc(&dp, 4 * (size_t)count * n) ||
+        cudaMalloc(&di2, 4 * (size_t)count) || cudaMalloc(&dit, 4 * (size_t)count)) {
+      cudaGetLastError();
+      rc = kErrAlloc;
+    }
+    if (rc == 0) {
+      fill_batch_kernel<<<std::min((int)((na + 255) / 256), 152 * 16), 256, 0, s>>>(count, n, dA0, dB, nrhs, 1234u + c);
+      double best = 1e30;
+      int bestw = saved[c];
+      for (int w : {1, 2, 4, 8}) {
+        g_sched[fp32 ? 1 : 0][c] = w;
+        BatchPlan *p = nullptr;
+        if (batched_plan_create(&p, count, nv.data(), sv.data(), nrhs, fp32, 10) < 0) continue;
+        float tot = 0;
+        for (int rep = 0; rep < 3; ++rep) {
+          cudaMemcpyAsync(dA, dA0, 8 * na, cudaMemcpyDeviceToDevice, s);
+          cudaEventRecord(e0, s);
+          batched_plan_execute(p, dA, dB, dX, dp, di2, dit, s);
+          cudaEventRecord(e1, s);
+          cudaEventSynchronize(e1);
+          float ms = 0;
+          cudaEventElapsedTime(&ms, e0, e1);
+          if (rep > 0) tot += ms;
+        }
+        batched_plan_destroy(p);
+        if (tot < best) { best = tot; bestw = w; }
+      }
+      g_sched[fp32 ? 1 : 0][c] = bestw;
+      saved[c] = bestw;
+      if (ms_out) ms_out[c] = best / 2;
+    }
+    cudaFree(dA); cudaFree(dA0); cudaFree(dB); cudaFree(dX); cudaFree(dp); cudaFree(di2); cudaFree(dit);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (int c = 0; c < kClasses; ++c) {
+    g_sched[fp32 ? 1 : 0][c] = saved[c];
+    if (chosen) chosen[c] = saved[c];
+  }
+  ZG_CUDA(cudaGetLastError());
+  return rc;
+}
+
+}  // namespace zg

@@ -19,6 +19,7 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "kernels_batched.h"
 #include "kernels_mixed.h"
 #include "kernels_tc.h"
 
@@ -632,6 +633,47 @@ int zml_gpu_dgesv_mpir(int n, int nrhs, const double *dA, int ldda, const double
   MpirResult local;
   return gesv_mpir_dev(n, nrhs, dA, ldda, dB, lddb, dX, lddx, o, res ? res : &local,
                        (cudaStream_t)stream);
+}
+
+// ---- batched small solves ----
+int zml_gpu_batched_plan_create(void **plan, int count, const int *n, const int *spd, int nrhs,
+                                int prec, int max_ir) {
+  if (!plan) return -1;
+  if (count < 0) return -2;
+  if (!n && count > 0) return -3;
+  if (nrhs < 1 || nrhs > 64) return -5;
+  if (prec != 0 && prec != 1) return -6;
+  for (int i = 0; i < count; ++i)
+    if (n[i] < 1 || n[i] > 256) {
+      set_last_error("batched: n[%d] = %d outside 1..256", i, n[i]);
+      return kErrInvalid;
+    }
+  BatchPlan *p = nullptr;
+  ZG_TRY(batched_plan_create(&p, count, n, spd, nrhs, prec, max_ir));
+  *plan = p;
+  return 0;
+}
+int zml_gpu_batched_execute(void *plan, double *dA, const double *dB, double *dX, int *dipiv,
+                            int *dinfo, int *diters, void *stream) {
+  if (!plan) return -1;
+  return batched_plan_execute((BatchPlan *)plan, dA, dB, dX, dipiv, dinfo, diters,
+                              (cudaStream_t)stream);
+}
+int zml_gpu_batched_run_graph(void *plan, double *dA, const double *dB, double *dX, int *dipiv,
+                              int *dinfo, int *diters, void *stream) {
+  if (!plan) return -1;
+  return batched_plan_run_graph((BatchPlan *)plan, dA, dB, dX, dipiv, dinfo, diters,
+                                (cudaStream_t)stream);
+}
+void zml_gpu_batched_plan_destroy(void *plan) { batched_plan_destroy((BatchPlan *)plan); }
+int zml_gpu_batched_schedule(int prec, int *warps, int *edges, int cap, int set) {
+  if (edges) batched_classes(edges, cap);
+  return batched_schedule(prec, warps, cap, set != 0);
+}
+int zml_gpu_batched_autotune(int prec, int nrhs, int *chosen, double *ms, void *stream) {
+  if (prec != 0 && prec != 1) return -1;
+  if (nrhs < 1 || nrhs > 64) return -2;
+  return batched_autotune(prec, nrhs, (cudaStream_t)stream, chosen, ms);
 }
 
 const char *zml_gpu_last_error(void) { return last_error(); }
