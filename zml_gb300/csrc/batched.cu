@@ -49,7 +49,7 @@ template <typename F> struct View {
 
 // argmax of |a(i,k)| over the group: first maximum wins (iamax.zig:29-38)
 template <typename F>
-__device__ void group_argmax(F &key, int &idx, int tid, int nt, int gid, float *sk, int *si) {
+__device__ void group_argmax(F &key, int &idx, int tid, int nt, int gid, double *sk, int *si) {
   const int lane = tid & 31, w = tid >> 5, nw = nt >> 5;
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
@@ -70,7 +70,7 @@ __device__ void group_argmax(F &key, int &idx, int tid, int nt, int gid, float *
 }
 
 template <typename F>
-__device__ int lu_inplace(View<F> M, int n, int *ipiv, int tid, int nt, int gid, float *sk,
+__device__ int lu_inplace(View<F> M, int n, int *ipiv, int tid, int nt, int gid, double *sk,
                           int *si) {
   int info = 0;
   for (int k = 0; k < n; ++k) {
@@ -133,19 +133,20 @@ template <typename F>
 __device__ void solve_inplace(View<F> M, int n, bool spd, const int *ipiv, double *X, int ldx,
                               int nrhs, int tid, int nt, int gid) {
   if (!spd) {
-    if (tid < nrhs)
+    for (int c = tid; c < nrhs; c += nt)
       for (int k = 0; k < n; ++k) {
         const int p = ipiv[k] - 1;
         if (p != k) {
-          const double t = X[k + tid * ldx];
-          X[k + tid * ldx] = X[p + tid * ldx];
-          X[p + tid * ldx] = t;
+          const double t = X[k + c * ldx];
+          X[k + c * ldx] = X[p + c * ldx];
+          X[p + c * ldx] = t;
         }
       }
     group_sync(gid, nt);
   }
   for (int k = 0; k < n; ++k) {  // forward: unit L (LU) or L (Cholesky)
-    if (spd && tid < nrhs) X[k + tid * ldx] /= (double)M(k, k);
+    if (spd)
+      for (int c = tid; c < nrhs; c += nt) X[k + c * ldx] /= (double)M(k, k);
     group_sync(gid, nt);
     for (int c = 0; c < nrhs; ++c) {
       const double xk = X[k + c * ldx];
@@ -154,7 +155,7 @@ __device__ void solve_inplace(View<F> M, int n, bool spd, const int *ipiv, doubl
     group_sync(gid, nt);
   }
   for (int k = n - 1; k >= 0; --k) {  // backward: U (LU) or L^T (Cholesky)
-    if (tid < nrhs) X[k + tid * ldx] /= (double)M(k, k);
+    for (int c = tid; c < nrhs; c += nt) X[k + c * ldx] /= (double)M(k, k);
     group_sync(gid, nt);
     for (int c = 0; c < nrhs; ++c) {
       const double xk = X[k + c * ldx];
@@ -185,7 +186,7 @@ __global__ void __launch_bounds__(256) batched_kernel(BatchArgs a, const BatchTa
                                                       long gscratch_per_group, unsigned *status) {
   extern __shared__ __align__(16) unsigned char bsm[];
   __shared__ unsigned s_task;
-  __shared__ float sk[8][16];
+  __shared__ double sk[8][8];  // per-group argmax keys, read back as F (8-byte aligned)
   __shared__ int si[8][8];
   __shared__ double red[8][8];
   const int tid = threadIdx.x;
