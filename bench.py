@@ -51,6 +51,7 @@ def parse():
     p.add_argument("--n", type=int, default=16384)
     p.add_argument("--prec", type=int, default=3, help="0 fp16, 1 bf16, 2 fp32, 3 bf16x3")
     p.add_argument("--mode", type=int, default=1, help="0 plain IR, 1 GMRES-IR")
+    p.add_argument("--batched", type=int, default=1, help="also run the batched config (1/0)")
     return p.parse_args()
 
 
@@ -184,6 +185,83 @@ def cpu_block(n, threads, label):
 
 
 # ---------------------------------------------------------------------------
+# Batched uneven solves: 20000 systems, n ~ U{8..256}; even index SPD
+# G G^T / n + 0.1 I (potrf + potrs), odd index N(0,1) (getrf + getrs); 4 RHS.
+def batched_workload(torch, dev, count=20000, nrhs=4, seed=7):
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    n = rng.integers(8, 257, size=count).astype(np.int32)
+    spd = (np.arange(count) % 2 == 0).astype(np.int32)
+    g = torch.Generator(device=dev).manual_seed(seed)
+    offs = np.concatenate([[0], np.cumsum(n.astype(np.int64) ** 2)])
+    A = torch.empty(int(offs[-1]), dtype=torch.float64, device=dev)
+    for k in np.unique(n):
+        idx = np.nonzero(n == k)[0]
+        for kind in (0, 1):
+            sel = idx[spd[idx] == kind]
+            if len(sel) == 0:
+                continue
+            G = torch.randn(len(sel), int(k), int(k), dtype=torch.float64, device=dev, generator=g)
+            if kind:
+                G = G @ G.transpose(1, 2) / float(k) + 0.1 * torch.eye(int(k), dtype=torch.float64,
+                                                                       device=dev)
+            flat = G.transpose(1, 2).reshape(len(sel), -1)  # column-major storage
+            for j, m in enumerate(sel):
+                A[offs[m]:offs[m + 1]] = flat[j]
+    B = torch.rand(int((n.astype(np.int64) * nrhs).sum()), dtype=torch.float64, device=dev,
+                   generator=g) * 2 - 1
+    flops = float(sum((k ** 3 / 3.0 if s else 2.0 * k ** 3 / 3) + 2.0 * k * k * nrhs
+                      for k, s in zip(n.astype(np.float64), spd)))
+    nbytes = float(sum(8.0 * (k * (k + 1) if s else 2 * k * k) + 16.0 * k * nrhs + (0 if s else 4 * k)
+                       for k, s in zip(n.astype(np.float64), spd)))
+    return n, spd, A, B, flops, nbytes
+
+
+def batched_bench(torch, zg, L, dev, st, steps, warmup, hbm):
+    n, spd, A0, B, flops, nbytes = batched_workload(torch, dev)
+    nrhs, count = 4, len(n)
+    out = {"workload": "%d systems, n~U{8..256}, half SPD (potrf+potrs), half N(0,1) "
+                       "(getrf+getrs), %d RHS" % (count, nrhs), "count": count,
+           "algorithmic_flops": flops, "algorithmic_bytes": nbytes}
+    for prec, name in ((0, "fp64"), (1, "fp32_factor_fp64_ir")):
+        ncls = L.zml_gpu_batched_schedule(prec, None, None, 0, 0)
+        chosen = (C.c_int * ncls)()
+        L.zml_gpu_batched_autotune(prec, nrhs, chosen, None, st.cuda_stream)
+        plan = C.c_void_p()
+        rc = L.zml_gpu_batched_plan_create(C.byref(plan), count, n.ctypes.data_as(C.c_void_p),
+                                           spd.ctypes.data_as(C.c_void_p), nrhs, prec, 10)
+        if rc != 0:
+            raise RuntimeError("batched plan: %s" % zg.last_error())
+        A = A0.clone()
+        X = torch.zeros_like(B)
+        P = torch.zeros(int(n.sum()), dtype=torch.int32, device=dev)
+        info = torch.zeros(count, dtype=torch.int32, device=dev)
+        iters = torch.zeros(count, dtype=torch.int32, device=dev)
+        args = (plan, A.data_ptr(), B.data_ptr(), X.data_ptr(), P.data_ptr(), info.data_ptr(),
+                iters.data_ptr(), st.cuda_stream)
+        total = 0.0
+        for it in range(max(3, warmup) + steps):
+            if prec == 0:
+                A.copy_(A0)  # the FP64 path factors A in place
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            if L.zml_gpu_batched_run_graph(*args) != 0:
+                raise RuntimeError("batched run: %s" % zg.last_error())
+            e1.record(st)
+            torch.cuda.synchronize()
+            if it >= max(3, warmup):
+                total += e0.elapsed_time(e1) / 1e3
+        t = total / steps
+        L.zml_gpu_batched_plan_destroy(plan)
+        ok = int((info == 0).sum().item())
+        out[name] = {"solves_per_s": count / t, "ms_per_batch": 1e3 * t,
+                     "tflops": flops / t / 1e12, "hbm_gbs": nbytes / t / 1e9,
+                     "hbm_frac": nbytes / t / 1e9 / hbm, "info_ok": ok,
+                     "schedule_warps_per_class": list(chosen),
+                     "max_refinement_steps": int(iters.max().item()) if prec else 0}
+    return out
+
+
 def main():
     a = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -324,11 +402,13 @@ def main():
         t_e2e = tt.item()
     e2e_ok = bool(torch.allclose(xh.to(dev), X, rtol=0, atol=1e-9))
 
+    hbm, bf16, src = peaks()
+    batched = batched_bench(torch, zg, L, dev, st, a.steps, a.warmup, hbm) if a.batched else None
+
     if rank != 0:
         dist.destroy_process_group()
         return 0
 
-    hbm, bf16, src = peaks()
     dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else None
     roof = None
     if dom:
@@ -370,6 +450,7 @@ def main():
         "e2e": {"value": world / t_e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * n * n + 8 * n,
                 "d2h_bytes_per_step": 8 * n, "matches_device_result": e2e_ok},
         "roofline": roof, "kernel_breakdown": breakdown, "gpu_launches": int(launches),
+        "batched": batched,
         "clocks": clk.summary(), "cpu_baseline": cpu,
     }
     print(json.dumps(out))
