@@ -148,6 +148,21 @@ int zml_dgesv_mpir(int matrix_layout, int n, int nrhs, const double *a, int lda,
  * fallback with *iter < 0); the mixed-precision form of gesv.zig:13. */
 int LAPACKE_dsgesv(int matrix_layout, int n, int nrhs, double *a, int lda, int *ipiv, double *b,
                    int ldb, double *x, int ldx, int *iter);
+/* The SPD problem of lapack/posv.zig:15 to FP64 backward error: Cholesky
+ * with trailing SYRK updates in `prec` (tensor cores for fp16/bf16/bf16x3),
+ * then IR / GMRES-IR with FP64 residuals.  Only the `uplo` triangle of A is
+ * read; A and B are not modified.  Host or device pointers. */
+int zml_dposv_mpir(int matrix_layout, char uplo, int n, int nrhs, const double *a, int lda,
+                   const double *b, int ldb, double *x, int ldx, int prec, int mode, double tol,
+                   int max_iter, zml_mpir_result *res);
+/* LAPACK dsposv semantics (FP32 Cholesky, FP64 refinement, FP64 potrf
+ * fallback with *iter < 0); the mixed-precision form of posv.zig:15. */
+int LAPACKE_dsposv(int matrix_layout, char uplo, int n, int nrhs, double *a, int lda, double *b,
+                   int ldb, double *x, int ldx, int *iter);
+/* Device-pointer, stream-ordered form of zml_dposv_mpir (column-major). */
+int zml_gpu_dposv_mpir(char uplo, int n, int nrhs, const double *dA, int ldda, const double *dB,
+                       int lddb, double *dX, int lddx, int prec, int mode, double tol,
+                       int max_iter, zml_mpir_result *res, void *stream);
 /* Device-pointer, stream-ordered form of zml_dgesv_mpir (column-major). */
 int zml_gpu_dgesv_mpir(int n, int nrhs, const double *dA, int ldda, const double *dB, int lddb,
                        double *dX, int lddx, int prec, int mode, double tol, int max_iter,

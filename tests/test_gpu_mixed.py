@@ -126,3 +126,73 @@ def test_dsgesv_lapack_semantics_and_fallback():
     assert it[0] < 0
     lu_ref, ipiv_ref, _ = ol.getrf(svd_matrix(n, 1e13, seed=4))
     np.testing.assert_array_equal(ipiv, ipiv_ref)
+
+
+# ---- SPD systems: mixed-precision Cholesky + refinement ---------------------
+
+def spd_matrix(n, seed, kappa=None):
+    rng = np.random.default_rng(seed)
+    if kappa is None:
+        g = rng.standard_normal((n, n))
+        return np.asfortranarray(g @ g.T / n + np.eye(n))
+    v, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    s = kappa ** (-np.arange(n) / (n - 1))
+    return np.asfortranarray((v * s) @ v.T)
+
+
+def solve_spd(a, b, prec, mode, uplo=b"L"):
+    n, nrhs = b.shape
+    x = np.zeros((n, nrhs), order="F")
+    res = zg.MpirResult()
+    r = zg.lib().zml_dposv_mpir(102, uplo, n, nrhs, P(a), n, P(b), n, P(x), n, prec, mode, 0.0,
+                                30, res)
+    assert r == 0, zg.last_error()
+    return x, res
+
+
+def fp64_chol_berr(a, b):
+    f, info = ol.potrf(a, 122)
+    return berr(a, ol.potrs(f, b, 122), b)
+
+
+@pytest.mark.parametrize("prec,mode", [(3, 1), (2, 0), (1, 1), (0, 0), (3, 0)])
+@pytest.mark.parametrize("n", [300, 1100])
+def test_mixed_cholesky_reaches_fp64_backward_error(n, prec, mode):
+    a = spd_matrix(n, seed=n + prec)
+    xt = np.random.default_rng(9).uniform(-1, 1, (n, 2))
+    b = np.asfortranarray(a @ xt)
+    x, res = solve_spd(a, b, prec, mode)
+    assert res.info == 0
+    assert res.converged, (res.berr, list(res.berr_history[:res.iters + 1]))
+    assert berr(a, x, b) <= 2 * fp64_chol_berr(a, b) + U64
+
+
+def test_mixed_cholesky_upper_and_ill_conditioned():
+    n = 512
+    a = spd_matrix(n, seed=3, kappa=1e6)
+    xt = np.random.default_rng(4).uniform(-1, 1, (n, 1))
+    b = np.asfortranarray(a @ xt)
+    # only the upper triangle is read: poison the strict lower one
+    au = np.triu(a) + np.tril(np.full((n, n), np.nan), -1)
+    x, res = solve_spd(np.asfortranarray(au), b, 3, 1, uplo=b"U")
+    assert res.info == 0 and res.converged, (res.berr, list(res.berr_history[:res.iters + 1]))
+    assert berr(a, x, b) <= 2 * fp64_chol_berr(a, b) + U64
+
+
+def test_mixed_cholesky_not_spd_and_dsposv():
+    n = 300
+    a = spd_matrix(n, seed=5)
+    a[200, 200] = -10.0
+    b = np.asfortranarray(np.ones((n, 1)))
+    _, res = solve_spd(a, b, 3, 1)
+    assert res.info > 0
+    good = spd_matrix(n, seed=6)
+    xt = np.random.default_rng(7).uniform(-1, 1, (n, 3))
+    bb = np.asfortranarray(good @ xt)
+    g0 = good.copy(order="F")
+    x = np.zeros((n, 3), order="F")
+    it = np.zeros(1, dtype=np.int32)
+    assert zg.lib().LAPACKE_dsposv(102, b"L", n, 3, P(good), n, P(bb), n, P(x), n, P(it)) == 0
+    assert it[0] >= 0
+    np.testing.assert_array_equal(good, g0)
+    np.testing.assert_allclose(x, xt, rtol=1e-10, atol=1e-11)

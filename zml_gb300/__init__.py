@@ -64,6 +64,11 @@ _SIGS.update({
     "zml_dgesv_mpir": (i32, [i32, i32, i32, vp, i32, vp, i32, vp, i32, i32, i32, f64, i32,
                              C.POINTER(MpirResult)]),
     "LAPACKE_dsgesv": (i32, [i32, i32, i32, vp, i32, vp, vp, i32, vp, i32, vp]),
+    "zml_dposv_mpir": (i32, [i32, ch, i32, i32, vp, i32, vp, i32, vp, i32, i32, i32, f64, i32,
+                             C.POINTER(MpirResult)]),
+    "LAPACKE_dsposv": (i32, [i32, ch, i32, i32, vp, i32, vp, i32, vp, i32, vp]),
+    "zml_gpu_dposv_mpir": (i32, [ch, i32, i32, vp, i32, vp, i32, vp, i32, i32, i32, f64, i32,
+                                 C.POINTER(MpirResult), vp]),
     "zml_gpu_dgesv_mpir": (i32, [i32, i32, vp, i32, vp, i32, vp, i32, i32, i32, f64, i32,
                                  C.POINTER(MpirResult), vp]),
 })

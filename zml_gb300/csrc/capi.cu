@@ -431,6 +431,29 @@ int mpir_any(int layout, int n, int nrhs, const double *a, int lda, const double
   return sync(s);
 }
 
+int posv_mpir_any(int layout, char uplo, int n, int nrhs, const double *a, int lda,
+                  const double *b, int ldb, double *x, int ldx, const MpirOpts &o,
+                  MpirResult *res) {
+  if (!lay_ok(layout)) return -1;
+  uplo = up(uplo);
+  if (uplo != 'U' && uplo != 'L') return -2;
+  if (n < 0) return -3;
+  if (nrhs < 0) return -4;
+  if (lda < std::max(1, n)) return -6;
+  if (ldb < std::max(1, layout == kColMajor ? n : nrhs)) return -8;
+  if (ldx < std::max(1, layout == kColMajor ? n : nrhs)) return -10;
+  *res = MpirResult{};
+  if (n == 0 || nrhs == 0) return 0;
+  cudaStream_t s = lib_stream();
+  ColMajor<double> A, B, X;
+  ZG_TRY(A.in(layout, a, lda, n, n, kSlotA, kSlotAT, true, s));
+  ZG_TRY(B.in(layout, b, ldb, n, nrhs, kSlotB, kSlotBT, true, s));
+  ZG_TRY(X.in(layout, x, ldx, n, nrhs, kSlotX, kSlotXT, false, s));
+  ZG_TRY(posv_mpir_dev(uplo == 'L', n, nrhs, A.d, A.ld, B.d, B.ld, X.d, X.ld, o, res, s));
+  ZG_TRY(X.out(s));
+  return sync(s);
+}
+
 }  // namespace
 
 static_assert(sizeof(MpirResult) == 6 * sizeof(int) + 34 * sizeof(double), "zml_mpir_result layout");
@@ -613,6 +636,68 @@ int LAPACKE_dsgesv(int layout, int n, int nrhs, double *a, int lda, int *ipiv, d
                          sizeof(double) * nrhs, n, cudaMemcpyDefault));
   }
   return gesv_any<double>(layout, n, nrhs, a, lda, ipiv, x, ldx);
+}
+
+// Mixed-precision SPD solve (low-precision Cholesky + FP64 refinement), host
+// or device pointers; only the `uplo` triangle of A is read.
+int zml_dposv_mpir(int layout, char uplo, int n, int nrhs, const double *a, int lda,
+                   const double *b, int ldb, double *x, int ldx, int prec, int mode, double tol,
+                   int max_iter, MpirResult *res) {
+  if (prec < 0 || prec > 3) return -11;
+  if (mode != 0 && mode != 1) return -12;
+  MpirOpts o;
+  o.prec = prec;
+  o.mode = mode;
+  o.tol = tol;
+  o.max_iter = max_iter > 0 ? max_iter : 30;
+  MpirResult local;
+  return posv_mpir_any(layout, uplo, n, nrhs, a, lda, b, ldb, x, ldx, o, res ? res : &local);
+}
+
+// LAPACK dsposv semantics: FP32 Cholesky + FP64 refinement; FP64 posv fallback
+// (iter < 0, a holding its factor) when refinement does not converge.
+int LAPACKE_dsposv(int layout, char uplo, int n, int nrhs, double *a, int lda, double *b, int ldb,
+                   double *x, int ldx, int *iter) {
+  MpirOpts o;
+  o.prec = kPrecFP32;
+  o.mode = kModeIR;
+  o.max_iter = 30;
+  MpirResult res;
+  int r = posv_mpir_any(layout, uplo, n, nrhs, a, lda, b, ldb, x, ldx, o, &res);
+  if (r < 0) return r;
+  if (iter) *iter = res.iters;
+  if (res.info == 0 && res.converged) return 0;
+  if (iter) *iter = -1;
+  if (layout == kColMajor) {
+    ZG_CUDA(cudaMemcpy2D(x, sizeof(double) * ldx, b, sizeof(double) * ldb, sizeof(double) * n,
+                         nrhs, cudaMemcpyDefault));
+  } else {
+    ZG_CUDA(cudaMemcpy2D(x, sizeof(double) * ldx, b, sizeof(double) * ldb,
+                         sizeof(double) * nrhs, n, cudaMemcpyDefault));
+  }
+  return posv_any<double>(layout, uplo, n, nrhs, a, lda, x, ldx);
+}
+
+int zml_gpu_dposv_mpir(char uplo, int n, int nrhs, const double *dA, int ldda, const double *dB,
+                       int lddb, double *dX, int lddx, int prec, int mode, double tol,
+                       int max_iter, MpirResult *res, void *stream) {
+  uplo = up(uplo);
+  if (uplo != 'U' && uplo != 'L') return -1;
+  if (n < 0) return -2;
+  if (nrhs < 0) return -3;
+  if (ldda < std::max(1, n)) return -5;
+  if (lddb < std::max(1, n)) return -7;
+  if (lddx < std::max(1, n)) return -9;
+  if (prec < 0 || prec > 3) return -10;
+  if (mode != 0 && mode != 1) return -11;
+  MpirOpts o;
+  o.prec = prec;
+  o.mode = mode;
+  o.tol = tol;
+  o.max_iter = max_iter > 0 ? max_iter : 30;
+  MpirResult local;
+  return posv_mpir_dev(uplo == 'L', n, nrhs, dA, ldda, dB, lddb, dX, lddx, o,
+                       res ? res : &local, (cudaStream_t)stream);
 }
 
 int zml_gpu_dgesv_mpir(int n, int nrhs, const double *dA, int ldda, const double *dB, int lddb,

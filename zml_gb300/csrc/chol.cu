@@ -63,18 +63,17 @@ __global__ void __launch_bounds__(256) potf2_kernel(int nb, T *A, long lda, bool
   }
 }
 
-template <typename T> int potrf_dev(int uplo, int n, T *A, long lda, int *info, cudaStream_t s) {
-  *info = 0;
-  if (n <= 0) return 0;
-  Control *ctl;
-  ZG_TRY(control(s, &ctl));
+// The blocked loop alone (no control block, no host sync): the first
+// non-positive pivot lands in ctl->info (1-based + info_base).
+template <typename T>
+int potrf_launch(int uplo, int n, T *A, long lda, Control *ctl, int info_base, cudaStream_t s) {
   const bool lower = uplo == kLower;
   const int nb = kCholNB;
   for (int j = 0; j < n; j += nb) {
     const int jb = min(nb, n - j);
     T *Ajj = A + j + (long)j * lda;
-    ZG_LAUNCH(kTagPotf2, 0, 0, s, potf2_kernel<T><<<1, 256, 0, s>>>(jb, Ajj, lda, lower, ctl, j));
-    ZG_CUDA(cudaGetLastError());
+    ZG_LAUNCH(kTagPotf2, jb * jb * jb / 3.0, 2.0 * sizeof(T) * jb * jb, s,
+              potf2_kernel<T><<<1, 256, 0, s>>>(jb, Ajj, lda, lower, ctl, info_base + j));
     const int rest = n - j - jb;
     if (rest <= 0) break;
     if (lower) {
@@ -88,6 +87,15 @@ template <typename T> int potrf_dev(int uplo, int n, T *A, long lda, int *info, 
       ZG_TRY(syrk_dev<T>(kUpper, kTrans, rest, jb, T(-1), A12, lda, T(1), A12 + jb, lda, s));
     }
   }
+  return 0;
+}
+
+template <typename T> int potrf_dev(int uplo, int n, T *A, long lda, int *info, cudaStream_t s) {
+  *info = 0;
+  if (n <= 0) return 0;
+  Control *ctl;
+  ZG_TRY(control(s, &ctl));
+  ZG_TRY(potrf_launch<T>(uplo, n, A, lda, ctl, 0, s));
   return check_status(s, ctl, info);
 }
 
@@ -105,6 +113,7 @@ int potrs_dev(int uplo, int n, int nrhs, const T *A, long lda, T *B, long ldb, c
 }
 
 #define INST(T)                                                                       \
+  template int potrf_launch<T>(int, int, T *, long, Control *, int, cudaStream_t);   \
   template int potrf_dev<T>(int, int, T *, long, int *, cudaStream_t);                \
   template int potrs_dev<T>(int, int, int, const T *, long, T *, long, cudaStream_t);
 INST(double)

@@ -92,7 +92,8 @@ enum Slot : int {
   kSlotBatch = 13,            // batched solver descriptors
   kSlotSwap = 14,             // composed row-interchange pairs
   kSlotQR = 15,               // QR: V, T, W, split-K partials, panel exchange
-  kNumSlots = 16
+  kSlotSym = 16,              // full symmetric FP64 copy for the mixed Cholesky solve
+  kNumSlots = 20
 };
 
 // Returns a device buffer of at least `bytes` bound to `stream` in `slot`.

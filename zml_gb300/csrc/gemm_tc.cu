@@ -41,8 +41,10 @@ template <int BN, int STAGES>
 __global__ void __launch_bounds__(256)
     gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    int M, int N, int K, float alpha, float beta, float *__restrict__ C, long ldc,
-                   int ab_type, unsigned *status) {
+                   int ab_type, unsigned *status, int tri) {
   using Cfg = TileCfg<BN, STAGES>;
+  // SYRK form: tiles strictly above the diagonal are not needed
+  if (tri && (int)(blockIdx.y * BN) >= (int)(blockIdx.x * kBM + kBM)) return;
   constexpr int kStages = STAGES;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *smem = reinterpret_cast<unsigned char *>(
@@ -180,7 +182,7 @@ int make_map(CUtensorMap *m, const void *base, int rows, int K, long ld, int box
 
 template <int BN, int STAGES>
 int launch(int M, int N, int K, float alpha, const void *A, long lda, const void *B, long ldb,
-           float beta, float *C, long ldc, int ab_type, unsigned *status, cudaStream_t s) {
+           float beta, float *C, long ldc, int ab_type, unsigned *status, int tri, cudaStream_t s) {
   CUtensorMap ta, tb;
   ZG_TRY(make_map(&ta, A, M, K, lda, kBM));
   ZG_TRY(make_map(&tb, B, N, K, ldb, BN));
@@ -193,7 +195,7 @@ int launch(int M, int N, int K, float alpha, const void *A, long lda, const void
   }
   dim3 grid(ceil_div(M, kBM), ceil_div(N, BN));
   ZG_LAUNCH(kTagGemmTC, 2.0 * M * N * K, 2.0 * ((double)M + N) * K + (beta != 0.f ? 8.0 : 4.0) * M * N, s, gemm_tc_kernel<BN, STAGES><<<grid, 256, Cfg::smem_bytes, s>>>(ta, tb, M, N, K, alpha, beta, C,
-                                                               ldc, ab_type, status));
+                                                               ldc, ab_type, status, tri));
   ZG_CUDA(cudaGetLastError());
   return 0;
 }
@@ -201,15 +203,16 @@ int launch(int M, int N, int K, float alpha, const void *A, long lda, const void
 }  // namespace
 
 int gemm_tc(int M, int N, int K, float alpha, const void *A, long lda, const void *B, long ldb,
-            float beta, float *C, long ldc, int ab_type, unsigned *status, cudaStream_t s) {
+            float beta, float *C, long ldc, int ab_type, unsigned *status, cudaStream_t s,
+            int tri) {
   if (M <= 0 || N <= 0) return 0;
   if (K <= 0) return scale_dev<float>(M, N, beta, C, ldc, s);
   if (ab_type != 0 && ab_type != 1) return kErrInvalid;
   // short K (the factorization updates): two stages, so three CTAs share an
   // SM and one CTA's epilogue overlaps the others' main loops; long K: four.
   if (K <= 256)
-    return launch<128, 2>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, ab_type, status, s);
-  return launch<128, 4>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, ab_type, status, s);
+    return launch<128, 2>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, ab_type, status, tri, s);
+  return launch<128, 4>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, ab_type, status, tri, s);
 }
 
 }  // namespace zg

@@ -51,6 +51,8 @@ int getrs_dev(int trans, int n, int nrhs, const T *A, long lda, const int *ipiv,
               cudaStream_t s);
 
 // chol.cu
+template <typename T>
+int potrf_launch(int uplo, int n, T *A, long lda, Control *ctl, int info_base, cudaStream_t s);
 template <typename T> int potrf_dev(int uplo, int n, T *A, long lda, int *info, cudaStream_t s);
 template <typename T>
 int potrs_dev(int uplo, int n, int nrhs, const T *A, long lda, T *B, long ldb, cudaStream_t s);

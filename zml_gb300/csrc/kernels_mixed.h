@@ -39,5 +39,11 @@ int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cud
 // low-precision factorization, then refinement of each right-hand side.
 int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, long ldb,
                   double *X, long ldx, const MpirOpts &o, MpirResult *res, cudaStream_t s);
+// SPD form: low-precision Cholesky (only the `lower` / upper triangle of A is
+// read) and the same refinement.
+int posv_mpir_dev(bool lower, int n, int nrhs, const double *A, long lda, const double *B,
+                  long ldb, double *X, long ldx, const MpirOpts &o, MpirResult *res,
+                  cudaStream_t s);
+int potrf_lowp(int n, float *A, long lda, int prec, Control *ctl, cudaStream_t s);
 
 }  // namespace zg

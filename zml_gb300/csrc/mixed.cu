@@ -42,7 +42,7 @@ template <> __device__ __forceinline__ __half to16(float v) { return __float2hal
 // each segment ldk wide (the A side of the three-product split GEMM).
 template <typename H>
 __global__ void to_kmajor_t_kernel(int rows, int k, const float *A, long lda, H *out, long ldo,
-                                   int ldk, bool split) {
+                                   int ldk, bool split, bool bside) {
   __shared__ float t[32][33];
   const int r0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
   for (int c = threadIdx.y; c < 32; c += 8) {
@@ -57,9 +57,10 @@ __global__ void to_kmajor_t_kernel(int rows, int k, const float *A, long lda, H 
     const H hi = to16<H>(v);
     H *o = out + (long)r * ldo + kk;
     o[0] = hi;
-    if (split) {
-      o[ldk] = hi;
-      o[2 * ldk] = to16<H>(v - (float)hi);
+    if (split) {  // A side [hi | hi | lo], B side [hi | lo | hi]
+      const H lo = to16<H>(v - (float)hi);
+      o[ldk] = bside ? lo : hi;
+      o[2 * ldk] = bside ? hi : lo;
     }
   }
 }
@@ -96,7 +97,7 @@ int d2s(int m, int n, const double *A, long lda, float *B, long ldb, cudaStream_
 // ldk: segment width (>= k, multiple of 8); the operand row stride is ldk,
 // or 3 ldk for the split (bf16x3) form.
 static int to_kmajor_t(int prec, int rows, int k, const float *A, long lda, void *out, int ldk,
-                       cudaStream_t s) {
+                       cudaStream_t s, bool bside = false) {
   if (rows <= 0) return 0;
   const bool split = prec == kPrecBF16x3;
   const long ldo = split ? 3L * ldk : ldk;
@@ -104,11 +105,11 @@ static int to_kmajor_t(int prec, int rows, int k, const float *A, long lda, void
   if (prec == kPrecFP16)
     ZG_LAUNCH(kTagConvert, 0, 4.0 * rows * k + 2.0 * rows * ldo, s,
               to_kmajor_t_kernel<__half><<<grid, blk, 0, s>>>(rows, k, A, lda, (__half *)out, ldo,
-                                                              ldk, false));
+                                                              ldk, false, false));
   else
     ZG_LAUNCH(kTagConvert, 0, 4.0 * rows * k + 2.0 * rows * ldo, s,
               to_kmajor_t_kernel<__nv_bfloat16><<<grid, blk, 0, s>>>(
-                  rows, k, A, lda, (__nv_bfloat16 *)out, ldo, ldk, split));
+                  rows, k, A, lda, (__nv_bfloat16 *)out, ldo, ldk, split, bside));
   return 0;
 }
 
@@ -176,6 +177,73 @@ int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cud
                    prec == kPrecFP16 ? 0 : 1, &ctl->status, s));
   }
   return 0;
+}
+
+// Low-precision Cholesky (lower) of an n x n SPD FP32 matrix: FP32 64-wide
+// diagonal blocks, FP32 block-column TRSM, trailing SYRK on the tensor cores
+// (lower 128 x 128 tiles only), NB = 256.  The first non-positive pivot lands
+// in ctl->info.
+int potrf_lowp(int n, float *A, long lda, int prec, Control *ctl, cudaStream_t s) {
+  if (n <= 0) return 0;
+  constexpr int NB = 256;
+  if (prec == kPrecFP32) return potrf_launch<float>(kLower, n, A, lda, ctl, 0, s);
+  const int segs = prec == kPrecBF16x3 ? 3 : 1;
+  void *wl, *wu;
+  ZG_TRY(workspace(s, kSlotL16, sizeof(uint16_t) * (size_t)n * NB * segs, &wl));
+  ZG_TRY(workspace(s, kSlotU16, sizeof(uint16_t) * (size_t)n * NB * segs, &wu));
+  for (int j = 0; j < n; j += NB) {
+    const int jb = std::min(NB, n - j);
+    float *Ajj = A + j + (long)j * lda;
+    ZG_TRY(potrf_launch<float>(kLower, jb, Ajj, lda, ctl, j, s));
+    const int rest = n - j - jb;
+    if (rest <= 0) break;
+    float *A21 = Ajj + jb;
+    ZG_TRY(trsm_dev<float>(kRight, kLower, kTrans, kNonUnit, rest, jb, 1.f, Ajj, lda, A21, lda, s));
+    const int ldk = ((jb + 7) / 8) * 8;
+    ZG_TRY(to_kmajor_t(prec, rest, jb, A21, lda, wl, ldk, s, false));
+    ZG_TRY(to_kmajor_t(prec, rest, jb, A21, lda, wu, ldk, s, true));
+    const long ldo = (long)ldk * segs;
+    ZG_TRY(gemm_tc(rest, rest, (int)ldo, -1.f, wl, ldo, wu, ldo, 1.f, A21 + (long)jb * lda, lda,
+                   prec == kPrecFP16 ? 0 : 1, &ctl->status, s, /*tri=*/1));
+  }
+  return 0;
+}
+
+// The strict lower triangle mirrored into the upper one (A(j,i) = A(i,j)),
+// through shared-memory tiles.
+template <typename T>
+__global__ void mirror_lower_kernel(int n, T *A, long lda) {
+  __shared__ T t[32][33];
+  const int bi = blockIdx.x, bj = blockIdx.y;  // source tile (rows bi, cols bj), bi >= bj
+  if (bi < bj) return;
+  const int i0 = bi * 32, j0 = bj * 32;
+  for (int c = threadIdx.y; c < 32; c += 8) {
+    const int i = i0 + threadIdx.x, j = j0 + c;
+    t[c][threadIdx.x] = (i < n && j < n) ? A[i + (long)j * lda] : T(0);
+  }
+  __syncthreads();
+  for (int c = threadIdx.y; c < 32; c += 8) {
+    const int i = j0 + threadIdx.x, j = i0 + c;  // destination (i, j) = source (j, i)
+    if (i < n && j < n && j > i) A[i + (long)j * lda] = t[threadIdx.x][c];
+  }
+}
+
+template <typename T> int mirror_lower(int n, T *A, long lda, cudaStream_t s) {
+  dim3 grid(ceil_div(n, 32), ceil_div(n, 32)), blk(32, 8);
+  ZG_LAUNCH(kTagConvert, 0, 1.0 * sizeof(T) * n * n, s,
+            mirror_lower_kernel<T><<<grid, blk, 0, s>>>(n, A, lda));
+  return 0;
+}
+
+// Full symmetric FP64 copy (ld n) of the `uplo` triangle of A.
+__global__ void sym_full_kernel(int n, const double *A, long lda, bool lower, double *S) {
+  const long total = (long)n * n;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total;
+       e += (long)gridDim.x * blockDim.x) {
+    const int i = e % n, j = e / n;
+    const bool in = lower ? i >= j : i <= j;
+    S[e] = in ? A[i + (long)j * lda] : A[j + (long)i * lda];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -333,7 +401,8 @@ __global__ void __launch_bounds__(kTT) trsv_lowp_kernel(int n, const float *__re
 // inversion in shared memory, one CTA per block.
 __global__ void __launch_bounds__(512) invert_diag_kernel(int n, const float *__restrict__ A,
                                                           long lda, double *Linv, double *Uinv,
-                                                          float *Linv32, float *Uinv32) {
+                                                          float *Linv32, float *Uinv32,
+                                                          bool lower_unit) {
   extern __shared__ double T[];  // T[i + j * kTB]
   const int blk = blockIdx.x, upper = blockIdx.y;
   const int r0 = blk * kTB, rows = min(kTB, n - r0);
@@ -343,7 +412,8 @@ __global__ void __launch_bounds__(512) invert_diag_kernel(int n, const float *__
     double v = 0;
     if (i < rows && j < rows) {
       if (upper) v = i <= j ? (double)A[(r0 + i) + (long)(r0 + j) * lda] : 0.0;
-      else v = i > j ? (double)A[(r0 + i) + (long)(r0 + j) * lda] : (i == j ? 1.0 : 0.0);
+      else if (lower_unit) v = i > j ? (double)A[(r0 + i) + (long)(r0 + j) * lda] : (i == j ? 1.0 : 0.0);
+      else v = i >= j ? (double)A[(r0 + i) + (long)(r0 + j) * lda] : 0.0;
     } else if (i == j) {
       v = 1.0;  // padding rows of the last block: identity
     }
@@ -364,15 +434,18 @@ __global__ void __launch_bounds__(512) invert_diag_kernel(int n, const float *__
       __syncthreads();
     }
   } else {
-    // columns right to left: T(j+1:, j) = -T(j+1:, j+1:) L(j+1:, j)
+    // columns right to left: T(j+1:, j) = -T(j+1:, j+1:) L(j+1:, j) / L(j, j),
+    // T(j, j) = 1 / L(j, j) (1 for the unit lower factor of LU)
     for (int j = kTB - 1; j >= 0; --j) {
+      const double djj = lower_unit ? 1.0 : 1.0 / T[j + j * kTB];
       double v = 0;
       const int i = j + 1 + tid;
       if (i < kTB) {
         for (int k = j + 1; k <= i; ++k) v = fma(T[i + k * kTB], T[k + j * kTB], v);
       }
       __syncthreads();
-      if (i < kTB) T[i + j * kTB] = -v;
+      if (i < kTB) T[i + j * kTB] = -v * djj;
+      if (tid == 0) T[j + j * kTB] = djj;
       __syncthreads();
     }
   }
@@ -385,7 +458,7 @@ __global__ void __launch_bounds__(512) invert_diag_kernel(int n, const float *__
 }
 
 int invert_diag_blocks(int n, const float *A, long lda, double *Linv, double *Uinv, float *Linv32,
-                       float *Uinv32, cudaStream_t s) {
+                       float *Uinv32, bool lower_unit, cudaStream_t s) {
   const int nblk = ceil_div(n, kTB);
   const size_t smem = sizeof(double) * kTB * kTB;
   static bool attr = false;
@@ -396,7 +469,7 @@ int invert_diag_blocks(int n, const float *A, long lda, double *Linv, double *Ui
   }
   ZG_LAUNCH(kTagTrsv, 2.0 * nblk * kTB * kTB * kTB / 3, 8.0 * nblk * kTB * kTB * 3, s,
             invert_diag_kernel<<<dim3(nblk, 2), 512, smem, s>>>(n, A, lda, Linv, Uinv, Linv32,
-                                                                Uinv32));
+                                                                Uinv32, lower_unit));
   return 0;
 }
 
@@ -653,12 +726,23 @@ static int gmres_correction(int n, const double *A, long lda, const LowLU &f, IR
   return 0;
 }
 
-int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, long ldb,
-                  double *X, long ldx, const MpirOpts &o, MpirResult *res, cudaStream_t s) {
+// spd: A symmetric positive definite, only its `lower` (else upper) triangle
+// is read; factored by the low-precision Cholesky.  Otherwise general, LU.
+static int solve_mpir_dev(bool spd, bool lower, int n, int nrhs, const double *A, long lda,
+                          const double *B, long ldb, double *X, long ldx, const MpirOpts &o,
+                          MpirResult *res, cudaStream_t s) {
   *res = MpirResult{};
   if (n <= 0 || nrhs <= 0) return 0;
   Control *ctl;
   ZG_TRY(control(s, &ctl));
+  if (spd) {  // the refinement works on the full symmetric FP64 matrix
+    void *ws;
+    ZG_TRY(workspace(s, kSlotSym, sizeof(double) * (size_t)n * n, &ws));
+    ZG_LAUNCH(kTagConvert, 0, 16.0 * n * n, s,
+              sym_full_kernel<<<grid1d((long)n * n), 256, 0, s>>>(n, A, lda, lower, (double *)ws));
+    A = (const double *)ws;
+    lda = n;
+  }
   const int m = std::max(1, std::min(o.gmres_restart, 200));
   // workspace: FP32 factor copy, ipiv, perm and FP64 vectors
   void *wf, *wv;
@@ -702,7 +786,10 @@ int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, l
   cudaEventCreate(&e1);
   cudaEventRecord(e0, s);
   ZG_TRY(d2s(n, n, A, lda, LU, n, s));
-  ZG_TRY(getrf_lowp(n, LU, n, ipiv, o.prec, ctl, s));
+  if (spd)
+    ZG_TRY(potrf_lowp(n, LU, n, o.prec, ctl, s));
+  else
+    ZG_TRY(getrf_lowp(n, LU, n, ipiv, o.prec, ctl, s));
   cudaEventRecord(e1, s);
   int info = 0;
   ZG_TRY(check_status(s, ctl, &info));
@@ -713,8 +800,17 @@ int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, l
   cudaEventDestroy(e1);
   res->info = info;
   if (info != 0) return 0;
-  ZG_TRY(perm_from_ipiv(n, ipiv, perm, s));
-  ZG_TRY(invert_diag_blocks(n, LU, n, Linv, Uinv, Linv32, Uinv32, s));
+  if (spd) {
+    // U = L^T into the free upper triangle; no interchanges
+    ZG_TRY(mirror_lower<float>(n, LU, n, s));
+    std::vector<int> id(n);
+    for (int i = 0; i < n; ++i) id[i] = i;
+    ZG_CUDA(cudaMemcpyAsync(perm, id.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    ZG_CUDA(cudaStreamSynchronize(s));
+  } else {
+    ZG_TRY(perm_from_ipiv(n, ipiv, perm, s));
+  }
+  ZG_TRY(invert_diag_blocks(n, LU, n, Linv, Uinv, Linv32, Uinv32, !spd, s));
 
   res->converged = 1;
   for (int q = 0; q < nrhs; ++q) {
@@ -765,6 +861,17 @@ int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, l
   }
   ZG_TRY(check_status(s, ctl, nullptr));
   return 0;
+}
+
+int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, long ldb,
+                  double *X, long ldx, const MpirOpts &o, MpirResult *res, cudaStream_t s) {
+  return solve_mpir_dev(false, false, n, nrhs, A, lda, B, ldb, X, ldx, o, res, s);
+}
+
+int posv_mpir_dev(bool lower, int n, int nrhs, const double *A, long lda, const double *B,
+                  long ldb, double *X, long ldx, const MpirOpts &o, MpirResult *res,
+                  cudaStream_t s) {
+  return solve_mpir_dev(true, lower, n, nrhs, A, lda, B, ldb, X, ldx, o, res, s);
 }
 
 }  // namespace zg
