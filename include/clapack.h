@@ -193,6 +193,71 @@ int zml_gpu_batched_schedule(int prec, int *warps, int *edges, int cap, int set)
  * and ms[i] (may be NULL) receive the result per class. */
 int zml_gpu_batched_autotune(int prec, int nrhs, int *chosen, double *ms, void *stream);
 
+/* ---- learned precision selector (no counterpart in the reference) ---------
+ * Structural features of an n x n FP64 matrix (device), 16 floats: [0] log2 n,
+ * [1] log10 scale, [2] row-scale spread, [3] column-scale spread, [4]-[5]
+ * diagonal dominance (worst, mean), [6] asymmetry, [7] entry spread, [8]
+ * diagonal spread, [9]-[11] norm ratios; [12]-[15] are left for the caller's
+ * refinement probe. */
+int zml_gpu_selector_features(int n, const double *dA, int ldda, float *dfeat, void *stream);
+/* MLP 16 -> 64 -> 64 -> 5 (ReLU), BF16 operands with FP32 accumulation,
+ * parameters packed W1[64x16] b1 W2[64x64] b2 W3[5x64] b3 (FP32 master). */
+int zml_gpu_mlp_num_params(void);
+long zml_gpu_mlp_work_floats(int batch);
+int zml_gpu_mlp_forward(int batch, const float *dX, const float *dP, float *dLogits, float *dWork,
+                        void *stream);
+/* Softmax cross-entropy gradients of the mean loss over the batch (dG), the
+ * per-sample losses (dLoss). */
+int zml_gpu_mlp_gradients(int batch, const float *dX, const int *dy, const float *dP, float *dG,
+                          float *dLoss, float *dWork, void *stream);
+int zml_gpu_mlp_adam(float *dP, const float *dG, float *dM, float *dV, float lr, float beta1,
+                     float beta2, float eps, int step, float weight_decay, void *stream);
+/* Floats of a selector model: the MLP parameters, then the means and the
+ * scales of the 16 input features (input k = (f_k - mean_k) / scale_k). */
+int zml_gpu_selector_model_floats(void);
+
+/* Precision classes of the ladder, cheapest first. */
+#define ZML_CLASS_BF16 0
+#define ZML_CLASS_FP16 1
+#define ZML_CLASS_BF16X3 2
+#define ZML_CLASS_FP32 3
+#define ZML_CLASS_FP64 4 /* plain FP64 LU (getrf.zig:14 + getrs.zig:13) */
+
+typedef struct zml_auto_result {
+  int info;          /* info of the returned attempt */
+  int predicted;     /* class chosen by the network, -1 if none was consulted */
+  int used;          /* class of the returned solution */
+  int attempts;      /* factorizations performed, the BF16 probe included */
+  int converged;     /* 1 if every column reached backward error <= 64 u */
+  int iters;         /* refinement steps of the returned attempt */
+  double berr;       /* its largest normwise backward error */
+  double ms;         /* wall time of the call */
+  float features[16]; /* the selector's input features: [0]-[11] as
+                         zml_gpu_selector_features; [12] log10 of the first
+                         BF16 backward error, [13]-[14] log10 of the next two
+                         step ratios, [15] 1 if the BF16 LU failed (0.5 if the
+                         solves moved to FP64 arithmetic) */
+  float proba[5];    /* predicted class probabilities */
+  int reserved;
+} zml_auto_result;
+
+/* A X = B (the problem of lapack/gesv.zig:13) to FP64 backward error by the
+ * precision ladder BF16 -> FP16 -> BF16x3 -> FP32 (GMRES-IR, at most
+ * max_iter steps each; 0 = 10) -> FP64 LU.  The BF16 attempt comes first and
+ * its first two refinement steps are the probe that completes the features;
+ * given a model (host memory, zml_gpu_selector_model_floats floats), the
+ * ladder then resumes at the smallest class whose cumulative predicted
+ * probability reaches `confidence` (0 < confidence <= 1) instead of the next
+ * rung.  The FP64 LU is the fallback of every path.  A and B are not
+ * modified.  Host or device pointers. */
+int zml_dgesv_auto(int matrix_layout, int n, int nrhs, const double *a, int lda, const double *b,
+                   int ldb, double *x, int ldx, const float *model, float confidence,
+                   int max_iter, zml_auto_result *res);
+/* Device-pointer, stream-ordered form of zml_dgesv_auto (column-major). */
+int zml_gpu_dgesv_auto(int n, int nrhs, const double *dA, int ldda, const double *dB, int lddb,
+                       double *dX, int lddx, const float *model, float confidence, int max_iter,
+                       zml_auto_result *res, void *stream);
+
 /* ---- instrumentation ------------------------------------------------------
  * Kernel classes: 0 tensor-core GEMM, 1 CUDA-core GEMM/SYRK, 2 LU panel,
  * 3 TRSM diagonal block, 4 row interchanges, 5 low-precision TRSV, 6 FP64

@@ -104,6 +104,32 @@ _SIGS.update({
     "zml_gpu_batched_autotune": (i32, [i32, i32, vp, vp, vp]),
 })
 
+_SIGS.update({
+    "zml_gpu_selector_features": (i32, [i32, vp, i32, vp, vp]),
+    "zml_gpu_mlp_num_params": (i32, []),
+    "zml_gpu_mlp_work_floats": (C.c_long, [i32]),
+    "zml_gpu_mlp_forward": (i32, [i32, vp, vp, vp, vp, vp]),
+    "zml_gpu_mlp_gradients": (i32, [i32, vp, vp, vp, vp, vp, vp, vp]),
+    "zml_gpu_mlp_adam": (i32, [vp, vp, vp, vp, f32, f32, f32, f32, i32, f32, vp]),
+    "zml_gpu_selector_model_floats": (i32, []),
+})
+
+
+class AutoResult(C.Structure):
+    """zml_auto_result of include/clapack.h."""
+    _fields_ = [("info", C.c_int), ("predicted", C.c_int), ("used", C.c_int),
+                ("attempts", C.c_int), ("converged", C.c_int), ("iters", C.c_int),
+                ("berr", C.c_double), ("ms", C.c_double),
+                ("features", C.c_float * 16), ("proba", C.c_float * 5), ("reserved", C.c_int)]
+
+
+_SIGS.update({
+    "zml_dgesv_auto": (i32, [i32, i32, i32, vp, i32, vp, i32, vp, i32, vp, f32, i32,
+                             C.POINTER(AutoResult)]),
+    "zml_gpu_dgesv_auto": (i32, [i32, i32, vp, i32, vp, i32, vp, i32, vp, f32, i32,
+                                 C.POINTER(AutoResult), vp]),
+})
+
 PREC_FP16, PREC_BF16, PREC_FP32, PREC_BF16X3 = 0, 1, 2, 3
 REFINE_IR, REFINE_GMRES = 0, 1
 

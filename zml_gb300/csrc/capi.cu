@@ -21,6 +21,7 @@
 #include "kernels.h"
 #include "kernels_batched.h"
 #include "kernels_mixed.h"
+#include "kernels_selector.h"
 #include "kernels_tc.h"
 
 using namespace zg;
@@ -431,6 +432,29 @@ int mpir_any(int layout, int n, int nrhs, const double *a, int lda, const double
   return sync(s);
 }
 
+int auto_any(int layout, int n, int nrhs, const double *a, int lda, const double *b, int ldb,
+             double *x, int ldx, const float *model, float confidence, int max_iter,
+             AutoResult *res) {
+  if (!lay_ok(layout)) return -1;
+  if (n < 0) return -2;
+  if (nrhs < 0) return -3;
+  if (lda < std::max(1, n)) return -5;
+  if (ldb < std::max(1, layout == kColMajor ? n : nrhs)) return -7;
+  if (ldx < std::max(1, layout == kColMajor ? n : nrhs)) return -9;
+  if (model && !(confidence > 0.f && confidence <= 1.f)) return -11;
+  *res = AutoResult{};
+  if (n == 0 || nrhs == 0) return 0;
+  cudaStream_t s = lib_stream();
+  ColMajor<double> A, B, X;
+  ZG_TRY(A.in(layout, a, lda, n, n, kSlotA, kSlotAT, true, s));
+  ZG_TRY(B.in(layout, b, ldb, n, nrhs, kSlotB, kSlotBT, true, s));
+  ZG_TRY(X.in(layout, x, ldx, n, nrhs, kSlotX, kSlotXT, false, s));
+  ZG_TRY(gesv_auto_dev(n, nrhs, A.d, A.ld, B.d, B.ld, X.d, X.ld, model, confidence, max_iter, res,
+                       s));
+  ZG_TRY(X.out(s));
+  return sync(s);
+}
+
 int posv_mpir_any(int layout, char uplo, int n, int nrhs, const double *a, int lda,
                   const double *b, int ldb, double *x, int ldx, const MpirOpts &o,
                   MpirResult *res) {
@@ -759,6 +783,54 @@ int zml_gpu_batched_autotune(int prec, int nrhs, int *chosen, double *ms, void *
   if (prec != 0 && prec != 1) return -1;
   if (nrhs < 1 || nrhs > 64) return -2;
   return batched_autotune(prec, nrhs, (cudaStream_t)stream, chosen, ms);
+}
+
+// ---- learned precision selector ----
+int zml_gpu_selector_features(int n, const double *dA, int ldda, float *dfeat, void *stream) {
+  if (n < 1) return -1;
+  if (ldda < n) return -3;
+  return selector_features(n, dA, ldda, dfeat, (cudaStream_t)stream);
+}
+int zml_gpu_mlp_num_params(void) { return selector_num_params(); }
+long zml_gpu_mlp_work_floats(int batch) { return (long)mlp_work_floats(batch); }
+int zml_gpu_mlp_forward(int batch, const float *dX, const float *dP, float *dLogits, float *dWork,
+                        void *stream) {
+  if (batch < 1) return -1;
+  return mlp_forward(batch, dX, dP, dLogits, dWork, (cudaStream_t)stream);
+}
+int zml_gpu_mlp_gradients(int batch, const float *dX, const int *dy, const float *dP, float *dG,
+                          float *dLoss, float *dWork, void *stream) {
+  if (batch < 1) return -1;
+  return mlp_gradients(batch, dX, dy, dP, dG, dLoss, dWork, (cudaStream_t)stream);
+}
+int zml_gpu_mlp_adam(float *dP, const float *dG, float *dM, float *dV, float lr, float beta1,
+                     float beta2, float eps, int step, float weight_decay, void *stream) {
+  if (step < 1) return -9;
+  return mlp_adam(dP, dG, dM, dV, lr, beta1, beta2, eps, step, weight_decay, (cudaStream_t)stream);
+}
+int zml_gpu_selector_model_floats(void) { return selector_num_params() + 2 * kSelFeatures; }
+
+// Solve with the precision ladder, started where the selector network
+// predicts (model != NULL) or at the bottom (model == NULL).
+int zml_dgesv_auto(int layout, int n, int nrhs, const double *a, int lda, const double *b, int ldb,
+                   double *x, int ldx, const float *model, float confidence, int max_iter,
+                   AutoResult *res) {
+  AutoResult local;
+  return auto_any(layout, n, nrhs, a, lda, b, ldb, x, ldx, model, confidence, max_iter,
+                  res ? res : &local);
+}
+int zml_gpu_dgesv_auto(int n, int nrhs, const double *dA, int ldda, const double *dB, int lddb,
+                       double *dX, int lddx, const float *model, float confidence, int max_iter,
+                       AutoResult *res, void *stream) {
+  if (n < 0) return -1;
+  if (nrhs < 0) return -2;
+  if (ldda < std::max(1, n)) return -4;
+  if (lddb < std::max(1, n)) return -6;
+  if (lddx < std::max(1, n)) return -8;
+  if (model && !(confidence > 0.f && confidence <= 1.f)) return -10;
+  AutoResult local;
+  return gesv_auto_dev(n, nrhs, dA, ldda, dB, lddb, dX, lddx, model, confidence, max_iter,
+                       res ? res : &local, (cudaStream_t)stream);
 }
 
 const char *zml_gpu_last_error(void) { return last_error(); }

@@ -93,6 +93,9 @@ enum Slot : int {
   kSlotSwap = 14,             // composed row-interchange pairs
   kSlotQR = 15,               // QR: V, T, W, split-K partials, panel exchange
   kSlotSym = 16,              // full symmetric FP64 copy for the mixed Cholesky solve
+  kSlotSel = 17,              // selector feature statistics
+  kSlotSelNet = 18,           // selector network parameters, input, logits, work
+  kSlotF64LU = 19,            // FP64 LU copy and pivots of the selector's last resort
   kNumSlots = 20
 };
 

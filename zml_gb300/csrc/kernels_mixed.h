@@ -46,4 +46,40 @@ int posv_mpir_dev(bool lower, int n, int nrhs, const double *A, long lda, const 
                   cudaStream_t s);
 int potrf_lowp(int n, float *A, long lda, int prec, Control *ctl, cudaStream_t s);
 
+// ---- precision selection -------------------------------------------------
+// Classes of the precision ladder, cheapest first; the last is the plain FP64
+// LU.  kClassPrec maps a refined class to its factor precision.
+enum : int { kClassBF16 = 0, kClassFP16 = 1, kClassBF16x3 = 2, kClassFP32 = 3, kClassFP64 = 4,
+             kNumClasses = 5 };
+constexpr int kClassPrec[4] = {kPrecBF16, kPrecFP16, kPrecBF16x3, kPrecFP32};
+constexpr int kSelFeatures = 16;
+
+struct AutoResult {
+  int info = 0;        // info of the returned attempt (FP64 getrf info for class 4)
+  int predicted = -1;  // class the network chose (-1: none consulted)
+  int used = -1;       // class of the returned solution
+  int attempts = 0;    // factorizations performed, the probe included
+  int converged = 0;   // backward error of every column <= 64 u
+  int iters = 0;       // refinement steps of the returned attempt
+  double berr = 0;     // its normwise backward error (max over columns)
+  double ms = 0;       // wall time of the call
+  float features[kSelFeatures] = {0};
+  float proba[kNumClasses] = {0};
+  int reserved = 0;
+};
+
+// A X = B (general A) to FP64 backward error by the ladder BF16 -> FP16 ->
+// BF16x3 -> FP32 (GMRES-IR, at most max_iter steps each) -> FP64 LU.  The
+// first attempt (BF16 factors) doubles as the probe: its first two
+// refinement steps give features 12..15, and it continues from there when it
+// is the class to try.  model (host, may be null): the selector network,
+// mlp parameters followed by the 16 feature means and 16 scales; with it the
+// ladder starts at the smallest class whose cumulative predicted probability
+// reaches `confidence`; without it the ladder is walked from the bottom.
+int gesv_auto_dev(int n, int nrhs, const double *A, long lda, const double *B, long ldb, double *X,
+                  long ldx, const float *model, float confidence, int max_iter, AutoResult *r,
+                  cudaStream_t s);
+// Features 12..15 from the probe's refinement record.
+void probe_features(const MpirResult &pr, float *f);
+
 }  // namespace zg

@@ -11,12 +11,15 @@
 // (restarted GMRES on the left-preconditioned system (LU)^-1 A d = (LU)^-1 r).
 // The residual r = b - A x, the update and the GMRES orthogonalisation are
 // FP64; the preconditioner applies the FP32 factors with FP64 accumulation.
+#include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <vector>
 
 #include "common.cuh"
 #include "kernels.h"
 #include "kernels_mixed.h"
+#include "kernels_selector.h"
 #include "kernels_tc.h"
 
 namespace zg {
@@ -726,13 +729,25 @@ static int gmres_correction(int n, const double *A, long lda, const LowLU &f, IR
   return 0;
 }
 
-// spd: A symmetric positive definite, only its `lower` (else upper) triangle
-// is read; factored by the low-precision Cholesky.  Otherwise general, LU.
-static int solve_mpir_dev(bool spd, bool lower, int n, int nrhs, const double *A, long lda,
-                          const double *B, long ldb, double *X, long ldx, const MpirOpts &o,
-                          MpirResult *res, cudaStream_t s) {
+// State of one low-precision factorization, shared by the refinement calls
+// that use it (the workspace slots stay valid until the next factorization on
+// the stream).
+struct MpirCtx {
+  int n = 0, m = 1;
+  const double *A = nullptr;  // FP64 matrix of the residuals (full, column-major)
+  long lda = 0;
+  double anrm = 0;            // ||A||_inf
+  Control *ctl = nullptr;
+  LowLU f{};
+  IRWork w{};
+};
+
+// Factor phase.  spd: A symmetric positive definite, only its `lower` (else
+// upper) triangle is read; factored by the low-precision Cholesky.
+// Otherwise general, LU.  res->info receives the factorization's info.
+static int mpir_factor(bool spd, bool lower, int n, const double *A, long lda, const MpirOpts &o,
+                       MpirCtx *c, MpirResult *res, cudaStream_t s) {
   *res = MpirResult{};
-  if (n <= 0 || nrhs <= 0) return 0;
   Control *ctl;
   ZG_TRY(control(s, &ctl));
   if (spd) {  // the refinement works on the full symmetric FP64 matrix
@@ -811,7 +826,29 @@ static int solve_mpir_dev(bool spd, bool lower, int n, int nrhs, const double *A
     ZG_TRY(perm_from_ipiv(n, ipiv, perm, s));
   }
   ZG_TRY(invert_diag_blocks(n, LU, n, Linv, Uinv, Linv32, Uinv32, !spd, s));
+  c->n = n;
+  c->m = m;
+  c->A = A;
+  c->lda = lda;
+  c->anrm = anrm;
+  c->ctl = ctl;
+  c->f = f;
+  c->w = w;
+  return 0;
+}
 
+// Refinement phase on the factors of c.  warm: X already holds an iterate
+// (a previous refinement call's result) and refinement continues from it;
+// otherwise it starts from x0 = (LU)^-1 P b.  Fills res's iteration fields.
+static int mpir_refine(MpirCtx &c, const MpirOpts &o, int nrhs, const double *B, long ldb,
+                       double *X, long ldx, bool warm, MpirResult *res, cudaStream_t s) {
+  const int n = c.n, m = c.m;
+  const double *A = c.A;
+  const long lda = c.lda;
+  const double anrm = c.anrm;
+  Control *ctl = c.ctl;
+  LowLU &f = c.f;
+  IRWork &w = c.w;
   res->converged = 1;
   for (int q = 0; q < nrhs; ++q) {
     const double *b = B + (long)q * ldb;
@@ -820,7 +857,7 @@ static int solve_mpir_dev(bool spd, bool lower, int n, int nrhs, const double *A
     double bnrm;
     ZG_TRY(host_scalar(w.scal, &bnrm, s));
     // x0 = (LU)^-1 P b
-    ZG_TRY(lu_apply(n, f, b, x, w.tw, &ctl->status, s));
+    if (!warm) ZG_TRY(lu_apply(n, f, b, x, w.tw, &ctl->status, s));
     double berr = 0, prev = INFINITY;
     ZG_TRY(berr_of(n, A, lda, b, x, anrm, bnrm, w, &berr, s));  // leaves r = b - A x
     if (q == 0) res->berr_history[0] = berr;
@@ -863,6 +900,17 @@ static int solve_mpir_dev(bool spd, bool lower, int n, int nrhs, const double *A
   return 0;
 }
 
+static int solve_mpir_dev(bool spd, bool lower, int n, int nrhs, const double *A, long lda,
+                          const double *B, long ldb, double *X, long ldx, const MpirOpts &o,
+                          MpirResult *res, cudaStream_t s) {
+  *res = MpirResult{};
+  if (n <= 0 || nrhs <= 0) return 0;
+  MpirCtx c;
+  ZG_TRY(mpir_factor(spd, lower, n, A, lda, o, &c, res, s));
+  if (res->info != 0) return 0;
+  return mpir_refine(c, o, nrhs, B, ldb, X, ldx, false, res, s);
+}
+
 int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, long ldb,
                   double *X, long ldx, const MpirOpts &o, MpirResult *res, cudaStream_t s) {
   return solve_mpir_dev(false, false, n, nrhs, A, lda, B, ldb, X, ldx, o, res, s);
@@ -872,6 +920,186 @@ int posv_mpir_dev(bool lower, int n, int nrhs, const double *A, long lda, const 
                   long ldb, double *X, long ldx, const MpirOpts &o, MpirResult *res,
                   cudaStream_t s) {
   return solve_mpir_dev(true, lower, n, nrhs, A, lda, B, ldb, X, ldx, o, res, s);
+}
+
+// ---------------------------------------------------------------------------
+// Precision selection.
+
+// The last resort: plain FP64 partial-pivot LU and solve (the reference's
+// gesv, getrf.zig:14 + getrs.zig:13) on a copy of A, with the backward error
+// of each column.
+static int fp64_solve(int n, int nrhs, const double *A, long lda, const double *B, long ldb,
+                      double *X, long ldx, double *berr, int *info, cudaStream_t s) {
+  const int nparts = ceil_div(n, kGemvCols);
+  const size_t nd = (size_t)n * n + (size_t)n * (1 + nparts) + 8;
+  void *wp;
+  ZG_TRY(workspace(s, kSlotF64LU, sizeof(double) * nd + sizeof(int) * (size_t)n + 256, &wp));
+  double *LU = (double *)wp;
+  IRWork w{};
+  w.r = LU + (size_t)n * n;
+  w.part = w.r + n;
+  w.scal = w.part + (size_t)n * nparts;
+  int *piv = (int *)(w.scal + 8);
+  ZG_CUDA(cudaMemcpy2DAsync(LU, sizeof(double) * n, A, sizeof(double) * lda, sizeof(double) * n,
+                            n, cudaMemcpyDeviceToDevice, s));
+  *berr = INFINITY;
+  ZG_TRY(getrf_dev<double>(n, n, LU, n, piv, info, s));
+  if (*info != 0) return 0;
+  ZG_CUDA(cudaMemcpy2DAsync(X, sizeof(double) * ldx, B, sizeof(double) * ldb, sizeof(double) * n,
+                            nrhs, cudaMemcpyDeviceToDevice, s));
+  ZG_TRY(getrs_dev<double>(kNoTrans, n, nrhs, LU, n, piv, X, ldx, s));
+  ZG_LAUNCH(kTagGemv, 0, 0, s, rowabs_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, A, lda, w.r));
+  ZG_LAUNCH(kTagVector, 0, 0, s, absmax_kernel<<<1, 256, 0, s>>>(n, w.r, w.scal));
+  double anrm;
+  ZG_TRY(host_scalar(w.scal, &anrm, s));
+  *berr = 0;
+  for (int q = 0; q < nrhs; ++q) {
+    const double *b = B + (long)q * ldb;
+    ZG_LAUNCH(kTagVector, 0, 0, s, absmax_kernel<<<1, 256, 0, s>>>(n, b, w.scal));
+    double bnrm, e;
+    ZG_TRY(host_scalar(w.scal, &bnrm, s));
+    ZG_TRY(berr_of(n, A, lda, b, X + (long)q * ldx, anrm, bnrm, w, &e, s));
+    *berr = std::isfinite(e) ? std::max(*berr, e) : INFINITY;
+  }
+  return 0;
+}
+
+void probe_features(const MpirResult &pr, float *f) {
+  // log10 of a backward error, clamped to [1e-18, 1e2] (non-finite: 1e2)
+  auto lg = [](double v) {
+    if (!std::isfinite(v)) v = 1e2;
+    return (float)std::log10(std::min(1e2, std::max(v, 1e-18)));
+  };
+  if (pr.info != 0) {
+    f[12] = f[13] = f[14] = 0.f;
+    f[15] = 1.f;
+    return;
+  }
+  const double h0 = pr.berr_history[0];
+  const double h1 = pr.iters >= 1 ? pr.berr_history[1] : h0;
+  const double h2 = pr.iters >= 2 ? pr.berr_history[2] : h1;
+  f[12] = lg(h0);
+  f[13] = lg(h1) - lg(h0);
+  f[14] = lg(h2) - lg(h1);
+  f[15] = pr.switched_f64 ? 0.5f : 0.f;
+}
+
+int gesv_auto_dev(int n, int nrhs, const double *A, long lda, const double *B, long ldb, double *X,
+                  long ldx, const float *model, float confidence, int max_iter, AutoResult *r,
+                  cudaStream_t s) {
+  *r = AutoResult{};
+  const auto t0 = std::chrono::steady_clock::now();
+  auto finish = [&]() -> int {
+    ZG_CUDA(cudaStreamSynchronize(s));
+    r->ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return 0;
+  };
+  if (n <= 0 || nrhs <= 0) {
+    r->used = kClassBF16;
+    r->converged = 1;
+    return finish();
+  }
+  if (max_iter <= 0) max_iter = 10;
+  const int probe_steps = std::min(2, max_iter);
+  const int np = selector_num_params();
+  void *wn;
+  const size_t nnet = (size_t)np + kSelFeatures + 8 + mlp_work_floats(1) + 64;
+  ZG_TRY(workspace(s, kSlotSelNet, sizeof(float) * nnet, &wn));
+  float *dP = (float *)wn, *dx = dP + np, *dz = dx + kSelFeatures, *dwork = dz + 8;
+
+  // structural features, then the probe: BF16 factors and their first
+  // refinement steps
+  float feat[kSelFeatures];
+  ZG_TRY(selector_features(n, A, lda, dx, s));
+  ZG_CUDA(cudaMemcpyAsync(feat, dx, sizeof feat, cudaMemcpyDeviceToHost, s));
+  MpirOpts o;
+  o.prec = kPrecBF16;
+  o.mode = kModeGMRES;
+  o.max_iter = probe_steps;
+  MpirCtx c;
+  MpirResult pr;
+  ZG_TRY(mpir_factor(false, false, n, A, lda, o, &c, &pr, s));
+  r->attempts = 1;
+  if (pr.info == 0) ZG_TRY(mpir_refine(c, o, nrhs, B, ldb, X, ldx, false, &pr, s));
+  ZG_CUDA(cudaStreamSynchronize(s));
+  probe_features(pr, feat);
+  std::copy(feat, feat + kSelFeatures, r->features);
+  if (pr.info == 0 && pr.converged) {
+    r->used = kClassBF16;
+    r->converged = 1;
+    r->iters = pr.iters;
+    r->berr = pr.berr;
+    return finish();
+  }
+
+  int start = kClassBF16;
+  if (model) {
+    const float *mu = model + np, *sd = mu + kSelFeatures;
+    float xin[kSelFeatures], z[kNumClasses];
+    for (int k = 0; k < kSelFeatures; ++k) xin[k] = (feat[k] - mu[k]) / sd[k];
+    ZG_CUDA(cudaMemcpyAsync(dP, model, sizeof(float) * np, cudaMemcpyHostToDevice, s));
+    ZG_CUDA(cudaMemcpyAsync(dx, xin, sizeof xin, cudaMemcpyHostToDevice, s));
+    ZG_TRY(mlp_forward(1, dx, dP, dz, dwork, s));
+    ZG_CUDA(cudaGetLastError());
+    ZG_CUDA(cudaMemcpyAsync(z, dz, sizeof z, cudaMemcpyDeviceToHost, s));
+    ZG_CUDA(cudaStreamSynchronize(s));
+    double zmax = z[0], den = 0, cum = 0;
+    for (int k = 1; k < kNumClasses; ++k) zmax = std::max(zmax, (double)z[k]);
+    for (int k = 0; k < kNumClasses; ++k) den += std::exp(z[k] - zmax);
+    start = kClassFP64;
+    for (int k = 0; k < kNumClasses; ++k) {
+      r->proba[k] = (float)(std::exp(z[k] - zmax) / den);
+      cum += r->proba[k];
+      if (cum >= confidence && start == kClassFP64) start = k;
+    }
+    r->predicted = start;
+  }
+
+  for (int cls = start; cls < kNumClasses; ++cls) {
+    if (cls == kClassBF16) {
+      // continue the probe's refinement from its iterate (it stopped early
+      // only when it stagnated, and then BF16 has failed)
+      if (pr.info != 0 || pr.iters < probe_steps || max_iter <= pr.iters) continue;
+      MpirOpts oc = o;
+      oc.max_iter = max_iter - pr.iters;
+      MpirResult cr;
+      ZG_TRY(mpir_refine(c, oc, nrhs, B, ldb, X, ldx, true, &cr, s));
+      if (cr.converged) {
+        r->used = kClassBF16;
+        r->converged = 1;
+        r->iters = pr.iters + cr.iters;
+        r->berr = cr.berr;
+        return finish();
+      }
+      continue;
+    }
+    if (cls == kClassFP64) {
+      int info = 0;
+      double berr = INFINITY;
+      ZG_TRY(fp64_solve(n, nrhs, A, lda, B, ldb, X, ldx, &berr, &info, s));
+      ++r->attempts;
+      r->used = kClassFP64;
+      r->info = info;
+      r->berr = berr;
+      r->converged = info == 0 && berr <= 64 * 1.1102230246251565e-16;
+      return finish();
+    }
+    MpirOpts oc;
+    oc.prec = kClassPrec[cls];
+    oc.mode = kModeGMRES;
+    oc.max_iter = max_iter;
+    MpirResult cr;
+    ZG_TRY(solve_mpir_dev(false, false, n, nrhs, A, lda, B, ldb, X, ldx, oc, &cr, s));
+    ++r->attempts;
+    if (cr.info == 0 && cr.converged) {
+      r->used = cls;
+      r->converged = 1;
+      r->iters = cr.iters;
+      r->berr = cr.berr;
+      return finish();
+    }
+  }
+  return finish();
 }
 
 }  // namespace zg
