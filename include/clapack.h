@@ -65,6 +65,13 @@ int LAPACKE_sposv(int matrix_layout, char uplo, int n, int nrhs, float *a, int l
  * R in the upper triangle, the Householder vectors below it, tau[min(m,n)] */
 int LAPACKE_dgeqrf(int matrix_layout, int m, int n, double *a, int lda, double *tau);
 int LAPACKE_sgeqrf(int matrix_layout, int m, int n, float *a, int lda, float *tau);
+/* replaces zml.linalg.lapack.orgqr (lapack.zig:5279 calls LAPACKE_dorgqr;
+ * kernel lapack/orgqr.zig:18 with org2r.zig:18):
+ * a (m x n, n <= m) <- the first n columns of Q = H(1) ... H(k) from the k
+ * reflectors geqrf left below the diagonal of a, k <= n.  Used by the
+ * reference's QR.q (qr.zig:44-156). */
+int LAPACKE_dorgqr(int matrix_layout, int m, int n, int k, double *a, int lda, const double *tau);
+int LAPACKE_sorgqr(int matrix_layout, int m, int n, int k, float *a, int lda, const float *tau);
 /* replaces zml.linalg.lapack.laswp (kernel lapack/laswp.zig:12): row
  * interchanges k1..k2 (1-based) of n columns, |incx| = 1 */
 int LAPACKE_dlaswp(int matrix_layout, int n, double *a, int lda, int k1, int k2, const int *ipiv,
@@ -101,6 +108,8 @@ int zml_gpu_dpotrs(char uplo, int n, int nrhs, const double *dA, int ldda, doubl
                    void *stream);
 /* device-pointer form of geqrf (lapack/geqrf.zig:18) */
 int zml_gpu_dgeqrf(int m, int n, double *dA, int ldda, double *dtau, void *stream);
+/* device-pointer form of orgqr (lapack/orgqr.zig:18) */
+int zml_gpu_dorgqr(int m, int n, int k, double *dA, int ldda, const double *dtau, void *stream);
 /* device-pointer form of gemm (blas/gemm.zig:14), CBLAS transpose codes */
 int zml_gpu_dgemm(int transa, int transb, int m, int n, int k, double alpha, const double *dA,
                   int ldda, const double *dB, int lddb, double beta, double *dC, int lddc,

@@ -488,5 +488,86 @@ int P(geqrf)(int order, int m, int n, T *a, int lda, T *tau, T *work, int lwork)
   return 0;
 }
 
+/* lapack/org2r.zig:18-102: the first n columns of Q = H(0) H(1) ... H(k-1)
+ * from the reflectors stored below the diagonal of a (geqrf's output),
+ * unblocked, the reflectors applied last to first. */
+int P(org2r)(int order, int m, int n, int k, T *a, int lda, const T *tau, T *work) {
+  if (m < 0 || n < 0 || n > m || k < 0 || k > n || lda < ZO_MAX(1, order == ZO_COL ? m : n))
+    return ZO_EINVAL;
+  if (n == 0) return 0;
+  for (int j = k; j < n; ++j) { /* columns k..n-1 start as unit vectors */
+    for (int l = 0; l < m; ++l) a[P(idx)(order, l, j, lda)] = (T)0;
+    a[P(idx)(order, j, j, lda)] = (T)1;
+  }
+  for (int i = k - 1; i >= 0; --i) {
+    if (i < n - 1)
+      P(larf1f)(order, ZO_LEFT, m - i, n - i - 1, a + P(idx)(order, i, i, lda),
+                P(col_ld)(order, lda), tau[i], a + P(idx)(order, i, i + 1, lda), lda, work);
+    if (i < m - 1)
+      P(scal)(m - i - 1, -tau[i], a + P(idx)(order, i + 1, i, lda), P(col_ld)(order, lda));
+    a[P(idx)(order, i, i, lda)] = (T)1 - tau[i];
+    for (int l = 0; l < i; ++l) a[P(idx)(order, l, i, lda)] = (T)0;
+  }
+  return 0;
+}
+
+/* lapack/orgqr.zig:18-194: blocked form, nb = 32, nx = 128; the last
+ * (k - kk) reflectors by org2r, then each nb-block by larft + larfb on the
+ * columns to its right and org2r on its own columns.  lwork == -1 stores
+ * n*nb in work[0]. */
+int P(orgqr)(int order, int m, int n, int k, T *a, int lda, const T *tau, T *work, int lwork) {
+  if (m < 0 || n < 0 || n > m || k < 0 || k > n || lda < ZO_MAX(1, order == ZO_COL ? m : n) ||
+      (lwork < ZO_MAX(1, n) && lwork != -1))
+    return ZO_EINVAL;
+  int nb = zo_ilaenv(1, "DORGQR", m, n, k, -1);
+  if (lwork == -1) {
+    work[0] = (T)(ZO_MAX(1, n) * nb);
+    return 0;
+  }
+  if (n == 0) {
+    work[0] = 1;
+    return 0;
+  }
+  int nbmin = 2, nx = 0, iws = n, ldwork = 0;
+  if (nb > 1 && nb < k) {
+    nx = ZO_MAX(0, zo_ilaenv(3, "DORGQR", m, n, k, -1));
+    if (nx < k) {
+      ldwork = order == ZO_COL ? n : nb;
+      iws = ldwork * nb;
+      if (lwork < iws) {
+        nb = lwork / ldwork;
+        nbmin = ZO_MAX(2, zo_ilaenv(2, "DORGQR", m, n, k, -1));
+      }
+    }
+  }
+  int ki = 0, kk = 0;
+  if (nb >= nbmin && nb < k && nx < k) {
+    ki = ((k - nx - 1) / nb) * nb;
+    kk = ZO_MIN(k, ki + nb);
+    for (int j = kk; j < n; ++j)
+      for (int i = 0; i < kk; ++i) a[P(idx)(order, i, j, lda)] = (T)0;
+  }
+  if (kk < n)
+    P(org2r)(order, m - kk, n - kk, k - kk, a + P(idx)(order, kk, kk, lda), lda, tau + kk, work);
+  if (kk > 0) {
+    for (int i = ki; i >= 0; i -= nb) {
+      const int ib = ZO_MIN(k - i, nb);
+      if (i + ib < n) {
+        P(larft)(order, 'F', 'C', m - i, ib, a + P(idx)(order, i, i, lda), lda, tau + i, work,
+                 ldwork);
+        P(larfb)(order, ZO_LEFT, ZO_NOTRANS, 'F', 'C', m - i, n - i - ib, ib,
+                 a + P(idx)(order, i, i, lda), lda, work, ldwork,
+                 a + P(idx)(order, i, i + ib, lda), lda, work + P(idx)(order, ib, 0, ldwork),
+                 ldwork);
+      }
+      P(org2r)(order, m - i, ib, ib, a + P(idx)(order, i, i, lda), lda, tau + i, work);
+      for (int j = i; j < i + ib; ++j)
+        for (int l = 0; l < i; ++l) a[P(idx)(order, l, j, lda)] = (T)0;
+    }
+  }
+  work[0] = (T)iws;
+  return 0;
+}
+
 #undef A_
 #undef B_

@@ -49,13 +49,13 @@ int zo_ilaenv(int ispec, const char *name, int n1, int n2, int n3, int n4) {
     if (!strncmp(c2, "GE", 2) && !strncmp(c3, "TRF", 3)) return 64;
     if (!strncmp(c2, "PO", 2) && !strncmp(c3, "TRF", 3)) return 64;
     if (!strncmp(c2, "GE", 2) && !strncmp(c3, "QRF", 3)) return 32;
-    if (!strncmp(c2, "OR", 2) && !strncmp(c3 - 1, "GQR", 3)) return 32;
+    if (!strncmp(c2, "OR", 2) && !strncmp(c3, "GQR", 3)) return 32;
     return 1;
   }
   if (ispec == 2) return 2;
   if (ispec == 3) {
     if (!strncmp(c2, "GE", 2) && !strncmp(c3, "QRF", 3)) return 128;
-    if (!strncmp(c2, "OR", 2) && !strncmp(c3 - 1, "GQR", 3)) return 128;
+    if (!strncmp(c2, "OR", 2) && !strncmp(c3, "GQR", 3)) return 128;
     return 0;
   }
   return -1;

@@ -72,7 +72,10 @@ void zo_set_trsm_as_written(int on);
                const T *tau, T *t, int ldt);                                                  \
   int P##larfb(int order, int side, int trans, int direct, int storev, int m, int n, int k,   \
                const T *v, int ldv, const T *t, int ldt, T *c, int ldc, T *work, int ldwork); \
-  int P##geqrf(int order, int m, int n, T *a, int lda, T *tau, T *work, int lwork);
+  int P##geqrf(int order, int m, int n, T *a, int lda, T *tau, T *work, int lwork); \
+  int P##org2r(int order, int m, int n, int k, T *a, int lda, const T *tau, T *work);        \
+  int P##orgqr(int order, int m, int n, int k, T *a, int lda, const T *tau, T *work,          \
+               int lwork);
 
 ZO_DECL(double, zo_d_)
 ZO_DECL(float, zo_s_)

@@ -47,6 +47,8 @@ def load():
                 "posv": (i32, [i32, i32, i32, i32, vp, i32, vp, i32]),
                 "geqr2": (i32, [i32, i32, i32, vp, i32, vp, vp]),
                 "geqrf": (i32, [i32, i32, i32, vp, i32, vp, vp, i32]),
+                "orgqr": (i32, [i32, i32, i32, i32, vp, i32, vp, vp, i32]),
+                "org2r": (i32, [i32, i32, i32, i32, vp, i32, vp, vp]),
                 "larft": (i32, [i32, i32, i32, i32, i32, vp, i32, vp, vp, i32]),
                 "larfg": (i32, [i32, vp, vp, i32, vp]),
             }
@@ -118,3 +120,19 @@ def geqrf(a):
     r = f(102, m, n, ptr(a), max(1, m), ptr(tau), ptr(work), lwork)
     assert r == 0
     return a, tau
+
+
+def orgqr(qr, tau, ncols=None):
+    """The first ncols columns of Q from geqrf's output (qr, tau)."""
+    m, n = qr.shape
+    k = min(m, n)
+    ncols = k if ncols is None else ncols
+    q = np.zeros((m, ncols), dtype=qr.dtype, order="F")
+    q[:, :min(n, ncols)] = qr[:, :min(n, ncols)]
+    f = fn("orgqr", qr.dtype)
+    w = np.zeros(1, dtype=qr.dtype)
+    assert f(102, m, ncols, k, ptr(q), max(1, m), ptr(tau), ptr(w), -1) == 0
+    lwork = max(1, int(w[0]))
+    work = np.zeros(lwork, dtype=qr.dtype)
+    assert f(102, m, ncols, k, ptr(q), max(1, m), ptr(tau), ptr(work), lwork) == 0
+    return q

@@ -111,3 +111,29 @@ def test_geqrf_against_scipy(m, n):
     q = lap.dorgqr(qr[:, : min(m, n)].copy(order="F"), tau[: min(m, n)])[0]
     err = np.linalg.norm(q @ np.triu(qr[: min(m, n)]) - a) / (np.linalg.norm(a) * m * EPS)
     assert err < 10
+
+
+@pytest.mark.parametrize("m,n,full", [(10, 10, False), (300, 200, False), (300, 200, True),
+                                      (513, 260, False), (160, 160, False), (200, 64, True)])
+def test_orgqr_against_scipy(m, n, full):
+    """orgqr.zig/org2r.zig restatement: the explicit Q of geqrf's reflectors
+    equals LAPACK's dorgqr and Q R reproduces A."""
+    a = gaussian(m, n, seed=m + n)
+    qr, tau = ol.geqrf(a)
+    k = min(m, n)
+    ncols = m if full else k
+    q = ol.orgqr(qr, tau[:k], ncols)
+    src = np.zeros((m, ncols), order="F")
+    src[:, :k] = qr[:, :k]
+    q2 = lap.dorgqr(src, tau[:k], lwork=max(1, ncols) * 64)[0]
+    np.testing.assert_allclose(q, q2, rtol=1e-9, atol=1e-12)
+    assert np.linalg.norm(q.T @ q - np.eye(ncols)) < 50 * m * EPS
+    err = np.linalg.norm(q[:, :k] @ np.triu(qr[:k]) - a) / (np.linalg.norm(a) * m * EPS)
+    assert err < 10
+
+
+def test_ilaenv_orgqr_block_sizes():
+    lib = ol.load()
+    assert lib.zo_ilaenv(1, b"DORGQR", 100, 100, 100, -1) == 32
+    assert lib.zo_ilaenv(2, b"DORGQR", 100, 100, 100, -1) == 2
+    assert lib.zo_ilaenv(3, b"DORGQR", 100, 100, 100, -1) == 128

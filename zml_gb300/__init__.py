@@ -37,11 +37,13 @@ for p, T in (("d", f64), ("s", f32)):
         "LAPACKE_%sposv" % p: (i32, [i32, ch, i32, i32, vp, i32, vp, i32]),
         "LAPACKE_%slaswp" % p: (i32, [i32, i32, vp, i32, i32, i32, vp, i32]),
         "LAPACKE_%sgeqrf" % p: (i32, [i32, i32, i32, vp, i32, vp]),
+        "LAPACKE_%sorgqr" % p: (i32, [i32, i32, i32, i32, vp, i32, vp]),
     })
 _SIGS.update({
     "zml_gpu_dgetrf": (i32, [i32, i32, vp, i32, vp, vp, vp]),
     "zml_gpu_dgetrs": (i32, [ch, i32, i32, vp, i32, vp, vp, i32, vp]),
     "zml_gpu_dgetrf_noalloc": (i32, [i32, i32, vp, i32, vp, vp, vp]),
+    "zml_gpu_dorgqr": (i32, [i32, i32, i32, vp, i32, vp, vp]),
     "zml_gpu_dgeqrf": (i32, [i32, i32, vp, i32, vp, vp]),
     "zml_gpu_dpotrf": (i32, [ch, i32, vp, i32, vp, vp]),
     "zml_gpu_dpotrs": (i32, [ch, i32, i32, vp, i32, vp, i32, vp]),
@@ -128,6 +130,49 @@ _SIGS.update({
                              C.POINTER(AutoResult)]),
     "zml_gpu_dgesv_auto": (i32, [i32, i32, vp, i32, vp, i32, vp, i32, vp, f32, i32,
                                  C.POINTER(AutoResult), vp]),
+})
+
+class DMatrix(C.Structure):
+    """zml_dmatrix of include/zml_linalg.h."""
+    _fields_ = [("data", C.POINTER(C.c_double)), ("rows", C.c_int), ("cols", C.c_int),
+                ("ld", C.c_int), ("layout", C.c_int), ("uplo", C.c_int), ("diag", C.c_int),
+                ("owns_data", C.c_int)]
+
+    def to_numpy(self):
+        """A copy of the (rows x cols) matrix the view describes."""
+        import numpy as np
+        if self.rows == 0 or self.cols == 0:
+            return np.zeros((self.rows, self.cols))
+        if self.layout == COL_MAJOR:
+            flat = np.ctypeslib.as_array(self.data, shape=(self.ld * (self.cols - 1) + self.rows,))
+            idx = np.arange(self.rows)[:, None] + self.ld * np.arange(self.cols)[None, :]
+        else:
+            flat = np.ctypeslib.as_array(self.data, shape=(self.ld * (self.rows - 1) + self.cols,))
+            idx = self.ld * np.arange(self.rows)[:, None] + np.arange(self.cols)[None, :]
+        return flat[idx].copy()
+
+
+ERR_INVALID_ARGUMENT, ERR_SINGULAR_MATRIX, ERR_OUT_OF_MEMORY = -2000, -2001, -2002
+QR_FULL, QR_ECONOMICAL = 0, 1
+_pp = C.POINTER(vp)
+_SIGS.update({
+    "zml_dmatrix_deinit": (None, [C.POINTER(DMatrix)]),
+    "zml_plu": (i32, [i32, i32, i32, vp, i32, _pp]),
+    "zml_plu_deinit": (None, [vp]),
+    "zml_plu_p": (i32, [vp, vp]),
+    "zml_plu_l": (DMatrix, [vp]),
+    "zml_plu_u": (DMatrix, [vp]),
+    "zml_plu_ipiv": (C.POINTER(C.c_int), [vp]),
+    "zml_llt": (i32, [i32, ch, i32, vp, i32, _pp]),
+    "zml_utu": (i32, [i32, ch, i32, vp, i32, _pp]),
+    "zml_cholesky": (i32, [i32, ch, i32, vp, i32, _pp]),
+    "zml_chol_deinit": (None, [vp]),
+    "zml_chol_factor": (DMatrix, [vp]),
+    "zml_qr": (i32, [i32, i32, i32, vp, i32, _pp]),
+    "zml_qr_deinit": (None, [vp]),
+    "zml_qr_q": (i32, [vp, i32, C.POINTER(DMatrix)]),
+    "zml_qr_r": (DMatrix, [vp, i32]),
+    "zml_qr_tau": (C.POINTER(C.c_double), [vp]),
 })
 
 PREC_FP16, PREC_BF16, PREC_FP32, PREC_BF16X3 = 0, 1, 2, 3

@@ -13,6 +13,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libzml_gb300.so")
@@ -30,7 +31,7 @@ def nvcc():
 
 def _compile(src, verbose=False, extra=()):
     obj = os.path.join(OBJ, os.path.basename(src).replace(".cu", ".o"))
-    cmd = [nvcc(), *NVCC_FLAGS, *extra, "-I", CSRC, "-c", src, "-o", obj]
+    cmd = [nvcc(), *NVCC_FLAGS, *extra, "-I", CSRC, "-I", INCLUDE, "-c", src, "-o", obj]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -388,6 +388,23 @@ template <typename T> int geqrf_any(int layout, int m, int n, T *a, int lda, T *
   return sync(s);
 }
 
+template <typename T> int orgqr_any(int layout, int m, int n, int k, T *a, int lda, const T *tau) {
+  if (!lay_ok(layout)) return -1;
+  if (m < 0) return -2;
+  if (n < 0 || n > m) return -3;
+  if (k < 0 || k > n) return -4;
+  if (lda < std::max(1, layout == kColMajor ? m : n)) return -6;
+  if (n == 0) return 0;
+  cudaStream_t s = lib_stream();
+  ColMajor<T> A;
+  Buf<T> Tau;
+  ZG_TRY(A.in(layout, a, lda, m, n, kSlotA, kSlotAT, true, s));
+  ZG_TRY(Tau.in(const_cast<T *>(tau), k, kSlotPiv, true, s));
+  ZG_TRY(orgqr_dev<T>(m, n, k, A.d, A.ld, Tau.d, s));
+  ZG_TRY(A.out(s));
+  return sync(s);
+}
+
 template <typename T>
 int laswp_any(int layout, int n, T *a, int lda, int k1, int k2, const int *ipiv, int incx) {
   if (!lay_ok(layout)) return -1;
@@ -538,6 +555,19 @@ int zml_gpu_dgeqrf(int m, int n, double *dA, int ldda, double *dtau, void *strea
   if (n < 0) return -2;
   if (ldda < std::max(1, m)) return -4;
   return geqrf_dev<double>(m, n, dA, ldda, dtau, (cudaStream_t)stream);
+}
+int LAPACKE_dorgqr(int layout, int m, int n, int k, double *a, int lda, const double *tau) {
+  return orgqr_any<double>(layout, m, n, k, a, lda, tau);
+}
+int LAPACKE_sorgqr(int layout, int m, int n, int k, float *a, int lda, const float *tau) {
+  return orgqr_any<float>(layout, m, n, k, a, lda, tau);
+}
+int zml_gpu_dorgqr(int m, int n, int k, double *dA, int ldda, const double *dtau, void *stream) {
+  if (m < 0) return -1;
+  if (n < 0 || n > m) return -2;
+  if (k < 0 || k > n) return -3;
+  if (ldda < std::max(1, m)) return -5;
+  return orgqr_dev<double>(m, n, k, dA, ldda, dtau, (cudaStream_t)stream);
 }
 
 int LAPACKE_dlaswp(int layout, int n, double *a, int lda, int k1, int k2, const int *ipiv,

@@ -21,6 +21,9 @@ int gemm_simt_splitk(int transa, int transb, int m, int n, int k, T alpha, const
 
 // qr.cu -- Householder QR (geqrf) with the T factor of each panel.
 template <typename T> int geqrf_dev(int m, int n, T *A, long lda, T *tau, cudaStream_t s);
+// The first n columns of Q from geqrf's reflectors (k of them) stored in A.
+template <typename T>
+int orgqr_dev(int m, int n, int k, T *A, long lda, const T *tau, cudaStream_t s);
 
 // trsm.cu -- B <- alpha op(A)^-1 B (left) or alpha B op(A)^-1 (right).
 template <typename T>

@@ -268,4 +268,91 @@ template <typename T> int geqrf_dev(int m, int n, T *A, long lda, T *tau, cudaSt
 template int geqrf_dev<double>(int, int, double *, long, double *, cudaStream_t);
 template int geqrf_dev<float>(int, int, float *, long, float *, cudaStream_t);
 
+// ---------------------------------------------------------------------------
+// orgqr: the explicit first n columns of Q = H(0) H(1) ... H(k-1) (zml's
+// lapack/orgqr.zig:18-194 with org2r.zig:18-102).  The reflectors are copied
+// out of A, A's m x n block is set to the identity and the nb-blocks of
+// reflectors are applied last to first as block reflectors from the left,
+// C <- (I - V T V^T) C on the rows and columns the block touches (columns to
+// the left of a block still hold identity columns that H leaves unchanged).
+// T comes from the block's Gram matrix G = V^T V:
+// T(0:j, j) = -tau_j T(0:j, 0:j) G(0:j, j), T(j, j) = tau_j (the T of
+// larft.zig).  Unlike the reference there is no unblocked tail (org2r for the
+// last nx = 128 columns): every block goes through the same three GEMMs.
+
+// One CTA: T (ib x ib, ld ib, upper) from G (ib x ib, ld ib) and tau.
+template <typename T>
+__global__ void larft_gram_kernel(int ib, const T *__restrict__ G, const T *__restrict__ tau,
+                                  T *__restrict__ Tm) {
+  __shared__ T sT[kQrNB * kQrNB];
+  __shared__ T sG[kQrNB * kQrNB];
+  for (int e = threadIdx.x; e < ib * ib; e += blockDim.x) {
+    sG[e] = G[e];
+    sT[e] = T(0);
+  }
+  __syncthreads();
+  for (int j = 0; j < ib; ++j) {
+    const T tj = tau[j];
+    T acc = T(0);
+    const int r = threadIdx.x;
+    if (r < j)
+      for (int c = r; c < j; ++c) acc += sT[r + c * ib] * sG[c + j * ib];
+    __syncthreads();
+    if (r < j) sT[r + j * ib] = -tj * acc;
+    if (r == j) sT[j + j * ib] = tj;
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < ib * ib; e += blockDim.x) Tm[e] = sT[e];
+}
+
+// A (m x n) <- the first n columns of the identity.
+template <typename T> __global__ void set_identity_kernel(int m, int n, T *A, long lda) {
+  const long total = (long)m * n;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total;
+       e += (long)gridDim.x * blockDim.x) {
+    const int i = e % m, j = e / m;
+    A[i + (long)j * lda] = i == j ? T(1) : T(0);
+  }
+}
+
+template <typename T>
+int orgqr_dev(int m, int n, int k, T *A, long lda, const T *tau, cudaStream_t s) {
+  if (n <= 0) return 0;
+  const int nb = kQrNB, splits = 8;
+  // workspace: all k reflectors (m x k), G and T (nb x nb), W and T W (nb x n), split-K partials
+  const size_t nv = (size_t)m * std::max(k, 1), nt = (size_t)nb * nb, nw = (size_t)nb * n;
+  void *w;
+  ZG_TRY(workspace(s, kSlotQR, sizeof(T) * (nv + 2 * nt + 2 * nw + splits * std::max(nw, nt)) + 1024,
+                   &w));
+  T *V = (T *)w, *G = V + nv, *Tm = G + nt, *W = Tm + nt, *W2 = W + nw, *P = W2 + nw;
+  const int grid = 152 * 8;
+  if (k > 0)
+    ZG_LAUNCH(kTagQR, 0, sizeof(T) * 2.0 * m * k, s,
+              build_v_kernel<T><<<(int)std::min<long>(ceil_div((long)m * k, 256), grid), 256, 0, s>>>(
+                  m, k, A, lda, V));
+  ZG_LAUNCH(kTagQR, 0, sizeof(T) * 1.0 * m * n, s,
+            set_identity_kernel<T><<<(int)std::min<long>(ceil_div((long)m * n, 256), grid), 256, 0, s>>>(
+                m, n, A, lda));
+  const int last = k > 0 ? ((k - 1) / nb) * nb : -1;
+  for (int i = last; i >= 0; i -= nb) {
+    const int ib = std::min(nb, k - i), mi = m - i, nc = n - i;
+    // V block: rows i.. of reflectors i..i+ib (unit diagonal at row i + j)
+    const T *Vi = V + i + (long)i * m;
+    T *C = A + i + (long)i * lda;
+    ZG_TRY(gemm_simt_splitk<T>(kTrans, kNoTrans, ib, ib, mi, T(1), Vi, m, Vi, m, T(0), G, ib,
+                               splits, P, s));
+    ZG_LAUNCH(kTagQR, 0, 0, s, larft_gram_kernel<T><<<1, 64, 0, s>>>(ib, G, tau + i, Tm));
+    // C <- C - V (T (V^T C))
+    ZG_TRY(gemm_simt_splitk<T>(kTrans, kNoTrans, ib, nc, mi, T(1), Vi, m, C, lda, T(0), W, ib,
+                               splits, P, s));
+    ZG_TRY(gemm_simt<T>(kNoTrans, kNoTrans, ib, nc, ib, T(1), Tm, ib, W, ib, T(0), W2, ib, 0, s));
+    ZG_TRY(gemm_simt<T>(kNoTrans, kNoTrans, mi, nc, ib, T(-1), Vi, m, W2, ib, T(1), C, lda, 0, s));
+  }
+  ZG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+template int orgqr_dev<double>(int, int, int, double *, long, const double *, cudaStream_t);
+template int orgqr_dev<float>(int, int, int, float *, long, const float *, cudaStream_t);
+
 }  // namespace zg
