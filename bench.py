@@ -187,12 +187,18 @@ def cpu_block(n, threads, label):
 # ---------------------------------------------------------------------------
 # Batched uneven solves: 20000 systems, n ~ U{8..256}; even index SPD
 # G G^T / n + 0.1 I (potrf + potrs), odd index N(0,1) (getrf + getrs); 4 RHS.
-def batched_workload(torch, dev, count=20000, nrhs=4, seed=7):
+def batched_workload(torch, dev, count=20000, nrhs=4, seed=7, rank=0, world=1):
+    """This rank's share of the batch: an n^3-balanced contiguous range of
+    the systems (all of them on one GPU)."""
     import numpy as np
+    from zml_gb300 import shard
     rng = np.random.default_rng(seed)
-    n = rng.integers(8, 257, size=count).astype(np.int32)
-    spd = (np.arange(count) % 2 == 0).astype(np.int32)
-    g = torch.Generator(device=dev).manual_seed(seed)
+    n_all = rng.integers(8, 257, size=count).astype(np.int32)
+    spd_all = (np.arange(count) % 2 == 0).astype(np.int32)
+    lo, hi = shard.shard(n_all, rank, world)
+    n, spd = n_all[lo:hi].copy(), spd_all[lo:hi].copy()
+    count = len(n)
+    g = torch.Generator(device=dev).manual_seed(seed + lo)
     offs = np.concatenate([[0], np.cumsum(n.astype(np.int64) ** 2)])
     A = torch.empty(int(offs[-1]), dtype=torch.float64, device=dev)
     for k in np.unique(n):
@@ -217,11 +223,20 @@ def batched_workload(torch, dev, count=20000, nrhs=4, seed=7):
     return n, spd, A, B, flops, nbytes
 
 
-def batched_bench(torch, zg, L, dev, st, steps, warmup, hbm):
-    n, spd, A0, B, flops, nbytes = batched_workload(torch, dev)
+def batched_bench(torch, zg, L, dev, st, steps, warmup, hbm, rank=0, world=1, dist=None):
+    """The batched workload, sharded over ranks by n^3-balanced index ranges
+    (strong scaling: the 20000 systems are split); time = max over ranks."""
+    total_count = 20000
+    n, spd, A0, B, flops, nbytes = batched_workload(torch, dev, total_count, rank=rank,
+                                                    world=world)
     nrhs, count = 4, len(n)
+    if dist:
+        tot = torch.tensor([flops, nbytes], dtype=torch.float64, device=dev)
+        dist.all_reduce(tot)
+        flops, nbytes = tot.tolist()
     out = {"workload": "%d systems, n~U{8..256}, half SPD (potrf+potrs), half N(0,1) "
-                       "(getrf+getrs), %d RHS" % (count, nrhs), "count": count,
+                       "(getrf+getrs), %d RHS" % (total_count, nrhs), "count": total_count,
+           "ranks": world, "scaling": "strong" if world > 1 else None,
            "algorithmic_flops": flops, "algorithmic_bytes": nbytes}
     for prec, name in ((0, "fp64"), (1, "fp32_factor_fp64_ir")):
         ncls = L.zml_gpu_batched_schedule(prec, None, None, 0, 0)
@@ -254,7 +269,14 @@ def batched_bench(torch, zg, L, dev, st, steps, warmup, hbm):
         t = total / steps
         L.zml_gpu_batched_plan_destroy(plan)
         ok = int((info == 0).sum().item())
-        out[name] = {"solves_per_s": count / t, "ms_per_batch": 1e3 * t,
+        if dist:
+            tt = torch.tensor([t], dtype=torch.float64, device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            t = tt.item()
+            okt = torch.tensor([ok], dtype=torch.int64, device=dev)
+            dist.all_reduce(okt)
+            ok = int(okt.item())
+        out[name] = {"solves_per_s": total_count / t, "ms_per_batch": 1e3 * t,
                      "tflops": flops / t / 1e12, "hbm_gbs": nbytes / t / 1e9,
                      "hbm_frac": nbytes / t / 1e9 / hbm, "info_ok": ok,
                      "schedule_warps_per_class": list(chosen),
@@ -403,7 +425,8 @@ def main():
     e2e_ok = bool(torch.allclose(xh.to(dev), X, rtol=0, atol=1e-9))
 
     hbm, bf16, src = peaks()
-    batched = batched_bench(torch, zg, L, dev, st, a.steps, a.warmup, hbm) if a.batched else None
+    batched = (batched_bench(torch, zg, L, dev, st, a.steps, a.warmup, hbm, rank, world, dist)
+               if a.batched else None)
 
     if rank != 0:
         dist.destroy_process_group()

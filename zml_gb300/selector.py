@@ -29,7 +29,7 @@ import time
 
 import numpy as np
 
-from . import AutoResult, last_error, lib
+from . import AutoResult, last_error, lib, shard
 
 CLASSES = ["bf16", "fp16", "bf16x3", "fp32", "fp64"]
 NF, NH, NO = 16, 64, 5
@@ -123,13 +123,17 @@ def fp64_ms(torch, t, b, n):
     return (time.perf_counter() - t0) * 1e3
 
 
-def build_dataset(torch, specs, dev, log=None):
+def build_dataset(torch, specs, dev, log=None, rank=0, world=1):
     """Features (float32, len x 16), labels (int32) and the plain ladder's
-    wall time (ms) per matrix."""
+    wall time (ms) per matrix.  With world > 1 (an initialised process group)
+    each rank labels its n^3-balanced contiguous share and every rank
+    returns the gathered whole."""
+    lo, hi = shard.shard([s[1] for s in specs], rank, world)
     X = np.zeros((len(specs), NF), dtype=np.float32)
     y = np.zeros(len(specs), dtype=np.int32)
     ms = np.zeros(len(specs))
-    for i, (kind, n, kappa, seed) in enumerate(specs):
+    for i in range(lo, hi):
+        kind, n, kappa, seed = specs[i]
         t, m = generate(torch, kind, n, kappa, seed, dev)
         b = rhs(torch, m, seed)
         x = torch.zeros_like(b)
@@ -140,8 +144,11 @@ def build_dataset(torch, specs, dev, log=None):
         X[i] = np.frombuffer(res.features, dtype=np.float32)
         y[i] = res.used
         ms[i] = res.ms
-        if log and (i + 1) % 500 == 0:
-            log("  %d/%d matrices labelled" % (i + 1, len(specs)))
+        if log and (i + 1 - lo) % 500 == 0:
+            log("  %d/%d matrices labelled" % (i + 1 - lo, hi - lo))
+    if world > 1:
+        for plo, phi, pX, py, pms in shard.gather((lo, hi, X[lo:hi], y[lo:hi], ms[lo:hi])):
+            X[plo:phi], y[plo:phi], ms[plo:phi] = pX, py, pms
     return X, y, ms
 
 
@@ -276,13 +283,15 @@ def warm_up(torch, dev, nmax):
     fp64_ms(torch, t, b, nmax)
 
 
-def evaluate(torch, specs, state, dev, confidence=DEFAULT_CONFIDENCE, log=None):
+def evaluate(torch, specs, state, dev, confidence=DEFAULT_CONFIDENCE, log=None, rank=0, world=1):
     """Solves every held-out matrix with the plain ladder and with the ladder
     guided by the network (alternating which goes first), plus the FP64 LU.
-    Returns per-matrix records and a summary."""
+    Returns per-matrix records and a summary (sharded like build_dataset)."""
     model = model_array(state)
     rec = []
-    for i, (kind, n, kappa, seed) in enumerate(specs):
+    lo, hi = shard.shard([s[1] for s in specs], rank, world)
+    for i in range(lo, hi):
+        kind, n, kappa, seed = specs[i]
         t, m = generate(torch, kind, n, kappa, seed, dev)
         b = rhs(torch, m, seed)
         runs = {}
@@ -297,8 +306,10 @@ def evaluate(torch, specs, state, dev, confidence=DEFAULT_CONFIDENCE, log=None):
                     "ladder_converged": bool(lad.converged), "berr": gui.berr,
                     "ladder_ms": lad.ms, "guided_ms": gui.ms, "fp64_ms": fp64_ms(torch, t, b, n),
                     "features": list(np.frombuffer(lad.features, dtype=np.float32).tolist())})
-        if log and (i + 1) % 250 == 0:
-            log("  %d/%d held-out matrices" % (i + 1, len(specs)))
+        if log and (i + 1 - lo) % 250 == 0:
+            log("  %d/%d held-out matrices" % (i + 1 - lo, hi - lo))
+    if world > 1:
+        rec = [r for part in shard.gather(rec) for r in part]
     return rec, summarize(rec)
 
 
@@ -343,15 +354,26 @@ def main():
     ap.add_argument("--out", default=None, help="model .npz to write")
     ap.add_argument("--report", default=None, help="summary JSON to write")
     a = ap.parse_args()
-    dev = torch.device("cuda", 0)
-    torch.cuda.set_device(0)
+    # under torchrun: one rank per GPU, labelling and evaluation sharded by
+    # n^3-balanced index ranges, results gathered on the host; every rank
+    # trains the same network on the gathered data (deterministic kernels)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
 
     def log(s):
-        print(s, flush=True)
+        if rank == 0:
+            print(s, flush=True)
 
     t0 = time.time()
     warm_up(torch, dev, a.nmax)
-    Xtr, ytr, _ = build_dataset(torch, sample_specs(a.train, seed=1, nmax=a.nmax), dev, log)
+    Xtr, ytr, _ = build_dataset(torch, sample_specs(a.train, seed=1, nmax=a.nmax), dev, log,
+                                rank, world)
     log("labelled %d training matrices in %.0f s, classes %s" %
         (a.train, time.time() - t0, np.bincount(ytr, minlength=NO).tolist()))
     t1 = time.time()
@@ -359,20 +381,23 @@ def main():
                   resume=a.resume)
     log("trained %d epochs in %.1f s, loss %.4f -> %.4f" %
         (a.epochs, time.time() - t1, state["loss_history"][0], state["loss_history"][-1]))
-    if a.out:
+    if a.out and rank == 0:
         save_checkpoint(a.out, state)
     rec, summ = evaluate(torch, sample_specs(a.heldout, seed=2, nmax=a.nmax), state, dev,
-                         a.confidence, log)
+                         a.confidence, log, rank, world)
     summ.update({"train": a.train, "nmax": a.nmax, "epochs": a.epochs,
                  "confidence": a.confidence, "train_label_counts":
                  np.bincount(ytr, minlength=NO).tolist(),
                  "loss_first": float(state["loss_history"][0]),
                  "loss_last": float(state["loss_history"][-1]),
                  "seconds": time.time() - t0})
+    summ["ranks"] = world
     log(json.dumps(summ))
-    if a.report:
+    if a.report and rank == 0:
         with open(a.report, "w") as f:
             json.dump({"summary": summ, "records": rec}, f)
+    if world > 1:
+        dist.destroy_process_group()
 
 
 if __name__ == "__main__":
