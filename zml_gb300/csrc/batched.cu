@@ -69,6 +69,182 @@ __device__ void group_argmax(F &key, int &idx, int tid, int nt, int gid, double 
   group_sync(gid, nt);
 }
 
+// ---- blocked factorizations ---------------------------------------------
+// Right-looking with kNB-column blocks: the column-serial work (pivot search,
+// interchanges, scaling, rank-1 updates) is confined to the kNB-wide panel;
+// the trailing matrix gets one register-tiled GEMM (LU) or SYRK (Cholesky)
+// per block, each thread accumulating a 4 x 4 tile over the panel's K.
+constexpr int kNB = 32;
+
+// Panel GEPP on columns [c0, c1), rows [c0, n): pivot search, interchange and
+// rank-1 update restricted to the panel's columns (getf2 of getrf2.zig:14-210
+// applied to one block column).  Returns the first zero pivot (1-based) or
+// the incoming info.
+template <typename F>
+__device__ int panel_getf2(View<F> M, int n, int c0, int c1, int *ipiv, int tid, int nt, int gid,
+                           double *sk, int *si, int info) {
+  for (int k = c0; k < c1; ++k) {
+    F key = F(-1);
+    int idx = 0x7fffffff;
+    for (int i = k + tid; i < n; i += nt) {
+      const F v = M(i, k);
+      const F kv = v != v ? (i == k ? F(INFINITY) : F(-1)) : fabs(v);
+      if (kv > key || (kv == key && i < idx)) { key = kv; idx = i; }
+    }
+    group_argmax(key, idx, tid, nt, gid, sk, si);
+    const int p = idx == 0x7fffffff ? k : idx;
+    if (tid == 0) ipiv[k] = p + 1;
+    const F piv = M(p, k);
+    if (piv == F(0)) {
+      if (info == 0) info = k + 1;
+    } else {
+      if (p != k)
+        for (int j = c0 + tid; j < c1; j += nt) {
+          const F t = M(k, j);
+          M(k, j) = M(p, j);
+          M(p, j) = t;
+        }
+      group_sync(gid, nt);
+      const F rp = F(1) / piv;
+      const bool recip = fabs(piv) >= Real<F>::sfmin();
+      for (int i = k + 1 + tid; i < n; i += nt) M(i, k) = recip ? M(i, k) * rp : M(i, k) / piv;
+    }
+    group_sync(gid, nt);
+    if (k + 1 < c1)
+      for (int i = k + 1 + tid; i < n; i += nt) {
+        const F lik = M(i, k);
+        for (int j = k + 1; j < c1; ++j) M(i, j) -= lik * M(k, j);
+      }
+    group_sync(gid, nt);
+  }
+  return info;
+}
+
+// C(r0.., r0..) -= A(r0.., c0:c1) * B(c0:c1, r0..) over the square trailing
+// block [r0, n)^2 of M (A and B are M's own panel blocks); lower = only the
+// tiles on or below the diagonal and, inside diagonal tiles, only i >= j
+// (SYRK with B = A^T read as M(j, k)).
+template <typename F, bool kLower>
+__device__ void trailing_update(View<F> M, int n, int r0, int c0, int c1, int tid, int nt) {
+  const int R = n - r0;
+  if (R <= 0) return;
+  const int tr = (R + 3) >> 2;
+  const int tiles = kLower ? tr * (tr + 1) / 2 : tr * tr;
+  for (int t = tid; t < tiles; t += nt) {
+    int bi, bj;
+    if (kLower) {  // t -> (bi, bj), bj <= bi, column-major over the lower triangle of tiles
+      bj = 0;
+      int rem = t, len = tr;
+      while (rem >= len) { rem -= len; ++bj; --len; }
+      bi = bj + rem;
+    } else {
+      bi = t % tr;
+      bj = t / tr;
+    }
+    const int i0 = r0 + 4 * bi, j0 = r0 + 4 * bj;
+    F acc[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[r][c] = F(0);
+    for (int k = c0; k < c1; ++k) {
+      F a[4], b[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) a[r] = i0 + r < n ? M(i0 + r, k) : F(0);
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+        b[c] = j0 + c < n ? (kLower ? M(j0 + c, k) : M(k, j0 + c)) : F(0);
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[r][c] = fma(a[r], b[c], acc[r][c]);
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int i = i0 + r, j = j0 + c;
+        if (i < n && j < n && (!kLower || i >= j)) M(i, j) -= acc[r][c];
+      }
+  }
+}
+
+template <typename F>
+__device__ int lu_blocked(View<F> M, int n, int *ipiv, int tid, int nt, int gid, double *sk,
+                          int *si) {
+  int info = 0;
+  for (int c0 = 0; c0 < n; c0 += kNB) {
+    const int c1 = min(n, c0 + kNB), kb = c1 - c0;
+    info = panel_getf2(M, n, c0, c1, ipiv, tid, nt, gid, sk, si, info);
+    // the panel's interchanges on the columns left and right of it
+    for (int j = tid; j < n - kb; j += nt) {
+      const int jj = j < c0 ? j : j + kb;
+      for (int k = c0; k < c1; ++k) {
+        const int p = ipiv[k] - 1;
+        if (p != k) {
+          const F t = M(k, jj);
+          M(k, jj) = M(p, jj);
+          M(p, jj) = t;
+        }
+      }
+    }
+    group_sync(gid, nt);
+    if (c1 >= n) break;
+    // U12 = L11^-1 A12 (unit lower), one column per thread held in registers
+    for (int j = c1 + tid; j < n; j += nt) {
+      F x[kNB];
+#pragma unroll
+      for (int i = 0; i < kNB; ++i) x[i] = i < kb ? M(c0 + i, j) : F(0);
+#pragma unroll
+      for (int i = 1; i < kNB; ++i) {
+        if (i < kb) {
+          F acc = x[i];
+#pragma unroll
+          for (int l = 0; l < i; ++l) acc = fma(-M(c0 + i, c0 + l), x[l], acc);
+          x[i] = acc;
+        }
+      }
+#pragma unroll
+      for (int i = 1; i < kNB; ++i)
+        if (i < kb) M(c0 + i, j) = x[i];
+    }
+    group_sync(gid, nt);
+    trailing_update<F, false>(M, n, c1, c0, c1, tid, nt);
+    group_sync(gid, nt);
+  }
+  return info;
+}
+
+// Blocked lower Cholesky: per block, the column-serial factorization of the
+// (n - c0) x kb block column (diagonal block and the rows below it), then one
+// SYRK of the trailing lower triangle.
+template <typename F> __device__ int chol_blocked(View<F> M, int n, int tid, int nt, int gid) {
+  for (int c0 = 0; c0 < n; c0 += kNB) {
+    const int c1 = min(n, c0 + kNB);
+    for (int k = c0; k < c1; ++k) {
+      const F d = M(k, k);
+      if (!(d > F(0))) return k + 1;
+      const F s = sqrt(d);
+      const F r = F(1) / s;
+      group_sync(gid, nt);
+      if (tid == 0) M(k, k) = s;
+      for (int i = k + 1 + tid; i < n; i += nt) M(i, k) *= r;
+      group_sync(gid, nt);
+      if (k + 1 < c1)
+        for (int i = k + 1 + tid; i < n; i += nt) {
+          const F lik = M(i, k);
+          const int jmax = min(i, c1 - 1);
+          for (int j = k + 1; j <= jmax; ++j) M(i, j) -= lik * M(j, k);
+        }
+      group_sync(gid, nt);
+    }
+    if (c1 >= n) break;
+    trailing_update<F, true>(M, n, c1, c0, c1, tid, nt);
+    group_sync(gid, nt);
+  }
+  return 0;
+}
+
 template <typename F>
 __device__ int lu_inplace(View<F> M, int n, int *ipiv, int tid, int nt, int gid, double *sk,
                           int *si) {
@@ -235,8 +411,8 @@ __global__ void __launch_bounds__(256) batched_kernel(BatchArgs a, const BatchTa
       if (fbuf != reinterpret_cast<F *>(Ag))
         for (int e = gt; e < n * n; e += nt) fbuf[e] = (F)Ag[e];
       group_sync(gid, nt);
-      const int info = spd ? chol_inplace<F>(M, n, gt, nt, gid)
-                           : lu_inplace<F>(M, n, ipiv, gt, nt, gid, sk[gid], si[gid]);
+      const int info = spd ? chol_blocked<F>(M, n, gt, nt, gid)
+                           : lu_blocked<F>(M, n, ipiv, gt, nt, gid, sk[gid], si[gid]);
       int iters = 0;
       if (info == 0) {
         for (int e = gt; e < n * nrhs; e += nt) Xg[e] = Bg[e];
