@@ -4,21 +4,26 @@
 // lapack/getrf.zig:14 / getrs.zig:13) or SPD A (potrf + potrs, lower,
 // potrf.zig:17 / potrs.zig:15), with nrhs right-hand sides.
 //
-// One persistent launch: CTAs pull tasks from an atomic queue in descending
-// estimated cost (longest processing time first).  A task is up to 8/w
-// matrices of one size class that the CTA processes concurrently with w warps
-// each -- the per-size warp schedule, chosen by the autotuner -- and each
-// group of w warps synchronises on its own named barrier.  A group's factor
-// lives in its w/8 share of the CTA's shared memory when it fits, otherwise
-// in L2-resident global memory (FP64: in place in the caller's matrix).
+// One persistent launch, one CTA of 16 warps per SM.  Each size class has a
+// warp count w (the per-size schedule, chosen by the autotuner); the matrices
+// of all classes with the same w form one queue, sorted by descending cost
+// (longest processing time first).  A CTA splits into 16/w groups of w warps
+// for a queue; each group pulls its next matrix from the queue with an atomic
+// and synchronises on its own named barrier (w > 1) or as a warp (w = 1), so
+// no group waits for another between matrices; the CTA meets only when it
+// moves to the next queue.  Factorizations are blocked (32-column panels,
+// register-tiled trailing updates).  A group's factor lives in its w/16
+// share of the CTA's shared memory when it fits, otherwise in L2-resident
+// global memory (FP64: in place in the caller's matrix).
 //
 // Precisions: FP64 (factor and solve in FP64; A is overwritten with the
 // factors like getrf/potrf), or FP32 factorization + FP64 iterative
 // refinement (A untouched; x += (LU)^-1 (b - A x) with the residual from the
-// FP64 A until ||r||inf <= 4 u ||A||inf ||x||inf or max_ir steps).
+// FP64 A and the triangular solves in FP32, until
+// ||r||inf <= 4 u ||A||inf ||x||inf or max_ir steps).
 //
 // A plan (zml_gpu_batched_plan_create) does the host work once -- sizes,
-// offsets, the task list -- so that executing it is a memset and one kernel
+// offsets, the queues -- so that executing it is a memset and one kernel
 // launch, which can be captured in a CUDA graph and replayed.
 #include <algorithm>
 #include <map>
@@ -32,7 +37,7 @@ namespace zg {
 
 namespace {
 
-constexpr int kSmemTotal = 200 * 1024;  // per CTA; a group of w warps owns w/8 of it
+constexpr int kSmemTotal = 200 * 1024;  // per CTA; a group of w warps owns w/kWarps of it
 
 __device__ __forceinline__ void group_sync(int gid, int nthreads) {
   if (nthreads == 32)
@@ -190,23 +195,32 @@ __device__ int lu_blocked(View<F> M, int n, int *ipiv, int tid, int nt, int gid,
     }
     group_sync(gid, nt);
     if (c1 >= n) break;
-    // U12 = L11^-1 A12 (unit lower), one column per thread held in registers
+    // U12 = L11^-1 A12 (unit lower), one column per thread, solved in two
+    // halves of 16 rows held in registers
     for (int j = c1 + tid; j < n; j += nt) {
-      F x[kNB];
+      for (int h0 = 0; h0 < kb; h0 += 16) {
+        F x[16];
 #pragma unroll
-      for (int i = 0; i < kNB; ++i) x[i] = i < kb ? M(c0 + i, j) : F(0);
+        for (int i = 0; i < 16; ++i) x[i] = h0 + i < kb ? M(c0 + h0 + i, j) : F(0);
+        for (int l = 0; l < h0; ++l) {  // rows solved in the first half
+          const F xl = M(c0 + l, j);
 #pragma unroll
-      for (int i = 1; i < kNB; ++i) {
-        if (i < kb) {
-          F acc = x[i];
-#pragma unroll
-          for (int l = 0; l < i; ++l) acc = fma(-M(c0 + i, c0 + l), x[l], acc);
-          x[i] = acc;
+          for (int i = 0; i < 16; ++i)
+            if (h0 + i < kb) x[i] = fma(-M(c0 + h0 + i, c0 + l), xl, x[i]);
         }
-      }
 #pragma unroll
-      for (int i = 1; i < kNB; ++i)
-        if (i < kb) M(c0 + i, j) = x[i];
+        for (int i = 1; i < 16; ++i) {
+          if (h0 + i < kb) {
+            F acc = x[i];
+#pragma unroll
+            for (int l = 0; l < i; ++l) acc = fma(-M(c0 + h0 + i, c0 + h0 + l), x[l], acc);
+            x[i] = acc;
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+          if (h0 + i < kb) M(c0 + h0 + i, j) = x[i];
+      }
     }
     group_sync(gid, nt);
     trailing_update<F, false>(M, n, c1, c0, c1, tid, nt);
@@ -304,16 +318,16 @@ template <typename F> __device__ int chol_inplace(View<F> M, int n, int tid, int
   return 0;
 }
 
-// X (n x nrhs, FP64, ld ldx) <- A^-1 X from the factors in M, FP64 arithmetic.
-template <typename F>
-__device__ void solve_inplace(View<F> M, int n, bool spd, const int *ipiv, double *X, int ldx,
+// X (n x nrhs, ld ldx) <- A^-1 X from the factors in M, in the arithmetic of V.
+template <typename F, typename V>
+__device__ void solve_inplace(View<F> M, int n, bool spd, const int *ipiv, V *X, int ldx,
                               int nrhs, int tid, int nt, int gid) {
   if (!spd) {
     for (int c = tid; c < nrhs; c += nt)
       for (int k = 0; k < n; ++k) {
         const int p = ipiv[k] - 1;
         if (p != k) {
-          const double t = X[k + c * ldx];
+          const V t = X[k + c * ldx];
           X[k + c * ldx] = X[p + c * ldx];
           X[p + c * ldx] = t;
         }
@@ -322,21 +336,21 @@ __device__ void solve_inplace(View<F> M, int n, bool spd, const int *ipiv, doubl
   }
   for (int k = 0; k < n; ++k) {  // forward: unit L (LU) or L (Cholesky)
     if (spd)
-      for (int c = tid; c < nrhs; c += nt) X[k + c * ldx] /= (double)M(k, k);
+      for (int c = tid; c < nrhs; c += nt) X[k + c * ldx] /= (V)M(k, k);
     group_sync(gid, nt);
     for (int c = 0; c < nrhs; ++c) {
-      const double xk = X[k + c * ldx];
-      for (int i = k + 1 + tid; i < n; i += nt) X[i + c * ldx] -= (double)M(i, k) * xk;
+      const V xk = X[k + c * ldx];
+      for (int i = k + 1 + tid; i < n; i += nt) X[i + c * ldx] -= (V)M(i, k) * xk;
     }
     group_sync(gid, nt);
   }
   for (int k = n - 1; k >= 0; --k) {  // backward: U (LU) or L^T (Cholesky)
-    for (int c = tid; c < nrhs; c += nt) X[k + c * ldx] /= (double)M(k, k);
+    for (int c = tid; c < nrhs; c += nt) X[k + c * ldx] /= (V)M(k, k);
     group_sync(gid, nt);
     for (int c = 0; c < nrhs; ++c) {
-      const double xk = X[k + c * ldx];
+      const V xk = X[k + c * ldx];
       for (int i = tid; i < k; i += nt)
-        X[i + c * ldx] -= (spd ? (double)M(k, i) : (double)M(i, k)) * xk;
+        X[i + c * ldx] -= (spd ? (V)M(k, i) : (V)M(i, k)) * xk;
     }
     group_sync(gid, nt);
   }
@@ -356,103 +370,137 @@ __device__ double group_max(double v, int tid, int nt, int gid, double *red) {
 
 }  // namespace
 
+// One matrix, factored and solved by the group gid (gt = thread in the
+// group, nt = its threads, groups = groups per CTA).
 template <typename F>
-__global__ void __launch_bounds__(256) batched_kernel(BatchArgs a, const BatchTask *__restrict__ tasks,
-                                                      int ntasks, unsigned *queue, F *gscratch,
-                                                      long gscratch_per_group, unsigned *status) {
-  extern __shared__ __align__(16) unsigned char bsm[];
-  __shared__ unsigned s_task;
-  __shared__ double sk[8][8];  // per-group argmax keys, read back as F (8-byte aligned)
-  __shared__ int si[8][8];
-  __shared__ double red[8][8];
-  const int tid = threadIdx.x;
-  for (;;) {
-    if (tid == 0) s_task = atomicAdd(queue, 1u);
-    __syncthreads();
-    const unsigned t = s_task;
-    __syncthreads();
-    if (t >= (unsigned)ntasks) break;
-    const BatchTask task = tasks[t];
-    const int w = task.warps, nt = 32 * w, groups = 8 / w;
-    const int gid = tid / nt, gt = tid % nt;
-    if (gid < groups && gid < task.count) {
-      const int mi = task.mat[gid];
-      const int n = a.n[mi];
-      const bool spd = a.spd[mi] != 0;
-      const int nrhs = a.nrhs;
-      double *Ag = a.A + a.a_off[mi];
-      const double *Bg = a.B + a.b_off[mi];
-      double *Xg = a.X + a.b_off[mi];
-      int *ipiv = a.ipiv + a.p_off[mi];
-      const int share = kSmemTotal / groups;
-      unsigned char *gsm = bsm + (long)gid * share;
-      const bool in_smem = (long)n * n * (long)sizeof(F) <= share;
-      F *fbuf;
-      if (in_smem)
-        fbuf = reinterpret_cast<F *>(gsm);
-      else if (sizeof(F) == sizeof(double))
-        fbuf = reinterpret_cast<F *>(Ag);  // FP64 factor in place, L2-resident
-      else
-        fbuf = gscratch + ((long)blockIdx.x * 8 + gid) * gscratch_per_group;
-      View<F> M{fbuf, n};
-      // ||A||inf of the input (refinement stopping test)
-      double anorm = 0;
-      if (sizeof(F) == sizeof(float)) {
-        for (int i = gt; i < n; i += nt) {
-          double rs = 0;
-          for (int j = 0; j < n; ++j) {
-            const double v = spd ? (i >= j ? Ag[i + (long)j * n] : Ag[j + (long)i * n]) : Ag[i + (long)j * n];
-            rs += fabs(v);
-          }
-          anorm = fmax(anorm, rs);
-        }
-        anorm = group_max(anorm, gt, nt, gid, red[gid]);
+__device__ void process_matrix(const BatchArgs &a, int mi, int gid, int gt, int nt, int groups,
+                               unsigned char *bsm, double (*sk)[kBatchWarps],
+                               int (*si)[kBatchWarps], double (*red)[kBatchWarps], F *gscratch,
+                               long gscratch_per_group) {
+  const int n = a.n[mi];
+  const bool spd = a.spd[mi] != 0;
+  const int nrhs = a.nrhs;
+  double *Ag = a.A + a.a_off[mi];
+  const double *Bg = a.B + a.b_off[mi];
+  double *Xg = a.X + a.b_off[mi];
+  int *ipiv = a.ipiv + a.p_off[mi];
+  const int share = kSmemTotal / groups;
+  unsigned char *gsm = bsm + (long)gid * share;
+  const bool in_smem = (long)n * n * (long)sizeof(F) <= share;
+  F *fbuf;
+  if (in_smem)
+    fbuf = reinterpret_cast<F *>(gsm);
+  else if (sizeof(F) == sizeof(double))
+    fbuf = reinterpret_cast<F *>(Ag);  // FP64 factor in place, L2-resident
+  else
+    fbuf = gscratch + ((long)blockIdx.x * kBatchWarps + gid) * gscratch_per_group;
+  View<F> M{fbuf, n};
+  // ||A||inf of the input (refinement stopping test)
+  double anorm = 0;
+  if (sizeof(F) == sizeof(float)) {
+    for (int i = gt; i < n; i += nt) {
+      double rs = 0;
+      for (int j = 0; j < n; ++j) {
+        const double v = spd ? (i >= j ? Ag[i + (long)j * n] : Ag[j + (long)i * n]) : Ag[i + (long)j * n];
+        rs += fabs(v);
       }
-      if (fbuf != reinterpret_cast<F *>(Ag))
-        for (int e = gt; e < n * n; e += nt) fbuf[e] = (F)Ag[e];
+      anorm = fmax(anorm, rs);
+    }
+    anorm = group_max(anorm, gt, nt, gid, red[gid]);
+  }
+  if (fbuf != reinterpret_cast<F *>(Ag))
+    for (int e = gt; e < n * n; e += nt) fbuf[e] = (F)Ag[e];
+  group_sync(gid, nt);
+  const int info = spd ? chol_blocked<F>(M, n, gt, nt, gid)
+                       : lu_blocked<F>(M, n, ipiv, gt, nt, gid, sk[gid], si[gid]);
+  int iters = 0;
+  if (info == 0) {
+    // FP32 factors: the solves run in FP32 on a per-group FP32 vector
+    float *Vf = nullptr;
+    if (sizeof(F) == sizeof(float))
+      Vf = reinterpret_cast<float *>(gscratch) +
+           ((long)blockIdx.x * kBatchWarps + gid) * gscratch_per_group + a.vec_off;
+    if (sizeof(F) == sizeof(double)) {
+      for (int e = gt; e < n * nrhs; e += nt) Xg[e] = Bg[e];
       group_sync(gid, nt);
-      const int info = spd ? chol_blocked<F>(M, n, gt, nt, gid)
-                           : lu_blocked<F>(M, n, ipiv, gt, nt, gid, sk[gid], si[gid]);
-      int iters = 0;
-      if (info == 0) {
-        for (int e = gt; e < n * nrhs; e += nt) Xg[e] = Bg[e];
-        group_sync(gid, nt);
-        solve_inplace<F>(M, n, spd, ipiv, Xg, n, nrhs, gt, nt, gid);
-        if (sizeof(F) == sizeof(float)) {
-          double *R = a.R + a.b_off[mi];
-          for (iters = 0; iters < a.max_ir; ++iters) {
-            double rmax = 0, xmax = 0;
-            for (int e = gt; e < n * nrhs; e += nt) {
-              const int i = e % n, c = e / n;
-              double acc = Bg[i + (long)c * n];
-              for (int j = 0; j < n; ++j) {
-                const double v =
-                    spd ? (i >= j ? Ag[i + (long)j * n] : Ag[j + (long)i * n]) : Ag[i + (long)j * n];
-                acc -= v * Xg[j + (long)c * n];
-              }
-              R[e] = acc;
-              rmax = fmax(rmax, fabs(acc));
-              xmax = fmax(xmax, fabs(Xg[e]));
-            }
-            rmax = group_max(rmax, gt, nt, gid, red[gid]);
-            xmax = group_max(xmax, gt, nt, gid, red[gid]);
-            if (rmax <= 4.0 * 1.1102230246251565e-16 * anorm * xmax) break;
-            solve_inplace<F>(M, n, spd, ipiv, R, n, nrhs, gt, nt, gid);
-            for (int e = gt; e < n * nrhs; e += nt) Xg[e] += R[e];
-            group_sync(gid, nt);
+      solve_inplace<F, double>(M, n, spd, ipiv, Xg, n, nrhs, gt, nt, gid);
+    } else {
+      for (int e = gt; e < n * nrhs; e += nt) Vf[e] = (float)Bg[e];
+      group_sync(gid, nt);
+      solve_inplace<F, float>(M, n, spd, ipiv, Vf, n, nrhs, gt, nt, gid);
+      for (int e = gt; e < n * nrhs; e += nt) Xg[e] = (double)Vf[e];
+      group_sync(gid, nt);
+    }
+    if (sizeof(F) == sizeof(float)) {
+      double *R = a.R + a.b_off[mi];
+      for (iters = 0; iters < a.max_ir; ++iters) {
+        double rmax = 0, xmax = 0;
+        for (int e = gt; e < n * nrhs; e += nt) {
+          const int i = e % n, c = e / n;
+          double acc = Bg[i + (long)c * n];
+          for (int j = 0; j < n; ++j) {
+            const double v =
+                spd ? (i >= j ? Ag[i + (long)j * n] : Ag[j + (long)i * n]) : Ag[i + (long)j * n];
+            acc -= v * Xg[j + (long)c * n];
           }
+          R[e] = acc;
+          rmax = fmax(rmax, fabs(acc));
+          xmax = fmax(xmax, fabs(Xg[e]));
         }
+        rmax = group_max(rmax, gt, nt, gid, red[gid]);
+        xmax = group_max(xmax, gt, nt, gid, red[gid]);
+        if (rmax <= 4.0 * 1.1102230246251565e-16 * anorm * xmax) break;
+        for (int e = gt; e < n * nrhs; e += nt) Vf[e] = (float)R[e];
+        group_sync(gid, nt);
+        solve_inplace<F, float>(M, n, spd, ipiv, Vf, n, nrhs, gt, nt, gid);
+        for (int e = gt; e < n * nrhs; e += nt) Xg[e] += (double)Vf[e];
+        group_sync(gid, nt);
       }
-      if (gt == 0) {
-        a.info[mi] = info;
-        if (a.iters) a.iters[mi] = iters;
+    }
+  }
+  if (gt == 0) {
+    a.info[mi] = info;
+    if (a.iters) a.iters[mi] = iters;
+  }
+  if (sizeof(F) == sizeof(double) && in_smem)  // FP64: A <- factors
+    for (int e = gt; e < n * n; e += nt) Ag[e] = (double)fbuf[e];
+}
+
+// Persistent kernel: the queues (one per warp count) are taken in turn; the
+// groups of a CTA pull their next matrix from the current queue on their own
+// (no CTA-wide wait between matrices), and the CTA meets only when a queue
+// runs dry.
+template <typename F>
+__global__ void __launch_bounds__(kBatchThreads, 1)
+    batched_kernel(BatchArgs a, const int *__restrict__ order, const BatchQueue *__restrict__ queues,
+                   int nq, unsigned *counters, F *gscratch, long gscratch_per_group) {
+  extern __shared__ __align__(16) unsigned char bsm[];
+  __shared__ unsigned s_slot[kBatchWarps];
+  __shared__ double sk[kBatchWarps][kBatchWarps];  // per-group argmax keys, read back as F
+  __shared__ int si[kBatchWarps][kBatchWarps];
+  __shared__ double red[kBatchWarps][kBatchWarps];
+  const int tid = threadIdx.x;
+  for (int q = 0; q < nq; ++q) {
+    const BatchQueue Q = queues[q];
+    const int w = Q.warps, nt = 32 * w, groups = kBatchWarps / w;
+    const int gid = tid / nt, gt = tid % nt;
+    for (;;) {
+      unsigned slot = 0;
+      if (w == 1) {
+        if (gt == 0) slot = atomicAdd(&counters[q], 1u);
+        slot = __shfl_sync(0xffffffffu, slot, 0);
+      } else {
+        if (gt == 0) s_slot[gid] = atomicAdd(&counters[q], 1u);
+        group_sync(gid, nt);
+        slot = s_slot[gid];
+        group_sync(gid, nt);
       }
-      if (sizeof(F) == sizeof(double) && in_smem)  // FP64: A <- factors
-        for (int e = gt; e < n * n; e += nt) Ag[e] = (double)fbuf[e];
+      if (slot >= (unsigned)Q.len) break;
+      process_matrix<F>(a, order[Q.start + slot], gid, gt, nt, groups, bsm, sk, si, red, gscratch,
+                        gscratch_per_group);
     }
     __syncthreads();
   }
-  (void)status;
 }
 
 // ---------------------------------------------------------------------------
@@ -468,7 +516,7 @@ int class_of(int n) {
   return c;
 }
 // warps per matrix by class; [0] FP64, [1] FP32 + refinement
-int g_sched[2][kClasses] = {{1, 1, 1, 2, 4, 8, 8, 8, 8, 8}, {1, 1, 1, 2, 2, 4, 8, 8, 8, 8}};
+int g_sched[2][kClasses] = {{1, 1, 1, 1, 1, 1, 1, 1, 1, 1}, {1, 1, 1, 1, 1, 1, 1, 1, 1, 1}};
 
 }  // namespace
 
@@ -480,7 +528,8 @@ int batched_classes(int *edges, int cap) {
 int batched_schedule(int fp32, int *warps, int cap, bool set) {
   for (int c = 0; c < std::min(cap, kClasses); ++c) {
     if (set) {
-      if (warps[c] != 1 && warps[c] != 2 && warps[c] != 4 && warps[c] != 8) return kErrInvalid;
+      if (warps[c] != 1 && warps[c] != 2 && warps[c] != 4 && warps[c] != 8 && warps[c] != 16)
+        return kErrInvalid;
       g_sched[fp32 ? 1 : 0][c] = warps[c];
     } else {
       warps[c] = g_sched[fp32 ? 1 : 0][c];
@@ -519,41 +568,42 @@ int batched_plan_create(BatchPlan **out, int count, const int *n, const int *spd
   p->b_elems = sb;
   p->p_elems = sp;
   p->nmax = nmax;
-  // tasks: matrices sorted by n (descending), grouped per class by its warp count
-  std::vector<int> order(count);
-  for (int i = 0; i < count; ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return n[x] > n[y]; });
-  std::vector<BatchTask> tasks;
-  std::vector<double> cost;
-  for (size_t q = 0; q < order.size();) {
-    const int c = class_of(n[order[q]]);
-    const int w = g_sched[fp32 ? 1 : 0][c];
-    BatchTask t{};
-    t.warps = w;
-    double cc = 0;
-    while (t.count < 8 / w && q < order.size() && class_of(n[order[q]]) == c) {
-      const double nn = n[order[q]];
-      cc = std::max(cc, nn * nn * nn / (2.0 + w));
-      t.mat[t.count++] = order[q++];
-    }
-    tasks.push_back(t);
-    cost.push_back(cc);
+  // queues: one per warp count, each holding its matrices in descending
+  // factorization cost (LU 2n^3/3, Cholesky n^3/3: longest first); the queues
+  // themselves in descending cost of their first matrix
+  auto mcost = [&](int i) {
+    const double nn = n[i];
+    return (spd && spd[i] ? 1.0 : 2.0) * nn * nn * nn;
+  };
+  std::vector<int> byw[kBatchWarpCounts];
+  for (int i = 0; i < count; ++i) {
+    const int w = g_sched[fp32 ? 1 : 0][class_of(n[i])];
+    int qi = 0;
+    while ((1 << qi) < w) ++qi;
+    byw[qi].push_back(i);
   }
-  std::vector<int> ti(tasks.size());
-  for (size_t i = 0; i < ti.size(); ++i) ti[i] = (int)i;
-  std::stable_sort(ti.begin(), ti.end(), [&](int x, int y) { return cost[x] > cost[y]; });
-  std::vector<BatchTask> sorted(tasks.size());
-  for (size_t i = 0; i < ti.size(); ++i) sorted[i] = tasks[ti[i]];
-  p->ntasks = (int)sorted.size();
+  std::vector<int> order;
+  std::vector<BatchQueue> queues;
+  for (int qi = 0; qi < kBatchWarpCounts; ++qi) {
+    if (byw[qi].empty()) continue;
+    std::stable_sort(byw[qi].begin(), byw[qi].end(),
+                     [&](int x, int y) { return mcost(x) > mcost(y); });
+    queues.push_back(BatchQueue{1 << qi, (int)order.size(), (int)byw[qi].size()});
+    order.insert(order.end(), byw[qi].begin(), byw[qi].end());
+  }
+  std::stable_sort(queues.begin(), queues.end(), [&](const BatchQueue &x, const BatchQueue &y) {
+    return mcost(order[x.start]) > mcost(order[y.start]);
+  });
+  p->nq = (int)queues.size();
   DeviceInfo di;
   int r = device_info(&di);
   if (r < 0) { delete p; return r; }
   p->grid = di.num_sms;
-  p->scratch_per_group = fp32 ? (long)nmax * nmax : 0;
+  p->scratch_per_group = fp32 ? (long)nmax * nmax + (long)nmax * nrhs : 0;
   // device buffers: descriptors, tasks, per-group FP32 scratch, residuals, queue
   const size_t bytes = sizeof(int) * 2 * count + sizeof(long) * 3 * count +
-                       sizeof(BatchTask) * sorted.size() +
-                       sizeof(float) * (size_t)p->grid * 8 * p->scratch_per_group +
+                       sizeof(int) * (size_t)count + sizeof(BatchQueue) * kBatchWarpCounts +
+                       sizeof(float) * (size_t)p->grid * kBatchWarps * p->scratch_per_group +
                        (fp32 ? sizeof(double) * sb : 0) + 4096;
   if (cudaMalloc(&p->dev, bytes) != cudaSuccess) {
     cudaGetLastError();
@@ -572,8 +622,9 @@ int batched_plan_create(BatchPlan **out, int count, const int *n, const int *spd
   p->d_aoff = (long *)take(sizeof(long) * count);
   p->d_boff = (long *)take(sizeof(long) * count);
   p->d_poff = (long *)take(sizeof(long) * count);
-  p->d_tasks = (BatchTask *)take(sizeof(BatchTask) * sorted.size());
-  p->d_scratch = (float *)take(sizeof(float) * (size_t)p->grid * 8 * p->scratch_per_group);
+  p->d_order = (int *)take(sizeof(int) * std::max(1, count));
+  p->d_queues = (BatchQueue *)take(sizeof(BatchQueue) * kBatchWarpCounts);
+  p->d_scratch = (float *)take(sizeof(float) * (size_t)p->grid * kBatchWarps * p->scratch_per_group);
   p->d_R = fp32 ? (double *)take(sizeof(double) * sb) : nullptr;
   p->d_queue = (unsigned *)take(64);
   std::vector<int> spdv(count);
@@ -583,8 +634,10 @@ int batched_plan_create(BatchPlan **out, int count, const int *n, const int *spd
   cudaMemcpy(p->d_aoff, aoff.data(), sizeof(long) * count, cudaMemcpyHostToDevice);
   cudaMemcpy(p->d_boff, boff.data(), sizeof(long) * count, cudaMemcpyHostToDevice);
   cudaMemcpy(p->d_poff, poff.data(), sizeof(long) * count, cudaMemcpyHostToDevice);
-  if (cudaMemcpy(p->d_tasks, sorted.data(), sizeof(BatchTask) * sorted.size(),
-                 cudaMemcpyHostToDevice) != cudaSuccess) {
+  if ((count > 0 && cudaMemcpy(p->d_order, order.data(), sizeof(int) * count,
+                                cudaMemcpyHostToDevice) != cudaSuccess) ||
+      (p->nq > 0 && cudaMemcpy(p->d_queues, queues.data(), sizeof(BatchQueue) * p->nq,
+                               cudaMemcpyHostToDevice) != cudaSuccess)) {
     cudaGetLastError();
     cudaFree(p->dev);
     delete p;
@@ -619,6 +672,7 @@ int batched_plan_execute(BatchPlan *p, double *A, const double *B, double *X, in
   a.p_off = p->d_poff;
   a.nrhs = p->nrhs;
   a.max_ir = p->max_ir;
+  a.vec_off = (long)p->nmax * p->nmax;
   a.A = A;
   a.B = B;
   a.X = X;
@@ -626,7 +680,7 @@ int batched_plan_execute(BatchPlan *p, double *A, const double *B, double *X, in
   a.ipiv = ipiv;
   a.info = info;
   a.iters = iters;
-  ZG_CUDA(cudaMemsetAsync(p->d_queue, 0, sizeof(unsigned), s));
+  ZG_CUDA(cudaMemsetAsync(p->d_queue, 0, sizeof(unsigned) * kBatchWarpCounts, s));
   if (p->fp32) {
     static bool attr = false;
     if (!attr) {
@@ -635,9 +689,9 @@ int batched_plan_execute(BatchPlan *p, double *A, const double *B, double *X, in
       attr = true;
     }
     ZG_LAUNCH(kTagBatched, p->flops, 0, s,
-              batched_kernel<float><<<p->grid, 256, kSmemTotal, s>>>(
-                  a, p->d_tasks, p->ntasks, p->d_queue, p->d_scratch, p->scratch_per_group,
-                  nullptr));
+              batched_kernel<float><<<p->grid, kBatchThreads, kSmemTotal, s>>>(
+                  a, p->d_order, p->d_queues, p->nq, p->d_queue, p->d_scratch,
+                  p->scratch_per_group));
   } else {
     static bool attr = false;
     if (!attr) {
@@ -646,8 +700,8 @@ int batched_plan_execute(BatchPlan *p, double *A, const double *B, double *X, in
       attr = true;
     }
     ZG_LAUNCH(kTagBatched, p->flops, 0, s,
-              batched_kernel<double><<<p->grid, 256, kSmemTotal, s>>>(
-                  a, p->d_tasks, p->ntasks, p->d_queue, nullptr, 0, nullptr));
+              batched_kernel<double><<<p->grid, kBatchThreads, kSmemTotal, s>>>(
+                  a, p->d_order, p->d_queues, p->nq, p->d_queue, nullptr, 0));
   }
   return 0;
 }
@@ -725,8 +779,8 @@ int batched_autotune(int fp32, int nrhs, cudaStream_t s, int *chosen, double *ms
   int rc = 0;
   for (int c = 0; c < kClasses && rc == 0; ++c) {
     const int n = std::min(kEdges[c], 256);
-    // enough matrices for a few full waves of groups
-    const int count = std::max(2 * di.num_sms, std::min(8 * di.num_sms * 2, (int)(4e8 / ((double)n * n * n))));
+    // two full waves of one-warp groups (every group of every CTA busy twice)
+    const int count = 2 * kBatchWarps * di.num_sms;
     std::vector<int> nv(count, n), sv(count);
     for (int i = 0; i < count; ++i) sv[i] = i & 1;
     double *dA = nullptr, *dA0 = nullptr, *dB = nullptr, *dX = nullptr;
@@ -742,7 +796,7 @@ int batched_autotune(int fp32, int nrhs, cudaStream_t s, int *chosen, double *ms
       fill_batch_kernel<<<std::min((int)((na + 255) / 256), 152 * 16), 256, 0, s>>>(count, n, dA0, dB, nrhs, 1234u + c);
       double best = 1e30;
       int bestw = saved[c];
-      for (int w : {1, 2, 4, 8}) {
+      for (int w : {1, 2, 4, 8, 16}) {
         g_sched[fp32 ? 1 : 0][c] = w;
         BatchPlan *p = nullptr;
         if (batched_plan_create(&p, count, nv.data(), sv.data(), nrhs, fp32, 10) < 0) continue;

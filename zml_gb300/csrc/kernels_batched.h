@@ -4,18 +4,22 @@
 
 namespace zg {
 
-// A unit of work: up to 8/warps matrices of one size class, processed
-// concurrently by groups of `warps` warps of one CTA.
-struct BatchTask {
-  int warps;
-  int count;
-  int mat[8];
+// One persistent CTA of kBatchWarps warps per SM.
+constexpr int kBatchWarps = 16, kBatchThreads = 32 * kBatchWarps;
+
+// Warp counts a matrix may be given: 1, 2, 4, 8, 16.
+constexpr int kBatchWarpCounts = 5;
+
+// The matrices factored by groups of `warps` warps: order[start .. start+len).
+struct BatchQueue {
+  int warps, start, len;
 };
 
 struct BatchArgs {
   const int *n, *spd;
   const long *a_off, *b_off, *p_off;
   int nrhs, max_ir;
+  long vec_off;  // FP32 path: offset of a group's FP32 vector in its scratch
   double *A;
   const double *B;
   double *X, *R;
@@ -23,13 +27,14 @@ struct BatchArgs {
 };
 
 struct BatchPlan {
-  int count = 0, nrhs = 1, fp32 = 0, max_ir = 10, ntasks = 0, grid = 0, nmax = 0;
+  int count = 0, nrhs = 1, fp32 = 0, max_ir = 10, nq = 0, grid = 0, nmax = 0;
   long a_elems = 0, b_elems = 0, p_elems = 0, scratch_per_group = 0;
   double flops = 0;
   void *dev = nullptr;
   int *d_n = nullptr, *d_spd = nullptr;
   long *d_aoff = nullptr, *d_boff = nullptr, *d_poff = nullptr;
-  BatchTask *d_tasks = nullptr;
+  int *d_order = nullptr;
+  BatchQueue *d_queues = nullptr;
   float *d_scratch = nullptr;
   double *d_R = nullptr;
   unsigned *d_queue = nullptr;
