@@ -52,6 +52,10 @@ def parse():
     p.add_argument("--prec", type=int, default=3, help="0 fp16, 1 bf16, 2 fp32, 3 bf16x3")
     p.add_argument("--mode", type=int, default=1, help="0 plain IR, 1 GMRES-IR")
     p.add_argument("--batched", type=int, default=1, help="also run the batched config (1/0)")
+    p.add_argument("--batched-count", type=int, default=20000,
+                   help="systems in the batched workload (20000 = the batched config)")
+    p.add_argument("--batched-autotune", type=int, default=1,
+                   help="autotune the per-size warp schedule first (1/0)")
     return p.parse_args()
 
 
@@ -223,10 +227,10 @@ def batched_workload(torch, dev, count=20000, nrhs=4, seed=7, rank=0, world=1):
     return n, spd, A, B, flops, nbytes
 
 
-def batched_bench(torch, zg, L, dev, st, steps, warmup, hbm, rank=0, world=1, dist=None):
+def batched_bench(torch, zg, L, dev, st, steps, warmup, hbm, rank=0, world=1, dist=None,
+                  total_count=20000, autotune=True):
     """The batched workload, sharded over ranks by n^3-balanced index ranges
     (strong scaling: the 20000 systems are split); time = max over ranks."""
-    total_count = 20000
     n, spd, A0, B, flops, nbytes = batched_workload(torch, dev, total_count, rank=rank,
                                                     world=world)
     nrhs, count = 4, len(n)
@@ -238,10 +242,29 @@ def batched_bench(torch, zg, L, dev, st, steps, warmup, hbm, rank=0, world=1, di
                        "(getrf+getrs), %d RHS" % (total_count, nrhs), "count": total_count,
            "ranks": world, "scaling": "strong" if world > 1 else None,
            "algorithmic_flops": flops, "algorithmic_bytes": nbytes}
+    # FP64 is the binding roof (about 8 flop per algorithmic byte): its peak
+    # is measured here as cuBLAS DGEMM 8192^3 through torch, best of 3
+    a64 = torch.randn(8192, 8192, dtype=torch.float64, device=dev)
+    torch.matmul(a64, a64)
+    best = 1e30
+    for _ in range(3):
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record(st)
+        torch.matmul(a64, a64)
+        g1.record(st)
+        torch.cuda.synchronize()
+        best = min(best, g0.elapsed_time(g1) / 1e3)
+    del a64
+    fp64_peak = 2.0 * 8192 ** 3 / best / 1e12
+    out["fp64_peak_tflops"] = fp64_peak
+    out["fp64_peak_source"] = "measured: cuBLAS DGEMM 8192^3 (torch.matmul), best of 3"
     for prec, name in ((0, "fp64"), (1, "fp32_factor_fp64_ir")):
         ncls = L.zml_gpu_batched_schedule(prec, None, None, 0, 0)
         chosen = (C.c_int * ncls)()
-        L.zml_gpu_batched_autotune(prec, nrhs, chosen, None, st.cuda_stream)
+        if autotune:
+            L.zml_gpu_batched_autotune(prec, nrhs, chosen, None, st.cuda_stream)
+        else:
+            L.zml_gpu_batched_schedule(prec, chosen, None, ncls, 0)
         plan = C.c_void_p()
         rc = L.zml_gpu_batched_plan_create(C.byref(plan), count, n.ctypes.data_as(C.c_void_p),
                                            spd.ctypes.data_as(C.c_void_p), nrhs, prec, 10)
@@ -277,6 +300,9 @@ def batched_bench(torch, zg, L, dev, st, steps, warmup, hbm, rank=0, world=1, di
             dist.all_reduce(okt)
             ok = int(okt.item())
         out[name] = {"solves_per_s": total_count / t, "ms_per_batch": 1e3 * t,
+                     "roofline": {"kernel": "batched_kernel", "bound": "fp64",
+                                  "achieved": flops / t / 1e12, "peak": fp64_peak,
+                                  "unit": "TFLOP/s", "frac": flops / t / 1e12 / fp64_peak},
                      "tflops": flops / t / 1e12, "hbm_gbs": nbytes / t / 1e9,
                      "hbm_frac": nbytes / t / 1e9 / hbm, "info_ok": ok,
                      "schedule_warps_per_class": list(chosen),
@@ -425,8 +451,8 @@ def main():
     e2e_ok = bool(torch.allclose(xh.to(dev), X, rtol=0, atol=1e-9))
 
     hbm, bf16, src = peaks()
-    batched = (batched_bench(torch, zg, L, dev, st, a.steps, a.warmup, hbm, rank, world, dist)
-               if a.batched else None)
+    batched = (batched_bench(torch, zg, L, dev, st, a.steps, a.warmup, hbm, rank, world, dist,
+                             a.batched_count, bool(a.batched_autotune)) if a.batched else None)
 
     if rank != 0:
         dist.destroy_process_group()
