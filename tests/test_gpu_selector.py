@@ -158,7 +158,7 @@ def test_ladder_easy_and_hard(torch, sel):
             assert r.attempts == 1
         assert r.attempts >= 1 + (r.used >= 1) * 1
         berr = _residual_berr(m, x, b)
-        assert berr <= 64 * U64 and abs(berr - r.berr) <= 0.5 * berr + 1e-18
+        assert berr <= 64 * U64 and abs(berr - r.berr) <= 0.5 * berr + 4 * U64  # roundoff level
 
 
 def test_model_that_predicts_fp64_jumps_straight_there(torch, sel):

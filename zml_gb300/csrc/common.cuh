@@ -96,7 +96,8 @@ enum Slot : int {
   kSlotSel = 17,              // selector feature statistics
   kSlotSelNet = 18,           // selector network parameters, input, logits, work
   kSlotF64LU = 19,            // FP64 LU copy and pivots of the selector's last resort
-  kNumSlots = 20
+  kSlotInvL = 20,             // mixed LU: inverse of the unit-lower diagonal block, block row
+  kNumSlots = 24
 };
 
 // Returns a device buffer of at least `bytes` bound to `stream` in `slot`.

@@ -212,16 +212,20 @@ __global__ void laswp_prep_kernel(int k1, int k2, const int *__restrict__ ipiv, 
   __shared__ int orow[kSwapMax];     // rows outside the segment that were touched
   __shared__ int ocont[kSwapMax];    // and their contents
   __shared__ int hkey[kHash], hval[kHash];
+  __shared__ int piv[kSwapMax];      // the chunk's pivots, staged once
   const int lane = threadIdx.x;
   const int base = k1 - 1, len = k2 - k1 + 1;
-  for (int t = lane; t < len; t += 32) seg[t] = base + t;
+  for (int t = lane; t < len; t += 32) {
+    seg[t] = base + t;
+    piv[t] = ipiv[base + t] - 1;
+  }
   for (int t = lane; t < kHash; t += 32) hkey[t] = -1;
   __syncwarp();
   if (lane != 0) return;
   int nout = 0;
   for (int st = 0; st < len; ++st) {
     const int i = incx > 0 ? base + st : base + len - 1 - st;
-    const int p = ipiv[i] - 1;
+    const int p = piv[i - base];
     if (p == i) continue;
     if (p >= base && p < base + len) {
       const int t = seg[i - base];

@@ -134,6 +134,96 @@ static int to_kmajor_n(int prec, int k, int cols, const float *A, long lda, void
 }
 
 // ---------------------------------------------------------------------------
+// Block-row solves of the low-precision LU through explicit inverses of the
+// unit-lower diagonal blocks: U12 = L11^-1 A12 as one FP32 GEMM instead of a
+// chain of latency-bound substitutions.  (The FP64 LU keeps the TRSM of
+// getrf.zig:104-114; here the factors only precondition the refinement.)
+
+// X (nb x nb, ld ldx) <- L^-1 for the unit-lower nb x nb block L (ld ldl),
+// nb <= 128; one CTA of 256 threads, everything in shared memory.  L is padded
+// to 128 with the identity; the 16 x 16 diagonal blocks are inverted by
+// substitution (one column per thread), then pairs of inverted blocks are
+// merged level by level, [A^-1 0; C B^-1] -> off-diagonal block -B^-1 C A^-1,
+// as two small matrix products over all threads.
+constexpr int kInvN = 128, kInvLd = kInvN + 1;
+__global__ void __launch_bounds__(256) inv_unit_lower_kernel(int nb, const float *__restrict__ L,
+                                                             long ldl, float *__restrict__ X,
+                                                             long ldx) {
+  extern __shared__ __align__(16) float ism[];
+  float *sL = ism;                    // sL[i * kInvLd + k] = L(i, k), padded
+  float *sX = sL + kInvN * kInvLd;    // sX[i * kInvLd + k] = X(i, k)
+  float *sT = sX + kInvN * kInvLd;    // 64 x 64 product scratch, ld 65
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < kInvN * kInvN; e += nt) {
+    const int i = e % kInvN, k = e / kInvN;
+    const float v = (i < nb && k < nb) ? L[i + (long)k * ldl] : (i == k ? 1.f : 0.f);
+    sL[i * kInvLd + k] = v;
+    sX[i * kInvLd + k] = 0.f;
+  }
+  __syncthreads();
+  // 16 x 16 diagonal blocks: thread = (block, column)
+  if (tid < kInvN) {
+    const int b0 = (tid >> 4) << 4, c = tid;
+    sX[c * kInvLd + c] = 1.f;
+    for (int i = c + 1; i < b0 + 16; ++i) {
+      float acc = 0.f;
+      for (int k = c; k < i; ++k) acc = fmaf(sL[i * kInvLd + k], sX[k * kInvLd + c], acc);
+      sX[i * kInvLd + c] = -acc;
+    }
+  }
+  __syncthreads();
+  for (int sz = 16; sz < kInvN; sz *= 2) {
+    const int pairs = kInvN / (2 * sz);
+    // T = C A^-1 for every pair (C = L rows b+sz.., cols b..; A^-1 = X block at b)
+    for (int e = tid; e < pairs * sz * sz; e += nt) {
+      const int q = e / (sz * sz), r = (e / sz) % sz, c = e % sz, b = q * 2 * sz;
+      float acc = 0.f;
+      for (int k = c; k < sz; ++k)  // A^-1 is lower: rows k >= c
+        acc = fmaf(sL[(b + sz + r) * kInvLd + b + k], sX[(b + k) * kInvLd + b + c], acc);
+      sT[(q * sz + r) * 65 + c] = acc;  // pairs * sz <= 64 rows
+    }
+    __syncthreads();
+    // off-diagonal block = -B^-1 T (B^-1 = X block at b + sz, lower)
+    for (int e = tid; e < pairs * sz * sz; e += nt) {
+      const int q = e / (sz * sz), r = (e / sz) % sz, c = e % sz, b = q * 2 * sz;
+      float acc = 0.f;
+      for (int k = 0; k <= r; ++k)
+        acc = fmaf(sX[(b + sz + r) * kInvLd + b + sz + k], sT[(q * sz + k) * 65 + c], acc);
+      sX[(b + sz + r) * kInvLd + b + c] = -acc;
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < nb * nb; e += nt) {
+    const int i = e % nb, k = e / nb;
+    X[i + (long)k * ldx] = sX[i * kInvLd + k];
+  }
+}
+
+static int inv_unit_lower(int nb, const float *L, long ldl, float *X, long ldx, cudaStream_t s) {
+  static bool attr = false;
+  const int smem = (2 * kInvN * kInvLd + 64 * 65) * sizeof(float);
+  if (!attr) {
+    ZG_CUDA(cudaFuncSetAttribute(inv_unit_lower_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem));
+    attr = true;
+  }
+  ZG_LAUNCH(kTagTrsmDiag, nb * (double)nb * nb / 3.0, 0, s,
+            inv_unit_lower_kernel<<<1, 256, smem, s>>>(nb, L, ldl, X, ldx));
+  return 0;
+}
+
+// B (k x cols, ld ldb) <- Linv B with Linv (k x k, ld ldi), through a scratch
+// copy T (k x cols, ld k).
+static int apply_inverse(int k, int cols, const float *Linv, long ldi, float *B, long ldb, float *T,
+                         cudaStream_t s) {
+  if (k <= 0 || cols <= 0) return 0;
+  ZG_TRY(gemm_simt<float>(kNoTrans, kNoTrans, k, cols, k, 1.f, Linv, ldi, B, ldb, 0.f, T, k, 0, s));
+  ZG_CUDA(cudaMemcpy2DAsync(B, sizeof(float) * ldb, T, sizeof(float) * k, sizeof(float) * k, cols,
+                            cudaMemcpyDeviceToDevice, s));
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
 // Low-precision LU of an n x n FP32 matrix (partial pivoting, ipiv 1-based).
 int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cudaStream_t s) {
   if (n <= 0) return 0;
@@ -143,11 +233,21 @@ int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cud
     return getrf_dev<float>(n, n, A, lda, ipiv, &info, s) < 0 ? kErrCuda : 0;
   }
   const int segs = prec == kPrecBF16x3 ? 3 : 1;
-  void *wl, *wu;
+  void *wl, *wu, *wi;
   ZG_TRY(workspace(s, kSlotL16, sizeof(uint16_t) * (size_t)n * NB * segs, &wl));
   ZG_TRY(workspace(s, kSlotU16, sizeof(uint16_t) * (size_t)n * NB * segs, &wu));
+  // L11^-1 (NB x NB), a temporary NBP x NBP block, and the block row's scratch
+  const size_t ntb = prec == kPrecBF16x3 ? (size_t)NBP * NBP : (size_t)NB * n;
+  ZG_TRY(workspace(s, kSlotInvL,
+                   sizeof(float) * ((size_t)NB * NB + NBP * NBP + ntb) +
+                       sizeof(uint16_t) * (size_t)NB * NB * segs + 256,
+                   &wi));
+  // L11^-1, a product scratch, the block row's scratch, L11^-1 as a 16-bit operand
+  float *Linv = (float *)wi, *Ttmp = Linv + NB * NB, *Tb = Ttmp + NBP * NBP;
+  void *wli = Tb + ntb;
   for (int j = 0; j < n; j += NB) {
     const int jb = std::min(NB, n - j);
+    ZG_CUDA(cudaMemsetAsync(Linv, 0, sizeof(float) * NB * NB, s));
     // panel: two cooperative FP32 half-panels with an FP32 update between
     for (int p = 0; p < jb; p += NBP) {
       const int r = j + p, pb = std::min(NBP, jb - p);
@@ -156,26 +256,46 @@ int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cud
       // interchanges of this half-panel inside the panel's other columns
       ZG_TRY(laswp_panel<float>(r - j, r + pb - j, jb, A + (long)j * lda, lda, r + 1, r + pb,
                                 ipiv, s));
+      // the half-panel's unit-lower diagonal block, inverted into L11^-1
+      float *Dinv = Linv + p + (long)p * NB;
+      ZG_TRY(inv_unit_lower(pb, A + r + (long)r * lda, lda, Dinv, NB, s));
       if (right > 0) {
         float *Ar = A + (long)(r + pb) * lda;
-        ZG_TRY(trsm_dev<float>(kLeft, kLower, kNoTrans, kUnit, pb, right, 1.f,
-                               A + r + (long)r * lda, lda, Ar + r, lda, s));
+        ZG_TRY(apply_inverse(pb, right, Dinv, NB, Ar + r, lda, Tb, s));
         ZG_TRY(gemm_simt<float>(kNoTrans, kNoTrans, n - r - pb, right, pb, -1.f,
                                 A + (r + pb) + (long)r * lda, lda, Ar + r, lda, 1.f,
                                 Ar + r + pb, lda, 0, s));
       }
     }
+    if (jb > NBP) {
+      // L11^-1 = [La^-1 0; -Lb^-1 Lc La^-1  Lb^-1]
+      const int pb2 = jb - NBP;
+      ZG_TRY(gemm_simt<float>(kNoTrans, kNoTrans, pb2, NBP, NBP, 1.f,
+                              A + (j + NBP) + (long)j * lda, lda, Linv, NB, 0.f, Ttmp, NBP, 0, s));
+      ZG_TRY(gemm_simt<float>(kNoTrans, kNoTrans, pb2, NBP, pb2, -1.f, Linv + NBP + (long)NBP * NB,
+                              NB, Ttmp, NBP, 0.f, Linv + NBP, NB, 0, s));
+    }
     ZG_TRY(laswp_panel<float>(j, j + jb, n, A, lda, j + 1, j + jb, ipiv, s));
     const int rest = n - j - jb;
     if (rest <= 0) break;
     float *A12 = A + j + (long)(j + jb) * lda;
-    ZG_TRY(trsm_dev<float>(kLeft, kLower, kNoTrans, kUnit, jb, rest, 1.f, A + j + (long)j * lda,
-                           lda, A12, lda, s));
-    // 16-bit operands: L21 (rest x jb) and U12^T (rest x jb), K-major
+    // U12 = L11^-1 A12.  BF16x3 (about 16 bits, the precision of its trailing
+    // updates): on the tensor cores, A12 read through its 16-bit copy and U12
+    // written over A12 in FP32.  Plain BF16 / FP16 would cut U's rows to 8 /
+    // 11 bits, so there the product is an FP32 GEMM.
     const int ldk = ((jb + 7) / 8) * 8;
+    const long ldo = (long)ldk * segs;
+    if (prec == kPrecBF16x3) {
+      ZG_TRY(to_kmajor_t(prec, jb, jb, Linv, NB, wli, ldk, s));
+      ZG_TRY(to_kmajor_n(prec, jb, rest, A12, lda, wu, ldk, s));
+      ZG_TRY(gemm_tc(jb, rest, (int)ldo, 1.f, wli, ldo, wu, ldo, 0.f, A12, lda, 1, &ctl->status,
+                     s));
+    } else {
+      ZG_TRY(apply_inverse(jb, rest, Linv, NB, A12, lda, Tb, s));
+    }
+    // 16-bit operands: L21 (rest x jb) and U12^T (rest x jb), K-major
     ZG_TRY(to_kmajor_t(prec, rest, jb, A + (j + jb) + (long)j * lda, lda, wl, ldk, s));
     ZG_TRY(to_kmajor_n(prec, jb, rest, A12, lda, wu, ldk, s));
-    const long ldo = (long)ldk * segs;
     ZG_TRY(gemm_tc(rest, rest, (int)ldo, -1.f, wl, ldo, wu, ldo, 1.f, A12 + jb, lda,
                    prec == kPrecFP16 ? 0 : 1, &ctl->status, s));
   }
