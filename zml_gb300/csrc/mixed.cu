@@ -212,12 +212,45 @@ static int inv_unit_lower(int nb, const float *L, long ldl, float *X, long ldx, 
   return 0;
 }
 
+// C = alpha A B + beta C for small NN products (one thread per element of C,
+// the K loop in registers): the 128 x 128 x 128 block products of the mixed
+// LU, too small to fill the GPU with 64 x 64 tiles.
+__global__ void gemm_small_kernel(int m, int n, int k, float alpha, const float *__restrict__ A,
+                                  long lda, const float *__restrict__ B, long ldb, float beta,
+                                  float *__restrict__ C, long ldc) {
+  const int i = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int j = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (i >= m || j >= n) return;
+  float a0 = 0.f, a1 = 0.f;
+  int q = 0;
+  for (; q + 1 < k; q += 2) {
+    a0 = fmaf(A[i + (long)q * lda], B[q + (long)j * ldb], a0);
+    a1 = fmaf(A[i + (long)(q + 1) * lda], B[q + 1 + (long)j * ldb], a1);
+  }
+  if (q < k) a0 = fmaf(A[i + (long)q * lda], B[q + (long)j * ldb], a0);
+  const float v = alpha * (a0 + a1);
+  C[i + (long)j * ldc] = beta == 0.f ? v : v + beta * C[i + (long)j * ldc];
+}
+
+static int gemm_small(int m, int n, int k, float alpha, const float *A, long lda, const float *B,
+                      long ldb, float beta, float *C, long ldc, cudaStream_t s) {
+  if (m <= 0 || n <= 0) return 0;
+  ZG_LAUNCH(kTagGemmSimt, 2.0 * m * n * k, 4.0 * ((double)m * k + (double)k * n + 2.0 * m * n), s,
+            gemm_small_kernel<<<dim3(ceil_div(m, 32), ceil_div(n, 8)), 256, 0, s>>>(
+                m, n, k, alpha, A, lda, B, ldb, beta, C, ldc));
+  return 0;
+}
+
 // B (k x cols, ld ldb) <- Linv B with Linv (k x k, ld ldi), through a scratch
 // copy T (k x cols, ld k).
 static int apply_inverse(int k, int cols, const float *Linv, long ldi, float *B, long ldb, float *T,
                          cudaStream_t s) {
   if (k <= 0 || cols <= 0) return 0;
-  ZG_TRY(gemm_simt<float>(kNoTrans, kNoTrans, k, cols, k, 1.f, Linv, ldi, B, ldb, 0.f, T, k, 0, s));
+  if (cols <= 256)
+    ZG_TRY(gemm_small(k, cols, k, 1.f, Linv, ldi, B, ldb, 0.f, T, k, s));
+  else
+    ZG_TRY(gemm_simt<float>(kNoTrans, kNoTrans, k, cols, k, 1.f, Linv, ldi, B, ldb, 0.f, T, k, 0,
+                            s));
   ZG_CUDA(cudaMemcpy2DAsync(B, sizeof(float) * ldb, T, sizeof(float) * k, sizeof(float) * k, cols,
                             cudaMemcpyDeviceToDevice, s));
   return 0;
@@ -262,18 +295,29 @@ int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cud
       if (right > 0) {
         float *Ar = A + (long)(r + pb) * lda;
         ZG_TRY(apply_inverse(pb, right, Dinv, NB, Ar + r, lda, Tb, s));
-        ZG_TRY(gemm_simt<float>(kNoTrans, kNoTrans, n - r - pb, right, pb, -1.f,
-                                A + (r + pb) + (long)r * lda, lda, Ar + r, lda, 1.f,
-                                Ar + r + pb, lda, 0, s));
+        const int rows = n - r - pb;
+        if (prec == kPrecBF16x3 && rows > 0) {
+          // the second half-panel's update in the block's update precision
+          const int ldk = ((pb + 7) / 8) * 8;
+          const long ldo = (long)ldk * segs;
+          ZG_TRY(to_kmajor_t(prec, rows, pb, A + (r + pb) + (long)r * lda, lda, wl, ldk, s));
+          ZG_TRY(to_kmajor_n(prec, pb, right, Ar + r, lda, wu, ldk, s));
+          ZG_TRY(gemm_tc(rows, right, (int)ldo, -1.f, wl, ldo, wu, ldo, 1.f, Ar + r + pb, lda, 1,
+                         &ctl->status, s));
+        } else {
+          ZG_TRY(gemm_simt<float>(kNoTrans, kNoTrans, rows, right, pb, -1.f,
+                                  A + (r + pb) + (long)r * lda, lda, Ar + r, lda, 1.f,
+                                  Ar + r + pb, lda, 0, s));
+        }
       }
     }
     if (jb > NBP) {
       // L11^-1 = [La^-1 0; -Lb^-1 Lc La^-1  Lb^-1]
       const int pb2 = jb - NBP;
-      ZG_TRY(gemm_simt<float>(kNoTrans, kNoTrans, pb2, NBP, NBP, 1.f,
-                              A + (j + NBP) + (long)j * lda, lda, Linv, NB, 0.f, Ttmp, NBP, 0, s));
-      ZG_TRY(gemm_simt<float>(kNoTrans, kNoTrans, pb2, NBP, pb2, -1.f, Linv + NBP + (long)NBP * NB,
-                              NB, Ttmp, NBP, 0.f, Linv + NBP, NB, 0, s));
+      ZG_TRY(gemm_small(pb2, NBP, NBP, 1.f, A + (j + NBP) + (long)j * lda, lda, Linv, NB, 0.f,
+                        Ttmp, NBP, s));
+      ZG_TRY(gemm_small(pb2, NBP, pb2, -1.f, Linv + NBP + (long)NBP * NB, NB, Ttmp, NBP, 0.f,
+                        Linv + NBP, NB, s));
     }
     ZG_TRY(laswp_panel<float>(j, j + jb, n, A, lda, j + 1, j + jb, ipiv, s));
     const int rest = n - j - jb;
