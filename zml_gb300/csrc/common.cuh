@@ -132,12 +132,15 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
 // complete once it reaches (g + 1) * nblocks, so a waiter sees the last
 // arrival directly.  The wait is bounded; on timeout the status bit is set
 // and the CTA carries on (the host then reports kErrTimeout).
+// Arrival is a release reduction and the wait an acquire load: with the CTA
+// barriers around them, every write of the CTA before the barrier is visible
+// to every CTA after it.
 __device__ __forceinline__ void grid_barrier(Control *ctl, unsigned nblocks, unsigned &gen) {
   __syncthreads();
   if (threadIdx.x == 0) {
     const unsigned target = (gen + 1) * nblocks;
-    __threadfence();
-    atomicAdd(&ctl->barrier[0], 1u);
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(&ctl->barrier[0]), "r"(1u)
+                 : "memory");
     long long spins = 0;
     while (ld_acquire(&ctl->barrier[0]) < target) {
       if (++spins > kSpinLimit) {
@@ -145,7 +148,6 @@ __device__ __forceinline__ void grid_barrier(Control *ctl, unsigned nblocks, uns
         break;
       }
     }
-    __threadfence();
   }
   ++gen;
   __syncthreads();

@@ -65,11 +65,22 @@ __device__ void block_argmax(T &key, int &idx, T *sk, int *si) {
 // Exchange layout (T words): for parity p in {0,1}:
 //   cand[p][b] : [key, row, v_0 .. v_{nb-1}]  (stride nb + 2), b < gridDim.x
 //   rowk[p]    : [v_0 .. v_{nb-1}]
+// FP32 keys: the candidate (|v| or -inf for a NaN off the diagonal, row) is
+// one 64-bit word -- the key's order-preserving bits + 1 (0 for -inf) above
+// 0xffffffff - row -- whose maximum is the pivot (largest key, then lowest
+// row).  Every CTA folds its word into winners[k] with atomicMax before the
+// barrier and reads the single word after it.
+__device__ __forceinline__ unsigned long long pack_candidate(float key, int idx) {
+  const unsigned ord = key == -INFINITY ? 0u : __float_as_uint(key) + 1u;
+  return ((unsigned long long)ord << 32) | (unsigned)(0xffffffffu - (unsigned)idx);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) panel_lu_kernel(int m, int nb, T *__restrict__ A, long lda,
                                                        int *__restrict__ ipiv, int ipiv_base,
                                                        Control *ctl, int info_base, int R,
-                                                       T *__restrict__ xchg) {
+                                                       T *__restrict__ xchg,
+                                                       unsigned long long *__restrict__ winners) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *S = reinterpret_cast<T *>(smem_raw);  // S[c * R + r], column-major slab
   __shared__ T sk[32];
@@ -101,23 +112,34 @@ __global__ void __launch_bounds__(256) panel_lu_kernel(int m, int nb, T *__restr
     }
     block_argmax(key, idx, sk, si);
     T *my = cand[p] + (long)b * stride;
-    if (tid == 0) { my[0] = key; my[1] = idx == 0x7fffffff ? T(-1) : T(idx); }
+    if (sizeof(T) == sizeof(float)) {
+      if (tid == 0) atomicMax(winners + k, pack_candidate((float)key, idx));
+    } else if (tid == 0) {
+      my[0] = key;
+      my[1] = idx == 0x7fffffff ? T(-1) : T(idx);
+    }
     if (idx != 0x7fffffff)
       for (int c = tid; c < nb; c += blockDim.x) my[2 + c] = S[c * R + (idx - r0)];
     if (k >= r0 && k < r0 + rows)
       for (int c = tid; c < nb; c += blockDim.x) rowk[p][c] = S[c * R + (k - r0)];
     // 2. meet every CTA
     grid_barrier(ctl, nblk, gen);
-    // 3. global pivot: identical reduction in every CTA
-    key = T(-INFINITY);
-    idx = 0x7fffffff;
+    // 3. global pivot: identical in every CTA
     int win = 0;
-    for (int q = tid; q < nblk; q += blockDim.x) {
-      const T *cq = cand[p] + (long)q * stride;
-      const T kq = __ldcg(cq), rq = __ldcg(cq + 1);
-      better(key, idx, kq, rq < T(0) ? 0x7fffffff : (int)rq);
+    if (sizeof(T) == sizeof(float)) {
+      const unsigned long long w = __ldcg(winners + k);
+      idx = (int)(0xffffffffu - (unsigned)(w & 0xffffffffu));
+      if (idx < k || idx >= m) idx = 0x7fffffff;  // only after a barrier timeout
+    } else {
+      key = T(-INFINITY);
+      idx = 0x7fffffff;
+      for (int q = tid; q < nblk; q += blockDim.x) {
+        const T *cq = cand[p] + (long)q * stride;
+        const T kq = __ldcg(cq), rq = __ldcg(cq + 1);
+        better(key, idx, kq, rq < T(0) ? 0x7fffffff : (int)rq);
+      }
+      block_argmax(key, idx, sk, si);
     }
-    block_argmax(key, idx, sk, si);
     // locate the slot that holds row idx
     if (idx != 0x7fffffff) win = idx / R;
     const T *prow = cand[p] + (long)win * stride + 2;
@@ -180,7 +202,12 @@ int panel_lu(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *c
   nblk = ceil_div(m, R);
   const size_t smem = (size_t)R * nb * sizeof(T);
   void *xchg;
-  ZG_TRY(workspace(s, kSlotPanel, sizeof(T) * (2L * nblk * (nb + 2) + 2L * nb), &xchg));
+  const size_t nx = sizeof(T) * (2L * nblk * (nb + 2) + 2L * nb);
+  ZG_TRY(workspace(s, kSlotPanel, nx + 8 * (size_t)nb + 256, &xchg));
+  // per-column winner words (FP32 panels), zeroed per launch
+  unsigned long long *winners =
+      (unsigned long long *)(((uintptr_t)xchg + nx + 255) & ~(uintptr_t)255);
+  if (sizeof(T) == sizeof(float)) ZG_CUDA(cudaMemsetAsync(winners, 0, 8 * (size_t)nb, s));
   static bool attr_set[2] = {false, false};
   const int ti = sizeof(T) == 8 ? 0 : 1;
   if (!attr_set[ti]) {
@@ -191,7 +218,7 @@ int panel_lu(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *c
   // barrier counters are per launch
   ZG_CUDA(cudaMemsetAsync(&ctl->barrier[0], 0, 2 * sizeof(unsigned), s));
   T *xp = (T *)xchg;
-  void *args[] = {&m, &nb, &A, &lda, &ipiv, &ipiv_base, &ctl, &info_base, &R, &xp};
+  void *args[] = {&m, &nb, &A, &lda, &ipiv, &ipiv_base, &ctl, &info_base, &R, &xp, &winners};
   ZG_LAUNCH(kTagPanel, 1.0 * m * nb * nb, 2.0 * sizeof(T) * m * nb, s,
             ZG_CUDA(cudaLaunchCooperativeKernel((void *)panel_lu_kernel<T>, dim3(nblk), dim3(256),
                                                 args, smem, s)));
@@ -485,7 +512,8 @@ int na_panel(const NaDevice &d, int m, int nb, double *A, long lda, int *ipiv, i
   nblk = ceil_div(m, R);
   const size_t smem = (size_t)R * nb * sizeof(double);
   ZG_CUDA(cudaMemsetAsync(&ctl->barrier[0], 0, 2 * sizeof(unsigned), s));
-  void *args[] = {&m, &nb, &A, &lda, &ipiv, &base, &ctl, &base, &R, &xchg};
+  unsigned long long *winners = nullptr;  // used by FP32 panels only
+  void *args[] = {&m, &nb, &A, &lda, &ipiv, &base, &ctl, &base, &R, &xchg, &winners};
   ZG_LAUNCH(kTagPanel, 1.0 * m * nb * nb, 2.0 * sizeof(double) * m * nb, s,
             ZG_CUDA(cudaLaunchCooperativeKernel((void *)panel_lu_kernel<double>, dim3(nblk),
                                                 dim3(256), args, smem, s)));
