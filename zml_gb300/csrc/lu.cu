@@ -232,56 +232,69 @@ int panel_lu(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *c
 // them in parallel, so no column walks a chain of dependent swaps.
 constexpr int kSwapMax = 256;  // pivots per composed chunk
 
-__global__ void laswp_prep_kernel(int k1, int k2, const int *__restrict__ ipiv, int incx,
-                                  int *pairs, int *npairs) {
-  constexpr int kHash = 1024;        // open-addressing table of touched outside rows
-  __shared__ int seg[kSwapMax];      // content of rows base .. base+len-1
-  __shared__ int orow[kSwapMax];     // rows outside the segment that were touched
-  __shared__ int ocont[kSwapMax];    // and their contents
-  __shared__ int hkey[kHash], hval[kHash];
-  __shared__ int piv[kSwapMax];      // the chunk's pivots, staged once
-  const int lane = threadIdx.x;
+__global__ void __launch_bounds__(256) laswp_prep_kernel(int k1, int k2,
+                                                         const int *__restrict__ ipiv, int incx,
+                                                         int *pairs, int *npairs) {
+  __shared__ int seg[kSwapMax];    // content of rows base .. base+len-1
+  __shared__ int piv[kSwapMax];    // the chunk's pivots (0-based target rows)
+  __shared__ int first[kSwapMax];  // for an outside target: index of its first occurrence
+  __shared__ int ocont[kSwapMax];  // content of the outside row first named at that index
+  __shared__ int np;
+  const int t = threadIdx.x;
   const int base = k1 - 1, len = k2 - k1 + 1;
-  for (int t = lane; t < len; t += 32) {
-    seg[t] = base + t;
-    piv[t] = ipiv[base + t] - 1;
+  if (t == 0) np = 0;
+  for (int i = t; i < len; i += blockDim.x) {
+    seg[i] = base + i;
+    piv[i] = ipiv[base + i] - 1;
   }
-  for (int t = lane; t < kHash; t += 32) hkey[t] = -1;
-  __syncwarp();
-  if (lane != 0) return;
-  int nout = 0;
-  for (int st = 0; st < len; ++st) {
-    const int i = incx > 0 ? base + st : base + len - 1 - st;
-    const int p = piv[i - base];
-    if (p == i) continue;
-    if (p >= base && p < base + len) {
-      const int t = seg[i - base];
-      seg[i - base] = seg[p - base];
-      seg[p - base] = t;
-    } else {
-      unsigned h = ((unsigned)p * 2654435761u) >> 22;
-      while (hkey[h] != -1 && hkey[h] != p) h = (h + 1) & (kHash - 1);
-      int idx;
-      if (hkey[h] == p) {
-        idx = hval[h];
+  __syncthreads();
+  // outside targets: the first index naming the same row owns its slot
+  for (int i = t; i < len; i += blockDim.x) {
+    const int p = piv[i];
+    int f = -1;
+    if (p < base || p >= base + len) {
+      f = i;
+      for (int j = 0; j < i; ++j)
+        if (piv[j] == p) { f = j; break; }
+      if (f == i) ocont[i] = p;
+    }
+    first[i] = f;
+  }
+  __syncthreads();
+  // the interchanges in application order, shared memory only
+  if (t == 0) {
+    for (int st = 0; st < len; ++st) {
+      const int i = incx > 0 ? st : len - 1 - st;
+      const int p = piv[i];
+      if (p == base + i) continue;
+      const int f = first[i];
+      if (f < 0) {
+        const int q = p - base, tmp = seg[i];
+        seg[i] = seg[q];
+        seg[q] = tmp;
       } else {
-        idx = nout++;
-        hkey[h] = p;
-        hval[h] = idx;
-        orow[idx] = p;
-        ocont[idx] = p;
+        const int tmp = seg[i];
+        seg[i] = ocont[f];
+        ocont[f] = tmp;
       }
-      const int t = seg[i - base];
-      seg[i - base] = ocont[idx];
-      ocont[idx] = t;
     }
   }
-  int np = 0;
-  for (int t = 0; t < len; ++t)
-    if (seg[t] != base + t) { pairs[2 * np] = base + t; pairs[2 * np + 1] = seg[t]; ++np; }
-  for (int t = 0; t < nout; ++t)
-    if (ocont[t] != orow[t]) { pairs[2 * np] = orow[t]; pairs[2 * np + 1] = ocont[t]; ++np; }
-  *npairs = np;
+  __syncthreads();
+  // every row whose content changed is one (destination, source) pair
+  for (int i = t; i < len; i += blockDim.x) {
+    if (seg[i] != base + i) {
+      const int k = atomicAdd(&np, 1);
+      pairs[2 * k] = base + i;
+      pairs[2 * k + 1] = seg[i];
+    }
+    if (first[i] == i && ocont[i] != piv[i]) {
+      const int k = atomicAdd(&np, 1);
+      pairs[2 * k] = piv[i];
+      pairs[2 * k + 1] = ocont[i];
+    }
+  }
+  __syncthreads();
+  if (t == 0) *npairs = np;
 }
 
 // 32 columns per CTA: all moved values of the 32 columns are staged in shared
@@ -291,16 +304,28 @@ __global__ void __launch_bounds__(256) laswp_apply_kernel(int n, T *A, long lda,
                                                           const int *__restrict__ pairs,
                                                           const int *__restrict__ npairs) {
   extern __shared__ __align__(16) unsigned char lsw_raw[];
-  T *stage = reinterpret_cast<T *>(lsw_raw);  // stage[t * 32 + lane]
+  int *pr = reinterpret_cast<int *>(lsw_raw);                       // the pairs, staged
+  T *stage = reinterpret_cast<T *>(lsw_raw + sizeof(int) * 4 * kSwapMax);  // stage[t * 32 + lane]
   const int np = *npairs;
+  for (int e = threadIdx.x; e < 2 * np; e += blockDim.x) pr[e] = pairs[e];
+  __syncthreads();
   const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
   const int c = blockIdx.x * 32 + lane;
   T *col = A + (long)c * lda;
-  if (c < n)
-    for (int t = g; t < np; t += 8) stage[t * 32 + lane] = col[__ldg(pairs + 2 * t + 1)];
+  if (c < n) {
+    int t = g;
+    for (; t + 56 < np; t += 64) {  // eight loads in flight per thread
+      T v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = col[pr[2 * (t + 8 * u) + 1]];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) stage[(t + 8 * u) * 32 + lane] = v[u];
+    }
+    for (; t < np; t += 8) stage[t * 32 + lane] = col[pr[2 * t + 1]];
+  }
   __syncthreads();
   if (c < n)
-    for (int t = g; t < np; t += 8) col[__ldg(pairs + 2 * t)] = stage[t * 32 + lane];
+    for (int t = g; t < np; t += 8) col[pr[2 * t]] = stage[t * 32 + lane];
 }
 
 // A composed row interchange: device pairs (dst, src) and their count.
@@ -317,18 +342,18 @@ static int laswp_compose(int k1, int k2, const int *ipiv, int incx, SwapPlan *pl
   plan->np = plan->pairs + 4 * kSwapMax;
   plan->rows = k2 - k1 + 1;
   ZG_LAUNCH(kTagLaswp, 0, 0, s,
-            laswp_prep_kernel<<<1, 32, 0, s>>>(k1, k2, ipiv, incx, plan->pairs, plan->np));
+            laswp_prep_kernel<<<1, 256, 0, s>>>(k1, k2, ipiv, incx, plan->pairs, plan->np));
   return 0;
 }
 
 template <typename T>
 static int laswp_apply(int n, T *A, long lda, const SwapPlan &plan, cudaStream_t s) {
   if (n <= 0 || plan.rows <= 0) return 0;
-  const size_t smem = sizeof(T) * 32 * 2 * plan.rows;
+  const size_t smem = sizeof(int) * 4 * kSwapMax + sizeof(T) * 32 * 2 * plan.rows;
   static bool attr = false;
   if (!attr) {
     ZG_CUDA(cudaFuncSetAttribute(laswp_apply_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(sizeof(T) * 32 * 2 * kSwapMax)));
+                                 (int)(sizeof(int) * 4 * kSwapMax + sizeof(T) * 32 * 2 * kSwapMax)));
     attr = true;
   }
   ZG_LAUNCH(kTagLaswp, 0, 4.0 * sizeof(T) * n * plan.rows, s,
@@ -491,7 +516,8 @@ int noalloc_setup(NaDevice **out) {
                                  d.smem_optin - 4096));
     ZG_CUDA(cudaFuncSetAttribute(laswp_apply_kernel<double>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(sizeof(double) * 32 * 2 * kSwapMax)));
+                                 (int)(sizeof(int) * 4 * kSwapMax +
+                                       sizeof(double) * 32 * 2 * kSwapMax)));
     d.scratch = (unsigned char *)p;
   }
   *out = &d;
@@ -524,8 +550,8 @@ int na_laswp(int n, double *A, long lda, int k1, int k2, const int *ipiv, int *p
              cudaStream_t s) {
   if (n <= 0 || k2 < k1) return 0;
   int *np = pairs + 4 * kSwapMax;
-  ZG_LAUNCH(kTagLaswp, 0, 0, s, laswp_prep_kernel<<<1, 32, 0, s>>>(k1, k2, ipiv, 1, pairs, np));
-  const size_t smem = sizeof(double) * 32 * 2 * (k2 - k1 + 1);
+  ZG_LAUNCH(kTagLaswp, 0, 0, s, laswp_prep_kernel<<<1, 256, 0, s>>>(k1, k2, ipiv, 1, pairs, np));
+  const size_t smem = sizeof(int) * 4 * kSwapMax + sizeof(double) * 32 * 2 * (k2 - k1 + 1);
   ZG_LAUNCH(kTagLaswp, 0, 4.0 * sizeof(double) * n * (k2 - k1 + 1), s,
             laswp_apply_kernel<double><<<ceil_div(n, 32), 256, smem, s>>>(n, A, lda, pairs, np));
   return 0;
