@@ -59,6 +59,9 @@ def parse():
                    help="systems in the batched workload (20000 = the batched config)")
     p.add_argument("--batched-autotune", type=int, default=1,
                    help="autotune the per-size warp schedule first (1/0)")
+    p.add_argument("--suite", type=int, default=1,
+                   help="also measure the FP64 drop-in (LU, Cholesky, QR) and the mixed-precision "
+                        "kappa sweep and n=32768 throughput once each (1/0)")
     return p.parse_args()
 
 
@@ -313,6 +316,158 @@ def batched_bench(torch, zg, L, dev, st, steps, warmup, hbm, rank=0, world=1, di
     return out
 
 
+# ---------------------------------------------------------------------------
+# Once-each measurements of the other configurations (not part of `value`):
+# the plain FP64 drop-in (LU and Cholesky at n = 8192 / 16384 with 1 and 64
+# right-hand sides, QR of a 32768 x 4096 matrix) and the mixed-precision solver
+# on A = U diag(s) V^T with kappa in {1e2, 1e6, 1e10} at n = 8192 and on an
+# n = 32768 Gaussian system.  Inputs are seeded and generated on the device.
+def suite_bench(torch, zg, L, dev, st):
+    sh = st.cuda_stream
+    U = 2.0 ** -53
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        r = fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3, r
+
+    def berr_of(M, X, B):  # M: logical matrix; X, B: n x nrhs
+        R = B - M @ X
+        return (R.abs().max(0).values / (M.abs().sum(1).max() * X.abs().max(0).values
+                                          + B.abs().max(0).values)).max().item()
+
+    out = {"fp64": {}, "mixed": {}}
+    g = torch.Generator(device=dev).manual_seed(2)
+    # ---- FP64 drop-in ----
+    for n in (8192, 16384):
+        S = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)  # storage of A^T
+        M = S.t()
+        row = {}
+        F = S.clone()
+        piv = torch.zeros(n, dtype=torch.int32, device=dev)
+        info = (C.c_int * 1)()
+        t, _ = timed(lambda: L.zml_gpu_dgetrf(n, n, F.data_ptr(), n, piv.data_ptr(), info, sh))
+        row["getrf_s"], row["getrf_tflops"] = t, (2.0 * n ** 3 / 3) / t / 1e12
+        for nrhs in (1, 64):
+            Bs = torch.rand(nrhs, n, dtype=torch.float64, device=dev, generator=g) * 2 - 1
+            Xs = Bs.clone()
+            t, _ = timed(lambda: L.zml_gpu_dgetrs(b"N", n, nrhs, F.data_ptr(), n, piv.data_ptr(),
+                                                  Xs.data_ptr(), n, sh))
+            row["getrs_%d_ms" % nrhs] = 1e3 * t
+            row["lu_berr_%d" % nrhs] = berr_of(M, Xs.t(), Bs.t())
+        del F
+        # SPD G G^T / n + I (the product formed in FP32, then symmetrised in FP64)
+        Sf = S.float()
+        P = (Sf @ Sf.t()).double() / n
+        P = (P + P.t()) / 2 + torch.eye(n, dtype=torch.float64, device=dev)
+        del Sf, S, M
+        F = P.clone()
+        t, _ = timed(lambda: L.zml_gpu_dpotrf(b"L", n, F.data_ptr(), n, info, sh))
+        row["potrf_s"], row["potrf_tflops"] = t, (n ** 3 / 3.0) / t / 1e12
+        row["potrf_info"] = info[0]
+        for nrhs in (1, 64):
+            Bs = torch.rand(nrhs, n, dtype=torch.float64, device=dev, generator=g) * 2 - 1
+            Xs = Bs.clone()
+            t, _ = timed(lambda: L.zml_gpu_dpotrs(b"L", n, nrhs, F.data_ptr(), n, Xs.data_ptr(), n,
+                                                  sh))
+            row["potrs_%d_ms" % nrhs] = 1e3 * t
+            row["chol_berr_%d" % nrhs] = berr_of(P, Xs.t(), Bs.t())
+        del F, P
+        out["fp64"]["n%d" % n] = row
+    # QR 32768 x 4096: column norms of A against those of R (size-independent check)
+    m, nq = 32768, 4096
+    Q = torch.randn(nq, m, dtype=torch.float64, device=dev, generator=g)  # column-major m x nq
+    norms = torch.linalg.norm(Q, dim=1)
+    tau = torch.zeros(nq, dtype=torch.float64, device=dev)
+    t, rc = timed(lambda: L.zml_gpu_dgeqrf(m, nq, Q.data_ptr(), m, tau.data_ptr(), sh))
+    Rn = torch.linalg.norm(torch.triu(Q.t()[:nq]), dim=0)
+    out["fp64"]["geqrf_32768x4096"] = {
+        "s": t, "tflops": (2.0 * m * nq * nq - 2.0 * nq ** 3 / 3) / t / 1e12, "rc": rc,
+        "max_rel_colnorm_dev": ((Rn - norms).abs() / norms).max().item()}
+    del Q, tau
+    # ---- mixed precision: kappa sweep at n = 8192 ----
+    n = 8192
+    U1, _ = torch.linalg.qr(torch.randn(n, n, dtype=torch.float64, device=dev, generator=g))
+    V1, _ = torch.linalg.qr(torch.randn(n, n, dtype=torch.float64, device=dev, generator=g))
+    for kappa in (1e2, 1e6, 1e10):
+        sv = kappa ** (-torch.arange(n, dtype=torch.float64, device=dev) / (n - 1))
+        M = (U1 * sv) @ V1.t()
+        S = M.t().contiguous()  # column-major storage of M
+        xt = torch.rand(n, 1, dtype=torch.float64, device=dev, generator=g) * 2 - 1
+        b = (M @ xt).contiguous()
+        F = S.clone()
+        piv = torch.zeros(n, dtype=torch.int32, device=dev)
+        info = (C.c_int * 1)()
+        bf = b.clone()
+        t64, _ = timed(lambda: (L.zml_gpu_dgetrf(n, n, F.data_ptr(), n, piv.data_ptr(), info, sh),
+                                L.zml_gpu_dgetrs(b"N", n, 1, F.data_ptr(), n, piv.data_ptr(),
+                                                 bf.data_ptr(), n, sh)))
+        target = berr_of(M, bf, b)
+        del F
+        row = {"fp64_lu_s": t64, "fp64_lu_berr": target}
+        for prec, name in ((3, "bf16x3"), (2, "fp32")):
+            X = torch.zeros_like(b)
+            res = zg.MpirResult()
+            L.zml_gpu_dgesv_mpir(n, 1, S.data_ptr(), n, b.data_ptr(), n, X.data_ptr(), n, prec, 1,
+                                 target, 30, res, sh)  # warm
+            t, rc = timed(lambda: L.zml_gpu_dgesv_mpir(n, 1, S.data_ptr(), n, b.data_ptr(), n,
+                                                       X.data_ptr(), n, prec, 1, target, 30, res,
+                                                       sh))
+            row["lu_" + name] = {"s": t, "rc": rc, "info": res.info, "converged": bool(res.converged),
+                                 "outer": res.iters, "gmres": res.inner_iters,
+                                 "switched_f64": bool(res.switched_f64),
+                                 "berr": berr_of(M, X, b), "speedup_vs_fp64": t64 / t}
+        # the precision ladder without the selector (BF16 -> ... -> FP64 LU)
+        X = torch.zeros_like(b)
+        ares = zg.AutoResult()
+        t, rc = timed(lambda: L.zml_gpu_dgesv_auto(n, 1, S.data_ptr(), n, b.data_ptr(), n,
+                                                   X.data_ptr(), n, None, 0.9, 10,
+                                                   C.byref(ares), sh))
+        row["ladder"] = {"s": t, "rc": rc, "used": ["bf16", "fp16", "bf16x3", "fp32", "fp64"][ares.used],
+                         "attempts": ares.attempts, "converged": bool(ares.converged),
+                         "berr": berr_of(M, X, b)}
+        # SPD with the same spectrum: U diag(s) U^T
+        P = (U1 * sv) @ U1.t()
+        P = (P + P.t()) / 2
+        bp = (P @ xt).contiguous()
+        X = torch.zeros_like(bp)
+        res = zg.MpirResult()
+        L.zml_gpu_dposv_mpir(b"L", n, 1, P.data_ptr(), n, bp.data_ptr(), n, X.data_ptr(), n, 3, 1,
+                             target, 30, res, sh)
+        t, rc = timed(lambda: L.zml_gpu_dposv_mpir(b"L", n, 1, P.data_ptr(), n, bp.data_ptr(), n,
+                                                   X.data_ptr(), n, 3, 1, target, 30, res, sh))
+        row["cholesky_bf16x3"] = {"s": t, "rc": rc, "info": res.info,
+                                  "converged": bool(res.converged),
+                                  "outer": res.iters, "gmres": res.inner_iters,
+                                  "berr": berr_of(P, X, bp)}
+        out["mixed"]["n8192_kappa%.0e" % kappa] = row
+        del M, S, P
+    del U1, V1
+    # ---- mixed precision throughput: n = 32768 Gaussian ----
+    n = 32768
+    S = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
+    xt = torch.rand(n, 1, dtype=torch.float64, device=dev, generator=g) * 2 - 1
+    b = (S.t() @ xt).contiguous()
+    X = torch.zeros_like(b)
+    res = zg.MpirResult()
+    tol = 64 * U
+    L.zml_gpu_dgesv_mpir(n, 1, S.data_ptr(), n, b.data_ptr(), n, X.data_ptr(), n, 3, 1, tol, 30,
+                         res, sh)
+    t, rc = timed(lambda: L.zml_gpu_dgesv_mpir(n, 1, S.data_ptr(), n, b.data_ptr(), n,
+                                               X.data_ptr(), n, 3, 1, tol, 30, res, sh))
+    out["mixed"]["n32768_gaussian"] = {
+        "s": t, "rc": rc, "tol": tol, "converged": bool(res.converged), "outer": res.iters,
+        "gmres": res.inner_iters, "berr": berr_of(S.t(), X, b),
+        "fp64_equiv_tflops": (2.0 * n ** 3 / 3) / t / 1e12}
+    del S
+    torch.cuda.empty_cache()
+    return out
+
+
 def main():
     a = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -462,6 +617,7 @@ def main():
     e2e_ok = bool(torch.allclose(xh.to(dev), X, rtol=0, atol=1e-9))
 
     hbm, bf16, src = peaks()
+    suite = suite_bench(torch, zg, L, dev, st) if (a.suite and rank == 0) else None
     batched = (batched_bench(torch, zg, L, dev, st, a.steps, a.warmup, hbm, rank, world, dist,
                              a.batched_count, bool(a.batched_autotune)) if a.batched else None)
 
@@ -513,6 +669,7 @@ def main():
                 "d2h_bytes_per_step": 8 * n, "matches_device_result": e2e_ok},
         "roofline": roof, "kernel_breakdown": breakdown, "gpu_launches": int(launches),
         "batched": batched,
+        "suite": suite,
         "clocks": clk.summary(), "cpu_baseline": cpu,
     }
     print(json.dumps(out))

@@ -1029,9 +1029,10 @@ static int mpir_refine(MpirCtx &c, const MpirOpts &o, int nrhs, const double *B,
     const double tol = o.tol > 0 ? o.tol : 0.0;
     while (it < o.max_iter) {
       if (berr <= tol) break;
-      if (tol == 0.0 && it > 0 && berr > 0.5 * prev) {
+      if (it > 0 && berr > 0.5 * prev) {
         // no progress: with FP32 application, retry in FP64 arithmetic
-        // (ill-conditioned factors); otherwise the floor is reached
+        // (ill-conditioned factors); otherwise the floor is reached, or the
+        // factors cannot take the error down to tol -- stop either way
         if (f.f64 || o.apply != kApplyAuto || berr < 1e3 * 1.1102230246251565e-16) break;
         f.f64 = true;
         res->switched_f64 = 1;
