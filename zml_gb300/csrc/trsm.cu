@@ -113,14 +113,125 @@ int transpose_dev(int rows, int cols, const T *src, long lds, T *dst, long ldd, 
   return 0;
 }
 
+// Left diagonal-block solve for at most 8 right-hand sides: one warp per
+// column of B, lane l holding rows l and l + 32 in registers; x_k goes to
+// every lane by shuffle, so a step needs no block barrier.  The arithmetic
+// per element is that of trsm_diag_kernel (divide by a(k,k), then
+// b_i -= a(i,k) x_k in step order).
+template <typename T>
+__global__ void __launch_bounds__(256) trsm_diag_few_kernel(int nbk, int nrhs,
+                                                            const T *__restrict__ A, long lda,
+                                                            bool transA, bool lower_eff, bool unit,
+                                                            T *B, long ldb) {
+  __shared__ T As[kTrsmNB][kTrsmNB + 1];  // As[i][k] = op(A)(i, k)
+  for (int e = threadIdx.x; e < nbk * nbk; e += blockDim.x) {
+    const int i = e % nbk, k = e / nbk;
+    const T v = A[i + (long)k * lda];
+    if (transA) As[k][i] = v; else As[i][k] = v;
+  }
+  __syncthreads();
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (w >= nrhs) return;
+  T *b = B + (long)w * ldb;
+  const int i0 = lane, i1 = lane + 32;
+  T x0 = i0 < nbk ? b[i0] : T(0), x1 = i1 < nbk ? b[i1] : T(0);
+  for (int s = 0; s < nbk; ++s) {
+    const int k = lower_eff ? s : nbk - 1 - s;
+    const T v0 = __shfl_sync(0xffffffffu, x0, k & 31), v1 = __shfl_sync(0xffffffffu, x1, k & 31);
+    T xk = k < 32 ? v0 : v1;
+    if (!unit) {
+      xk = xk / As[k][k];
+      if (i0 == k) x0 = xk;
+      if (i1 == k) x1 = xk;
+    }
+    if (i0 < nbk && (lower_eff ? i0 > k : i0 < k)) x0 -= As[i0][k] * xk;
+    if (i1 < nbk && (lower_eff ? i1 > k : i1 < k)) x1 -= As[i1][k] * xk;
+  }
+  if (i0 < nbk) b[i0] = x0;
+  if (i1 < nbk) b[i1] = x1;
+}
+
+constexpr int kFewRhsMax = 8;  // trsm_diag_few_kernel: one warp per right-hand side
+
+
 template <typename T>
 static int diag_solve(int nbk, int nrhs, const T *A, long lda, bool transA, bool right,
                       bool lower_eff, bool unit, T *B, long ldb, cudaStream_t s) {
   if (nbk <= 0 || nrhs <= 0) return 0;
+  if (!right && nrhs <= kFewRhsMax) {
+    ZG_LAUNCH(kTagTrsmDiag, 1.0 * nbk * nbk * nrhs, sizeof(T) * (1.0 * nbk * nbk + 2.0 * nbk * nrhs),
+              s, trsm_diag_few_kernel<T><<<1, 256, 0, s>>>(nbk, nrhs, A, lda, transA, lower_eff,
+                                                           unit, B, ldb));
+    return 0;
+  }
   int grid = ceil_div(nrhs, kTrsmNC);
   ZG_LAUNCH(kTagTrsmDiag, 1.0 * nbk * nbk * nrhs, sizeof(T) * (1.0 * nbk * nbk + 2.0 * nbk * nrhs), s, trsm_diag_kernel<T><<<grid, 256, 0, s>>>(nbk, nrhs, A, lda, transA, right, lower_eff, unit, B,
                                            ldb));
   ZG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// Block update of a left solve with few right-hand sides (n <= kSkinny):
+// C (m x n) -= op(A) (m x k) X (k x n), k <= 64.  A CTA covers 32 rows; its
+// 8 warps each take 8 of the k columns (eight loads in flight per thread, a
+// warp's loads contiguous along the rows), and the 8 partial sums of each
+// row are added in shared memory in a fixed order.  A GEMM tile would spend
+// a whole 64 x 64 output tile of FP64 work per column here.
+constexpr int kSkinny = 16;
+template <typename T>
+__global__ void __launch_bounds__(256) skinny_update_kernel(int m, int n, int k, bool tr,
+                                                            const T *__restrict__ A, long lda,
+                                                            const T *__restrict__ X, long ldx,
+                                                            T *__restrict__ C, long ldc) {
+  __shared__ T xs[kTrsmNB * kSkinny];          // xs[q * n + j] = X(q, j)
+  __shared__ T red[8][32][kSkinny + 1];        // partial sums by k-slice
+  for (int e = threadIdx.x; e < k * n; e += blockDim.x) {
+    const int q = e % k, j = e / k;
+    xs[q * n + j] = X[q + (long)j * ldx];
+  }
+  __syncthreads();
+  const int lr = threadIdx.x & 31, ks = threadIdx.x >> 5;
+  const int i = blockIdx.x * 32 + lr;
+  T acc[kSkinny];
+#pragma unroll
+  for (int j = 0; j < kSkinny; ++j) acc[j] = T(0);
+  if (i < m) {
+    const int q0 = ks * 8;
+    T a[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int q = q0 + u;
+      a[u] = q < k ? (tr ? A[q + (long)i * lda] : A[i + (long)q * lda]) : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int q = q0 + u;
+      if (q < k)
+#pragma unroll
+        for (int j = 0; j < kSkinny; ++j)
+          if (j < n) acc[j] = fma(a[u], xs[q * n + j], acc[j]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < kSkinny; ++j)
+    if (j < n) red[ks][lr][j] = acc[j];
+  __syncthreads();
+  if (ks == 0 && i < m)
+    for (int j = 0; j < n; ++j) {
+      T sum = red[0][lr][j];
+#pragma unroll
+      for (int q = 1; q < 8; ++q) sum += red[q][lr][j];
+      C[i + (long)j * ldc] -= sum;
+    }
+}
+
+template <typename T>
+static int skinny_update(int m, int n, int k, bool tr, const T *A, long lda, const T *X, long ldx,
+                         T *C, long ldc, cudaStream_t s) {
+  if (m <= 0) return 0;
+  ZG_LAUNCH(kTagGemmSimt, 2.0 * m * n * k, sizeof(T) * ((double)m * k + 2.0 * m * n), s,
+            skinny_update_kernel<T><<<ceil_div(m, 32), 256, 0, s>>>(m, n, k, tr, A, lda, X, ldx,
+                                                                     C, ldc));
   return 0;
 }
 
@@ -144,12 +255,18 @@ int trsm_dev(int side, int uplo, int transa, int diag, int m, int n, T alpha, co
       if (lower_eff && kb + nbk < m) {  // B[kb+nbk:] -= op(A)[kb+nbk:, kb:kb+nbk] X
         const int rows = m - kb - nbk;
         const T *Ab = tr ? A + kb + (long)(kb + nbk) * lda : A + (kb + nbk) + (long)kb * lda;
-        ZG_TRY(gemm_simt<T>(tr ? kTrans : kNoTrans, kNoTrans, rows, n, nbk, T(-1), Ab, lda, B + kb,
-                            ldb, T(1), B + kb + nbk, ldb, 0, s));
+        if (n <= kSkinny)
+          ZG_TRY(skinny_update<T>(rows, n, nbk, tr, Ab, lda, B + kb, ldb, B + kb + nbk, ldb, s));
+        else
+          ZG_TRY(gemm_simt<T>(tr ? kTrans : kNoTrans, kNoTrans, rows, n, nbk, T(-1), Ab, lda,
+                              B + kb, ldb, T(1), B + kb + nbk, ldb, 0, s));
       } else if (!lower_eff && kb > 0) {  // B[0:kb] -= op(A)[0:kb, kb:kb+nbk] X
         const T *Ab = tr ? A + kb : A + (long)kb * lda;
-        ZG_TRY(gemm_simt<T>(tr ? kTrans : kNoTrans, kNoTrans, kb, n, nbk, T(-1), Ab, lda, B + kb,
-                            ldb, T(1), B, ldb, 0, s));
+        if (n <= kSkinny)
+          ZG_TRY(skinny_update<T>(kb, n, nbk, tr, Ab, lda, B + kb, ldb, B, ldb, s));
+        else
+          ZG_TRY(gemm_simt<T>(tr ? kTrans : kNoTrans, kNoTrans, kb, n, nbk, T(-1), Ab, lda, B + kb,
+                              ldb, T(1), B, ldb, 0, s));
       }
     }
   } else {
