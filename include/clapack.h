@@ -195,7 +195,7 @@ int zml_gpu_batched_execute(void *plan, double *dA, const double *dB, double *dX
 int zml_gpu_batched_run_graph(void *plan, double *dA, const double *dB, double *dX, int *dipiv,
                               int *dinfo, int *diters, void *stream);
 void zml_gpu_batched_plan_destroy(void *plan);
-/* Per-size-class warp schedule (warps per matrix; class i holds n <= edges[i]):
+/* Per-size-class warp schedule (warps per matrix: 1, 2, 4, 8 or 16; class i holds n <= edges[i]):
  * read (set = 0) or replace (set = 1).  Returns the number of classes. */
 int zml_gpu_batched_schedule(int prec, int *warps, int *edges, int cap, int set);
 /* Times every warp count for every class and keeps the fastest; chosen[i]

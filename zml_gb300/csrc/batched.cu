@@ -432,25 +432,45 @@ __device__ void process_matrix(const BatchArgs &a, int mi, int gid, int gt, int 
       group_sync(gid, nt);
     }
     if (sizeof(F) == sizeof(float)) {
-      double *R = a.R + a.b_off[mi];
       for (iters = 0; iters < a.max_ir; ++iters) {
+        // r = b - A x in FP64, one thread per row and four right-hand sides
+        // at a time (each element of A loaded once per four columns; for an
+        // SPD matrix the stored lower triangle supplies the upper half by
+        // columns), rounded to FP32 straight into the correction vector
         double rmax = 0, xmax = 0;
-        for (int e = gt; e < n * nrhs; e += nt) {
-          const int i = e % n, c = e / n;
-          double acc = Bg[i + (long)c * n];
-          for (int j = 0; j < n; ++j) {
-            const double v =
-                spd ? (i >= j ? Ag[i + (long)j * n] : Ag[j + (long)i * n]) : Ag[i + (long)j * n];
-            acc -= v * Xg[j + (long)c * n];
+        for (int c0 = 0; c0 < nrhs; c0 += 4) {
+          const int nc = min(4, nrhs - c0);
+          const double *Xc = Xg + (long)c0 * n;
+          for (int i = gt; i < n; i += nt) {
+            double acc[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) acc[u] = u < nc ? Bg[i + (long)(c0 + u) * n] : 0.0;
+            const int jl = spd ? i + 1 : n;
+            for (int j = 0; j < jl; ++j) {
+              const double v = Ag[i + (long)j * n];
+#pragma unroll
+              for (int u = 0; u < 4; ++u)
+                if (u < nc) acc[u] = fma(-v, Xc[j + (long)u * n], acc[u]);
+            }
+            if (spd)
+              for (int j = i + 1; j < n; ++j) {
+                const double v = Ag[j + (long)i * n];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                  if (u < nc) acc[u] = fma(-v, Xc[j + (long)u * n], acc[u]);
+              }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+              if (u < nc) {
+                Vf[i + (long)(c0 + u) * n] = (float)acc[u];
+                rmax = fmax(rmax, fabs(acc[u]));
+                xmax = fmax(xmax, fabs(Xc[i + (long)u * n]));
+              }
           }
-          R[e] = acc;
-          rmax = fmax(rmax, fabs(acc));
-          xmax = fmax(xmax, fabs(Xg[e]));
         }
         rmax = group_max(rmax, gt, nt, gid, red[gid]);
         xmax = group_max(xmax, gt, nt, gid, red[gid]);
         if (rmax <= 4.0 * 1.1102230246251565e-16 * anorm * xmax) break;
-        for (int e = gt; e < n * nrhs; e += nt) Vf[e] = (float)R[e];
         group_sync(gid, nt);
         solve_inplace<F, float>(M, n, spd, ipiv, Vf, n, nrhs, gt, nt, gid);
         for (int e = gt; e < n * nrhs; e += nt) Xg[e] += (double)Vf[e];
