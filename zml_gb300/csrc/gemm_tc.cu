@@ -107,28 +107,38 @@ __global__ void __launch_bounds__(256)
   }
   __syncwarp();
 
-  // Epilogue: every warp waits for the accumulator, then drains its 32 rows.
+  // Epilogue.  Every warp first loads its part of the old C (beta != 0) into
+  // registers, so those loads overlap the MMAs still in flight, then waits
+  // for the accumulator and drains its 32 rows.
+  const int quarter = warp & 3, half = warp >> 2;
+  const int row = m0 + quarter * 32 + lane;
+  constexpr int kCols = BN / 2, kChunks = kCols / 32;
+  float old[kChunks][32];
+  const bool pre = beta != 0.f && row < M && K > 0;
+#pragma unroll
+  for (int q = 0; q < kChunks; ++q) {
+    const int c = half * kCols + q * 32;
+    const float *base = C + row + (long)(n0 + c) * ldc;
+    const int nc = min(32, N - (n0 + c));
+#pragma unroll
+    for (int j = 0; j < 32; ++j) old[q][j] = (pre && j < nc) ? __ldcs(base + (long)j * ldc) : 0.f;
+  }
   const bool have = tc::mbar_wait(done, 0, status);
   tc::tc_fence_after();
   if (have && K > 0) {
-    const int quarter = warp & 3, half = warp >> 2;
-    const int row = m0 + quarter * 32 + lane;
     const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16);
-    constexpr int kCols = BN / 2;
-#pragma unroll 1
-    for (int c = half * kCols; c < (half + 1) * kCols; c += 32) {
+#pragma unroll
+    for (int q = 0; q < kChunks; ++q) {
+      const int c = half * kCols + q * 32;
       float v[32];
       tc::tmem_ld32(trow + c, v);
       if (row < M) {
         float *base = C + row + (long)(n0 + c) * ldc;
         const int nc = min(32, N - (n0 + c));
         if (beta != 0.f) {
-          float old[32];
-#pragma unroll
-          for (int j = 0; j < 32; ++j) old[j] = j < nc ? __ldcs(base + (long)j * ldc) : 0.f;
 #pragma unroll
           for (int j = 0; j < 32; ++j)
-            if (j < nc) __stcs(base + (long)j * ldc, fmaf(alpha, v[j], beta * old[j]));
+            if (j < nc) __stcs(base + (long)j * ldc, fmaf(alpha, v[j], beta * old[q][j]));
         } else {
 #pragma unroll
           for (int j = 0; j < 32; ++j)
