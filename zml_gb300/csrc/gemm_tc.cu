@@ -218,11 +218,12 @@ int gemm_tc(int M, int N, int K, float alpha, const void *A, long lda, const voi
   if (M <= 0 || N <= 0) return 0;
   if (K <= 0) return scale_dev<float>(M, N, beta, C, ldc, s);
   if (ab_type != 0 && ab_type != 1) return kErrInvalid;
-  // short K (the factorization updates): two stages, so three CTAs share an
-  // SM and one CTA's epilogue overlaps the others' main loops; long K: four.
+  // short K: two stages; longer K (768 for the split-BF16 updates): three.
+  // Either way two CTAs share an SM (128 registers x 256 threads each), so
+  // one CTA's epilogue overlaps the other's main loop.
   if (K <= 256)
     return launch<128, 2>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, ab_type, status, tri, s);
-  return launch<128, 4>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, ab_type, status, tri, s);
+  return launch<128, 3>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, ab_type, status, tri, s);
 }
 
 }  // namespace zg
