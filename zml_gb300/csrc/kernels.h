@@ -47,6 +47,11 @@ int laswp_panel(int c_left, int c_right, int n, T *A, long lda, int k1, int k2, 
 template <typename T>
 int panel_lu(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *ctl, int info_base,
              cudaStream_t s);
+// The same panel (FP32, m >= nb, nb <= 128, m <= 32768) factored by one
+// thread-block cluster; *launched is false when the shape or the device
+// leaves it to panel_lu.
+int panel_lu_cluster(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base, Control *ctl,
+                     int info_base, cudaStream_t s, bool *launched);
 template <typename T>
 int getrf_dev(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s);
 template <typename T>

@@ -401,6 +401,18 @@ int laswp_panel(int c_left, int c_right, int n, T *A, long lda, int k1, int k2, 
 
 template <typename T> static int lu_block() { return sizeof(T) == 8 ? 64 : 128; }
 
+// FP32 panels go to the cluster-resident panel where it applies.
+template <typename T>
+static int panel_any(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *ctl,
+                     int info_base, cudaStream_t s) {
+  if constexpr (sizeof(T) == sizeof(float)) {
+    bool done = false;
+    ZG_TRY(panel_lu_cluster(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, &done));
+    if (done) return 0;
+  }
+  return panel_lu<T>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s);
+}
+
 template <typename T>
 int getrf_dev(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s) {
   *info = 0;
@@ -412,7 +424,7 @@ int getrf_dev(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s
   for (int j = 0; j < mn; j += nb) {
     const int jb = min(nb, mn - j);
     T *Ajj = A + j + (long)j * lda;
-    ZG_TRY(panel_lu<T>(m - j, jb, Ajj, lda, ipiv + j, j, ctl, j, s));
+    ZG_TRY(panel_any<T>(m - j, jb, Ajj, lda, ipiv + j, j, ctl, j, s));
     ZG_TRY(laswp_panel<T>(j, std::min(n, j + jb), n, A, lda, j + 1, j + jb, ipiv, s));
     if (j + jb < n) {
       T *Aright = A + (long)(j + jb) * lda;

@@ -281,10 +281,14 @@ int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cud
   for (int j = 0; j < n; j += NB) {
     const int jb = std::min(NB, n - j);
     ZG_CUDA(cudaMemsetAsync(Linv, 0, sizeof(float) * NB * NB, s));
-    // panel: two cooperative FP32 half-panels with an FP32 update between
+    // panel: two FP32 half-panels (one cluster each) with an update between
     for (int p = 0; p < jb; p += NBP) {
       const int r = j + p, pb = std::min(NBP, jb - p);
-      ZG_TRY(panel_lu<float>(n - r, pb, A + r + (long)r * lda, lda, ipiv + r, r, ctl, r, s));
+      bool done = false;
+      ZG_TRY(panel_lu_cluster(n - r, pb, A + r + (long)r * lda, lda, ipiv + r, r, ctl, r, s,
+                              &done));
+      if (!done)
+        ZG_TRY(panel_lu<float>(n - r, pb, A + r + (long)r * lda, lda, ipiv + r, r, ctl, r, s));
       const int right = j + jb - r - pb;
       // interchanges of this half-panel inside the panel's other columns
       ZG_TRY(laswp_panel<float>(r - j, r + pb - j, jb, A + (long)j * lda, lda, r + 1, r + pb,
