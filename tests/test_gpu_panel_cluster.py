@@ -9,8 +9,9 @@ per 128-column block.  Against the oracle's sgetrf on the same inputs:
   * normwise backward error ||PA-LU||/(||A|| max(m,n) u32) below 8 and never
     above 4x the oracle's own;
   * info (first zero pivot) identical, ties resolved to the lowest row.
-Panel heights cover one CTA, a partly filled last CTA, 16 CTAs of 1024 rows
-and the 4-rows-a-thread layout (m > 16384); widths cover 32-column
+Panel heights cover one CTA, a partly filled last CTA, thread counts that are
+not multiples of 64, 16 CTAs of 2 rows a thread and the 4-rows-a-thread
+layout (m > 16384); widths cover 32-column
 sub-panels and ragged last sub-panels.
 """
 import numpy as np
@@ -68,7 +69,7 @@ def gauss32(m, n, seed):
     return np.asfortranarray(rng.standard_normal((m, n)).astype(np.float32))
 
 
-@pytest.mark.parametrize("m,n", [(128, 128), (700, 128), (1024, 128), (1025, 128),
+@pytest.mark.parametrize("m,n", [(128, 128), (700, 128), (1024, 128), (1025, 128), (2500, 128), (2600, 96),
                                  (5000, 128), (16384, 128), (20000, 128), (32768, 128),
                                  (3000, 100), (3000, 77), (2048, 1), (4096, 33)])
 def test_panel_vs_oracle(m, n):

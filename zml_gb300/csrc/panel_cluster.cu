@@ -10,9 +10,11 @@
 // memory before it, so a column takes one barrier and no dependent global
 // read.
 //
-// Layout.  Up to 16 CTAs of 512 threads form one cluster; CTA q owns the
-// panel rows [q R, (q+1) R), R = 512 RPT, and thread t owns rows
-// q R + t + 512 i, i < RPT.  The panel is factored in sub-panels of W
+// Layout.  Up to 16 CTAs of T <= 512 threads form one cluster; CTA q owns
+// the panel rows [q R, (q+1) R), R = T RPT, and thread t owns rows
+// q R + t + T i, i < RPT.  T is the smallest multiple of 32 (at least 128
+// and enough for nb rows) that spreads the rows over 16 CTAs, so shorter
+// panels get less work a thread.  The panel is factored in sub-panels of W
 // columns (W RPT = 64 FP32 registers a thread).  Within a sub-panel the
 // columns not yet factored live in registers, rotated so that the current
 // column is always register 0 (every register index stays static and the
@@ -20,9 +22,10 @@
 //   per column k: local argmax (one packed 64-bit word: |v| order bits above
 //   the inverted row, so the maximum is the largest |v|, lowest row on a
 //   tie) folded with a shared-memory atomicMax; the CTA's winning row, its
-//   word and the old row k are pushed into every CTA's exchange slots; one
-//   cluster barrier; every warp reduces the words with shuffles, and every
-//   CTA swaps, scales and updates its rows.
+//   word and the old row k are pushed into every CTA's exchange slots with
+//   st.async, each store completing its bytes on the destination's mbarrier
+//   (no cluster barrier, no fence); every CTA waits for its own mbarrier,
+//   reduces the words with redux.sync, swaps, scales and updates its rows.
 // Between sub-panels: the sub-panel is written back; its interchanges are
 // composed into (destination, source) pairs and applied to the panel's other
 // columns (column-partitioned over the CTAs); U12 = L11^-1 A12 is solved by
@@ -31,6 +34,7 @@
 // into registers.
 #include "common.cuh"
 #include "kernels.h"
+#include "tc_common.cuh"
 
 namespace zg {
 namespace {
@@ -67,6 +71,19 @@ __device__ __forceinline__ void st_cluster(unsigned addr, float v) {
 __device__ __forceinline__ void st_cluster(unsigned addr, unsigned long long v) {
   asm volatile("st.shared::cluster.u64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
 }
+// Remote stores that complete their bytes on the destination CTA's mbarrier.
+__device__ __forceinline__ void st_async(unsigned addr, float v, unsigned mbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.f32 [%0], %1, [%2];" ::"r"(
+                   addr),
+               "f"(v), "r"(mbar)
+               : "memory");
+}
+__device__ __forceinline__ void st_async(unsigned addr, unsigned long long v, unsigned mbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(
+                   addr),
+               "l"(v), "r"(mbar)
+               : "memory");
+}
 
 // Candidate word of row `row` with value v for pivot column k: a NaN counts
 // as +inf on the diagonal and as -inf below it; -inf orders below every
@@ -77,20 +94,38 @@ __device__ __forceinline__ unsigned long long pc_word(float v, int row, int k) {
   const unsigned ord = key == -INFINITY ? 0u : __float_as_uint(key) + 1u;
   return ((unsigned long long)ord << 32) | (unsigned)(0xffffffffu - (unsigned)row);
 }
+// Warp maximum of 64-bit words: the high halves first, then the low halves
+// among the lanes that hold the highest one.
+__device__ __forceinline__ unsigned long long warp_max64(unsigned long long w) {
+  const unsigned hi = (unsigned)(w >> 32), lo = (unsigned)w;
+  const unsigned mh = __reduce_max_sync(~0u, hi);
+  const unsigned ml = __reduce_max_sync(~0u, hi == mh ? lo : 0u);
+  return ((unsigned long long)mh << 32) | ml;
+}
 __device__ __forceinline__ int pc_row(unsigned long long w) {
   return (int)(0xffffffffu - (unsigned)(w & 0xffffffffu));
 }
 
+// Exchange buffers are used round robin over three columns: a column's
+// pivot row is still read (by the deferred update) while the next column's
+// pushes land, and the column after that cannot push before this CTA has
+// pushed the next one.
+constexpr int kPcBuf = 3;
+
 struct __align__(16) PcShared {
-  float slot[2][kPcMaxCta][kPcSlot];  // candidate rows pushed by every CTA (parity k & 1)
-  float rowk[2][32];                  // row k before the interchange, pushed by CTA 0
-  float cand[32];                     // this CTA's winning row, staged for the push
-  float krow[32];                     // row k, staged by its owner
-  unsigned long long cmax[2];         // this CTA's best candidate word (atomicMax)
-  unsigned long long skey[2][kPcMaxCta];  // every CTA's best word, pushed by that CTA
-  int piv[32];                        // pivot rows of the sub-panel (panel-relative)
-  int mdst[64], msrc[64];             // the sub-panel's interchanges, composed
-  float L11[32][33];                  // unit-lower diagonal block of the sub-panel
+  // Exchanged rows at column kk, 64 words: [c] = column kk + 1 + c (zero
+  // past the register window), [32] = column kk, [33 + c] = finished column
+  // c < kk.
+  float slot[kPcBuf][kPcMaxCta][kPcSlot];  // candidate rows pushed by every CTA
+  float rowk[kPcBuf][kPcSlot];             // row k before the interchange, pushed by CTA 0
+  float cand[33];                          // this CTA's winning row (register part), staged
+  float krow[33];                          // row k (register part), staged by its owner
+  unsigned long long cmax[2];              // this CTA's best candidate word (atomicMax)
+  unsigned long long skey[kPcBuf][kPcMaxCta];  // every CTA's best word, pushed by that CTA
+  uint64_t mbar[kPcBuf];                   // completes when a column's pushes have all landed
+  int piv[32];                             // pivot rows of the sub-panel (panel-relative)
+  int mdst[64], msrc[64];                  // the sub-panel's interchanges, composed
+  float L11[32][33];                       // unit-lower diagonal block of the sub-panel
   alignas(16) float U[kPcMaxRight][kPcUStride];  // U12 by right column: U[c][k]
 };
 
@@ -110,15 +145,25 @@ __global__ void __launch_bounds__(kPcThreads, 1)
                          int ipiv_base, Control *ctl, int info_base) {
   static_assert(W <= 32 && W % 4 == 0 && RPT * W <= 64, "sub-panel shape");
   __shared__ PcShared sh;
-  extern __shared__ __align__(16) float Lsm[];  // finished columns: Lsm[c R + local row]
+  extern __shared__ __align__(16) float Lsm[];  // finished columns: Lsm[c LD + local row]
   const int rank = (int)cl_rank(), nct = (int)cl_size();
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  constexpr int R = kPcThreads * RPT;
+  const int T = blockDim.x, nwarps = T >> 5, R = T * RPT;
+  const int LD = R + 1;  // Lsm column stride, odd: a row's finished columns hit distinct banks
   const int r0 = rank * R;
   float v[RPT][W];
-  for (int e = tid; e < 2 * kPcMaxCta * kPcSlot; e += kPcThreads) (&sh.slot[0][0][0])[e] = 0.f;
+  for (int e = tid; e < kPcBuf * kPcMaxCta * kPcSlot; e += T) (&sh.slot[0][0][0])[e] = 0.f;
+  // bytes landing in this CTA per column: every CTA's candidate row (two
+  // words a lane) and word, and row k from CTA 0
+  const unsigned xbytes = nct * (2 * 32 * 4 + 8) + 2 * 32 * 4;
   if (tid < 2) sh.cmax[tid] = 0;
-  // every CTA of the cluster runs, and its slots are zero, before any remote write
+  if (tid == 0) {
+    for (int q = 0; q < kPcBuf; ++q) tc::mbar_init(&sh.mbar[q], 1);
+    tc::fence_barrier_init();
+    for (int q = 0; q < kPcBuf; ++q) tc::mbar_expect_tx(&sh.mbar[q], xbytes);
+  }
+  // every CTA of the cluster runs, and its slots and mbarriers are ready,
+  // before any remote write
   cl_sync();
 
   for (int c0 = 0; c0 < nb; c0 += W) {
@@ -126,63 +171,81 @@ __global__ void __launch_bounds__(kPcThreads, 1)
     // A. the thread's rows of the sub-panel
 #pragma unroll
     for (int i = 0; i < RPT; ++i) {
-      const int row = r0 + tid + i * kPcThreads;
+      const int row = r0 + tid + i * T;
 #pragma unroll
       for (int c = 0; c < W; ++c)
         v[i][c] = (row < m && c < ws) ? __ldcg(A + row + (long)(c0 + c) * lda) : 0.f;
     }
 
-    // B. factor the sub-panel, one cluster barrier per column.  v[i][c]
-    // holds column kk + c of the thread's rows; Lsm holds columns < kk.
+    // B. factor the sub-panel, one exchange per column.  v[i][c] holds
+    // column kk + c of the thread's rows; Lsm holds columns < kk.
 #pragma unroll 1
     for (int kk = 0; kk < ws; ++kk) {
-      const int k = c0 + kk, par = k & 1;
+      const int k = c0 + kk, par = k & 1, b = k % kPcBuf;
       unsigned long long best = 0;
 #pragma unroll
       for (int i = 0; i < RPT; ++i) {
-        const int row = r0 + tid + i * kPcThreads;
+        const int row = r0 + tid + i * T;
         if (row >= k && row < m) best = max(best, pc_word(v[i][0], row, k));
       }
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) best = max(best, __shfl_xor_sync(~0u, best, off));
+      best = warp_max64(best);
       if (lane == 0 && best != 0) atomicMax(&sh.cmax[par], best);
       __syncthreads();
       // every thread has read the previous column's word: clear it for the next
       if (tid == 0) sh.cmax[par ^ 1] = 0;
       const unsigned long long cbest = sh.cmax[par];
       const int wrow = cbest != 0 ? pc_row(cbest) : -1;
+      // owners stage the register part of the CTA's winning row and of row k:
+      // [c] = column kk + 1 + c, [32] = column kk
 #pragma unroll
       for (int i = 0; i < RPT; ++i) {
-        const int row = r0 + tid + i * kPcThreads, lr = tid + i * kPcThreads;
+        const int row = r0 + tid + i * T;
         if (row == wrow || row == k) {
           float *dst = row == wrow ? sh.cand : sh.krow;
-          for (int c = 0; c < kk; ++c) dst[c] = Lsm[c * R + lr];
 #pragma unroll
-          for (int c = 0; c < W; ++c)
-            if (kk + c < W) dst[kk + c] = v[i][c];
+          for (int c = 0; c + 1 < W; ++c) dst[c] = v[i][c + 1];
+#pragma unroll
+          for (int c = W - 1; c < 32; ++c) dst[c] = 0.f;
+          dst[32] = v[i][0];
           if (row == wrow && row == k)
-            for (int c = 0; c < W; ++c) sh.krow[c] = sh.cand[c];
+#pragma unroll
+            for (int c = 0; c < 33; ++c) sh.krow[c] = sh.cand[c];
         }
       }
       __syncthreads();
-      if (warp == 0) {
-        const float val = lane < W ? sh.cand[lane] : 0.f;
-        for (int d = 0; d < nct; ++d) {
-          st_cluster(remote_addr(&sh.slot[par][rank][lane], d), val);
-          if (lane == 0) st_cluster(remote_addr(&sh.skey[par][rank], d), cbest);
+      // warp w pushes to CTAs w, w + nwarps, ...: the candidate, its word,
+      // and (CTA 0) row k
+      if (warp < nct) {
+        float lo = 0.f, hi = 0.f;
+        if (wrow >= 0) {
+          lo = sh.cand[lane];
+          hi = lane == 0 ? sh.cand[32] : (lane - 1 < kk ? Lsm[(lane - 1) * LD + (wrow - r0)] : 0.f);
         }
-      } else if (warp == 1 && rank == 0) {  // row k < nb <= R lies in CTA 0
-        const float val = lane < W ? sh.krow[lane] : 0.f;
-        for (int d = 0; d < nct; ++d) st_cluster(remote_addr(&sh.rowk[par][lane], d), val);
+        float klo = 0.f, khi = 0.f;
+        if (rank == 0) {  // row k < nb <= R lies in CTA 0
+          klo = sh.krow[lane];
+          khi = lane == 0 ? sh.krow[32] : (lane - 1 < kk ? Lsm[(lane - 1) * LD + k] : 0.f);
+        }
+        for (int d = warp; d < nct; d += nwarps) {
+          const unsigned mb = remote_addr(&sh.mbar[b], d);
+          st_async(remote_addr(&sh.slot[b][rank][lane], d), lo, mb);
+          st_async(remote_addr(&sh.slot[b][rank][32 + lane], d), hi, mb);
+          if (lane == 0) st_async(remote_addr(&sh.skey[b][rank], d), cbest, mb);
+          if (rank == 0) {
+            st_async(remote_addr(&sh.rowk[b][lane], d), klo, mb);
+            st_async(remote_addr(&sh.rowk[b][32 + lane], d), khi, mb);
+          }
+        }
       }
-      cl_sync();
+      // this column's pushes from every CTA have landed; then the buffer is
+      // armed for column k + kPcBuf
+      tc::mbar_wait(&sh.mbar[b], (k / kPcBuf) & 1, &ctl->status);
+      if (tid == 0) tc::mbar_expect_tx(&sh.mbar[b], xbytes);
       // the cluster's pivot, identical in every CTA
-      unsigned long long g = lane < nct ? sh.skey[par][lane] : 0ull;
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) g = max(g, __shfl_xor_sync(~0u, g, off));
+      const unsigned long long g = warp_max64(lane < nct ? sh.skey[b][lane] : 0ull);
       const int p = pc_row(g);
-      const float *prow = sh.slot[par][p / R];
-      const float piv = prow[kk];
+      const float *prow = sh.slot[b][p / R];
+      const float piv = prow[32];
       const bool swap = piv != 0.f && p != k;
       if (tid == 0) {
         sh.piv[kk] = swap ? p : k;
@@ -191,29 +254,62 @@ __global__ void __launch_bounds__(kPcThreads, 1)
           if (piv == 0.f) atomicCAS(&ctl->info, 0, k + 1 + info_base);
         }
       }
+      if (swap) {  // the finished part of rows k and p, one warp each
+        if (warp == nwarps - 2 && rank == 0 && lane < kk) Lsm[lane * LD + k] = prow[33 + lane];
+        if (warp == nwarps - 1 && p / R == rank && lane < kk)
+          Lsm[lane * LD + (p - r0)] = sh.rowk[b][33 + lane];
+      }
       const bool recip = fabsf(piv) >= Real<float>::sfmin();
       const float rp = 1.f / piv;
+      const int live = ws - 1 - kk;  // columns right of kk still to update
+      const float4 *p4 = reinterpret_cast<const float4 *>(prow);
 #pragma unroll
       for (int i = 0; i < RPT; ++i) {
-        const int row = r0 + tid + i * kPcThreads, lr = tid + i * kPcThreads;
+        const int row = r0 + tid + i * T, lr = tid + i * T;
         if (swap && (row == k || row == p)) {
-          const float *src = row == k ? prow : sh.rowk[par];
-          for (int c = 0; c < kk; ++c) Lsm[c * R + lr] = src[c];
+          const float *src = row == k ? prow : sh.rowk[b];
+          v[i][0] = src[32];
 #pragma unroll
-          for (int c = 0; c < W; ++c)
-            if (kk + c < W) v[i][c] = src[kk + c];
+          for (int c = 1; c < W; ++c) v[i][c] = src[c - 1];
         }
         float x = v[i][0];
         const bool below = row > k && row < m;
-        if (below && piv != 0.f) x = recip ? x * rp : x / piv;
-        Lsm[kk * R + lr] = x;
-        // rotate: column kk + 1 + c moves to register c
+        if (below && piv != 0.f) {
+          if (recip) x *= rp;
+          else x = x / piv;
+        }
+        Lsm[kk * LD + lr] = x;
+        // rotate: column kk + 1 + c moves to register c; only the first
+        // `live` positions carry data, the rest are zero.  Rows not below
+        // the pivot move without arithmetic (an inf in the pivot row must
+        // not reach them through 0 * inf).
         if (below) {
+          if (live > W / 2) {
 #pragma unroll
-          for (int c = 0; c + 1 < W; ++c) v[i][c] = fmaf(-x, prow[kk + 1 + c], v[i][c + 1]);
+            for (int j = 0; j < W / 4; ++j) {
+              const float4 q = p4[j];
+              v[i][4 * j + 0] = fmaf(-x, q.x, v[i][4 * j + 1]);
+              v[i][4 * j + 1] = fmaf(-x, q.y, v[i][4 * j + 2]);
+              v[i][4 * j + 2] = fmaf(-x, q.z, v[i][4 * j + 3]);
+              if (4 * j + 4 < W) v[i][4 * j + 3] = fmaf(-x, q.w, v[i][4 * j + 4]);
+            }
+          } else {
+#pragma unroll
+            for (int j = 0; j < W / 8; ++j) {
+              const float4 q = p4[j];
+              v[i][4 * j + 0] = fmaf(-x, q.x, v[i][4 * j + 1]);
+              v[i][4 * j + 1] = fmaf(-x, q.y, v[i][4 * j + 2]);
+              v[i][4 * j + 2] = fmaf(-x, q.z, v[i][4 * j + 3]);
+              v[i][4 * j + 3] = fmaf(-x, q.w, v[i][4 * j + 4]);
+            }
+          }
         } else {
 #pragma unroll
           for (int c = 0; c + 1 < W; ++c) v[i][c] = v[i][c + 1];
+        }
+        if (live <= W / 2) {
+#pragma unroll
+          for (int c = W / 2; c + 1 < W; ++c) v[i][c] = 0.f;
         }
         v[i][W - 1] = 0.f;
       }
@@ -223,10 +319,10 @@ __global__ void __launch_bounds__(kPcThreads, 1)
     // C. the factored sub-panel back to the panel; L21 into registers
 #pragma unroll
     for (int i = 0; i < RPT; ++i) {
-      const int row = r0 + tid + i * kPcThreads, lr = tid + i * kPcThreads;
+      const int row = r0 + tid + i * T, lr = tid + i * T;
 #pragma unroll
       for (int c = 0; c < W; ++c) {
-        v[i][c] = c < ws ? Lsm[c * R + lr] : 0.f;
+        v[i][c] = c < ws ? Lsm[c * LD + lr] : 0.f;
         if (row < m && c < ws) A[row + (long)(c0 + c) * lda] = v[i][c];
       }
     }
@@ -253,14 +349,15 @@ __global__ void __launch_bounds__(kPcThreads, 1)
     }
     __syncthreads();
     {
-      constexpr int kEnt = 2 * W, kCpr = kPcThreads / kEnt;  // entries per column, columns per round
+      constexpr int kEnt = 2 * W;  // entries per column
+      const int kCpr = T / kEnt;   // columns per round
       const int no = nb - ws;                                // the other columns
       const int mine = no > rank ? (no - rank + nct - 1) / nct : 0;
       const int e = tid % kEnt;
       const int dst = sh.mdst[e], src = sh.msrc[e];
       for (int base = 0; base < mine; base += kCpr) {
-        const int jl = base + tid / kEnt;
-        const bool act = jl < mine && dst >= 0;
+        const int jl = base + tid / kEnt;  // threads past kCpr whole columns sit out
+        const bool act = tid < kCpr * kEnt && jl < mine && dst >= 0;
         float val = 0.f;
         long col = 0;
         if (act) {
@@ -278,11 +375,11 @@ __global__ void __launch_bounds__(kPcThreads, 1)
     // G. U12 = L11^-1 A12 over the right columns, in every CTA
     const int nr = nb - c0 - ws;
     if (nr > 0) {
-      for (int e = tid; e < ws * ws; e += kPcThreads) {
+      for (int e = tid; e < ws * ws; e += T) {
         const int r = e % ws, c = e / ws;
         sh.L11[r][c] = __ldcg(A + (c0 + r) + (long)(c0 + c) * lda);
       }
-      for (int e = tid; e < ws * nr; e += kPcThreads) {
+      for (int e = tid; e < ws * nr; e += T) {
         const int r = e % ws, c = e / ws;
         sh.U[c][r] = __ldcg(A + (c0 + r) + (long)(c0 + ws + c) * lda);
       }
@@ -292,45 +389,52 @@ __global__ void __launch_bounds__(kPcThreads, 1)
 #pragma unroll
         for (int r = 0; r < W; ++r) u[r] = r < ws ? sh.U[tid][r] : 0.f;
 #pragma unroll
-        for (int r = 1; r < W; ++r)
+        for (int q = 0; q + 1 < W; ++q)
 #pragma unroll
-          for (int q = 0; q < r; ++q) u[r] = fmaf(-sh.L11[r][q], u[q], u[r]);
+          for (int r = q + 1; r < W; ++r) u[r] = fmaf(-sh.L11[r][q], u[q], u[r]);
 #pragma unroll
         for (int r = 0; r < W; ++r) sh.U[tid][r] = r < ws ? u[r] : 0.f;
       }
       __syncthreads();
       if (rank == 0)
-        for (int e = tid; e < ws * nr; e += kPcThreads) {
+        for (int e = tid; e < ws * nr; e += T) {
           const int r = e % ws, c = e / ws;
           A[(c0 + r) + (long)(c0 + ws + c) * lda] = sh.U[c][r];
         }
       // H. A22 -= L21 U12 on this CTA's rows below the sub-panel
       const int rs = c0 + ws;
+      // four columns a step; the next step's loads are issued before this
+      // step's arithmetic so their latency overlaps it
+      float a[4][RPT], an[4][RPT];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int i = 0; i < RPT; ++i) {
+          const int row = r0 + tid + i * T;
+          a[q][i] = (q < nr && row >= rs && row < m) ? __ldcg(A + row + (long)(rs + q) * lda) : 0.f;
+        }
       for (int cb = 0; cb < nr; cb += 4) {
-        float a[4][RPT];
 #pragma unroll
         for (int q = 0; q < 4; ++q)
 #pragma unroll
           for (int i = 0; i < RPT; ++i) {
-            const int row = r0 + tid + i * kPcThreads;
-            a[q][i] = (cb + q < nr && row >= rs && row < m)
-                          ? __ldcg(A + row + (long)(rs + cb + q) * lda)
-                          : 0.f;
+            const int row = r0 + tid + i * T, col = cb + 4 + q;
+            an[q][i] = (col < nr && row >= rs && row < m)
+                           ? __ldcg(A + row + (long)(rs + col) * lda)
+                           : 0.f;
           }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          if (cb + q < nr) {
-            const float *u = sh.U[cb + q];
+          const float *u = sh.U[min(cb + q, nr - 1)];
 #pragma unroll
-            for (int k4 = 0; k4 < W / 4; ++k4) {
-              const float4 uu = *reinterpret_cast<const float4 *>(u + 4 * k4);
+          for (int k4 = 0; k4 < W / 4; ++k4) {
+            const float4 uu = *reinterpret_cast<const float4 *>(u + 4 * k4);
 #pragma unroll
-              for (int i = 0; i < RPT; ++i) {
-                a[q][i] = fmaf(-v[i][4 * k4 + 0], uu.x, a[q][i]);
-                a[q][i] = fmaf(-v[i][4 * k4 + 1], uu.y, a[q][i]);
-                a[q][i] = fmaf(-v[i][4 * k4 + 2], uu.z, a[q][i]);
-                a[q][i] = fmaf(-v[i][4 * k4 + 3], uu.w, a[q][i]);
-              }
+            for (int i = 0; i < RPT; ++i) {
+              a[q][i] = fmaf(-v[i][4 * k4 + 0], uu.x, a[q][i]);
+              a[q][i] = fmaf(-v[i][4 * k4 + 1], uu.y, a[q][i]);
+              a[q][i] = fmaf(-v[i][4 * k4 + 2], uu.z, a[q][i]);
+              a[q][i] = fmaf(-v[i][4 * k4 + 3], uu.w, a[q][i]);
             }
           }
         }
@@ -338,8 +442,9 @@ __global__ void __launch_bounds__(kPcThreads, 1)
         for (int q = 0; q < 4; ++q)
 #pragma unroll
           for (int i = 0; i < RPT; ++i) {
-            const int row = r0 + tid + i * kPcThreads;
+            const int row = r0 + tid + i * T;
             if (cb + q < nr && row >= rs && row < m) A[row + (long)(rs + cb + q) * lda] = a[q][i];
+            a[q][i] = an[q][i];
           }
       }
     }
@@ -354,8 +459,15 @@ struct PcState {
 template <int RPT, int W>
 int launch_pc(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base, Control *ctl,
               int info_base, cudaStream_t s, bool *launched) {
-  constexpr int R = kPcThreads * RPT;
-  const int nct = ceil_div(m, R);
+  // rows spread over up to 16 CTAs; a CTA holds at least nb rows (row k of
+  // every column lies in CTA 0) and at most 512 RPT
+  int T = ceil_div(ceil_div(m, kPcMaxCta * RPT), 32) * 32;
+  T = std::max(T, ceil_div(ceil_div(nb, RPT), 32) * 32);
+  T = std::max(T, 128);
+  if (T > kPcThreads) return 0;
+  const int R = T * RPT, nct = ceil_div(m, R);
+  if (nct > kPcMaxCta) return 0;
+  const size_t lsm = sizeof(float) * (R + 1) * W;
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
@@ -363,26 +475,34 @@ int launch_pc(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base, Contr
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
   cfg.gridDim = dim3(nct);
-  cfg.blockDim = dim3(kPcThreads);
-  const size_t lsm = sizeof(float) * R * W;
+  cfg.blockDim = dim3(T);
   cfg.dynamicSmemBytes = lsm;
   cfg.stream = s;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  static PcState st[kPcMaxCta + 1];
-  if (!st[nct].checked) {
-    st[nct].checked = true;
+  // one check per variant on its largest shape: 16 CTAs of 512 threads
+  static PcState st;
+  if (!st.checked) {
+    st.checked = true;
+    const size_t lmax = sizeof(float) * (kPcThreads * RPT + 1) * W;
     ZG_CUDA(cudaFuncSetAttribute(panel_cluster_kernel<RPT, W>,
                                  cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     ZG_CUDA(cudaFuncSetAttribute(panel_cluster_kernel<RPT, W>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsm));
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lmax));
+    cudaLaunchConfig_t big = cfg;
+    cudaLaunchAttribute bat[1] = {at[0]};
+    bat[0].val.clusterDim.x = kPcMaxCta;
+    big.gridDim = dim3(kPcMaxCta);
+    big.blockDim = dim3(kPcThreads);
+    big.dynamicSmemBytes = lmax;
+    big.attrs = bat;
     int nclusters = 0;
     const cudaError_t e =
-        cudaOccupancyMaxActiveClusters(&nclusters, (void *)panel_cluster_kernel<RPT, W>, &cfg);
+        cudaOccupancyMaxActiveClusters(&nclusters, (void *)panel_cluster_kernel<RPT, W>, &big);
     if (e != cudaSuccess) (void)cudaGetLastError();
-    st[nct].ok = e == cudaSuccess && nclusters >= 1;
+    st.ok = e == cudaSuccess && nclusters >= 1;
   }
-  if (!st[nct].ok) return 0;
+  if (!st.ok) return 0;
   ZG_LAUNCH(kTagPanel, 1.0 * m * nb * nb, 2.0 * sizeof(float) * m * nb, s,
             ZG_CUDA(cudaLaunchKernelEx(&cfg, panel_cluster_kernel<RPT, W>, m, nb, A, lda, ipiv,
                                        ipiv_base, ctl, info_base)));
@@ -400,6 +520,8 @@ int panel_lu_cluster(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base
     return 0;
   }
   if (nb > kPcMaxNb || m < nb) return 0;
+  if (m <= kPcMaxCta * kPcThreads)
+    return launch_pc<1, 32>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, launched);
   if (m <= kPcMaxCta * kPcThreads * 2)
     return launch_pc<2, 32>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, launched);
   if (m <= kPcMaxCta * kPcThreads * 4)
