@@ -466,11 +466,17 @@ int gemv_d(int n, const double *A, long lda, const double *x, const double *b, d
 // The factor is cut into 128-row blocks.  One CTA per block row claims its
 // block in dependency order through a ticket, streams its off-diagonal tiles
 // L(blk, cb) (the load of the next tile is issued before waiting for the
-// flag of the current one, so the HBM stream overlaps the dependency chain),
+// current one's x, so the HBM stream overlaps the dependency chain),
 // accumulates L(blk, cb) x(cb) in FP64 as earlier blocks publish, and then
 // applies the FP64 inverse of its diagonal block (precomputed once per
 // factorization) and publishes x(blk).  lower = unit lower L (forward),
 // upper = non-unit upper U (backward).
+//
+// Publication needs no flag and no fence: x(blk) is written to a separate
+// buffer that starts filled with an all-ones word (a NaN no arithmetic
+// produces; a computed NaN is published in canonical form), and a consumer
+// polls the 8-byte words themselves, so the value arrives with the first
+// load that sees it.
 constexpr int kTB = 128;          // block rows
 constexpr int kTT = 512;          // threads: 128 rows x 4 column phases
 constexpr int kTC = kTB / 4;      // columns per phase and tile
@@ -485,20 +491,29 @@ __device__ __forceinline__ void trsv_load_tile(float (&v)[kTC], const float *A, 
 }
 
 // F = float: every product FP32 (GB300's FP64 rate is a small fraction of
-// FP32; right for well-conditioned factors).  F = double: products and the
-// diagonal inverse in FP64, for ill-conditioned factors where an FP32
-// triangular solve would not apply (LU)^-1.  Tile sums are accumulated in
-// FP64 in both forms; x stays FP64.
+// FP32; right for well-conditioned factors), tile sums accumulated as a
+// compensated FP32 pair.  F = double: products, sums and the diagonal
+// inverse in FP64, for ill-conditioned factors where an FP32 triangular
+// solve would not apply (LU)^-1.  x stays FP64.
+constexpr unsigned long long kTrsvEmpty = ~0ull;  // an unpublished x word
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const double *p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
 template <typename F>
 __global__ void __launch_bounds__(kTT) trsv_lowp_kernel(int n, const float *__restrict__ A, long lda,
                                                         const F *__restrict__ Dinv, double *x,
-                                                        unsigned *flags, unsigned *ticket,
+                                                        double *xpub, unsigned *ticket,
                                                         bool upper, unsigned *status) {
   extern __shared__ __align__(16) unsigned char tsv_raw[];
   F *DiS = reinterpret_cast<F *>(tsv_raw);  // this block's diagonal inverse, column-major
   __shared__ unsigned sb;
   __shared__ double part[4][kTB];
-  __shared__ F xs[kTB];
+  __shared__ float partf[2][4][kTB];
+  __shared__ F xs2[2][kTB];
   __shared__ F ys[kTB];
   const int tid = threadIdx.x;
   if (tid == 0) sb = atomicAdd(ticket, 1u);
@@ -518,38 +533,89 @@ __global__ void __launch_bounds__(kTT) trsv_lowp_kernel(int n, const float *__re
     for (int e = tid; e < words; e += kTT) dst[e] = __ldcs(src + e);
   }
   const double rhs = (ph == 0 && row_ok) ? x[row] : 0.0;
+  // FP32 forms: the running sum of tile products is an unevaluated pair
+  // (ah + al, TwoSum), as accurate as an FP64 accumulator for this length
+  // without touching the FP64 pipe; FP64 forms accumulate in FP64
   double acc = 0;
-  float cur[kTC], nxt[kTC];
-  if (t > 0) trsv_load_tile(cur, A, lda, row, row_ok, (upper ? nblk - 1 : 0) * kTB, ph, n);
-  for (int q = 0; q < t; ++q) {
-    const int cb = upper ? nblk - 1 - q : q;
-    if (q + 1 < t)
-      trsv_load_tile(nxt, A, lda, row, row_ok, (upper ? nblk - 2 - q : q + 1) * kTB, ph, n);
-    if (tid == 0) {
-      long long spins = 0;
-      while (ld_acquire(&flags[cb]) == 0u) {
-        if (++spins > kSpinLimit) { atomicOr(status, kStatusQueueTimeout); break; }
-        __nanosleep(20);
+  float ah = 0.f, al = 0.f;
+  // tiles in the order they become ready; A tiles prefetched two ahead and
+  // the next tile's x fetched while the current one is multiplied
+  auto tile_col = [&](int q) { return (upper ? nblk - 1 - q : q) * kTB; };
+  auto fetch_x = [&](int q, F *dst) {
+    if (tid < kTB) {
+      const int c = tile_col(q) + tid;
+      F xv = F(0);
+      if (c < n) {
+        unsigned long long w = ld_relaxed_u64(xpub + c);
+        long long spins = 0;
+        while (w == kTrsvEmpty) {
+          if (++spins > kSpinLimit) {
+            atomicOr(status, kStatusQueueTimeout);
+            break;
+          }
+          if (spins > 64) __nanosleep(32);
+          w = ld_relaxed_u64(xpub + c);
+        }
+        xv = (F)__longlong_as_double((long long)w);
       }
+      dst[tid] = xv;
     }
-    __syncthreads();
-    const int c0 = cb * kTB;
-    if (tid < kTB) xs[tid] = (c0 + tid < n) ? (F)__ldcg(x + c0 + tid) : F(0);
-    __syncthreads();
+  };
+  float cur[kTC], nxt[kTC], nn[kTC];
+  if (t > 0) {
+    trsv_load_tile(cur, A, lda, row, row_ok, tile_col(0), ph, n);
+    if (t > 1) trsv_load_tile(nxt, A, lda, row, row_ok, tile_col(1), ph, n);
+    fetch_x(0, xs2[0]);
+  }
+  __syncthreads();
+  for (int q = 0; q < t; ++q) {
+    if (q + 2 < t) trsv_load_tile(nn, A, lda, row, row_ok, tile_col(q + 2), ph, n);
+    if (q + 1 < t) fetch_x(q + 1, xs2[(q + 1) & 1]);
+    const F *xq = xs2[q & 1];
     F p0 = 0, p1 = 0;
 #pragma unroll
     for (int j = 0; j < kTC; j += 2) {
-      p0 = fma((F)cur[j], xs[ph + 4 * j], p0);
-      p1 = fma((F)cur[j + 1], xs[ph + 4 * (j + 1)], p1);
+      p0 = fma((F)cur[j], xq[ph + 4 * j], p0);
+      p1 = fma((F)cur[j + 1], xq[ph + 4 * (j + 1)], p1);
     }
-    acc += (double)p0 + (double)p1;
+    if constexpr (sizeof(F) == sizeof(float)) {
+      const float pt = p0 + p1, sum = ah + pt, bv = sum - ah;
+      al += (ah - (sum - bv)) + (pt - bv);
+      ah = sum;
+    } else {
+      acc += (double)p0 + (double)p1;
+    }
+    // x of tile q + 1 visible; xs2[q & 1] free for tile q + 2
+    __syncthreads();
 #pragma unroll
-    for (int j = 0; j < kTC; ++j) cur[j] = nxt[j];
+    for (int j = 0; j < kTC; ++j) {
+      cur[j] = nxt[j];
+      nxt[j] = nn[j];
+    }
   }
-  part[ph][lr] = acc;
+  if constexpr (sizeof(F) == sizeof(float)) {
+    partf[0][ph][lr] = ah;
+    partf[1][ph][lr] = al;
+  } else {
+    part[ph][lr] = acc;
+  }
   __syncthreads();
-  if (tid < kTB)
-    ys[tid] = row_ok ? (F)(rhs - (part[0][tid] + part[1][tid] + part[2][tid] + part[3][tid])) : F(0);
+  if (tid < kTB) {
+    double sum;
+    if constexpr (sizeof(F) == sizeof(float)) {
+      float sh_ = partf[0][0][tid], sl = partf[1][0][tid];
+#pragma unroll
+      for (int q = 1; q < 4; ++q) {
+        const float h = partf[0][q][tid], t2 = sh_ + h, bv = t2 - sh_;
+        sl += (sh_ - (t2 - bv)) + (h - bv) + partf[1][q][tid];
+        sh_ = t2;
+      }
+      sum = (double)sh_ + (double)sl;
+    } else {
+      sum = part[0][tid] + part[1][tid] + part[2][tid] + part[3][tid];
+    }
+    ys[tid] = row_ok ? (F)(rhs - sum) : F(0);
+  }
   __syncthreads();
   // x(blk) = inv(D) * rhs
   F y0 = 0, y1 = 0;
@@ -558,12 +624,20 @@ __global__ void __launch_bounds__(kTT) trsv_lowp_kernel(int n, const float *__re
     y0 = fma(DiS[lr + j * kTB], ys[j], y0);
     y1 = fma(DiS[lr + (j + 4) * kTB], ys[j + 4], y1);
   }
-  part[ph][lr] = (double)y0 + (double)y1;
+  if constexpr (sizeof(F) == sizeof(float))
+    partf[0][ph][lr] = y0 + y1;
+  else
+    part[ph][lr] = (double)y0 + (double)y1;
   __syncthreads();
-  if (tid < kTB && row_ok) x[row] = part[0][tid] + part[1][tid] + part[2][tid] + part[3][tid];
-  __threadfence();
-  __syncthreads();
-  if (tid == 0) atomicExch(&flags[blk], 1u);
+  if (tid < kTB && row_ok) {
+    double xv;
+    if constexpr (sizeof(F) == sizeof(float))
+      xv = (double)((partf[0][0][tid] + partf[0][1][tid]) + (partf[0][2][tid] + partf[0][3][tid]));
+    else
+      xv = part[0][tid] + part[1][tid] + part[2][tid] + part[3][tid];
+    x[row] = xv;
+    xpub[row] = xv != xv ? __longlong_as_double(0x7ff8000000000000ll) : xv;
+  }
 }
 
 // FP64 inverses of the kTB x kTB diagonal blocks of the FP32 LU factors:
@@ -646,13 +720,17 @@ int invert_diag_blocks(int n, const float *A, long lda, double *Linv, double *Ui
 
 // x <- op^-1 x with op = unit-lower L (upper=false) or non-unit upper U of
 // the FP32 LU factors in A, Dinv their diagonal-block inverses (FP32 or
-// FP64: the arithmetic of the solve).  work: n/128 + 1 unsigned words.
+// FP64: the arithmetic of the solve).  work: 8-byte aligned, trsv_work_bytes(n).
+size_t trsv_work_bytes(int n) { return sizeof(double) * ((size_t)n + 1); }
+
 template <typename F>
 int trsv_lowp(int n, const float *A, long lda, const F *Dinv, double *x, bool upper,
               unsigned *work, unsigned *status, cudaStream_t s) {
   if (n <= 0) return 0;
   const int nblk = ceil_div(n, kTB);
-  ZG_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned) * (nblk + 1), s));
+  double *xpub = reinterpret_cast<double *>(work) + 1;
+  ZG_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned), s));
+  ZG_CUDA(cudaMemsetAsync(xpub, 0xff, sizeof(double) * n, s));
   const size_t smem = sizeof(F) * kTB * kTB;
   static bool attr = false;
   if (!attr) {
@@ -661,7 +739,7 @@ int trsv_lowp(int n, const float *A, long lda, const F *Dinv, double *x, bool up
     attr = true;
   }
   ZG_LAUNCH(kTagTrsv, 1.0 * n * n, 2.0 * n * n + 16.0 * n + sizeof(F) * nblk * kTB * kTB, s,
-            trsv_lowp_kernel<F><<<nblk, kTT, smem, s>>>(n, A, lda, Dinv, x, work + 1, work, upper,
+            trsv_lowp_kernel<F><<<nblk, kTT, smem, s>>>(n, A, lda, Dinv, x, xpub, work, upper,
                                                         status));
   return 0;
 }
@@ -944,7 +1022,7 @@ static int mpir_factor(bool spd, bool lower, int n, const double *A, long lda, c
   LowLU f{LU, (long)n, perm, Linv, Uinv, Linv32, Uinv32, o.apply == kApplyF64};
   const int nparts = ceil_div(n, kGemvCols);
   const size_t nv = (size_t)n * (4 + nparts + (m + 1)) + 4 * (m + 2) + 64;
-  ZG_TRY(workspace(s, kSlotIRVec, sizeof(double) * nv + sizeof(unsigned) * (n / kTB + 8), &wv));
+  ZG_TRY(workspace(s, kSlotIRVec, sizeof(double) * nv + trsv_work_bytes(n), &wv));
   IRWork w;
   double *p = (double *)wv;
   w.r = p; p += n;
