@@ -297,35 +297,35 @@ __global__ void __launch_bounds__(256) laswp_prep_kernel(int k1, int k2,
   if (t == 0) *npairs = np;
 }
 
-// 32 columns per CTA: all moved values of the 32 columns are staged in shared
-// memory (every read completes before any write), then scattered.
+// One warp per column, lanes over the pairs: every moved value of the column
+// is loaded into registers (all loads of the column in flight at once, and
+// all inside one column's span of memory), then the warp stores them.
 template <typename T>
 __global__ void __launch_bounds__(256) laswp_apply_kernel(int n, T *A, long lda,
-                                                          const int *__restrict__ pairs,
-                                                          const int *__restrict__ npairs) {
-  extern __shared__ __align__(16) unsigned char lsw_raw[];
-  int *pr = reinterpret_cast<int *>(lsw_raw);                       // the pairs, staged
-  T *stage = reinterpret_cast<T *>(lsw_raw + sizeof(int) * 4 * kSwapMax);  // stage[t * 32 + lane]
+                                                               const int *__restrict__ pairs,
+                                                               const int *__restrict__ npairs) {
+  __shared__ int pr[4 * kSwapMax];
   const int np = *npairs;
   for (int e = threadIdx.x; e < 2 * np; e += blockDim.x) pr[e] = pairs[e];
   __syncthreads();
-  const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
-  const int c = blockIdx.x * 32 + lane;
-  T *col = A + (long)c * lda;
-  if (c < n) {
-    int t = g;
-    for (; t + 56 < np; t += 64) {  // eight loads in flight per thread
-      T v[8];
+  const int lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+  constexpr int kPer = 2 * kSwapMax / 32;  // pairs a lane holds at most
+  for (int c = blockIdx.x * wpb + (threadIdx.x >> 5); c < n; c += gridDim.x * wpb) {
+    T *col = A + (long)c * lda;
+    T v[kPer];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) v[u] = col[pr[2 * (t + 8 * u) + 1]];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) stage[(t + 8 * u) * 32 + lane] = v[u];
+    for (int u = 0; u < kPer; ++u) {
+      const int t = lane + 32 * u;
+      if (t < np) v[u] = col[pr[2 * t + 1]];
     }
-    for (; t < np; t += 8) stage[t * 32 + lane] = col[pr[2 * t + 1]];
+    __syncwarp();
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      const int t = lane + 32 * u;
+      if (t < np) col[pr[2 * t]] = v[u];
+    }
+    __syncwarp();
   }
-  __syncthreads();
-  if (c < n)
-    for (int t = g; t < np; t += 8) col[pr[2 * t]] = stage[t * 32 + lane];
 }
 
 // A composed row interchange: device pairs (dst, src) and their count.
@@ -349,16 +349,11 @@ static int laswp_compose(int k1, int k2, const int *ipiv, int incx, SwapPlan *pl
 template <typename T>
 static int laswp_apply(int n, T *A, long lda, const SwapPlan &plan, cudaStream_t s) {
   if (n <= 0 || plan.rows <= 0) return 0;
-  const size_t smem = sizeof(int) * 4 * kSwapMax + sizeof(T) * 32 * 2 * plan.rows;
-  static bool attr = false;
-  if (!attr) {
-    ZG_CUDA(cudaFuncSetAttribute(laswp_apply_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(sizeof(int) * 4 * kSwapMax + sizeof(T) * 32 * 2 * kSwapMax)));
-    attr = true;
-  }
+  DeviceInfo di;
+  ZG_TRY(device_info(&di));
+  const int grid = std::min(ceil_div(n, 8), di.num_sms * 8);
   ZG_LAUNCH(kTagLaswp, 0, 4.0 * sizeof(T) * n * plan.rows, s,
-            laswp_apply_kernel<T><<<ceil_div(n, 32), 256, smem, s>>>(n, A, lda, plan.pairs,
-                                                                      plan.np));
+            laswp_apply_kernel<T><<<grid, 256, 0, s>>>(n, A, lda, plan.pairs, plan.np));
   return 0;
 }
 
@@ -526,10 +521,6 @@ int noalloc_setup(NaDevice **out) {
     ZG_CUDA(cudaFuncSetAttribute(panel_lu_kernel<double>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  d.smem_optin - 4096));
-    ZG_CUDA(cudaFuncSetAttribute(laswp_apply_kernel<double>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(sizeof(int) * 4 * kSwapMax +
-                                       sizeof(double) * 32 * 2 * kSwapMax)));
     d.scratch = (unsigned char *)p;
   }
   *out = &d;
@@ -558,14 +549,14 @@ int na_panel(const NaDevice &d, int m, int nb, double *A, long lda, int *ipiv, i
   return 0;
 }
 
-int na_laswp(int n, double *A, long lda, int k1, int k2, const int *ipiv, int *pairs,
-             cudaStream_t s) {
+int na_laswp(const NaDevice &d, int n, double *A, long lda, int k1, int k2, const int *ipiv,
+             int *pairs, cudaStream_t s) {
   if (n <= 0 || k2 < k1) return 0;
   int *np = pairs + 4 * kSwapMax;
   ZG_LAUNCH(kTagLaswp, 0, 0, s, laswp_prep_kernel<<<1, 256, 0, s>>>(k1, k2, ipiv, 1, pairs, np));
-  const size_t smem = sizeof(int) * 4 * kSwapMax + sizeof(double) * 32 * 2 * (k2 - k1 + 1);
+  const int grid = std::min(ceil_div(n, 8), d.sms * 8);
   ZG_LAUNCH(kTagLaswp, 0, 4.0 * sizeof(double) * n * (k2 - k1 + 1), s,
-            laswp_apply_kernel<double><<<ceil_div(n, 32), 256, smem, s>>>(n, A, lda, pairs, np));
+            laswp_apply_kernel<double><<<grid, 256, 0, s>>>(n, A, lda, pairs, np));
   return 0;
 }
 
@@ -608,10 +599,10 @@ extern "C" int zml_gpu_dgetrf_noalloc(int m, int n, double *dA, int ldda, int *d
     const int jb = std::min(kNaNb, mn - j);
     double *Ajj = dA + j + (long)j * lda;
     ZG_TRY(na_panel(*d, m - j, jb, Ajj, lda, dipiv + j, j, ctl, xchg, s));
-    ZG_TRY(na_laswp(j, dA, lda, j + 1, j + jb, dipiv, pairs, s));
+    ZG_TRY(na_laswp(*d, j, dA, lda, j + 1, j + jb, dipiv, pairs, s));
     if (j + jb < n) {
       double *Aright = dA + (long)(j + jb) * lda;
-      ZG_TRY(na_laswp(n - j - jb, Aright, lda, j + 1, j + jb, dipiv, pairs, s));
+      ZG_TRY(na_laswp(*d, n - j - jb, Aright, lda, j + 1, j + jb, dipiv, pairs, s));
       ZG_TRY(trsm_dev<double>(kLeft, kLower, kNoTrans, kUnit, jb, n - j - jb, 1.0, Ajj, lda,
                               Aright + j, lda, s));
       if (j + jb < m)
