@@ -49,9 +49,12 @@ int panel_lu(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *c
              cudaStream_t s);
 // The same panel (FP32, m >= nb, nb <= 128, m <= 32768) factored by one
 // thread-block cluster; *launched is false when the shape or the device
-// leaves it to panel_lu.
+// leaves it to panel_lu.  The interchanges are also applied to the xl
+// columns at XL and the xr columns at XR (leading dim lda, rows aligned with
+// the panel's), as laswp would.
 int panel_lu_cluster(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base, Control *ctl,
-                     int info_base, cudaStream_t s, bool *launched);
+                     int info_base, cudaStream_t s, bool *launched, float *XL = nullptr,
+                     int xl = 0, float *XR = nullptr, int xr = 0);
 template <typename T>
 int getrf_dev(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s);
 template <typename T>

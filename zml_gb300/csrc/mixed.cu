@@ -284,15 +284,17 @@ int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cud
     // panel: two FP32 half-panels (one cluster each) with an update between
     for (int p = 0; p < jb; p += NBP) {
       const int r = j + p, pb = std::min(NBP, jb - p);
+      const int right = j + jb - r - pb;
+      // the half-panel, its interchanges applied inside the block's other columns
       bool done = false;
       ZG_TRY(panel_lu_cluster(n - r, pb, A + r + (long)r * lda, lda, ipiv + r, r, ctl, r, s,
-                              &done));
-      if (!done)
+                              &done, A + r + (long)j * lda, r - j, A + r + (long)(r + pb) * lda,
+                              right));
+      if (!done) {
         ZG_TRY(panel_lu<float>(n - r, pb, A + r + (long)r * lda, lda, ipiv + r, r, ctl, r, s));
-      const int right = j + jb - r - pb;
-      // interchanges of this half-panel inside the panel's other columns
-      ZG_TRY(laswp_panel<float>(r - j, r + pb - j, jb, A + (long)j * lda, lda, r + 1, r + pb,
-                                ipiv, s));
+        ZG_TRY(laswp_panel<float>(r - j, r + pb - j, jb, A + (long)j * lda, lda, r + 1, r + pb,
+                                  ipiv, s));
+      }
       // the half-panel's unit-lower diagonal block, inverted into L11^-1
       float *Dinv = Linv + p + (long)p * NB;
       ZG_TRY(inv_unit_lower(pb, A + r + (long)r * lda, lda, Dinv, NB, s));

@@ -28,7 +28,8 @@
 //   reduces the words with redux.sync, swaps, scales and updates its rows.
 // Between sub-panels: the sub-panel is written back; its interchanges are
 // composed into (destination, source) pairs and applied to the panel's other
-// columns (column-partitioned over the CTAs); U12 = L11^-1 A12 is solved by
+// columns and to up to two extra column ranges beside the panel (the rest of
+// the caller's column block), column-partitioned over the CTAs; U12 = L11^-1 A12 is solved by
 // every CTA into shared memory (CTA 0 writes it back) and each CTA updates
 // its own rows of the columns to the right, A22 -= L21 U12, with L21 loaded
 // into registers.
@@ -142,7 +143,8 @@ __device__ __forceinline__ int pc_trace(int x, int c0, int ws, const int *piv) {
 template <int RPT, int W>
 __global__ void __launch_bounds__(kPcThreads, 1)
     panel_cluster_kernel(int m, int nb, float *__restrict__ A, long lda, int *__restrict__ ipiv,
-                         int ipiv_base, Control *ctl, int info_base) {
+                         int ipiv_base, Control *ctl, int info_base, float *XL, int xl,
+                         float *XR, int xr) {
   static_assert(W <= 32 && W % 4 == 0 && RPT * W <= 64, "sub-panel shape");
   __shared__ PcShared sh;
   extern __shared__ __align__(16) float Lsm[];  // finished columns: Lsm[c LD + local row]
@@ -351,22 +353,25 @@ __global__ void __launch_bounds__(kPcThreads, 1)
     {
       constexpr int kEnt = 2 * W;  // entries per column
       const int kCpr = T / kEnt;   // columns per round
-      const int no = nb - ws;                                // the other columns
-      const int mine = no > rank ? (no - rank + nct - 1) / nct : 0;
+      const int no = nb - ws;                                // the other panel columns
+      const int ntot = no + xl + xr;                         // and the extra ranges
+      const int mine = ntot > rank ? (ntot - rank + nct - 1) / nct : 0;
       const int e = tid % kEnt;
       const int dst = sh.mdst[e], src = sh.msrc[e];
       for (int base = 0; base < mine; base += kCpr) {
         const int jl = base + tid / kEnt;  // threads past kCpr whole columns sit out
         const bool act = tid < kCpr * kEnt && jl < mine && dst >= 0;
         float val = 0.f;
-        long col = 0;
+        float *colp = A;
         if (act) {
           const int j = rank + jl * nct;
-          col = j < c0 ? j : j + ws;
-          val = __ldcg(A + src + col * lda);
+          if (j < no) colp = A + (long)(j < c0 ? j : j + ws) * lda;
+          else if (j < no + xl) colp = XL + (long)(j - no) * lda;
+          else colp = XR + (long)(j - no - xl) * lda;
+          val = __ldcg(colp + src);
         }
         __syncthreads();
-        if (act) A[dst + col * lda] = val;
+        if (act) colp[dst] = val;
       }
     }
     __threadfence();
@@ -458,7 +463,8 @@ struct PcState {
 
 template <int RPT, int W>
 int launch_pc(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base, Control *ctl,
-              int info_base, cudaStream_t s, bool *launched) {
+              int info_base, cudaStream_t s, bool *launched, float *XL, int xl, float *XR,
+              int xr) {
   // rows spread over up to 16 CTAs; a CTA holds at least nb rows (row k of
   // every column lies in CTA 0) and at most 512 RPT
   int T = ceil_div(ceil_div(m, kPcMaxCta * RPT), 32) * 32;
@@ -505,7 +511,7 @@ int launch_pc(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base, Contr
   if (!st.ok) return 0;
   ZG_LAUNCH(kTagPanel, 1.0 * m * nb * nb, 2.0 * sizeof(float) * m * nb, s,
             ZG_CUDA(cudaLaunchKernelEx(&cfg, panel_cluster_kernel<RPT, W>, m, nb, A, lda, ipiv,
-                                       ipiv_base, ctl, info_base)));
+                                       ipiv_base, ctl, info_base, XL, xl, XR, xr)));
   *launched = true;
   return 0;
 }
@@ -513,19 +519,23 @@ int launch_pc(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base, Contr
 }  // namespace
 
 int panel_lu_cluster(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base, Control *ctl,
-                     int info_base, cudaStream_t s, bool *launched) {
+                     int info_base, cudaStream_t s, bool *launched, float *XL, int xl, float *XR,
+                     int xr) {
   *launched = false;
   if (m <= 0 || nb <= 0) {
     *launched = true;
     return 0;
   }
-  if (nb > kPcMaxNb || m < nb) return 0;
+  if (nb > kPcMaxNb || m < nb || xl < 0 || xr < 0) return 0;
   if (m <= kPcMaxCta * kPcThreads)
-    return launch_pc<1, 32>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, launched);
+    return launch_pc<1, 32>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, launched, XL, xl,
+                            XR, xr);
   if (m <= kPcMaxCta * kPcThreads * 2)
-    return launch_pc<2, 32>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, launched);
+    return launch_pc<2, 32>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, launched, XL, xl,
+                            XR, xr);
   if (m <= kPcMaxCta * kPcThreads * 4)
-    return launch_pc<4, 16>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, launched);
+    return launch_pc<4, 16>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, launched, XL, xl,
+                            XR, xr);
   return 0;
 }
 
