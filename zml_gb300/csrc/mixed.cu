@@ -140,75 +140,58 @@ static int to_kmajor_n(int prec, int k, int cols, const float *A, long lda, void
 // getrf.zig:104-114; here the factors only precondition the refinement.)
 
 // X (nb x nb, ld ldx) <- L^-1 for the unit-lower nb x nb block L (ld ldl),
-// nb <= 128; one CTA of 256 threads, everything in shared memory.  L is padded
-// to 128 with the identity; the 16 x 16 diagonal blocks are inverted by
-// substitution (one column per thread), then pairs of inverted blocks are
-// merged level by level, [A^-1 0; C B^-1] -> off-diagonal block -B^-1 C A^-1,
-// as two small matrix products over all threads.
+// nb <= 128.
 constexpr int kInvN = 128, kInvLd = kInvN + 1;
-__global__ void __launch_bounds__(256) inv_unit_lower_kernel(int nb, const float *__restrict__ L,
-                                                             long ldl, float *__restrict__ X,
-                                                             long ldx) {
-  extern __shared__ __align__(16) float ism[];
-  float *sL = ism;                    // sL[i * kInvLd + k] = L(i, k), padded
-  float *sX = sL + kInvN * kInvLd;    // sX[i * kInvLd + k] = X(i, k)
-  float *sT = sX + kInvN * kInvLd;    // 64 x 64 product scratch, ld 65
-  const int tid = threadIdx.x, nt = blockDim.x;
-  for (int e = tid; e < kInvN * kInvN; e += nt) {
-    const int i = e % kInvN, k = e / kInvN;
-    const float v = (i < nb && k < nb) ? L[i + (long)k * ldl] : (i == k ? 1.f : 0.f);
-    sL[i * kInvLd + k] = v;
-    sX[i * kInvLd + k] = 0.f;
-  }
-  __syncthreads();
-  // 16 x 16 diagonal blocks: thread = (block, column)
-  if (tid < kInvN) {
-    const int b0 = (tid >> 4) << 4, c = tid;
-    sX[c * kInvLd + c] = 1.f;
-    for (int i = c + 1; i < b0 + 16; ++i) {
-      float acc = 0.f;
-      for (int k = c; k < i; ++k) acc = fmaf(sL[i * kInvLd + k], sX[k * kInvLd + c], acc);
-      sX[i * kInvLd + c] = -acc;
-    }
-  }
-  __syncthreads();
-  for (int sz = 16; sz < kInvN; sz *= 2) {
-    const int pairs = kInvN / (2 * sz);
-    // T = C A^-1 for every pair (C = L rows b+sz.., cols b..; A^-1 = X block at b)
-    for (int e = tid; e < pairs * sz * sz; e += nt) {
-      const int q = e / (sz * sz), r = (e / sz) % sz, c = e % sz, b = q * 2 * sz;
-      float acc = 0.f;
-      for (int k = c; k < sz; ++k)  // A^-1 is lower: rows k >= c
-        acc = fmaf(sL[(b + sz + r) * kInvLd + b + k], sX[(b + k) * kInvLd + b + c], acc);
-      sT[(q * sz + r) * 65 + c] = acc;  // pairs * sz <= 64 rows
-    }
-    __syncthreads();
-    // off-diagonal block = -B^-1 T (B^-1 = X block at b + sz, lower)
-    for (int e = tid; e < pairs * sz * sz; e += nt) {
-      const int q = e / (sz * sz), r = (e / sz) % sz, c = e % sz, b = q * 2 * sz;
-      float acc = 0.f;
-      for (int k = 0; k <= r; ++k)
-        acc = fmaf(sX[(b + sz + r) * kInvLd + b + sz + k], sT[(q * sz + k) * 65 + c], acc);
-      sX[(b + sz + r) * kInvLd + b + c] = -acc;
-    }
-    __syncthreads();
-  }
-  for (int e = tid; e < nb * nb; e += nt) {
+// One column of the identity per warp (16 CTAs of 8 warps for nb = 128): lane l holds rows l, l + 32, l + 64, l + 96 of the column;
+// step k broadcasts the solved x_k from its lane and every lane updates its
+// rows below k.  L sits in shared memory with an odd stride, so the lanes'
+// reads of one column hit distinct banks.
+constexpr int kInvColsPerCta = 8;
+__global__ void __launch_bounds__(32 * kInvColsPerCta)
+    inv_unit_lower_cols_kernel(int nb, const float *__restrict__ L, long ldl, float *X, long ldx) {
+  extern __shared__ float sLc[];  // sLc[i * kInvLd + k] = L(i, k)
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int j0 = blockIdx.x * kInvColsPerCta;
+  // rows >= j0 and columns j0 .. nb-1 are all this CTA's columns can touch
+  for (int e = tid; e < nb * nb; e += blockDim.x) {
     const int i = e % nb, k = e / nb;
-    X[i + (long)k * ldx] = sX[i * kInvLd + k];
+    if (i >= j0 && k >= j0 && k < i) sLc[i * kInvLd + k] = L[i + (long)k * ldl];
+  }
+  __syncthreads();
+  const int j = j0 + warp;
+  if (j >= nb) return;
+  float x[kInvN / 32];
+#pragma unroll
+  for (int q = 0; q < kInvN / 32; ++q) x[q] = (lane + 32 * q == j) ? 1.f : 0.f;
+  for (int k = j; k < nb - 1; ++k) {
+    const int kq = k >> 5;  // static register choice: no local-memory indexing
+    const float xs = kq == 0 ? x[0] : kq == 1 ? x[1] : kq == 2 ? x[2] : x[3];
+    const float xk = __shfl_sync(~0u, xs, k & 31);
+#pragma unroll
+    for (int q = 0; q < kInvN / 32; ++q) {
+      const int i = lane + 32 * q;
+      if (i > k && i < nb) x[q] = fmaf(-sLc[i * kInvLd + k], xk, x[q]);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < kInvN / 32; ++q) {
+    const int i = lane + 32 * q;
+    if (i < nb) X[i + (long)j * ldx] = i < j ? 0.f : x[q];
   }
 }
 
 static int inv_unit_lower(int nb, const float *L, long ldl, float *X, long ldx, cudaStream_t s) {
+  if (nb <= 0) return 0;
   static bool attr = false;
-  const int smem = (2 * kInvN * kInvLd + 64 * 65) * sizeof(float);
+  const int smem = kInvN * kInvLd * sizeof(float);
   if (!attr) {
-    ZG_CUDA(cudaFuncSetAttribute(inv_unit_lower_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 smem));
+    ZG_CUDA(cudaFuncSetAttribute(inv_unit_lower_cols_kernel,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     attr = true;
   }
   ZG_LAUNCH(kTagTrsmDiag, nb * (double)nb * nb / 3.0, 0, s,
-            inv_unit_lower_kernel<<<1, 256, smem, s>>>(nb, L, ldl, X, ldx));
+            inv_unit_lower_cols_kernel<<<ceil_div(nb, kInvColsPerCta), 32 * kInvColsPerCta, smem,
+                                         s>>>(nb, L, ldl, X, ldx));
   return 0;
 }
 
