@@ -29,8 +29,9 @@
 // Between sub-panels: the sub-panel is written back; its interchanges are
 // composed into (destination, source) pairs and applied to the panel's other
 // columns and to up to two extra column ranges beside the panel (the rest of
-// the caller's column block), column-partitioned over the CTAs; U12 = L11^-1 A12 is solved by
-// every CTA into shared memory (CTA 0 writes it back) and each CTA updates
+// the caller's column block), column-partitioned over the CTAs; U12 =
+// L11^-1 A12 is solved by every CTA into shared memory (CTA 0 writes it
+// back) and each CTA updates
 // its own rows of the columns to the right, A22 -= L21 U12, with L21 loaded
 // into registers.
 #include "common.cuh"
@@ -107,10 +108,9 @@ __device__ __forceinline__ int pc_row(unsigned long long w) {
   return (int)(0xffffffffu - (unsigned)(w & 0xffffffffu));
 }
 
-// Exchange buffers are used round robin over three columns: a column's
-// pivot row is still read (by the deferred update) while the next column's
-// pushes land, and the column after that cannot push before this CTA has
-// pushed the next one.
+// Exchange buffers are used round robin over three columns.  Column k + 3's
+// pushes into buffer k % 3 cannot start before this CTA has pushed column
+// k + 2, by which time every thread here is done with column k's rows.
 constexpr int kPcBuf = 3;
 
 struct __align__(16) PcShared {
