@@ -36,9 +36,10 @@ METRIC = "n=16384 Ax=b to FP64 backward err: IR-BF16 vs FP64 LU time; batched so
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) over the
 # algorithmic bytes of one launch, per kernel class, from ncu captures of the
 # n = 8192 case; the roofline's "traffic" scales a launch's algorithmic bytes
-# by it.  panel: the slab is read once, its write-back is still in L2 when the
-# kernel ends; gemm_tc: part of C is L2-resident; trsv: the factor streams once.
-TRAFFIC_RATIO = {"panel": 0.506, "gemm_tc": 0.761, "trsv": 1.006}
+# by it.  panel: the panel is read once (partly from L2, where the previous
+# update left it) and its write-back is still in L2 when the kernel ends;
+# gemm_tc: part of C is L2-resident; trsv: the factor streams once.
+TRAFFIC_RATIO = {"panel": 0.734, "gemm_tc": 0.803, "trsv": 1.006}
 UNIT = "solves/s"
 
 

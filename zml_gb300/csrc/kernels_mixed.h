@@ -33,7 +33,6 @@ struct MpirResult {
   double berr_history[32] = {0};
 };
 
-int d2s(int m, int n, const double *A, long lda, float *B, long ldb, cudaStream_t s);
 int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cudaStream_t s);
 // Solves A X = B (device pointers, column-major) to FP64 accuracy: one
 // low-precision factorization, then refinement of each right-hand side.

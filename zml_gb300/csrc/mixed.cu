@@ -26,15 +26,6 @@ namespace zg {
 
 // ---------------------------------------------------------------------------
 // Conversions
-__global__ void d2s_kernel(int m, int n, const double *A, long lda, float *B, long ldb) {
-  long total = (long)m * n;
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total;
-       e += (long)gridDim.x * blockDim.x) {
-    int i = e % m, j = e / m;
-    B[i + (long)j * ldb] = (float)A[i + (long)j * lda];
-  }
-}
-
 template <typename H> __device__ __forceinline__ H to16(float v);
 template <> __device__ __forceinline__ __nv_bfloat16 to16(float v) { return __float2bfloat16_rn(v); }
 template <> __device__ __forceinline__ __half to16(float v) { return __float2half_rn(v); }
@@ -89,13 +80,6 @@ __global__ void to_kmajor_n_kernel(int k, int cols, const float *A, long lda, H 
 }
 
 static int grid1d(long total) { return (int)std::min<long>((total + 255) / 256, 152L * 16); }
-
-int d2s(int m, int n, const double *A, long lda, float *B, long ldb, cudaStream_t s) {
-  if (m <= 0 || n <= 0) return 0;
-  ZG_LAUNCH(kTagConvert, 0, 0, s, d2s_kernel<<<grid1d((long)m * n), 256, 0, s>>>(m, n, A, lda, B, ldb));
-  ZG_CUDA(cudaGetLastError());
-  return 0;
-}
 
 // ldk: segment width (>= k, multiple of 8); the operand row stride is ldk,
 // or 3 ldk for the split (bf16x3) form.
@@ -792,12 +776,60 @@ __global__ void absmax_kernel(int n, const double *x, double *out) {
   if (threadIdx.x == 0) *out = sm[0];
 }
 
-// ||A||_inf: row sums of |A| (column-major), then the maximum.
-__global__ void rowabs_kernel(int n, const double *A, long lda, double *rs) {
+// One pass over the FP64 matrix: B = fp32(A), and the row sums of |A| for
+// ||A||_inf, as FP32 partial sums over 512-column chunks (positive terms, at
+// most 512 a chunk: relative error below 1e-4, ample for a norm that only
+// scales the backward error) that a second kernel adds in FP64.
+__global__ void __launch_bounds__(kGemvRows) d2s_rowabs_kernel(int n, const double *A, long lda,
+                                                                float *B, long ldb, float *part) {
+  const int i = blockIdx.x * kGemvRows + threadIdx.x;
+  const int c0 = blockIdx.y * kGemvCols, c1 = min(n, c0 + kGemvCols);
+  if (i >= n) return;
+  float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
+  int j = c0;
+  for (; j + 3 < c1; j += 4) {
+    const double a0 = A[i + (long)j * lda], a1 = A[i + (long)(j + 1) * lda];
+    const double a2 = A[i + (long)(j + 2) * lda], a3 = A[i + (long)(j + 3) * lda];
+    const float f0 = (float)a0, f1 = (float)a1, f2 = (float)a2, f3 = (float)a3;
+    B[i + (long)j * ldb] = f0;
+    B[i + (long)(j + 1) * ldb] = f1;
+    B[i + (long)(j + 2) * ldb] = f2;
+    B[i + (long)(j + 3) * ldb] = f3;
+    acc0 += fabsf(f0);
+    acc1 += fabsf(f1);
+    acc2 += fabsf(f2);
+    acc3 += fabsf(f3);
+  }
+  for (; j < c1; ++j) {
+    const float f = (float)A[i + (long)j * lda];
+    B[i + (long)j * ldb] = f;
+    acc0 += fabsf(f);
+  }
+  part[(long)blockIdx.y * n + i] = (acc0 + acc1) + (acc2 + acc3);
+}
+
+// Row sums of |A| over 512-column chunks in FP64 (the FP64 solve's norm);
+// gemv_finish_kernel adds the chunks.
+__global__ void __launch_bounds__(kGemvRows) rowabs_partial_kernel(int n, const double *A, long lda,
+                                                                    double *part) {
+  const int i = blockIdx.x * kGemvRows + threadIdx.x;
+  const int c0 = blockIdx.y * kGemvCols, c1 = min(n, c0 + kGemvCols);
+  if (i >= n) return;
+  double acc0 = 0, acc1 = 0;
+  int j = c0;
+  for (; j + 1 < c1; j += 2) {
+    acc0 += fabs(A[i + (long)j * lda]);
+    acc1 += fabs(A[i + (long)(j + 1) * lda]);
+  }
+  if (j < c1) acc0 += fabs(A[i + (long)j * lda]);
+  part[(long)blockIdx.y * n + i] = acc0 + acc1;
+}
+
+__global__ void rowabs_finish_kernel(int n, int nparts, const float *part, double *rs) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double acc = 0;
-  for (int j = 0; j < n; ++j) acc += fabs(A[i + (long)j * lda]);
+  for (int p = 0; p < nparts; ++p) acc += (double)part[(long)p * n + i];
   rs[i] = acc;
 }
 
@@ -1019,8 +1051,15 @@ static int mpir_factor(bool spd, bool lower, int n, const double *A, long lda, c
   w.scal = p; p += 8;
   w.tw = (unsigned *)p;
 
-  // ||A||_inf
-  ZG_LAUNCH(kTagGemv, 0, 0, s, rowabs_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, A, lda, w.r));
+  // the FP32 working copy of A and ||A||_inf, in one pass over A
+  {
+    float *rpart = reinterpret_cast<float *>(w.part);  // n x nparts floats fit in w.part
+    ZG_LAUNCH(kTagConvert, 0, 12.0 * n * n, s,
+              d2s_rowabs_kernel<<<dim3(ceil_div(n, kGemvRows), nparts), kGemvRows, 0, s>>>(
+                  n, A, lda, LU, n, rpart));
+    ZG_LAUNCH(kTagVector, 0, 0, s,
+              rowabs_finish_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, nparts, rpart, w.r));
+  }
   ZG_LAUNCH(kTagVector, 0, 0, s, absmax_kernel<<<1, 256, 0, s>>>(n, w.r, w.scal));
   ZG_CUDA(cudaGetLastError());
   double anrm;
@@ -1031,7 +1070,6 @@ static int mpir_factor(bool spd, bool lower, int n, const double *A, long lda, c
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, s);
-  ZG_TRY(d2s(n, n, A, lda, LU, n, s));
   if (spd)
     ZG_TRY(potrf_lowp(n, LU, n, o.prec, ctl, s));
   else
@@ -1180,7 +1218,11 @@ static int fp64_solve(int n, int nrhs, const double *A, long lda, const double *
   ZG_CUDA(cudaMemcpy2DAsync(X, sizeof(double) * ldx, B, sizeof(double) * ldb, sizeof(double) * n,
                             nrhs, cudaMemcpyDeviceToDevice, s));
   ZG_TRY(getrs_dev<double>(kNoTrans, n, nrhs, LU, n, piv, X, ldx, s));
-  ZG_LAUNCH(kTagGemv, 0, 0, s, rowabs_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, A, lda, w.r));
+  ZG_LAUNCH(kTagGemv, 0, 8.0 * n * n, s,
+            rowabs_partial_kernel<<<dim3(ceil_div(n, kGemvRows), nparts), kGemvRows, 0, s>>>(
+                n, A, lda, w.part));
+  ZG_LAUNCH(kTagGemv, 0, 0, s,
+            gemv_finish_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, nparts, w.part, nullptr, w.r));
   ZG_LAUNCH(kTagVector, 0, 0, s, absmax_kernel<<<1, 256, 0, s>>>(n, w.r, w.scal));
   double anrm;
   ZG_TRY(host_scalar(w.scal, &anrm, s));
