@@ -17,7 +17,11 @@ struct MpirOpts {
   double tol = 0;           // stop when berr <= tol; 0 = iterate to stagnation
   int max_iter = 30;        // outer refinement steps
   int gmres_restart = 50;   // inner GMRES iterations per outer step
-  double gmres_rtol = 1e-6; // inner relative tolerance (preconditioned residual)
+  // inner relative tolerance (preconditioned residual).  An outer step gains
+  // about 1e4 at most with FP32-applied factors, so asking GMRES for 1e-4
+  // instead of 1e-6 saves inner iterations without adding outer steps
+  // (n = 16384 Gaussian: 3 outer / 15 inner steps instead of 3 / 20).
+  double gmres_rtol = 1e-4;
   int apply = kApplyAuto;   // FP32 first, FP64 once refinement stops improving
 };
 

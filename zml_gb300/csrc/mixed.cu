@@ -1290,6 +1290,7 @@ int gesv_auto_dev(int n, int nrhs, const double *A, long lda, const double *B, l
   o.prec = kPrecBF16;
   o.mode = kModeGMRES;
   o.max_iter = probe_steps;
+  o.gmres_rtol = 1e-6;  // the probe features are the backward errors after 1e-6 GMRES steps
   MpirCtx c;
   MpirResult pr;
   ZG_TRY(mpir_factor(false, false, n, A, lda, o, &c, &pr, s));
