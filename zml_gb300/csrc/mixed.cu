@@ -199,20 +199,99 @@ __global__ void gemm_small_kernel(int m, int n, int k, float alpha, const float 
   C[i + (long)j * ldc] = beta == 0.f ? v : v + beta * C[i + (long)j * ldc];
 }
 
+// C (m x n) = alpha A B + beta C for m, k <= 128: one CTA per 32 columns of
+// C loads all of A (column-major, padded) and its k x 32 slice of B into
+// shared memory, then every thread forms a 4 x 4 register tile (rows lane +
+// 32 u, columns warp + 8 v).  The slice of B is read completely before any
+// of C is written, so C may be B itself (beta = 0).
+constexpr int kG128 = 128;
+__global__ void __launch_bounds__(256) gemm128_kernel(int m, int n, int k, float alpha,
+                                                      const float *A, long lda, const float *B,
+                                                      long ldb, float beta, float *C, long ldc) {
+  extern __shared__ float g128[];
+  float *sA = g128;                      // sA[q * (kG128 + 1) + r] = A(r, q)
+  float *sB = g128 + kG128 * (kG128 + 1);  // sB[q * 33 + c] = B(q, j0 + c)
+  const int j0 = blockIdx.x * 32, nc = min(32, n - j0);
+  // thread = (row t & 127, column phase t >> 7): column-contiguous loads, eight
+  // independent loads in flight a thread
+  const int lr = threadIdx.x & 127, cp = threadIdx.x >> 7;
+  for (int q0 = cp; q0 < k; q0 += 16) {
+    float t[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int q = q0 + 2 * u;
+      t[u] = (lr < m && q < k) ? A[lr + (long)q * lda] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int q = q0 + 2 * u;
+      if (q < k) sA[q * (kG128 + 1) + lr] = t[u];
+    }
+  }
+  {
+    float t[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int c = cp + 2 * u;
+      t[u] = (lr < k && c < nc) ? B[lr + (long)(j0 + c) * ldb] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 16; ++u) sB[lr * 33 + cp + 2 * u] = t[u];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float acc[4][4] = {};
+  for (int q = 0; q < k; ++q) {
+    float a[4], bv[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) a[u] = sA[q * (kG128 + 1) + lane + 32 * u];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) bv[v] = sB[q * 33 + warp + 8 * v];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(a[u], bv[v], acc[u][v]);
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int r = lane + 32 * u, c = warp + 8 * v;
+      if (r < m && c < nc) {
+        float *cp = C + r + (long)(j0 + c) * ldc;
+        *cp = beta != 0.f ? fmaf(alpha, acc[u][v], beta * *cp) : alpha * acc[u][v];
+      }
+    }
+}
+
 static int gemm_small(int m, int n, int k, float alpha, const float *A, long lda, const float *B,
                       long ldb, float beta, float *C, long ldc, cudaStream_t s) {
   if (m <= 0 || n <= 0) return 0;
+  if (m <= kG128 && k <= kG128) {
+    const int smem = sizeof(float) * (kG128 * (kG128 + 1) + kG128 * 33);
+    static bool attr = false;
+    if (!attr) {
+      ZG_CUDA(cudaFuncSetAttribute(gemm128_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   smem));
+      attr = true;
+    }
+    ZG_LAUNCH(kTagGemmSimt, 2.0 * m * n * k, 4.0 * ((double)m * k + (double)k * n + 2.0 * m * n),
+              s, gemm128_kernel<<<ceil_div(n, 32), 256, smem, s>>>(m, n, k, alpha, A, lda, B, ldb,
+                                                                  beta, C, ldc));
+    return 0;
+  }
   ZG_LAUNCH(kTagGemmSimt, 2.0 * m * n * k, 4.0 * ((double)m * k + (double)k * n + 2.0 * m * n), s,
             gemm_small_kernel<<<dim3(ceil_div(m, 32), ceil_div(n, 8)), 256, 0, s>>>(
                 m, n, k, alpha, A, lda, B, ldb, beta, C, ldc));
   return 0;
 }
 
-// B (k x cols, ld ldb) <- Linv B with Linv (k x k, ld ldi), through a scratch
-// copy T (k x cols, ld k).
+// B (k x cols, ld ldb) <- Linv B with Linv (k x k, ld ldi): in place for
+// k <= 128, otherwise through a scratch copy T (k x cols, ld k).
 static int apply_inverse(int k, int cols, const float *Linv, long ldi, float *B, long ldb, float *T,
                          cudaStream_t s) {
   if (k <= 0 || cols <= 0) return 0;
+  if (k <= kG128) return gemm_small(k, cols, k, 1.f, Linv, ldi, B, ldb, 0.f, B, ldb, s);  // in place
   if (cols <= 256)
     ZG_TRY(gemm_small(k, cols, k, 1.f, Linv, ldi, B, ldb, 0.f, T, k, s));
   else
