@@ -136,10 +136,24 @@ __global__ void __launch_bounds__(32 * kInvColsPerCta)
   extern __shared__ float sLc[];  // sLc[i * kInvLd + k] = L(i, k)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int j0 = blockIdx.x * kInvColsPerCta;
-  // rows >= j0 and columns j0 .. nb-1 are all this CTA's columns can touch
-  for (int e = tid; e < nb * nb; e += blockDim.x) {
-    const int i = e % nb, k = e / nb;
-    if (i >= j0 && k >= j0 && k < i) sLc[i * kInvLd + k] = L[i + (long)k * ldl];
+  // columns j0 .. nb-1 below the diagonal are all this CTA's columns touch;
+  // thread = (row t & 127, column phase t >> 7), column-contiguous loads with
+  // eight in flight a thread
+  {
+    const int i = tid & 127, cp = tid >> 7;
+    for (int k0 = j0 + cp; k0 < nb; k0 += 16) {
+      float t[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = k0 + 2 * u;
+        t[u] = (k < nb && i > k && i < nb) ? L[i + (long)k * ldl] : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = k0 + 2 * u;
+        if (k < nb && i < nb) sLc[i * kInvLd + k] = t[u];
+      }
+    }
   }
   __syncthreads();
   const int j = j0 + warp;
