@@ -358,20 +358,29 @@ __global__ void __launch_bounds__(kPcThreads, 1)
       const int mine = ntot > rank ? (ntot - rank + nct - 1) / nct : 0;
       const int e = tid % kEnt;
       const int dst = sh.mdst[e], src = sh.msrc[e];
-      for (int base = 0; base < mine; base += kCpr) {
-        const int jl = base + tid / kEnt;  // threads past kCpr whole columns sit out
-        const bool act = tid < kCpr * kEnt && jl < mine && dst >= 0;
-        float val = 0.f;
-        float *colp = A;
-        if (act) {
-          const int j = rank + jl * nct;
-          if (j < no) colp = A + (long)(j < c0 ? j : j + ws) * lda;
-          else if (j < no + xl) colp = XL + (long)(j - no) * lda;
-          else colp = XR + (long)(j - no - xl) * lda;
-          val = __ldcg(colp + src);
+      auto column = [&](int jl) {
+        const int j = rank + jl * nct;
+        if (j < no) return A + (long)(j < c0 ? j : j + ws) * lda;
+        if (j < no + xl) return XL + (long)(j - no) * lda;
+        return XR + (long)(j - no - xl) * lda;
+      };
+      // up to kRounds rounds of columns gathered into registers behind one
+      // barrier, then scattered (threads past kCpr whole columns sit out)
+      constexpr int kRounds = 16;
+      const bool part = tid < kCpr * kEnt && dst >= 0;
+      for (int base = 0; base < mine; base += kRounds * kCpr) {
+        float val[kRounds];
+#pragma unroll
+        for (int u = 0; u < kRounds; ++u) {
+          const int jl = base + u * kCpr + tid / kEnt;
+          val[u] = (part && jl < mine) ? __ldcg(column(jl) + src) : 0.f;
         }
         __syncthreads();
-        if (act) colp[dst] = val;
+#pragma unroll
+        for (int u = 0; u < kRounds; ++u) {
+          const int jl = base + u * kCpr + tid / kEnt;
+          if (part && jl < mine) column(jl)[dst] = val[u];
+        }
       }
     }
     __threadfence();
@@ -380,13 +389,32 @@ __global__ void __launch_bounds__(kPcThreads, 1)
     // G. U12 = L11^-1 A12 over the right columns, in every CTA
     const int nr = nb - c0 - ws;
     if (nr > 0) {
-      for (int e = tid; e < ws * ws; e += T) {
-        const int r = e % ws, c = e / ws;
-        sh.L11[r][c] = __ldcg(A + (c0 + r) + (long)(c0 + c) * lda);
-      }
-      for (int e = tid; e < ws * nr; e += T) {
-        const int r = e % ws, c = e / ws;
-        sh.U[c][r] = __ldcg(A + (c0 + r) + (long)(c0 + ws + c) * lda);
+      // lanes over rows (contiguous), warps over columns, several loads in flight
+      {
+        float t[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int c = warp + nwarps * u;
+          t[u] = (lane < ws && c < ws) ? __ldcg(A + (c0 + lane) + (long)(c0 + c) * lda) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int c = warp + nwarps * u;
+          if (lane < ws && c < ws) sh.L11[lane][c] = t[u];
+        }
+        for (int cb = 0; cb < nr; cb += 8 * nwarps) {
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int c = cb + warp + nwarps * u;
+            t[u] = (lane < ws && c < nr) ? __ldcg(A + (c0 + lane) + (long)(c0 + ws + c) * lda)
+                                         : 0.f;
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int c = cb + warp + nwarps * u;
+            if (lane < ws && c < nr) sh.U[c][lane] = t[u];
+          }
+        }
       }
       __syncthreads();
       if (tid < nr) {
