@@ -13,6 +13,8 @@
 // FP64; the preconditioner applies the FP32 factors with FP64 accumulation.
 #include <algorithm>
 #include <chrono>
+#include <map>
+#include <mutex>
 #include <cmath>
 #include <vector>
 
@@ -318,17 +320,83 @@ static int apply_inverse(int k, int cols, const float *Linv, long ldi, float *B,
 
 // ---------------------------------------------------------------------------
 // Low-precision LU of an n x n FP32 matrix (partial pivoting, ipiv 1-based).
+//
+// Lookahead: a 256-column block's trailing update is split into the next
+// block's columns (on the panel stream, at high priority) and the rest (on
+// a low-priority bulk stream), so the bulk of the update runs beside the
+// next block's panel, which holds 16 SMs for most of its time.  Events keep
+// the order: block b's panel waits for the bulk update of block b-2 (the
+// last one to touch its columns), block b's full-width interchanges for
+// that of block b-1.  The 16-bit operand buffers alternate by block parity.
+
+namespace {
+// Streams and events of the lookahead, one set per (device, caller stream),
+// created on first use and kept.
+struct Lookahead {
+  static constexpr int kRing = 4;
+  cudaStream_t panel = nullptr, bulk = nullptr;
+  cudaEvent_t first = nullptr, upd[kRing] = {}, bulk_done[kRing] = {}, end_panel = nullptr,
+              end_bulk = nullptr;
+};
+std::mutex g_la_mu;
+std::map<std::pair<int, cudaStream_t>, Lookahead> g_la;
+
+int lookahead(cudaStream_t s, Lookahead **out) {
+  int dev = 0;
+  ZG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_la_mu);
+  Lookahead &l = g_la[{dev, s}];
+  if (!l.panel) {
+    int least = 0, greatest = 0;
+    ZG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    ZG_CUDA(cudaStreamCreateWithPriority(&l.panel, cudaStreamNonBlocking, greatest));
+    ZG_CUDA(cudaStreamCreateWithPriority(&l.bulk, cudaStreamNonBlocking, least));
+    const unsigned fl = cudaEventDisableTiming;
+    ZG_CUDA(cudaEventCreateWithFlags(&l.first, fl));
+    ZG_CUDA(cudaEventCreateWithFlags(&l.end_panel, fl));
+    ZG_CUDA(cudaEventCreateWithFlags(&l.end_bulk, fl));
+    for (int q = 0; q < Lookahead::kRing; ++q) {
+      ZG_CUDA(cudaEventCreateWithFlags(&l.upd[q], fl));
+      ZG_CUDA(cudaEventCreateWithFlags(&l.bulk_done[q], fl));
+    }
+  }
+  *out = &l;
+  return 0;
+}
+}  // namespace
+
+static int getrf_lowp_blocks(int n, float *A, long lda, int *ipiv, int prec, Control *ctl,
+                             cudaStream_t s, Lookahead &la);
+
 int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cudaStream_t s) {
   if (n <= 0) return 0;
-  constexpr int NB = 256, NBP = 128;
   if (prec == kPrecFP32) {
     int info = 0;
     return getrf_dev<float>(n, n, A, lda, ipiv, &info, s) < 0 ? kErrCuda : 0;
   }
+  Lookahead *la;
+  ZG_TRY(lookahead(s, &la));
+  // both internal streams start after the caller's earlier work and the
+  // caller's stream resumes after both
+  ZG_CUDA(cudaEventRecord(la->first, s));
+  ZG_CUDA(cudaStreamWaitEvent(la->panel, la->first, 0));
+  ZG_CUDA(cudaStreamWaitEvent(la->bulk, la->first, 0));
+  const int rc = getrf_lowp_blocks(n, A, lda, ipiv, prec, ctl, s, *la);
+  ZG_CUDA(cudaEventRecord(la->end_panel, la->panel));
+  ZG_CUDA(cudaEventRecord(la->end_bulk, la->bulk));
+  ZG_CUDA(cudaStreamWaitEvent(s, la->end_panel, 0));
+  ZG_CUDA(cudaStreamWaitEvent(s, la->end_bulk, 0));
+  return rc;
+}
+
+static int getrf_lowp_blocks(int n, float *A, long lda, int *ipiv, int prec, Control *ctl,
+                             cudaStream_t s, Lookahead &la) {
+  constexpr int NB = 256, NBP = 128;
   const int segs = prec == kPrecBF16x3 ? 3 : 1;
-  void *wl, *wu, *wi;
-  ZG_TRY(workspace(s, kSlotL16, sizeof(uint16_t) * (size_t)n * NB * segs, &wl));
-  ZG_TRY(workspace(s, kSlotU16, sizeof(uint16_t) * (size_t)n * NB * segs, &wu));
+  const size_t nop = (size_t)n * NB * segs;  // 16-bit elements of one operand buffer
+  void *wl0, *wu0, *wi;
+  ZG_TRY(workspace(s, kSlotL16, sizeof(uint16_t) * 2 * nop, &wl0));
+  ZG_TRY(workspace(s, kSlotU16, sizeof(uint16_t) * 2 * nop, &wu0));
   // L11^-1 (NB x NB), a temporary NBP x NBP block, and the block row's scratch
   const size_t ntb = prec == kPrecBF16x3 ? (size_t)NBP * NBP : (size_t)NB * n;
   ZG_TRY(workspace(s, kSlotInvL,
@@ -338,42 +406,47 @@ int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cud
   // L11^-1, a product scratch, the block row's scratch, L11^-1 as a 16-bit operand
   float *Linv = (float *)wi, *Ttmp = Linv + NB * NB, *Tb = Ttmp + NBP * NBP;
   void *wli = Tb + ntb;
-  for (int j = 0; j < n; j += NB) {
+  const cudaStream_t sp = la.panel, sb = la.bulk;
+  constexpr int R = Lookahead::kRing;
+  for (int j = 0, b = 0; j < n; j += NB, ++b) {
     const int jb = std::min(NB, n - j);
-    ZG_CUDA(cudaMemsetAsync(Linv, 0, sizeof(float) * NB * NB, s));
+    uint16_t *wl = (uint16_t *)wl0 + (b & 1) * nop, *wu = (uint16_t *)wu0 + (b & 1) * nop;
+    // this block's columns were last updated by block b-2's bulk update
+    if (b >= 2) ZG_CUDA(cudaStreamWaitEvent(sp, la.bulk_done[(b - 2) % R], 0));
+    ZG_CUDA(cudaMemsetAsync(Linv, 0, sizeof(float) * NB * NB, sp));
     // panel: two FP32 half-panels (one cluster each) with an update between
     for (int p = 0; p < jb; p += NBP) {
       const int r = j + p, pb = std::min(NBP, jb - p);
       const int right = j + jb - r - pb;
       // the half-panel, its interchanges applied inside the block's other columns
       bool done = false;
-      ZG_TRY(panel_lu_cluster(n - r, pb, A + r + (long)r * lda, lda, ipiv + r, r, ctl, r, s,
+      ZG_TRY(panel_lu_cluster(n - r, pb, A + r + (long)r * lda, lda, ipiv + r, r, ctl, r, sp,
                               &done, A + r + (long)j * lda, r - j, A + r + (long)(r + pb) * lda,
                               right));
       if (!done) {
-        ZG_TRY(panel_lu<float>(n - r, pb, A + r + (long)r * lda, lda, ipiv + r, r, ctl, r, s));
+        ZG_TRY(panel_lu<float>(n - r, pb, A + r + (long)r * lda, lda, ipiv + r, r, ctl, r, sp));
         ZG_TRY(laswp_panel<float>(r - j, r + pb - j, jb, A + (long)j * lda, lda, r + 1, r + pb,
-                                  ipiv, s));
+                                  ipiv, sp));
       }
       // the half-panel's unit-lower diagonal block, inverted into L11^-1
       float *Dinv = Linv + p + (long)p * NB;
-      ZG_TRY(inv_unit_lower(pb, A + r + (long)r * lda, lda, Dinv, NB, s));
+      ZG_TRY(inv_unit_lower(pb, A + r + (long)r * lda, lda, Dinv, NB, sp));
       if (right > 0) {
         float *Ar = A + (long)(r + pb) * lda;
-        ZG_TRY(apply_inverse(pb, right, Dinv, NB, Ar + r, lda, Tb, s));
+        ZG_TRY(apply_inverse(pb, right, Dinv, NB, Ar + r, lda, Tb, sp));
         const int rows = n - r - pb;
         if (prec == kPrecBF16x3 && rows > 0) {
           // the second half-panel's update in the block's update precision
           const int ldk = ((pb + 7) / 8) * 8;
           const long ldo = (long)ldk * segs;
-          ZG_TRY(to_kmajor_t(prec, rows, pb, A + (r + pb) + (long)r * lda, lda, wl, ldk, s));
-          ZG_TRY(to_kmajor_n(prec, pb, right, Ar + r, lda, wu, ldk, s));
+          ZG_TRY(to_kmajor_t(prec, rows, pb, A + (r + pb) + (long)r * lda, lda, wl, ldk, sp));
+          ZG_TRY(to_kmajor_n(prec, pb, right, Ar + r, lda, wu, ldk, sp));
           ZG_TRY(gemm_tc(rows, right, (int)ldo, -1.f, wl, ldo, wu, ldo, 1.f, Ar + r + pb, lda, 1,
-                         &ctl->status, s));
+                         &ctl->status, sp));
         } else {
           ZG_TRY(gemm_simt<float>(kNoTrans, kNoTrans, rows, right, pb, -1.f,
                                   A + (r + pb) + (long)r * lda, lda, Ar + r, lda, 1.f,
-                                  Ar + r + pb, lda, 0, s));
+                                  Ar + r + pb, lda, 0, sp));
         }
       }
     }
@@ -381,11 +454,13 @@ int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cud
       // L11^-1 = [La^-1 0; -Lb^-1 Lc La^-1  Lb^-1]
       const int pb2 = jb - NBP;
       ZG_TRY(gemm_small(pb2, NBP, NBP, 1.f, A + (j + NBP) + (long)j * lda, lda, Linv, NB, 0.f,
-                        Ttmp, NBP, s));
+                        Ttmp, NBP, sp));
       ZG_TRY(gemm_small(pb2, NBP, pb2, -1.f, Linv + NBP + (long)NBP * NB, NB, Ttmp, NBP, 0.f,
-                        Linv + NBP, NB, s));
+                        Linv + NBP, NB, sp));
     }
-    ZG_TRY(laswp_panel<float>(j, j + jb, n, A, lda, j + 1, j + jb, ipiv, s));
+    // the interchanges reach every other column: wait for block b-1's bulk update
+    if (b >= 1) ZG_CUDA(cudaStreamWaitEvent(sp, la.bulk_done[(b - 1) % R], 0));
+    ZG_TRY(laswp_panel<float>(j, j + jb, n, A, lda, j + 1, j + jb, ipiv, sp));
     const int rest = n - j - jb;
     if (rest <= 0) break;
     float *A12 = A + j + (long)(j + jb) * lda;
@@ -396,22 +471,32 @@ int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cud
     const int ldk = ((jb + 7) / 8) * 8;
     const long ldo = (long)ldk * segs;
     if (prec == kPrecBF16x3) {
-      ZG_TRY(to_kmajor_t(prec, jb, jb, Linv, NB, wli, ldk, s));
-      ZG_TRY(to_kmajor_n(prec, jb, rest, A12, lda, wu, ldk, s));
+      ZG_TRY(to_kmajor_t(prec, jb, jb, Linv, NB, wli, ldk, sp));
+      ZG_TRY(to_kmajor_n(prec, jb, rest, A12, lda, wu, ldk, sp));
       ZG_TRY(gemm_tc(jb, rest, (int)ldo, 1.f, wli, ldo, wu, ldo, 0.f, A12, lda, 1, &ctl->status,
-                     s));
+                     sp));
     } else {
-      ZG_TRY(apply_inverse(jb, rest, Linv, NB, A12, lda, Tb, s));
+      ZG_TRY(apply_inverse(jb, rest, Linv, NB, A12, lda, Tb, sp));
     }
     // 16-bit operands: L21 (rest x jb) and U12^T (rest x jb), K-major
-    ZG_TRY(to_kmajor_t(prec, rest, jb, A + (j + jb) + (long)j * lda, lda, wl, ldk, s));
-    ZG_TRY(to_kmajor_n(prec, jb, rest, A12, lda, wu, ldk, s));
-    ZG_TRY(gemm_tc(rest, rest, (int)ldo, -1.f, wl, ldo, wu, ldo, 1.f, A12 + jb, lda,
-                   prec == kPrecFP16 ? 0 : 1, &ctl->status, s));
+    ZG_TRY(to_kmajor_t(prec, rest, jb, A + (j + jb) + (long)j * lda, lda, wl, ldk, sp));
+    ZG_TRY(to_kmajor_n(prec, jb, rest, A12, lda, wu, ldk, sp));
+    const int abt = prec == kPrecFP16 ? 0 : 1;  // 16-bit operand type: FP16 0, BF16 1
+    // the next block's columns now, on the panel stream ...
+    const int near = std::min(NB, rest);
+    ZG_TRY(gemm_tc(rest, near, (int)ldo, -1.f, wl, ldo, wu, ldo, 1.f, A12 + jb, lda, abt,
+                   &ctl->status, sp));
+    // ... the rest on the bulk stream, beside the next block's panel
+    if (rest > near) {
+      ZG_CUDA(cudaEventRecord(la.upd[b % R], sp));
+      ZG_CUDA(cudaStreamWaitEvent(sb, la.upd[b % R], 0));
+      ZG_TRY(gemm_tc(rest, rest - near, (int)ldo, -1.f, wl, ldo, wu + (long)near * ldo, ldo, 1.f,
+                     A12 + jb + (long)near * lda, lda, abt, &ctl->status, sb));
+    }
+    ZG_CUDA(cudaEventRecord(la.bulk_done[b % R], sb));
   }
   return 0;
 }
-
 // Low-precision Cholesky (lower) of an n x n SPD FP32 matrix: FP32 64-wide
 // diagonal blocks, FP32 block-column TRSM, trailing SYRK on the tensor cores
 // (lower 128 x 128 tiles only), NB = 256.  The first non-positive pivot lands
