@@ -109,7 +109,9 @@ __global__ void __launch_bounds__(256)
 
   // Epilogue.  Every warp first loads its part of the old C (beta != 0) into
   // registers, so those loads overlap the MMAs still in flight, then waits
-  // for the accumulator and drains its 32 rows.
+  // for the accumulator and drains its 32 rows.  The old C is read through
+  // L2 only (ld.global.cg): with the factorization's two streams, kernels of
+  // the other stream may have rewritten C since this SM last cached it.
   const int quarter = warp & 3, half = warp >> 2;
   const int row = m0 + quarter * 32 + lane;
   constexpr int kCols = BN / 2, kChunks = kCols / 32;
@@ -121,7 +123,7 @@ __global__ void __launch_bounds__(256)
     const float *base = C + row + (long)(n0 + c) * ldc;
     const int nc = min(32, N - (n0 + c));
 #pragma unroll
-    for (int j = 0; j < 32; ++j) old[q][j] = (pre && j < nc) ? __ldcs(base + (long)j * ldc) : 0.f;
+    for (int j = 0; j < 32; ++j) old[q][j] = (pre && j < nc) ? __ldcg(base + (long)j * ldc) : 0.f;
   }
   const bool have = tc::mbar_wait(done, 0, status);
   tc::tc_fence_after();

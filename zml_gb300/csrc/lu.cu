@@ -299,7 +299,10 @@ __global__ void __launch_bounds__(256) laswp_prep_kernel(int k1, int k2,
 
 // One warp per column, lanes over the pairs: every moved value of the column
 // is loaded into registers (all loads of the column in flight at once, and
-// all inside one column's span of memory), then the warp stores them.
+// all inside one column's span of memory), then the warp stores them.  Loads
+// and stores go through L2 only: the mixed LU runs this kernel beside kernels
+// of another stream that rewrite the same columns, and a line this SM cached
+// earlier would be stale.
 template <typename T>
 __global__ void __launch_bounds__(256) laswp_apply_kernel(int n, T *A, long lda,
                                                                const int *__restrict__ pairs,
@@ -316,13 +319,13 @@ __global__ void __launch_bounds__(256) laswp_apply_kernel(int n, T *A, long lda,
 #pragma unroll
     for (int u = 0; u < kPer; ++u) {
       const int t = lane + 32 * u;
-      if (t < np) v[u] = col[pr[2 * t + 1]];
+      if (t < np) v[u] = __ldcg(col + pr[2 * t + 1]);
     }
     __syncwarp();
 #pragma unroll
     for (int u = 0; u < kPer; ++u) {
       const int t = lane + 32 * u;
-      if (t < np) col[pr[2 * t]] = v[u];
+      if (t < np) __stcg(col + pr[2 * t], v[u]);
     }
     __syncwarp();
   }

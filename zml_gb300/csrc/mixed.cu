@@ -43,7 +43,7 @@ __global__ void to_kmajor_t_kernel(int rows, int k, const float *A, long lda, H 
   const int r0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
   for (int c = threadIdx.y; c < 32; c += 8) {
     int r = r0 + threadIdx.x, kk = k0 + c;
-    t[c][threadIdx.x] = (r < rows && kk < k) ? A[r + (long)kk * lda] : 0.f;
+    t[c][threadIdx.x] = (r < rows && kk < k) ? __ldcg(A + r + (long)kk * lda) : 0.f;
   }
   __syncthreads();
   for (int c = threadIdx.y; c < 32; c += 8) {
@@ -70,7 +70,7 @@ __global__ void to_kmajor_n_kernel(int k, int cols, const float *A, long lda, H 
   for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total;
        e += (long)gridDim.x * blockDim.x) {
     int kk = e % ldk, c = e / ldk;
-    const float v = kk < k ? A[kk + (long)c * lda] : 0.f;
+    const float v = kk < k ? __ldcg(A + kk + (long)c * lda) : 0.f;
     const H hi = to16<H>(v);
     H *o = out + (long)c * ldo + kk;
     o[0] = hi;
@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(32 * kInvColsPerCta)
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int k = k0 + 2 * u;
-        t[u] = (k < nb && i > k && i < nb) ? L[i + (long)k * ldl] : 0.f;
+        t[u] = (k < nb && i > k && i < nb) ? __ldcg(L + i + (long)k * ldl) : 0.f;
       }
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
@@ -207,12 +207,12 @@ __global__ void gemm_small_kernel(int m, int n, int k, float alpha, const float 
   float a0 = 0.f, a1 = 0.f;
   int q = 0;
   for (; q + 1 < k; q += 2) {
-    a0 = fmaf(A[i + (long)q * lda], B[q + (long)j * ldb], a0);
-    a1 = fmaf(A[i + (long)(q + 1) * lda], B[q + 1 + (long)j * ldb], a1);
+    a0 = fmaf(__ldcg(A + i + (long)q * lda), __ldcg(B + q + (long)j * ldb), a0);
+    a1 = fmaf(__ldcg(A + i + (long)(q + 1) * lda), __ldcg(B + q + 1 + (long)j * ldb), a1);
   }
-  if (q < k) a0 = fmaf(A[i + (long)q * lda], B[q + (long)j * ldb], a0);
+  if (q < k) a0 = fmaf(__ldcg(A + i + (long)q * lda), __ldcg(B + q + (long)j * ldb), a0);
   const float v = alpha * (a0 + a1);
-  C[i + (long)j * ldc] = beta == 0.f ? v : v + beta * C[i + (long)j * ldc];
+  C[i + (long)j * ldc] = beta == 0.f ? v : v + beta * __ldcg(C + i + (long)j * ldc);
 }
 
 // C (m x n) = alpha A B + beta C for m, k <= 128: one CTA per 32 columns of
@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(256) gemm128_kernel(int m, int n, int k, float
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       const int q = q0 + 2 * u;
-      t[u] = (lr < m && q < k) ? A[lr + (long)q * lda] : 0.f;
+      t[u] = (lr < m && q < k) ? __ldcg(A + lr + (long)q * lda) : 0.f;
     }
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(256) gemm128_kernel(int m, int n, int k, float
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
       const int c = cp + 2 * u;
-      t[u] = (lr < k && c < nc) ? B[lr + (long)(j0 + c) * ldb] : 0.f;
+      t[u] = (lr < k && c < nc) ? __ldcg(B + lr + (long)(j0 + c) * ldb) : 0.f;
     }
 #pragma unroll
     for (int u = 0; u < 16; ++u) sB[lr * 33 + cp + 2 * u] = t[u];
@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(256) gemm128_kernel(int m, int n, int k, float
       const int r = lane + 32 * u, c = warp + 8 * v;
       if (r < m && c < nc) {
         float *cp = C + r + (long)(j0 + c) * ldc;
-        *cp = beta != 0.f ? fmaf(alpha, acc[u][v], beta * *cp) : alpha * acc[u][v];
+        *cp = beta != 0.f ? fmaf(alpha, acc[u][v], beta * __ldcg(cp)) : alpha * acc[u][v];
       }
     }
 }
