@@ -356,6 +356,134 @@ __device__ void solve_inplace(View<F> M, int n, bool spd, const int *ipiv, V *X,
   }
 }
 
+// The same solve with X held in registers: thread t owns rows t + nt r
+// (r < 4) of up to four right-hand sides at a time, loaded with the row
+// interchanges already applied (row i takes row src(i), the swaps traced
+// backwards); at step k the owner of row k forms x_k and broadcasts it (a
+// shuffle for a one-warp group, else one of two alternating shared slots
+// behind one barrier), and every thread updates its rows, the factor's next
+// column prefetched meanwhile.  Needs n <= 4 nt; xs: 2 x 4 values of shared
+// memory for the group.
+template <typename F, typename V>
+__device__ void solve_regs(View<F> M, int n, bool spd, const int *ipiv, V *X, int ldx, int nrhs,
+                           int tid, int nt, int gid, V (*xs)[4]) {
+  constexpr int RM = 4, RC = 4;
+  for (int c0 = 0; c0 < nrhs; c0 += RC) {
+    const int nc = min(RC, nrhs - c0);
+    V xr[RM][RC];
+#pragma unroll
+    for (int r = 0; r < RM; ++r) {
+      const int i = tid + nt * r;
+      int src = i;
+      if (!spd && i < n)
+        for (int k = n - 1; k >= 0; --k) {
+          const int p = ipiv[k] - 1;
+          if (src == k) src = p;
+          else if (src == p) src = k;
+        }
+#pragma unroll
+      for (int c = 0; c < RC; ++c)
+        xr[r][c] = (i < n && c < nc) ? X[src + (long)(c0 + c) * ldx] : V(0);
+    }
+    group_sync(gid, nt);  // every source row read before any row is written back
+    auto step = [&](int k, const F (&mc)[RM], bool below) {
+      const int owner = k % nt, slot = k / nt;
+      V xk[RC];
+#pragma unroll
+      for (int c = 0; c < RC; ++c) xk[c] = V(0);
+      if (tid == owner) {
+        const V d = (below && !spd) ? V(1) : (V)M(k, k);
+#pragma unroll
+        for (int r = 0; r < RM; ++r)
+          if (r == slot)
+#pragma unroll
+            for (int c = 0; c < RC; ++c) {
+              xr[r][c] = (below && !spd) ? xr[r][c] : xr[r][c] / d;
+              xk[c] = xr[r][c];
+            }
+        if (nt > 32)
+#pragma unroll
+          for (int c = 0; c < RC; ++c) xs[k & 1][c] = xk[c];
+      }
+      if (nt == 32) {
+#pragma unroll
+        for (int c = 0; c < RC; ++c) xk[c] = __shfl_sync(0xffffffffu, xk[c], owner);
+      } else {
+        group_sync(gid, nt);
+#pragma unroll
+        for (int c = 0; c < RC; ++c) xk[c] = xs[k & 1][c];
+      }
+#pragma unroll
+      for (int r = 0; r < RM; ++r) {
+        const int i = tid + nt * r;
+        if (i < n && (below ? i > k : i < k))
+#pragma unroll
+          for (int c = 0; c < RC; ++c) xr[r][c] -= (V)mc[r] * xk[c];
+      }
+    };
+    // forward: unit L (LU) or L (Cholesky)
+    {
+      F mc[RM], mn[RM];
+#pragma unroll
+      for (int r = 0; r < RM; ++r) {
+        const int i = tid + nt * r;
+        mc[r] = (i > 0 && i < n) ? M(i, 0) : F(0);
+      }
+      for (int k = 0; k < n; ++k) {
+#pragma unroll
+        for (int r = 0; r < RM; ++r) {
+          const int i = tid + nt * r;
+          mn[r] = (k + 1 < n && i > k + 1 && i < n) ? M(i, k + 1) : F(0);
+        }
+        step(k, mc, true);
+#pragma unroll
+        for (int r = 0; r < RM; ++r) mc[r] = mn[r];
+      }
+    }
+    // backward: U (LU) or L^T (Cholesky)
+    {
+      F mc[RM], mn[RM];
+      auto u = [&](int i, int k) { return spd ? M(k, i) : M(i, k); };
+#pragma unroll
+      for (int r = 0; r < RM; ++r) {
+        const int i = tid + nt * r;
+        mc[r] = (i < n - 1) ? u(i, n - 1) : F(0);
+      }
+      for (int k = n - 1; k >= 0; --k) {
+#pragma unroll
+        for (int r = 0; r < RM; ++r) {
+          const int i = tid + nt * r;
+          mn[r] = (k > 0 && i < k - 1) ? u(i, k - 1) : F(0);
+        }
+        step(k, mc, false);
+#pragma unroll
+        for (int r = 0; r < RM; ++r) mc[r] = mn[r];
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < RM; ++r) {
+      const int i = tid + nt * r;
+      if (i < n)
+#pragma unroll
+        for (int c = 0; c < RC; ++c)
+          if (c < nc) X[i + (long)(c0 + c) * ldx] = xr[r][c];
+    }
+    group_sync(gid, nt);
+  }
+}
+
+// Register-resident solve where the rows fit four to a thread, else the
+// shared/global one; xs_raw: the group's 16-double scratch.
+template <typename F, typename V>
+__device__ void solve_any(View<F> M, int n, bool spd, const int *ipiv, V *X, int ldx, int nrhs,
+                          int tid, int nt, int gid, double *xs_raw) {
+  if (n <= 4 * nt)
+    solve_regs<F, V>(M, n, spd, ipiv, X, ldx, nrhs, tid, nt, gid,
+                     reinterpret_cast<V (*)[4]>(xs_raw));
+  else
+    solve_inplace<F, V>(M, n, spd, ipiv, X, ldx, nrhs, tid, nt, gid);
+}
+
 // max over the group (for norms)
 __device__ double group_max(double v, int tid, int nt, int gid, double *red) {
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -423,11 +551,11 @@ __device__ void process_matrix(const BatchArgs &a, int mi, int gid, int gt, int 
     if (sizeof(F) == sizeof(double)) {
       for (int e = gt; e < n * nrhs; e += nt) Xg[e] = Bg[e];
       group_sync(gid, nt);
-      solve_inplace<F, double>(M, n, spd, ipiv, Xg, n, nrhs, gt, nt, gid);
+      solve_any<F, double>(M, n, spd, ipiv, Xg, n, nrhs, gt, nt, gid, red[gid]);
     } else {
       for (int e = gt; e < n * nrhs; e += nt) Vf[e] = (float)Bg[e];
       group_sync(gid, nt);
-      solve_inplace<F, float>(M, n, spd, ipiv, Vf, n, nrhs, gt, nt, gid);
+      solve_any<F, float>(M, n, spd, ipiv, Vf, n, nrhs, gt, nt, gid, red[gid]);
       for (int e = gt; e < n * nrhs; e += nt) Xg[e] = (double)Vf[e];
       group_sync(gid, nt);
     }
@@ -472,7 +600,7 @@ __device__ void process_matrix(const BatchArgs &a, int mi, int gid, int gt, int 
         xmax = group_max(xmax, gt, nt, gid, red[gid]);
         if (rmax <= 4.0 * 1.1102230246251565e-16 * anorm * xmax) break;
         group_sync(gid, nt);
-        solve_inplace<F, float>(M, n, spd, ipiv, Vf, n, nrhs, gt, nt, gid);
+        solve_any<F, float>(M, n, spd, ipiv, Vf, n, nrhs, gt, nt, gid, red[gid]);
         for (int e = gt; e < n * nrhs; e += nt) Xg[e] += (double)Vf[e];
         group_sync(gid, nt);
       }
