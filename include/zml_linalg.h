@@ -84,6 +84,22 @@ zml_dmatrix zml_qr_r(const zml_qr_t *f, int mode);
 /* The min(m,n) reflector scalars. */
 const double *zml_qr_tau(const zml_qr_t *f);
 
+/* ---- matmul facade (linalg/matmul.zig:19, its dense cases) -------------- */
+#define ZML_ERR_DIMENSION_MISMATCH (-2003) /* error.DimensionMismatch */
+/* c = a b as a new owned general matrix in a's layout (matmul/dgedge.zig:11-41:
+ * gemm with b transposed when its layout differs from a's), on the GPU GEMM.
+ * a or b may be triangular views (uplo / diag): they are multiplied as the
+ * dense matrices they stand for (zeros outside the triangle, ones on a unit
+ * diagonal), as matmul.zig's element loops for those cases do.  a->cols must
+ * equal b->rows. */
+int zml_dmatmul(const zml_dmatrix *a, const zml_dmatrix *b, zml_dmatrix *c);
+/* y = a x (matmul/dgedv.zig:11, gemv): x has a->cols entries, y a->rows,
+ * strides incx / incy (non-zero; negative as in BLAS). */
+int zml_dmatvec(const zml_dmatrix *a, const double *x, int incx, double *y, int incy);
+/* y = x^T b (matmul/dvdge.zig:11, gemv transposed): x has b->rows entries,
+ * y b->cols. */
+int zml_dvecmat(const double *x, int incx, const zml_dmatrix *b, double *y, int incy);
+
 #ifdef __cplusplus
 }
 #endif

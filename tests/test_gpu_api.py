@@ -132,3 +132,76 @@ def test_qr_objects(m, n, layout):
                                        atol=1e-11 * np.abs(qr_ref).max())
     finally:
         L.zml_qr_deinit(h)
+
+
+def _view(a, layout, uplo=0, diag=0):
+    buf, ld = _layout_buf(a, layout)
+    v = zg.DMatrix()
+    v.data = buf.ctypes.data_as(C.POINTER(C.c_double))
+    v.rows, v.cols = a.shape
+    v.ld = max(1, ld)
+    v.layout, v.uplo, v.diag, v.owns_data = layout, uplo, diag, 0
+    return v, buf
+
+
+def _dense(a, uplo, diag):
+    if uplo == 0:
+        return a
+    t = np.triu(a) if uplo == 121 else np.tril(a)
+    if diag == 132:
+        np.fill_diagonal(t, 1.0)
+    return t
+
+
+@pytest.mark.parametrize("la,lb", [(102, 102), (101, 101), (102, 101), (101, 102)])
+@pytest.mark.parametrize("m,k,n", [(150, 90, 70), (64, 257, 33)])
+def test_matmul_facade_general(la, lb, m, k, n):
+    """c = a b (matmul/dgedge.zig): result in a's layout, any layout of b."""
+    L = zg.lib()
+    a, b = gaussian(m, k, seed=1), gaussian(k, n, seed=2)
+    va, ka = _view(a, la)
+    vb, kb = _view(b, lb)
+    c = zg.DMatrix()
+    assert L.zml_dmatmul(C.byref(va), C.byref(vb), C.byref(c)) == 0
+    assert (c.rows, c.cols, c.layout, c.owns_data) == (m, n, la, 1)
+    ref = a @ b
+    np.testing.assert_allclose(c.to_numpy(), ref, rtol=0, atol=8 * k * EPS * np.abs(a).max() * np.abs(b).max())
+    L.zml_dmatrix_deinit(C.byref(c))
+
+
+@pytest.mark.parametrize("uplo,diag", [(121, 131), (122, 132)])
+def test_matmul_facade_triangular_views(uplo, diag):
+    """Triangular views multiply as the dense matrices they stand for."""
+    L = zg.lib()
+    n = 96
+    a, b = gaussian(n, seed=3), gaussian(n, 40, seed=4)
+    va, ka = _view(a, 101, uplo, diag)
+    vb, kb = _view(b, 102)
+    c = zg.DMatrix()
+    assert L.zml_dmatmul(C.byref(va), C.byref(vb), C.byref(c)) == 0
+    np.testing.assert_allclose(c.to_numpy(), _dense(a, uplo, diag) @ b, rtol=0, atol=1e-12)
+    L.zml_dmatrix_deinit(C.byref(c))
+    # and on the right
+    vt, kt = _view(a, 102, uplo, diag)
+    vg, kg = _view(gaussian(30, n, seed=5), 101)
+    assert L.zml_dmatmul(C.byref(vg), C.byref(vt), C.byref(c)) == 0
+    np.testing.assert_allclose(c.to_numpy(), gaussian(30, n, seed=5) @ _dense(a, uplo, diag),
+                               rtol=0, atol=1e-12)
+    L.zml_dmatrix_deinit(C.byref(c))
+
+
+@pytest.mark.parametrize("layout", [101, 102])
+def test_matvec_and_vecmat_facade(layout):
+    """y = a x (dgedv.zig) and y = x^T a (dvdge.zig), with strides."""
+    L = zg.lib()
+    m, n = 120, 77
+    a = gaussian(m, n, seed=6)
+    va, ka = _view(a, layout)
+    x = np.random.default_rng(7).standard_normal(2 * n)
+    y = np.zeros(3 * m)
+    assert L.zml_dmatvec(C.byref(va), _ptr(x), 2, _ptr(y), 3) == 0
+    np.testing.assert_allclose(y[::3], a @ x[::2], rtol=0, atol=1e-12)
+    xv = np.random.default_rng(8).standard_normal(m)
+    yv = np.zeros(n)
+    assert L.zml_dvecmat(_ptr(xv), -1, C.byref(va), _ptr(yv), 1) == 0
+    np.testing.assert_allclose(yv, xv[::-1] @ a, rtol=0, atol=1e-12)

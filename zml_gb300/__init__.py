@@ -153,6 +153,7 @@ class DMatrix(C.Structure):
 
 
 ERR_INVALID_ARGUMENT, ERR_SINGULAR_MATRIX, ERR_OUT_OF_MEMORY = -2000, -2001, -2002
+ERR_DIMENSION_MISMATCH = -2003
 QR_FULL, QR_ECONOMICAL = 0, 1
 _pp = C.POINTER(vp)
 _SIGS.update({
@@ -173,6 +174,9 @@ _SIGS.update({
     "zml_qr_q": (i32, [vp, i32, C.POINTER(DMatrix)]),
     "zml_qr_r": (DMatrix, [vp, i32]),
     "zml_qr_tau": (C.POINTER(C.c_double), [vp]),
+    "zml_dmatmul": (i32, [C.POINTER(DMatrix), C.POINTER(DMatrix), C.POINTER(DMatrix)]),
+    "zml_dmatvec": (i32, [C.POINTER(DMatrix), vp, i32, vp, i32]),
+    "zml_dvecmat": (i32, [vp, i32, C.POINTER(DMatrix), vp, i32]),
 })
 
 PREC_FP16, PREC_BF16, PREC_FP32, PREC_BF16X3 = 0, 1, 2, 3

@@ -11,10 +11,16 @@
 // frees it when qr returns), and QR.q copies only the columns the factor
 // storage has (qr.zig:57-68 copies m columns from an m x n array in full
 // mode; orgqr overwrites the extra ones with identity columns either way).
+//
+// The matmul facade (linalg/matmul.zig:19) routes its dense cases to the
+// library's GEMM: matrix x matrix as matmul/dgedge.zig:11-41 (result in a's
+// layout, b transposed when its layout differs), matrix x vector and vector
+// x matrix as dgedv.zig:11 / dvdge.zig:11 (gemv, here one-column GEMMs).
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
 
+#include "cblas.h"
 #include "clapack.h"
 #include "zml_linalg.h"
 
@@ -278,5 +284,123 @@ zml_dmatrix zml_qr_r(const zml_qr_t *f, int mode) {
 }
 
 const double *zml_qr_tau(const zml_qr_t *f) { return f ? f->tau : nullptr; }
+
+}  // extern "C"
+
+namespace {
+
+bool matrix_ok(const zml_dmatrix *x) {
+  if (!x || !layout_ok(x->layout) || x->rows < 0 || x->cols < 0) return false;
+  if (x->uplo != 0 && x->uplo != 121 && x->uplo != 122) return false;
+  if (x->uplo != 0 && x->diag != 131 && x->diag != 132) return false;
+  const int inner = x->layout == LAPACK_COL_MAJOR ? x->rows : x->cols;
+  if (x->ld < std::max(1, inner)) return false;
+  return x->data || (long)x->rows * x->cols == 0;
+}
+
+// Element (i, j) of the dense matrix a view stands for.
+double element(const zml_dmatrix &x, int i, int j) {
+  if (x.uplo != 0) {
+    if (x.uplo == 121 ? i > j : i < j) return 0.0;
+    if (i == j && x.diag == 132) return 1.0;
+  }
+  return x.data[at(x.layout, i, j, x.ld)];
+}
+
+// A general operand for GEMM: the view itself, or (triangular views) a packed
+// dense copy in the view's layout, returned in *tmp for the caller to free.
+const double *operand(const zml_dmatrix &x, int *ld, double **tmp) {
+  *tmp = nullptr;
+  if (x.uplo == 0) {
+    *ld = x.ld;
+    return x.data;
+  }
+  const int pld = std::max(1, x.layout == LAPACK_COL_MAJOR ? x.rows : x.cols);
+  double *d = (double *)std::malloc(sizeof(double) * std::max<size_t>(1, (size_t)x.rows * x.cols));
+  if (!d) return nullptr;
+  for (int i = 0; i < x.rows; ++i)
+    for (int j = 0; j < x.cols; ++j) d[at(x.layout, i, j, pld)] = element(x, i, j);
+  *tmp = d;
+  *ld = pld;
+  return d;
+}
+
+long vindex(int i, int len, int inc) { return inc > 0 ? (long)i * inc : (long)(len - 1 - i) * -inc; }
+
+// y (len_y) = op(a) x (len_x), op = a or a^T, through a one-column GEMM.
+int gemv_facade(const zml_dmatrix *a, bool trans, const double *x, int incx, double *y,
+                int incy) {
+  if (!matrix_ok(a) || incx == 0 || incy == 0) return ZML_ERR_INVALID_ARGUMENT;
+  const int len_x = trans ? a->rows : a->cols, len_y = trans ? a->cols : a->rows;
+  if ((!x && len_x > 0) || (!y && len_y > 0)) return ZML_ERR_INVALID_ARGUMENT;
+  if (len_y == 0) return 0;
+  double *xc = (double *)std::malloc(sizeof(double) * std::max(1, len_x));
+  double *yc = (double *)std::malloc(sizeof(double) * len_y);
+  double *tmp = nullptr;
+  int lda = 0;
+  const double *A = xc && yc ? operand(*a, &lda, &tmp) : nullptr;
+  if (!A) {
+    std::free(xc);
+    std::free(yc);
+    return ZML_ERR_OUT_OF_MEMORY;
+  }
+  for (int i = 0; i < len_x; ++i) xc[i] = x[vindex(i, len_x, incx)];
+  if (len_x == 0) {
+    std::fill(yc, yc + len_y, 0.0);
+  } else {
+    // one column: ld 1 in row-major order, the vector length in column-major
+    const bool col = a->layout == LAPACK_COL_MAJOR;
+    cblas_dgemm((CBLAS_ORDER)a->layout, trans ? CblasTrans : CblasNoTrans, CblasNoTrans, len_y, 1,
+                len_x, 1.0, A, lda, xc, col ? len_x : 1, 0.0, yc, col ? len_y : 1);
+  }
+  for (int i = 0; i < len_y; ++i) y[vindex(i, len_y, incy)] = yc[i];
+  std::free(tmp);
+  std::free(xc);
+  std::free(yc);
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int zml_dmatmul(const zml_dmatrix *a, const zml_dmatrix *b, zml_dmatrix *c) {
+  if (!c) return ZML_ERR_INVALID_ARGUMENT;
+  std::memset(c, 0, sizeof *c);
+  if (!matrix_ok(a) || !matrix_ok(b)) return ZML_ERR_INVALID_ARGUMENT;
+  if (a->cols != b->rows) return ZML_ERR_DIMENSION_MISMATCH;
+  const int m = a->rows, k = a->cols, n = b->cols;
+  const int layout = a->layout;
+  const int ldc = std::max(1, layout == LAPACK_COL_MAJOR ? m : n);
+  double *d = (double *)std::calloc(std::max<size_t>(1, (size_t)m * n), sizeof(double));
+  if (!d) return ZML_ERR_OUT_OF_MEMORY;
+  if (m > 0 && n > 0 && k > 0) {
+    double *ta = nullptr, *tb = nullptr;
+    int lda = 0, ldb = 0;
+    const double *A = operand(*a, &lda, &ta), *B = operand(*b, &ldb, &tb);
+    if (!A || !B) {
+      std::free(ta);
+      std::free(tb);
+      std::free(d);
+      return ZML_ERR_OUT_OF_MEMORY;
+    }
+    cblas_dgemm((CBLAS_ORDER)layout, CblasNoTrans,
+                b->layout == layout ? CblasNoTrans : CblasTrans, m, n, k, 1.0, A, lda, B, ldb, 0.0,
+                d, ldc);
+    std::free(ta);
+    std::free(tb);
+  }
+  *c = view(d, m, n, ldc, layout, 0, 0);
+  c->owns_data = 1;
+  return 0;
+}
+
+int zml_dmatvec(const zml_dmatrix *a, const double *x, int incx, double *y, int incy) {
+  return gemv_facade(a, false, x, incx, y, incy);
+}
+
+int zml_dvecmat(const double *x, int incx, const zml_dmatrix *b, double *y, int incy) {
+  return gemv_facade(b, true, x, incx, y, incy);
+}
 
 }  // extern "C"
