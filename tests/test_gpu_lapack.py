@@ -115,6 +115,39 @@ def test_dgetrs_vs_oracle(trans, nrhs):
     np.testing.assert_allclose(bg, x, rtol=1e-8, atol=1e-9)
 
 
+@pytest.mark.parametrize("n,nrhs", [(512, 1), (641, 3), (1300, 1), (2100, 4)])
+def test_dgetrs_one_launch_solves_vs_oracle(n, nrhs):
+    """Up to four right-hand sides with n >= 512 take the one-launch triangular
+    solves (blocks of 128 rows; n = 641, 1300 and 2100 end on a ragged block);
+    leading dimensions larger than n on the device."""
+    import torch
+    a = gaussian(n, seed=n)
+    x = np.random.default_rng(n + 1).uniform(-1, 1, (n, nrhs))
+    b = a @ x
+    lda, ldb = n + 3, n + 5
+    da = torch.zeros((n, lda), dtype=torch.float64)
+    da[:, :n] = torch.from_numpy(a.T.copy())
+    da = da.cuda()
+    db = torch.zeros((nrhs, ldb), dtype=torch.float64)
+    db[:, :n] = torch.from_numpy(b.T.copy())
+    db = db.cuda()
+    dp = torch.zeros(n, dtype=torch.int32, device="cuda")
+    info = np.zeros(1, dtype=np.int32)
+    L = zg.lib()
+    assert L.zml_gpu_dgetrf(n, n, da.data_ptr(), lda, dp.data_ptr(), P(info), None) == 0
+    assert info[0] == 0
+    assert L.zml_gpu_dgetrs(b"N", n, nrhs, da.data_ptr(), lda, dp.data_ptr(), db.data_ptr(), ldb,
+                            None) == 0
+    lu = np.asfortranarray(da.cpu().numpy()[:, :n].T)
+    ipiv = dp.cpu().numpy()
+    br = ol.getrs(lu, ipiv, np.asfortranarray(b), 111)
+    xg = db.cpu().numpy()[:, :n].T
+    np.testing.assert_allclose(xg, br, rtol=1e-9, atol=1e-10)
+    np.testing.assert_allclose(xg, x, rtol=1e-7, atol=1e-8)
+    # the padding between columns is untouched
+    assert not db.cpu().numpy()[:, n:].any()
+
+
 def test_dgesv_row_major():
     n, nrhs = 200, 3
     a = gaussian(n, seed=31)

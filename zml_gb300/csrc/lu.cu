@@ -436,11 +436,225 @@ int getrf_dev(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s
   return check_status(s, ctl, info);
 }
 
+// ---------------------------------------------------------------------------
+// One right-hand side against an FP64 factor in one launch (getrs, trans N).
+// 128-row blocks, one CTA each, claimed in dependency order by ticket: a CTA
+// streams its block row's off-diagonal tiles (128 x 64 halves, the next half
+// prefetched), each multiplied by the x an earlier block published, then
+// solves its diagonal block by substitution (the backward-stable arithmetic
+// of trsm, not an inverse) and publishes its x.  GB300 runs about two FP64
+// FMAs per clock per SM, so the substitution keeps only each 32-row
+// sub-triangle on its serial chain (one warp, a row a lane, x_k by shuffle,
+// the upper solve multiplying by reciprocals formed up front) and all 16 warps
+// subtract the solved sub-block from the rows still to solve.  Publication: a
+// buffer pre-filled with an all-ones word, polled word by word (bounded; a
+// timeout sets the stream's status bit).
+constexpr int kFB = 128, kFT = 512, kFH = 16;  // block rows, threads, columns a thread per half tile
+constexpr unsigned long long kFEmpty = ~0ull;
+
+__device__ __forceinline__ unsigned long long ld_relaxed_b64(const double *p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__global__ void __launch_bounds__(kFT) trsv_f64_kernel(int n, const double *__restrict__ A,
+                                                       long lda, const double *rhs_in, double *x,
+                                                       double *xpub, unsigned *ticket, bool upper,
+                                                       unsigned *status) {
+  extern __shared__ double sD[];  // the diagonal block, sD[i + j kFB]
+  __shared__ unsigned sb;
+  __shared__ double part[4][kFB];
+  __shared__ double xs[kFB];
+  __shared__ double rd[kFB];  // reciprocals of the diagonal (upper)
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) sb = atomicAdd(ticket, 1u);
+  __syncthreads();
+  const int nblk = (n + kFB - 1) / kFB, t = sb;
+  const int blk = upper ? nblk - 1 - t : t;
+  const int r0 = blk * kFB, rows = min(kFB, n - r0);
+  const int lr = tid % kFB, ph = tid / kFB, row = r0 + lr;
+  const bool row_ok = lr < rows;
+  for (int e = tid; e < kFB * kFB; e += kFT) {
+    const int i = e % kFB, j = e / kFB;
+    sD[e] = (i < rows && j < rows) ? __ldcg(A + (r0 + i) + (long)(r0 + j) * lda)
+                                   : (i == j ? 1.0 : 0.0);
+  }
+  if (upper && tid < kFB)
+    rd[tid] = tid < rows ? 1.0 / __ldcg(A + (r0 + tid) + (long)(r0 + tid) * lda) : 1.0;
+  const double rhs = (ph == 0 && row_ok) ? rhs_in[row] : 0.0;
+  auto col0 = [&](int q) { return (upper ? nblk - 1 - q : q) * kFB; };
+  auto load_half = [&](int hq, double (&v)[kFH]) {
+    const int c0 = col0(hq >> 1) + 64 * (hq & 1);
+#pragma unroll
+    for (int j = 0; j < kFH; ++j) {
+      const int c = c0 + ph + 4 * j;
+      v[j] = (row_ok && c < n) ? __ldcs(A + row + (long)c * lda) : 0.0;
+    }
+  };
+  double acc0 = 0, acc1 = 0;
+  double cur[kFH], nxt[kFH];
+  const int nh = 2 * t;
+  if (nh > 0) load_half(0, cur);
+  for (int hq = 0; hq < nh; ++hq) {
+    if (hq + 1 < nh) load_half(hq + 1, nxt);
+    if ((hq & 1) == 0) {
+      if (tid < kFB) {
+        const int c = col0(hq >> 1) + tid;
+        double xv = 0.0;
+        if (c < n) {
+          unsigned long long w = ld_relaxed_b64(xpub + c);
+          long long spins = 0;
+          while (w == kFEmpty) {
+            if (++spins > kSpinLimit) {
+              atomicOr(status, kStatusQueueTimeout);
+              break;
+            }
+            if (spins > 64) __nanosleep(32);
+            w = ld_relaxed_b64(xpub + c);
+          }
+          xv = __longlong_as_double((long long)w);
+        }
+        xs[tid] = xv;
+      }
+      __syncthreads();
+    }
+    const int xo = 64 * (hq & 1) + ph;
+#pragma unroll
+    for (int j = 0; j < kFH; j += 2) {
+      acc0 = fma(cur[j], xs[xo + 4 * j], acc0);
+      acc1 = fma(cur[j + 1], xs[xo + 4 * (j + 1)], acc1);
+    }
+    if (hq & 1) __syncthreads();  // xs free for the next tile
+#pragma unroll
+    for (int j = 0; j < kFH; ++j) cur[j] = nxt[j];
+  }
+  part[ph][lr] = acc0 + acc1;
+  __syncthreads();
+  if (tid < kFB)
+    xs[tid] = row_ok ? rhs - (part[0][tid] + part[1][tid] + part[2][tid] + part[3][tid]) : 0.0;
+  __syncthreads();
+  // the diagonal block (padded with the identity past `rows`)
+  for (int s4 = 0; s4 < 4; ++s4) {
+    const int o = 32 * (upper ? 3 - s4 : s4);
+    if (warp == 0) {
+      double y = xs[o + lane];
+      const double *dcol = sD + o + lane + o * kFB;
+      if (!upper) {
+#pragma unroll
+        for (int k = 0; k < 31; ++k) {
+          const double xk = __shfl_sync(0xffffffffu, y, k);
+          if (lane > k) y = fma(-dcol[k * kFB], xk, y);
+        }
+      } else {
+#pragma unroll
+        for (int k = 31; k >= 0; --k) {
+          if (lane == k) y *= rd[o + k];
+          const double xk = __shfl_sync(0xffffffffu, y, k);
+          if (lane < k) y = fma(-dcol[k * kFB], xk, y);
+        }
+      }
+      xs[o + lane] = y;
+    }
+    __syncthreads();
+    const int lo = upper ? 0 : o + 32, hi = upper ? o : kFB;  // rows still to solve
+    if (lo < hi) {
+      if (lr >= lo && lr < hi) {
+        double a = 0.0;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) a = fma(sD[lr + (o + 8 * ph + c) * kFB], xs[o + 8 * ph + c], a);
+        part[ph][lr] = a;
+      }
+      __syncthreads();
+      if (tid >= lo && tid < hi) xs[tid] -= (part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]);
+      __syncthreads();
+    }
+  }
+  if (tid < rows) {
+    const double v = xs[tid];
+    x[r0 + tid] = v;
+    xpub[r0 + tid] = v != v ? __longlong_as_double(0x7ff8000000000000ll) : v;
+  }
+}
+
+// y = P b for nrhs columns, P the interchanges ipiv[0..n) applied in order
+// (dlaswp, incx = 1): row i of the result is row sigma(i) of b, found by
+// walking the interchanges from the last to the first (an interchange of
+// rows j and p moves whatever sits at j to p and back), one thread a row.
+// An index outside [1, n] yields NaN rows instead of an out-of-bounds read.
+__global__ void __launch_bounds__(128) perm_gather_kernel(int n, int nrhs,
+                                                          const int *__restrict__ ipiv,
+                                                          const double *__restrict__ B, long ldb,
+                                                          double *Y) {
+  __shared__ int sp[1024];
+  const int i = blockIdx.x * 128 + threadIdx.x;
+  int pos = i;
+  for (int hi = n - 1; hi >= 0; hi -= 1024) {
+    const int lo = max(0, hi - 1023);
+    __syncthreads();
+    for (int e = threadIdx.x; e <= hi - lo; e += 128) sp[e] = ipiv[lo + e] - 1;
+    __syncthreads();
+#pragma unroll 8
+    for (int j = hi; j >= lo; --j) {
+      const int p = sp[j - lo];
+      pos = pos == j ? p : (pos == p ? j : pos);
+    }
+  }
+  if (i < n) {
+    const bool ok = (unsigned)pos < (unsigned)n;
+    for (int c = 0; c < nrhs; ++c)
+      Y[i + (long)c * n] = ok ? __ldcg(B + pos + (long)c * ldb)
+                              : __longlong_as_double(0x7ff8000000000000ll);
+  }
+}
+
+// x <- op^-1 rhs for one column, op = unit lower L or non-unit upper U of the
+// FP64 factor A (rhs may be x); xw: n + 1 doubles of scratch.
+static int trsv_f64(int n, const double *A, long lda, const double *rhs, double *x, bool upper,
+                    double *xw, unsigned *status, cudaStream_t s) {
+  const int nblk = ceil_div(n, kFB);
+  const size_t smem = sizeof(double) * kFB * kFB;
+  static bool attr = false;
+  if (!attr) {
+    ZG_CUDA(cudaFuncSetAttribute(trsv_f64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+    attr = true;
+  }
+  unsigned *ticket = reinterpret_cast<unsigned *>(xw);
+  double *xpub = xw + 1;
+  ZG_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned), s));
+  ZG_CUDA(cudaMemsetAsync(xpub, 0xff, sizeof(double) * n, s));
+  ZG_LAUNCH(kTagTrsmDiag, 1.0 * n * n, 4.0 * n * n + 16.0 * n, s,
+            trsv_f64_kernel<<<nblk, kFT, smem, s>>>(n, A, lda, rhs, x, xpub, ticket, upper,
+                                                    status));
+  return 0;
+}
+
 template <typename T>
 int getrs_dev(int trans, int n, int nrhs, const T *A, long lda, const int *ipiv, T *B, long ldb,
               cudaStream_t s) {
   if (n <= 0 || nrhs <= 0) return 0;
   const bool nt = trans == kNoTrans || trans == kConjNoTrans;
+  if constexpr (sizeof(T) == sizeof(double)) {
+    // a few right-hand sides: one launch per column and triangle
+    if (nt && nrhs <= 4 && n >= 512) {
+      Control *ctl;
+      ZG_TRY(control(s, &ctl));
+      void *w;
+      ZG_TRY(workspace(s, kSlotPanel, sizeof(double) * ((size_t)n * (nrhs + 1) + 1), &w));
+      double *xw = (double *)w, *Y = xw + n + 1;
+      double *Bd = reinterpret_cast<double *>(B);
+      const double *Ad = reinterpret_cast<const double *>(A);
+      ZG_LAUNCH(kTagLaswp, 0, 16.0 * n * nrhs, s,
+                perm_gather_kernel<<<ceil_div(n, 128), 128, 0, s>>>(n, nrhs, ipiv, Bd, ldb, Y));
+      for (int c = 0; c < nrhs; ++c) {
+        double *x = Bd + (long)c * ldb;
+        ZG_TRY(trsv_f64(n, Ad, lda, Y + (long)c * n, x, false, xw, &ctl->status, s));
+        ZG_TRY(trsv_f64(n, Ad, lda, x, x, true, xw, &ctl->status, s));
+      }
+      return 0;
+    }
+  }
   if (nt) {
     ZG_TRY(laswp_dev<T>(nrhs, B, ldb, 1, n, ipiv, 1, s));
     ZG_TRY(trsm_dev<T>(kLeft, kLower, kNoTrans, kUnit, n, nrhs, T(1), A, lda, B, ldb, s));
