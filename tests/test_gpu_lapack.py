@@ -115,15 +115,16 @@ def test_dgetrs_vs_oracle(trans, nrhs):
     np.testing.assert_allclose(bg, x, rtol=1e-8, atol=1e-9)
 
 
+@pytest.mark.parametrize("trans", [b"N", b"T"])
 @pytest.mark.parametrize("n,nrhs", [(512, 1), (641, 3), (1300, 1), (2100, 4)])
-def test_dgetrs_one_launch_solves_vs_oracle(n, nrhs):
+def test_dgetrs_one_launch_solves_vs_oracle(n, nrhs, trans):
     """Up to four right-hand sides with n >= 512 take the one-launch triangular
     solves (blocks of 128 rows; n = 641, 1300 and 2100 end on a ragged block);
     leading dimensions larger than n on the device."""
     import torch
     a = gaussian(n, seed=n)
     x = np.random.default_rng(n + 1).uniform(-1, 1, (n, nrhs))
-    b = a @ x
+    b = (a if trans == b"N" else a.T) @ x
     lda, ldb = n + 3, n + 5
     da = torch.zeros((n, lda), dtype=torch.float64)
     da[:, :n] = torch.from_numpy(a.T.copy())
@@ -136,11 +137,11 @@ def test_dgetrs_one_launch_solves_vs_oracle(n, nrhs):
     L = zg.lib()
     assert L.zml_gpu_dgetrf(n, n, da.data_ptr(), lda, dp.data_ptr(), P(info), None) == 0
     assert info[0] == 0
-    assert L.zml_gpu_dgetrs(b"N", n, nrhs, da.data_ptr(), lda, dp.data_ptr(), db.data_ptr(), ldb,
+    assert L.zml_gpu_dgetrs(trans, n, nrhs, da.data_ptr(), lda, dp.data_ptr(), db.data_ptr(), ldb,
                             None) == 0
     lu = np.asfortranarray(da.cpu().numpy()[:, :n].T)
     ipiv = dp.cpu().numpy()
-    br = ol.getrs(lu, ipiv, np.asfortranarray(b), 111)
+    br = ol.getrs(lu, ipiv, np.asfortranarray(b), 111 if trans == b"N" else 112)
     xg = db.cpu().numpy()[:, :n].T
     np.testing.assert_allclose(xg, br, rtol=1e-9, atol=1e-10)
     np.testing.assert_allclose(xg, x, rtol=1e-7, atol=1e-8)
@@ -209,6 +210,32 @@ def test_dposv_and_potrs(uplo, nrhs):
     b2 = b.copy(order="F")
     assert zg.lib().LAPACKE_dpotrs(102, uplo, n, nrhs, P(f), n, P(b2), n) == 0
     np.testing.assert_allclose(b2, bg, rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize("uplo", [b"L", b"U"])
+@pytest.mark.parametrize("n,nrhs", [(512, 2), (1300, 1), (2100, 4)])
+def test_dpotrs_one_launch_solves_vs_oracle(uplo, n, nrhs):
+    """potrs with up to four right-hand sides and n >= 512 (the one-launch
+    solves: L then L^T, or U^T then U, the transposed triangle walked along
+    A's columns), leading dimension larger than n; the other triangle holds
+    NaNs that must not be read."""
+    a = spd(n, seed=n + 5)
+    x = np.random.default_rng(n + 6).uniform(-1, 1, (n, nrhs))
+    b = a @ x
+    lda = n + 3
+    f = np.zeros((lda, n), order="F")
+    f[:n, :] = a
+    assert zg.lib().LAPACKE_dpotrf(102, uplo, n, P(f), lda) == 0
+    ul = 122 if uplo == b"L" else 121
+    fr, _ = ol.potrf(a, ul)
+    other = np.triu_indices(n, 1) if uplo == b"L" else np.tril_indices(n, -1)
+    fn = f.copy(order="F")
+    fn[other] = np.nan
+    bg = np.asfortranarray(b.copy())
+    assert zg.lib().LAPACKE_dpotrs(102, uplo, n, nrhs, P(fn), lda, P(bg), n) == 0
+    br = ol.potrs(fr, b, ul)
+    np.testing.assert_allclose(bg, br, rtol=1e-9, atol=1e-10)
+    np.testing.assert_allclose(bg, x, rtol=1e-7, atol=1e-8)
 
 
 def test_device_pointer_getrf_getrs():

@@ -102,6 +102,22 @@ template <typename T> int potrf_dev(int uplo, int n, T *A, long lda, int *info, 
 template <typename T>
 int potrs_dev(int uplo, int n, int nrhs, const T *A, long lda, T *B, long ldb, cudaStream_t s) {
   if (n <= 0 || nrhs <= 0) return 0;
+  if constexpr (sizeof(T) == sizeof(double)) {
+    // a few right-hand sides: one launch per column and triangle
+    if (nrhs <= kTrsvMaxRhs && n >= kTrsvMinN) {
+      void *w;
+      ZG_TRY(workspace(s, kSlotPanel, sizeof(double) * ((size_t)n + 1), &w));
+      double *xw = (double *)w;
+      const double *Ad = reinterpret_cast<const double *>(A);
+      const bool up = uplo == kUpper;  // A = U^T U, else A = L L^T
+      for (int c = 0; c < nrhs; ++c) {
+        double *x = reinterpret_cast<double *>(B) + (long)c * ldb;
+        ZG_TRY(trsv_f64(n, Ad, lda, up, false, false, x, x, xw, s));
+        ZG_TRY(trsv_f64(n, Ad, lda, !up, true, false, x, x, xw, s));
+      }
+      return 0;
+    }
+  }
   if (uplo == kUpper) {
     ZG_TRY(trsm_dev<T>(kLeft, kUpper, kTrans, kNonUnit, n, nrhs, T(1), A, lda, B, ldb, s));
     ZG_TRY(trsm_dev<T>(kLeft, kUpper, kNoTrans, kNonUnit, n, nrhs, T(1), A, lda, B, ldb, s));

@@ -85,7 +85,7 @@ enum Slot : int {
   kSlotPiv = 4,               // C ABI: pivots
   kSlotC = 5,                 // C ABI: third matrix (gemm/syrk C)
   kSlotX = 6, kSlotXT = 7,    // C ABI: solution X
-  kSlotPanel = 8,             // LU panel candidate exchange
+  kSlotPanel = 8,             // LU panel candidate exchange; one-launch trsv publication
   kSlotIRVec = 9,             // refinement vectors
   kSlotLowLU = 10,            // low-precision factor copy, pivots, permutation
   kSlotL16 = 11, kSlotU16 = 12,  // 16-bit L21 / U12 operands of the tensor-core update

@@ -65,6 +65,19 @@ int getrs_dev(int trans, int n, int nrhs, const T *A, long lda, const int *ipiv,
 template <typename T>
 int potrf_launch(int uplo, int n, T *A, long lda, Control *ctl, int info_base, cudaStream_t s);
 template <typename T> int potrf_dev(int uplo, int n, T *A, long lda, int *info, cudaStream_t s);
+// Triangular solve of one FP64 column in one launch: x = op(A)^-1 rhs, op(A)
+// = A or A^T (trans), lower or upper, unit or non-unit diagonal; rhs may be
+// x.  xw: n + 1 doubles of device scratch.
+int trsv_f64(int n, const double *A, long lda, bool trans, bool upper, bool unit,
+             const double *rhs, double *x, double *xw, cudaStream_t s);
+// Y = P B, P the interchanges ipiv (1-based, n of them) applied in increasing
+// (forward) or decreasing order; Y must not overlap B.
+int perm_gather_f64(int n, int nrhs, const int *ipiv, bool forward, const double *B, long ldb,
+                    double *Y, long ldy, cudaStream_t s);
+// getrs / potrs take the one-launch solves for up to this many right-hand
+// sides from this order on (FP64).
+constexpr int kTrsvMaxRhs = 4, kTrsvMinN = 512;
+
 template <typename T>
 int potrs_dev(int uplo, int n, int nrhs, const T *A, long lda, T *B, long ldb, cudaStream_t s);
 

@@ -437,19 +437,23 @@ int getrf_dev(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s
 }
 
 // ---------------------------------------------------------------------------
-// One right-hand side against an FP64 factor in one launch (getrs, trans N).
-// 128-row blocks, one CTA each, claimed in dependency order by ticket: a CTA
-// streams its block row's off-diagonal tiles (128 x 64 halves, the next half
-// prefetched), each multiplied by the x an earlier block published, then
-// solves its diagonal block by substitution (the backward-stable arithmetic
-// of trsm, not an inverse) and publishes its x.  GB300 runs about two FP64
-// FMAs per clock per SM, so the substitution keeps only each 32-row
-// sub-triangle on its serial chain (one warp, a row a lane, x_k by shuffle,
-// the upper solve multiplying by reciprocals formed up front) and all 16 warps
-// subtract the solved sub-block from the rows still to solve.  Publication: a
-// buffer pre-filled with an all-ones word, polled word by word (bounded; a
-// timeout sets the stream's status bit).
-constexpr int kFB = 128, kFT = 512, kFH = 16;  // block rows, threads, columns a thread per half tile
+// One right-hand side against a triangle of an FP64 factor in one launch
+// (getrs, potrs): T x = rhs with T = op(A) lower (a forward solve) or upper (a
+// backward solve), op(A) = A or A^T, unit or non-unit diagonal.  128-row
+// blocks, one CTA each, claimed in dependency order by ticket: a CTA streams
+// its block row's off-diagonal tiles (128 x 64 halves, the next half
+// prefetched; for A^T the lanes run along A's columns so that the loads stay
+// coalesced), each multiplied by the x an earlier block published, then solves
+// its diagonal block by substitution (the backward-stable arithmetic of trsm,
+// not an inverse) and publishes its x.  GB300 runs about two FP64 FMAs per
+// clock per SM, so the substitution keeps only each 32-row sub-triangle on its
+// serial chain (one warp, a row a lane, x_k by shuffle, multiplies by
+// reciprocals of the diagonal formed up front) and all 16 warps subtract the
+// solved sub-block from the rows still to solve.  Publication: a buffer
+// pre-filled with an all-ones word, polled word by word (bounded; a timeout
+// sets the stream's status bit).
+constexpr int kFB = 128, kFT = 512, kFH = 16;  // block rows, threads, values a thread per half tile
+constexpr int kFLD = kFB + 1;                  // the diagonal block's leading dimension in SMEM
 constexpr unsigned long long kFEmpty = ~0ull;
 
 __device__ __forceinline__ unsigned long long ld_relaxed_b64(const double *p) {
@@ -458,41 +462,76 @@ __device__ __forceinline__ unsigned long long ld_relaxed_b64(const double *p) {
   return v;
 }
 
+// One 32-row sub-triangle by substitution, a row a lane: x_k broadcast by
+// shuffle, then subtracted from the rows still to solve; a unit diagonal
+// keeps the multiply off the chain.
+template <bool UPPER, bool UNIT>
+__device__ __forceinline__ double chain32(double y, const double *dcol, const double *rd,
+                                          int lane) {
+#pragma unroll
+  for (int s = 0; s < 32; ++s) {
+    const int k = UPPER ? 31 - s : s;
+    if (!UNIT && lane == k) y *= rd[k];
+    const double xk = __shfl_sync(0xffffffffu, y, k);
+    if (UPPER ? lane < k : lane > k) y = fma(-dcol[k * kFLD], xk, y);
+  }
+  return y;
+}
+
+template <bool TRANS>
 __global__ void __launch_bounds__(kFT) trsv_f64_kernel(int n, const double *__restrict__ A,
                                                        long lda, const double *rhs_in, double *x,
-                                                       double *xpub, unsigned *ticket, bool upper,
-                                                       unsigned *status) {
-  extern __shared__ double sD[];  // the diagonal block, sD[i + j kFB]
+                                                       double *xpub, unsigned *ticket,
+                                                       bool upper, bool unit, unsigned *status) {
+  extern __shared__ double sD[];  // the diagonal block of op(A), sD[i + j kFLD]
   __shared__ unsigned sb;
   __shared__ double part[4][kFB];
   __shared__ double xs[kFB];
-  __shared__ double rd[kFB];  // reciprocals of the diagonal (upper)
+  __shared__ double rd[kFB];  // reciprocals of the diagonal
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) sb = atomicAdd(ticket, 1u);
   __syncthreads();
   const int nblk = (n + kFB - 1) / kFB, t = sb;
   const int blk = upper ? nblk - 1 - t : t;
   const int r0 = blk * kFB, rows = min(kFB, n - r0);
-  const int lr = tid % kFB, ph = tid / kFB, row = r0 + lr;
-  const bool row_ok = lr < rows;
+  const int lr = tid % kFB, ph = tid / kFB;
   for (int e = tid; e < kFB * kFB; e += kFT) {
-    const int i = e % kFB, j = e / kFB;
-    sD[e] = (i < rows && j < rows) ? __ldcg(A + (r0 + i) + (long)(r0 + j) * lda)
-                                   : (i == j ? 1.0 : 0.0);
+    // A's contiguous index runs over the threads: op(A) row i for A, column for A^T
+    const int a = e % kFB, b = e / kFB;
+    const int i = TRANS ? b : a, j = TRANS ? a : b;
+    sD[i + j * kFLD] = (a < rows && b < rows) ? __ldcg(A + (r0 + a) + (long)(r0 + b) * lda)
+                                              : (i == j ? 1.0 : 0.0);
   }
-  if (upper && tid < kFB)
-    rd[tid] = tid < rows ? 1.0 / __ldcg(A + (r0 + tid) + (long)(r0 + tid) * lda) : 1.0;
-  const double rhs = (ph == 0 && row_ok) ? rhs_in[row] : 0.0;
+  if (tid < kFB)
+    rd[tid] = (!unit && tid < rows) ? 1.0 / __ldcg(A + (r0 + tid) + (long)(r0 + tid) * lda) : 1.0;
+  const double rhs = tid < rows ? rhs_in[r0 + tid] : 0.0;
   auto col0 = [&](int q) { return (upper ? nblk - 1 - q : q) * kFB; };
+  // A: thread (lr, ph) holds row lr, columns ph + 4 j of the half tile.
+  // A^T: warp w holds rows 8 w .. 8 w + 7, lane columns lane and lane + 32.
   auto load_half = [&](int hq, double (&v)[kFH]) {
     const int c0 = col0(hq >> 1) + 64 * (hq & 1);
+    if constexpr (!TRANS) {
+      const bool ok = lr < rows;
 #pragma unroll
-    for (int j = 0; j < kFH; ++j) {
-      const int c = c0 + ph + 4 * j;
-      v[j] = (row_ok && c < n) ? __ldcs(A + row + (long)c * lda) : 0.0;
+      for (int j = 0; j < kFH; ++j) {
+        const int c = c0 + ph + 4 * j;
+        v[j] = (ok && c < n) ? __ldcs(A + r0 + lr + (long)c * lda) : 0.0;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int rr = 8 * warp + k;
+#pragma unroll
+        for (int m = 0; m < 2; ++m) {
+          const int c = c0 + lane + 32 * m;
+          v[2 * k + m] = (rr < rows && c < n) ? __ldcs(A + c + (long)(r0 + rr) * lda) : 0.0;
+        }
+      }
     }
   };
-  double acc0 = 0, acc1 = 0;
+  double acc[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) acc[k] = 0.0;
   double cur[kFH], nxt[kFH];
   const int nh = 2 * t;
   if (nh > 0) load_half(0, cur);
@@ -519,41 +558,55 @@ __global__ void __launch_bounds__(kFT) trsv_f64_kernel(int n, const double *__re
       }
       __syncthreads();
     }
-    const int xo = 64 * (hq & 1) + ph;
+    if constexpr (!TRANS) {
+      const int xo = 64 * (hq & 1) + ph;
 #pragma unroll
-    for (int j = 0; j < kFH; j += 2) {
-      acc0 = fma(cur[j], xs[xo + 4 * j], acc0);
-      acc1 = fma(cur[j + 1], xs[xo + 4 * (j + 1)], acc1);
+      for (int j = 0; j < kFH; j += 2) {
+        acc[0] = fma(cur[j], xs[xo + 4 * j], acc[0]);
+        acc[1] = fma(cur[j + 1], xs[xo + 4 * (j + 1)], acc[1]);
+      }
+    } else {
+      const double x0 = xs[64 * (hq & 1) + lane], x1 = xs[64 * (hq & 1) + lane + 32];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) acc[k] = fma(cur[2 * k + 1], x1, fma(cur[2 * k], x0, acc[k]));
     }
     if (hq & 1) __syncthreads();  // xs free for the next tile
 #pragma unroll
     for (int j = 0; j < kFH; ++j) cur[j] = nxt[j];
   }
-  part[ph][lr] = acc0 + acc1;
+  if constexpr (!TRANS) {
+    part[ph][lr] = acc[0] + acc[1];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      double v = acc[k];
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+      if (lane == 0) {
+        part[0][8 * warp + k] = v;
+        part[1][8 * warp + k] = 0.0;
+        part[2][8 * warp + k] = 0.0;
+        part[3][8 * warp + k] = 0.0;
+      }
+    }
+  }
   __syncthreads();
   if (tid < kFB)
-    xs[tid] = row_ok ? rhs - (part[0][tid] + part[1][tid] + part[2][tid] + part[3][tid]) : 0.0;
+    xs[tid] = tid < rows ? rhs - ((part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]))
+                         : 0.0;
   __syncthreads();
   // the diagonal block (padded with the identity past `rows`)
   for (int s4 = 0; s4 < 4; ++s4) {
     const int o = 32 * (upper ? 3 - s4 : s4);
     if (warp == 0) {
+      const double *dcol = sD + o + lane + o * kFLD;
       double y = xs[o + lane];
-      const double *dcol = sD + o + lane + o * kFB;
-      if (!upper) {
-#pragma unroll
-        for (int k = 0; k < 31; ++k) {
-          const double xk = __shfl_sync(0xffffffffu, y, k);
-          if (lane > k) y = fma(-dcol[k * kFB], xk, y);
-        }
-      } else {
-#pragma unroll
-        for (int k = 31; k >= 0; --k) {
-          if (lane == k) y *= rd[o + k];
-          const double xk = __shfl_sync(0xffffffffu, y, k);
-          if (lane < k) y = fma(-dcol[k * kFB], xk, y);
-        }
-      }
+      if (!upper)
+        y = unit ? chain32<false, true>(y, dcol, rd + o, lane)
+                 : chain32<false, false>(y, dcol, rd + o, lane);
+      else
+        y = unit ? chain32<true, true>(y, dcol, rd + o, lane)
+                 : chain32<true, false>(y, dcol, rd + o, lane);
       xs[o + lane] = y;
     }
     __syncthreads();
@@ -562,11 +615,13 @@ __global__ void __launch_bounds__(kFT) trsv_f64_kernel(int n, const double *__re
       if (lr >= lo && lr < hi) {
         double a = 0.0;
 #pragma unroll
-        for (int c = 0; c < 8; ++c) a = fma(sD[lr + (o + 8 * ph + c) * kFB], xs[o + 8 * ph + c], a);
+        for (int c = 0; c < 8; ++c)
+          a = fma(sD[lr + (o + 8 * ph + c) * kFLD], xs[o + 8 * ph + c], a);
         part[ph][lr] = a;
       }
       __syncthreads();
-      if (tid >= lo && tid < hi) xs[tid] -= (part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]);
+      if (tid >= lo && tid < hi)
+        xs[tid] -= (part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]);
       __syncthreads();
     }
   }
@@ -577,57 +632,86 @@ __global__ void __launch_bounds__(kFT) trsv_f64_kernel(int n, const double *__re
   }
 }
 
-// y = P b for nrhs columns, P the interchanges ipiv[0..n) applied in order
-// (dlaswp, incx = 1): row i of the result is row sigma(i) of b, found by
-// walking the interchanges from the last to the first (an interchange of
-// rows j and p moves whatever sits at j to p and back), one thread a row.
-// An index outside [1, n] yields NaN rows instead of an out-of-bounds read.
+// Y = P B for nrhs columns, P the interchanges ipiv[0..n) applied in
+// increasing order (dlaswp incx = 1, forward) or decreasing order (incx = -1):
+// row i of Y is row sigma(i) of B, found by undoing the interchanges from the
+// last applied to the first (an interchange of rows j and p moves whatever sits
+// at j to p and back), one thread a row.  An index outside [1, n] yields NaN
+// rows instead of an out-of-bounds read.
 __global__ void __launch_bounds__(128) perm_gather_kernel(int n, int nrhs,
                                                           const int *__restrict__ ipiv,
+                                                          bool forward,
                                                           const double *__restrict__ B, long ldb,
-                                                          double *Y) {
+                                                          double *Y, long ldy) {
   __shared__ int sp[1024];
   const int i = blockIdx.x * 128 + threadIdx.x;
   int pos = i;
-  for (int hi = n - 1; hi >= 0; hi -= 1024) {
-    const int lo = max(0, hi - 1023);
+  for (int q = 0; q * 1024 < n; ++q) {
+    const int lo = forward ? max(0, n - 1024 * (q + 1)) : 1024 * q;
+    const int len = forward ? n - 1024 * q - lo : min(1024, n - lo);
     __syncthreads();
-    for (int e = threadIdx.x; e <= hi - lo; e += 128) sp[e] = ipiv[lo + e] - 1;
+    for (int e = threadIdx.x; e < len; e += 128) sp[e] = ipiv[lo + e] - 1;
     __syncthreads();
+    if (forward) {
 #pragma unroll 8
-    for (int j = hi; j >= lo; --j) {
-      const int p = sp[j - lo];
-      pos = pos == j ? p : (pos == p ? j : pos);
+      for (int e = len - 1; e >= 0; --e) {
+        const int p = sp[e], j = lo + e;
+        pos = pos == j ? p : (pos == p ? j : pos);
+      }
+    } else {
+#pragma unroll 8
+      for (int e = 0; e < len; ++e) {
+        const int p = sp[e], j = lo + e;
+        pos = pos == j ? p : (pos == p ? j : pos);
+      }
     }
   }
   if (i < n) {
     const bool ok = (unsigned)pos < (unsigned)n;
     for (int c = 0; c < nrhs; ++c)
-      Y[i + (long)c * n] = ok ? __ldcg(B + pos + (long)c * ldb)
-                              : __longlong_as_double(0x7ff8000000000000ll);
+      Y[i + (long)c * ldy] = ok ? __ldcg(B + pos + (long)c * ldb)
+                                : __longlong_as_double(0x7ff8000000000000ll);
   }
 }
 
-// x <- op^-1 rhs for one column, op = unit lower L or non-unit upper U of the
-// FP64 factor A (rhs may be x); xw: n + 1 doubles of scratch.
-static int trsv_f64(int n, const double *A, long lda, const double *rhs, double *x, bool upper,
-                    double *xw, unsigned *status, cudaStream_t s) {
-  const int nblk = ceil_div(n, kFB);
-  const size_t smem = sizeof(double) * kFB * kFB;
+int perm_gather_f64(int n, int nrhs, const int *ipiv, bool forward, const double *B, long ldb,
+                    double *Y, long ldy, cudaStream_t s) {
+  if (n <= 0 || nrhs <= 0) return 0;
+  ZG_LAUNCH(kTagLaswp, 0, 16.0 * n * nrhs, s,
+            perm_gather_kernel<<<ceil_div(n, 128), 128, 0, s>>>(n, nrhs, ipiv, forward, B, ldb,
+                                                                Y, ldy));
+  return 0;
+}
+
+template <bool TRANS>
+static int trsv_f64_launch(int n, const double *A, long lda, const double *rhs, double *x,
+                           bool upper, bool unit, double *xpub, unsigned *ticket,
+                           unsigned *status, cudaStream_t s) {
+  const size_t smem = sizeof(double) * kFB * kFLD;
   static bool attr = false;
   if (!attr) {
-    ZG_CUDA(cudaFuncSetAttribute(trsv_f64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
+    ZG_CUDA(cudaFuncSetAttribute(trsv_f64_kernel<TRANS>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
+  ZG_LAUNCH(kTagTrsmDiag, 1.0 * n * n, 4.0 * n * n + 16.0 * n, s,
+            trsv_f64_kernel<TRANS><<<ceil_div(n, kFB), kFT, smem, s>>>(
+                n, A, lda, rhs, x, xpub, ticket, upper, unit, status));
+  return 0;
+}
+
+int trsv_f64(int n, const double *A, long lda, bool trans, bool upper, bool unit,
+             const double *rhs, double *x, double *xw, cudaStream_t s) {
+  if (n <= 0) return 0;
+  Control *ctl;
+  ZG_TRY(control(s, &ctl));
   unsigned *ticket = reinterpret_cast<unsigned *>(xw);
   double *xpub = xw + 1;
   ZG_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned), s));
   ZG_CUDA(cudaMemsetAsync(xpub, 0xff, sizeof(double) * n, s));
-  ZG_LAUNCH(kTagTrsmDiag, 1.0 * n * n, 4.0 * n * n + 16.0 * n, s,
-            trsv_f64_kernel<<<nblk, kFT, smem, s>>>(n, A, lda, rhs, x, xpub, ticket, upper,
-                                                    status));
-  return 0;
+  if (trans) return trsv_f64_launch<true>(n, A, lda, rhs, x, upper, unit, xpub, ticket,
+                                          &ctl->status, s);
+  return trsv_f64_launch<false>(n, A, lda, rhs, x, upper, unit, xpub, ticket, &ctl->status, s);
 }
 
 template <typename T>
@@ -637,20 +721,26 @@ int getrs_dev(int trans, int n, int nrhs, const T *A, long lda, const int *ipiv,
   const bool nt = trans == kNoTrans || trans == kConjNoTrans;
   if constexpr (sizeof(T) == sizeof(double)) {
     // a few right-hand sides: one launch per column and triangle
-    if (nt && nrhs <= 4 && n >= 512) {
-      Control *ctl;
-      ZG_TRY(control(s, &ctl));
+    if (nrhs <= kTrsvMaxRhs && n >= kTrsvMinN) {
       void *w;
       ZG_TRY(workspace(s, kSlotPanel, sizeof(double) * ((size_t)n * (nrhs + 1) + 1), &w));
       double *xw = (double *)w, *Y = xw + n + 1;
       double *Bd = reinterpret_cast<double *>(B);
       const double *Ad = reinterpret_cast<const double *>(A);
-      ZG_LAUNCH(kTagLaswp, 0, 16.0 * n * nrhs, s,
-                perm_gather_kernel<<<ceil_div(n, 128), 128, 0, s>>>(n, nrhs, ipiv, Bd, ldb, Y));
-      for (int c = 0; c < nrhs; ++c) {
-        double *x = Bd + (long)c * ldb;
-        ZG_TRY(trsv_f64(n, Ad, lda, Y + (long)c * n, x, false, xw, &ctl->status, s));
-        ZG_TRY(trsv_f64(n, Ad, lda, x, x, true, xw, &ctl->status, s));
+      if (nt) {  // x = U^-1 L^-1 P b
+        ZG_TRY(perm_gather_f64(n, nrhs, ipiv, true, Bd, ldb, Y, n, s));
+        for (int c = 0; c < nrhs; ++c) {
+          double *x = Bd + (long)c * ldb;
+          ZG_TRY(trsv_f64(n, Ad, lda, false, false, true, Y + (long)c * n, x, xw, s));
+          ZG_TRY(trsv_f64(n, Ad, lda, false, true, false, x, x, xw, s));
+        }
+      } else {  // x = P^T L^-T U^-T b
+        for (int c = 0; c < nrhs; ++c) {
+          double *y = Y + (long)c * n;
+          ZG_TRY(trsv_f64(n, Ad, lda, true, false, false, Bd + (long)c * ldb, y, xw, s));
+          ZG_TRY(trsv_f64(n, Ad, lda, true, true, true, y, y, xw, s));
+        }
+        ZG_TRY(perm_gather_f64(n, nrhs, ipiv, false, Y, n, Bd, ldb, s));
       }
       return 0;
     }
