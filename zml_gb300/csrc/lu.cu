@@ -559,16 +559,21 @@ __global__ void __launch_bounds__(kFT) trsv_f64_kernel(int n, const double *__re
       __syncthreads();
     }
     if constexpr (!TRANS) {
+      // each half tile summed on its own, then added to the running sums: the
+      // depth of a sum grows with the tiles, not with the columns
       const int xo = 64 * (hq & 1) + ph;
+      double p0 = cur[0] * xs[xo], p1 = cur[1] * xs[xo + 4];
 #pragma unroll
-      for (int j = 0; j < kFH; j += 2) {
-        acc[0] = fma(cur[j], xs[xo + 4 * j], acc[0]);
-        acc[1] = fma(cur[j + 1], xs[xo + 4 * (j + 1)], acc[1]);
+      for (int j = 2; j < kFH; j += 2) {
+        p0 = fma(cur[j], xs[xo + 4 * j], p0);
+        p1 = fma(cur[j + 1], xs[xo + 4 * (j + 1)], p1);
       }
+      acc[0] += p0;
+      acc[1] += p1;
     } else {
       const double x0 = xs[64 * (hq & 1) + lane], x1 = xs[64 * (hq & 1) + lane + 32];
 #pragma unroll
-      for (int k = 0; k < 8; ++k) acc[k] = fma(cur[2 * k + 1], x1, fma(cur[2 * k], x0, acc[k]));
+      for (int k = 0; k < 8; ++k) acc[k] += fma(cur[2 * k + 1], x1, cur[2 * k] * x0);
     }
     if (hq & 1) __syncthreads();  // xs free for the next tile
 #pragma unroll
