@@ -1,0 +1,945 @@
+/*
+ * oracle_z_impl.h -- the complex (cfloat) body of the zml oracle (TEST
+ * INFRASTRUCTURE).
+ *
+ * Included once per component type by zml_oracle.c with
+ *   R     = the component type (double / float), ZT = struct {R re, im}
+ *   ZP(x) = the exported name prefix (zo_z_x / zo_c_x)
+ *   ZFMA  = the fused multiply-add of R (fma / fmaf)
+ * The arithmetic restates zml's cfloat operations (cfloat.zig) with their
+ * explicit fused multiply-adds; every BLAS / LAPACK routine restates the
+ * cited generic Zig routine of srmadrid/zml in its loop order and with each
+ * product's operands in the order written there (zml's complex product
+ * rounds its imaginary part asymmetrically).  Complex arrays are
+ * interleaved (re, im) pairs, the layout of numpy's complex128 / complex64.
+ */
+
+/* ---- cfloat arithmetic ---------------------------------------------------- */
+static inline ZT ZP(c)(R re, R im) {
+  ZT z;
+  z.re = re;
+  z.im = im;
+  return z;
+}
+/* cfloat.zig:75-88 / 112-125 */
+static inline ZT ZP(cadd)(ZT x, ZT y) { return ZP(c)(x.re + y.re, x.im + y.im); }
+static inline ZT ZP(csub)(ZT x, ZT y) { return ZP(c)(x.re - y.re, x.im - y.im); }
+/* cfloat.zig:149-174: re = fma(x.re, y.re, -x.im * y.im),
+ * im = fma(x.re, y.im, x.im * y.re). */
+static inline ZT ZP(cmul)(ZT x, ZT y) {
+  return ZP(c)(ZFMA(x.re, y.re, (-x.im) * y.im), ZFMA(x.re, y.im, x.im * y.re));
+}
+/* cfloat.zig:206-290: Smith's division with fused updates, the ratio taken
+ * against the larger component of y (strictly larger real part). */
+static inline ZT ZP(cdiv)(ZT x, ZT y) {
+  if (ZO_ABS(y.im) < ZO_ABS(y.re)) {
+    const R t1 = y.im / y.re;
+    const R t2 = (R)1 / ZFMA(t1, y.im, y.re);
+    return ZP(c)(ZFMA(x.im, t1, x.re) * t2, ZFMA(-x.re, t1, x.im) * t2);
+  }
+  const R t1 = y.re / y.im;
+  const R t2 = (R)1 / ZFMA(t1, y.re, y.im);
+  return ZP(c)(ZFMA(x.re, t1, x.im) * t2, ZFMA(x.im, t1, -x.re) * t2);
+}
+/* cfloat.zig:322-334 */
+static inline ZT ZP(cconj)(ZT x) { return ZP(c)(x.re, -x.im); }
+/* conj when the flag says so (the conj_* transposes) */
+static inline ZT ZP(cj)(ZT x, int conj) { return conj ? ZP(cconj)(x) : x; }
+/* cfloat/abs1.zig:11-17: |re| + |im| */
+static inline R ZP(cabs1)(ZT x) { return ZO_ABS(x.re) + ZO_ABS(x.im); }
+/* cfloat.zig eq: both components equal (a real operand has im = 0) */
+static inline int ZP(ceq)(ZT x, ZT y) { return x.re == y.re && x.im == y.im; }
+static inline int ZP(cis0)(ZT x) { return x.re == (R)0 && x.im == (R)0; }
+static inline int ZP(cis1)(ZT x) { return x.re == (R)1 && x.im == (R)0; }
+static const ZT ZP(zero) = {(R)0, (R)0};
+static const ZT ZP(one) = {(R)1, (R)0};
+static const ZT ZP(mone) = {(R)-1, (R)0};
+
+/* A real x divided by a complex y: x / y, the quotient zml's own test pins
+ * (test/cfloat/div.zig:42-44: div(7, 1 + 2i) = 1.4 - 2.8i), formed as
+ * (x + 0i) / y with the division above.  cfloat.zig:489-492 as written
+ * returns y / x for this operand order; zo_set_cdiv_as_written(1) restates
+ * that instead.  getrf2.zig:66-75 reaches it as div(1, a[0]). */
+static inline ZT ZP(crdiv)(R x, ZT y) {
+  if (zo_cdiv_as_written) return ZP(c)(y.re / x, y.im / x); /* cfloat.zig:292-305 divReal */
+  return ZP(cdiv)(ZP(c)(x, (R)0), y);
+}
+
+#define ZA_(i, j) a[(long)(i) + (long)(j) * lda]
+#define ZB_(i, j) b[(long)(i) + (long)(j) * ldb]
+#define ZC_(i, j) c[(long)(i) + (long)(j) * ldc]
+
+/* ---- BLAS level 1 ------------------------------------------------------------ */
+
+/* blas/iamax.zig:39-53 (complex branch): the first maximum of |re| + |im|
+ * (strict '>'), NaN never replaces the running maximum. */
+int ZP(iamax)(int n, const ZT *x, int incx) {
+  if (n <= 0 || incx <= 0) return ZO_EINVAL;
+  if (n == 1) return 0;
+  int imax = 0;
+  R max = ZP(cabs1)(x[0]);
+  long ix = incx;
+  for (int i = 1; i < n; ++i) {
+    const R absx = ZP(cabs1)(x[ix]);
+    if (absx > max) {
+      max = absx;
+      imax = i;
+    }
+    ix += incx;
+  }
+  return imax;
+}
+
+/* blas/scal.zig:9-41: x *= alpha, early return when alpha == 1. */
+int ZP(scal)(int n, ZT alpha, ZT *x, int incx) {
+  if (n < 0 || incx <= 0) return ZO_EINVAL;
+  if (n == 0) return 0;
+  if (ZP(cis1)(alpha)) return 0;
+  long ix = 0;
+  for (int i = 0; i < n; ++i) {
+    x[ix] = ZP(cmul)(x[ix], alpha);
+    ix += incx;
+  }
+  return 0;
+}
+
+/* ---- BLAS level 3: gemm ---------------------------------------------------- */
+
+/* blas/gemm.zig:68-1027 (k_gemm): the four loop forms of the real routine
+ * (NN and NT axpy forms, TN and TT dot forms), with a or b conjugated for
+ * the conj_no_trans / conj_trans operands (noconja / noconjb, 93-96). */
+static int ZP(k_gemm)(int transa, int transb, int m, int n, int k, ZT alpha, const ZT *a, int lda,
+                      const ZT *b, int ldb, ZT beta, ZT *c, int ldc) {
+  const int nota = transa == ZO_NOTRANS || transa == ZO_CONJNOTRANS;
+  const int notb = transb == ZO_NOTRANS || transb == ZO_CONJNOTRANS;
+  const int cja = !(transa == ZO_NOTRANS || transa == ZO_TRANS);
+  const int cjb = !(transb == ZO_NOTRANS || transb == ZO_TRANS);
+  const int nrowa = nota ? m : k;
+  const int nrowb = notb ? k : n;
+  if (m < 0 || n < 0 || k < 0 || lda < ZO_MAX(1, nrowa) || ldb < ZO_MAX(1, nrowb) ||
+      ldc < ZO_MAX(1, m))
+    return ZO_EINVAL;                                                         /* 101-102 */
+  if (m == 0 || n == 0 || ((ZP(cis0)(alpha) || k == 0) && ZP(cis1)(beta))) return 0; /* 105-108 */
+  if (ZP(cis0)(alpha)) { /* 111-140 */
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < m; ++i) ZC_(i, j) = ZP(cis0)(beta) ? ZP(zero) : ZP(cmul)(ZC_(i, j), beta);
+    return 0;
+  }
+  if (nota) { /* 142-336 (b not transposed), 584-778 (b transposed): axpy forms */
+    /* operand order as written: alpha * b and temp * a in the plain NN branch
+     * (171, 179), b * alpha and a * temp in every other one (218-226, 267-275,
+     * 314-322, 613-621, 660-668, 709-717, 756-764) */
+    const int plain = notb && !cja && !cjb;
+    for (int j = 0; j < n; ++j) {
+      if (ZP(cis0)(beta)) {
+        for (int i = 0; i < m; ++i) ZC_(i, j) = ZP(zero);
+      } else if (!ZP(cis1)(beta)) {
+        for (int i = 0; i < m; ++i) ZC_(i, j) = ZP(cmul)(ZC_(i, j), beta);
+      }
+      for (int l = 0; l < k; ++l) {
+        const ZT bl = ZP(cj)(notb ? ZB_(l, j) : ZB_(j, l), cjb);
+        const ZT temp = plain ? ZP(cmul)(alpha, bl) : ZP(cmul)(bl, alpha);
+        for (int i = 0; i < m; ++i) {
+          const ZT al = ZP(cj)(ZA_(i, l), cja);
+          ZC_(i, j) = ZP(cadd)(ZC_(i, j), plain ? ZP(cmul)(temp, al) : ZP(cmul)(al, temp));
+        }
+      }
+    }
+  } else { /* 337-583 (b not transposed), 779-1020 (b transposed): dot forms */
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < m; ++i) {
+        ZT temp = ZP(zero);
+        for (int l = 0; l < k; ++l) {
+          const ZT bl = notb ? ZB_(l, j) : ZB_(j, l);
+          temp = ZP(cadd)(temp, ZP(cmul)(ZP(cj)(ZA_(l, i), cja), ZP(cj)(bl, cjb)));
+        }
+        if (ZP(cis0)(beta)) {
+          ZC_(i, j) = ZP(cmul)(alpha, temp);
+        } else if (ZP(cis1)(beta)) {
+          ZC_(i, j) = ZP(cadd)(ZC_(i, j), ZP(cmul)(alpha, temp));
+        } else {
+          ZC_(i, j) = ZP(cmul)(ZC_(i, j), beta);
+          ZC_(i, j) = ZP(cadd)(ZC_(i, j), ZP(cmul)(alpha, temp));
+        }
+      }
+  }
+  return 0;
+}
+
+/* blas/gemm.zig:14-66: row-major maps to column-major by swapping the
+ * operands (A<->B, m<->n). */
+int ZP(gemm)(int order, int transa, int transb, int m, int n, int k, ZT alpha, const ZT *a,
+             int lda, const ZT *b, int ldb, ZT beta, ZT *c, int ldc) {
+  if (order == ZO_COL)
+    return ZP(k_gemm)(transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc);
+  return ZP(k_gemm)(transb, transa, n, m, k, alpha, b, ldb, a, lda, beta, c, ldc);
+}
+
+/* ---- BLAS level 3: trsm ---------------------------------------------------- */
+
+/* blas/trsm.zig:66-735 (k_trsm), the real routine's loops with a
+ * conjugated for conj_no_trans / conj_trans.  The left/no-trans divisions
+ * read b[k + j*lda] as written (137, 177, 222, 245) unless as-written mode
+ * is off.  Operand order as written, including alpha * b at 208 and 343
+ * (b * alpha elsewhere). */
+static int ZP(k_trsm)(int side, int uplo, int transa, int diag, int m, int n, ZT alpha,
+                      const ZT *a, int lda, ZT *b, int ldb) {
+  const int notr = transa == ZO_NOTRANS || transa == ZO_CONJNOTRANS;
+  const int cj = !(transa == ZO_NOTRANS || transa == ZO_TRANS);
+  const int nrowa = side == ZO_LEFT ? m : n;
+  const int nonunit = diag == ZO_NONUNIT;
+  const long ldq = zo_trsm_as_written ? lda : ldb;
+  if (m < 0 || n < 0 || lda < ZO_MAX(1, nrowa) || ldb < ZO_MAX(1, m)) return ZO_EINVAL; /* 91 */
+  if (m == 0 || n == 0) return 0;
+  if (ZP(cis0)(alpha)) { /* 99-113 */
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < m; ++i) ZB_(i, j) = ZP(zero);
+    return 0;
+  }
+  if (side == ZO_LEFT) {
+    if (notr) {
+      if (uplo == ZO_UPPER) { /* 117-201: back substitution */
+        for (int j = 0; j < n; ++j) {
+          if (!ZP(cis1)(alpha))
+            for (int i = 0; i < m; ++i) ZB_(i, j) = ZP(cmul)(ZB_(i, j), alpha);
+          for (int k = m - 1; k >= 0; --k) {
+            if (!ZP(cis0)(ZB_(k, j))) {
+              if (nonunit)
+                ZB_(k, j) = ZP(cdiv)(b[(long)k + (long)j * ldq], ZP(cj)(ZA_(k, k), cj));
+              for (int i = 0; i < k; ++i)
+                ZB_(i, j) = ZP(csub)(ZB_(i, j), ZP(cmul)(ZB_(k, j), ZP(cj)(ZA_(i, k), cj)));
+            }
+          }
+        }
+      } else { /* 202-270: forward substitution */
+        for (int j = 0; j < n; ++j) {
+          if (!ZP(cis1)(alpha))
+            for (int i = 0; i < m; ++i) ZB_(i, j) = ZP(cmul)(alpha, ZB_(i, j));
+          for (int k = 0; k < m; ++k) {
+            if (!ZP(cis0)(ZB_(k, j))) {
+              if (nonunit)
+                ZB_(k, j) = ZP(cdiv)(b[(long)k + (long)j * ldq], ZP(cj)(ZA_(k, k), cj));
+              for (int i = k + 1; i < m; ++i)
+                ZB_(i, j) = ZP(csub)(ZB_(i, j), ZP(cmul)(ZB_(k, j), ZP(cj)(ZA_(i, k), cj)));
+            }
+          }
+        }
+      }
+    } else {
+      if (uplo == ZO_UPPER) { /* 272-337: dot form, op(A) lower */
+        for (int j = 0; j < n; ++j)
+          for (int i = 0; i < m; ++i) {
+            ZT temp = ZP(cmul)(ZB_(i, j), alpha);
+            for (int k = 0; k < i; ++k)
+              temp = ZP(csub)(temp, ZP(cmul)(ZP(cj)(ZA_(k, i), cj), ZB_(k, j)));
+            if (nonunit) temp = ZP(cdiv)(temp, ZP(cj)(ZA_(i, i), cj));
+            ZB_(i, j) = temp;
+          }
+      } else { /* 338-404 */
+        for (int j = 0; j < n; ++j)
+          for (int i = m - 1; i >= 0; --i) {
+            ZT temp = ZP(cmul)(alpha, ZB_(i, j));
+            for (int k = i + 1; k < m; ++k)
+              temp = ZP(csub)(temp, ZP(cmul)(ZP(cj)(ZA_(k, i), cj), ZB_(k, j)));
+            if (nonunit) temp = ZP(cdiv)(temp, ZP(cj)(ZA_(i, i), cj));
+            ZB_(i, j) = temp;
+          }
+      }
+    }
+  } else {
+    if (notr) {
+      if (uplo == ZO_UPPER) { /* 408-487 */
+        for (int j = 0; j < n; ++j) {
+          if (!ZP(cis1)(alpha))
+            for (int i = 0; i < m; ++i) ZB_(i, j) = ZP(cmul)(ZB_(i, j), alpha);
+          for (int k = 0; k < j; ++k)
+            if (!ZP(cis0)(ZA_(k, j)))
+              for (int i = 0; i < m; ++i)
+                ZB_(i, j) = ZP(csub)(ZB_(i, j), ZP(cmul)(ZP(cj)(ZA_(k, j), cj), ZB_(i, k)));
+          if (nonunit) {
+            const ZT temp = ZP(cdiv)(ZP(one), ZP(cj)(ZA_(j, j), cj));
+            for (int i = 0; i < m; ++i) ZB_(i, j) = ZP(cmul)(ZB_(i, j), temp);
+          }
+        }
+      } else { /* 488-568 */
+        for (int j = n - 1; j >= 0; --j) {
+          if (!ZP(cis1)(alpha))
+            for (int i = 0; i < m; ++i) ZB_(i, j) = ZP(cmul)(ZB_(i, j), alpha);
+          for (int k = j + 1; k < n; ++k)
+            if (!ZP(cis0)(ZA_(k, j)))
+              for (int i = 0; i < m; ++i)
+                ZB_(i, j) = ZP(csub)(ZB_(i, j), ZP(cmul)(ZP(cj)(ZA_(k, j), cj), ZB_(i, k)));
+          if (nonunit) {
+            const ZT temp = ZP(cdiv)(ZP(one), ZP(cj)(ZA_(j, j), cj));
+            for (int i = 0; i < m; ++i) ZB_(i, j) = ZP(cmul)(ZB_(i, j), temp);
+          }
+        }
+      }
+    } else {
+      if (uplo == ZO_UPPER) { /* 570-647 */
+        for (int k = n - 1; k >= 0; --k) {
+          if (nonunit) {
+            const ZT temp = ZP(cdiv)(ZP(one), ZP(cj)(ZA_(k, k), cj));
+            for (int i = 0; i < m; ++i) ZB_(i, k) = ZP(cmul)(ZB_(i, k), temp);
+          }
+          for (int j = 0; j < k; ++j)
+            if (!ZP(cis0)(ZA_(j, k))) {
+              const ZT temp = ZP(cj)(ZA_(j, k), cj);
+              for (int i = 0; i < m; ++i)
+                ZB_(i, j) = ZP(csub)(ZB_(i, j), ZP(cmul)(temp, ZB_(i, k)));
+            }
+          if (!ZP(cis1)(alpha))
+            for (int i = 0; i < m; ++i) ZB_(i, k) = ZP(cmul)(ZB_(i, k), alpha);
+        }
+      } else { /* 648-727 */
+        for (int k = 0; k < n; ++k) {
+          if (nonunit) {
+            const ZT temp = ZP(cdiv)(ZP(one), ZP(cj)(ZA_(k, k), cj));
+            for (int i = 0; i < m; ++i) ZB_(i, k) = ZP(cmul)(ZB_(i, k), temp);
+          }
+          for (int j = k + 1; j < n; ++j)
+            if (!ZP(cis0)(ZA_(j, k))) {
+              const ZT temp = ZP(cj)(ZA_(j, k), cj);
+              for (int i = 0; i < m; ++i)
+                ZB_(i, j) = ZP(csub)(ZB_(i, j), ZP(cmul)(temp, ZB_(i, k)));
+            }
+          if (!ZP(cis1)(alpha))
+            for (int i = 0; i < m; ++i) ZB_(i, k) = ZP(cmul)(ZB_(i, k), alpha);
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+/* blas/trsm.zig:18-64: row-major -> side.invert(), uplo.invert(), m<->n. */
+int ZP(trsm)(int order, int side, int uplo, int transa, int diag, int m, int n, ZT alpha,
+             const ZT *a, int lda, ZT *b, int ldb) {
+  if (order == ZO_COL) return ZP(k_trsm)(side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb);
+  return ZP(k_trsm)(side == ZO_LEFT ? ZO_RIGHT : ZO_LEFT, uplo == ZO_UPPER ? ZO_LOWER : ZO_UPPER,
+                    transa, diag, n, m, alpha, a, lda, b, ldb);
+}
+
+/* ---- BLAS level 3: syrk (complex symmetric) and herk ------------------------ */
+
+/* blas/syrk.zig:60-366 (k_syrk): C = alpha A A^T + beta C without any
+ * conjugation; rejects the conjugate transposes (82-84). */
+static int ZP(k_syrk)(int uplo, int trans, int n, int k, ZT alpha, const ZT *a, int lda, ZT beta,
+                      ZT *c, int ldc) {
+  const int nrowa = trans == ZO_NOTRANS ? n : k;
+  if (trans == ZO_CONJNOTRANS || trans == ZO_CONJTRANS || n < 0 || k < 0 ||
+      lda < ZO_MAX(1, nrowa) || ldc < ZO_MAX(1, n))
+    return ZO_EINVAL;
+  if (n == 0 || ((ZP(cis0)(alpha) || k == 0) && ZP(cis1)(beta))) return 0; /* 87-90 */
+  if (ZP(cis0)(alpha)) {                                                 /* 93-151 */
+    for (int j = 0; j < n; ++j) {
+      const int i0 = uplo == ZO_UPPER ? 0 : j, i1 = uplo == ZO_UPPER ? j + 1 : n;
+      for (int i = i0; i < i1; ++i)
+        ZC_(i, j) = ZP(cis0)(beta) ? ZP(zero) : ZP(cmul)(ZC_(i, j), beta);
+    }
+    return 0;
+  }
+  if (trans == ZO_NOTRANS) { /* 153-252 */
+    for (int j = 0; j < n; ++j) {
+      const int i0 = uplo == ZO_UPPER ? 0 : j, i1 = uplo == ZO_UPPER ? j + 1 : n;
+      if (ZP(cis0)(beta)) {
+        for (int i = i0; i < i1; ++i) ZC_(i, j) = ZP(zero);
+      } else if (!ZP(cis1)(beta)) {
+        for (int i = i0; i < i1; ++i) ZC_(i, j) = ZP(cmul)(ZC_(i, j), beta);
+      }
+      for (int l = 0; l < k; ++l) {
+        if (!ZP(cis0)(ZA_(j, l))) {
+          const ZT temp = ZP(cmul)(alpha, ZA_(j, l));
+          for (int i = i0; i < i1; ++i)
+            ZC_(i, j) = ZP(cadd)(ZC_(i, j), ZP(cmul)(temp, ZA_(i, l)));
+        }
+      }
+    }
+  } else { /* 253-359 */
+    for (int j = 0; j < n; ++j) {
+      const int i0 = uplo == ZO_UPPER ? 0 : j, i1 = uplo == ZO_UPPER ? j + 1 : n;
+      for (int i = i0; i < i1; ++i) {
+        ZT temp = ZP(zero);
+        for (int l = 0; l < k; ++l) temp = ZP(cadd)(temp, ZP(cmul)(ZA_(l, i), ZA_(l, j)));
+        if (ZP(cis0)(beta)) {
+          ZC_(i, j) = ZP(cmul)(alpha, temp);
+        } else {
+          ZC_(i, j) = ZP(cmul)(ZC_(i, j), beta);
+          ZC_(i, j) = ZP(cadd)(ZC_(i, j), ZP(cmul)(alpha, temp));
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+/* blas/syrk.zig:15-58: row-major -> uplo.invert(), trans.invert(). */
+int ZP(syrk)(int order, int uplo, int trans, int n, int k, ZT alpha, const ZT *a, int lda,
+             ZT beta, ZT *c, int ldc) {
+  if (order == ZO_COL) return ZP(k_syrk)(uplo, trans, n, k, alpha, a, lda, beta, c, ldc);
+  return ZP(k_syrk)(uplo == ZO_UPPER ? ZO_LOWER : ZO_UPPER, zo_trans_invert(trans), n, k, alpha,
+                    a, lda, beta, c, ldc);
+}
+
+/* A complex value scaled by a real one, component by component
+ * (cfloat.zig:176-189 mulReal, reached by mul with one real operand). */
+static inline ZT ZP(cscale)(ZT x, R s) { return ZP(c)(x.re * s, x.im * s); }
+
+/* blas/herk.zig:60-504 (k_herk): C = alpha A A^H + beta C (no_trans) or
+ * alpha A^H A + beta C (conj_trans) with real alpha and beta; the diagonal
+ * keeps only its real part.  Rejects trans and conj_no_trans (83-85). */
+static int ZP(k_herk)(int uplo, int trans, int n, int k, R alpha, const ZT *a, int lda, R beta,
+                      ZT *c, int ldc) {
+  const int nrowa = trans == ZO_NOTRANS ? n : k;
+  if (trans == ZO_CONJNOTRANS || trans == ZO_TRANS || n < 0 || k < 0 ||
+      lda < ZO_MAX(1, nrowa) || ldc < ZO_MAX(1, n))
+    return ZO_EINVAL;
+  if (n == 0 || ((alpha == (R)0 || k == 0) && beta == (R)1)) return 0; /* 88-91 */
+  const int up = uplo == ZO_UPPER;
+  if (alpha == (R)0) { /* 94-166 */
+    for (int j = 0; j < n; ++j) {
+      const int i0 = up ? 0 : j + 1, i1 = up ? j : n;
+      if (beta == (R)0) {
+        for (int i = up ? 0 : j; i < (up ? j + 1 : n); ++i) ZC_(i, j) = ZP(zero);
+      } else {
+        if (!up) ZC_(j, j) = ZP(c)(beta * ZC_(j, j).re, (R)0);
+        for (int i = i0; i < i1; ++i) ZC_(i, j) = ZP(cscale)(ZC_(i, j), beta);
+        if (up) ZC_(j, j) = ZP(c)(beta * ZC_(j, j).re, (R)0);
+      }
+    }
+    return 0;
+  }
+  if (trans == ZO_NOTRANS) { /* 168-315 */
+    for (int j = 0; j < n; ++j) {
+      const int i0 = up ? 0 : j + 1, i1 = up ? j : n; /* the off-diagonal rows of column j */
+      if (beta == (R)0) {
+        for (int i = up ? 0 : j; i < (up ? j + 1 : n); ++i) ZC_(i, j) = ZP(zero);
+      } else if (beta != (R)1) {
+        if (!up) ZC_(j, j) = ZP(c)(beta * ZC_(j, j).re, (R)0);
+        for (int i = i0; i < i1; ++i) ZC_(i, j) = ZP(cscale)(ZC_(i, j), beta);
+        if (up) ZC_(j, j) = ZP(c)(beta * ZC_(j, j).re, (R)0);
+      } else {
+        ZC_(j, j) = ZP(c)(ZC_(j, j).re, (R)0);
+      }
+      for (int l = 0; l < k; ++l) {
+        if (!ZP(cis0)(ZA_(j, l))) {
+          const ZT temp = ZP(cscale)(ZP(cconj)(ZA_(j, l)), alpha);
+          if (up) {
+            for (int i = i0; i < i1; ++i)
+              ZC_(i, j) = ZP(cadd)(ZC_(i, j), ZP(cmul)(temp, ZA_(i, l)));
+            ZC_(j, j) = ZP(c)(ZC_(j, j).re + ZP(cmul)(temp, ZA_(j, l)).re, (R)0);
+          } else {
+            ZC_(j, j) = ZP(c)(ZC_(j, j).re + ZP(cmul)(temp, ZA_(j, l)).re, (R)0);
+            for (int i = i0; i < i1; ++i)
+              ZC_(i, j) = ZP(cadd)(ZC_(i, j), ZP(cmul)(temp, ZA_(i, l)));
+          }
+        }
+      }
+    }
+  } else { /* 316-500 */
+    for (int j = 0; j < n; ++j) {
+      const int i0 = up ? 0 : j + 1, i1 = up ? j : n;
+      for (int pass = 0; pass < 2; ++pass) {
+        /* upper: the off-diagonal entries, then the diagonal; lower: the reverse */
+        const int diag = up ? pass == 1 : pass == 0;
+        if (diag) {
+          R rtemp = 0;
+          for (int l = 0; l < k; ++l)
+            rtemp = rtemp + ZP(cmul)(ZP(cconj)(ZA_(l, j)), ZA_(l, j)).re;
+          if (beta == (R)0) {
+            ZC_(j, j) = ZP(c)(alpha * rtemp, (R)0);
+          } else {
+            ZC_(j, j) = ZP(c)(beta * ZC_(j, j).re, (R)0);
+            ZC_(j, j) = ZP(c)(ZC_(j, j).re + alpha * rtemp, ZC_(j, j).im);
+          }
+        } else {
+          for (int i = i0; i < i1; ++i) {
+            ZT temp = ZP(zero);
+            for (int l = 0; l < k; ++l)
+              temp = ZP(cadd)(temp, ZP(cmul)(ZP(cconj)(ZA_(l, i)), ZA_(l, j)));
+            if (beta == (R)0) {
+              ZC_(i, j) = ZP(cscale)(temp, alpha);
+            } else {
+              ZC_(i, j) = ZP(cscale)(ZC_(i, j), beta);
+              ZC_(i, j) = ZP(cadd)(ZC_(i, j), ZP(cscale)(temp, alpha));
+            }
+          }
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+/* blas/herk.zig:14-58: row-major -> uplo.invert(), trans.reverse()
+ * (no_trans <-> conj_trans, linalg.zig:121-128). */
+int ZP(herk)(int order, int uplo, int trans, int n, int k, R alpha, const ZT *a, int lda, R beta,
+             ZT *c, int ldc) {
+  if (order == ZO_COL) return ZP(k_herk)(uplo, trans, n, k, alpha, a, lda, beta, c, ldc);
+  const int rt = trans == ZO_NOTRANS ? ZO_CONJTRANS
+               : trans == ZO_TRANS ? ZO_CONJNOTRANS
+               : trans == ZO_CONJNOTRANS ? ZO_TRANS : ZO_NOTRANS;
+  return ZP(k_herk)(uplo == ZO_UPPER ? ZO_LOWER : ZO_UPPER, rt, n, k, alpha, a, lda, beta, c, ldc);
+}
+
+/* ---- BLAS level 3: trmm ---------------------------------------------------- */
+
+/* blas/trmm.zig:65-724 (k_trmm), the real routine's loops with a
+ * conjugated for conj_no_trans / conj_trans; operand order as written. */
+static int ZP(k_trmm)(int side, int uplo, int transa, int diag, int m, int n, ZT alpha,
+                      const ZT *a, int lda, ZT *b, int ldb) {
+  const int notr = transa == ZO_NOTRANS || transa == ZO_CONJNOTRANS;
+  const int cj = !(transa == ZO_NOTRANS || transa == ZO_TRANS);
+  const int nonunit = diag == ZO_NONUNIT;
+  const int nrowa = side == ZO_LEFT ? m : n;
+  if (m < 0 || n < 0 || lda < ZO_MAX(1, nrowa) || ldb < ZO_MAX(1, m)) return ZO_EINVAL;
+  if (m == 0 || n == 0) return 0;
+  if (ZP(cis0)(alpha)) {
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < m; ++i) ZB_(i, j) = ZP(zero);
+    return 0;
+  }
+  if (side == ZO_LEFT) {
+    if (notr) {
+      if (uplo == ZO_UPPER) { /* 118-190 */
+        for (int j = 0; j < n; ++j)
+          for (int k = 0; k < m; ++k)
+            if (!ZP(cis0)(ZB_(k, j))) {
+              const ZT temp1 = ZP(cmul)(alpha, ZB_(k, j));
+              for (int i = 0; i < k; ++i)
+                ZB_(i, j) = ZP(cadd)(ZB_(i, j), ZP(cmul)(temp1, ZP(cj)(ZA_(i, k), cj)));
+              ZB_(k, j) = nonunit ? ZP(cmul)(temp1, ZP(cj)(ZA_(k, k), cj)) : temp1;
+            }
+      } else { /* 191-259 */
+        for (int j = 0; j < n; ++j)
+          for (int k = m - 1; k >= 0; --k)
+            if (!ZP(cis0)(ZB_(k, j))) {
+              const ZT temp1 = ZP(cmul)(alpha, ZB_(k, j));
+              ZB_(k, j) = temp1;
+              if (nonunit) ZB_(k, j) = ZP(cmul)(ZB_(k, j), ZP(cj)(ZA_(k, k), cj));
+              for (int i = k + 1; i < m; ++i)
+                ZB_(i, j) = ZP(cadd)(ZB_(i, j), ZP(cmul)(temp1, ZP(cj)(ZA_(i, k), cj)));
+            }
+      }
+    } else {
+      if (uplo == ZO_UPPER) { /* 261-323 */
+        for (int j = 0; j < n; ++j)
+          for (int i = m - 1; i >= 0; --i) {
+            ZT temp = ZB_(i, j);
+            if (nonunit) temp = ZP(cmul)(temp, ZP(cj)(ZA_(i, i), cj));
+            for (int k = 0; k < i; ++k)
+              temp = ZP(cadd)(temp, ZP(cmul)(ZP(cj)(ZA_(k, i), cj), ZB_(k, j)));
+            ZB_(i, j) = ZP(cmul)(alpha, temp);
+          }
+      } else { /* 324-386 */
+        for (int j = 0; j < n; ++j)
+          for (int i = 0; i < m; ++i) {
+            ZT temp = ZB_(i, j);
+            if (nonunit) temp = ZP(cmul)(temp, ZP(cj)(ZA_(i, i), cj));
+            for (int k = i + 1; k < m; ++k)
+              temp = ZP(cadd)(temp, ZP(cmul)(ZP(cj)(ZA_(k, i), cj), ZB_(k, j)));
+            ZB_(i, j) = ZP(cmul)(alpha, temp);
+          }
+      }
+    }
+  } else {
+    if (notr) {
+      if (uplo == ZO_UPPER) { /* 391-479 */
+        for (int j = n - 1; j >= 0; --j) {
+          ZT temp = alpha;
+          if (nonunit) temp = ZP(cmul)(temp, ZP(cj)(ZA_(j, j), cj));
+          for (int i = 0; i < m; ++i) ZB_(i, j) = ZP(cmul)(ZB_(i, j), temp);
+          for (int k = 0; k < j; ++k)
+            if (!ZP(cis0)(ZA_(k, j))) {
+              temp = ZP(cmul)(alpha, ZP(cj)(ZA_(k, j), cj));
+              for (int i = 0; i < m; ++i)
+                ZB_(i, j) = ZP(cadd)(ZB_(i, j), ZP(cmul)(temp, ZB_(i, k)));
+            }
+        }
+      } else { /* 480-568 */
+        for (int j = 0; j < n; ++j) {
+          ZT temp = alpha;
+          if (nonunit) temp = ZP(cmul)(temp, ZP(cj)(ZA_(j, j), cj));
+          for (int i = 0; i < m; ++i) ZB_(i, j) = ZP(cmul)(ZB_(i, j), temp);
+          for (int k = j + 1; k < n; ++k)
+            if (!ZP(cis0)(ZA_(k, j))) {
+              temp = ZP(cmul)(alpha, ZP(cj)(ZA_(k, j), cj));
+              for (int i = 0; i < m; ++i)
+                ZB_(i, j) = ZP(cadd)(ZB_(i, j), ZP(cmul)(temp, ZB_(i, k)));
+            }
+        }
+      }
+    } else {
+      if (uplo == ZO_UPPER) { /* 571-642 */
+        for (int k = 0; k < n; ++k) {
+          for (int j = 0; j < k; ++j)
+            if (!ZP(cis0)(ZA_(j, k))) {
+              ZT temp = alpha;
+              temp = ZP(cmul)(temp, ZP(cj)(ZA_(j, k), cj));
+              for (int i = 0; i < m; ++i)
+                ZB_(i, j) = ZP(cadd)(ZB_(i, j), ZP(cmul)(temp, ZB_(i, k)));
+            }
+          ZT temp = alpha;
+          if (nonunit) temp = ZP(cmul)(temp, ZP(cj)(ZA_(k, k), cj));
+          if (!ZP(cis1)(temp))
+            for (int i = 0; i < m; ++i) ZB_(i, k) = ZP(cmul)(ZB_(i, k), temp);
+        }
+      } else { /* 643-716 */
+        for (int k = n - 1; k >= 0; --k) {
+          for (int j = k + 1; j < n; ++j)
+            if (!ZP(cis0)(ZA_(j, k))) {
+              ZT temp = alpha;
+              temp = ZP(cmul)(temp, ZP(cj)(ZA_(j, k), cj));
+              for (int i = 0; i < m; ++i)
+                ZB_(i, j) = ZP(cadd)(ZB_(i, j), ZP(cmul)(temp, ZB_(i, k)));
+            }
+          ZT temp = alpha;
+          if (nonunit) temp = ZP(cmul)(temp, ZP(cj)(ZA_(k, k), cj));
+          if (!ZP(cis1)(temp))
+            for (int i = 0; i < m; ++i) ZB_(i, k) = ZP(cmul)(ZB_(i, k), temp);
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+/* blas/trmm.zig:14-63: row-major -> side.invert(), uplo.invert(), m<->n. */
+int ZP(trmm)(int order, int side, int uplo, int transa, int diag, int m, int n, ZT alpha,
+             const ZT *a, int lda, ZT *b, int ldb) {
+  if (order == ZO_COL) return ZP(k_trmm)(side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb);
+  return ZP(k_trmm)(side == ZO_LEFT ? ZO_RIGHT : ZO_LEFT, uplo == ZO_UPPER ? ZO_LOWER : ZO_UPPER,
+                    transa, diag, n, m, alpha, a, lda, b, ldb);
+}
+
+/* ---- BLAS level 2: gemv, geru, gerc --------------------------------------- */
+
+/* blas/gemv.zig:62-365 (k_gemv); conj_no_trans forms y = alpha conj(A) x +
+ * beta y, conj_trans y = alpha A^H x + beta y (noconj, 93). */
+static int ZP(k_gemv)(int transa, int m, int n, ZT alpha, const ZT *a, int lda, const ZT *x,
+                      int incx, ZT beta, ZT *y, int incy) {
+  if (m < 0 || n < 0 || lda < ZO_MAX(1, m) || incx == 0 || incy == 0) return ZO_EINVAL;
+  if (m == 0 || n == 0 || (ZP(cis0)(alpha) && ZP(cis1)(beta))) return 0;
+  const int notr = transa == ZO_NOTRANS || transa == ZO_CONJNOTRANS;
+  const int cj = !(transa == ZO_NOTRANS || transa == ZO_TRANS);
+  const int lenx = notr ? n : m, leny = notr ? m : n;
+  const long kx = incx < 0 ? (long)(-lenx + 1) * incx : 0;
+  const long ky = incy < 0 ? (long)(-leny + 1) * incy : 0;
+  if (!ZP(cis1)(beta)) { /* 111-157 */
+    long iy = ky;
+    for (int i = 0; i < leny; ++i) {
+      y[iy] = ZP(cis0)(beta) ? ZP(zero) : ZP(cmul)(y[iy], beta);
+      iy += incy;
+    }
+  }
+  if (ZP(cis0)(alpha)) return 0;
+  if (notr) { /* 161-252 */
+    long jx = kx;
+    for (int j = 0; j < n; ++j) {
+      const ZT temp = ZP(cmul)(alpha, x[jx]);
+      long iy = ky;
+      for (int i = 0; i < m; ++i) {
+        y[iy] = ZP(cadd)(y[iy], ZP(cmul)(temp, ZP(cj)(ZA_(i, j), cj)));
+        iy += incy;
+      }
+      jx += incx;
+    }
+  } else { /* 253-358 */
+    long jy = ky;
+    for (int j = 0; j < n; ++j) {
+      ZT temp = ZP(zero);
+      long ix = kx;
+      for (int i = 0; i < m; ++i) {
+        temp = ZP(cadd)(temp, ZP(cmul)(ZP(cj)(ZA_(i, j), cj), x[ix]));
+        ix += incx;
+      }
+      y[jy] = ZP(cadd)(y[jy], ZP(cmul)(alpha, temp));
+      jy += incy;
+    }
+  }
+  return 0;
+}
+
+/* blas/gemv.zig:14-60: row-major -> transa.invert(), m<->n. */
+int ZP(gemv)(int order, int transa, int m, int n, ZT alpha, const ZT *a, int lda, const ZT *x,
+             int incx, ZT beta, ZT *y, int incy) {
+  if (order == ZO_COL) return ZP(k_gemv)(transa, m, n, alpha, a, lda, x, incx, beta, y, incy);
+  return ZP(k_gemv)(zo_trans_invert(transa), n, m, alpha, a, lda, x, incx, beta, y, incy);
+}
+
+/* blas/geru.zig:33-120 and gerc.zig:33-186: A += alpha x y^T (geru) or
+ * alpha x y^H (gerc); column j skipped when y[j] == 0.  cy conjugates y
+ * (gerc column-major), cx conjugates x (gerc row-major: the operands swap,
+ * gerc.zig:26-30, and the conjugation moves onto the new x). */
+static int ZP(k_ger)(int m, int n, ZT alpha, const ZT *x, int incx, const ZT *y, int incy, ZT *a,
+                     int lda, int cx, int cy) {
+  if (m < 0 || n < 0 || lda < ZO_MAX(1, m) || incx == 0 || incy == 0) return ZO_EINVAL;
+  if (m == 0 || n == 0 || ZP(cis0)(alpha)) return 0;
+  long jy = incy < 0 ? (long)(-n + 1) * incy : 0;
+  const long kx = incx < 0 ? (long)(-m + 1) * incx : 0;
+  for (int j = 0; j < n; ++j) {
+    if (!ZP(cis0)(y[jy])) {
+      const ZT temp = ZP(cmul)(alpha, ZP(cj)(y[jy], cy));
+      long ix = kx;
+      for (int i = 0; i < m; ++i) {
+        ZA_(i, j) = ZP(cadd)(ZA_(i, j), ZP(cmul)(ZP(cj)(x[ix], cx), temp));
+        ix += incx;
+      }
+    }
+    jy += incy;
+  }
+  return 0;
+}
+int ZP(geru)(int order, int m, int n, ZT alpha, const ZT *x, int incx, const ZT *y, int incy,
+             ZT *a, int lda) {
+  if (order == ZO_COL) return ZP(k_ger)(m, n, alpha, x, incx, y, incy, a, lda, 0, 0);
+  return ZP(k_ger)(n, m, alpha, y, incy, x, incx, a, lda, 0, 0);
+}
+int ZP(gerc)(int order, int m, int n, ZT alpha, const ZT *x, int incx, const ZT *y, int incy,
+             ZT *a, int lda) {
+  if (order == ZO_COL) return ZP(k_ger)(m, n, alpha, x, incx, y, incy, a, lda, 0, 1);
+  return ZP(k_ger)(n, m, alpha, y, incy, x, incx, a, lda, 1, 0);
+}
+
+/* ---- LAPACK: LU ------------------------------------------------------------ */
+
+/* lapack/laswp.zig:12-96 (element-type generic): interchanges in blocks of
+ * 32 columns, then the remainder; negative incx walks the pivots backwards. */
+int ZP(laswp)(int order, int n, ZT *a, int lda, int k1, int k2, const int *ipiv, int incx) {
+  if (n < 0 || (order == ZO_ROW && lda < ZO_MAX(1, n)) || incx == 0) return ZO_EINVAL;
+  if (n == 0) return 0;
+  int ix0, I1, I2, inc;
+  if (incx > 0) {
+    ix0 = k1 - 1; I1 = k1 - 1; I2 = k2 - 1; inc = 1;
+  } else {
+    ix0 = k1 - 1 + (k1 - k2) * incx; I1 = k2 - 1; I2 = k1 - 1; inc = -1;
+  }
+  const int n32 = (n >> 5) << 5;
+  for (int j0 = 0; j0 < n; j0 += 32) {
+    const int j1 = j0 < n32 ? j0 + 32 : n;
+    int ix = ix0;
+    for (int i = I1; i != I2 + inc; i += inc) {
+      const int ip = ipiv[ix] - 1;
+      if (ip != i)
+        for (int k = j0; k < j1; ++k) {
+          const ZT temp = a[zo_index(order, i, k, lda)];
+          a[zo_index(order, i, k, lda)] = a[zo_index(order, ip, k, lda)];
+          a[zo_index(order, ip, k, lda)] = temp;
+        }
+      ix += incx;
+    }
+    if (j1 == n) break;
+  }
+  return 0;
+}
+
+/* lapack/getrf2.zig:14-210: recursive LU with partial pivoting; the pivot
+ * is the first maximum of |re| + |im| (iamax), the column is scaled by
+ * 1 / a[0] when |a[0]|_1 >= sfmin (div(1, a[0]), see crdiv), else divided
+ * entry by entry. */
+int ZP(getrf2)(int order, int m, int n, ZT *a, int lda, int *ipiv) {
+  if (m < 0 || n < 0 || lda < ZO_MAX(1, order == ZO_COL ? m : n)) return ZO_EINVAL;
+  int info = 0;
+  if (m == 0 || n == 0) return info;
+  const int cl = order == ZO_COL ? 1 : lda;
+  if (m == 1) { /* 35-40 */
+    ipiv[0] = 1;
+    if (ZP(cis0)(a[0])) info = 1;
+  } else if (n == 1) { /* 41-89 */
+    const R sfmin = ZP(lamch_s)();
+    const int ii = ZP(iamax)(m, a, cl);
+    ipiv[0] = ii + 1;
+    if (!ZP(cis0)(a[zo_index(order, ii, 0, lda)])) {
+      if (ii != 0) {
+        const ZT temp = a[0];
+        a[0] = a[zo_index(order, ii, 0, lda)];
+        a[zo_index(order, ii, 0, lda)] = temp;
+      }
+      if (ZP(cabs1)(a[0]) >= sfmin) {
+        ZP(scal)(m - 1, ZP(crdiv)((R)1, a[0]), a + zo_index(order, 1, 0, lda), cl);
+      } else {
+        for (int i = 0; i < m - 1; ++i)
+          a[zo_index(order, i + 1, 0, lda)] = ZP(cdiv)(a[zo_index(order, i + 1, 0, lda)], a[0]);
+      }
+    } else {
+      info = 1;
+    }
+  } else { /* 90-196 */
+    const int n1 = ZO_MIN(m, n) / 2;
+    const int n2 = n - n1;
+    int iinfo = ZP(getrf2)(order, m, n1, a, lda, ipiv);
+    if (info == 0 && iinfo > 0) info = iinfo;
+    ZP(laswp)(order, n2, a + zo_index(order, 0, n1, lda), lda, 1, n1, ipiv, 1);
+    ZP(trsm)(order, ZO_LEFT, ZO_LOWER, ZO_NOTRANS, ZO_UNIT, n1, n2, ZP(one), a, lda,
+             a + zo_index(order, 0, n1, lda), lda);
+    ZP(gemm)(order, ZO_NOTRANS, ZO_NOTRANS, m - n1, n2, n1, ZP(mone),
+             a + zo_index(order, n1, 0, lda), lda, a + zo_index(order, 0, n1, lda), lda, ZP(one),
+             a + zo_index(order, n1, n1, lda), lda);
+    iinfo = ZP(getrf2)(order, m - n1, n2, a + zo_index(order, n1, n1, lda), lda, ipiv + n1);
+    if (info == 0 && iinfo > 0) info = iinfo + n1;
+    for (int i = n1; i < ZO_MIN(m, n); ++i) ipiv[i] = ipiv[i] + n1;
+    ZP(laswp)(order, n1, a, lda, n1 + 1, ZO_MIN(m, n), ipiv, 1);
+  }
+  return info;
+}
+
+/* lapack/getrf.zig:14-152: right-looking blocked LU, nb = ilaenv = 64. */
+int ZP(getrf)(int order, int m, int n, ZT *a, int lda, int *ipiv) {
+  if (m < 0 || n < 0 || lda < ZO_MAX(1, order == ZO_COL ? m : n)) return ZO_EINVAL;
+  int info = 0;
+  if (m == 0 || n == 0) return info;
+  const int nb = zo_ilaenv(1, "DGETRF", m, n, -1, -1);
+  const int mn = ZO_MIN(m, n);
+  if (nb <= 1 || nb >= mn) return ZP(getrf2)(order, m, n, a, lda, ipiv);
+  for (int j = 0; j < mn; j += nb) {
+    const int jb = ZO_MIN(mn - j, nb);
+    const int iinfo = ZP(getrf2)(order, m - j, jb, a + zo_index(order, j, j, lda), lda, ipiv + j);
+    if (info == 0 && iinfo > 0) info = iinfo + j;
+    for (int i = j; i < ZO_MIN(m, j + jb); ++i) ipiv[i] = ipiv[i] + j;
+    ZP(laswp)(order, j, a, lda, j + 1, j + jb, ipiv, 1);
+    if (j + jb < n) {
+      ZP(laswp)(order, n - j - jb, a + zo_index(order, 0, j + jb, lda), lda, j + 1, j + jb, ipiv,
+                1);
+      ZP(trsm)(order, ZO_LEFT, ZO_LOWER, ZO_NOTRANS, ZO_UNIT, jb, n - j - jb, ZP(one),
+               a + zo_index(order, j, j, lda), lda, a + zo_index(order, j, j + jb, lda), lda);
+      if (j + jb < m)
+        ZP(gemm)(order, ZO_NOTRANS, ZO_NOTRANS, m - j - jb, n - j - jb, jb, ZP(mone),
+                 a + zo_index(order, j + jb, j, lda), lda, a + zo_index(order, j, j + jb, lda),
+                 lda, ZP(one), a + zo_index(order, j + jb, j + jb, lda), lda);
+    }
+  }
+  return info;
+}
+
+/* lapack/getrs.zig:13-142: trans N / conj_no_trans: laswp, L, U; trans T /
+ * conj_trans: U^T (U^H), L^T (L^H), laswp backwards. */
+int ZP(getrs)(int order, int trans, int n, int nrhs, const ZT *a, int lda, const int *ipiv, ZT *b,
+              int ldb) {
+  const int nota = trans == ZO_NOTRANS || trans == ZO_CONJNOTRANS;
+  if (n < 0 || nrhs < 0 || lda < ZO_MAX(1, n) || ldb < ZO_MAX(1, order == ZO_COL ? n : nrhs))
+    return ZO_EINVAL;
+  if (n == 0 || nrhs == 0) return 0;
+  if (nota) {
+    ZP(laswp)(order, nrhs, b, ldb, 1, n, ipiv, 1);
+    ZP(trsm)(order, ZO_LEFT, ZO_LOWER, trans, ZO_UNIT, n, nrhs, ZP(one), a, lda, b, ldb);
+    ZP(trsm)(order, ZO_LEFT, ZO_UPPER, trans, ZO_NONUNIT, n, nrhs, ZP(one), a, lda, b, ldb);
+  } else {
+    ZP(trsm)(order, ZO_LEFT, ZO_UPPER, trans, ZO_NONUNIT, n, nrhs, ZP(one), a, lda, b, ldb);
+    ZP(trsm)(order, ZO_LEFT, ZO_LOWER, trans, ZO_UNIT, n, nrhs, ZP(one), a, lda, b, ldb);
+    ZP(laswp)(order, nrhs, b, ldb, 1, n, ipiv, -1);
+  }
+  return 0;
+}
+
+/* lapack/gesv.zig:13-70 */
+int ZP(gesv)(int order, int n, int nrhs, ZT *a, int lda, int *ipiv, ZT *b, int ldb) {
+  if (n < 0 || nrhs < 0 || lda < ZO_MAX(1, n) || ldb < ZO_MAX(1, order == ZO_COL ? n : nrhs))
+    return ZO_EINVAL;
+  if (n == 0 || nrhs == 0) return 0;
+  const int info = ZP(getrf)(order, n, n, a, lda, ipiv);
+  if (info == 0) ZP(getrs)(order, ZO_NOTRANS, n, nrhs, a, lda, ipiv, b, ldb);
+  return info;
+}
+
+/* ---- LAPACK: Cholesky (Hermitian) ----------------------------------------- */
+
+/* lapack/potrf2.zig:17-217: recursive Cholesky, A = U^H U or L L^H; a
+ * diagonal entry is re(a) (its imaginary part is not read), and a
+ * non-positive or NaN one stops the factorization. */
+int ZP(potrf2)(int order, int uplo, int n, ZT *a, int lda) {
+  if (n < 0 || lda < ZO_MAX(1, n)) return ZO_EINVAL;
+  if (n == 0) return 0;
+  if (n == 1) { /* 37-54 */
+    const R ajj = a[0].re;
+    if (ajj <= (R)0 || ajj != ajj) return 1;
+    a[0] = ZP(c)(ZO_SQRT(ajj), (R)0);
+    return 0;
+  }
+  const int n1 = n / 2, n2 = n - n1;
+  int iinfo = ZP(potrf2)(order, uplo, n1, a, lda);
+  if (iinfo != 0) return iinfo;
+  if (uplo == ZO_UPPER) { /* 72-130 */
+    ZP(trsm)(order, ZO_LEFT, ZO_UPPER, ZO_CONJTRANS, ZO_NONUNIT, n1, n2, ZP(one), a, lda,
+             a + zo_index(order, 0, n1, lda), lda);
+    ZP(herk)(order, uplo, ZO_CONJTRANS, n2, n1, (R)-1, a + zo_index(order, 0, n1, lda), lda,
+             (R)1, a + zo_index(order, n1, n1, lda), lda);
+  } else { /* 133-197 */
+    ZP(trsm)(order, ZO_RIGHT, ZO_LOWER, ZO_CONJTRANS, ZO_NONUNIT, n2, n1, ZP(one), a, lda,
+             a + zo_index(order, n1, 0, lda), lda);
+    ZP(herk)(order, uplo, ZO_NOTRANS, n2, n1, (R)-1, a + zo_index(order, n1, 0, lda), lda, (R)1,
+             a + zo_index(order, n1, n1, lda), lda);
+  }
+  iinfo = ZP(potrf2)(order, uplo, n2, a + zo_index(order, n1, n1, lda), lda);
+  if (iinfo != 0) return iinfo + n1;
+  return 0;
+}
+
+/* lapack/potrf.zig:17-240: blocked left-looking Cholesky, nb = 64, herk for
+ * the diagonal block updates (59-90, 149-180). */
+int ZP(potrf)(int order, int uplo, int n, ZT *a, int lda) {
+  if (n < 0 || lda < ZO_MAX(1, n)) return ZO_EINVAL;
+  if (n == 0) return 0;
+  const int nb = zo_ilaenv(1, "DPOTRF", n, -1, -1, -1);
+  if (nb <= 1 || nb >= n) return ZP(potrf2)(order, uplo, n, a, lda);
+  int info = 0;
+  if (uplo == ZO_UPPER) { /* 52-141 */
+    for (int j = 0; j < n; j += nb) {
+      const int jb = ZO_MIN(nb, n - j);
+      ZP(herk)(order, ZO_UPPER, ZO_CONJTRANS, jb, j, (R)-1, a + zo_index(order, 0, j, lda), lda,
+               (R)1, a + zo_index(order, j, j, lda), lda);
+      info = ZP(potrf2)(order, ZO_UPPER, jb, a + zo_index(order, j, j, lda), lda);
+      if (info != 0) return info + j;
+      if (j + jb < n) {
+        ZP(gemm)(order, ZO_CONJTRANS, ZO_NOTRANS, jb, n - j - jb, j, ZP(mone),
+                 a + zo_index(order, 0, j, lda), lda, a + zo_index(order, 0, j + jb, lda), lda,
+                 ZP(one), a + zo_index(order, j, j + jb, lda), lda);
+        ZP(trsm)(order, ZO_LEFT, ZO_UPPER, ZO_CONJTRANS, ZO_NONUNIT, jb, n - j - jb, ZP(one),
+                 a + zo_index(order, j, j, lda), lda, a + zo_index(order, j, j + jb, lda), lda);
+      }
+    }
+  } else { /* 144-231 */
+    for (int j = 0; j < n; j += nb) {
+      const int jb = ZO_MIN(nb, n - j);
+      ZP(herk)(order, ZO_LOWER, ZO_NOTRANS, jb, j, (R)-1, a + zo_index(order, j, 0, lda), lda,
+               (R)1, a + zo_index(order, j, j, lda), lda);
+      info = ZP(potrf2)(order, ZO_LOWER, jb, a + zo_index(order, j, j, lda), lda);
+      if (info != 0) return info + j;
+      if (j + jb < n) {
+        ZP(gemm)(order, ZO_NOTRANS, ZO_CONJTRANS, n - j - jb, jb, j, ZP(mone),
+                 a + zo_index(order, j + jb, 0, lda), lda, a + zo_index(order, j, 0, lda), lda,
+                 ZP(one), a + zo_index(order, j + jb, j, lda), lda);
+        ZP(trsm)(order, ZO_RIGHT, ZO_LOWER, ZO_CONJTRANS, ZO_NONUNIT, n - j - jb, jb, ZP(one),
+                 a + zo_index(order, j, j, lda), lda, a + zo_index(order, j + jb, j, lda), lda);
+      }
+    }
+  }
+  return info;
+}
+
+/* lapack/potrs.zig:15-117: U^H U x = b or L L^H x = b. */
+int ZP(potrs)(int order, int uplo, int n, int nrhs, const ZT *a, int lda, ZT *b, int ldb) {
+  if (n < 0 || nrhs < 0 || lda < ZO_MAX(1, n) || ldb < ZO_MAX(1, n)) return ZO_EINVAL;
+  if (n == 0 || nrhs == 0) return 0;
+  if (uplo == ZO_UPPER) {
+    ZP(trsm)(order, ZO_LEFT, ZO_UPPER, ZO_CONJTRANS, ZO_NONUNIT, n, nrhs, ZP(one), a, lda, b, ldb);
+    ZP(trsm)(order, ZO_LEFT, ZO_UPPER, ZO_NOTRANS, ZO_NONUNIT, n, nrhs, ZP(one), a, lda, b, ldb);
+  } else {
+    ZP(trsm)(order, ZO_LEFT, ZO_LOWER, ZO_NOTRANS, ZO_NONUNIT, n, nrhs, ZP(one), a, lda, b, ldb);
+    ZP(trsm)(order, ZO_LEFT, ZO_LOWER, ZO_CONJTRANS, ZO_NONUNIT, n, nrhs, ZP(one), a, lda, b, ldb);
+  }
+  return 0;
+}
+
+/* lapack/posv.zig:15-70 */
+int ZP(posv)(int order, int uplo, int n, int nrhs, ZT *a, int lda, ZT *b, int ldb) {
+  if (n < 0 || nrhs < 0 || lda < ZO_MAX(1, n) || ldb < ZO_MAX(1, order == ZO_COL ? n : nrhs))
+    return ZO_EINVAL;
+  if (n == 0 || nrhs == 0) return 0;
+  const int info = ZP(potrf)(order, uplo, n, a, lda);
+  if (info == 0) ZP(potrs)(order, uplo, n, nrhs, a, lda, b, ldb);
+  return info;
+}
+
+#undef ZA_
+#undef ZB_
+#undef ZC_

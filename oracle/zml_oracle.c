@@ -1,6 +1,7 @@
 /*
  * zml_oracle.c -- instantiates the type-generic oracle for binary64 and
- * binary32 (TEST INFRASTRUCTURE; see zml_oracle.h).
+ * binary32, real (oracle_impl.h, oracle_qr_impl.h) and complex
+ * (oracle_z_impl.h) (TEST INFRASTRUCTURE; see zml_oracle.h).
  *
  * Build with -O2 -ffp-contract=off: Zig does not contract a*b+c into an FMA,
  * and gcc does so by default on aarch64.
@@ -103,6 +104,55 @@ int zo_ilaenv(int ispec, const char *name, int n1, int n2, int n3, int n4) {
 #include "oracle_qr_impl.h"
 #undef T
 #undef P
+
+#undef ZO_ABS
+#undef ZO_SQRT
+#undef ZO_EPS
+#undef ZO_TMIN
+#undef ZO_TMAX
+#undef ZO_COPYSIGN
+#undef ZO_EMIN
+#undef ZO_EMAX
+#undef ZO_BITS
+
+/* ---- complex ------------------------------------------------------------- */
+static int zo_cdiv_as_written = 0;
+void zo_set_cdiv_as_written(int on) { zo_cdiv_as_written = on ? 1 : 0; }
+
+/* linalg/utils.zig:4-6 */
+static inline long zo_index(int order, int i, int j, int ld) {
+  return order == ZO_COL ? (long)i + (long)j * ld : (long)i * ld + j;
+}
+
+#define R double
+#define ZT zo_cf64
+#define ZP(x) zo_z_##x
+#define ZFMA fma
+#define ZO_ABS fabs
+#define ZO_SQRT sqrt
+static inline double zo_z_lamch_s(void) { return zo_d_lamch('s'); }
+#include "oracle_z_impl.h"
+#undef R
+#undef ZT
+#undef ZP
+#undef ZFMA
+#undef ZO_ABS
+#undef ZO_SQRT
+
+#define R float
+#define ZT zo_cf32
+#define ZP(x) zo_c_##x
+#define ZFMA fmaf
+#define ZO_ABS fabsf
+#define ZO_SQRT sqrtf
+static inline float zo_c_lamch_s(void) { return zo_s_lamch('s'); }
+#include "oracle_z_impl.h"
+#undef R
+#undef ZT
+#undef ZP
+#undef ZFMA
+#undef ZO_ABS
+#undef ZO_SQRT
 
 /* ---- seeded inputs ------------------------------------------------------ */
 static unsigned long long zo_splitmix(unsigned long long *s) {

@@ -81,6 +81,53 @@ ZO_DECL(double, zo_d_)
 ZO_DECL(float, zo_s_)
 #undef ZO_DECL
 
+/* ---- complex (cfloat) ----------------------------------------------------
+ * Interleaved (re, im) pairs: numpy complex128 / complex64.  The arithmetic
+ * restates zml's cfloat operations (cfloat.zig), whose products and Smith
+ * divisions use explicit fused multiply-adds; herk takes real alpha, beta. */
+typedef struct { double re, im; } zo_cf64;
+typedef struct { float re, im; } zo_cf32;
+
+/* A real x divided by a complex y.  zml's own test pins x / y
+ * (test/cfloat/div.zig:42-44); cfloat.zig:489-492 as written computes y / x.
+ * 0 (default) restates the tested quotient, 1 the code as written.  getrf2
+ * reaches it as div(1, a[0]) (lapack/getrf2.zig:66-75). */
+void zo_set_cdiv_as_written(int on);
+
+#define ZO_ZDECL(Z, R, P)                                                                      \
+  int P##gemm(int order, int transa, int transb, int m, int n, int k, Z alpha, const Z *a,    \
+              int lda, const Z *b, int ldb, Z beta, Z *c, int ldc);                           \
+  int P##trsm(int order, int side, int uplo, int transa, int diag, int m, int n, Z alpha,     \
+              const Z *a, int lda, Z *b, int ldb);                                            \
+  int P##syrk(int order, int uplo, int trans, int n, int k, Z alpha, const Z *a, int lda,     \
+              Z beta, Z *c, int ldc);                                                         \
+  int P##herk(int order, int uplo, int trans, int n, int k, R alpha, const Z *a, int lda,     \
+              R beta, Z *c, int ldc);                                                         \
+  int P##trmm(int order, int side, int uplo, int transa, int diag, int m, int n, Z alpha,     \
+              const Z *a, int lda, Z *b, int ldb);                                            \
+  int P##gemv(int order, int transa, int m, int n, Z alpha, const Z *a, int lda, const Z *x,  \
+              int incx, Z beta, Z *y, int incy);                                              \
+  int P##geru(int order, int m, int n, Z alpha, const Z *x, int incx, const Z *y, int incy,   \
+              Z *a, int lda);                                                                 \
+  int P##gerc(int order, int m, int n, Z alpha, const Z *x, int incx, const Z *y, int incy,   \
+              Z *a, int lda);                                                                 \
+  int P##iamax(int n, const Z *x, int incx);                                                  \
+  int P##scal(int n, Z alpha, Z *x, int incx);                                                \
+  int P##laswp(int order, int n, Z *a, int lda, int k1, int k2, const int *ipiv, int incx);   \
+  int P##getrf2(int order, int m, int n, Z *a, int lda, int *ipiv);                           \
+  int P##getrf(int order, int m, int n, Z *a, int lda, int *ipiv);                            \
+  int P##getrs(int order, int trans, int n, int nrhs, const Z *a, int lda, const int *ipiv,   \
+               Z *b, int ldb);                                                                \
+  int P##gesv(int order, int n, int nrhs, Z *a, int lda, int *ipiv, Z *b, int ldb);           \
+  int P##potrf2(int order, int uplo, int n, Z *a, int lda);                                   \
+  int P##potrf(int order, int uplo, int n, Z *a, int lda);                                    \
+  int P##potrs(int order, int uplo, int n, int nrhs, const Z *a, int lda, Z *b, int ldb);     \
+  int P##posv(int order, int uplo, int n, int nrhs, Z *a, int lda, Z *b, int ldb);
+
+ZO_ZDECL(zo_cf64, double, zo_z_)
+ZO_ZDECL(zo_cf32, float, zo_c_)
+#undef ZO_ZDECL
+
 /* ilaenv restatement (lapack/ilaenv.zig): ispec 1 = NB, 2 = NBMIN, 3 = NX.
  * name is the 6-letter routine name, e.g. "DGETRF". */
 int zo_ilaenv(int ispec, const char *name, int n1, int n2, int n3, int n4);

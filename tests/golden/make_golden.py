@@ -14,8 +14,9 @@ part of each test, a replayable list of steps:
     {"op": "expect_ret", "value": 127}                 # scalar results
 
 The replay harness (tests/golden_replay.py) runs them against the oracle
-and, on a GPU, against the C ABI.  Only the complex (cf64) parts of the
-files are skipped; the fixtures are regenerated with
+and, on a GPU, against the C ABI.  The complex (cf64) parts, and the
+complex-only herk / geru / gerc tests, go to blas_z<name>.json with complex
+values as [re, im] pairs.  The fixtures are regenerated with
 
     python tests/golden/make_golden.py /path/to/zml
 
@@ -118,6 +119,91 @@ def parse_chain(path, fn):
     return {"name": fn, "source": "test/linalg/blas/%s.zig" % fn, "steps": steps}
 
 
+# files with a complex (cf64) chain: the cf64 part of the real files above,
+# and the complex-only routines
+COMPLEX = ["gemm", "trsm", "syrk", "herk", "trmm", "gemv", "geru", "gerc"]
+
+CINIT = re.compile(r"cf64\.init\(\s*([^,()]+?)\s*,\s*([^,()]+?)\s*\)")
+
+
+def parse_chain_complex(path, fn):
+    """The complex part of a test: every statement from the first cf64
+    allocation on (constants are read from the whole test).  Complex values
+    are [re, im] pairs, complex scalar arguments {"c": [re, im]}, and an
+    expectation on a component carries "part": "re" | "im"."""
+    text = open(path).read()
+    body = text[text.index("test " + fn):]
+    stmts = [re.sub(r"//[^\n]*", "", x).strip() for x in re.split(r";\s*\n", body)]
+    consts, cconsts, steps, started = {}, {}, [], False
+    for st in stmts:
+        if not st:
+            continue
+        m = re.match(r"const (\w+)(?::\s*f64)? = (-?[\d.]+)$", st)
+        if m:
+            v = m.group(2)
+            consts[m.group(1)] = float(v) if "." in v else int(v)
+            continue
+        m = re.match(r"const (\w+)(?::\s*cf64)? = " + CINIT.pattern + "$", st)
+        if m:
+            cconsts[m.group(1)] = [float(ev(m.group(2), consts)), float(ev(m.group(3), consts))]
+            continue
+        m = re.match(r"(?:const|var) (\w+) = try a\.alloc\((f64|cf64), (.+)\)$", st)
+        if m:
+            started = started or m.group(2) == "cf64"
+            if started:
+                steps.append({"op": "alloc", "name": m.group(1), "size": int(ev(m.group(3), consts)),
+                              "complex": m.group(2) == "cf64"})
+            continue
+        if not started:
+            continue
+        m = re.match(r"@memcpy\((\w+)\.ptr, &\[_\](f64|cf64)\{(.*)\}\)$", st, re.S)
+        if m:
+            if m.group(2) == "cf64":
+                vals = [[float(ev(x, consts)), float(ev(y, consts))] for x, y in CINIT.findall(m.group(3))]
+            else:
+                vals = [float(x) for x in re.split(r"[,\s]+", m.group(3).strip()) if x]
+            steps.append({"op": "init", "name": m.group(1), "values": vals})
+            continue
+        m = re.match(r"(\w+)\((.*)\) catch unreachable$", st, re.S)
+        if m and m.group(1) == fn:
+            args = []
+            for x in split_args(m.group(2)):
+                if x == ".{}":
+                    continue
+                if x in ENUMS:
+                    args.append(ENUMS[x])
+                elif x.endswith(".ptr"):
+                    args.append({"arr": x[:-4]})
+                elif x in cconsts:
+                    args.append({"c": cconsts[x]})
+                elif CINIT.fullmatch(x):
+                    mm = CINIT.fullmatch(x)
+                    args.append({"c": [float(ev(mm.group(1), consts)), float(ev(mm.group(2), consts))]})
+                else:
+                    args.append(ev(x, consts))
+            steps.append({"op": "call", "fn": fn, "args": args})
+            continue
+        m = re.match(r"try std\.testing\.expectEqual\((-?[\d.e+-]+), (\w+)\[(\d+)\](?:\.(re|im))?\)$", st)
+        if m:
+            steps.append({"op": "expect", "arr": m.group(2), "idx": int(m.group(3)),
+                          "part": m.group(4), "value": float(m.group(1)), "rel": 0.0})
+            continue
+        m = re.match(r"try std\.testing\.expectApproxEqRel\((-?[\d.e+-]+), (\w+)\[(\d+)\](?:\.(re|im))?, "
+                     r"([\d.e+-]+)\)$", st)
+        if m:
+            steps.append({"op": "expect", "arr": m.group(2), "idx": int(m.group(3)),
+                          "part": m.group(4), "value": float(m.group(1)), "rel": float(m.group(5))})
+            continue
+        m = re.match(r"try std\.testing\.expectApproxEqAbs\((-?[\d.e+-]+), (\w+)\[(\d+)\](?:\.(re|im))?, "
+                     r"([\d.e+-]+)\)$", st)
+        if m:
+            steps.append({"op": "expect", "arr": m.group(2), "idx": int(m.group(3)),
+                          "part": m.group(4), "value": float(m.group(1)), "rel": 0.0,
+                          "abs": float(m.group(5))})
+            continue
+    return {"name": "z" + fn, "source": "test/linalg/blas/%s.zig" % fn, "steps": steps}
+
+
 def parse_scalar_tests(root):
     """iamax and nrm2: their expected scalars, read from the files."""
     out = {}
@@ -151,6 +237,13 @@ def main():
         with open(os.path.join(here, "blas_%s.json" % fn), "w") as f:
             json.dump(fx, f, separators=(",", ":"))
         print("%-5s %3d calls %5d expectations" % (fn, n_calls, n_exp))
+    for fn in COMPLEX:
+        fx = parse_chain_complex(os.path.join(root, "test/linalg/blas/%s.zig" % fn), fn)
+        n_calls = sum(1 for s in fx["steps"] if s["op"] == "call")
+        n_exp = sum(1 for s in fx["steps"] if s["op"] == "expect")
+        with open(os.path.join(here, "blas_z%s.json" % fn), "w") as f:
+            json.dump(fx, f, separators=(",", ":"))
+        print("z%-5s %3d calls %5d expectations" % (fn, n_calls, n_exp))
     sc = parse_scalar_tests(root)
     with open(os.path.join(here, "blas_scalars.json"), "w") as f:
         json.dump(sc, f, indent=1)

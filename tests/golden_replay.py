@@ -1,8 +1,10 @@
 """Replays zml's BLAS known-answer chains (tests/golden/blas_*.json).
 
 A backend is a mapping  name -> callable(*args)  where array arguments are
-float64 numpy buffers that the callable updates in place.  The same fixture
-drives the oracle (CPU) and the C ABI of the GPU library.
+numpy buffers (float64, or complex128 for the complex fixtures
+blas_z*.json) that the callable updates in place, and a complex scalar
+argument is a Python complex.  The same fixture drives the oracle (CPU) and
+the C ABI of the GPU library.
 """
 import json
 import os
@@ -23,17 +25,30 @@ def replay(fixture, call):
     for st in fixture["steps"]:
         op = st["op"]
         if op == "alloc":
-            arrays[st["name"]] = np.zeros(st["size"], dtype=np.float64)
+            dt = np.complex128 if st.get("complex") else np.float64
+            arrays[st["name"]] = np.zeros(st["size"], dtype=dt)
         elif op == "init":
-            arrays[st["name"]][: len(st["values"])] = st["values"]
+            vals = st["values"]
+            if vals and isinstance(vals[0], list):
+                vals = [complex(re_, im_) for re_, im_ in vals]
+            arrays[st["name"]][: len(vals)] = vals
         elif op == "call":
-            args = [arrays[a["arr"]] if isinstance(a, dict) else a for a in st["args"]]
+            args = []
+            for a in st["args"]:
+                if isinstance(a, dict):
+                    args.append(arrays[a["arr"]] if "arr" in a else complex(*a["c"]))
+                else:
+                    args.append(a)
             call(st["fn"], args)
         elif op == "expect":
             got = arrays[st["arr"]][st["idx"]]
+            part = st.get("part")
+            got = got.real if part == "re" else got.imag if part == "im" else got
             want = st["value"]
             checked += 1
-            if st["rel"] == 0.0:
+            if "abs" in st:  # std.testing.expectApproxEqAbs
+                ok = abs(got - want) <= st["abs"]
+            elif st["rel"] == 0.0:
                 ok = got == want
             else:  # std.testing.expectApproxEqRel
                 ok = abs(got - want) <= st["rel"] * max(abs(got), abs(want)) or got == want

@@ -18,6 +18,22 @@ _lib = None
 i32, f64, f32, vp = C.c_int, C.c_double, C.c_float, C.c_void_p
 
 
+class CF64(C.Structure):
+    """zo_cf64: a complex128 scalar passed by value."""
+    _fields_ = [("re", C.c_double), ("im", C.c_double)]
+
+
+class CF32(C.Structure):
+    """zo_cf32: a complex64 scalar passed by value."""
+    _fields_ = [("re", C.c_float), ("im", C.c_float)]
+
+
+def cs(x, dtype=np.complex128):
+    """A Python / numpy number as the complex scalar struct of `dtype`."""
+    x = complex(x)
+    return (CF64 if np.dtype(dtype) == np.complex128 else CF32)(x.real, x.imag)
+
+
 def load():
     global _lib
     if _lib is None:
@@ -55,6 +71,32 @@ def load():
             for name, (res, args) in sig.items():
                 fn = getattr(_lib, pfx + name)
                 fn.restype, fn.argtypes = res, args
+        for pfx, Z, R in (("zo_z_", CF64, f64), ("zo_c_", CF32, f32)):
+            sig = {
+                "gemm": (i32, [i32, i32, i32, i32, i32, i32, Z, vp, i32, vp, i32, Z, vp, i32]),
+                "trsm": (i32, [i32, i32, i32, i32, i32, i32, i32, Z, vp, i32, vp, i32]),
+                "trmm": (i32, [i32, i32, i32, i32, i32, i32, i32, Z, vp, i32, vp, i32]),
+                "syrk": (i32, [i32, i32, i32, i32, i32, Z, vp, i32, Z, vp, i32]),
+                "herk": (i32, [i32, i32, i32, i32, i32, R, vp, i32, R, vp, i32]),
+                "gemv": (i32, [i32, i32, i32, i32, Z, vp, i32, vp, i32, Z, vp, i32]),
+                "geru": (i32, [i32, i32, i32, Z, vp, i32, vp, i32, vp, i32]),
+                "gerc": (i32, [i32, i32, i32, Z, vp, i32, vp, i32, vp, i32]),
+                "iamax": (i32, [i32, vp, i32]),
+                "scal": (i32, [i32, Z, vp, i32]),
+                "laswp": (i32, [i32, i32, vp, i32, i32, i32, vp, i32]),
+                "getrf2": (i32, [i32, i32, i32, vp, i32, vp]),
+                "getrf": (i32, [i32, i32, i32, vp, i32, vp]),
+                "getrs": (i32, [i32, i32, i32, i32, vp, i32, vp, vp, i32]),
+                "gesv": (i32, [i32, i32, i32, vp, i32, vp, vp, i32]),
+                "potrf2": (i32, [i32, i32, i32, vp, i32]),
+                "potrf": (i32, [i32, i32, i32, vp, i32]),
+                "potrs": (i32, [i32, i32, i32, i32, vp, i32, vp, i32]),
+                "posv": (i32, [i32, i32, i32, i32, vp, i32, vp, i32]),
+            }
+            for name, (res, args) in sig.items():
+                f = getattr(_lib, pfx + name)
+                f.restype, f.argtypes = res, args
+        _lib.zo_set_cdiv_as_written.argtypes = [i32]
         _lib.zo_set_trsm_as_written.argtypes = [i32]
         _lib.zo_ilaenv.argtypes = [i32, C.c_char_p, i32, i32, i32, i32]
         _lib.zo_ilaenv.restype = i32
@@ -65,8 +107,12 @@ def ptr(a):
     return a.ctypes.data_as(vp) if a is not None else None
 
 
+PREFIX = {np.dtype(np.float64): "zo_d_", np.dtype(np.float32): "zo_s_",
+          np.dtype(np.complex128): "zo_z_", np.dtype(np.complex64): "zo_c_"}
+
+
 def fn(name, dtype=np.float64):
-    return getattr(load(), ("zo_d_" if dtype == np.float64 else "zo_s_") + name)
+    return getattr(load(), PREFIX[np.dtype(dtype)] + name)
 
 
 # ---- numpy-level conveniences (column-major, Fortran-ordered arrays) --------

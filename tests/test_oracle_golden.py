@@ -1,7 +1,8 @@
 """The oracle against zml's own known-answer BLAS tests (CPU only).
 
 The fixtures in tests/golden/ are the literal expectations of zml's
-test/linalg/blas/{gemm,trsm,syrk,trmm,gemv,ger,iamax,nrm2}.zig; an oracle that
+test/linalg/blas/{gemm,trsm,syrk,trmm,gemv,ger,iamax,nrm2}.zig (real parts)
+and of the cf64 parts and herk / geru / gerc (blas_z*.json); an oracle that
 fails one of them does not restate the reference.
 """
 import json
@@ -25,6 +26,32 @@ def oracle_call(name, args):
 def test_oracle_matches_reference_fixtures(name):
     fx = load_fixture(name)
     checked, failures = replay(fx, oracle_call)
+    assert checked > 0
+    assert not failures, failures[:5]
+
+
+def oracle_zcall(name, args):
+    """A complex fixture's call on the zo_z_ routines: complex scalars go by
+    value as the struct the signature names (herk's alpha / beta are real)."""
+    f = ol.fn(name, np.complex128)
+    conv = []
+    for a, t in zip(args, f.argtypes):
+        if isinstance(a, np.ndarray):
+            conv.append(ol.ptr(a))
+        elif t is ol.CF64:
+            conv.append(ol.cs(a))
+        else:
+            conv.append(a)
+    r = f(*conv)
+    assert r == 0, (name, args[:8], r)
+
+
+@pytest.mark.parametrize("name", ["gemm", "trsm", "syrk", "herk", "trmm", "gemv", "geru", "gerc"])
+def test_complex_oracle_matches_reference_fixtures(name):
+    """The cf64 parts of zml's BLAS tests (and its complex-only herk, geru,
+    gerc tests) replayed on the complex oracle."""
+    fx = load_fixture("z" + name)
+    checked, failures = replay(fx, oracle_zcall)
     assert checked > 0
     assert not failures, failures[:5]
 
