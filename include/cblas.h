@@ -57,6 +57,31 @@ void cblas_dtrsm(const CBLAS_ORDER order, const CBLAS_SIDE side, const CBLAS_UPL
                  const CBLAS_TRANSPOSE transa, const CBLAS_DIAG diag, const int m, const int n,
                  const double alpha, const double *a, const int lda, double *b, const int ldb);
 
+/* Complex level 3 (reference include/cblas.h:218-219, 224-225, 237-238):
+ * matrices are interleaved (re, im) pairs, leading dimensions in complex
+ * elements; alpha / beta point to one {re, im} pair (herk: real scalars).
+ * Computed as real GEMMs on the GPU (a complex product is four real ones). */
+void cblas_cgemm(const CBLAS_ORDER order, const CBLAS_TRANSPOSE transa,
+                 const CBLAS_TRANSPOSE transb, const int m, const int n, const int k,
+                 const void *alpha, const void *a, const int lda, const void *b, const int ldb,
+                 const void *beta, void *c, const int ldc);
+void cblas_zgemm(const CBLAS_ORDER order, const CBLAS_TRANSPOSE transa,
+                 const CBLAS_TRANSPOSE transb, const int m, const int n, const int k,
+                 const void *alpha, const void *a, const int lda, const void *b, const int ldb,
+                 const void *beta, void *c, const int ldc);
+void cblas_cherk(const CBLAS_ORDER order, const CBLAS_UPLO uplo, const CBLAS_TRANSPOSE trans,
+                 const int n, const int k, const float alpha, const void *a, const int lda,
+                 const float beta, void *c, const int ldc);
+void cblas_zherk(const CBLAS_ORDER order, const CBLAS_UPLO uplo, const CBLAS_TRANSPOSE trans,
+                 const int n, const int k, const double alpha, const void *a, const int lda,
+                 const double beta, void *c, const int ldc);
+void cblas_csyrk(const CBLAS_ORDER order, const CBLAS_UPLO uplo, const CBLAS_TRANSPOSE trans,
+                 const int n, const int k, const void *alpha, const void *a, const int lda,
+                 const void *beta, void *c, const int ldc);
+void cblas_zsyrk(const CBLAS_ORDER order, const CBLAS_UPLO uplo, const CBLAS_TRANSPOSE trans,
+                 const int n, const int k, const void *alpha, const void *a, const int lda,
+                 const void *beta, void *c, const int ldc);
+
 #ifdef __cplusplus
 }
 #endif

@@ -39,6 +39,12 @@ for p, T in (("d", f64), ("s", f32)):
         "LAPACKE_%sgeqrf" % p: (i32, [i32, i32, i32, vp, i32, vp]),
         "LAPACKE_%sorgqr" % p: (i32, [i32, i32, i32, i32, vp, i32, vp]),
     })
+for p, R in (("z", f64), ("c", f32)):  # complex: scalars by pointer, herk's real
+    _SIGS.update({
+        "cblas_%sgemm" % p: (None, [i32, i32, i32, i32, i32, i32, vp, vp, i32, vp, i32, vp, vp, i32]),
+        "cblas_%sherk" % p: (None, [i32, i32, i32, i32, i32, R, vp, i32, R, vp, i32]),
+        "cblas_%ssyrk" % p: (None, [i32, i32, i32, i32, i32, vp, vp, i32, vp, vp, i32]),
+    })
 _SIGS.update({
     "zml_gpu_dgetrf": (i32, [i32, i32, vp, i32, vp, vp, vp]),
     "zml_gpu_dgetrs": (i32, [ch, i32, i32, vp, i32, vp, vp, i32, vp]),

@@ -16,6 +16,7 @@
 // Every pointer may be host memory (staged through device workspaces) or
 // device / managed memory (used in place).  Calls are synchronous.
 #include <cstring>
+#include <type_traits>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -150,6 +151,86 @@ int gemm_any(int order, int ta, int tb, int m, int n, int k, T alpha, const T *a
   ZG_TRY(C.in(c, ldc, m, n, kSlotC, beta != T(0), s));
   ZG_TRY(gemm_simt<T>(ta, tb, m, n, use_ab ? k : 0, alpha, A.d, A.ld ? A.ld : 1, B.d,
                       B.ld ? B.ld : 1, beta, C.d, C.ld, 0, s));
+  ZG_TRY(C.out(s));
+  return sync(s);
+}
+
+// Complex gemm (cblas_zgemm / cblas_cgemm, reference include/cblas.h:218-219;
+// the checks and the row-major swap of blas/gemm.zig:14-66, 101-108).
+// Scalars are {re, im} pairs of R, matrices interleaved pairs.
+template <typename R>
+int zgemm_any(int order, int ta, int tb, int m, int n, int k, const R *alpha, const R *a, int lda,
+              const R *b, int ldb, const R *beta, R *c, int ldc) {
+  using C2 = typename std::conditional<sizeof(R) == 8, double2, float2>::type;
+  if (!alpha || !beta) return kErrInvalid;
+  if (order != kRowMajor && order != kColMajor) return kErrInvalid;
+  if (!is_trans(ta) || !is_trans(tb)) return kErrInvalid;
+  if (order == kRowMajor) {
+    std::swap(ta, tb); std::swap(m, n); std::swap(a, b); std::swap(lda, ldb);
+  }
+  const bool nota = ta == kNoTrans || ta == kConjNoTrans;
+  const bool notb = tb == kNoTrans || tb == kConjNoTrans;
+  const int nrowa = nota ? m : k, ncola = nota ? k : m;
+  const int nrowb = notb ? k : n, ncolb = notb ? n : k;
+  if (m < 0 || n < 0 || k < 0 || lda < std::max(1, nrowa) || ldb < std::max(1, nrowb) ||
+      ldc < std::max(1, m))
+    return kErrInvalid;
+  const bool azero = alpha[0] == R(0) && alpha[1] == R(0);
+  const bool bone = beta[0] == R(1) && beta[1] == R(0);
+  if (m == 0 || n == 0 || ((azero || k == 0) && bone)) return 0;
+  cudaStream_t s = lib_stream();
+  Staged<C2> A, B, C;
+  const bool use_ab = !azero && k > 0;
+  if (use_ab) {
+    ZG_TRY(A.in((const C2 *)a, lda, nrowa, ncola, kSlotA, true, s));
+    ZG_TRY(B.in((const C2 *)b, ldb, nrowb, ncolb, kSlotB, true, s));
+  }
+  const bool bzero = beta[0] == R(0) && beta[1] == R(0);
+  ZG_TRY(C.in((const C2 *)c, ldc, m, n, kSlotC, !bzero, s));
+  ZG_TRY(zgemm_dev<R>(ta, tb, m, n, use_ab ? k : 0, alpha, (const R *)A.d, A.ld ? A.ld : 1,
+                      (const R *)B.d, B.ld ? B.ld : 1, beta, (R *)C.d, C.ld, s));
+  ZG_TRY(C.out(s));
+  return sync(s);
+}
+
+// Complex herk (herm) and syrk (cblas_zherk / cblas_zsyrk and the c forms,
+// reference include/cblas.h:224-225, 237-238): row-major inverts uplo and
+// reverses (herk, herk.zig:14-58) or inverts (syrk, syrk.zig:15-58) the
+// transpose; herk accepts no_trans / conj_trans, syrk no_trans / trans.
+template <typename R>
+int zsyherk_any(bool herm, int order, int uplo, int trans, int n, int k, const R *alpha,
+                const R *a, int lda, const R *beta, R *c, int ldc) {
+  using C2 = typename std::conditional<sizeof(R) == 8, double2, float2>::type;
+  if (!alpha || !beta) return kErrInvalid;
+  if (order != kRowMajor && order != kColMajor) return kErrInvalid;
+  if (uplo != kUpper && uplo != kLower) return kErrInvalid;
+  if (!is_trans(trans)) return kErrInvalid;
+  if (order == kRowMajor) {
+    uplo = uplo == kUpper ? kLower : kUpper;
+    if (herm)
+      trans = trans == kNoTrans ? kConjTrans
+            : trans == kConjTrans ? kNoTrans
+            : trans == kTrans ? kConjNoTrans : kTrans;
+    else
+      trans = trans_invert(trans);
+  }
+  const bool ok_trans = herm ? (trans == kNoTrans || trans == kConjTrans)
+                             : (trans == kNoTrans || trans == kTrans);
+  const int nrowa = trans == kNoTrans ? n : k;
+  if (!ok_trans || n < 0 || k < 0 || lda < std::max(1, nrowa) || ldc < std::max(1, n))
+    return kErrInvalid;
+  const bool azero = alpha[0] == R(0) && alpha[1] == R(0);
+  const bool bone = beta[0] == R(1) && beta[1] == R(0);
+  if (n == 0 || ((azero || k == 0) && bone)) return 0;
+  cudaStream_t s = lib_stream();
+  Staged<C2> A, C;
+  const bool use_a = !azero && k > 0;
+  if (use_a) ZG_TRY(A.in((const C2 *)a, lda, nrowa, trans == kNoTrans ? k : n, kSlotA, true, s));
+  // C: the whole n x n square is staged so that the other triangle survives
+  ZG_TRY(C.in((const C2 *)c, ldc, n, n, kSlotC, true, s));
+  const R a0[2] = {use_a ? alpha[0] : R(0), use_a ? alpha[1] : R(0)};
+  ZG_TRY(zsyherk_dev<R>(herm, uplo, trans, n, use_a ? k : 0, a0, (const R *)A.d,
+                        A.ld ? A.ld : 1, beta, (R *)C.d, C.ld, s));
   ZG_TRY(C.out(s));
   return sync(s);
 }
@@ -518,6 +599,27 @@ extern "C" {
 CBLAS_GEMM(d, double)
 CBLAS_GEMM(s, float)
 #undef CBLAS_GEMM
+
+#define CBLAS_ZGEMM(P, R)                                                                          \
+  void cblas_##P##gemm(int order, int ta, int tb, int m, int n, int k, const void *alpha,           \
+                       const void *a, int lda, const void *b, int ldb, const void *beta, void *c,   \
+                       int ldc) {                                                                   \
+    zgemm_any<R>(order, ta, tb, m, n, k, (const R *)alpha, (const R *)a, lda, (const R *)b, ldb,    \
+                 (const R *)beta, (R *)c, ldc);                                                     \
+  }                                                                                                 \
+  void cblas_##P##herk(int order, int uplo, int trans, int n, int k, R alpha, const void *a,        \
+                       int lda, R beta, void *c, int ldc) {                                         \
+    const R al[2] = {alpha, R(0)}, be[2] = {beta, R(0)};                                            \
+    zsyherk_any<R>(true, order, uplo, trans, n, k, al, (const R *)a, lda, be, (R *)c, ldc);         \
+  }                                                                                                 \
+  void cblas_##P##syrk(int order, int uplo, int trans, int n, int k, const void *alpha,             \
+                       const void *a, int lda, const void *beta, void *c, int ldc) {                \
+    zsyherk_any<R>(false, order, uplo, trans, n, k, (const R *)alpha, (const R *)a, lda,            \
+                   (const R *)beta, (R *)c, ldc);                                                   \
+  }
+CBLAS_ZGEMM(z, double)
+CBLAS_ZGEMM(c, float)
+#undef CBLAS_ZGEMM
 
 // ---- LAPACKE-shaped (include/clapack.h) ----
 #define LAPACKE_FNS(P, T)                                                                        \

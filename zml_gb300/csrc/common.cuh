@@ -97,6 +97,9 @@ enum Slot : int {
   kSlotSelNet = 18,           // selector network parameters, input, logits, work
   kSlotF64LU = 19,            // FP64 LU copy and pivots of the selector's last resort
   kSlotInvL = 20,             // mixed LU: inverse of the unit-lower diagonal block, block row
+  kSlotZExp = 21,             // complex GEMM: the expanded real 2m x 2k operand
+  kSlotZOpB = 22,             // complex GEMM: op(B) materialized
+  kSlotZTmp = 23,             // complex herk / syrk: the full product
   kNumSlots = 24
 };
 

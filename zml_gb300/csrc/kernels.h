@@ -19,6 +19,19 @@ int gemm_simt_splitk(int transa, int transb, int m, int n, int k, T alpha, const
                      const T *B, long ldb, T beta, T *C, long ldc, int splits, T *work,
                      cudaStream_t s);
 
+// zblas.cu -- complex level 3 on the real SIMT GEMM.  Complex matrices are
+// interleaved (re, im) pairs of R, leading dimensions in complex elements,
+// scalars as {re, im}.  zgemm: C <- alpha op(A) op(B) + beta C, any of the
+// four transposes.  zsyherk: the triangle of C <- alpha op(A) op(A)^H + beta C
+// (herm; alpha, beta real) or alpha op(A) op(A)^T + beta C, trans kNoTrans
+// (A n x k) or kConjTrans / kTrans (A k x n).
+template <typename R>
+int zgemm_dev(int ta, int tb, int m, int n, int k, const R *alpha, const R *A, long lda,
+              const R *B, long ldb, const R *beta, R *C, long ldc, cudaStream_t s);
+template <typename R>
+int zsyherk_dev(bool herm, int uplo, int trans, int n, int k, const R *alpha, const R *A, long lda,
+                const R *beta, R *C, long ldc, cudaStream_t s);
+
 // qr.cu -- Householder QR (geqrf) with the T factor of each panel.
 template <typename T> int geqrf_dev(int m, int n, T *A, long lda, T *tau, cudaStream_t s);
 // The first n columns of Q from geqrf's reflectors (k of them) stored in A.
