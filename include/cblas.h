@@ -81,6 +81,13 @@ void cblas_csyrk(const CBLAS_ORDER order, const CBLAS_UPLO uplo, const CBLAS_TRA
 void cblas_zsyrk(const CBLAS_ORDER order, const CBLAS_UPLO uplo, const CBLAS_TRANSPOSE trans,
                  const int n, const int k, const void *alpha, const void *a, const int lda,
                  const void *beta, void *c, const int ldc);
+/* reference include/cblas.h:252-253: B <- alpha op(A)^-1 B or alpha B op(A)^-1 */
+void cblas_ctrsm(const CBLAS_ORDER order, const CBLAS_SIDE side, const CBLAS_UPLO uplo,
+                 const CBLAS_TRANSPOSE transa, const CBLAS_DIAG diag, const int m, const int n,
+                 const void *alpha, const void *a, const int lda, void *b, const int ldb);
+void cblas_ztrsm(const CBLAS_ORDER order, const CBLAS_SIDE side, const CBLAS_UPLO uplo,
+                 const CBLAS_TRANSPOSE transa, const CBLAS_DIAG diag, const int m, const int n,
+                 const void *alpha, const void *a, const int lda, void *b, const int ldb);
 
 #ifdef __cplusplus
 }

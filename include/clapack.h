@@ -61,6 +61,33 @@ int LAPACKE_dposv(int matrix_layout, char uplo, int n, int nrhs, double *a, int 
 int LAPACKE_sposv(int matrix_layout, char uplo, int n, int nrhs, float *a, int lda, float *b,
                   int ldb);
 
+/* ---- complex (zml's cfloat branches of the same routines) ---------------
+ * Matrices are interleaved (re, im) pairs (LAPACKE's lapack_complex_double /
+ * lapack_complex_float layout), passed as void pointers; trans 'N', 'T' or
+ * 'C'; potrf factors the Hermitian matrix (A = U^H U or L L^H, the diagonal
+ * real).  Called by lapack.zig:1181/1190 (getrf), 1592/1606 (getrs),
+ * 2117/2128 (gesv), 3023/3031 (potrf), 3482/3495 (potrs), 3962/3973 (posv). */
+int LAPACKE_zgetrf(int matrix_layout, int m, int n, void *a, int lda, int *ipiv);
+int LAPACKE_cgetrf(int matrix_layout, int m, int n, void *a, int lda, int *ipiv);
+int LAPACKE_zgetrs(int matrix_layout, char trans, int n, int nrhs, const void *a, int lda,
+                   const int *ipiv, void *b, int ldb);
+int LAPACKE_cgetrs(int matrix_layout, char trans, int n, int nrhs, const void *a, int lda,
+                   const int *ipiv, void *b, int ldb);
+int LAPACKE_zgesv(int matrix_layout, int n, int nrhs, void *a, int lda, int *ipiv, void *b,
+                  int ldb);
+int LAPACKE_cgesv(int matrix_layout, int n, int nrhs, void *a, int lda, int *ipiv, void *b,
+                  int ldb);
+int LAPACKE_zpotrf(int matrix_layout, char uplo, int n, void *a, int lda);
+int LAPACKE_cpotrf(int matrix_layout, char uplo, int n, void *a, int lda);
+int LAPACKE_zpotrs(int matrix_layout, char uplo, int n, int nrhs, const void *a, int lda,
+                   void *b, int ldb);
+int LAPACKE_cpotrs(int matrix_layout, char uplo, int n, int nrhs, const void *a, int lda,
+                   void *b, int ldb);
+int LAPACKE_zposv(int matrix_layout, char uplo, int n, int nrhs, void *a, int lda, void *b,
+                  int ldb);
+int LAPACKE_cposv(int matrix_layout, char uplo, int n, int nrhs, void *a, int lda, void *b,
+                  int ldb);
+
 /* replaces zml.linalg.lapack.geqrf (lapack.zig:5060; kernel lapack/geqrf.zig:18):
  * R in the upper triangle, the Householder vectors below it, tau[min(m,n)] */
 int LAPACKE_dgeqrf(int matrix_layout, int m, int n, double *a, int lda, double *tau);

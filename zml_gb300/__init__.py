@@ -44,6 +44,13 @@ for p, R in (("z", f64), ("c", f32)):  # complex: scalars by pointer, herk's rea
         "cblas_%sgemm" % p: (None, [i32, i32, i32, i32, i32, i32, vp, vp, i32, vp, i32, vp, vp, i32]),
         "cblas_%sherk" % p: (None, [i32, i32, i32, i32, i32, R, vp, i32, R, vp, i32]),
         "cblas_%ssyrk" % p: (None, [i32, i32, i32, i32, i32, vp, vp, i32, vp, vp, i32]),
+        "cblas_%strsm" % p: (None, [i32, i32, i32, i32, i32, i32, i32, vp, vp, i32, vp, i32]),
+        "LAPACKE_%sgetrf" % p: (i32, [i32, i32, i32, vp, i32, vp]),
+        "LAPACKE_%sgetrs" % p: (i32, [i32, ch, i32, i32, vp, i32, vp, vp, i32]),
+        "LAPACKE_%sgesv" % p: (i32, [i32, i32, i32, vp, i32, vp, vp, i32]),
+        "LAPACKE_%spotrf" % p: (i32, [i32, ch, i32, vp, i32]),
+        "LAPACKE_%spotrs" % p: (i32, [i32, ch, i32, i32, vp, i32, vp, i32]),
+        "LAPACKE_%sposv" % p: (i32, [i32, ch, i32, i32, vp, i32, vp, i32]),
     })
 _SIGS.update({
     "zml_gpu_dgetrf": (i32, [i32, i32, vp, i32, vp, vp, vp]),

@@ -235,6 +235,36 @@ int zsyherk_any(bool herm, int order, int uplo, int trans, int n, int k, const R
   return sync(s);
 }
 
+// Complex trsm (cblas_ztrsm / cblas_ctrsm, reference include/cblas.h:252-253;
+// the row-major mapping of trsm.zig:18-64).
+template <typename R>
+int ztrsm_any(int order, int side, int uplo, int ta, int diag, int m, int n, const R *alpha,
+              const R *a, int lda, R *b, int ldb) {
+  using C2 = typename Cx<R>::T;
+  if (!alpha) return kErrInvalid;
+  if (order != kRowMajor && order != kColMajor) return kErrInvalid;
+  if ((side != kLeft && side != kRight) || (uplo != kUpper && uplo != kLower) || !is_trans(ta) ||
+      (diag != kUnit && diag != kNonUnit))
+    return kErrInvalid;
+  if (order == kRowMajor) {
+    side = side == kLeft ? kRight : kLeft;
+    uplo = uplo == kUpper ? kLower : kUpper;
+    std::swap(m, n);
+  }
+  const int nrowa = side == kLeft ? m : n;
+  if (m < 0 || n < 0 || lda < std::max(1, nrowa) || ldb < std::max(1, m)) return kErrInvalid;
+  if (m == 0 || n == 0) return 0;
+  const bool azero = alpha[0] == R(0) && alpha[1] == R(0);
+  cudaStream_t s = lib_stream();
+  Staged<C2> A, B;
+  if (!azero) ZG_TRY(A.in((const C2 *)a, lda, nrowa, nrowa, kSlotA, true, s));
+  ZG_TRY(B.in((const C2 *)b, ldb, m, n, kSlotB, !azero, s));
+  ZG_TRY(ztrsm_dev<R>(side, uplo, ta, diag, m, n, alpha, (const R *)A.d, A.ld ? A.ld : 1,
+                      (R *)B.d, B.ld, s));
+  ZG_TRY(B.out(s));
+  return sync(s);
+}
+
 template <typename T>
 int syrk_any(int order, int uplo, int trans, int n, int k, T alpha, const T *a, int lda, T beta,
              T *c, int ldc) {
@@ -452,6 +482,147 @@ int posv_any(int layout, char uplo, int n, int nrhs, T *a, int lda, T *b, int ld
   return info;
 }
 
+// ---- complex LAPACK (LAPACKE_z* / LAPACKE_c*, lapack.zig cfloat branches,
+// e.g. :1190 LAPACKE_zgetrf) --------------------------------------------------
+// Matrices are interleaved (re, im) pairs of R; argument checks and return
+// codes as the real wrappers above.
+template <typename R> int zgetrf_any(int layout, int m, int n, R *a, int lda, int *ipiv) {
+  using C2 = typename Cx<R>::T;
+  if (!lay_ok(layout)) return -1;
+  if (m < 0) return -2;
+  if (n < 0) return -3;
+  if (lda < std::max(1, layout == kColMajor ? m : n)) return -5;
+  if (m == 0 || n == 0) return 0;
+  cudaStream_t s = lib_stream();
+  ColMajor<C2> A;
+  Buf<int> P;
+  ZG_TRY(A.in(layout, (const C2 *)a, lda, m, n, kSlotA, kSlotAT, true, s));
+  ZG_TRY(P.in(ipiv, std::min(m, n), kSlotPiv, false, s));
+  int info = 0;
+  ZG_TRY(zgetrf_dev<R>(m, n, (R *)A.d, A.ld, P.d, &info, s));
+  ZG_TRY(A.out(s));
+  ZG_TRY(P.out(s));
+  ZG_TRY(sync(s));
+  return info;
+}
+
+int ztrans_code(char t) { return t == 'N' ? kNoTrans : t == 'T' ? kTrans : kConjTrans; }
+
+template <typename R>
+int zgetrs_any(int layout, char trans, int n, int nrhs, const R *a, int lda, const int *ipiv,
+               R *b, int ldb) {
+  using C2 = typename Cx<R>::T;
+  if (!lay_ok(layout)) return -1;
+  trans = up(trans);
+  if (trans != 'N' && trans != 'T' && trans != 'C') return -2;
+  if (n < 0) return -3;
+  if (nrhs < 0) return -4;
+  if (lda < std::max(1, n)) return -6;
+  if (ldb < std::max(1, layout == kColMajor ? n : nrhs)) return -9;
+  if (n == 0 || nrhs == 0) return 0;
+  cudaStream_t s = lib_stream();
+  ColMajor<C2> A, B;
+  Buf<int> P;
+  ZG_TRY(A.in(layout, (const C2 *)a, lda, n, n, kSlotA, kSlotAT, true, s));
+  ZG_TRY(B.in(layout, (const C2 *)b, ldb, n, nrhs, kSlotB, kSlotBT, true, s));
+  ZG_TRY(P.in(const_cast<int *>(ipiv), n, kSlotPiv, true, s));
+  ZG_TRY(zgetrs_dev<R>(ztrans_code(trans), n, nrhs, (const R *)A.d, A.ld, P.d, (R *)B.d, B.ld,
+                       s));
+  ZG_TRY(B.out(s));
+  ZG_TRY(sync(s));
+  return 0;
+}
+
+template <typename R>
+int zgesv_any(int layout, int n, int nrhs, R *a, int lda, int *ipiv, R *b, int ldb) {
+  using C2 = typename Cx<R>::T;
+  if (!lay_ok(layout)) return -1;
+  if (n < 0) return -2;
+  if (nrhs < 0) return -3;
+  if (lda < std::max(1, n)) return -5;
+  if (ldb < std::max(1, layout == kColMajor ? n : nrhs)) return -8;
+  if (n == 0 || nrhs == 0) return 0;
+  cudaStream_t s = lib_stream();
+  ColMajor<C2> A, B;
+  Buf<int> P;
+  ZG_TRY(A.in(layout, (const C2 *)a, lda, n, n, kSlotA, kSlotAT, true, s));
+  ZG_TRY(B.in(layout, (const C2 *)b, ldb, n, nrhs, kSlotB, kSlotBT, true, s));
+  ZG_TRY(P.in(ipiv, n, kSlotPiv, false, s));
+  int info = 0;
+  ZG_TRY(zgetrf_dev<R>(n, n, (R *)A.d, A.ld, P.d, &info, s));
+  if (info == 0) ZG_TRY(zgetrs_dev<R>(kNoTrans, n, nrhs, (const R *)A.d, A.ld, P.d, (R *)B.d, B.ld, s));
+  ZG_TRY(A.out(s));
+  ZG_TRY(P.out(s));
+  if (info == 0) ZG_TRY(B.out(s));
+  ZG_TRY(sync(s));
+  return info;
+}
+
+template <typename R> int zpotrf_any(int layout, char uplo, int n, R *a, int lda) {
+  using C2 = typename Cx<R>::T;
+  if (!lay_ok(layout)) return -1;
+  uplo = up(uplo);
+  if (uplo != 'U' && uplo != 'L') return -2;
+  if (n < 0) return -3;
+  if (lda < std::max(1, n)) return -5;
+  if (n == 0) return 0;
+  cudaStream_t s = lib_stream();
+  ColMajor<C2> A;
+  ZG_TRY(A.in(layout, (const C2 *)a, lda, n, n, kSlotA, kSlotAT, true, s));
+  int info = 0;
+  ZG_TRY(zpotrf_dev<R>(uplo == 'L' ? kLower : kUpper, n, (R *)A.d, A.ld, &info, s));
+  ZG_TRY(A.out(s));
+  ZG_TRY(sync(s));
+  return info;
+}
+
+template <typename R>
+int zpotrs_any(int layout, char uplo, int n, int nrhs, const R *a, int lda, R *b, int ldb) {
+  using C2 = typename Cx<R>::T;
+  if (!lay_ok(layout)) return -1;
+  uplo = up(uplo);
+  if (uplo != 'U' && uplo != 'L') return -2;
+  if (n < 0) return -3;
+  if (nrhs < 0) return -4;
+  if (lda < std::max(1, n)) return -6;
+  if (ldb < std::max(1, layout == kColMajor ? n : nrhs)) return -8;
+  if (n == 0 || nrhs == 0) return 0;
+  cudaStream_t s = lib_stream();
+  ColMajor<C2> A, B;
+  ZG_TRY(A.in(layout, (const C2 *)a, lda, n, n, kSlotA, kSlotAT, true, s));
+  ZG_TRY(B.in(layout, (const C2 *)b, ldb, n, nrhs, kSlotB, kSlotBT, true, s));
+  ZG_TRY(zpotrs_dev<R>(uplo == 'L' ? kLower : kUpper, n, nrhs, (const R *)A.d, A.ld, (R *)B.d,
+                       B.ld, s));
+  ZG_TRY(B.out(s));
+  ZG_TRY(sync(s));
+  return 0;
+}
+
+template <typename R>
+int zposv_any(int layout, char uplo, int n, int nrhs, R *a, int lda, R *b, int ldb) {
+  using C2 = typename Cx<R>::T;
+  if (!lay_ok(layout)) return -1;
+  uplo = up(uplo);
+  if (uplo != 'U' && uplo != 'L') return -2;
+  if (n < 0) return -3;
+  if (nrhs < 0) return -4;
+  if (lda < std::max(1, n)) return -6;
+  if (ldb < std::max(1, layout == kColMajor ? n : nrhs)) return -8;
+  if (n == 0 || nrhs == 0) return 0;
+  cudaStream_t s = lib_stream();
+  ColMajor<C2> A, B;
+  ZG_TRY(A.in(layout, (const C2 *)a, lda, n, n, kSlotA, kSlotAT, true, s));
+  ZG_TRY(B.in(layout, (const C2 *)b, ldb, n, nrhs, kSlotB, kSlotBT, true, s));
+  const int ul = uplo == 'L' ? kLower : kUpper;
+  int info = 0;
+  ZG_TRY(zpotrf_dev<R>(ul, n, (R *)A.d, A.ld, &info, s));
+  if (info == 0) ZG_TRY(zpotrs_dev<R>(ul, n, nrhs, (const R *)A.d, A.ld, (R *)B.d, B.ld, s));
+  ZG_TRY(A.out(s));
+  if (info == 0) ZG_TRY(B.out(s));
+  ZG_TRY(sync(s));
+  return info;
+}
+
 template <typename T> int geqrf_any(int layout, int m, int n, T *a, int lda, T *tau) {
   if (!lay_ok(layout)) return -1;
   if (m < 0) return -2;
@@ -620,6 +791,38 @@ CBLAS_GEMM(s, float)
 CBLAS_ZGEMM(z, double)
 CBLAS_ZGEMM(c, float)
 #undef CBLAS_ZGEMM
+
+#define ZLAPACK_FNS(P, R)                                                                        \
+  void cblas_##P##trsm(int order, int side, int uplo, int ta, int diag, int m, int n,             \
+                       const void *alpha, const void *a, int lda, void *b, int ldb) {             \
+    ztrsm_any<R>(order, side, uplo, ta, diag, m, n, (const R *)alpha, (const R *)a, lda,         \
+                 (R *)b, ldb);                                                                   \
+  }                                                                                              \
+  int LAPACKE_##P##getrf(int layout, int m, int n, void *a, int lda, int *ipiv) {                \
+    return zgetrf_any<R>(layout, m, n, (R *)a, lda, ipiv);                                       \
+  }                                                                                              \
+  int LAPACKE_##P##getrs(int layout, char trans, int n, int nrhs, const void *a, int lda,        \
+                         const int *ipiv, void *b, int ldb) {                                    \
+    return zgetrs_any<R>(layout, trans, n, nrhs, (const R *)a, lda, ipiv, (R *)b, ldb);          \
+  }                                                                                              \
+  int LAPACKE_##P##gesv(int layout, int n, int nrhs, void *a, int lda, int *ipiv, void *b,       \
+                        int ldb) {                                                               \
+    return zgesv_any<R>(layout, n, nrhs, (R *)a, lda, ipiv, (R *)b, ldb);                        \
+  }                                                                                              \
+  int LAPACKE_##P##potrf(int layout, char uplo, int n, void *a, int lda) {                       \
+    return zpotrf_any<R>(layout, uplo, n, (R *)a, lda);                                          \
+  }                                                                                              \
+  int LAPACKE_##P##potrs(int layout, char uplo, int n, int nrhs, const void *a, int lda,         \
+                         void *b, int ldb) {                                                     \
+    return zpotrs_any<R>(layout, uplo, n, nrhs, (const R *)a, lda, (R *)b, ldb);                 \
+  }                                                                                              \
+  int LAPACKE_##P##posv(int layout, char uplo, int n, int nrhs, void *a, int lda, void *b,       \
+                        int ldb) {                                                               \
+    return zposv_any<R>(layout, uplo, n, nrhs, (R *)a, lda, (R *)b, ldb);                        \
+  }
+ZLAPACK_FNS(z, double)
+ZLAPACK_FNS(c, float)
+#undef ZLAPACK_FNS
 
 // ---- LAPACKE-shaped (include/clapack.h) ----
 #define LAPACKE_FNS(P, T)                                                                        \

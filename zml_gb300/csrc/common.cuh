@@ -100,7 +100,8 @@ enum Slot : int {
   kSlotZExp = 21,             // complex GEMM: the expanded real 2m x 2k operand
   kSlotZOpB = 22,             // complex GEMM: op(B) materialized
   kSlotZTmp = 23,             // complex herk / syrk: the full product
-  kNumSlots = 24
+  kSlotZTr = 24,              // complex trsm: the transposed right-hand side (right side)
+  kNumSlots = 28
 };
 
 // Returns a device buffer of at least `bytes` bound to `stream` in `slot`.

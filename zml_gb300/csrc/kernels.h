@@ -19,6 +19,11 @@ int gemm_simt_splitk(int transa, int transb, int m, int n, int k, T alpha, const
                      const T *B, long ldb, T beta, T *C, long ldc, int splits, T *work,
                      cudaStream_t s);
 
+// The storage type of a complex number with components R.
+template <typename R> struct Cx;
+template <> struct Cx<double> { using T = double2; };
+template <> struct Cx<float> { using T = float2; };
+
 // zblas.cu -- complex level 3 on the real SIMT GEMM.  Complex matrices are
 // interleaved (re, im) pairs of R, leading dimensions in complex elements,
 // scalars as {re, im}.  zgemm: C <- alpha op(A) op(B) + beta C, any of the
@@ -31,6 +36,21 @@ int zgemm_dev(int ta, int tb, int m, int n, int k, const R *alpha, const R *A, l
 template <typename R>
 int zsyherk_dev(bool herm, int uplo, int trans, int n, int k, const R *alpha, const R *A, long lda,
                 const R *beta, R *C, long ldc, cudaStream_t s);
+
+// zlapack.cu -- complex triangular solve, LU and Cholesky (same storage
+// conventions; ipiv device, 1-based; info as LAPACK's, read back on the
+// stream).  ztrsm_dev: B <- alpha op(A)^-1 B (left) or alpha B op(A)^-1.
+template <typename R>
+int ztrsm_dev(int side, int uplo, int transa, int diag, int m, int n, const R *alpha, const R *A,
+              long lda, R *B, long ldb, cudaStream_t s);
+template <typename R> int zgetrf_dev(int m, int n, R *A, long lda, int *ipiv, int *info,
+                                     cudaStream_t s);
+template <typename R>
+int zgetrs_dev(int trans, int n, int nrhs, const R *A, long lda, const int *ipiv, R *B, long ldb,
+               cudaStream_t s);
+template <typename R> int zpotrf_dev(int uplo, int n, R *A, long lda, int *info, cudaStream_t s);
+template <typename R>
+int zpotrs_dev(int uplo, int n, int nrhs, const R *A, long lda, R *B, long ldb, cudaStream_t s);
 
 // qr.cu -- Householder QR (geqrf) with the T factor of each panel.
 template <typename T> int geqrf_dev(int m, int n, T *A, long lda, T *tau, cudaStream_t s);

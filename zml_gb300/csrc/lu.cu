@@ -771,6 +771,9 @@ int getrs_dev(int trans, int n, int nrhs, const T *A, long lda, const int *ipiv,
 INST(double)
 INST(float)
 #undef INST
+// complex elements: the interchanges move 16- / 8-byte pairs
+template int laswp_dev<double2>(int, double2 *, long, int, int, const int *, int, cudaStream_t);
+template int laswp_dev<float2>(int, float2 *, long, int, int, const int *, int, cudaStream_t);
 
 }  // namespace zg
 

@@ -302,5 +302,7 @@ int trsm_dev(int side, int uplo, int transa, int diag, int m, int n, T alpha, co
 INST(double)
 INST(float)
 #undef INST
+template int transpose_dev<double2>(int, int, const double2 *, long, double2 *, long, cudaStream_t);
+template int transpose_dev<float2>(int, int, const float2 *, long, float2 *, long, cudaStream_t);
 
 }  // namespace zg

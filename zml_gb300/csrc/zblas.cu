@@ -18,10 +18,6 @@
 
 namespace zg {
 
-template <typename R> struct Cx;
-template <> struct Cx<double> { using T = double2; };
-template <> struct Cx<float> { using T = float2; };
-
 // op(A)(i, l) of an operand stored column-major, conjugated on request
 template <typename C2>
 __device__ __forceinline__ C2 op_at(const C2 *A, long lda, bool nota, bool cj, int i, int l) {
