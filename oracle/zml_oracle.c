@@ -1,6 +1,6 @@
 /*
  * zml_oracle.c -- instantiates the type-generic oracle for binary64 and
- * binary32, real (oracle_impl.h, oracle_qr_impl.h) and complex
+ * binary32, real (oracle_impl.h, oracle_qr_impl.h, oracle_sy_impl.h) and complex
  * (oracle_z_impl.h) (TEST INFRASTRUCTURE; see zml_oracle.h).
  *
  * Build with -O2 -ffp-contract=off: Zig does not contract a*b+c into an FMA,
@@ -41,8 +41,8 @@ static int zo_trans_invert(int t) {
 }
 
 /* lapack/ilaenv.zig:9-745, the entries this path reads: NB (ispec 1) = 64
- * for xGETRF and xPOTRF, 32 for xGEQRF; NBMIN (ispec 2) = 2; NX (ispec 3) =
- * 128 for xGEQRF. */
+ * for xGETRF, xPOTRF and xSYTRF, 32 for xGEQRF; NBMIN (ispec 2) = 8 for
+ * xSYTRF, else 2; NX (ispec 3) = 128 for xGEQRF. */
 int zo_ilaenv(int ispec, const char *name, int n1, int n2, int n3, int n4) {
   (void)n1; (void)n2; (void)n3; (void)n4;
   const char *c2 = name + 1, *c3 = name + 3;
@@ -51,9 +51,13 @@ int zo_ilaenv(int ispec, const char *name, int n1, int n2, int n3, int n4) {
     if (!strncmp(c2, "PO", 2) && !strncmp(c3, "TRF", 3)) return 64;
     if (!strncmp(c2, "GE", 2) && !strncmp(c3, "QRF", 3)) return 32;
     if (!strncmp(c2, "OR", 2) && !strncmp(c3, "GQR", 3)) return 32;
+    if (!strncmp(c2, "SY", 2) && !strncmp(c3, "TRF", 3)) return 64;
     return 1;
   }
-  if (ispec == 2) return 2;
+  if (ispec == 2) {
+    if (!strncmp(c2, "SY", 2) && !strncmp(c3, "TRF", 3)) return 8; /* ilaenv.zig:406-412 */
+    return 2;
+  }
   if (ispec == 3) {
     if (!strncmp(c2, "GE", 2) && !strncmp(c3, "QRF", 3)) return 128;
     if (!strncmp(c2, "OR", 2) && !strncmp(c3, "GQR", 3)) return 128;
@@ -76,6 +80,7 @@ int zo_ilaenv(int ispec, const char *name, int n1, int n2, int n3, int n4) {
 #define ZO_BITS 64
 #include "oracle_impl.h"
 #include "oracle_qr_impl.h"
+#include "oracle_sy_impl.h"
 #undef T
 #undef P
 #undef ZO_ABS
@@ -102,6 +107,7 @@ int zo_ilaenv(int ispec, const char *name, int n1, int n2, int n3, int n4) {
 #define ZO_BITS 32
 #include "oracle_impl.h"
 #include "oracle_qr_impl.h"
+#include "oracle_sy_impl.h"
 #undef T
 #undef P
 

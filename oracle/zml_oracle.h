@@ -75,7 +75,14 @@ void zo_set_trsm_as_written(int on);
   int P##geqrf(int order, int m, int n, T *a, int lda, T *tau, T *work, int lwork); \
   int P##org2r(int order, int m, int n, int k, T *a, int lda, const T *tau, T *work);        \
   int P##orgqr(int order, int m, int n, int k, T *a, int lda, const T *tau, T *work,          \
-               int lwork);
+               int lwork);                                                                    \
+  int P##syr(int order, int uplo, int n, T alpha, const T *x, int incx, T *a, int lda);       \
+  int P##gemmtr(int order, int uplo, int transa, int transb, int n, int k, T alpha,           \
+                const T *a, int lda, const T *b, int ldb, T beta, T *c, int ldc);             \
+  int P##sytf2(int order, int uplo, int n, T *a, int lda, int *ipiv);                         \
+  int P##lasyf(int order, int uplo, int n, int nb, int *kb, T *a, int lda, int *ipiv, T *w,   \
+               int ldw);                                                                      \
+  int P##sytrf(int order, int uplo, int n, T *a, int lda, int *ipiv, T *work, int lwork);
 
 ZO_DECL(double, zo_d_)
 ZO_DECL(float, zo_s_)

@@ -67,6 +67,11 @@ def load():
                 "org2r": (i32, [i32, i32, i32, i32, vp, i32, vp, vp]),
                 "larft": (i32, [i32, i32, i32, i32, i32, vp, i32, vp, vp, i32]),
                 "larfg": (i32, [i32, vp, vp, i32, vp]),
+                "syr": (i32, [i32, i32, i32, T, vp, i32, vp, i32]),
+                "gemmtr": (i32, [i32, i32, i32, i32, i32, i32, T, vp, i32, vp, i32, T, vp, i32]),
+                "sytf2": (i32, [i32, i32, i32, vp, i32, vp]),
+                "lasyf": (i32, [i32, i32, i32, i32, vp, vp, i32, vp, vp, i32]),
+                "sytrf": (i32, [i32, i32, i32, vp, i32, vp, vp, i32]),
             }
             for name, (res, args) in sig.items():
                 fn = getattr(_lib, pfx + name)
@@ -152,6 +157,20 @@ def potrs(l, b, uplo=122):
     r = fn("potrs", l.dtype)(102, uplo, n, nrhs, ptr(l), max(1, n), ptr(b), max(1, n))
     assert r == 0
     return b
+
+
+def sytrf(a, uplo=122, order=102):
+    """Bunch-Kaufman factorization of a copy of symmetric `a` (its `uplo`
+    triangle); returns (factor, ipiv, info) in LAPACK's dsytrf conventions."""
+    a = np.array(a, dtype=a.dtype, order="F" if order == 102 else "C", copy=True)
+    n = a.shape[0]
+    ipiv = np.zeros(n, dtype=np.int32)
+    f = fn("sytrf", a.dtype)
+    q = np.zeros(1, dtype=a.dtype)
+    assert f(order, uplo, n, ptr(a), max(1, n), ptr(ipiv), ptr(q), -1) == 0
+    work = np.zeros(max(1, int(q[0])), dtype=a.dtype)
+    info = f(order, uplo, n, ptr(a), max(1, n), ptr(ipiv), ptr(work), work.size)
+    return a, ipiv, info
 
 
 def geqrf(a):
