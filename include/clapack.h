@@ -61,6 +61,15 @@ int LAPACKE_dposv(int matrix_layout, char uplo, int n, int nrhs, double *a, int 
 int LAPACKE_sposv(int matrix_layout, char uplo, int n, int nrhs, float *a, int lda, float *b,
                   int ldb);
 
+/* replaces zml.linalg.lapack.sytrf (lapack.zig:4400-4409; kernel
+ * lapack/sytrf.zig:17, used by linalg/bunchkaufman.zig:180-726):
+ * Bunch-Kaufman A = U D U^T or L D L^T of the uplo triangle, D with 1x1 and
+ * 2x2 blocks; ipiv as LAPACK's dsytrf (k+1 for a 1x1 block with interchange
+ * row k, -(p+1) on both columns of a 2x2 block); info > 0: D(info,info) is
+ * zero (the first such column in the order the factorization runs). */
+int LAPACKE_dsytrf(int matrix_layout, char uplo, int n, double *a, int lda, int *ipiv);
+int LAPACKE_ssytrf(int matrix_layout, char uplo, int n, float *a, int lda, int *ipiv);
+
 /* ---- complex (zml's cfloat branches of the same routines) ---------------
  * Matrices are interleaved (re, im) pairs (LAPACKE's lapack_complex_double /
  * lapack_complex_float layout), passed as void pointers; trans 'N', 'T' or

@@ -1,0 +1,92 @@
+"""GPU parity for Bunch-Kaufman (LAPACKE_dsytrf / ssytrf) against the oracle.
+
+The GPU runs zml's unblocked pivoting step by step with every product and sum
+rounded on its own (no FMA), so its factors and ipiv are the oracle's sytf2
+bit for bit at every size; zml's sytrf switches to the blocked lasyf above
+64 columns, against which the pivots agree and the factors to rounding.
+"""
+import numpy as np
+import pytest
+import scipy.linalg.lapack as lap
+
+import oracle_lib as ol
+import zml_gb300 as zg
+from gpu_util import P
+
+pytestmark = pytest.mark.gpu
+
+
+def sym(n, seed, dtype=np.float64):
+    g = np.random.default_rng(seed).standard_normal((n, n))
+    return np.asfortranarray(((g + g.T) / 2).astype(dtype))
+
+
+def gpu_sytrf(a, uplo, layout=102):
+    n = a.shape[0]
+    buf = np.array(a, order="F" if layout == 102 else "C", copy=True)
+    ipiv = np.zeros(n, dtype=np.int32)
+    f = zg.lib().LAPACKE_dsytrf if a.dtype == np.float64 else zg.lib().LAPACKE_ssytrf
+    info = f(layout, uplo, n, P(buf), n, P(ipiv))
+    return buf, ipiv, info
+
+
+def oracle_sytf2(a, ul):
+    f = np.asfortranarray(a.copy())
+    ipiv = np.zeros(a.shape[0], dtype=np.int32)
+    info = ol.fn("sytf2", a.dtype)(102, ul, a.shape[0], ol.ptr(f), max(1, a.shape[0]), ol.ptr(ipiv))
+    return f, ipiv, info
+
+
+@pytest.mark.parametrize("uplo", [b"U", b"L"])
+@pytest.mark.parametrize("n", [1, 2, 5, 64, 65, 130])
+def test_dsytrf_bitwise_equals_oracle_sytf2(n, uplo):
+    a = sym(n, seed=n * 7 + uplo[0])
+    f, ipiv, info = gpu_sytrf(a, uplo)
+    ul = 121 if uplo == b"U" else 122
+    fr, ipr, infr = oracle_sytf2(a, ul)
+    assert info == infr == 0
+    np.testing.assert_array_equal(ipiv, ipr)
+    tri = np.triu if uplo == b"U" else np.tril
+    np.testing.assert_array_equal(tri(f), tri(fr))
+    np.testing.assert_array_equal(f - tri(f), a - tri(a))  # the other triangle untouched
+
+
+@pytest.mark.parametrize("uplo", [b"U", b"L"])
+def test_dsytrf_vs_blocked_oracle_and_lapack_solve(uplo):
+    n = 200
+    a = sym(n, seed=9)
+    f, ipiv, info = gpu_sytrf(a, uplo)
+    ul = 121 if uplo == b"U" else 122
+    fb, ipb, _ = ol.sytrf(a, ul)
+    np.testing.assert_array_equal(ipiv, ipb)
+    tri = np.triu if uplo == b"U" else np.tril
+    assert np.abs(tri(f) - tri(fb)).max() <= 1e-10 * np.abs(fb).max()
+    x = np.random.default_rng(1).standard_normal((n, 2))
+    sol, inf = lap.dsytrs(f, ipiv, a @ x, lower=int(uplo == b"L"))
+    assert inf == 0
+    np.testing.assert_allclose(sol, x, rtol=1e-8, atol=1e-8)
+
+
+def test_dsytrf_row_major_and_zero_column_info():
+    a = sym(80, seed=4)
+    fc, pc, _ = gpu_sytrf(a, b"L")
+    fr, pr, _ = gpu_sytrf(a, b"L", layout=101)
+    np.testing.assert_array_equal(pr, pc)
+    np.testing.assert_array_equal(np.tril(fr), np.tril(fc))
+    z = sym(30, seed=6)
+    z[11, :] = 0
+    z[:, 11] = 0
+    for uplo, ul in ((b"U", 121), (b"L", 122)):
+        _, ipiv, info = gpu_sytrf(z, uplo)
+        _, ipr, infr = oracle_sytf2(z, ul)
+        assert info == infr > 0
+        np.testing.assert_array_equal(ipiv, ipr)
+
+
+def test_ssytrf_bitwise_equals_oracle():
+    a = sym(90, seed=12, dtype=np.float32)
+    f, ipiv, info = gpu_sytrf(a, b"L")
+    fr, ipr, infr = oracle_sytf2(a, 122)
+    assert info == infr == 0
+    np.testing.assert_array_equal(ipiv, ipr)
+    np.testing.assert_array_equal(np.tril(f), np.tril(fr))

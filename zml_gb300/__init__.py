@@ -36,6 +36,7 @@ for p, T in (("d", f64), ("s", f32)):
         "LAPACKE_%spotrs" % p: (i32, [i32, ch, i32, i32, vp, i32, vp, i32]),
         "LAPACKE_%sposv" % p: (i32, [i32, ch, i32, i32, vp, i32, vp, i32]),
         "LAPACKE_%slaswp" % p: (i32, [i32, i32, vp, i32, i32, i32, vp, i32]),
+        "LAPACKE_%ssytrf" % p: (i32, [i32, ch, i32, vp, i32, vp]),
         "LAPACKE_%sgeqrf" % p: (i32, [i32, i32, i32, vp, i32, vp]),
         "LAPACKE_%sorgqr" % p: (i32, [i32, i32, i32, i32, vp, i32, vp]),
     })

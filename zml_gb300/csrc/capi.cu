@@ -623,6 +623,29 @@ int zposv_any(int layout, char uplo, int n, int nrhs, R *a, int lda, R *b, int l
   return info;
 }
 
+// Bunch-Kaufman (LAPACKE_dsytrf / ssytrf, called from lapack.zig:4400-4409):
+// the uplo triangle of the symmetric n x n matrix is overwritten with the
+// block-diagonal D and the multipliers; ipiv as LAPACK's dsytrf.
+template <typename T> int sytrf_any(int layout, char uplo, int n, T *a, int lda, int *ipiv) {
+  if (!lay_ok(layout)) return -1;
+  uplo = up(uplo);
+  if (uplo != 'U' && uplo != 'L') return -2;
+  if (n < 0) return -3;
+  if (lda < std::max(1, n)) return -5;
+  if (n == 0) return 0;
+  cudaStream_t s = lib_stream();
+  ColMajor<T> A;
+  Buf<int> P;
+  ZG_TRY(A.in(layout, a, lda, n, n, kSlotA, kSlotAT, true, s));
+  ZG_TRY(P.in(ipiv, n, kSlotPiv, false, s));
+  int info = 0;
+  ZG_TRY(sytrf_dev<T>(uplo == 'U' ? kUpper : kLower, n, A.d, A.ld, P.d, &info, s));
+  ZG_TRY(A.out(s));
+  ZG_TRY(P.out(s));
+  ZG_TRY(sync(s));
+  return info;
+}
+
 template <typename T> int geqrf_any(int layout, int m, int n, T *a, int lda, T *tau) {
   if (!lay_ok(layout)) return -1;
   if (m < 0) return -2;
@@ -820,6 +843,12 @@ CBLAS_ZGEMM(c, float)
                         int ldb) {                                                               \
     return zposv_any<R>(layout, uplo, n, nrhs, (R *)a, lda, (R *)b, ldb);                        \
   }
+int LAPACKE_dsytrf(int layout, char uplo, int n, double *a, int lda, int *ipiv) {
+  return sytrf_any<double>(layout, uplo, n, a, lda, ipiv);
+}
+int LAPACKE_ssytrf(int layout, char uplo, int n, float *a, int lda, int *ipiv) {
+  return sytrf_any<float>(layout, uplo, n, a, lda, ipiv);
+}
 ZLAPACK_FNS(z, double)
 ZLAPACK_FNS(c, float)
 #undef ZLAPACK_FNS

@@ -101,6 +101,7 @@ enum Slot : int {
   kSlotZOpB = 22,             // complex GEMM: op(B) materialized
   kSlotZTmp = 23,             // complex herk / syrk: the full product
   kSlotZTr = 24,              // complex trsm: the transposed right-hand side (right side)
+  kSlotSytrf = 25,            // Bunch-Kaufman: the step's block size read back by the host
   kNumSlots = 28
 };
 

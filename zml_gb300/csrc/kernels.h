@@ -52,6 +52,10 @@ template <typename R> int zpotrf_dev(int uplo, int n, R *A, long lda, int *info,
 template <typename R>
 int zpotrs_dev(int uplo, int n, int nrhs, const R *A, long lda, R *B, long ldb, cudaStream_t s);
 
+// sytrf.cu -- Bunch-Kaufman A = U D U^T / L D L^T (LAPACK ipiv and info).
+template <typename T>
+int sytrf_dev(int uplo, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s);
+
 // qr.cu -- Householder QR (geqrf) with the T factor of each panel.
 template <typename T> int geqrf_dev(int m, int n, T *A, long lda, T *tau, cudaStream_t s);
 // The first n columns of Q from geqrf's reflectors (k of them) stored in A.

@@ -1,0 +1,315 @@
+// sytrf.cu -- Bunch-Kaufman symmetric-indefinite factorization on the GPU:
+// A = U D U^T or L D L^T with 1x1 and 2x2 pivot blocks (LAPACK's dsytf2
+// pivoting, as zml restates it in lapack/sytf2.zig:13-522).
+//
+// One step per pivot block, driven by the host: a single-CTA kernel finds
+// the pivot (|a_kk|, the column maximum, and when needed the maximum of row
+// imax, with zml's iamax semantics: the first maximum wins, a NaN never
+// displaces it, a NaN at the first position blocks the search), decides the
+// 1x1 / 2x2 block, performs the symmetric interchange and writes ipiv / info;
+// the host reads the block size back (one 8-byte copy) and launches the
+// update of the remaining triangle.  Every product and sum of the update is
+// rounded on its own (__dmul_rn / __dadd_rn; the compiler may not contract
+// them into an FMA), in the association sytf2.zig writes, so the result is
+// the restated unblocked algorithm's, bit for bit.  zml's sytrf factors
+// matrices above nb = 64 columns with the blocked lasyf, whose sums are
+// grouped differently; against it the factors agree to rounding.
+#include <climits>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace zg {
+
+template <typename T> struct Rn;
+template <> struct Rn<double> {
+  static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+  static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+  static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+  static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+};
+template <> struct Rn<float> {
+  static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+  static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+  static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+  static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+};
+
+// the C macro max of the restatement: (a) > (b) ? (a) : (b)
+template <typename T> __device__ __forceinline__ T cmax(T a, T b) { return a > b ? a : b; }
+
+// zml's iamax over len values v(t), t = 0 .. len-1, by the whole CTA:
+// first maximum of |v|, NaN never chosen, a NaN first blocks (index 0).
+template <typename T, typename F>
+__device__ int cta_iamax(int len, F v, T *sv, int *si) {
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  T best = T(-1);
+  int bi = INT_MAX;
+  for (int q = t; q < len; q += blockDim.x) {
+    const T a = fabs(v(q));
+    if (a > best) {
+      best = a;
+      bi = q;
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    const T ov = __shfl_down_sync(0xffffffffu, best, off);
+    const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+    if (ov > best || (ov == best && oi < bi)) {
+      best = ov;
+      bi = oi;
+    }
+  }
+  __syncthreads();
+  if (lane == 0) {
+    sv[w] = best;
+    si[w] = bi;
+  }
+  __syncthreads();
+  if (t == 0) {
+    for (int q = 1; q < (int)(blockDim.x >> 5); ++q)
+      if (sv[q] > best || (sv[q] == best && si[q] < bi)) {
+        best = sv[q];
+        bi = si[q];
+      }
+    const T a0 = len > 0 ? fabs(v(0)) : T(0);
+    si[0] = (len <= 0 || a0 != a0 || bi == INT_MAX) ? 0 : bi;
+  }
+  __syncthreads();
+  const int r = si[0];
+  __syncthreads();
+  return r;
+}
+
+// info: the first zero pivot column in the order the steps run (the upper
+// factorization runs from the last column down), as sytf2.zig:67-68 sets it.
+__device__ __forceinline__ void record_first(int *info, int v) { atomicCAS(info, 0, v); }
+
+// Step k (sytf2.zig:30-296 upper, 297-515 lower): pivot choice, interchange,
+// ipiv, info.  out[0] = kstep, out[1] = 1 when the column is zero (or its
+// diagonal NaN) and the step makes no update.
+template <typename T>
+__global__ void __launch_bounds__(1024) sytf2_pivot_kernel(int n, T *A, long lda, bool upper,
+                                                           int k, T alpha, int *ipiv, int *out,
+                                                           int *info) {
+  __shared__ T sv[32];
+  __shared__ int si[32];
+  auto a = [&](int i, int j) -> T & { return A[i + (long)j * lda]; };
+  const T absakk = fabs(a(k, k));
+  int imax = 0;
+  T colmax = T(0);
+  if (upper) {
+    if (k > 0) {
+      imax = cta_iamax<T>(k, [&](int q) { return a(q, k); }, sv, si);
+      colmax = fabs(a(imax, k));
+    }
+  } else if (k < n - 1) {
+    imax = k + 1 + cta_iamax<T>(n - k - 1, [&](int q) { return a(k + 1 + q, k); }, sv, si);
+    colmax = fabs(a(imax, k));
+  }
+  int kp = k, kstep = 1, skip = 0;
+  if (cmax(absakk, colmax) == T(0) || absakk != absakk) {
+    skip = 1;
+  } else if (!(absakk >= Rn<T>::mul(alpha, colmax))) {
+    T rowmax;
+    if (upper) {
+      int jmax = imax + 1 + cta_iamax<T>(k - imax, [&](int q) { return a(imax, imax + 1 + q); }, sv, si);
+      rowmax = fabs(a(imax, jmax));
+      if (imax > 0) {
+        jmax = cta_iamax<T>(imax, [&](int q) { return a(q, imax); }, sv, si);
+        rowmax = cmax(rowmax, fabs(a(jmax, imax)));
+      }
+    } else {
+      int jmax = k + cta_iamax<T>(imax - k, [&](int q) { return a(imax, k + q); }, sv, si);
+      rowmax = fabs(a(imax, jmax));
+      if (imax < n - 1) {
+        jmax = imax + 1 + cta_iamax<T>(n - imax - 1, [&](int q) { return a(imax + 1 + q, imax); }, sv, si);
+        rowmax = cmax(rowmax, fabs(a(jmax, imax)));
+      }
+    }
+    if (absakk >= Rn<T>::mul(alpha, Rn<T>::mul(colmax, Rn<T>::div(colmax, rowmax)))) {
+      kp = k;
+    } else if (fabs(a(imax, imax)) >= Rn<T>::mul(alpha, rowmax)) {
+      kp = imax;
+    } else {
+      kp = imax;
+      kstep = 2;
+    }
+  }
+  const int t = threadIdx.x;
+  __syncthreads();  // every thread has read what the decision needs
+  if (!skip) {
+    const int kk = upper ? k - kstep + 1 : k + kstep - 1;
+    if (kp != kk) {  // the interchange: disjoint pairs, all at once
+      if (upper) {
+        for (int i = t; i < kp; i += blockDim.x) {  // columns kk and kp above row kp
+          const T x = a(i, kk);
+          a(i, kk) = a(i, kp);
+          a(i, kp) = x;
+        }
+        for (int q = t; q < kk - kp - 1; q += blockDim.x) {  // column kk below kp <-> row kp
+          const T x = a(kp + 1 + q, kk);
+          a(kp + 1 + q, kk) = a(kp, kp + 1 + q);
+          a(kp, kp + 1 + q) = x;
+        }
+      } else {
+        for (int q = t; q < n - kp - 1; q += blockDim.x) {  // columns kk and kp below row kp
+          const T x = a(kp + 1 + q, kk);
+          a(kp + 1 + q, kk) = a(kp + 1 + q, kp);
+          a(kp + 1 + q, kp) = x;
+        }
+        for (int q = t; q < kp - kk - 1; q += blockDim.x) {  // column kk below kk <-> row kp
+          const T x = a(kk + 1 + q, kk);
+          a(kk + 1 + q, kk) = a(kp, kk + 1 + q);
+          a(kp, kk + 1 + q) = x;
+        }
+      }
+      if (t == 0) {
+        T x = a(kk, kk);
+        a(kk, kk) = a(kp, kp);
+        a(kp, kp) = x;
+        if (kstep == 2) {
+          const int r = upper ? k - 1 : k + 1;
+          x = a(r, k);
+          a(r, k) = a(kp, k);
+          a(kp, k) = x;
+        }
+      }
+    }
+  }
+  if (t == 0) {
+    if (skip) record_first(info, k + 1);
+    if (kstep == 1) {
+      ipiv[k] = kp + 1;
+    } else {
+      ipiv[k] = -(kp + 1);
+      ipiv[upper ? k - 1 : k + 1] = -(kp + 1);
+    }
+    out[0] = kstep;
+    out[1] = skip;
+  }
+}
+
+// The update of step k.  1x1 (sytf2.zig:158-180 / 404-426): syr with
+// alpha = -1/d on the triangle still to factor, a_ij += x_i (x_j (-1/d)),
+// column j skipped where x_j == 0 (syr.zig:62, 142).  2x2 (185-236 /
+// 430-482): the multipliers of column j from the original columns k, k-1
+// (upper) or k, k+1 (lower), then a_ij -= a_ik wk + a_ik' wk'.  The columns
+// of the block are rewritten afterwards by sytf2_store_kernel.
+template <typename T>
+__global__ void __launch_bounds__(256) sytf2_update_kernel(int n, T *A, long lda, bool upper,
+                                                           int k, int kstep) {
+  auto a = [&](int i, int j) -> T & { return A[i + (long)j * lda]; };
+  // the triangle to update: upper rows/cols [0, m), lower [k + kstep, n)
+  const int m = upper ? k - kstep + 1 : n - k - kstep;
+  const int o = upper ? 0 : k + kstep;
+  const long tot = (long)m * m;
+  if (kstep == 1) {
+    const T r1 = T(1) / a(k, k);
+    const T nr1 = -r1;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < tot;
+         e += (long)gridDim.x * blockDim.x) {
+      const int i = o + (int)(e % m), j = o + (int)(e / m);
+      if (upper ? i > j : i < j) continue;
+      const T xj = a(j, k);
+      if (xj == T(0)) continue;
+      const T temp = Rn<T>::mul(xj, nr1);
+      a(i, j) = Rn<T>::add(a(i, j), Rn<T>::mul(a(i, k), temp));
+    }
+  } else {
+    const int k2 = upper ? k - 1 : k + 1;  // the block's other column
+    T d = a(k2, k);  // d12 (upper) / d21 (lower)
+    const T dkk = Rn<T>::div(a(k2, k2), d);  // d22 (upper) / d11 (lower)
+    const T dk = Rn<T>::div(a(k, k), d);     // d11 (upper) / d22 (lower)
+    const T t = T(1) / Rn<T>::sub(Rn<T>::mul(upper ? dk : dkk, upper ? dkk : dk), T(1));
+    d = Rn<T>::div(t, d);
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < tot;
+         e += (long)gridDim.x * blockDim.x) {
+      const int i = o + (int)(e % m), j = o + (int)(e / m);
+      if (upper ? i > j : i < j) continue;
+      T wk, wo;  // the multipliers of columns k and k2 in column j
+      if (upper) {  // wkm1 = d12 (d11 a_j,k-1 - a_jk), wk = d12 (d22 a_jk - a_j,k-1)
+        wo = Rn<T>::mul(d, Rn<T>::sub(Rn<T>::mul(dk, a(j, k2)), a(j, k)));
+        wk = Rn<T>::mul(d, Rn<T>::sub(Rn<T>::mul(dkk, a(j, k)), a(j, k2)));
+      } else {  // wk = d21 (d11 a_jk - a_j,k+1), wkp1 = d21 (d22 a_j,k+1 - a_jk)
+        wk = Rn<T>::mul(d, Rn<T>::sub(Rn<T>::mul(dkk, a(j, k)), a(j, k2)));
+        wo = Rn<T>::mul(d, Rn<T>::sub(Rn<T>::mul(dk, a(j, k2)), a(j, k)));
+      }
+      a(i, j) = Rn<T>::sub(a(i, j), Rn<T>::add(Rn<T>::mul(a(i, k), wk), Rn<T>::mul(a(i, k2), wo)));
+    }
+  }
+}
+
+// The block's columns after the update: x / d (1x1) or the multipliers (2x2).
+template <typename T>
+__global__ void __launch_bounds__(256) sytf2_store_kernel(int n, T *A, long lda, bool upper, int k,
+                                                          int kstep) {
+  auto a = [&](int i, int j) -> T & { return A[i + (long)j * lda]; };
+  const int m = upper ? k - kstep + 1 : n - k - kstep;
+  const int o = upper ? 0 : k + kstep;
+  const int j0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (kstep == 1) {
+    const T r1 = T(1) / a(k, k);
+    for (int j = j0; j < m; j += gridDim.x * blockDim.x) a(o + j, k) = Rn<T>::mul(a(o + j, k), r1);
+    return;
+  }
+  const int k2 = upper ? k - 1 : k + 1;
+  T d = a(k2, k);
+  const T dkk = Rn<T>::div(a(k2, k2), d), dk = Rn<T>::div(a(k, k), d);
+  const T t = T(1) / Rn<T>::sub(Rn<T>::mul(upper ? dk : dkk, upper ? dkk : dk), T(1));
+  d = Rn<T>::div(t, d);
+  for (int q = j0; q < m; q += gridDim.x * blockDim.x) {
+    const int j = o + q;
+    T wk, wo;
+    if (upper) {
+      wo = Rn<T>::mul(d, Rn<T>::sub(Rn<T>::mul(dk, a(j, k2)), a(j, k)));
+      wk = Rn<T>::mul(d, Rn<T>::sub(Rn<T>::mul(dkk, a(j, k)), a(j, k2)));
+    } else {
+      wk = Rn<T>::mul(d, Rn<T>::sub(Rn<T>::mul(dkk, a(j, k)), a(j, k2)));
+      wo = Rn<T>::mul(d, Rn<T>::sub(Rn<T>::mul(dk, a(j, k2)), a(j, k)));
+    }
+    a(j, k) = wk;
+    a(j, k2) = wo;
+  }
+}
+
+template <typename T>
+int sytrf_dev(int uplo, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s) {
+  *info = 0;
+  if (n <= 0) return 0;
+  Control *ctl;
+  ZG_TRY(control(s, &ctl));
+  void *w;
+  ZG_TRY(workspace(s, kSlotSytrf, sizeof(int) * 2, &w));
+  int *out = (int *)w;
+  DeviceInfo di;
+  ZG_TRY(device_info(&di));
+  const bool upper = uplo == kUpper;
+  const T alpha = (T(1) + std::sqrt(T(17))) / T(8);
+  int k = upper ? n - 1 : 0;
+  int hout[2];
+  while (upper ? k >= 0 : k < n) {
+    ZG_LAUNCH(kTagPanel, 0, 0, s,
+              (sytf2_pivot_kernel<T><<<1, 1024, 0, s>>>(n, A, lda, upper, k, alpha, ipiv, out,
+                                                        &ctl->info)));
+    ZG_CUDA(cudaMemcpyAsync(hout, out, sizeof(hout), cudaMemcpyDeviceToHost, s));
+    ZG_CUDA(cudaStreamSynchronize(s));
+    const int kstep = hout[0];
+    const int m = upper ? k - kstep + 1 : n - k - kstep;
+    if (!hout[1] && m > 0) {
+      const long tot = (long)m * m;
+      const int grid = (int)std::max(1L, std::min((tot + 255) / 256, (long)di.num_sms * 8));
+      ZG_LAUNCH(kTagPotf2, 1.0 * tot, 24.0 * tot / 2, s,
+                (sytf2_update_kernel<T><<<grid, 256, 0, s>>>(n, A, lda, upper, k, kstep)));
+      ZG_LAUNCH(kTagPotf2, 0, 0, s,
+                (sytf2_store_kernel<T><<<ceil_div(m, 256), 256, 0, s>>>(n, A, lda, upper, k, kstep)));
+    }
+    k = upper ? k - kstep : k + kstep;
+  }
+  return check_status(s, ctl, info);
+}
+
+template int sytrf_dev<double>(int, int, double *, long, int *, int *, cudaStream_t);
+template int sytrf_dev<float>(int, int, float *, long, int *, int *, cudaStream_t);
+
+}  // namespace zg
