@@ -943,3 +943,270 @@ int ZP(posv)(int order, int uplo, int n, int nrhs, ZT *a, int lda, ZT *b, int ld
 #undef ZA_
 #undef ZB_
 #undef ZC_
+
+/* ---- complex Householder QR (geqrf and the branches it takes) ------------- */
+
+/* blas/copy.zig and lapack/lacgv.zig (element-type generic) */
+static int ZP(copy)(int n, const ZT *x, int incx, ZT *y, int incy) {
+  long ix = incx < 0 ? (long)(-n + 1) * incx : 0, iy = incy < 0 ? (long)(-n + 1) * incy : 0;
+  for (int i = 0; i < n; ++i, ix += incx, iy += incy) y[iy] = x[ix];
+  return 0;
+}
+static void ZP(lacgv)(int n, ZT *x, int incx) {
+  long ix = incx < 0 ? (long)(-n + 1) * incx : 0;
+  for (int i = 0; i < n; ++i, ix += incx) x[ix].im = -x[ix].im;
+}
+
+/* blas/nrm2.zig:60-134 (cfloat branch): Blue's scaled sum of squares as in
+ * the real branch, every element contributing its re and then its im part. */
+R ZP(nrm2)(int n, const ZT *x, int incx) {
+  if (n < 0) return (R)-1;
+  if (n == 0) return 0;
+  const R huge = ZR_TMAX;
+  const R tsml = (R)ldexp(1.0, (int)ceil((ZR_EMIN - 1) * 0.5));
+  const R tbig = (R)ldexp(1.0, (int)floor((ZR_EMAX - ZR_BITS + 1) * 0.5));
+  const R ssml = (R)ldexp(1.0, -(int)floor((ZR_EMIN - ZR_BITS) * 0.5));
+  const R sbig = (R)ldexp(1.0, -(int)ceil((ZR_EMAX + ZR_BITS - 1) * 0.5));
+  R scl = 1, sumsq = 0, abig = 0, amed = 0, asml = 0;
+  int notbig = 1;
+  long ix = incx < 0 ? (long)(-n + 1) * incx : 0;
+  for (int i = 0; i < n; ++i) {
+    for (int part = 0; part < 2; ++part) {
+      const R ax = ZO_ABS(part == 0 ? x[ix].re : x[ix].im);
+      if (ax > tbig) {
+        abig += (ax * sbig) * (ax * sbig);
+        notbig = 0;
+      } else if (ax < tsml) {
+        if (notbig) asml += (ax * ssml) * (ax * ssml);
+      } else {
+        amed += ax * ax;
+      }
+    }
+    ix += incx;
+  }
+  if (abig > 0) {
+    if (amed > 0 || amed > huge || amed != amed) abig += (amed * sbig) * (amed * sbig);
+    scl = (R)1 / sbig;
+    sumsq = abig;
+  } else if (asml > 0) {
+    if (amed > 0 || amed > huge || amed != amed) {
+      const R sqrt_amed = ZO_SQRT(amed);
+      const R sqrt_asml = ZO_SQRT(asml) / ssml;
+      const R ymin = sqrt_asml > sqrt_amed ? sqrt_amed : sqrt_asml;
+      const R ymax = sqrt_asml > sqrt_amed ? sqrt_asml : sqrt_amed;
+      scl = 1;
+      sumsq = (ymax * ymax) * ((R)1 + (ymin / ymax) * (ymin / ymax));
+    } else {
+      scl = (R)1 / ssml;
+      sumsq = asml;
+    }
+  } else {
+    scl = 1;
+    sumsq = amed;
+  }
+  return scl * ZO_SQRT(sumsq);
+}
+
+/* lapack/larfg.zig:17-170 (complex): H^H (alpha; x) = (beta; 0) with beta
+ * real; tau = (beta - alpha) / beta; x scaled by 1 / (alpha - beta), the
+ * real-by-complex quotient of crdiv (larfg.zig:130-137 reaches it as
+ * div(1, alpha - beta)); H = I when x = 0 and alpha is real. */
+int ZP(larfg)(int n, ZT *alpha, ZT *x, int incx, ZT *tau) {
+  if (n <= 0) {
+    *tau = ZP(zero);
+    return 0;
+  }
+  R xnorm = ZP(nrm2)(n - 1, x, incx);
+  if (xnorm == (R)0 && alpha->im == (R)0) {
+    *tau = ZP(zero);
+    return 0;
+  }
+  R beta = -ZCOPYSIGN(ZLAPY3(alpha->re, alpha->im, xnorm), alpha->re);
+  const R safmin = ZLAMCH('s') / ZLAMCH('e');
+  const R rsafmn = (R)1 / safmin;
+  int knt = 0;
+  if (ZO_ABS(beta) < safmin) {
+    while (ZO_ABS(beta) < safmin && knt < 20) {
+      ZP(scal)(n - 1, ZP(c)(rsafmn, (R)0), x, incx);
+      beta = beta * rsafmn;
+      *alpha = ZP(cscale)(*alpha, rsafmn);
+      ++knt;
+    }
+    xnorm = ZP(nrm2)(n - 1, x, incx);
+    beta = -ZCOPYSIGN(ZLAPY3(alpha->re, alpha->im, xnorm), alpha->re);
+  }
+  *tau = ZP(c)((-alpha->re + beta) / beta, (-alpha->im) / beta);
+  *alpha = ZP(crdiv)((R)1, ZP(c)(alpha->re - beta, alpha->im));
+  ZP(scal)(n - 1, *alpha, x, incx);
+  for (int j = 0; j < knt; ++j) beta = beta * safmin;
+  *alpha = ZP(c)(beta, (R)0);
+  return 0;
+}
+
+/* lapack/ilalc.zig: the last non-zero column (1-based count), 0 if none */
+static int ZP(ilalc)(int order, int m, int n, const ZT *a, int lda) {
+  if (n == 0) return 0;
+  if (!ZP(cis0)(a[zo_index(order, 0, n - 1, lda)]) ||
+      !ZP(cis0)(a[zo_index(order, m - 1, n - 1, lda)]))
+    return n;
+  for (int j = n - 1; j >= 0; --j)
+    for (int i = 0; i < m; ++i)
+      if (!ZP(cis0)(a[zo_index(order, i, j, lda)])) return j + 1;
+  return 0;
+}
+
+/* lapack/larf1f.zig:17-259, side left (the only side geqr2 takes):
+ * C <- (I - tau v v^H) C with v(0) = 1 implied: w = C(1:,:)^H v(1:) +
+ * conj(C(0,:)), C(0,:) -= tau conj(w), C(1:,:) -= tau v(1:) w^H (gerc). */
+int ZP(larf1f)(int order, int side, int m, int n, const ZT *v, int incv, ZT tau, ZT *c, int ldc,
+               ZT *work) {
+  if (side != ZO_LEFT) return ZO_EINVAL; /* not on this path */
+  int lastv = 1, lastc = 0;
+  if (!ZP(cis0)(tau)) {
+    lastv = m;
+    long i = incv > 0 ? (long)(lastv - 1) * incv : 0;
+    while (lastv > 1 && ZP(cis0)(v[i])) {
+      lastv -= 1;
+      i -= incv;
+    }
+    lastc = ZP(ilalc)(order, lastv, n, c, ldc);
+  }
+  if (lastc == 0) return 0;
+  const int rld = order == ZO_COL ? ldc : 1;
+  if (lastv == 1) {
+    ZP(scal)(lastc, ZP(c)(-tau.re + (R)1, -tau.im), c, rld);
+    return 0;
+  }
+  ZP(gemv)(order, ZO_CONJTRANS, lastv - 1, lastc, ZP(one), c + zo_index(order, 1, 0, ldc), ldc,
+           v + incv, incv, ZP(zero), work, 1);
+  for (int i = 0; i < lastc; ++i)
+    work[i] = ZP(cadd)(work[i], ZP(cconj)(c[zo_index(order, 0, i, ldc)]));
+  for (int i = 0; i < lastc; ++i)
+    c[zo_index(order, 0, i, ldc)] =
+        ZP(csub)(c[zo_index(order, 0, i, ldc)], ZP(cmul)(tau, ZP(cconj)(work[i])));
+  ZP(gerc)(order, lastv - 1, lastc, ZP(c)(-tau.re, -tau.im), v + incv, incv, work, 1,
+           c + zo_index(order, 1, 0, ldc), ldc);
+  return 0;
+}
+
+/* lapack/geqr2.zig:17-59: H(i) from larfg, applied as H(i)^H (conj(tau)). */
+int ZP(geqr2)(int order, int m, int n, ZT *a, int lda, ZT *tau, ZT *work) {
+  if (m < 0 || n < 0 || lda < ZO_MAX(1, order == ZO_COL ? m : n)) return ZO_EINVAL;
+  const int cld = order == ZO_COL ? 1 : lda;
+  for (int i = 0; i < ZO_MIN(m, n); ++i) {
+    ZP(larfg)(m - i, &a[zo_index(order, i, i, lda)], a + zo_index(order, ZO_MIN(i + 1, m - 1), i, lda),
+              cld, &tau[i]);
+    if (i < n - 1)
+      ZP(larf1f)(order, ZO_LEFT, m - i, n - i - 1, a + zo_index(order, i, i, lda), cld,
+                 ZP(cconj)(tau[i]), a + zo_index(order, i, i + 1, lda), lda, work);
+  }
+  return 0;
+}
+
+/* lapack/larft.zig:18-231, the QR branch (forward, columnwise): the
+ * recursive T factor, V's entries copied conjugated (larft.zig:104-112). */
+int ZP(larft)(int order, int direct, int storev, int n, int k, const ZT *v, int ldv,
+              const ZT *tau, ZT *t, int ldt) {
+  if (n == 0 || k == 0) return 0;
+  if (n == 1 || k == 1) {
+    t[zo_index(order, 0, 0, ldt)] = tau[0];
+    return 0;
+  }
+  if (!(direct == 'F' && storev == 'C')) return ZO_EINVAL; /* not on this path */
+  const int l = k / 2;
+  ZP(larft)(order, direct, storev, n, l, v, ldv, tau, t, ldt);
+  ZP(larft)(order, direct, storev, n - l, k - l, v + zo_index(order, l, l, ldv), ldv, tau + l,
+            t + zo_index(order, l, l, ldt), ldt);
+  for (int j = 0; j < l; ++j)
+    for (int i = 0; i < k - l; ++i)
+      t[zo_index(order, j, l + i, ldt)] = ZP(cconj)(v[zo_index(order, l + i, j, ldv)]);
+  ZP(trmm)(order, ZO_RIGHT, ZO_LOWER, ZO_NOTRANS, ZO_UNIT, l, k - l, ZP(one),
+           v + zo_index(order, l, l, ldv), ldv, t + zo_index(order, 0, l, ldt), ldt);
+  ZP(gemm)(order, ZO_CONJTRANS, ZO_NOTRANS, l, k - l, n - k, ZP(one),
+           v + zo_index(order, k, 0, ldv), ldv, v + zo_index(order, k, l, ldv), ldv, ZP(one),
+           t + zo_index(order, 0, l, ldt), ldt);
+  ZP(trmm)(order, ZO_LEFT, ZO_UPPER, ZO_NOTRANS, ZO_NONUNIT, l, k - l, ZP(mone), t, ldt,
+           t + zo_index(order, 0, l, ldt), ldt);
+  ZP(trmm)(order, ZO_RIGHT, ZO_UPPER, ZO_NOTRANS, ZO_NONUNIT, l, k - l, ZP(one),
+           t + zo_index(order, l, l, ldt), ldt, t + zo_index(order, 0, l, ldt), ldt);
+  return 0;
+}
+
+/* lapack/larfb.zig:20-178, side left / forward / columnwise: W := C1^H
+ * (copy, lacgv), the T factor applied with trans.reverse(), C1 -= W^H. */
+int ZP(larfb)(int order, int side, int trans, int direct, int storev, int m, int n, int k,
+              const ZT *v, int ldv, const ZT *t, int ldt, ZT *c, int ldc, ZT *work, int ldwork) {
+  if (m <= 0 || n <= 0) return 0;
+  if (!(storev == 'C' && direct == 'F' && side == ZO_LEFT)) return ZO_EINVAL; /* not on path */
+  const int rldc = order == ZO_COL ? ldc : 1;
+  const int cldw = order == ZO_COL ? 1 : ldwork;
+  const int rtrans = trans == ZO_NOTRANS ? ZO_CONJTRANS
+                   : trans == ZO_TRANS ? ZO_CONJNOTRANS
+                   : trans == ZO_CONJNOTRANS ? ZO_TRANS : ZO_NOTRANS; /* linalg.zig:121-128 */
+  for (int j = 0; j < k; ++j) {
+    ZP(copy)(n, c + zo_index(order, j, 0, ldc), rldc, work + zo_index(order, 0, j, ldwork), cldw);
+    ZP(lacgv)(n, work + zo_index(order, 0, j, ldwork), cldw);
+  }
+  ZP(trmm)(order, ZO_RIGHT, ZO_LOWER, ZO_NOTRANS, ZO_UNIT, n, k, ZP(one), v, ldv, work, ldwork);
+  if (m > k)
+    ZP(gemm)(order, ZO_CONJTRANS, ZO_NOTRANS, n, k, m - k, ZP(one), c + zo_index(order, k, 0, ldc),
+             ldc, v + zo_index(order, k, 0, ldv), ldv, ZP(one), work, ldwork);
+  ZP(trmm)(order, ZO_RIGHT, ZO_UPPER, rtrans, ZO_NONUNIT, n, k, ZP(one), t, ldt, work, ldwork);
+  if (m > k)
+    ZP(gemm)(order, ZO_NOTRANS, ZO_CONJTRANS, m - k, n, k, ZP(mone), v + zo_index(order, k, 0, ldv),
+             ldv, work, ldwork, ZP(one), c + zo_index(order, k, 0, ldc), ldc);
+  ZP(trmm)(order, ZO_RIGHT, ZO_LOWER, ZO_CONJTRANS, ZO_UNIT, n, k, ZP(one), v, ldv, work, ldwork);
+  for (int j = 0; j < k; ++j)
+    for (int i = 0; i < n; ++i)
+      c[zo_index(order, j, i, ldc)] =
+          ZP(csub)(c[zo_index(order, j, i, ldc)], ZP(cconj)(work[zo_index(order, i, j, ldwork)]));
+  return 0;
+}
+
+/* lapack/geqrf.zig:18-157 (cfloat): blocked Householder QR, nb = 32,
+ * nx = 128, the block reflector applied as H^H (conj_trans, :116). */
+int ZP(geqrf)(int order, int m, int n, ZT *a, int lda, ZT *tau, ZT *work, int lwork) {
+  if (m < 0 || n < 0 || lda < ZO_MAX(1, order == ZO_COL ? m : n) ||
+      (lwork != -1 && (lwork < 1 || (m > 0 && lwork < ZO_MAX(1, n)))))
+    return ZO_EINVAL;
+  const int k = ZO_MIN(m, n);
+  int nb = zo_ilaenv(1, "DGEQRF", m, n, -1, -1);
+  if (lwork == -1) {
+    work[0] = ZP(c)((R)(k == 0 ? 1 : n * nb), (R)0);
+    return 0;
+  }
+  if (k == 0) {
+    work[0] = ZP(one);
+    return 0;
+  }
+  int nbmin = 2, nx = 0, iws = n, ldwork = 0;
+  if (nb > 1 && nb < k) {
+    nx = ZO_MAX(0, zo_ilaenv(3, "DGEQRF", m, n, -1, -1));
+    if (nx < k) {
+      ldwork = order == ZO_COL ? n : nb;
+      iws = ldwork * nb;
+      if (lwork < iws) {
+        nb = lwork / ldwork;
+        nbmin = ZO_MAX(2, zo_ilaenv(2, "DGEQRF", m, n, -1, -1));
+      }
+    }
+  }
+  int i = 0;
+  if (nb >= nbmin && nb < k && nx < k) {
+    for (; i < k - nx; i += nb) {
+      const int ib = ZO_MIN(k - i, nb);
+      ZP(geqr2)(order, m - i, ib, a + zo_index(order, i, i, lda), lda, tau + i, work);
+      if (i + ib < n) {
+        ZP(larft)(order, 'F', 'C', m - i, ib, a + zo_index(order, i, i, lda), lda, tau + i, work,
+                  ldwork);
+        ZP(larfb)(order, ZO_LEFT, ZO_CONJTRANS, 'F', 'C', m - i, n - i - ib, ib,
+                  a + zo_index(order, i, i, lda), lda, work, ldwork,
+                  a + zo_index(order, i, i + ib, lda), lda, work + zo_index(order, ib, 0, ldwork),
+                  ldwork);
+      }
+    }
+  }
+  if (i < k) ZP(geqr2)(order, m - i, n - i, a + zo_index(order, i, i, lda), lda, tau + i, work);
+  work[0] = ZP(c)((R)iws, (R)0);
+  return 0;
+}

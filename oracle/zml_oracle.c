@@ -136,6 +136,13 @@ static inline long zo_index(int order, int i, int j, int ld) {
 #define ZFMA fma
 #define ZO_ABS fabs
 #define ZO_SQRT sqrt
+#define ZLAPY3 zo_d_lapy3
+#define ZLAMCH zo_d_lamch
+#define ZCOPYSIGN copysign
+#define ZR_TMAX DBL_MAX
+#define ZR_EMIN (-1022)
+#define ZR_EMAX 1023
+#define ZR_BITS 64
 static inline double zo_z_lamch_s(void) { return zo_d_lamch('s'); }
 #include "oracle_z_impl.h"
 #undef R
@@ -144,6 +151,13 @@ static inline double zo_z_lamch_s(void) { return zo_d_lamch('s'); }
 #undef ZFMA
 #undef ZO_ABS
 #undef ZO_SQRT
+#undef ZLAPY3
+#undef ZLAMCH
+#undef ZCOPYSIGN
+#undef ZR_TMAX
+#undef ZR_EMIN
+#undef ZR_EMAX
+#undef ZR_BITS
 
 #define R float
 #define ZT zo_cf32
@@ -151,6 +165,13 @@ static inline double zo_z_lamch_s(void) { return zo_d_lamch('s'); }
 #define ZFMA fmaf
 #define ZO_ABS fabsf
 #define ZO_SQRT sqrtf
+#define ZLAPY3 zo_s_lapy3
+#define ZLAMCH zo_s_lamch
+#define ZCOPYSIGN copysignf
+#define ZR_TMAX FLT_MAX
+#define ZR_EMIN (-126)
+#define ZR_EMAX 127
+#define ZR_BITS 32
 static inline float zo_c_lamch_s(void) { return zo_s_lamch('s'); }
 #include "oracle_z_impl.h"
 #undef R
@@ -159,6 +180,13 @@ static inline float zo_c_lamch_s(void) { return zo_s_lamch('s'); }
 #undef ZFMA
 #undef ZO_ABS
 #undef ZO_SQRT
+#undef ZLAPY3
+#undef ZLAMCH
+#undef ZCOPYSIGN
+#undef ZR_TMAX
+#undef ZR_EMIN
+#undef ZR_EMAX
+#undef ZR_BITS
 
 /* ---- seeded inputs ------------------------------------------------------ */
 static unsigned long long zo_splitmix(unsigned long long *s) {

@@ -129,7 +129,17 @@ void zo_set_cdiv_as_written(int on);
   int P##potrf2(int order, int uplo, int n, Z *a, int lda);                                   \
   int P##potrf(int order, int uplo, int n, Z *a, int lda);                                    \
   int P##potrs(int order, int uplo, int n, int nrhs, const Z *a, int lda, Z *b, int ldb);     \
-  int P##posv(int order, int uplo, int n, int nrhs, Z *a, int lda, Z *b, int ldb);
+  int P##posv(int order, int uplo, int n, int nrhs, Z *a, int lda, Z *b, int ldb);            \
+  R P##nrm2(int n, const Z *x, int incx);                                                     \
+  int P##larfg(int n, Z *alpha, Z *x, int incx, Z *tau);                                      \
+  int P##larf1f(int order, int side, int m, int n, const Z *v, int incv, Z tau, Z *c,         \
+                int ldc, Z *work);                                                            \
+  int P##geqr2(int order, int m, int n, Z *a, int lda, Z *tau, Z *work);                      \
+  int P##larft(int order, int direct, int storev, int n, int k, const Z *v, int ldv,          \
+               const Z *tau, Z *t, int ldt);                                                  \
+  int P##larfb(int order, int side, int trans, int direct, int storev, int m, int n, int k,   \
+               const Z *v, int ldv, const Z *t, int ldt, Z *c, int ldc, Z *work, int ldwork); \
+  int P##geqrf(int order, int m, int n, Z *a, int lda, Z *tau, Z *work, int lwork);
 
 ZO_ZDECL(zo_cf64, double, zo_z_)
 ZO_ZDECL(zo_cf32, float, zo_c_)

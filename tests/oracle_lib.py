@@ -97,6 +97,10 @@ def load():
                 "potrf": (i32, [i32, i32, i32, vp, i32]),
                 "potrs": (i32, [i32, i32, i32, i32, vp, i32, vp, i32]),
                 "posv": (i32, [i32, i32, i32, i32, vp, i32, vp, i32]),
+                "nrm2": (R, [i32, vp, i32]),
+                "larfg": (i32, [i32, vp, vp, i32, vp]),
+                "geqr2": (i32, [i32, i32, i32, vp, i32, vp, vp]),
+                "geqrf": (i32, [i32, i32, i32, vp, i32, vp, vp, i32]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(_lib, pfx + name)
@@ -180,7 +184,7 @@ def geqrf(a):
     q = np.zeros(1, dtype=a.dtype)
     f = fn("geqrf", a.dtype)
     assert f(102, m, n, ptr(a), max(1, m), ptr(tau), ptr(q), -1) == 0
-    lwork = max(1, int(q[0]))
+    lwork = max(1, int(np.real(q[0])))
     work = np.zeros(lwork, dtype=a.dtype)
     r = f(102, m, n, ptr(a), max(1, m), ptr(tau), ptr(work), lwork)
     assert r == 0
@@ -197,7 +201,7 @@ def orgqr(qr, tau, ncols=None):
     f = fn("orgqr", qr.dtype)
     w = np.zeros(1, dtype=qr.dtype)
     assert f(102, m, ncols, k, ptr(q), max(1, m), ptr(tau), ptr(w), -1) == 0
-    lwork = max(1, int(w[0]))
+    lwork = max(1, int(np.real(w[0])))
     work = np.zeros(lwork, dtype=qr.dtype)
     assert f(102, m, ncols, k, ptr(q), max(1, m), ptr(tau), ptr(work), lwork) == 0
     return q

@@ -158,3 +158,48 @@ def test_zpotrs_row_major_ldb_check_as_written():
     assert f(101, 122, n, ol.ptr(h), n) == 0
     b = np.ascontiguousarray(cgaussian(n, 2, seed=6))
     assert ol.fn("potrs", np.complex128)(101, 122, n, 2, ol.ptr(h), n, ol.ptr(b), 2) == -1
+
+
+@pytest.mark.parametrize("m,n", [(1, 1), (5, 3), (3, 5), (64, 40), (200, 150), (300, 260)])
+def test_zgeqrf_equals_lapack(m, n):
+    """zgeqrf (blocked above nx = 128 columns) against scipy's: R, the
+    reflectors and tau to rounding; Q formed by LAPACK's zungqr from the
+    oracle's output is unitary and Q R = A."""
+    a = cgaussian(m, n, seed=m + n)
+    qr, tau = ol.geqrf(a)
+    qr2, tau2, _, info = lap.zgeqrf(a)
+    k = min(m, n)
+    scale = np.abs(qr2).max()
+    assert np.abs(np.triu(qr) - np.triu(qr2)).max() <= 1e-12 * scale
+    assert np.abs(np.tril(qr, -1) - np.tril(qr2, -1)).max() <= 1e-12 * max(1.0, scale)
+    np.testing.assert_allclose(tau[:k], tau2[:k], rtol=0, atol=1e-12)
+    q, _, _ = lap.zungqr(qr[:, :k], tau[:k], lwork=max(1, 64 * m))
+    assert np.abs(q.conj().T @ q - np.eye(k)).max() < 1e-13
+    assert np.abs(q @ np.triu(qr[:k, :]) - a).max() < 1e-13 * np.abs(a).max() * m
+
+
+def test_cgeqrf_single_precision():
+    a = cgaussian(90, 60, seed=4, dtype=np.complex64)
+    qr, tau = ol.geqrf(a)
+    q, _, _ = lap.cungqr(qr[:, :60], tau[:60], lwork=64 * 90)
+    assert np.abs(q.conj().T @ q - np.eye(60)).max() < 1e-5
+
+
+def test_zlarfg_as_written_breaks_householder():
+    """larfg scales x by div(1, alpha - beta) (larfg.zig:130-137): with the
+    tested quotient H is unitary; as written (the reciprocal of the intended
+    value) the reflectors no longer are."""
+    lib = ol.load()
+    a = cgaussian(40, 30, seed=7)
+    qr, tau = ol.geqrf(a)
+    q, _, _ = lap.zungqr(qr[:, :30], tau, lwork=64 * 40)
+    assert np.abs(q.conj().T @ q - np.eye(30)).max() < 1e-13
+    lib.zo_set_cdiv_as_written(1)
+    try:
+        qw, tw = ol.geqrf(a)
+    finally:
+        lib.zo_set_cdiv_as_written(0)
+    with np.errstate(all="ignore"):
+        q2, _, _ = lap.zungqr(qw[:, :30], tw, lwork=64 * 40)
+        err = np.abs(q2 @ np.triu(qw[:30, :]) - a).max()
+    assert not err <= 1e-3 * np.abs(a).max()  # far off, or not finite at all
