@@ -55,3 +55,49 @@ def test_quick_returns_touch_nothing():
     L.cblas_dtrsm(102, 999, 121, 111, 131, 2, 2, 1.0, ap, 2, ap, 2)
     L.cblas_dsyrk(102, 121, 113, 2, 2, 1.0, ap, 2, 0.0, ap, 2)  # conj_trans rejected
     assert list(a) == [0.0, 1.0, 2.0, 3.0]
+
+
+@pytest.mark.parametrize("call,expect", [
+    (lambda L, a, p: L.LAPACKE_zgetrf(103, 4, 4, a, 4, p), -1),
+    (lambda L, a, p: L.LAPACKE_zgetrf(102, -1, 4, a, 4, p), -2),
+    (lambda L, a, p: L.LAPACKE_zgetrf(102, 4, 4, a, 3, p), -5),
+    (lambda L, a, p: L.LAPACKE_cgetrf(101, 4, 5, a, 4, p), -5),
+    (lambda L, a, p: L.LAPACKE_zgetrs(102, b"X", 4, 1, a, 4, p, a, 4), -2),
+    (lambda L, a, p: L.LAPACKE_zgetrs(102, b"C", 4, 1, a, 3, p, a, 4), -6),
+    (lambda L, a, p: L.LAPACKE_zgetrs(101, b"N", 4, 2, a, 4, p, a, 1), -9),
+    (lambda L, a, p: L.LAPACKE_zgesv(102, 4, -1, a, 4, p, a, 4), -3),
+    (lambda L, a, p: L.LAPACKE_zpotrf(102, b"Q", 4, a, 4), -2),
+    (lambda L, a, p: L.LAPACKE_cpotrf(102, b"L", -2, a, 4), -3),
+    (lambda L, a, p: L.LAPACKE_zpotrs(102, b"L", 4, -1, a, 4, a, 4), -4),
+    (lambda L, a, p: L.LAPACKE_zposv(102, b"L", 4, 1, a, 4, a, 2), -8),
+    (lambda L, a, p: L.LAPACKE_dsytrf(103, b"L", 4, a, 4, p), -1),
+    (lambda L, a, p: L.LAPACKE_dsytrf(102, b"X", 4, a, 4, p), -2),
+    (lambda L, a, p: L.LAPACKE_dsytrf(102, b"U", -1, a, 4, p), -3),
+    (lambda L, a, p: L.LAPACKE_ssytrf(102, b"U", 4, a, 3, p), -5),
+])
+def test_complex_and_sytrf_argument_checks(call, expect):
+    """The complex LAPACKE entries and sytrf check their arguments as the real
+    ones do, before any device work."""
+    L = zg.lib()
+    a = np.zeros(128)
+    p = np.zeros(8, dtype=np.int32)
+    assert call(L, a.ctypes.data_as(C.c_void_p), p.ctypes.data_as(C.c_void_p)) == expect
+
+
+def test_complex_blas_invalid_arguments_and_quick_returns_touch_nothing():
+    """cblas_z* return silently on invalid arguments (zml swallows the error)
+    and do nothing for empty products or alpha = 0, beta = 1."""
+    L = zg.lib()
+    c = np.arange(8.0)  # four complex numbers
+    cp = c.ctypes.data_as(C.c_void_p)
+    one = np.array([1.0, 0.0]).ctypes.data_as(C.c_void_p)
+    zero = np.array([0.0, 0.0]).ctypes.data_as(C.c_void_p)
+    L.cblas_zgemm(102, 111, 111, -1, 2, 2, one, cp, 1, cp, 1, zero, cp, 1)   # m < 0
+    L.cblas_zgemm(102, 999, 111, 2, 2, 2, one, cp, 2, cp, 2, zero, cp, 2)    # bad transpose
+    L.cblas_zgemm(102, 111, 111, 2, 2, 2, zero, cp, 2, cp, 2, one, cp, 2)    # alpha 0, beta 1
+    L.cblas_zgemm(102, 111, 111, 0, 2, 2, one, cp, 1, cp, 2, zero, cp, 1)    # m = 0
+    L.cblas_zherk(102, 121, 112, 2, 2, 1.0, cp, 2, 0.0, cp, 2)               # trans rejected
+    L.cblas_zsyrk(102, 121, 113, 2, 2, one, cp, 2, zero, cp, 2)              # conj_trans rejected
+    L.cblas_ztrsm(102, 141, 999, 111, 131, 2, 2, one, cp, 2, cp, 2)          # bad uplo
+    L.cblas_zgemm(102, 111, 111, 2, 2, 2, one, cp, 2, cp, 2, None, cp, 2)    # no beta
+    assert list(c) == [float(i) for i in range(8)]
