@@ -466,6 +466,102 @@ def suite_bench(torch, zg, L, dev, st):
         "fp64_equiv_tflops": (2.0 * n ** 3 / 3) / t / 1e12}
     del S
     torch.cuda.empty_cache()
+    out["next"] = next_rows_bench(torch, L, dev, g)
+    return out
+
+
+def next_rows_bench(torch, L, dev, g):
+    """The complex variants and Bunch-Kaufman at n = 4096 (device pointers):
+    zgemm (as one real GEMM over the expanded operand), zgetrf + zgetrs,
+    zpotrf, dsytrf.  These C entries run on the library's stream and return
+    synchronized, so each is timed by the host clock around one call (after a
+    warm-up call).  An entry that raises records its error instead of ending
+    the bench line."""
+    import time
+    import numpy as np
+
+    out = {"timer": "host wall clock around one synchronous call, after a warm-up call"}
+    n = 4096
+    one = np.array([1.0, 0.0])
+    zero = np.array([0.0, 0.0])
+    P = lambda a: a.ctypes.data  # noqa: E731
+
+    def wall(fn):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, r
+
+    def guarded(name, fn):
+        try:
+            out[name] = fn()
+        except Exception as e:  # noqa: BLE001 - reported in the line
+            out[name] = {"error": str(e)[:200]}
+
+    def zgemm():
+        A = torch.randn(n, n, dtype=torch.complex128, device=dev, generator=g)
+        B = torch.randn(n, n, dtype=torch.complex128, device=dev, generator=g)
+        C = torch.zeros(n, n, dtype=torch.complex128, device=dev)
+        t, _ = wall(lambda: L.cblas_zgemm(102, 111, 111, n, n, n, P(one), A.data_ptr(), n,
+                                          B.data_ptr(), n, P(zero), C.data_ptr(), n))
+        ref = B @ A  # the row-major storages hold A^T, B^T: C^T = B^T A^T
+        err = ((C - ref).abs().max() / ref.abs().max()).item()
+        return {"s": t, "real_tflops": 8.0 * n ** 3 / t / 1e12, "rel_err_vs_torch": err}
+
+    def zgetrf():
+        S = torch.randn(n, n, dtype=torch.complex128, device=dev, generator=g)  # storage of A^T
+        F = S.clone()
+        piv = torch.zeros(n, dtype=torch.int32, device=dev)
+
+        def factor():
+            F.copy_(S)
+            return L.LAPACKE_zgetrf(102, n, n, F.data_ptr(), n, piv.data_ptr())
+        t, info = wall(factor)
+        b = torch.randn(n, dtype=torch.complex128, device=dev, generator=g)
+        x = b.clone()
+
+        def solve():
+            x.copy_(b)
+            return L.LAPACKE_zgetrs(102, b"N", n, 1, F.data_ptr(), n, piv.data_ptr(),
+                                    x.data_ptr(), n)
+        ts, rc = wall(solve)
+        M = S.t()
+        r = b - M @ x
+        berr = (r.abs().max() / (M.abs().sum(1).max() * x.abs().max() + b.abs().max())).item()
+        return {"getrf_s": t, "getrf_real_tflops": 8.0 * n ** 3 / 3 / t / 1e12, "info": info,
+                "getrs_1_s": ts, "rc": rc, "berr": berr}
+
+    def zpotrf():
+        G = torch.randn(n, n, dtype=torch.complex128, device=dev, generator=g)
+        H = G @ G.conj().t() / n + torch.eye(n, dtype=torch.complex128, device=dev)
+        F = H.clone()
+
+        def factor():
+            F.copy_(H)
+            return L.LAPACKE_zpotrf(102, b"L", n, F.data_ptr(), n)
+        t, info = wall(factor)
+        return {"s": t, "real_tflops": 4.0 * n ** 3 / 3 / t / 1e12, "info": info}
+
+    def dsytrf():
+        G = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
+        Sy = (G + G.t()) / 2
+        F = Sy.clone()
+        piv = torch.zeros(n, dtype=torch.int32, device=dev)
+
+        def factor():
+            F.copy_(Sy)
+            return L.LAPACKE_dsytrf(102, b"L", n, F.data_ptr(), n, piv.data_ptr())
+        t, info = wall(factor)
+        return {"s": t, "tflops": n ** 3 / 3 / t / 1e12, "info": info,
+                "two_by_two_blocks": int((piv < 0).sum().item() // 2)}
+
+    guarded("zgemm_n4096", zgemm)
+    guarded("zgetrf_n4096", zgetrf)
+    guarded("zpotrf_n4096", zpotrf)
+    guarded("dsytrf_n4096", dsytrf)
+    torch.cuda.empty_cache()
     return out
 
 
