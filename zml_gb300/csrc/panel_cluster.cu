@@ -67,12 +67,6 @@ __device__ __forceinline__ unsigned remote_addr(const void *local, unsigned rank
   asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
   return r;
 }
-__device__ __forceinline__ void st_cluster(unsigned addr, float v) {
-  asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
-}
-__device__ __forceinline__ void st_cluster(unsigned addr, unsigned long long v) {
-  asm volatile("st.shared::cluster.u64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
-}
 // Remote stores that complete their bytes on the destination CTA's mbarrier.
 __device__ __forceinline__ void st_async(unsigned addr, float v, unsigned mbar) {
   asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.f32 [%0], %1, [%2];" ::"r"(
