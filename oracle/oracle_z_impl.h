@@ -1210,3 +1210,194 @@ int ZP(geqrf)(int order, int m, int n, ZT *a, int lda, ZT *tau, ZT *work, int lw
   work[0] = ZP(c)((R)iws, (R)0);
   return 0;
 }
+
+/* ---- Hermitian Bunch-Kaufman (unblocked) ------------------------------------ */
+
+/* blas/her.zig:19-380 (k_her): A := alpha x x^H + A on the uplo triangle,
+ * alpha real, the diagonal kept real; column j skipped when x[j] == 0 (its
+ * diagonal still made real); row-major inverts uplo and conjugates x[i]
+ * where column-major conjugates x[j] (her.zig:12-16). */
+#define HZ_(i, j) a[(long)(i) + (long)(j) * lda]
+static int ZP(k_her)(int uplo, int n, R alpha, const ZT *x, int incx, ZT *a, int lda, int noconj) {
+  if (n < 0 || lda < ZO_MAX(1, n) || incx == 0) return ZO_EINVAL;
+  if (n == 0 || alpha == (R)0) return 0;
+  const long kx = incx < 0 ? (long)(-n + 1) * incx : 0;
+  long jx = kx;
+  for (int j = 0; j < n; ++j) {
+    if (!ZP(cis0)(x[jx])) {
+      const ZT temp = ZP(cscale)(noconj ? ZP(cconj)(x[jx]) : x[jx], alpha);
+      const ZT xj = noconj ? x[jx] : ZP(cconj)(x[jx]);
+      if (uplo == ZO_UPPER) {
+        long ix = kx;
+        for (int i = 0; i < j; ++i, ix += incx)
+          HZ_(i, j) = ZP(cadd)(HZ_(i, j), ZP(cmul)(ZP(cj)(x[ix], !noconj), temp));
+        HZ_(j, j) = ZP(c)(HZ_(j, j).re + ZP(cmul)(xj, temp).re, (R)0);
+      } else {
+        HZ_(j, j) = ZP(c)(HZ_(j, j).re + ZP(cmul)(xj, temp).re, (R)0);
+        long ix = jx;
+        for (int i = j + 1; i < n; ++i) {
+          ix += incx;
+          HZ_(i, j) = ZP(cadd)(HZ_(i, j), ZP(cmul)(ZP(cj)(x[ix], !noconj), temp));
+        }
+      }
+    } else {
+      HZ_(j, j) = ZP(c)(HZ_(j, j).re, (R)0);
+    }
+    jx += incx;
+  }
+  return 0;
+}
+#undef HZ_
+int ZP(her)(int order, int uplo, int n, R alpha, const ZT *x, int incx, ZT *a, int lda) {
+  if (order == ZO_COL) return ZP(k_her)(uplo, n, alpha, x, incx, a, lda, 1);
+  return ZP(k_her)(uplo == ZO_UPPER ? ZO_LOWER : ZO_UPPER, n, alpha, x, incx, a, lda, 0);
+}
+
+/* lapack/hetf2.zig:13-666: unblocked Bunch-Kaufman of a Hermitian matrix
+ * (LAPACK zhetf2): pivot magnitudes |re a_kk| and |re| + |im| elsewhere, the
+ * interchange conjugates the entries it moves across the diagonal, 1x1 steps
+ * update with her and a real scaling, 2x2 steps with d = |a_k-1,k| and the
+ * conjugated multipliers.  One deliberate difference: for a 2x2 block
+ * without interchange the upper branch clears the imaginary part of
+ * a(k+1, k+1) as written (hetf2.zig:180-187; past the matrix when
+ * k = n - 1); LAPACK's zhetf2 clears a(k-1, k-1), the block's other
+ * diagonal entry, and so does this restatement. */
+int ZP(hetf2)(int order, int uplo, int n, ZT *a, int lda, int *ipiv) {
+  if (n < 0 || lda < ZO_MAX(1, n)) return ZO_EINVAL;
+  int info = 0;
+  const R alpha = ((R)1 + ZO_SQRT((R)17)) / (R)8;
+  const int cl = order == ZO_COL ? 1 : lda, rl = order == ZO_COL ? lda : 1;
+#define HA(i, j) a[zo_index(order, (i), (j), lda)]
+  const int up = uplo == ZO_UPPER;
+  int k = up ? n - 1 : 0;
+  while (up ? k >= 0 : k < n) {
+    int kstep = 1, imax = 0, kp;
+    const R absakk = ZO_ABS(HA(k, k).re);
+    R colmax = 0;
+    if (up ? k > 0 : k < n - 1) {
+      imax = up ? ZP(iamax)(k, a + zo_index(order, 0, k, lda), cl)
+                : k + 1 + ZP(iamax)(n - k - 1, a + zo_index(order, k + 1, k, lda), cl);
+      colmax = ZP(cabs1)(HA(imax, k));
+    }
+    if (ZO_MAX(absakk, colmax) == (R)0 || absakk != absakk) {
+      if (info == 0) info = k + 1;
+      kp = k;
+    } else {
+      if (absakk >= alpha * colmax) {
+        kp = k;
+      } else {
+        int jmax;
+        R rowmax;
+        if (up) {
+          jmax = imax + 1 + ZP(iamax)(k - imax, a + zo_index(order, imax, imax + 1, lda), rl);
+          rowmax = ZP(cabs1)(HA(imax, jmax));
+          if (imax > 0) {
+            jmax = ZP(iamax)(imax, a + zo_index(order, 0, imax, lda), cl);
+            rowmax = ZO_MAX(rowmax, ZP(cabs1)(HA(jmax, imax)));
+          }
+        } else {
+          jmax = k + ZP(iamax)(imax - k, a + zo_index(order, imax, k, lda), rl);
+          rowmax = ZP(cabs1)(HA(imax, jmax));
+          if (imax < n - 1) {
+            jmax = imax + 1 + ZP(iamax)(n - imax - 1, a + zo_index(order, imax + 1, imax, lda), cl);
+            rowmax = ZO_MAX(rowmax, ZP(cabs1)(HA(jmax, imax)));
+          }
+        }
+        if (absakk >= alpha * (colmax * (colmax / rowmax))) {
+          kp = k;
+        } else if (ZP(cabs1)(HA(imax, imax)) >= alpha * rowmax) {
+          kp = imax;
+        } else {
+          kp = imax;
+          kstep = 2;
+        }
+      }
+      const int kk = up ? k - kstep + 1 : k + kstep - 1;
+      if (kp != kk) {
+        if (up) {
+          for (int i = 0; i < kp; ++i) {
+            const ZT t = HA(i, kk);
+            HA(i, kk) = HA(i, kp);
+            HA(i, kp) = t;
+          }
+          for (int j = kp + 1; j < kk; ++j) {
+            const ZT t = ZP(cconj)(HA(j, kk));
+            HA(j, kk) = ZP(cconj)(HA(kp, j));
+            HA(kp, j) = t;
+          }
+        } else {
+          for (int i = kp + 1; i < n; ++i) {
+            const ZT t = HA(i, kk);
+            HA(i, kk) = HA(i, kp);
+            HA(i, kp) = t;
+          }
+          for (int j = kk + 1; j < kp; ++j) {
+            const ZT t = ZP(cconj)(HA(j, kk));
+            HA(j, kk) = ZP(cconj)(HA(kp, j));
+            HA(kp, j) = t;
+          }
+        }
+        HA(kp, kk) = ZP(cconj)(HA(kp, kk));
+        const R r1 = HA(kk, kk).re;
+        HA(kk, kk) = ZP(c)(HA(kp, kp).re, (R)0);
+        HA(kp, kp) = ZP(c)(r1, (R)0);
+        if (kstep == 2) {
+          HA(k, k).im = 0;
+          const int o = up ? k - 1 : k + 1;
+          const ZT t = HA(o, k);
+          HA(o, k) = HA(kp, k);
+          HA(kp, k) = t;
+        }
+      } else {
+        HA(k, k).im = 0;
+        if (kstep == 2) HA(up ? k - 1 : k + 1, up ? k - 1 : k + 1).im = 0;
+      }
+      if (kstep == 1) {
+        if (up || k < n - 1) {
+          const R r1 = (R)1 / HA(k, k).re;
+          const int len = up ? k : n - k - 1;
+          ZT *x = up ? a + zo_index(order, 0, k, lda) : a + zo_index(order, k + 1, k, lda);
+          ZP(her)(order, uplo, len, -r1, x, cl, up ? a : a + zo_index(order, k + 1, k + 1, lda),
+                  lda);
+          long ix = 0;
+          for (int i = 0; i < len; ++i, ix += cl) x[ix] = ZP(cscale)(x[ix], r1);
+        }
+      } else if (up ? k > 1 : k < n - 2) {
+        const int o = up ? k - 1 : k + 1; /* the block's other column */
+        R d = hypot(HA(o, k).re, HA(o, k).im);
+        const R dother = HA(o, o).re / d; /* d22 (upper) / d11 (lower) */
+        const R dk = HA(k, k).re / d;     /* d11 (upper) / d22 (lower) */
+        const R t = (R)1 / (dk * dother - (R)1);
+        const ZT dd = ZP(c)(HA(o, k).re / d, HA(o, k).im / d); /* d12 / d21 */
+        d = t / d;
+        for (int q = 0; q < (up ? k - 1 : n - k - 2); ++q) {
+          const int j = up ? k - 2 - q : k + 2 + q;
+          ZT wk, wo;
+          if (up) { /* wkm1 = d (d11 a_j,k-1 - conj(d12) a_jk), wk = d (d22 a_jk - d12 a_j,k-1) */
+            wo = ZP(cscale)(ZP(csub)(ZP(cscale)(HA(j, o), dk), ZP(cmul)(ZP(cconj)(dd), HA(j, k))), d);
+            wk = ZP(cscale)(ZP(csub)(ZP(cscale)(HA(j, k), dother), ZP(cmul)(dd, HA(j, o))), d);
+          } else { /* wk = d (d11 a_jk - d21 a_j,k+1), wkp1 = d (d22 a_j,k+1 - conj(d21) a_jk) */
+            wk = ZP(cscale)(ZP(csub)(ZP(cscale)(HA(j, k), dother), ZP(cmul)(dd, HA(j, o))), d);
+            wo = ZP(cscale)(ZP(csub)(ZP(cscale)(HA(j, o), dk), ZP(cmul)(ZP(cconj)(dd), HA(j, k))), d);
+          }
+          const int i0 = up ? 0 : j, i1 = up ? j + 1 : n;
+          for (int i = (up ? j : i0); up ? i >= i0 : i < i1; i += up ? -1 : 1)
+            HA(i, j) = ZP(csub)(HA(i, j), ZP(cadd)(ZP(cmul)(HA(i, k), ZP(cconj)(wk)),
+                                                   ZP(cmul)(HA(i, o), ZP(cconj)(wo))));
+          HA(j, k) = wk;
+          HA(j, o) = wo;
+          HA(j, j) = ZP(c)(HA(j, j).re, (R)0);
+        }
+      }
+    }
+    if (kstep == 1) {
+      ipiv[k] = kp + 1;
+    } else {
+      ipiv[k] = -(kp + 1);
+      ipiv[up ? k - 1 : k + 1] = -(kp + 1);
+    }
+    k = up ? k - kstep : k + kstep;
+  }
+#undef HA
+  return info;
+}

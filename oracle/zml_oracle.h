@@ -139,7 +139,9 @@ void zo_set_cdiv_as_written(int on);
                const Z *tau, Z *t, int ldt);                                                  \
   int P##larfb(int order, int side, int trans, int direct, int storev, int m, int n, int k,   \
                const Z *v, int ldv, const Z *t, int ldt, Z *c, int ldc, Z *work, int ldwork); \
-  int P##geqrf(int order, int m, int n, Z *a, int lda, Z *tau, Z *work, int lwork);
+  int P##geqrf(int order, int m, int n, Z *a, int lda, Z *tau, Z *work, int lwork);          \
+  int P##her(int order, int uplo, int n, R alpha, const Z *x, int incx, Z *a, int lda);       \
+  int P##hetf2(int order, int uplo, int n, Z *a, int lda, int *ipiv);
 
 ZO_ZDECL(zo_cf64, double, zo_z_)
 ZO_ZDECL(zo_cf32, float, zo_c_)

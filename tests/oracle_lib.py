@@ -101,6 +101,8 @@ def load():
                 "larfg": (i32, [i32, vp, vp, i32, vp]),
                 "geqr2": (i32, [i32, i32, i32, vp, i32, vp, vp]),
                 "geqrf": (i32, [i32, i32, i32, vp, i32, vp, vp, i32]),
+                "her": (i32, [i32, i32, i32, R, vp, i32, vp, i32]),
+                "hetf2": (i32, [i32, i32, i32, vp, i32, vp]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(_lib, pfx + name)

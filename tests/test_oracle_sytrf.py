@@ -5,7 +5,9 @@ dsytf2 (lapack/sytrf.zig, lasyf.zig, sytf2.zig), so the oracle is pinned
 against scipy's bundled LAPACK running the same algorithm: identical ipiv
 (the 1x1 / 2x2 pivot blocks and interchanges) and factors to rounding, below
 (unblocked) and above (blocked, nb = 64) the block size, both triangles; and
-the factors solve A x = b through LAPACK's own dsytrs.
+the factors solve A x = b through LAPACK's own dsytrs.  The Hermitian form
+(hetf2, unblocked) is pinned the same way against zhetrf, which runs zhetf2
+itself up to nb = 64 columns, and through zhetrs beyond.
 """
 import numpy as np
 import pytest
@@ -65,3 +67,42 @@ def test_ilaenv_sytrf():
     lib = ol.load()
     assert lib.zo_ilaenv(1, b"DSYTRF", 500, -1, -1, -1) == 64
     assert lib.zo_ilaenv(2, b"DSYTRF", 500, -1, -1, -1) == 8
+
+
+def herm(n, seed):
+    rng = np.random.default_rng(seed)
+    g = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    return np.asfortranarray((g + g.conj().T) / 2)
+
+
+def zhetf2(a, uplo):
+    f = a.copy(order="F")
+    ipiv = np.zeros(a.shape[0], dtype=np.int32)
+    info = ol.fn("hetf2", np.complex128)(102, uplo, a.shape[0], ol.ptr(f), max(1, a.shape[0]),
+                                         ol.ptr(ipiv))
+    return f, ipiv, info
+
+
+@pytest.mark.parametrize("uplo", [121, 122])
+@pytest.mark.parametrize("n", [1, 2, 5, 20, 64])
+def test_zhetf2_equals_lapack_zhetrf(n, uplo):
+    a = herm(n, seed=n + uplo)
+    f, ipiv, info = zhetf2(a, uplo)
+    ldu, ipiv2, info2 = lap.zhetrf(a, lower=int(uplo == 122))
+    assert info == info2 == 0
+    np.testing.assert_array_equal(ipiv, ipiv2)
+    tri = np.triu if uplo == 121 else np.tril
+    assert np.abs(tri(f) - tri(ldu)).max() <= 1e-11 * max(1.0, np.abs(ldu).max())
+    assert not np.diag(f).imag.any()
+
+
+@pytest.mark.parametrize("uplo", [121, 122])
+def test_zhetf2_solves_through_zhetrs(uplo):
+    n = 150
+    a = herm(n, seed=uplo)
+    f, ipiv, info = zhetf2(a, uplo)
+    assert info == 0
+    x = np.random.default_rng(2).standard_normal((n, 2)) + 0j
+    sol, inf = lap.zhetrs(f, ipiv, a @ x, lower=int(uplo == 122))
+    assert inf == 0
+    np.testing.assert_allclose(sol, x, rtol=1e-9, atol=1e-9)
