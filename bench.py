@@ -470,7 +470,7 @@ def suite_bench(torch, zg, L, dev, st):
     return out
 
 
-def next_rows_bench(torch, L, dev, g):
+def next_rows_bench(torch, L, dev, g, n=4096):
     """The complex variants and Bunch-Kaufman at n = 4096 (device pointers):
     zgemm (as one real GEMM over the expanded operand), zgetrf + zgetrs,
     zpotrf, dsytrf.  These C entries run on the library's stream and return
@@ -481,7 +481,6 @@ def next_rows_bench(torch, L, dev, g):
     import numpy as np
 
     out = {"timer": "host wall clock around one synchronous call, after a warm-up call"}
-    n = 4096
     one = np.array([1.0, 0.0])
     zero = np.array([0.0, 0.0])
     P = lambda a: a.ctypes.data  # noqa: E731
@@ -557,10 +556,10 @@ def next_rows_bench(torch, L, dev, g):
         return {"s": t, "tflops": n ** 3 / 3 / t / 1e12, "info": info,
                 "two_by_two_blocks": int((piv < 0).sum().item() // 2)}
 
-    guarded("zgemm_n4096", zgemm)
-    guarded("zgetrf_n4096", zgetrf)
-    guarded("zpotrf_n4096", zpotrf)
-    guarded("dsytrf_n4096", dsytrf)
+    guarded("zgemm_n%d" % n, zgemm)
+    guarded("zgetrf_n%d" % n, zgetrf)
+    guarded("zpotrf_n%d" % n, zpotrf)
+    guarded("dsytrf_n%d" % n, dsytrf)
     torch.cuda.empty_cache()
     return out
 
