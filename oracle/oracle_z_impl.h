@@ -1401,3 +1401,365 @@ int ZP(hetf2)(int order, int uplo, int n, ZT *a, int lda, int *ipiv) {
 #undef HA
   return info;
 }
+
+/* ---- blocked Hermitian Bunch-Kaufman (hetrf over lahef) -------------------- */
+
+/* blas/gemmtr.zig:69-1032 (complex): the uplo triangle of
+ * C := alpha op(A) op(B) + beta C, the loops of complex gemm with the row
+ * range cut to the triangle (operand order as gemm's). */
+static int ZP(k_gemmtr)(int uplo, int transa, int transb, int n, int k, ZT alpha, const ZT *a,
+                        int lda, const ZT *b, int ldb, ZT beta, ZT *c, int ldc) {
+  const int nota = transa == ZO_NOTRANS || transa == ZO_CONJNOTRANS;
+  const int notb = transb == ZO_NOTRANS || transb == ZO_CONJNOTRANS;
+  const int cja = !(transa == ZO_NOTRANS || transa == ZO_TRANS);
+  const int cjb = !(transb == ZO_NOTRANS || transb == ZO_TRANS);
+  if (n < 0 || k < 0) return ZO_EINVAL;
+  if (n == 0) return 0;
+  const int up = uplo == ZO_UPPER;
+#define GA(i, j) a[(long)(i) + (long)(j) * lda]
+#define GB(i, j) b[(long)(i) + (long)(j) * ldb]
+#define GC(i, j) c[(long)(i) + (long)(j) * ldc]
+  if (ZP(cis0)(alpha)) {
+    for (int j = 0; j < n; ++j)
+      for (int i = up ? 0 : j; i < (up ? j + 1 : n); ++i)
+        GC(i, j) = ZP(cis0)(beta) ? ZP(zero) : ZP(cmul)(GC(i, j), beta);
+    return 0;
+  }
+  if (nota) {
+    const int plain = notb && !cja && !cjb;
+    for (int j = 0; j < n; ++j) {
+      const int i0 = up ? 0 : j, i1 = up ? j + 1 : n;
+      if (ZP(cis0)(beta)) {
+        for (int i = i0; i < i1; ++i) GC(i, j) = ZP(zero);
+      } else if (!ZP(cis1)(beta)) {
+        for (int i = i0; i < i1; ++i) GC(i, j) = ZP(cmul)(GC(i, j), beta);
+      }
+      for (int l = 0; l < k; ++l) {
+        const ZT bl = ZP(cj)(notb ? GB(l, j) : GB(j, l), cjb);
+        const ZT temp = plain ? ZP(cmul)(alpha, bl) : ZP(cmul)(bl, alpha);
+        for (int i = i0; i < i1; ++i) {
+          const ZT al = ZP(cj)(GA(i, l), cja);
+          GC(i, j) = ZP(cadd)(GC(i, j), plain ? ZP(cmul)(temp, al) : ZP(cmul)(al, temp));
+        }
+      }
+    }
+  } else {
+    for (int j = 0; j < n; ++j)
+      for (int i = up ? 0 : j; i < (up ? j + 1 : n); ++i) {
+        ZT temp = ZP(zero);
+        for (int l = 0; l < k; ++l)
+          temp = ZP(cadd)(temp, ZP(cmul)(ZP(cj)(GA(l, i), cja), ZP(cj)(notb ? GB(l, j) : GB(j, l), cjb)));
+        if (ZP(cis0)(beta)) {
+          GC(i, j) = ZP(cmul)(alpha, temp);
+        } else if (ZP(cis1)(beta)) {
+          GC(i, j) = ZP(cadd)(GC(i, j), ZP(cmul)(alpha, temp));
+        } else {
+          GC(i, j) = ZP(cmul)(GC(i, j), beta);
+          GC(i, j) = ZP(cadd)(GC(i, j), ZP(cmul)(alpha, temp));
+        }
+      }
+  }
+#undef GA
+#undef GB
+#undef GC
+  return 0;
+}
+static int ZP(gemmtr)(int order, int uplo, int transa, int transb, int n, int k, ZT alpha,
+                      const ZT *a, int lda, const ZT *b, int ldb, ZT beta, ZT *c, int ldc) {
+  if (order == ZO_COL)
+    return ZP(k_gemmtr)(uplo, transa, transb, n, k, alpha, a, lda, b, ldb, beta, c, ldc);
+  return ZP(k_gemmtr)(uplo == ZO_UPPER ? ZO_LOWER : ZO_UPPER, transb, transa, n, k, alpha, b, ldb,
+                      a, lda, beta, c, ldc);
+}
+
+static inline void ZP(swapv)(int n, ZT *x, int incx, ZT *y, int incy) {
+  for (long i = 0, ix = 0, iy = 0; i < n; ++i, ix += incx, iy += incy) {
+    const ZT t = x[ix];
+    x[ix] = y[iy];
+    y[iy] = t;
+  }
+}
+
+/* lapack/lahef.zig:17-1034 (LAPACK zlahef with gemmtr): up to nb columns of
+ * the Hermitian Bunch-Kaufman factorization with W = U12 D (upper) or
+ * L21 D (lower) built alongside (conjugated rows by lacgv, real
+ * diagonals), the rest of the triangle updated by gemmtr, the interchanges
+ * of U12 / L21 undone; *kb = the columns factored.  The 2x2 step's
+ * d21 = t / d21 is the real-by-complex quotient of crdiv. */
+int ZP(lahef)(int order, int uplo, int n, int nb, int *kb, ZT *a, int lda, int *ipiv, ZT *w,
+              int ldw) {
+  int info = 0;
+  const R alpha = ((R)1 + ZO_SQRT((R)17)) / (R)8;
+  const int cl = order == ZO_COL ? 1 : lda, rl = order == ZO_COL ? lda : 1;
+  const int clw = order == ZO_COL ? 1 : ldw, rlw = order == ZO_COL ? ldw : 1;
+#define LA(i, j) a[zo_index(order, (i), (j), lda)]
+#define LW(i, j) w[zo_index(order, (i), (j), ldw)]
+#define PA(i, j) (a + zo_index(order, (i), (j), lda))
+#define PW(i, j) (w + zo_index(order, (i), (j), ldw))
+  if (uplo == ZO_UPPER) {
+    int k = n - 1, kw;
+    while (1) {
+      kw = nb + k - n;
+      if ((k <= n - nb && nb < n) || k < 0) break;
+      ZP(copy)(k, PA(0, k), cl, PW(0, kw), clw);
+      LW(k, kw) = ZP(c)(LA(k, k).re, (R)0);
+      if (k < n - 1) {
+        ZP(gemv)(order, ZO_NOTRANS, k + 1, n - (k + 1), ZP(mone), PA(0, k + 1), lda, PW(k, kw + 1),
+                 rlw, ZP(one), PW(0, kw), clw);
+        LW(k, kw) = ZP(c)(LW(k, kw).re, (R)0);
+      }
+      int kstep = 1, imax = 0, kp;
+      const R absakk = ZO_ABS(LW(k, kw).re);
+      R colmax = 0;
+      if (k > 0) {
+        imax = ZP(iamax)(k, PW(0, kw), clw);
+        colmax = ZP(cabs1)(LW(imax, kw));
+      }
+      if (ZO_MAX(absakk, colmax) == (R)0) {
+        if (info == 0) info = k + 1;
+        kp = k;
+        LA(k, k) = ZP(c)(LA(k, k).re, (R)0);
+      } else {
+        if (absakk >= alpha * colmax) {
+          kp = k;
+        } else {
+          ZP(copy)(imax, PA(0, imax), cl, PW(0, kw - 1), clw);
+          LW(imax, kw - 1) = ZP(c)(LA(imax, imax).re, (R)0);
+          ZP(copy)(k - imax, PA(imax, imax + 1), rl, PW(imax + 1, kw - 1), clw);
+          ZP(lacgv)(k - imax, PW(imax + 1, kw - 1), clw);
+          if (k < n - 1) {
+            ZP(gemv)(order, ZO_NOTRANS, k + 1, n - (k + 1), ZP(mone), PA(0, k + 1), lda,
+                     PW(imax, kw + 1), rlw, ZP(one), PW(0, kw - 1), clw);
+            LW(imax, kw - 1) = ZP(c)(LW(imax, kw - 1).re, (R)0);
+          }
+          int jmax = imax + 1 + ZP(iamax)(k - imax, PW(imax + 1, kw - 1), clw);
+          R rowmax = ZP(cabs1)(LW(jmax, kw - 1));
+          if (imax > 0) {
+            jmax = ZP(iamax)(imax, PW(0, kw - 1), clw);
+            rowmax = ZO_MAX(rowmax, ZP(cabs1)(LW(jmax, kw - 1)));
+          }
+          if (absakk >= alpha * (colmax * (colmax / rowmax))) {
+            kp = k;
+          } else if (ZO_ABS(LW(imax, kw - 1).re) >= alpha * rowmax) {
+            kp = imax;
+            ZP(copy)(k + 1, PW(0, kw - 1), clw, PW(0, kw), clw);
+          } else {
+            kp = imax;
+            kstep = 2;
+          }
+        }
+        const int kk = k - kstep + 1, kkw = nb + kk - n;
+        if (kp != kk) {
+          LA(kp, kp) = ZP(c)(LA(kk, kk).re, (R)0);
+          ZP(copy)(kk - kp - 1, PA(kp + 1, kk), cl, PA(kp, kp + 1), rl);
+          ZP(lacgv)(kk - kp - 1, PA(kp, kp + 1), rl);
+          if (kp > 0) ZP(copy)(kp, PA(0, kk), cl, PA(0, kp), cl);
+          if (k < n - 1) ZP(swapv)(n - (k + 1), PA(kk, k + 1), rl, PA(kp, k + 1), rl);
+          ZP(swapv)(n - kk, PW(kk, kkw), rlw, PW(kp, kkw), rlw);
+        }
+        if (kstep == 1) {
+          ZP(copy)(k + 1, PW(0, kw), clw, PA(0, k), cl);
+          if (k > 0) {
+            const R r1 = (R)1 / LA(k, k).re;
+            for (int i = 0; i < k; ++i) LA(i, k) = ZP(cscale)(LA(i, k), r1);
+            ZP(lacgv)(k, PW(0, kw), clw);
+          }
+        } else {
+          if (k > 1) {
+            ZT d21 = LW(k - 1, kw);
+            const ZT d11 = ZP(cdiv)(LW(k, kw), ZP(cconj)(d21));
+            const ZT d22 = ZP(cdiv)(LW(k - 1, kw - 1), d21);
+            const R t = (R)1 / (ZP(cmul)(d11, d22).re - (R)1);
+            d21 = ZP(crdiv)(t, d21);
+            for (int j = 0; j < k - 1; ++j) {
+              LA(j, k - 1) = ZP(cmul)(d21, ZP(csub)(ZP(cmul)(d11, LW(j, kw - 1)), LW(j, kw)));
+              LA(j, k) = ZP(cmul)(ZP(cconj)(d21), ZP(csub)(ZP(cmul)(d22, LW(j, kw)), LW(j, kw - 1)));
+            }
+          }
+          LA(k - 1, k - 1) = LW(k - 1, kw - 1);
+          LA(k - 1, k) = LW(k - 1, kw);
+          LA(k, k) = LW(k, kw);
+          ZP(lacgv)(k, PW(0, kw), clw);
+          ZP(lacgv)(k - 1, PW(0, kw - 1), clw);
+        }
+      }
+      if (kstep == 1) {
+        ipiv[k] = kp + 1;
+      } else {
+        ipiv[k] = -(kp + 1);
+        ipiv[k - 1] = -(kp + 1);
+      }
+      k -= kstep;
+    }
+    ZP(gemmtr)(order, ZO_UPPER, ZO_NOTRANS, ZO_TRANS, k + 1, n - (k + 1), ZP(mone), PA(0, k + 1),
+               lda, PW(0, kw + 1), ldw, ZP(one), a, lda);
+    int j = k + 1;
+    while (j < n) {
+      const int jj = j;
+      int jp = ipiv[j];
+      if (jp < 0) {
+        jp = -jp;
+        j += 1;
+      }
+      j += 1;
+      if (jp - 1 != jj && j < n) ZP(swapv)(n - j, PA(jp - 1, j), rl, PA(jj, j), rl);
+    }
+    *kb = n - k - 1;
+  } else {
+    int k = 0;
+    while (1) {
+      if ((k >= nb - 1 && nb < n) || k > n - 1) break;
+      LW(k, k) = ZP(c)(LA(k, k).re, (R)0);
+      if (k < n - 1) ZP(copy)(n - k - 1, PA(k + 1, k), cl, PW(k + 1, k), clw);
+      ZP(gemv)(order, ZO_NOTRANS, n - k, k, ZP(mone), PA(k, 0), lda, PW(k, 0), rlw, ZP(one),
+               PW(k, k), clw);
+      LW(k, k) = ZP(c)(LW(k, k).re, (R)0);
+      int kstep = 1, imax = 0, kp;
+      const R absakk = ZO_ABS(LW(k, k).re);
+      R colmax = 0;
+      if (k < n - 1) {
+        imax = k + 1 + ZP(iamax)(n - k - 1, PW(k + 1, k), clw);
+        colmax = ZP(cabs1)(LW(imax, k));
+      }
+      if (ZO_MAX(absakk, colmax) == (R)0) {
+        if (info == 0) info = k + 1;
+        kp = k;
+        LA(k, k) = ZP(c)(LA(k, k).re, (R)0);
+      } else {
+        if (absakk >= alpha * colmax) {
+          kp = k;
+        } else {
+          ZP(copy)(imax - k, PA(imax, k), rl, PW(k, k + 1), clw);
+          ZP(lacgv)(imax - k, PW(k, k + 1), clw);
+          LW(imax, k + 1) = ZP(c)(LA(imax, imax).re, (R)0);
+          if (imax < n - 1) ZP(copy)(n - imax - 1, PA(imax + 1, imax), cl, PW(imax + 1, k + 1), clw);
+          ZP(gemv)(order, ZO_NOTRANS, n - k, k, ZP(mone), PA(k, 0), lda, PW(imax, 0), rlw, ZP(one),
+                   PW(k, k + 1), clw);
+          LW(imax, k + 1) = ZP(c)(LW(imax, k + 1).re, (R)0);
+          int jmax = k + ZP(iamax)(imax - k, PW(k, k + 1), clw);
+          R rowmax = ZP(cabs1)(LW(jmax, k + 1));
+          if (imax < n - 1) {
+            jmax = imax + 1 + ZP(iamax)(n - imax - 1, PW(imax + 1, k + 1), clw);
+            rowmax = ZO_MAX(rowmax, ZP(cabs1)(LW(jmax, k + 1)));
+          }
+          if (absakk >= alpha * (colmax * (colmax / rowmax))) {
+            kp = k;
+          } else if (ZO_ABS(LW(imax, k + 1).re) >= alpha * rowmax) {
+            kp = imax;
+            ZP(copy)(n - k, PW(k, k + 1), clw, PW(k, k), clw);
+          } else {
+            kp = imax;
+            kstep = 2;
+          }
+        }
+        const int kk = k + kstep - 1;
+        if (kp != kk) {
+          LA(kp, kp) = ZP(c)(LA(kk, kk).re, (R)0);
+          ZP(copy)(kp - kk - 1, PA(kk + 1, kk), cl, PA(kp, kk + 1), rl);
+          ZP(lacgv)(kp - kk - 1, PA(kp, kk + 1), rl);
+          if (kp < n - 1) ZP(copy)(n - kp - 1, PA(kp + 1, kk), cl, PA(kp + 1, kp), cl);
+          if (k > 0) ZP(swapv)(k, PA(kk, 0), rl, PA(kp, 0), rl);
+          ZP(swapv)(kk + 1, PW(kk, 0), rlw, PW(kp, 0), rlw);
+        }
+        if (kstep == 1) {
+          ZP(copy)(n - k, PW(k, k), clw, PA(k, k), cl);
+          if (k < n - 1) {
+            const R r1 = (R)1 / LA(k, k).re;
+            for (int i = k + 1; i < n; ++i) LA(i, k) = ZP(cscale)(LA(i, k), r1);
+            ZP(lacgv)(n - k - 1, PW(k + 1, k), clw);
+          }
+        } else {
+          if (k < n - 2) {
+            ZT d21 = LW(k + 1, k);
+            const ZT d11 = ZP(cdiv)(LW(k + 1, k + 1), d21);
+            const ZT d22 = ZP(cdiv)(LW(k, k), ZP(cconj)(d21));
+            const R t = (R)1 / (ZP(cmul)(d11, d22).re - (R)1);
+            d21 = ZP(crdiv)(t, d21);
+            for (int j = k + 2; j < n; ++j) {
+              LA(j, k) = ZP(cmul)(ZP(cconj)(d21), ZP(csub)(ZP(cmul)(d11, LW(j, k)), LW(j, k + 1)));
+              LA(j, k + 1) = ZP(cmul)(d21, ZP(csub)(ZP(cmul)(d22, LW(j, k + 1)), LW(j, k)));
+            }
+          }
+          LA(k, k) = LW(k, k);
+          LA(k + 1, k) = LW(k + 1, k);
+          LA(k + 1, k + 1) = LW(k + 1, k + 1);
+          ZP(lacgv)(n - k - 1, PW(k + 1, k), clw);
+          ZP(lacgv)(n - k - 2, PW(k + 2, k + 1), clw);
+        }
+      }
+      if (kstep == 1) {
+        ipiv[k] = kp + 1;
+      } else {
+        ipiv[k] = -(kp + 1);
+        ipiv[k + 1] = -(kp + 1);
+      }
+      k += kstep;
+    }
+    ZP(gemmtr)(order, ZO_LOWER, ZO_NOTRANS, ZO_TRANS, n - k, k, ZP(mone), PA(k, 0), lda, PW(k, 0),
+               ldw, ZP(one), PA(k, k), lda);
+    int j = k - 1;
+    while (j > 0) {
+      const int jj = j;
+      int jp = ipiv[j];
+      if (jp < 0) {
+        jp = -jp;
+        j -= 1;
+      }
+      j -= 1;
+      if (jp - 1 != jj && j >= 0) ZP(swapv)(j + 1, PA(jp - 1, 0), rl, PA(jj, 0), rl);
+    }
+    *kb = k;
+  }
+#undef LA
+#undef LW
+#undef PA
+#undef PW
+  return info;
+}
+
+/* lapack/hetrf.zig:17-187: blocks of nb = ilaenv("CHETRF") = 64 by lahef
+ * while more than nb columns remain, the rest by hetf2 (LAPACK zhetrf). */
+int ZP(hetrf)(int order, int uplo, int n, ZT *a, int lda, int *ipiv, ZT *work, int lwork) {
+  if (n < 0 || lda < ZO_MAX(1, n) || (lwork < 1 && lwork != -1)) return ZO_EINVAL;
+  int info = 0;
+  int nb = zo_ilaenv(1, "CHETRF", n, -1, -1, -1);
+  work[0] = ZP(c)((R)ZO_MAX(1, n * nb), (R)0);
+  if (lwork == -1) return info;
+  int nbmin = 2;
+  const int ldwork = order == ZO_COL ? n : nb;
+  if (nb > 1 && nb < n && lwork < ldwork * nb) {
+    nb = ZO_MAX(lwork / ldwork, 1);
+    nbmin = ZO_MAX(2, zo_ilaenv(2, "DSYTRF", n, -1, -1, -1));
+  }
+  if (nb < nbmin) nb = n;
+  if (uplo == ZO_UPPER) {
+    int k = n - 1;
+    while (k >= 0) {
+      int kb, iinfo;
+      if (k + 1 > nb) {
+        iinfo = ZP(lahef)(order, ZO_UPPER, k + 1, nb, &kb, a, lda, ipiv, work, ldwork);
+      } else {
+        iinfo = ZP(hetf2)(order, ZO_UPPER, k + 1, a, lda, ipiv);
+        kb = k + 1;
+      }
+      if (info == 0 && iinfo > 0) info = iinfo;
+      k -= kb;
+    }
+  } else {
+    int k = 0;
+    while (k < n) {
+      int kb, iinfo;
+      if (k <= n - nb - 1) {
+        iinfo = ZP(lahef)(order, ZO_LOWER, n - k, nb, &kb, a + zo_index(order, k, k, lda), lda,
+                          ipiv + k, work, ldwork);
+      } else {
+        iinfo = ZP(hetf2)(order, ZO_LOWER, n - k, a + zo_index(order, k, k, lda), lda, ipiv + k);
+        kb = n - k;
+      }
+      if (info == 0 && iinfo > 0) info = iinfo + k;
+      for (int j = k; j < k + kb; ++j) ipiv[j] = ipiv[j] > 0 ? ipiv[j] + k : ipiv[j] - k;
+      k += kb;
+    }
+  }
+  return info;
+}

@@ -52,6 +52,7 @@ int zo_ilaenv(int ispec, const char *name, int n1, int n2, int n3, int n4) {
     if (!strncmp(c2, "GE", 2) && !strncmp(c3, "QRF", 3)) return 32;
     if (!strncmp(c2, "OR", 2) && !strncmp(c3, "GQR", 3)) return 32;
     if (!strncmp(c2, "SY", 2) && !strncmp(c3, "TRF", 3)) return 64;
+    if (!strncmp(c2, "HE", 2) && !strncmp(c3, "TRF", 3)) return 64; /* ilaenv.zig:255-261 */
     return 1;
   }
   if (ispec == 2) {

@@ -141,7 +141,10 @@ void zo_set_cdiv_as_written(int on);
                const Z *v, int ldv, const Z *t, int ldt, Z *c, int ldc, Z *work, int ldwork); \
   int P##geqrf(int order, int m, int n, Z *a, int lda, Z *tau, Z *work, int lwork);          \
   int P##her(int order, int uplo, int n, R alpha, const Z *x, int incx, Z *a, int lda);       \
-  int P##hetf2(int order, int uplo, int n, Z *a, int lda, int *ipiv);
+  int P##hetf2(int order, int uplo, int n, Z *a, int lda, int *ipiv);                         \
+  int P##lahef(int order, int uplo, int n, int nb, int *kb, Z *a, int lda, int *ipiv, Z *w,   \
+               int ldw);                                                                      \
+  int P##hetrf(int order, int uplo, int n, Z *a, int lda, int *ipiv, Z *work, int lwork);
 
 ZO_ZDECL(zo_cf64, double, zo_z_)
 ZO_ZDECL(zo_cf32, float, zo_c_)

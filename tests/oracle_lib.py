@@ -103,6 +103,7 @@ def load():
                 "geqrf": (i32, [i32, i32, i32, vp, i32, vp, vp, i32]),
                 "her": (i32, [i32, i32, i32, R, vp, i32, vp, i32]),
                 "hetf2": (i32, [i32, i32, i32, vp, i32, vp]),
+                "hetrf": (i32, [i32, i32, i32, vp, i32, vp, vp, i32]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(_lib, pfx + name)

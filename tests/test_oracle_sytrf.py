@@ -5,9 +5,10 @@ dsytf2 (lapack/sytrf.zig, lasyf.zig, sytf2.zig), so the oracle is pinned
 against scipy's bundled LAPACK running the same algorithm: identical ipiv
 (the 1x1 / 2x2 pivot blocks and interchanges) and factors to rounding, below
 (unblocked) and above (blocked, nb = 64) the block size, both triangles; and
-the factors solve A x = b through LAPACK's own dsytrs.  The Hermitian form
-(hetf2, unblocked) is pinned the same way against zhetrf, which runs zhetf2
-itself up to nb = 64 columns, and through zhetrs beyond.
+the factors solve A x = b through LAPACK's own dsytrs.  The Hermitian form is
+pinned the same way against zhetrf: hetf2 alone (which zhetrf runs itself up
+to nb = 64 columns, and which solves through zhetrs beyond), and the blocked
+hetrf over lahef at every size.
 """
 import numpy as np
 import pytest
@@ -106,3 +107,69 @@ def test_zhetf2_solves_through_zhetrs(uplo):
     sol, inf = lap.zhetrs(f, ipiv, a @ x, lower=int(uplo == 122))
     assert inf == 0
     np.testing.assert_allclose(sol, x, rtol=1e-9, atol=1e-9)
+
+
+def zhetrf(a, uplo, order=102):
+    n = a.shape[0]
+    f = a.copy(order="F") if order == 102 else a.copy(order="C")
+    ipiv = np.zeros(n, dtype=np.int32)
+    lw = max(1, n * 64)
+    work = np.zeros(lw, dtype=np.complex128)
+    info = ol.fn("hetrf", np.complex128)(order, uplo, n, ol.ptr(f), max(1, n), ol.ptr(ipiv),
+                                         ol.ptr(work), lw)
+    return f, ipiv, info
+
+
+@pytest.mark.parametrize("uplo", [121, 122])
+@pytest.mark.parametrize("n", [1, 20, 64, 65, 150, 200])
+def test_zhetrf_blocked_equals_lapack(n, uplo):
+    """hetrf over lahef (nb = 64 columns a block) against LAPACK's zhetrf,
+    which runs zlahef the same way: identical pivots, factors to rounding."""
+    a = herm(n, seed=7 * n + uplo)
+    f, ipiv, info = zhetrf(a, uplo)
+    ldu, ipiv2, info2 = lap.zhetrf(a, lower=int(uplo == 122))
+    assert info == info2 == 0
+    np.testing.assert_array_equal(ipiv, ipiv2)
+    tri = np.triu if uplo == 121 else np.tril
+    assert np.abs(tri(f) - tri(ldu)).max() <= 1e-10 * max(1.0, np.abs(ldu).max())
+    x = np.random.default_rng(n).standard_normal((n, 2)) + 0j
+    sol, inf = lap.zhetrs(f, ipiv, a @ x, lower=int(uplo == 122))
+    assert inf == 0
+    np.testing.assert_allclose(sol, x, rtol=1e-8, atol=1e-8)
+
+
+def test_zhetrf_row_major_same_pivots():
+    a = herm(130, seed=4)
+    fc, pc, _ = zhetrf(a, 122)
+    fr, pr, _ = zhetrf(a, 122, order=101)
+    np.testing.assert_array_equal(pc, pr)
+    np.testing.assert_allclose(np.tril(fr), np.tril(fc), rtol=0, atol=1e-11 * np.abs(fc).max())
+
+
+def test_zhetrf_zero_column_info():
+    a = herm(100, seed=9)
+    a[70, :] = 0
+    a[:, 70] = 0
+    _, _, info = zhetrf(a, 121)
+    _, _, info2 = lap.zhetrf(a, lower=0)
+    assert info == info2 > 0
+
+
+def test_ilaenv_hetrf():
+    assert ol.load().zo_ilaenv(1, b"CHETRF", 500, -1, -1, -1) == 64
+
+
+def test_zhetrf_as_written_quotient_breaks_the_factor():
+    """lahef's 2x2 step computes d21 = t / d21, a real by complex quotient;
+    zml's cfloat returns y / x for it, and with that the blocked factor of a
+    150 x 150 Hermitian matrix no longer solves (a zero pivot appears)."""
+    a = herm(150, seed=1)
+    lib = ol.load()
+    lib.zo_set_cdiv_as_written(1)
+    try:
+        f, ipiv, info = zhetrf(a, 122)
+    finally:
+        lib.zo_set_cdiv_as_written(0)
+    x = np.ones((150, 1)) + 0j
+    sol, _ = lap.zhetrs(f, ipiv, a @ x, lower=1)
+    assert info > 0 or not np.allclose(sol, x)
