@@ -55,7 +55,7 @@ int P(syr)(int order, int uplo, int n, T alpha, const T *x, int incx, T *a, int 
   return P(k_syr)(uplo == ZO_UPPER ? ZO_LOWER : ZO_UPPER, n, alpha, x, incx, a, lda);
 }
 
-/* blas/gemmtr.zig:60-1000 (k_gemmtr): the uplo triangle of
+/* blas/gemmtr.zig:69-1032 (k_gemmtr): the uplo triangle of
  * C := alpha op(A) op(B) + beta C (C n x n, inner dimension k), gemm's four
  * loop forms with the row range cut to the triangle; row-major inverts uplo
  * and swaps the operands (gemmtr.zig:30-64). */

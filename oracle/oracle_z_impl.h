@@ -1763,3 +1763,466 @@ int ZP(hetrf)(int order, int uplo, int n, ZT *a, int lda, int *ipiv, ZT *work, i
   }
   return info;
 }
+
+/* ---- complex symmetric Bunch-Kaufman (sytrf over lasyf / sytf2) ------------ */
+/* The same routines as the real ones, instantiated for cfloat: A = U D U^T or
+ * L D L^T without conjugation, pivots chosen by |re| + |im|.  zml's scalar
+ * "1 / z" (the 1x1 step's r1, the 2x2 step's t) is a real by complex
+ * quotient and goes through crdiv; sub(z, 1) is component-wise. */
+
+static inline ZT ZP(sub1)(ZT z) { return ZP(c)(z.re - (R)1, z.im); }
+
+/* blas/syr.zig:19-210 (complex): A := alpha x x^T + A on the uplo triangle,
+ * column j skipped when x[j] == 0; row-major inverts uplo. */
+static int ZP(k_syr)(int uplo, int n, ZT alpha, const ZT *x, int incx, ZT *a, int lda) {
+  if (n < 0 || lda < ZO_MAX(1, n) || incx == 0) return ZO_EINVAL;
+  if (n == 0 || ZP(cis0)(alpha)) return 0;
+  const long kx = incx < 0 ? (long)(-n + 1) * incx : 0;
+  long jx = kx;
+#define YA(i, j) a[(long)(i) + (long)(j) * lda]
+  for (int j = 0; j < n; ++j) {
+    if (!ZP(cis0)(x[jx])) {
+      const ZT temp = ZP(cmul)(x[jx], alpha);
+      if (uplo == ZO_UPPER) {
+        long ix = kx;
+        for (int i = 0; i < j; ++i) {
+          YA(i, j) = ZP(cadd)(YA(i, j), ZP(cmul)(x[ix], temp));
+          ix += incx;
+        }
+        YA(j, j) = ZP(cadd)(YA(j, j), ZP(cmul)(x[jx], temp));
+      } else {
+        YA(j, j) = ZP(cadd)(YA(j, j), ZP(cmul)(x[jx], temp));
+        long ix = jx;
+        for (int i = j + 1; i < n; ++i) {
+          ix += incx;
+          YA(i, j) = ZP(cadd)(YA(i, j), ZP(cmul)(x[ix], temp));
+        }
+      }
+    }
+    jx += incx;
+  }
+#undef YA
+  return 0;
+}
+int ZP(syr)(int order, int uplo, int n, ZT alpha, const ZT *x, int incx, ZT *a, int lda) {
+  return ZP(k_syr)(order == ZO_COL ? uplo : (uplo == ZO_UPPER ? ZO_LOWER : ZO_UPPER), n, alpha, x,
+                   incx, a, lda);
+}
+
+#define YA(i, j) a[zo_index(order, (i), (j), lda)]
+#define YW(i, j) w[zo_index(order, (i), (j), ldw)]
+#define QA(i, j) (a + zo_index(order, (i), (j), lda))
+#define QW(i, j) (w + zo_index(order, (i), (j), ldw))
+
+/* lapack/sytf2.zig:13-522 (complex): unblocked Bunch-Kaufman (LAPACK
+ * zsytf2); a zero or NaN pivot column records info and is left as it is. */
+int ZP(sytf2)(int order, int uplo, int n, ZT *a, int lda, int *ipiv) {
+  if (n < 0 || lda < ZO_MAX(1, n)) return ZO_EINVAL;
+  int info = 0;
+  const R alpha = ((R)1 + ZO_SQRT((R)17)) / (R)8;
+  const int cl = order == ZO_COL ? 1 : lda, rl = order == ZO_COL ? lda : 1;
+  if (uplo == ZO_UPPER) {
+    int k = n - 1;
+    while (k >= 0) {
+      int kstep = 1, kp, imax = 0;
+      const R absakk = ZP(cabs1)(YA(k, k));
+      R colmax = 0;
+      if (k > 0) {
+        imax = ZP(iamax)(k, QA(0, k), cl);
+        colmax = ZP(cabs1)(YA(imax, k));
+      }
+      if (ZO_MAX(absakk, colmax) == (R)0 || absakk != absakk) {
+        if (info == 0) info = k + 1;
+        kp = k;
+      } else {
+        if (absakk >= alpha * colmax) {
+          kp = k;
+        } else {
+          int jmax = imax + 1 + ZP(iamax)(k - imax, QA(imax, imax + 1), rl);
+          R rowmax = ZP(cabs1)(YA(imax, jmax));
+          if (imax > 0) {
+            jmax = ZP(iamax)(imax, QA(0, imax), cl);
+            rowmax = ZO_MAX(rowmax, ZP(cabs1)(YA(jmax, imax)));
+          }
+          if (absakk >= alpha * (colmax * (colmax / rowmax))) {
+            kp = k;
+          } else if (ZP(cabs1)(YA(imax, imax)) >= alpha * rowmax) {
+            kp = imax;
+          } else {
+            kp = imax;
+            kstep = 2;
+          }
+        }
+        const int kk = k - kstep + 1;
+        if (kp != kk) {
+          ZP(swapv)(kp, QA(0, kk), cl, QA(0, kp), cl);
+          ZP(swapv)(kk - kp - 1, QA(kp + 1, kk), cl, QA(kp, kp + 1), rl);
+          ZT t = YA(kk, kk);
+          YA(kk, kk) = YA(kp, kp);
+          YA(kp, kp) = t;
+          if (kstep == 2) {
+            t = YA(k - 1, k);
+            YA(k - 1, k) = YA(kp, k);
+            YA(kp, k) = t;
+          }
+        }
+        if (kstep == 1) {
+          const ZT r1 = ZP(crdiv)((R)1, YA(k, k));
+          ZP(syr)(order, uplo, k, ZP(c)(-r1.re, -r1.im), QA(0, k), cl, a, lda);
+          ZP(scal)(k, r1, QA(0, k), cl);
+        } else if (k > 1) {
+          ZT d12 = YA(k - 1, k);
+          const ZT d22 = ZP(cdiv)(YA(k - 1, k - 1), d12);
+          const ZT d11 = ZP(cdiv)(YA(k, k), d12);
+          const ZT t = ZP(crdiv)((R)1, ZP(sub1)(ZP(cmul)(d11, d22)));
+          d12 = ZP(cdiv)(t, d12);
+          for (int j = k - 2; j >= 0; --j) {
+            const ZT wkm1 = ZP(cmul)(d12, ZP(csub)(ZP(cmul)(d11, YA(j, k - 1)), YA(j, k)));
+            const ZT wk = ZP(cmul)(d12, ZP(csub)(ZP(cmul)(d22, YA(j, k)), YA(j, k - 1)));
+            for (int i = j; i >= 0; --i)
+              YA(i, j) = ZP(csub)(YA(i, j), ZP(cadd)(ZP(cmul)(YA(i, k), wk), ZP(cmul)(YA(i, k - 1), wkm1)));
+            YA(j, k) = wk;
+            YA(j, k - 1) = wkm1;
+          }
+        }
+      }
+      if (kstep == 1) {
+        ipiv[k] = kp + 1;
+      } else {
+        ipiv[k] = -(kp + 1);
+        ipiv[k - 1] = -(kp + 1);
+      }
+      k -= kstep;
+    }
+  } else {
+    int k = 0;
+    while (k < n) {
+      int kstep = 1, kp, imax = 0;
+      const R absakk = ZP(cabs1)(YA(k, k));
+      R colmax = 0;
+      if (k < n - 1) {
+        imax = k + 1 + ZP(iamax)(n - k - 1, QA(k + 1, k), cl);
+        colmax = ZP(cabs1)(YA(imax, k));
+      }
+      if (ZO_MAX(absakk, colmax) == (R)0 || absakk != absakk) {
+        if (info == 0) info = k + 1;
+        kp = k;
+      } else {
+        if (absakk >= alpha * colmax) {
+          kp = k;
+        } else {
+          int jmax = k + ZP(iamax)(imax - k, QA(imax, k), rl);
+          R rowmax = ZP(cabs1)(YA(imax, jmax));
+          if (imax < n - 1) {
+            jmax = imax + 1 + ZP(iamax)(n - imax - 1, QA(imax + 1, imax), cl);
+            rowmax = ZO_MAX(rowmax, ZP(cabs1)(YA(jmax, imax)));
+          }
+          if (absakk >= alpha * (colmax * (colmax / rowmax))) {
+            kp = k;
+          } else if (ZP(cabs1)(YA(imax, imax)) >= alpha * rowmax) {
+            kp = imax;
+          } else {
+            kp = imax;
+            kstep = 2;
+          }
+        }
+        const int kk = k + kstep - 1;
+        if (kp != kk) {
+          if (kp < n - 1) ZP(swapv)(n - kp - 1, QA(kp + 1, kk), cl, QA(kp + 1, kp), cl);
+          ZP(swapv)(kp - kk - 1, QA(kk + 1, kk), cl, QA(kp, kk + 1), rl);
+          ZT t = YA(kk, kk);
+          YA(kk, kk) = YA(kp, kp);
+          YA(kp, kp) = t;
+          if (kstep == 2) {
+            t = YA(k + 1, k);
+            YA(k + 1, k) = YA(kp, k);
+            YA(kp, k) = t;
+          }
+        }
+        if (kstep == 1) {
+          if (k < n - 1) {
+            const ZT d11 = ZP(crdiv)((R)1, YA(k, k));
+            ZP(syr)(order, uplo, n - k - 1, ZP(c)(-d11.re, -d11.im), QA(k + 1, k), cl,
+                    QA(k + 1, k + 1), lda);
+            ZP(scal)(n - k - 1, d11, QA(k + 1, k), cl);
+          }
+        } else if (k < n - 2) {
+          ZT d21 = YA(k + 1, k);
+          const ZT d11 = ZP(cdiv)(YA(k + 1, k + 1), d21);
+          const ZT d22 = ZP(cdiv)(YA(k, k), d21);
+          const ZT t = ZP(crdiv)((R)1, ZP(sub1)(ZP(cmul)(d11, d22)));
+          d21 = ZP(cdiv)(t, d21);
+          for (int j = k + 2; j < n; ++j) {
+            const ZT wk = ZP(cmul)(d21, ZP(csub)(ZP(cmul)(d11, YA(j, k)), YA(j, k + 1)));
+            const ZT wkp1 = ZP(cmul)(d21, ZP(csub)(ZP(cmul)(d22, YA(j, k + 1)), YA(j, k)));
+            for (int i = j; i < n; ++i)
+              YA(i, j) = ZP(csub)(YA(i, j), ZP(cadd)(ZP(cmul)(YA(i, k), wk), ZP(cmul)(YA(i, k + 1), wkp1)));
+            YA(j, k) = wk;
+            YA(j, k + 1) = wkp1;
+          }
+        }
+      }
+      if (kstep == 1) {
+        ipiv[k] = kp + 1;
+      } else {
+        ipiv[k] = -(kp + 1);
+        ipiv[k + 1] = -(kp + 1);
+      }
+      k += kstep;
+    }
+  }
+  return info;
+}
+
+/* lapack/lasyf.zig:14-896 (complex, LAPACK zlasyf with gemmtr): up to nb
+ * columns with W = U12 D or L21 D built alongside, the rest of the triangle
+ * updated by gemmtr, the later interchanges undone; *kb = columns factored. */
+int ZP(lasyf)(int order, int uplo, int n, int nb, int *kb, ZT *a, int lda, int *ipiv, ZT *w,
+              int ldw) {
+  int info = 0;
+  const R alpha = ((R)1 + ZO_SQRT((R)17)) / (R)8;
+  const int cl = order == ZO_COL ? 1 : lda, rl = order == ZO_COL ? lda : 1;
+  const int clw = order == ZO_COL ? 1 : ldw, rlw = order == ZO_COL ? ldw : 1;
+  if (uplo == ZO_UPPER) {
+    int k = n - 1, kw;
+    while (1) {
+      kw = nb + k - n;
+      if ((k <= n - nb && nb < n) || k < 0) break;
+      ZP(copy)(k + 1, QA(0, k), cl, QW(0, kw), clw);
+      if (k < n - 1)
+        ZP(gemv)(order, ZO_NOTRANS, k + 1, n - (k + 1), ZP(mone), QA(0, k + 1), lda, QW(k, kw + 1),
+                 rlw, ZP(one), QW(0, kw), clw);
+      int kstep = 1, imax = 0, kp;
+      const R absakk = ZP(cabs1)(YW(k, kw));
+      R colmax = 0;
+      if (k > 0) {
+        imax = ZP(iamax)(k, QW(0, kw), clw);
+        colmax = ZP(cabs1)(YW(imax, kw));
+      }
+      if (ZO_MAX(absakk, colmax) == (R)0) {
+        if (info == 0) info = k + 1;
+        kp = k;
+      } else {
+        if (absakk >= alpha * colmax) {
+          kp = k;
+        } else {
+          ZP(copy)(imax + 1, QA(0, imax), cl, QW(0, kw - 1), clw);
+          ZP(copy)(k - imax, QA(imax, imax + 1), rl, QW(imax + 1, kw - 1), clw);
+          if (k < n - 1)
+            ZP(gemv)(order, ZO_NOTRANS, k + 1, n - (k + 1), ZP(mone), QA(0, k + 1), lda,
+                     QW(imax, kw + 1), rlw, ZP(one), QW(0, kw - 1), clw);
+          int jmax = imax + 1 + ZP(iamax)(k - imax, QW(imax + 1, kw - 1), clw);
+          R rowmax = ZP(cabs1)(YW(jmax, kw - 1));
+          if (imax > 0) {
+            jmax = ZP(iamax)(imax, QW(0, kw - 1), clw);
+            rowmax = ZO_MAX(rowmax, ZP(cabs1)(YW(jmax, kw - 1)));
+          }
+          if (absakk >= alpha * (colmax * (colmax / rowmax))) {
+            kp = k;
+          } else if (ZP(cabs1)(YW(imax, kw - 1)) >= alpha * rowmax) {
+            kp = imax;
+            ZP(copy)(k + 1, QW(0, kw - 1), clw, QW(0, kw), clw);
+          } else {
+            kp = imax;
+            kstep = 2;
+          }
+        }
+        const int kk = k - kstep + 1, kkw = nb + kk - n;
+        if (kp != kk) {
+          YA(kp, kp) = YA(kk, kk);
+          ZP(copy)(kk - kp - 1, QA(kp + 1, kk), cl, QA(kp, kp + 1), rl);
+          if (kp > 0) ZP(copy)(kp, QA(0, kk), cl, QA(0, kp), cl);
+          if (k < n - 1) ZP(swapv)(n - (k + 1), QA(kk, k + 1), rl, QA(kp, k + 1), rl);
+          ZP(swapv)(n - kk, QW(kk, kkw), rlw, QW(kp, kkw), rlw);
+        }
+        if (kstep == 1) {
+          ZP(copy)(k + 1, QW(0, kw), clw, QA(0, k), cl);
+          const ZT r1 = ZP(crdiv)((R)1, YA(k, k));
+          ZP(scal)(k, r1, QA(0, k), cl);
+        } else {
+          if (k > 1) {
+            ZT d21 = YW(k - 1, kw);
+            const ZT d11 = ZP(cdiv)(YW(k, kw), d21);
+            const ZT d22 = ZP(cdiv)(YW(k - 1, kw - 1), d21);
+            const ZT t = ZP(crdiv)((R)1, ZP(sub1)(ZP(cmul)(d11, d22)));
+            d21 = ZP(cdiv)(t, d21);
+            for (int j = 0; j < k - 1; ++j) {
+              YA(j, k - 1) = ZP(cmul)(d21, ZP(csub)(ZP(cmul)(d11, YW(j, kw - 1)), YW(j, kw)));
+              YA(j, k) = ZP(cmul)(d21, ZP(csub)(ZP(cmul)(d22, YW(j, kw)), YW(j, kw - 1)));
+            }
+          }
+          YA(k - 1, k - 1) = YW(k - 1, kw - 1);
+          YA(k - 1, k) = YW(k - 1, kw);
+          YA(k, k) = YW(k, kw);
+        }
+      }
+      if (kstep == 1) {
+        ipiv[k] = kp + 1;
+      } else {
+        ipiv[k] = -(kp + 1);
+        ipiv[k - 1] = -(kp + 1);
+      }
+      k -= kstep;
+    }
+    ZP(gemmtr)(order, ZO_UPPER, ZO_NOTRANS, ZO_TRANS, k + 1, n - (k + 1), ZP(mone), QA(0, k + 1),
+               lda, QW(0, kw + 1), ldw, ZP(one), a, lda);
+    int j = k + 1;
+    while (j < n) {
+      const int jj = j;
+      int jp = ipiv[j];
+      if (jp < 0) {
+        jp = -jp;
+        j += 1;
+      }
+      j += 1;
+      if (jp - 1 != jj && j < n) ZP(swapv)(n - j, QA(jp - 1, j), rl, QA(jj, j), rl);
+    }
+    *kb = n - k - 1;
+  } else {
+    int k = 0;
+    while (1) {
+      if ((k >= nb - 1 && nb < n) || k > n - 1) break;
+      ZP(copy)(n - k, QA(k, k), cl, QW(k, k), clw);
+      ZP(gemv)(order, ZO_NOTRANS, n - k, k, ZP(mone), QA(k, 0), lda, QW(k, 0), rlw, ZP(one),
+               QW(k, k), clw);
+      int kstep = 1, imax = 0, kp;
+      const R absakk = ZP(cabs1)(YW(k, k));
+      R colmax = 0;
+      if (k < n - 1) {
+        imax = k + 1 + ZP(iamax)(n - k - 1, QW(k + 1, k), clw);
+        colmax = ZP(cabs1)(YW(imax, k));
+      }
+      if (ZO_MAX(absakk, colmax) == (R)0) {
+        if (info == 0) info = k + 1;
+        kp = k;
+      } else {
+        if (absakk >= alpha * colmax) {
+          kp = k;
+        } else {
+          ZP(copy)(imax - k, QA(imax, k), rl, QW(k, k + 1), clw);
+          ZP(copy)(n - imax, QA(imax, imax), cl, QW(imax, k + 1), clw);
+          ZP(gemv)(order, ZO_NOTRANS, n - k, k, ZP(mone), QA(k, 0), lda, QW(imax, 0), rlw, ZP(one),
+                   QW(k, k + 1), clw);
+          int jmax = k + ZP(iamax)(imax - k, QW(k, k + 1), clw);
+          R rowmax = ZP(cabs1)(YW(jmax, k + 1));
+          if (imax < n - 1) {
+            jmax = imax + 1 + ZP(iamax)(n - imax - 1, QW(imax + 1, k + 1), clw);
+            rowmax = ZO_MAX(rowmax, ZP(cabs1)(YW(jmax, k + 1)));
+          }
+          if (absakk >= alpha * (colmax * (colmax / rowmax))) {
+            kp = k;
+          } else if (ZP(cabs1)(YW(imax, k + 1)) >= alpha * rowmax) {
+            kp = imax;
+            ZP(copy)(n - k, QW(k, k + 1), clw, QW(k, k), clw);
+          } else {
+            kp = imax;
+            kstep = 2;
+          }
+        }
+        const int kk = k + kstep - 1;
+        if (kp != kk) {
+          YA(kp, kp) = YA(kk, kk);
+          ZP(copy)(kp - kk - 1, QA(kk + 1, kk), cl, QA(kp, kk + 1), rl);
+          if (kp < n - 1) ZP(copy)(n - kp - 1, QA(kp + 1, kk), cl, QA(kp + 1, kp), cl);
+          if (k > 0) ZP(swapv)(k, QA(kk, 0), rl, QA(kp, 0), rl);
+          ZP(swapv)(kk + 1, QW(kk, 0), rlw, QW(kp, 0), rlw);
+        }
+        if (kstep == 1) {
+          ZP(copy)(n - k, QW(k, k), clw, QA(k, k), cl);
+          if (k < n - 1) {
+            const ZT r1 = ZP(crdiv)((R)1, YA(k, k));
+            ZP(scal)(n - k - 1, r1, QA(k + 1, k), cl);
+          }
+        } else {
+          if (k < n - 2) {
+            ZT d21 = YW(k + 1, k);
+            const ZT d11 = ZP(cdiv)(YW(k + 1, k + 1), d21);
+            const ZT d22 = ZP(cdiv)(YW(k, k), d21);
+            const ZT t = ZP(crdiv)((R)1, ZP(sub1)(ZP(cmul)(d11, d22)));
+            d21 = ZP(cdiv)(t, d21);
+            for (int j = k + 2; j < n; ++j) {
+              YA(j, k) = ZP(cmul)(d21, ZP(csub)(ZP(cmul)(d11, YW(j, k)), YW(j, k + 1)));
+              YA(j, k + 1) = ZP(cmul)(d21, ZP(csub)(ZP(cmul)(d22, YW(j, k + 1)), YW(j, k)));
+            }
+          }
+          YA(k, k) = YW(k, k);
+          YA(k + 1, k) = YW(k + 1, k);
+          YA(k + 1, k + 1) = YW(k + 1, k + 1);
+        }
+      }
+      if (kstep == 1) {
+        ipiv[k] = kp + 1;
+      } else {
+        ipiv[k] = -(kp + 1);
+        ipiv[k + 1] = -(kp + 1);
+      }
+      k += kstep;
+    }
+    ZP(gemmtr)(order, ZO_LOWER, ZO_NOTRANS, ZO_TRANS, n - k, k, ZP(mone), QA(k, 0), lda, QW(k, 0),
+               ldw, ZP(one), QA(k, k), lda);
+    int j = k - 1;
+    while (j > 0) {
+      const int jj = j;
+      int jp = ipiv[j];
+      if (jp < 0) {
+        jp = -jp;
+        j -= 1;
+      }
+      j -= 1;
+      if (jp - 1 != jj && j >= 0) ZP(swapv)(j + 1, QA(jp - 1, 0), rl, QA(jj, 0), rl);
+    }
+    *kb = k;
+  }
+  return info;
+}
+#undef YA
+#undef YW
+#undef QA
+#undef QW
+
+/* lapack/sytrf.zig:17-187 (complex): blocks of nb = ilaenv("DSYTRF") = 64 by
+ * lasyf while more than nb columns remain, the rest by sytf2 (LAPACK zsytrf). */
+int ZP(sytrf)(int order, int uplo, int n, ZT *a, int lda, int *ipiv, ZT *work, int lwork) {
+  if (n < 0 || lda < ZO_MAX(1, n) || (lwork < 1 && lwork != -1)) return ZO_EINVAL;
+  int info = 0;
+  int nb = zo_ilaenv(1, "DSYTRF", n, -1, -1, -1);
+  work[0] = ZP(c)((R)ZO_MAX(1, n * nb), (R)0);
+  if (lwork == -1) return info;
+  int nbmin = 2;
+  const int ldwork = order == ZO_COL ? n : nb;
+  if (nb > 1 && nb < n && lwork < ldwork * nb) {
+    nb = ZO_MAX(lwork / ldwork, 1);
+    nbmin = ZO_MAX(2, zo_ilaenv(2, "DSYTRF", n, -1, -1, -1));
+  }
+  if (nb < nbmin) nb = n;
+  if (uplo == ZO_UPPER) {
+    int k = n - 1;
+    while (k >= 0) {
+      int kb, iinfo;
+      if (k + 1 > nb) {
+        iinfo = ZP(lasyf)(order, ZO_UPPER, k + 1, nb, &kb, a, lda, ipiv, work, ldwork);
+      } else {
+        iinfo = ZP(sytf2)(order, ZO_UPPER, k + 1, a, lda, ipiv);
+        kb = k + 1;
+      }
+      if (info == 0 && iinfo > 0) info = iinfo;
+      k -= kb;
+    }
+  } else {
+    int k = 0;
+    while (k < n) {
+      int kb, iinfo;
+      if (k <= n - nb - 1) {
+        iinfo = ZP(lasyf)(order, ZO_LOWER, n - k, nb, &kb, a + zo_index(order, k, k, lda), lda,
+                          ipiv + k, work, ldwork);
+      } else {
+        iinfo = ZP(sytf2)(order, ZO_LOWER, n - k, a + zo_index(order, k, k, lda), lda, ipiv + k);
+        kb = n - k;
+      }
+      if (info == 0 && iinfo > 0) info = iinfo + k;
+      for (int j = k; j < k + kb; ++j) ipiv[j] = ipiv[j] > 0 ? ipiv[j] + k : ipiv[j] - k;
+      k += kb;
+    }
+  }
+  return info;
+}

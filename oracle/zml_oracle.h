@@ -144,7 +144,12 @@ void zo_set_cdiv_as_written(int on);
   int P##hetf2(int order, int uplo, int n, Z *a, int lda, int *ipiv);                         \
   int P##lahef(int order, int uplo, int n, int nb, int *kb, Z *a, int lda, int *ipiv, Z *w,   \
                int ldw);                                                                      \
-  int P##hetrf(int order, int uplo, int n, Z *a, int lda, int *ipiv, Z *work, int lwork);
+  int P##hetrf(int order, int uplo, int n, Z *a, int lda, int *ipiv, Z *work, int lwork);      \
+  int P##syr(int order, int uplo, int n, Z alpha, const Z *x, int incx, Z *a, int lda);        \
+  int P##sytf2(int order, int uplo, int n, Z *a, int lda, int *ipiv);                         \
+  int P##lasyf(int order, int uplo, int n, int nb, int *kb, Z *a, int lda, int *ipiv, Z *w,   \
+               int ldw);                                                                      \
+  int P##sytrf(int order, int uplo, int n, Z *a, int lda, int *ipiv, Z *work, int lwork);
 
 ZO_ZDECL(zo_cf64, double, zo_z_)
 ZO_ZDECL(zo_cf32, float, zo_c_)

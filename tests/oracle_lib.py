@@ -104,6 +104,8 @@ def load():
                 "her": (i32, [i32, i32, i32, R, vp, i32, vp, i32]),
                 "hetf2": (i32, [i32, i32, i32, vp, i32, vp]),
                 "hetrf": (i32, [i32, i32, i32, vp, i32, vp, vp, i32]),
+                "sytf2": (i32, [i32, i32, i32, vp, i32, vp]),
+                "sytrf": (i32, [i32, i32, i32, vp, i32, vp, vp, i32]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(_lib, pfx + name)
@@ -168,14 +170,15 @@ def potrs(l, b, uplo=122):
 
 def sytrf(a, uplo=122, order=102):
     """Bunch-Kaufman factorization of a copy of symmetric `a` (its `uplo`
-    triangle); returns (factor, ipiv, info) in LAPACK's dsytrf conventions."""
+    triangle, real or complex, no conjugation); returns (factor, ipiv, info)
+    in LAPACK's dsytrf / zsytrf conventions."""
     a = np.array(a, dtype=a.dtype, order="F" if order == 102 else "C", copy=True)
     n = a.shape[0]
     ipiv = np.zeros(n, dtype=np.int32)
     f = fn("sytrf", a.dtype)
     q = np.zeros(1, dtype=a.dtype)
     assert f(order, uplo, n, ptr(a), max(1, n), ptr(ipiv), ptr(q), -1) == 0
-    work = np.zeros(max(1, int(q[0])), dtype=a.dtype)
+    work = np.zeros(max(1, int(np.real(q[0]))), dtype=a.dtype)
     info = f(order, uplo, n, ptr(a), max(1, n), ptr(ipiv), ptr(work), work.size)
     return a, ipiv, info
 

@@ -8,7 +8,8 @@ against scipy's bundled LAPACK running the same algorithm: identical ipiv
 the factors solve A x = b through LAPACK's own dsytrs.  The Hermitian form is
 pinned the same way against zhetrf: hetf2 alone (which zhetrf runs itself up
 to nb = 64 columns, and which solves through zhetrs beyond), and the blocked
-hetrf over lahef at every size.
+hetrf over lahef at every size.  Complex symmetric matrices (no conjugation)
+go through the same sytrf over cfloat and are pinned against zsytrf / csytrf.
 """
 import numpy as np
 import pytest
@@ -172,4 +173,60 @@ def test_zhetrf_as_written_quotient_breaks_the_factor():
         lib.zo_set_cdiv_as_written(0)
     x = np.ones((150, 1)) + 0j
     sol, _ = lap.zhetrs(f, ipiv, a @ x, lower=1)
+    assert info > 0 or not np.allclose(sol, x)
+
+
+def csym(n, seed, dtype=np.complex128):
+    rng = np.random.default_rng(seed)
+    g = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    return np.asfortranarray(((g + g.T) / 2).astype(dtype))
+
+
+@pytest.mark.parametrize("uplo", [121, 122])
+@pytest.mark.parametrize("n", [1, 2, 5, 64, 65, 150])
+def test_zsytrf_equals_lapack(n, uplo):
+    """Complex symmetric (not Hermitian) Bunch-Kaufman: the same sytrf /
+    lasyf / sytf2 over cfloat, against LAPACK's zsytrf."""
+    a = csym(n, seed=3 * n + uplo)
+    f, ipiv, info = ol.sytrf(a, uplo)
+    ldu, ipiv2, info2 = lap.zsytrf(a, lower=int(uplo == 122))
+    assert info == info2 == 0
+    np.testing.assert_array_equal(ipiv, ipiv2)
+    tri = np.triu if uplo == 121 else np.tril
+    assert np.abs(tri(f) - tri(ldu)).max() <= 1e-10 * max(1.0, np.abs(ldu).max())
+    x = np.random.default_rng(n).standard_normal((n, 2)) + 0j
+    sol, inf = lap.zsytrs(f, ipiv, a @ x, lower=int(uplo == 122))
+    assert inf == 0
+    np.testing.assert_allclose(sol, x, rtol=1e-8, atol=1e-8)
+
+
+def test_csytrf_equals_lapack():
+    a = csym(100, seed=8, dtype=np.complex64)
+    f, ipiv, _ = ol.sytrf(a, 121)
+    ldu, ipiv2, _ = lap.csytrf(a, lower=0)
+    np.testing.assert_array_equal(ipiv, ipiv2)
+    assert np.abs(np.triu(f) - np.triu(ldu)).max() <= 1e-3 * np.abs(ldu).max()
+
+
+def test_zsytrf_row_major_same_pivots():
+    a = csym(90, seed=12)
+    fc, pc, _ = ol.sytrf(a, 121)
+    fr, pr, _ = ol.sytrf(a, 121, order=101)
+    np.testing.assert_array_equal(pc, pr)
+    np.testing.assert_allclose(np.triu(fr), np.triu(fc), rtol=0, atol=1e-11 * np.abs(fc).max())
+
+
+def test_zsytrf_as_written_quotient_breaks_the_factor():
+    """The 1x1 step scales by div(1, a(k,k)) and the 2x2 step forms
+    t = div(1, d11 d22 - 1), both real by complex; with zml's cfloat
+    quotient as written (y / x) the factor no longer solves."""
+    a = csym(80, seed=2)
+    lib = ol.load()
+    lib.zo_set_cdiv_as_written(1)
+    try:
+        f, ipiv, info = ol.sytrf(a, 122)
+    finally:
+        lib.zo_set_cdiv_as_written(0)
+    x = np.ones((80, 1)) + 0j
+    sol, _ = lap.zsytrs(f, ipiv, a @ x, lower=1)
     assert info > 0 or not np.allclose(sol, x)
