@@ -230,3 +230,25 @@ def test_zsytrf_as_written_quotient_breaks_the_factor():
     x = np.ones((80, 1)) + 0j
     sol, _ = lap.zsytrs(f, ipiv, a @ x, lower=1)
     assert info > 0 or not np.allclose(sol, x)
+
+
+@pytest.mark.parametrize("uplo", [121, 122])
+def test_zsytrf_zero_column_info(uplo):
+    a = csym(100, seed=21)
+    a[30, :] = 0
+    a[:, 30] = 0
+    _, _, info = ol.sytrf(a, uplo)
+    _, _, info2 = lap.zsytrf(a, lower=int(uplo == 122))
+    assert info == info2 > 0
+
+
+@pytest.mark.parametrize("name", ["sytrf", "hetrf"])
+def test_complex_bunch_kaufman_workspace_query_and_empty(name):
+    f = ol.fn(name, np.complex128)
+    q = np.zeros(1, dtype=np.complex128)
+    ipiv = np.zeros(1, dtype=np.int32)
+    a = np.zeros((1, 1), dtype=np.complex128)
+    assert f(102, 122, 300, ol.ptr(a), 300, ol.ptr(ipiv), ol.ptr(q), -1) == 0
+    assert q[0] == 300 * 64
+    assert f(102, 122, 0, ol.ptr(a), 1, ol.ptr(ipiv), ol.ptr(q), 1) == 0
+    assert f(102, 122, 5, ol.ptr(a), 4, ol.ptr(ipiv), ol.ptr(q), 1) < 0  # lda < n
