@@ -3,7 +3,8 @@
  * over libzml_gb300's GPU factorizations, FP64.
  *
  * Mirrors src/linalg/lu.zig (PLU, plu), src/linalg/cholesky.zig (LLT, UTU,
- * llt, utu, cholesky) and src/linalg/qr.zig (QR, qr, QR.q, QR.r): the
+ * llt, utu, cholesky), src/linalg/bunchkaufman.zig (LDLT, UDUT, ldlt, udut,
+ * bunchkaufman) and src/linalg/qr.zig (QR, qr, QR.q, QR.r): the
  * constructor copies the input matrix into storage the factor object owns
  * (host memory, in the input's layout), factors it with the library's GPU
  * LAPACK (getrf / potrf / geqrf, orgqr for Q), and the accessors return
@@ -99,6 +100,50 @@ int zml_dmatvec(const zml_dmatrix *a, const double *x, int incx, double *y, int 
 /* y = x^T b (matmul/dvdge.zig:11, gemv transposed): x has b->rows entries,
  * y b->cols. */
 int zml_dvecmat(const double *x, int incx, const zml_dmatrix *b, double *y, int incy);
+
+/* ---- Bunch-Kaufman: LDLT / UDUT (bunchkaufman.zig:20-179) -------------- */
+#define ZML_ERR_FACTORIZATION_FAILED (-2004) /* linalg.Error.FactorizationFailed */
+/* One object type for both forms; the ldlt_* accessors require a lower
+ * (LDLT) object and the udut_* ones an upper (UDUT) object. */
+typedef struct zml_bk_s zml_ldlt_t;
+typedef struct zml_bk_s zml_udut_t;
+/* ldlt (bunchkaufman.zig:180-443): copies the `uplo` triangle of the n x n
+ * symmetric a into the lower triangle of a packed matrix (copyInverseUplo when
+ * upper-stored) and factors it with dsytrf, A = P L D L^T P^T.  Any info != 0
+ * is ZML_ERR_FACTORIZATION_FAILED and no object is created. */
+int zml_ldlt(int layout, char uplo, int n, const double *a, int lda, zml_ldlt_t **out);
+/* udut (bunchkaufman.zig:445-707): the same into the upper triangle,
+ * A = P U D U^T P^T. */
+int zml_udut(int layout, char uplo, int n, const double *a, int lda, zml_udut_t **out);
+/* bunchkaufman (bunchkaufman.zig:709-726): ldlt for a lower-stored matrix
+ * (*lo set, *up NULL), udut for an upper-stored one (*up set, *lo NULL). */
+int zml_bunchkaufman(int layout, char uplo, int n, const double *a, int lda, zml_ldlt_t **lo,
+                     zml_udut_t **up);
+/* LDLT.init / UDUT.init (bunchkaufman.zig:27-34, 107-114): an object over an
+ * existing dsytrf factor (lower / upper, leading dimension ld) and its ipiv,
+ * both copied (the reference takes ownership of its arguments instead). */
+int zml_ldlt_init(int layout, int n, const double *f, int ld, const int *ipiv, zml_ldlt_t **out);
+int zml_udut_init(int layout, int n, const double *f, int ld, const int *ipiv, zml_udut_t **out);
+void zml_ldlt_deinit(zml_ldlt_t *f);
+void zml_udut_deinit(zml_udut_t *f);
+/* LDLT.p / UDUT.p (:43-55, :123-135): perm (n entries) from the identity by
+ * ipiv's interchanges in factorization order (lpermute / upermute), so that
+ * (P^T A P)(i, j) = A(perm[i], perm[j]); the reference returns the
+ * Permutation over perm transposed. */
+int zml_ldlt_p(const zml_ldlt_t *f, unsigned *perm);
+int zml_udut_p(const zml_udut_t *f, unsigned *perm);
+/* LDLT.l / UDUT.u (:57-72, :137-152): a new owned n x n unit-triangular
+ * matrix in the object's layout (lconvert / uconvert: the multipliers, rows
+ * permuted into P's order; zero outside the triangle, one on the diagonal).
+ * data is NULL when the allocation fails. */
+zml_dmatrix zml_ldlt_l(const zml_ldlt_t *f);
+zml_dmatrix zml_udut_u(const zml_udut_t *f);
+/* LDLT.d / UDUT.d (:74-89, :154-169): the block-diagonal D as a tridiagonal
+ * (sub and sup n-1 entries, diag n), zero between blocks. */
+int zml_ldlt_d(const zml_ldlt_t *f, double *sub, double *diag, double *sup);
+int zml_udut_d(const zml_udut_t *f, double *sub, double *diag, double *sup);
+const int *zml_ldlt_ipiv(const zml_ldlt_t *f);
+const int *zml_udut_ipiv(const zml_udut_t *f);
 
 #ifdef __cplusplus
 }

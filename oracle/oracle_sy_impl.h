@@ -20,7 +20,7 @@ static inline int P(row_ld)(int order, int ld) { return order == ZO_COL ? ld : 1
 #define SYB_(i, j) b[(long)(i) + (long)(j) * ldb]
 #define SYC_(i, j) c[(long)(i) + (long)(j) * ldc]
 
-/* blas/syr.zig:19-210 (k_syr): A := alpha x x^T + A on the uplo triangle;
+/* blas/syr.zig:32-225 (k_syr): A := alpha x x^T + A on the uplo triangle;
  * column j skipped when x[j] == 0; row-major inverts uplo (14-17). */
 static int P(k_syr)(int uplo, int n, T alpha, const T *x, int incx, T *a, int lda) {
   if (n < 0 || lda < ZO_MAX(1, n) || incx == 0) return ZO_EINVAL;
@@ -112,7 +112,7 @@ int P(gemmtr)(int order, int uplo, int transa, int transb, int n, int k, T alpha
                      a, lda, beta, c, ldc);
 }
 
-/* lapack/sytf2.zig:13-522: unblocked Bunch-Kaufman (LAPACK dsytf2), alpha =
+/* lapack/sytf2.zig:17-522: unblocked Bunch-Kaufman (LAPACK dsytf2), alpha =
  * (1 + sqrt(17)) / 8; a zero (or NaN) pivot column records info and is left
  * as it is. */
 int P(sytf2)(int order, int uplo, int n, T *a, int lda, int *ipiv) {
@@ -277,7 +277,7 @@ int P(sytf2)(int order, int uplo, int n, T *a, int lda, int *ipiv) {
   return info;
 }
 
-/* lapack/lasyf.zig:14-896 (LAPACK dlasyf, the trailing update by gemmtr):
+/* lapack/lasyf.zig:17-896 (LAPACK dlasyf, the trailing update by gemmtr):
  * factors up to nb columns (nb - 1 when the last step takes a 2x2 block) at
  * the bottom-right (upper) or top-left (lower) of A, builds W = U12 D or
  * L21 D alongside, updates the rest of the triangle with gemmtr and puts

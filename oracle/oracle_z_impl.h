@@ -1772,7 +1772,7 @@ int ZP(hetrf)(int order, int uplo, int n, ZT *a, int lda, int *ipiv, ZT *work, i
 
 static inline ZT ZP(sub1)(ZT z) { return ZP(c)(z.re - (R)1, z.im); }
 
-/* blas/syr.zig:19-210 (complex): A := alpha x x^T + A on the uplo triangle,
+/* blas/syr.zig:32-225 (complex): A := alpha x x^T + A on the uplo triangle,
  * column j skipped when x[j] == 0; row-major inverts uplo. */
 static int ZP(k_syr)(int uplo, int n, ZT alpha, const ZT *x, int incx, ZT *a, int lda) {
   if (n < 0 || lda < ZO_MAX(1, n) || incx == 0) return ZO_EINVAL;
@@ -1814,7 +1814,7 @@ int ZP(syr)(int order, int uplo, int n, ZT alpha, const ZT *x, int incx, ZT *a, 
 #define QA(i, j) (a + zo_index(order, (i), (j), lda))
 #define QW(i, j) (w + zo_index(order, (i), (j), ldw))
 
-/* lapack/sytf2.zig:13-522 (complex): unblocked Bunch-Kaufman (LAPACK
+/* lapack/sytf2.zig:17-522 (complex): unblocked Bunch-Kaufman (LAPACK
  * zsytf2); a zero or NaN pivot column records info and is left as it is. */
 int ZP(sytf2)(int order, int uplo, int n, ZT *a, int lda, int *ipiv) {
   if (n < 0 || lda < ZO_MAX(1, n)) return ZO_EINVAL;
@@ -1974,7 +1974,7 @@ int ZP(sytf2)(int order, int uplo, int n, ZT *a, int lda, int *ipiv) {
   return info;
 }
 
-/* lapack/lasyf.zig:14-896 (complex, LAPACK zlasyf with gemmtr): up to nb
+/* lapack/lasyf.zig:17-896 (complex, LAPACK zlasyf with gemmtr): up to nb
  * columns with W = U12 D or L21 D built alongside, the rest of the triangle
  * updated by gemmtr, the later interchanges undone; *kb = columns factored. */
 int ZP(lasyf)(int order, int uplo, int n, int nb, int *kb, ZT *a, int lda, int *ipiv, ZT *w,

@@ -90,3 +90,27 @@ def test_ssytrf_bitwise_equals_oracle():
     assert info == infr == 0
     np.testing.assert_array_equal(ipiv, ipr)
     np.testing.assert_array_equal(np.tril(f), np.tril(fr))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("uplo", [b"L", b"U"])
+@pytest.mark.parametrize("layout", [102, 101])
+def test_bunchkaufman_facade_reconstructs(uplo, layout):
+    """zml_bunchkaufman: ldlt for a lower-stored matrix, udut for an upper
+    one, factored on the GPU; its p / l|u / d reconstruct A."""
+    import ctypes as C
+    from test_api_host import _bk_unpack
+    L = zg.lib()
+    n = 150
+    g = np.random.default_rng(5).standard_normal((n, n))
+    a = (g + g.T) / 2
+    ac = np.ascontiguousarray(a) if layout == 101 else np.asfortranarray(a)
+    lo, up = C.c_void_p(), C.c_void_p()
+    assert L.zml_bunchkaufman(layout, uplo, n, ac.ctypes.data_as(C.c_void_p), n, C.byref(lo),
+                              C.byref(up)) == 0
+    upper = uplo == b"U"
+    h = up if upper else lo
+    assert h.value and not (lo if upper else up).value
+    perm, t, D = _bk_unpack(L, h, upper, n)
+    (L.zml_udut_deinit if upper else L.zml_ldlt_deinit)(h)
+    assert np.abs(a[np.ix_(perm, perm)] - t @ D @ t.T).max() <= 1e-10 * np.abs(a).max()

@@ -168,6 +168,7 @@ class DMatrix(C.Structure):
 
 ERR_INVALID_ARGUMENT, ERR_SINGULAR_MATRIX, ERR_OUT_OF_MEMORY = -2000, -2001, -2002
 ERR_DIMENSION_MISMATCH = -2003
+ERR_FACTORIZATION_FAILED = -2004
 QR_FULL, QR_ECONOMICAL = 0, 1
 _pp = C.POINTER(vp)
 _SIGS.update({
@@ -191,6 +192,21 @@ _SIGS.update({
     "zml_dmatmul": (i32, [C.POINTER(DMatrix), C.POINTER(DMatrix), C.POINTER(DMatrix)]),
     "zml_dmatvec": (i32, [C.POINTER(DMatrix), vp, i32, vp, i32]),
     "zml_dvecmat": (i32, [vp, i32, C.POINTER(DMatrix), vp, i32]),
+    "zml_ldlt": (i32, [i32, ch, i32, vp, i32, _pp]),
+    "zml_udut": (i32, [i32, ch, i32, vp, i32, _pp]),
+    "zml_bunchkaufman": (i32, [i32, ch, i32, vp, i32, _pp, _pp]),
+    "zml_ldlt_init": (i32, [i32, i32, vp, i32, vp, _pp]),
+    "zml_udut_init": (i32, [i32, i32, vp, i32, vp, _pp]),
+    "zml_ldlt_deinit": (None, [vp]),
+    "zml_udut_deinit": (None, [vp]),
+    "zml_ldlt_p": (i32, [vp, vp]),
+    "zml_udut_p": (i32, [vp, vp]),
+    "zml_ldlt_l": (DMatrix, [vp]),
+    "zml_udut_u": (DMatrix, [vp]),
+    "zml_ldlt_d": (i32, [vp, vp, vp, vp]),
+    "zml_udut_d": (i32, [vp, vp, vp, vp]),
+    "zml_ldlt_ipiv": (C.POINTER(C.c_int), [vp]),
+    "zml_udut_ipiv": (C.POINTER(C.c_int), [vp]),
 })
 
 PREC_FP16, PREC_BF16, PREC_FP32, PREC_BF16X3 = 0, 1, 2, 3

@@ -2,7 +2,8 @@
 // the library's GPU LAPACK.  Host code only.
 //
 // Mirrors src/linalg/lu.zig:62-216 (PLU, plu), cholesky.zig:17-188 (LLT, UTU,
-// llt, utu, cholesky) and qr.zig:21-263 (QR, qr, QR.q, QR.r).  As in the
+// llt, utu, cholesky), bunchkaufman.zig:20-726 (LDLT, UDUT, ldlt, udut,
+// bunchkaufman) and qr.zig:21-263 (QR, qr, QR.q, QR.r).  As in the
 // reference the constructor copies the input (host memory, same layout,
 // packed leading dimension), factors the copy in place (here through
 // LAPACKE_dgetrf / dpotrf / dgeqrf, which stage to the GPU), and fails with
@@ -40,6 +41,15 @@ struct zml_qr_s {
   int layout, m, n, ld;
   double *qr;
   double *tau;
+};
+
+// LDLT (upper false) or UDUT (upper true): the packed n x n dsytrf factor in
+// `layout` and its ipiv (LAPACK's convention, 1-based).
+struct zml_bk_s {
+  int layout, n;
+  bool upper;
+  double *f;
+  int *ipiv;
 };
 
 namespace {
@@ -118,6 +128,229 @@ int chol_new(int layout, char uplo, int n, const double *a, int lda, bool lower,
   c->f = f;
   *out = c;
   return 0;
+}
+
+zml_bk_s *bk_new(int layout, int n, bool upper, double *f, const int *ipiv) {
+  zml_bk_s *o = (zml_bk_s *)std::malloc(sizeof(zml_bk_s));
+  int *p = (int *)std::malloc(sizeof(int) * std::max(1, n));
+  if (!o || !p) {
+    std::free(o);
+    std::free(p);
+    return nullptr;
+  }
+  if (n > 0) std::memcpy(p, ipiv, sizeof(int) * n);
+  o->layout = layout;
+  o->n = n;
+  o->upper = upper;
+  o->f = f;
+  o->ipiv = p;
+  return o;
+}
+
+// ldlt / udut (bunchkaufman.zig:180-707, the LAPACKE branch): the stored
+// triangle (mirrored when it is not the one factored) into a zeroed packed
+// copy, then dsytrf on the factored triangle.
+int bk_factor(int layout, char uplo, int n, const double *a, int lda, bool upper, zml_bk_s **out) {
+  if (!out) return ZML_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  uplo = (char)(uplo == 'l' ? 'L' : uplo == 'u' ? 'U' : uplo);
+  if (!layout_ok(layout) || (uplo != 'L' && uplo != 'U') || n < 0 || lda < std::max(1, n) ||
+      (!a && n > 0))
+    return ZML_ERR_INVALID_ARGUMENT;
+  double *f = (double *)std::calloc(std::max<size_t>(1, (size_t)n * n), sizeof(double));
+  int *ipiv = (int *)std::calloc(std::max(1, n), sizeof(int));
+  if (!f || !ipiv) {
+    std::free(f);
+    std::free(ipiv);
+    return ZML_ERR_OUT_OF_MEMORY;
+  }
+  const bool src_lower = uplo == 'L';
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) {
+      if (upper ? i > j : i < j) continue;
+      const bool in_src = src_lower ? i >= j : i <= j;
+      f[at(layout, i, j, n)] = in_src ? a[at(layout, i, j, lda)] : a[at(layout, j, i, lda)];
+    }
+  const int info = n > 0 ? LAPACKE_dsytrf(layout, upper ? 'U' : 'L', n, f, n, ipiv) : 0;
+  if (info != 0) {
+    std::free(f);
+    std::free(ipiv);
+    // bunchkaufman.zig:231-232: any non-zero info fails the factorization
+    return info > 0 ? ZML_ERR_FACTORIZATION_FAILED : status_of(info);
+  }
+  zml_bk_s *o = bk_new(layout, n, upper, f, ipiv);
+  std::free(ipiv);
+  if (!o) {
+    std::free(f);
+    return ZML_ERR_OUT_OF_MEMORY;
+  }
+  *out = o;
+  return 0;
+}
+
+int bk_init(int layout, int n, const double *f, int ld, const int *ipiv, bool upper,
+            zml_bk_s **out) {
+  if (!out) return ZML_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (!layout_ok(layout) || n < 0 || ld < std::max(1, n) || ((!f || !ipiv) && n > 0))
+    return ZML_ERR_INVALID_ARGUMENT;
+  // every interchange row inside the matrix; a 2x2 block's partner inside too
+  for (int i = 0; i < n; ++i) {
+    const int r = ipiv[i] > 0 ? ipiv[i] : -ipiv[i];
+    if (ipiv[i] == 0 || r > n) return ZML_ERR_INVALID_ARGUMENT;
+    if (ipiv[i] < 0 && (upper ? i == 0 : i == n - 1)) return ZML_ERR_INVALID_ARGUMENT;
+  }
+  int ldc = 1;
+  double *c = copy_matrix(layout, n, n, f, ld, &ldc);
+  if (!c) return ZML_ERR_OUT_OF_MEMORY;
+  zml_bk_s *o = bk_new(layout, n, upper, c, ipiv);
+  if (!o) {
+    std::free(c);
+    return ZML_ERR_OUT_OF_MEMORY;
+  }
+  *out = o;
+  return 0;
+}
+
+// lpermute / upermute (bunchkaufman.zig:426-443, 690-707): ipiv's
+// interchanges applied to the identity in factorization order (forward for
+// L, backward for U); a 2x2 block's interchange acts on its second (L) or
+// first (U) row.
+void bk_permute(const zml_bk_s *o, unsigned *p) {
+  const int n = o->n;
+  const int *ipiv = o->ipiv;
+  for (int i = 0; i < n; ++i) p[i] = (unsigned)i;
+  if (!o->upper) {
+    for (int i = 0; i < n; ++i) {
+      if (ipiv[i] > 0) {
+        std::swap(p[i], p[ipiv[i] - 1]);
+      } else {
+        std::swap(p[i + 1], p[-ipiv[i] - 1]);
+        ++i;
+      }
+    }
+  } else {
+    for (int i = n - 1; i >= 0; --i) {
+      if (ipiv[i] > 0) {
+        std::swap(p[i], p[ipiv[i] - 1]);
+      } else {
+        std::swap(p[i - 1], p[-ipiv[i] - 1]);
+        --i;
+      }
+    }
+  }
+}
+
+// lconvert / uconvert (bunchkaufman.zig:312-424, 576-688): walks the blocks
+// in factorization order, tracking the permutation p as bk_permute does;
+// each block's multiplier columns are copied into t (when given) and the
+// rows of the columns already placed (L: left of the block, U: right of it)
+// are swapped along p's cycle until p[i] == i; D's blocks go to
+// (sub, diag, sup) (when given), zero between blocks.
+void bk_convert(const zml_bk_s *o, double *t, double *sub, double *diag, double *sup) {
+  const int n = o->n, lay = o->layout;
+  const int *ipiv = o->ipiv;
+  const double *a = o->f;
+  unsigned *p = (unsigned *)std::malloc(sizeof(unsigned) * std::max(1, n));
+  if (!p) return;
+  for (int i = 0; i < n; ++i) p[i] = (unsigned)i;
+  auto A = [&](int i, int j) { return a[at(lay, i, j, n)]; };
+  auto T = [&](int i, int j) -> double & { return t[at(lay, i, j, n)]; };
+  auto settle = [&](int i, int c0, int c1) {
+    while (p[i] != (unsigned)i) {
+      const unsigned jr = p[i];
+      if (t)
+        for (int j = c0; j < c1; ++j) std::swap(T(i, j), T((int)jr, j));
+      std::swap(p[i], p[jr]);
+    }
+  };
+  if (!o->upper) {
+    for (int i = 0; i < n; ++i) {
+      if (ipiv[i] > 0) {
+        std::swap(p[i], p[ipiv[i] - 1]);
+        if (diag) {
+          diag[i] = A(i, i);
+          if (i < n - 1) sub[i] = sup[i] = 0.0;
+        }
+        if (t)
+          for (int j = i + 1; j < n; ++j) T(j, i) = A(j, i);
+        settle(i, 0, i);
+      } else {
+        std::swap(p[i + 1], p[-ipiv[i] - 1]);
+        if (diag) {
+          diag[i] = A(i, i);
+          sub[i] = sup[i] = A(i + 1, i);
+          diag[i + 1] = A(i + 1, i + 1);
+        }
+        if (t) {
+          T(i + 1, i) = 0.0;
+          for (int j = i + 2; j < n; ++j) {
+            T(j, i) = A(j, i);
+            T(j, i + 1) = A(j, i + 1);
+          }
+        }
+        ++i;
+        settle(i, 0, i - 1);
+        if (diag && i < n - 1) sub[i] = sup[i] = 0.0;
+      }
+    }
+  } else {
+    for (int i = n - 1; i >= 0; --i) {
+      if (ipiv[i] > 0) {
+        std::swap(p[i], p[ipiv[i] - 1]);
+        if (diag) {
+          diag[i] = A(i, i);
+          if (i < n - 1) sub[i] = sup[i] = 0.0;
+        }
+        if (t)
+          for (int j = 0; j < i; ++j) T(j, i) = A(j, i);
+        settle(i, i + 1, n);
+      } else {
+        std::swap(p[i - 1], p[-ipiv[i] - 1]);
+        if (diag) {
+          diag[i - 1] = A(i - 1, i - 1);
+          sub[i - 1] = sup[i - 1] = A(i - 1, i);
+          diag[i] = A(i, i);
+          if (i < n - 1) sub[i] = sup[i] = 0.0;
+        }
+        if (t) {
+          for (int j = 0; j < i - 1; ++j) {
+            T(j, i - 1) = A(j, i - 1);
+            T(j, i) = A(j, i);
+          }
+          T(i - 1, i) = 0.0;
+        }
+        --i;
+        settle(i, i + 2, n);
+      }
+    }
+  }
+  std::free(p);
+}
+
+zml_dmatrix bk_triangle(const zml_bk_s *o) {
+  const int n = o->n;
+  double *t = (double *)std::calloc(std::max<size_t>(1, (size_t)n * n), sizeof(double));
+  if (t) {
+    for (int i = 0; i < n; ++i) t[at(o->layout, i, i, n)] = 1.0;
+    bk_convert(o, t, nullptr, nullptr, nullptr);
+  }
+  zml_dmatrix v = view(t, n, n, std::max(1, n), o->layout, o->upper ? 121 : 122, 132);
+  v.owns_data = t ? 1 : 0;
+  return v;
+}
+
+int bk_d(const zml_bk_s *o, double *sub, double *diag, double *sup) {
+  if ((o->n > 0 && !diag) || (o->n > 1 && (!sub || !sup))) return ZML_ERR_INVALID_ARGUMENT;
+  bk_convert(o, nullptr, sub, diag, sup);
+  return 0;
+}
+
+void bk_free(zml_bk_s *o) {
+  if (!o) return;
+  std::free(o->f);
+  std::free(o->ipiv);
+  std::free(o);
 }
 
 }  // namespace
@@ -402,5 +635,69 @@ int zml_dmatvec(const zml_dmatrix *a, const double *x, int incx, double *y, int 
 int zml_dvecmat(const double *x, int incx, const zml_dmatrix *b, double *y, int incy) {
   return gemv_facade(b, true, x, incx, y, incy);
 }
+
+// ---- Bunch-Kaufman ----
+int zml_ldlt(int layout, char uplo, int n, const double *a, int lda, zml_ldlt_t **out) {
+  return bk_factor(layout, uplo, n, a, lda, false, out);
+}
+
+int zml_udut(int layout, char uplo, int n, const double *a, int lda, zml_udut_t **out) {
+  return bk_factor(layout, uplo, n, a, lda, true, out);
+}
+
+int zml_bunchkaufman(int layout, char uplo, int n, const double *a, int lda, zml_ldlt_t **lo,
+                     zml_udut_t **up) {
+  if (!lo || !up) return ZML_ERR_INVALID_ARGUMENT;
+  *lo = *up = nullptr;
+  if (uplo == 'L' || uplo == 'l') return bk_factor(layout, uplo, n, a, lda, false, lo);
+  if (uplo == 'U' || uplo == 'u') return bk_factor(layout, uplo, n, a, lda, true, up);
+  return ZML_ERR_INVALID_ARGUMENT;
+}
+
+int zml_ldlt_init(int layout, int n, const double *f, int ld, const int *ipiv, zml_ldlt_t **out) {
+  return bk_init(layout, n, f, ld, ipiv, false, out);
+}
+
+int zml_udut_init(int layout, int n, const double *f, int ld, const int *ipiv, zml_udut_t **out) {
+  return bk_init(layout, n, f, ld, ipiv, true, out);
+}
+
+void zml_ldlt_deinit(zml_ldlt_t *f) { bk_free(f); }
+void zml_udut_deinit(zml_udut_t *f) { bk_free(f); }
+
+int zml_ldlt_p(const zml_ldlt_t *f, unsigned *perm) {
+  if (!f || f->upper || (!perm && f->n > 0)) return ZML_ERR_INVALID_ARGUMENT;
+  bk_permute(f, perm);
+  return 0;
+}
+
+int zml_udut_p(const zml_udut_t *f, unsigned *perm) {
+  if (!f || !f->upper || (!perm && f->n > 0)) return ZML_ERR_INVALID_ARGUMENT;
+  bk_permute(f, perm);
+  return 0;
+}
+
+zml_dmatrix zml_ldlt_l(const zml_ldlt_t *f) {
+  if (!f || f->upper) return view(nullptr, 0, 0, 1, LAPACK_COL_MAJOR, 0, 0);
+  return bk_triangle(f);
+}
+
+zml_dmatrix zml_udut_u(const zml_udut_t *f) {
+  if (!f || !f->upper) return view(nullptr, 0, 0, 1, LAPACK_COL_MAJOR, 0, 0);
+  return bk_triangle(f);
+}
+
+int zml_ldlt_d(const zml_ldlt_t *f, double *sub, double *diag, double *sup) {
+  if (!f || f->upper) return ZML_ERR_INVALID_ARGUMENT;
+  return bk_d(f, sub, diag, sup);
+}
+
+int zml_udut_d(const zml_udut_t *f, double *sub, double *diag, double *sup) {
+  if (!f || !f->upper) return ZML_ERR_INVALID_ARGUMENT;
+  return bk_d(f, sub, diag, sup);
+}
+
+const int *zml_ldlt_ipiv(const zml_ldlt_t *f) { return f ? f->ipiv : nullptr; }
+const int *zml_udut_ipiv(const zml_udut_t *f) { return f ? f->ipiv : nullptr; }
 
 }  // extern "C"

@@ -1,6 +1,6 @@
 // sytrf.cu -- Bunch-Kaufman symmetric-indefinite factorization on the GPU:
 // A = U D U^T or L D L^T with 1x1 and 2x2 pivot blocks (LAPACK's dsytf2
-// pivoting, as zml restates it in lapack/sytf2.zig:13-522).
+// pivoting, as zml restates it in lapack/sytf2.zig:17-522).
 //
 // One step per pivot block, driven by the host: a single-CTA kernel finds
 // the pivot (|a_kk|, the column maximum, and when needed the maximum of row
