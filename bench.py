@@ -421,6 +421,9 @@ def suite_bench(torch, zg, L, dev, st):
             row["lu_" + name] = {"s": t, "rc": rc, "info": res.info, "converged": bool(res.converged),
                                  "outer": res.iters, "gmres": res.inner_iters,
                                  "switched_f64": bool(res.switched_f64),
+                                 "fp64_fallback": bool(res.fp64_fallback),
+                                 "refine_history": [res.berr_history[i]
+                                                    for i in range(min(8, res.iters + 1))],
                                  "berr": berr_of(M, X, b), "speedup_vs_fp64": t64 / t}
         # the precision ladder without the selector (BF16 -> ... -> FP64 LU)
         X = torch.zeros_like(b)
@@ -444,6 +447,7 @@ def suite_bench(torch, zg, L, dev, st):
         row["cholesky_bf16x3"] = {"s": t, "rc": rc, "info": res.info,
                                   "converged": bool(res.converged),
                                   "outer": res.iters, "gmres": res.inner_iters,
+                                  "fp64_fallback": bool(res.fp64_fallback),
                                   "berr": berr_of(P, X, bp)}
         out["mixed"]["n8192_kappa%.0e" % kappa] = row
         del M, S, P
@@ -462,8 +466,26 @@ def suite_bench(torch, zg, L, dev, st):
                                                X.data_ptr(), n, 3, 1, tol, 30, res, sh))
     out["mixed"]["n32768_gaussian"] = {
         "s": t, "rc": rc, "tol": tol, "converged": bool(res.converged), "outer": res.iters,
-        "gmres": res.inner_iters, "berr": berr_of(S.t(), X, b),
-        "fp64_equiv_tflops": (2.0 * n ** 3 / 3) / t / 1e12}
+        "gmres": res.inner_iters, "fp64_fallback": bool(res.fp64_fallback),
+        "berr": berr_of(S.t(), X, b), "fp64_equiv_tflops": (2.0 * n ** 3 / 3) / t / 1e12}
+    del S
+    # ---- plain 16-bit factors at n = 16384 Gaussian (FP16, BF16; GMRES-IR) ----
+    n = 16384
+    S = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
+    xt = torch.rand(n, 1, dtype=torch.float64, device=dev, generator=g) * 2 - 1
+    b = (S.t() @ xt).contiguous()
+    tol = 64 * U
+    for prec, name in ((0, "fp16"), (1, "bf16")):
+        X = torch.zeros_like(b)
+        res = zg.MpirResult()
+        t, rc = timed(lambda: L.zml_gpu_dgesv_mpir(n, 1, S.data_ptr(), n, b.data_ptr(), n,
+                                                   X.data_ptr(), n, prec, 1, tol, 30, res, sh))
+        out["mixed"]["n16384_gaussian_" + name] = {
+            "s": t, "rc": rc, "tol": tol, "info": res.info, "converged": bool(res.converged),
+            "outer": res.iters, "gmres": res.inner_iters,
+            "switched_f64": bool(res.switched_f64), "fp64_fallback": bool(res.fp64_fallback),
+            "refine_history": [res.berr_history[i] for i in range(min(8, res.iters + 1))],
+            "berr": berr_of(S.t(), X, b)}
     del S
     torch.cuda.empty_cache()
     out["next"] = next_rows_bench(torch, L, dev, g)
@@ -756,6 +778,7 @@ def main():
                    "n": n, "nrhs": 1, "parallelism": "replicas" if world > 1 else "1 GPU",
                    "l2": "inputs larger than L2 (A is %.1f GiB FP64)" % (8 * n * n / 2 ** 30)},
         "berr": berr, "berr_reported": last.berr, "berr_target": tol,
+        "fp64_fallback": bool(last.fp64_fallback),
         "berr_history": [last.berr_history[i] for i in range(min(32, last.iters + 1))],
         "ferr": ferr, "outer_iters": last.iters,
         "gmres_iters": last.inner_iters, "factor_ms": last.factor_ms, "converged": bool(last.converged),

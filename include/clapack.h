@@ -122,15 +122,15 @@ int LAPACKE_slaswp(int matrix_layout, int n, float *a, int lda, int k1, int k2, 
 int zml_gpu_dgetrf(int m, int n, double *dA, int ldda, int *dipiv, int *info, void *stream);
 /* FP64 getrf on device memory that allocates nothing; no counterpart in the
  * reference.  For callers that cannot allocate device memory at solve time:
- * code being captured into a CUDA graph (cudaMalloc cannot be captured),
- * hosts whose device memory belongs to another allocator, loops that must not
- * allocate after start-up.  Same factorization, bit for bit, as
- * zml_gpu_dgetrf.  Its scratch is one static device array of about 273 KB
- * that every GPU loading the library holds until exit; the first call on a
- * device resolves that array's address (make it before any stream capture).
- * Every call shares the array: calls that overlap on the GPU race.  Limit: m
- * at most what one 64-column panel holds in shared memory (about 446 rows per
- * SM), on devices of at most 256 SMs; larger sizes return
+ * hosts whose device memory belongs to another allocator (a caching pool or a
+ * fixed arena that a cudaMalloc from the library would fragment or overrun),
+ * and loops that must not allocate after start-up.  Same factorization, bit
+ * for bit, as zml_gpu_dgetrf.  Its scratch is one static device array of
+ * about 273 KB that every GPU loading the library holds until exit; the first
+ * call on a device resolves that array's address (make it before any stream
+ * capture).  Every call shares the array: calls that overlap on the GPU race.
+ * Limit: m at most what one 64-column panel holds in shared memory (about 446
+ * rows per SM), on devices of at most 256 SMs; larger sizes return
  * ZML_GPU_ERR_INVALID with a message in zml_gpu_last_error(). */
 int zml_gpu_dgetrf_noalloc(int m, int n, double *dA, int ldda, int *dipiv, int *info,
                            void *stream);
@@ -163,12 +163,17 @@ int zml_gpu_gemm_lowp(int prec, int m, int n, int k, float alpha, const void *dA
 /* Outcome of a mixed-precision solve (no counterpart in the reference, whose
  * path is FP64 only). */
 typedef struct zml_mpir_result {
-  int info;              /* info of the low-precision getrf (> 0: zero pivot) */
+  int info;              /* info (> 0: zero pivot / non-positive minor) of the
+                            factorization whose solution is returned: the
+                            low-precision one, or the FP64 one after a fallback */
   int iters;             /* outer refinement steps (max over right-hand sides) */
   int inner_iters;       /* total GMRES iterations */
   int converged;         /* 1 if every right-hand side reached FP64 backward error */
   int switched_f64;      /* 1 if the solves moved from FP32 to FP64 arithmetic */
-  int reserved;
+  int fp64_fallback;     /* 1 if the low-precision factorization failed or
+                            refinement stopped short of tol, and the system was
+                            solved again by the plain FP64 getrf+getrs
+                            (potrf+potrs for zml_*posv_mpir) */
   double berr;           /* largest final ||b - A x||inf / (||A||inf ||x||inf + ||b||inf) */
   double factor_ms;      /* device time of the factorization */
   double berr_history[32]; /* backward error per outer step, first right-hand side */
@@ -184,7 +189,9 @@ typedef struct zml_mpir_result {
 /* Solves A X = B (the problem of lapack/gesv.zig:13) to FP64 backward error:
  * LU with trailing updates in `prec` (tensor cores for fp16/bf16/bf16x3,
  * FP32 panels), then plain IR or GMRES-IR with FP64 residuals.  A and B are not
- * modified.  tol = 0 refines until the backward error stops improving.
+ * modified.  tol = 0 refines until the backward error stops improving.  When
+ * the low-precision LU fails or refinement stops short (of tol, or of 64 u
+ * with tol = 0), the system is solved again by the FP64 LU (fp64_fallback).
  * Host or device pointers. */
 int zml_dgesv_mpir(int matrix_layout, int n, int nrhs, const double *a, int lda, const double *b,
                    int ldb, double *x, int ldx, int prec, int mode, double tol, int max_iter,
@@ -196,7 +203,8 @@ int LAPACKE_dsgesv(int matrix_layout, int n, int nrhs, double *a, int lda, int *
 /* The SPD problem of lapack/posv.zig:15 to FP64 backward error: Cholesky
  * with trailing SYRK updates in `prec` (tensor cores for fp16/bf16/bf16x3),
  * then IR / GMRES-IR with FP64 residuals.  Only the `uplo` triangle of A is
- * read; A and B are not modified.  Host or device pointers. */
+ * read; A and B are not modified.  Falls back to the FP64 Cholesky as
+ * zml_dgesv_mpir falls back to the FP64 LU.  Host or device pointers. */
 int zml_dposv_mpir(int matrix_layout, char uplo, int n, int nrhs, const double *a, int lda,
                    const double *b, int ldb, double *x, int ldx, int prec, int mode, double tol,
                    int max_iter, zml_mpir_result *res);
@@ -319,6 +327,13 @@ unsigned long long zml_gpu_launch_count(void);
 
 /* Text of the last library error on this thread. */
 const char *zml_gpu_last_error(void);
+/* Iteration limit of every bounded device-side wait of the library (grid
+ * barriers, mbarrier waits, polls of published values) on the current
+ * device; tries <= 0 restores the default of 1 << 22 (about a second).  A
+ * wait that runs out sets a status bit and its kernel finishes with every
+ * index kept in range; the call then returns ZML_GPU_ERR_TIMEOUT.  For tests
+ * of that path; no counterpart in the reference. */
+int zml_gpu_set_spin_limit(long long tries);
 /* ABI version of this library. */
 int zml_gpu_version(void);
 

@@ -139,7 +139,9 @@ int zml_udut_p(const zml_udut_t *f, unsigned *perm);
 zml_dmatrix zml_ldlt_l(const zml_ldlt_t *f);
 zml_dmatrix zml_udut_u(const zml_udut_t *f);
 /* LDLT.d / UDUT.d (:74-89, :154-169): the block-diagonal D as a tridiagonal
- * (sub and sup n-1 entries, diag n), zero between blocks. */
+ * (sub and sup n-1 entries, diag n), zero between blocks.  Returns 0,
+ * ZML_ERR_INVALID_ARGUMENT, or ZML_ERR_OUT_OF_MEMORY (nothing written) when
+ * its scratch cannot be allocated. */
 int zml_ldlt_d(const zml_ldlt_t *f, double *sub, double *diag, double *sup);
 int zml_udut_d(const zml_udut_t *f, double *sub, double *diag, double *sup);
 const int *zml_ldlt_ipiv(const zml_ldlt_t *f);

@@ -441,6 +441,13 @@ int P(laswp)(int order, int n, T *a, int lda, int k1, int k2, const int *ipiv, i
   return 0;
 }
 
+/* Test hook, off unless set: the one-column step of getrf2 records each
+ * column's relative gap between its largest and second-largest candidate,
+ * (top1 - top2) / top1, at margin_out[ipiv - margin_ipiv].  The parity tests
+ * stop comparing pivots at the first column whose gap is a near-tie. */
+static double *P(margin_out) = 0;
+static const int *P(margin_ipiv) = 0;
+
 /* lapack/getrf2.zig:14-210: recursive LU with partial pivoting. */
 int P(getrf2)(int order, int m, int n, T *a, int lda, int *ipiv) {
   if (m < 0 || n < 0 || lda < ZO_MAX(1, order == ZO_COL ? m : n)) return ZO_EINVAL;
@@ -453,6 +460,14 @@ int P(getrf2)(int order, int m, int n, T *a, int lda, int *ipiv) {
     const T sfmin = P(lamch)('s');
     const int ii = P(iamax)(m, a, P(col_ld)(order, lda));
     ipiv[0] = ii + 1;
+    if (P(margin_out)) {
+      const double top = ZO_ABS(a[P(idx)(order, ii, 0, lda)]);
+      double second = 0;
+      for (int i = 0; i < m; ++i)
+        if (i != ii && ZO_ABS(a[P(idx)(order, i, 0, lda)]) > second)
+          second = ZO_ABS(a[P(idx)(order, i, 0, lda)]);
+      P(margin_out)[ipiv - P(margin_ipiv)] = top > 0 ? (top - second) / top : 0.0;
+    }
     if (a[P(idx)(order, ii, 0, lda)] != (T)0) {
       if (ii != 0) {
         T temp = a[0];

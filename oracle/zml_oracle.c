@@ -82,6 +82,7 @@ int zo_ilaenv(int ispec, const char *name, int n1, int n2, int n3, int n4) {
 #include "oracle_impl.h"
 #include "oracle_qr_impl.h"
 #include "oracle_sy_impl.h"
+#include "oracle_mt.h"
 #undef T
 #undef P
 #undef ZO_ABS

@@ -88,6 +88,12 @@ ZO_DECL(double, zo_d_)
 ZO_DECL(float, zo_s_)
 #undef ZO_DECL
 
+/* Threaded forms (column-major, binary64) of zo_d_getrf and zo_d_potrf for the
+ * large parity cases: bit-identical results (oracle_mt.h).  margin
+ * (optional, min(m, n) entries) receives each column's pivot gap. */
+int zo_d_getrf_mt(int m, int n, double *a, int lda, int *ipiv, double *margin, int threads);
+int zo_d_potrf_mt(int uplo, int n, double *a, int lda, int threads);
+
 /* ---- complex (cfloat) ----------------------------------------------------
  * Interleaved (re, im) pairs: numpy complex128 / complex64.  The arithmetic
  * restates zml's cfloat operations (cfloat.zig), whose products and Smith

@@ -228,7 +228,9 @@ def parse_scalar_tests(root):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <root of the srmadrid/zml tree>")
+    root = sys.argv[1]
     here = os.path.dirname(os.path.abspath(__file__))
     for fn in CHAINED:
         fx = parse_chain(os.path.join(root, "test/linalg/blas/%s.zig" % fn), fn)

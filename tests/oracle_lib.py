@@ -141,6 +141,31 @@ def getrf(a, order=102):
     return a, ipiv, info
 
 
+def getrf_mt(a, threads=None, margins=False):
+    """The oracle's getrf of a copy of `a` (binary64, column-major) on host
+    threads, bit-identical to getrf(); with margins=True also each column's
+    pivot gap (top1 - top2) / top1."""
+    f = load().zo_d_getrf_mt
+    f.restype, f.argtypes = i32, [i32, i32, vp, i32, vp, vp, i32]
+    a = np.array(a, dtype=np.float64, order="F", copy=True)
+    m, n = a.shape
+    ipiv = np.zeros(min(m, n), dtype=np.int32)
+    gap = np.full(min(m, n), np.inf) if margins else None
+    info = f(m, n, ptr(a), max(1, m), ptr(ipiv), ptr(gap), threads or os.cpu_count() or 1)
+    return (a, ipiv, info, gap) if margins else (a, ipiv, info)
+
+
+def potrf_mt(a, uplo=122, threads=None):
+    """The oracle's potrf (binary64, column-major) on host threads,
+    bit-identical to potrf()."""
+    f = load().zo_d_potrf_mt
+    f.restype, f.argtypes = i32, [i32, i32, vp, i32, i32]
+    a = np.array(a, dtype=np.float64, order="F", copy=True)
+    n = a.shape[0]
+    info = f(uplo, n, ptr(a), max(1, n), threads or os.cpu_count() or 1)
+    return a, info
+
+
 def getrs(lu, ipiv, b, trans=111):
     b = np.array(b, dtype=lu.dtype, order="F", copy=True)
     if b.ndim == 1:

@@ -222,3 +222,44 @@ def test_lookahead_factorization_is_repeatable():
     for x, hist in runs[1:]:
         assert hist == runs[0][1]
         np.testing.assert_array_equal(x, runs[0][0])
+
+
+# ---- the ill-conditioned sweep: refinement, or the FP64 fallback ------------
+
+@pytest.mark.parametrize("kappa", [1e6, 1e10])
+@pytest.mark.parametrize("prec", [3, 2])  # bf16x3, fp32 factors; GMRES-IR
+def test_mpir_kappa_sweep_n2048_reaches_fp64_lu(prec, kappa):
+    """A = U diag(s) V^T, s_i = kappa^(-(i-1)/(n-1)).  zml_dgesv_mpir refines
+    until the backward error is the FP64 LU's; where the low-precision factors
+    cannot take it there (kappa u_f well above 1 leaves GMRES a spread of
+    small eigenvalues that would take O(n) steps), it solves again with the
+    FP64 LU and says so in fp64_fallback.  Either way the answer meets the bar."""
+    n = 2048
+    a = svd_matrix(n, kappa, seed=int(np.log10(kappa)) + prec)
+    xt = np.random.default_rng(11).uniform(-1, 1, (n, 1))
+    b = np.asfortranarray(a @ xt)
+    lu, ipiv, info = ol.getrf_mt(a)
+    e64 = berr(a, ol.getrs(lu, ipiv, b), b)
+    x, res = solve(a, b, prec, 1, tol=e64)
+    assert res.converged, (res.berr, res.fp64_fallback, list(res.berr_history[:res.iters + 1]))
+    assert berr(a, x, b) <= 2 * e64 + U64
+    if prec == 2 and kappa == 1e6:
+        assert not res.fp64_fallback  # FP32 factors refine this one on their own
+    if res.fp64_fallback:
+        assert res.info == 0
+
+
+def test_mpir_fallback_when_the_low_precision_cholesky_fails():
+    """BF16x3 updates of an SPD matrix with kappa 1e12 lose positive
+    definiteness; zml_dposv_mpir then solves with the FP64 Cholesky."""
+    n = 1024
+    a = spd_matrix(n, seed=21, kappa=1e12)
+    xt = np.random.default_rng(22).uniform(-1, 1, (n, 1))
+    b = np.asfortranarray(a @ xt)
+    x, res = solve_spd(a, b, 3, 1)
+    f, info = ol.potrf(a, 122)
+    if info != 0:
+        pytest.skip("not positive definite in FP64 either")
+    e64 = berr(a, ol.potrs(f, b, 122), b)
+    assert res.converged, (res.info, res.berr, res.fp64_fallback)
+    assert berr(a, x, b) <= 2 * e64 + U64

@@ -137,3 +137,41 @@ def test_ilaenv_orgqr_block_sizes():
     assert lib.zo_ilaenv(1, b"DORGQR", 100, 100, 100, -1) == 32
     assert lib.zo_ilaenv(2, b"DORGQR", 100, 100, 100, -1) == 2
     assert lib.zo_ilaenv(3, b"DORGQR", 100, 100, 100, -1) == 128
+
+
+# ---- the threaded drivers used by the parity tests at the workload's sizes ----
+
+@pytest.mark.parametrize("m,n,threads", [(700, 700, 4), (513, 300, 3), (200, 450, 7),
+                                         (64, 64, 2), (65, 65, 5)])
+def test_getrf_mt_equals_serial(m, n, threads):
+    a = gaussian(m, n, seed=m + n)
+    a[:, 37 % n] = 0.0  # a zero column: info and the skipped scaling
+    lu, ipiv, info = ol.getrf(a)
+    lu2, ipiv2, info2, gap = ol.getrf_mt(a, threads=threads, margins=True)
+    assert info2 == info
+    np.testing.assert_array_equal(ipiv2, ipiv)
+    np.testing.assert_array_equal(lu2, lu)
+    # one candidate left (the last row): no tie possible, the gap stays inf
+    assert gap.shape == (min(m, n),) and np.all(gap >= 0)
+    assert np.all((gap <= 1) | np.isinf(gap))
+
+
+def test_getrf_mt_margins_match_numpy_replay():
+    import gpu_util
+    a = gaussian(150, seed=9)
+    _, _, _, gap = ol.getrf_mt(a, threads=3, margins=True)
+    ref = gpu_util.pivot_margins(a)
+    np.testing.assert_allclose(gap[:-1], ref[:-1], rtol=1e-6, atol=1e-12)
+
+
+@pytest.mark.parametrize("uplo", [121, 122])
+@pytest.mark.parametrize("n,threads", [(700, 4), (65, 3), (129, 16)])
+def test_potrf_mt_equals_serial(uplo, n, threads):
+    g = gaussian(n, seed=n)
+    a = np.asfortranarray(g @ g.T / n + np.eye(n))
+    f, info = ol.potrf(a, uplo)
+    f2, info2 = ol.potrf_mt(a, uplo, threads=threads)
+    assert info2 == info == 0
+    np.testing.assert_array_equal(f2, f)
+    a[90 % n, 90 % n] = -1.0  # a non-positive minor: same info
+    assert ol.potrf_mt(a, uplo, threads=threads)[1] == ol.potrf(a, uplo)[1]

@@ -1,12 +1,15 @@
 """zml_gpu_dgetrf_noalloc: the FP64 LU for callers that cannot allocate.
 
-Callers inside a CUDA-graph capture, or whose device memory is owned by
-another allocator, cannot let the library call cudaMalloc.  This entry point
-takes its scratch from a static device array instead.  It must produce the
-same factorization as zml_gpu_dgetrf (the test allows the parity tolerance of
-the other LU tests, |dLU| <= 1e-9 max|LU|, identical pivots and info), on two
-calls in a row -- the scratch keeps the previous call's contents, so the
-second call checks that everything that must start at zero is cleared.
+Some hosts own all device memory through their own allocator (a caching pool,
+or an arena reserved at start-up); a cudaMalloc from the library would
+fragment or overrun it.  Some loops must not allocate after initialisation.
+This entry point takes its scratch from a static device array instead.  It
+runs the same panel grid, interchanges, trsm and gemm as zml_gpu_dgetrf, so
+the factors must be identical bit for bit, with identical pivots and info.
+That is checked on two calls in a row: the scratch keeps the previous call's
+contents, so the second call shows that everything that must start at zero is
+cleared.  A third check reads the device's free memory around a call: any
+cudaMalloc takes at least one 2 MiB page, and none may happen.
 
 This file is collected last so that a failure here leaves every other test
 already run.
@@ -19,8 +22,6 @@ import pytest
 import zml_gb300 as zg
 
 pytestmark = pytest.mark.gpu
-
-TOL = 1e-9
 
 
 def factor(entry, a):
@@ -46,7 +47,29 @@ def test_noalloc_matches_dgetrf_twice(m, n, seed):
         lu, piv, info = factor("zml_gpu_dgetrf_noalloc", a)
         np.testing.assert_array_equal(piv, piv_ref)
         assert info == info_ref == (18 if call == 1 else 0)
-        assert np.abs(lu - lu_ref).max() <= TOL * np.abs(lu_ref).max()
+        np.testing.assert_array_equal(lu, lu_ref)
+
+
+def test_noalloc_takes_no_device_memory():
+    import torch
+    m = n = 1024
+    a = np.random.default_rng(3).standard_normal((m, n))
+    da = torch.from_numpy(np.asfortranarray(a).T.copy()).cuda()
+    dp = torch.zeros(n, dtype=torch.int32, device="cuda")
+    info = np.zeros(1, dtype=np.int32)
+    L = zg.lib()
+    # a first call loads the module (its static array) and resolves the address
+    assert L.zml_gpu_dgetrf_noalloc(m, n, da.data_ptr(), m, dp.data_ptr(),
+                                    info.ctypes.data_as(C.c_void_p), None) == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(2):
+        da.copy_(torch.from_numpy(np.asfortranarray(a).T.copy()))
+        assert L.zml_gpu_dgetrf_noalloc(m, n, da.data_ptr(), m, dp.data_ptr(),
+                                        info.ctypes.data_as(C.c_void_p), None) == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free0 - free1 < 2 << 20, (free0, free1)
 
 
 def test_noalloc_rejects_too_many_rows():

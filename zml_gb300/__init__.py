@@ -64,6 +64,7 @@ _SIGS.update({
     "zml_gpu_dgemm": (i32, [i32, i32, i32, i32, i32, f64, vp, i32, vp, i32, f64, vp, i32, vp]),
     "zml_gpu_gemm_lowp": (i32, [i32, i32, i32, i32, f32, vp, i32, vp, i32, f32, vp, i32, vp]),
     "zml_gpu_last_error": (C.c_char_p, []),
+    "zml_gpu_set_spin_limit": (i32, [C.c_longlong]),
     "zml_gpu_version": (i32, []),
 })
 
@@ -71,7 +72,7 @@ _SIGS.update({
 
 class MpirResult(C.Structure):
     _fields_ = [("info", C.c_int), ("iters", C.c_int), ("inner_iters", C.c_int),
-                ("converged", C.c_int), ("switched_f64", C.c_int), ("reserved", C.c_int),
+                ("converged", C.c_int), ("switched_f64", C.c_int), ("fp64_fallback", C.c_int),
                 ("berr", C.c_double), ("factor_ms", C.c_double),
                 ("berr_history", C.c_double * 32)]
 

@@ -246,13 +246,15 @@ void bk_permute(const zml_bk_s *o, unsigned *p) {
 // each block's multiplier columns are copied into t (when given) and the
 // rows of the columns already placed (L: left of the block, U: right of it)
 // are swapped along p's cycle until p[i] == i; D's blocks go to
-// (sub, diag, sup) (when given), zero between blocks.
-void bk_convert(const zml_bk_s *o, double *t, double *sub, double *diag, double *sup) {
+// (sub, diag, sup) (when given), zero between blocks.  Returns
+// ZML_ERR_OUT_OF_MEMORY, with nothing written, when the permutation's scratch
+// cannot be allocated.
+int bk_convert(const zml_bk_s *o, double *t, double *sub, double *diag, double *sup) {
   const int n = o->n, lay = o->layout;
   const int *ipiv = o->ipiv;
   const double *a = o->f;
   unsigned *p = (unsigned *)std::malloc(sizeof(unsigned) * std::max(1, n));
-  if (!p) return;
+  if (!p) return ZML_ERR_OUT_OF_MEMORY;
   for (int i = 0; i < n; ++i) p[i] = (unsigned)i;
   auto A = [&](int i, int j) { return a[at(lay, i, j, n)]; };
   auto T = [&](int i, int j) -> double & { return t[at(lay, i, j, n)]; };
@@ -326,14 +328,20 @@ void bk_convert(const zml_bk_s *o, double *t, double *sub, double *diag, double 
     }
   }
   std::free(p);
+  return 0;
 }
 
+// The unit triangle of the factor, owned by the caller; NULL data when an
+// allocation fails.
 zml_dmatrix bk_triangle(const zml_bk_s *o) {
   const int n = o->n;
   double *t = (double *)std::calloc(std::max<size_t>(1, (size_t)n * n), sizeof(double));
   if (t) {
     for (int i = 0; i < n; ++i) t[at(o->layout, i, i, n)] = 1.0;
-    bk_convert(o, t, nullptr, nullptr, nullptr);
+    if (bk_convert(o, t, nullptr, nullptr, nullptr) != 0) {
+      std::free(t);
+      t = nullptr;
+    }
   }
   zml_dmatrix v = view(t, n, n, std::max(1, n), o->layout, o->upper ? 121 : 122, 132);
   v.owns_data = t ? 1 : 0;
@@ -342,8 +350,7 @@ zml_dmatrix bk_triangle(const zml_bk_s *o) {
 
 int bk_d(const zml_bk_s *o, double *sub, double *diag, double *sup) {
   if ((o->n > 0 && !diag) || (o->n > 1 && (!sub || !sup))) return ZML_ERR_INVALID_ARGUMENT;
-  bk_convert(o, nullptr, sub, diag, sup);
-  return 0;
+  return bk_convert(o, nullptr, sub, diag, sup);
 }
 
 void bk_free(zml_bk_s *o) {

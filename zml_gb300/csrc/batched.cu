@@ -830,23 +830,13 @@ int batched_plan_execute(BatchPlan *p, double *A, const double *B, double *X, in
   a.iters = iters;
   ZG_CUDA(cudaMemsetAsync(p->d_queue, 0, sizeof(unsigned) * kBatchWarpCounts, s));
   if (p->fp32) {
-    static bool attr = false;
-    if (!attr) {
-      ZG_CUDA(cudaFuncSetAttribute(batched_kernel<float>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTotal));
-      attr = true;
-    }
+    ZG_TRY(smem_optin(batched_kernel<float>, kSmemTotal));
     ZG_LAUNCH(kTagBatched, p->flops, 0, s,
               batched_kernel<float><<<p->grid, kBatchThreads, kSmemTotal, s>>>(
                   a, p->d_order, p->d_queues, p->nq, p->d_queue, p->d_scratch,
                   p->scratch_per_group));
   } else {
-    static bool attr = false;
-    if (!attr) {
-      ZG_CUDA(cudaFuncSetAttribute(batched_kernel<double>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemTotal));
-      attr = true;
-    }
+    ZG_TRY(smem_optin(batched_kernel<double>, kSmemTotal));
     ZG_LAUNCH(kTagBatched, p->flops, 0, s,
               batched_kernel<double><<<p->grid, kBatchThreads, kSmemTotal, s>>>(
                   a, p->d_order, p->d_queues, p->nq, p->d_queue, nullptr, 0));

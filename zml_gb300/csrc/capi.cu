@@ -995,6 +995,7 @@ int zml_dgesv_mpir(int layout, int n, int nrhs, const double *a, int lda, const 
   o.mode = mode;
   o.tol = tol;
   o.max_iter = max_iter > 0 ? max_iter : 30;
+  o.fallback = true;
   MpirResult local;
   return mpir_any(layout, n, nrhs, a, lda, b, ldb, x, ldx, o, res ? res : &local);
 }
@@ -1038,6 +1039,7 @@ int zml_dposv_mpir(int layout, char uplo, int n, int nrhs, const double *a, int 
   o.mode = mode;
   o.tol = tol;
   o.max_iter = max_iter > 0 ? max_iter : 30;
+  o.fallback = true;
   MpirResult local;
   return posv_mpir_any(layout, uplo, n, nrhs, a, lda, b, ldb, x, ldx, o, res ? res : &local);
 }
@@ -1083,6 +1085,7 @@ int zml_gpu_dposv_mpir(char uplo, int n, int nrhs, const double *dA, int ldda, c
   o.mode = mode;
   o.tol = tol;
   o.max_iter = max_iter > 0 ? max_iter : 30;
+  o.fallback = true;
   MpirResult local;
   return posv_mpir_dev(uplo == 'L', n, nrhs, dA, ldda, dB, lddb, dX, lddx, o,
                        res ? res : &local, (cudaStream_t)stream);
@@ -1103,6 +1106,7 @@ int zml_gpu_dgesv_mpir(int n, int nrhs, const double *dA, int ldda, const double
   o.mode = mode;
   o.tol = tol;
   o.max_iter = max_iter > 0 ? max_iter : 30;
+  o.fallback = true;
   MpirResult local;
   return gesv_mpir_dev(n, nrhs, dA, ldda, dB, lddb, dX, lddx, o, res ? res : &local,
                        (cudaStream_t)stream);
@@ -1198,6 +1202,8 @@ int zml_gpu_dgesv_auto(int n, int nrhs, const double *dA, int ldda, const double
 }
 
 const char *zml_gpu_last_error(void) { return last_error(); }
+
+int zml_gpu_set_spin_limit(long long tries) { return set_spin_limit(tries); }
 
 int zml_gpu_version(void) { return 1; }
 

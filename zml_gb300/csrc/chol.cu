@@ -110,12 +110,14 @@ int potrs_dev(int uplo, int n, int nrhs, const T *A, long lda, T *B, long ldb, c
       double *xw = (double *)w;
       const double *Ad = reinterpret_cast<const double *>(A);
       const bool up = uplo == kUpper;  // A = U^T U, else A = L L^T
+      Control *ctl;  // one status word for every solve of the call
+      ZG_TRY(control(s, &ctl));
       for (int c = 0; c < nrhs; ++c) {
         double *x = reinterpret_cast<double *>(B) + (long)c * ldb;
-        ZG_TRY(trsv_f64(n, Ad, lda, up, false, false, x, x, xw, s));
-        ZG_TRY(trsv_f64(n, Ad, lda, !up, true, false, x, x, xw, s));
+        ZG_TRY(trsv_f64(n, Ad, lda, up, false, false, x, x, xw, ctl, s));
+        ZG_TRY(trsv_f64(n, Ad, lda, !up, true, false, x, x, xw, ctl, s));
       }
-      return 0;
+      return check_status(s, ctl, nullptr);  // a poll that ran out: kErrTimeout
     }
   }
   if (uplo == kUpper) {

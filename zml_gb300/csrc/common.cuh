@@ -77,6 +77,14 @@ struct DeviceInfo {
 
 int device_info(DeviceInfo *out);  // for the current device
 
+// Allows `func` up to `bytes` of dynamic shared memory on the current device.
+// The attribute belongs to one device, so it is set once per (device, kernel)
+// and again only for a larger size.
+int smem_optin_raw(const void *func, int bytes);
+template <typename F> int smem_optin(F *func, int bytes) {
+  return smem_optin_raw(reinterpret_cast<const void *>(func), bytes);
+}
+
 // Workspace slots: every user owns its slot, so a nested routine never
 // reallocates a buffer its caller still holds.
 enum Slot : int {
@@ -123,6 +131,20 @@ int check_status(cudaStream_t stream, Control *ctl, int *info_out);
 
 // Bounded spin limit for device-side waits (~1 s at GB300 clocks).
 constexpr long long kSpinLimit = 1ll << 22;
+// The limit the waits use, per device: kSpinLimit unless
+// zml_gpu_set_spin_limit changed it.  Without relocatable device code every
+// translation unit holds its own copy, so each registers a setter and one
+// host call updates them all.
+static __device__ long long g_spin_limit = kSpinLimit;
+__device__ __forceinline__ long long spin_limit() { return g_spin_limit; }
+int register_spin_setter(int (*set)(long long));
+int set_spin_limit(long long tries);  // every translation unit, current device
+namespace {
+inline int set_spin_limit_here(long long tries) {
+  return cudaMemcpyToSymbol(g_spin_limit, &tries, sizeof tries) == cudaSuccess ? 0 : -1001;
+}
+const int g_spin_setter_registered = register_spin_setter(&set_spin_limit_here);
+}  // namespace
 
 // ---------------------------------------------------------------------------
 // Device helpers
@@ -147,8 +169,9 @@ __device__ __forceinline__ void grid_barrier(Control *ctl, unsigned nblocks, uns
     asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(&ctl->barrier[0]), "r"(1u)
                  : "memory");
     long long spins = 0;
+    const long long lim = spin_limit();
     while (ld_acquire(&ctl->barrier[0]) < target) {
-      if (++spins > kSpinLimit) {
+      if (++spins > lim) {
         atomicOr(&ctl->status, kStatusBarrierTimeout);
         break;
       }

@@ -9,11 +9,13 @@
 //     a multiple of 8 elements).
 //
 // One CTA computes a 128 x BN tile.  Warp 0 (one lane) streams 128 x 64 K
-// slices of A and B into a 4-stage shared-memory ring with TMA (128-byte
-// swizzle); warp 1 (one lane) issues tcgen05.mma (M=128, N=BN, K=16) into a
-// TMEM accumulator and releases each stage with tcgen05.commit; then all four
-// warps drain TMEM (warp w owns accumulator rows 32w..32w+31) and apply the
-// epilogue to C with coalesced column-major stores.
+// slices of A and B into a STAGES-deep shared-memory ring (2 or 3 stages, so
+// that two CTAs share an SM) with TMA (128-byte swizzle); warp 1 (one lane)
+// issues tcgen05.mma (M=128, N=BN, K=16) into a TMEM accumulator and releases
+// each stage with tcgen05.commit; all eight warps load their slice of the old
+// C while the MMAs run, then drain TMEM (warps w and w+4 share accumulator
+// rows 32(w%4)..32(w%4)+31 and split the columns) and apply the epilogue to C
+// with column-major stores.
 #include <cudaTypedefs.h>
 
 #include "common.cuh"
@@ -199,12 +201,7 @@ int launch(int M, int N, int K, float alpha, const void *A, long lda, const void
   ZG_TRY(make_map(&ta, A, M, K, lda, kBM));
   ZG_TRY(make_map(&tb, B, N, K, ldb, BN));
   using Cfg = TileCfg<BN, STAGES>;
-  static bool attr = false;
-  if (!attr) {
-    ZG_CUDA(cudaFuncSetAttribute(gemm_tc_kernel<BN, STAGES>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::smem_bytes));
-    attr = true;
-  }
+  ZG_TRY(smem_optin(gemm_tc_kernel<BN, STAGES>, Cfg::smem_bytes));
   dim3 grid(ceil_div(M, kBM), ceil_div(N, BN));
   ZG_LAUNCH(kTagGemmTC, 2.0 * M * N * K, 2.0 * ((double)M + N) * K + (beta != 0.f ? 8.0 : 4.0) * M * N, s, gemm_tc_kernel<BN, STAGES><<<grid, 256, Cfg::smem_bytes, s>>>(ta, tb, M, N, K, alpha, beta, C,
                                                                ldc, ab_type, status, tri));

@@ -104,9 +104,10 @@ int potrf_launch(int uplo, int n, T *A, long lda, Control *ctl, int info_base, c
 template <typename T> int potrf_dev(int uplo, int n, T *A, long lda, int *info, cudaStream_t s);
 // Triangular solve of one FP64 column in one launch: x = op(A)^-1 rhs, op(A)
 // = A or A^T (trans), lower or upper, unit or non-unit diagonal; rhs may be
-// x.  xw: n + 1 doubles of device scratch.
+// x.  xw: n + 1 doubles of device scratch.  A poll that runs out sets a bit
+// in ctl->status, which the caller reads with check_status.
 int trsv_f64(int n, const double *A, long lda, bool trans, bool upper, bool unit,
-             const double *rhs, double *x, double *xw, cudaStream_t s);
+             const double *rhs, double *x, double *xw, Control *ctl, cudaStream_t s);
 // Y = P B, P the interchanges ipiv (1-based, n of them) applied in increasing
 // (forward) or decreasing order; Y must not overlap B.
 int perm_gather_f64(int n, int nrhs, const int *ipiv, bool forward, const double *B, long ldb,

@@ -23,15 +23,18 @@ struct MpirOpts {
   // (n = 16384 Gaussian: 3 outer / 15 inner steps instead of 3 / 20).
   double gmres_rtol = 1e-4;
   int apply = kApplyAuto;   // FP32 first, FP64 once refinement stops improving
+  // when the low-precision factorization fails or refinement stops short of
+  // the target, solve again with the plain FP64 factorization of A
+  bool fallback = false;
 };
 
 struct MpirResult {
-  int info = 0;             // getrf info of the low-precision factorization
+  int info = 0;             // info of the factorization whose solution is returned
   int iters = 0;            // outer refinement steps taken
   int inner_iters = 0;      // total GMRES iterations
   int converged = 0;        // berr reached FP64 level (or tol)
   int switched_f64 = 0;     // the solves moved to FP64 arithmetic
-  int reserved = 0;
+  int fp64_fallback = 0;    // the solution came from the FP64 factorization
   double berr = 0;          // final normwise backward error
   double factor_ms = 0;     // device time of the factorization
   double berr_history[32] = {0};

@@ -129,7 +129,6 @@ __global__ void __launch_bounds__(256) panel_lu_kernel(int m, int nb, T *__restr
     if (sizeof(T) == sizeof(float)) {
       const unsigned long long w = __ldcg(winners + k);
       idx = (int)(0xffffffffu - (unsigned)(w & 0xffffffffu));
-      if (idx < k || idx >= m) idx = 0x7fffffff;  // only after a barrier timeout
     } else {
       key = T(-INFINITY);
       idx = 0x7fffffff;
@@ -140,8 +139,13 @@ __global__ void __launch_bounds__(256) panel_lu_kernel(int m, int nb, T *__restr
       }
       block_argmax(key, idx, sk, si);
     }
+    // A pivot row outside [k, m) only arises after a barrier timeout (stale
+    // exchange words): row k stands in, so that every index below -- the
+    // candidate slot, the swap, ipiv and the interchanges run on it later --
+    // stays inside the matrix.  The host then reports the timeout.
+    if (idx < k || idx >= m) idx = k;
     // locate the slot that holds row idx
-    if (idx != 0x7fffffff) win = idx / R;
+    win = idx / R;
     const T *prow = cand[p] + (long)win * stride + 2;
     for (int c = tid; c < nb; c += blockDim.x) urow[c] = __ldcg(prow + c);
     __syncthreads();
@@ -208,13 +212,7 @@ int panel_lu(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *c
   unsigned long long *winners =
       (unsigned long long *)(((uintptr_t)xchg + nx + 255) & ~(uintptr_t)255);
   if (sizeof(T) == sizeof(float)) ZG_CUDA(cudaMemsetAsync(winners, 0, 8 * (size_t)nb, s));
-  static bool attr_set[2] = {false, false};
-  const int ti = sizeof(T) == 8 ? 0 : 1;
-  if (!attr_set[ti]) {
-    ZG_CUDA(cudaFuncSetAttribute(panel_lu_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)limit));
-    attr_set[ti] = true;
-  }
+  ZG_TRY(smem_optin(panel_lu_kernel<T>, (int)limit));
   // barrier counters are per launch
   ZG_CUDA(cudaMemsetAsync(&ctl->barrier[0], 0, 2 * sizeof(unsigned), s));
   T *xp = (T *)xchg;
@@ -544,8 +542,9 @@ __global__ void __launch_bounds__(kFT) trsv_f64_kernel(int n, const double *__re
         if (c < n) {
           unsigned long long w = ld_relaxed_b64(xpub + c);
           long long spins = 0;
+          const long long lim = spin_limit();
           while (w == kFEmpty) {
-            if (++spins > kSpinLimit) {
+            if (++spins > lim) {
               atomicOr(status, kStatusQueueTimeout);
               break;
             }
@@ -693,12 +692,7 @@ static int trsv_f64_launch(int n, const double *A, long lda, const double *rhs, 
                            bool upper, bool unit, double *xpub, unsigned *ticket,
                            unsigned *status, cudaStream_t s) {
   const size_t smem = sizeof(double) * kFB * kFLD;
-  static bool attr = false;
-  if (!attr) {
-    ZG_CUDA(cudaFuncSetAttribute(trsv_f64_kernel<TRANS>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  ZG_TRY(smem_optin(trsv_f64_kernel<TRANS>, (int)smem));
   ZG_LAUNCH(kTagTrsmDiag, 1.0 * n * n, 4.0 * n * n + 16.0 * n, s,
             trsv_f64_kernel<TRANS><<<ceil_div(n, kFB), kFT, smem, s>>>(
                 n, A, lda, rhs, x, xpub, ticket, upper, unit, status));
@@ -706,10 +700,8 @@ static int trsv_f64_launch(int n, const double *A, long lda, const double *rhs, 
 }
 
 int trsv_f64(int n, const double *A, long lda, bool trans, bool upper, bool unit,
-             const double *rhs, double *x, double *xw, cudaStream_t s) {
+             const double *rhs, double *x, double *xw, Control *ctl, cudaStream_t s) {
   if (n <= 0) return 0;
-  Control *ctl;
-  ZG_TRY(control(s, &ctl));
   unsigned *ticket = reinterpret_cast<unsigned *>(xw);
   double *xpub = xw + 1;
   ZG_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned), s));
@@ -732,22 +724,24 @@ int getrs_dev(int trans, int n, int nrhs, const T *A, long lda, const int *ipiv,
       double *xw = (double *)w, *Y = xw + n + 1;
       double *Bd = reinterpret_cast<double *>(B);
       const double *Ad = reinterpret_cast<const double *>(A);
+      Control *ctl;  // one status word for every solve of the call
+      ZG_TRY(control(s, &ctl));
       if (nt) {  // x = U^-1 L^-1 P b
         ZG_TRY(perm_gather_f64(n, nrhs, ipiv, true, Bd, ldb, Y, n, s));
         for (int c = 0; c < nrhs; ++c) {
           double *x = Bd + (long)c * ldb;
-          ZG_TRY(trsv_f64(n, Ad, lda, false, false, true, Y + (long)c * n, x, xw, s));
-          ZG_TRY(trsv_f64(n, Ad, lda, false, true, false, x, x, xw, s));
+          ZG_TRY(trsv_f64(n, Ad, lda, false, false, true, Y + (long)c * n, x, xw, ctl, s));
+          ZG_TRY(trsv_f64(n, Ad, lda, false, true, false, x, x, xw, ctl, s));
         }
       } else {  // x = P^T L^-T U^-T b
         for (int c = 0; c < nrhs; ++c) {
           double *y = Y + (long)c * n;
-          ZG_TRY(trsv_f64(n, Ad, lda, true, false, false, Bd + (long)c * ldb, y, xw, s));
-          ZG_TRY(trsv_f64(n, Ad, lda, true, true, true, y, y, xw, s));
+          ZG_TRY(trsv_f64(n, Ad, lda, true, false, false, Bd + (long)c * ldb, y, xw, ctl, s));
+          ZG_TRY(trsv_f64(n, Ad, lda, true, true, true, y, y, xw, ctl, s));
         }
         ZG_TRY(perm_gather_f64(n, nrhs, ipiv, false, Y, n, Bd, ldb, s));
       }
-      return 0;
+      return check_status(s, ctl, nullptr);  // a poll that ran out: kErrTimeout
     }
   }
   if (nt) {
@@ -780,11 +774,10 @@ template int laswp_dev<float2>(int, float2 *, long, int, int, const int *, int, 
 // ===========================================================================
 // LU without any allocation: zml_gpu_dgetrf_noalloc.
 //
-// Some callers cannot allocate device memory at solve time: code that is being
-// captured into a CUDA graph (cudaMalloc is not a capturable operation), hosts
-// whose device memory belongs to another allocator (a framework's caching
-// allocator, a fixed arena set up at start-up), and real-time loops that may
-// not allocate after initialisation.  This entry point gives them the FP64
+// Some callers cannot allocate device memory at solve time: hosts whose device
+// memory belongs to another allocator (a framework's caching allocator, a fixed
+// arena set up at start-up, which a cudaMalloc from the library would fragment
+// or overrun), and real-time loops that may not allocate after initialisation.  This entry point gives them the FP64
 // getrf with every scratch buffer it needs -- the panel's control words, the
 // candidate-pivot exchange and the composed row-interchange pairs -- carved
 // from one static device array that every GPU loading the library holds

@@ -182,13 +182,8 @@ __global__ void __launch_bounds__(32 * kInvColsPerCta)
 
 static int inv_unit_lower(int nb, const float *L, long ldl, float *X, long ldx, cudaStream_t s) {
   if (nb <= 0) return 0;
-  static bool attr = false;
   const int smem = kInvN * kInvLd * sizeof(float);
-  if (!attr) {
-    ZG_CUDA(cudaFuncSetAttribute(inv_unit_lower_cols_kernel,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    attr = true;
-  }
+  ZG_TRY(smem_optin(inv_unit_lower_cols_kernel, smem));
   ZG_LAUNCH(kTagTrsmDiag, nb * (double)nb * nb / 3.0, 0, s,
             inv_unit_lower_cols_kernel<<<ceil_div(nb, kInvColsPerCta), 32 * kInvColsPerCta, smem,
                                          s>>>(nb, L, ldl, X, ldx));
@@ -285,12 +280,7 @@ static int gemm_small(int m, int n, int k, float alpha, const float *A, long lda
   if (m <= 0 || n <= 0) return 0;
   if (m <= kG128 && k <= kG128) {
     const int smem = sizeof(float) * (kG128 * (kG128 + 1) + kG128 * 33);
-    static bool attr = false;
-    if (!attr) {
-      ZG_CUDA(cudaFuncSetAttribute(gemm128_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   smem));
-      attr = true;
-    }
+    ZG_TRY(smem_optin(gemm128_kernel, smem));
     ZG_LAUNCH(kTagGemmSimt, 2.0 * m * n * k, 4.0 * ((double)m * k + (double)k * n + 2.0 * m * n),
               s, gemm128_kernel<<<ceil_div(n, 32), 256, smem, s>>>(m, n, k, alpha, A, lda, B, ldb,
                                                                   beta, C, ldc));
@@ -695,8 +685,9 @@ __global__ void __launch_bounds__(kTT) trsv_lowp_kernel(int n, const float *__re
       if (c < n) {
         unsigned long long w = ld_relaxed_u64(xpub + c);
         long long spins = 0;
+        const long long lim = spin_limit();
         while (w == kTrsvEmpty) {
-          if (++spins > kSpinLimit) {
+          if (++spins > lim) {
             atomicOr(status, kStatusQueueTimeout);
             break;
           }
@@ -853,12 +844,7 @@ int invert_diag_blocks(int n, const float *A, long lda, double *Linv, double *Ui
                        float *Uinv32, bool lower_unit, cudaStream_t s) {
   const int nblk = ceil_div(n, kTB);
   const size_t smem = sizeof(double) * kTB * kTB;
-  static bool attr = false;
-  if (!attr) {
-    ZG_CUDA(cudaFuncSetAttribute(invert_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-    attr = true;
-  }
+  ZG_TRY(smem_optin(invert_diag_kernel, (int)smem));
   ZG_LAUNCH(kTagTrsv, 2.0 * nblk * kTB * kTB * kTB / 3, 8.0 * nblk * kTB * kTB * 3, s,
             invert_diag_kernel<<<dim3(nblk, 2), 512, smem, s>>>(n, A, lda, Linv, Uinv, Linv32,
                                                                 Uinv32, lower_unit));
@@ -879,12 +865,7 @@ int trsv_lowp(int n, const float *A, long lda, const F *Dinv, double *x, bool up
   ZG_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned), s));
   ZG_CUDA(cudaMemsetAsync(xpub, 0xff, sizeof(double) * n, s));
   const size_t smem = sizeof(F) * kTB * kTB;
-  static bool attr = false;
-  if (!attr) {
-    ZG_CUDA(cudaFuncSetAttribute(trsv_lowp_kernel<F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-    attr = true;
-  }
+  ZG_TRY(smem_optin(trsv_lowp_kernel<F>, (int)smem));
   ZG_LAUNCH(kTagTrsv, 1.0 * n * n, 2.0 * n * n + 16.0 * n + sizeof(F) * nblk * kTB * kTB, s,
             trsv_lowp_kernel<F><<<nblk, kTT, smem, s>>>(n, A, lda, Dinv, x, xpub, work, upper,
                                                         status));
@@ -1348,54 +1329,15 @@ static int mpir_refine(MpirCtx &c, const MpirOpts &o, int nrhs, const double *B,
   return 0;
 }
 
-static int solve_mpir_dev(bool spd, bool lower, int n, int nrhs, const double *A, long lda,
-                          const double *B, long ldb, double *X, long ldx, const MpirOpts &o,
-                          MpirResult *res, cudaStream_t s) {
-  *res = MpirResult{};
-  if (n <= 0 || nrhs <= 0) return 0;
-  MpirCtx c;
-  ZG_TRY(mpir_factor(spd, lower, n, A, lda, o, &c, res, s));
-  if (res->info != 0) return 0;
-  return mpir_refine(c, o, nrhs, B, ldb, X, ldx, false, res, s);
-}
-
-int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, long ldb,
-                  double *X, long ldx, const MpirOpts &o, MpirResult *res, cudaStream_t s) {
-  return solve_mpir_dev(false, false, n, nrhs, A, lda, B, ldb, X, ldx, o, res, s);
-}
-
-int posv_mpir_dev(bool lower, int n, int nrhs, const double *A, long lda, const double *B,
-                  long ldb, double *X, long ldx, const MpirOpts &o, MpirResult *res,
-                  cudaStream_t s) {
-  return solve_mpir_dev(true, lower, n, nrhs, A, lda, B, ldb, X, ldx, o, res, s);
-}
-
 // ---------------------------------------------------------------------------
-// Precision selection.
+// The plain FP64 factorizations, on a copy of A, as the last resort of the
+// mixed solvers (their refinement stopped short) and of the precision ladder.
 
-// The last resort: plain FP64 partial-pivot LU and solve (the reference's
-// gesv, getrf.zig:14 + getrs.zig:13) on a copy of A, with the backward error
-// of each column.
-static int fp64_solve(int n, int nrhs, const double *A, long lda, const double *B, long ldb,
-                      double *X, long ldx, double *berr, int *info, cudaStream_t s) {
+// Largest normwise backward error over the nrhs columns of X for A X = B (A
+// full, column-major); infinite if any column's is not finite.
+static int berr_cols(int n, int nrhs, const double *A, long lda, const double *B, long ldb,
+                     const double *X, long ldx, IRWork &w, double *berr, cudaStream_t s) {
   const int nparts = ceil_div(n, kGemvCols);
-  const size_t nd = (size_t)n * n + (size_t)n * (1 + nparts) + 8;
-  void *wp;
-  ZG_TRY(workspace(s, kSlotF64LU, sizeof(double) * nd + sizeof(int) * (size_t)n + 256, &wp));
-  double *LU = (double *)wp;
-  IRWork w{};
-  w.r = LU + (size_t)n * n;
-  w.part = w.r + n;
-  w.scal = w.part + (size_t)n * nparts;
-  int *piv = (int *)(w.scal + 8);
-  ZG_CUDA(cudaMemcpy2DAsync(LU, sizeof(double) * n, A, sizeof(double) * lda, sizeof(double) * n,
-                            n, cudaMemcpyDeviceToDevice, s));
-  *berr = INFINITY;
-  ZG_TRY(getrf_dev<double>(n, n, LU, n, piv, info, s));
-  if (*info != 0) return 0;
-  ZG_CUDA(cudaMemcpy2DAsync(X, sizeof(double) * ldx, B, sizeof(double) * ldb, sizeof(double) * n,
-                            nrhs, cudaMemcpyDeviceToDevice, s));
-  ZG_TRY(getrs_dev<double>(kNoTrans, n, nrhs, LU, n, piv, X, ldx, s));
   ZG_LAUNCH(kTagGemv, 0, 8.0 * n * n, s,
             rowabs_partial_kernel<<<dim3(ceil_div(n, kGemvRows), nparts), kGemvRows, 0, s>>>(
                 n, A, lda, w.part));
@@ -1415,6 +1357,108 @@ static int fp64_solve(int n, int nrhs, const double *A, long lda, const double *
   }
   return 0;
 }
+
+// Workspace of the FP64 fallback: the factor copy (ld n), the pivots and the
+// vectors of berr_cols.
+static int fp64_work(int n, double **F, int **piv, IRWork *w, cudaStream_t s) {
+  const int nparts = ceil_div(n, kGemvCols);
+  const size_t nd = (size_t)n * n + (size_t)n * (1 + nparts) + 8;
+  void *wp;
+  ZG_TRY(workspace(s, kSlotF64LU, sizeof(double) * nd + sizeof(int) * (size_t)n + 256, &wp));
+  *F = (double *)wp;
+  *w = IRWork{};
+  w->r = *F + (size_t)n * n;
+  w->part = w->r + n;
+  w->scal = w->part + (size_t)n * nparts;
+  *piv = (int *)(w->scal + 8);
+  return 0;
+}
+
+// Plain FP64 partial-pivot LU and solve (the reference's gesv, getrf.zig:14 +
+// getrs.zig:13) on a copy of A, with the largest backward error over the
+// columns; X is left unset when info > 0.
+static int fp64_solve(int n, int nrhs, const double *A, long lda, const double *B, long ldb,
+                      double *X, long ldx, double *berr, int *info, cudaStream_t s) {
+  double *LU;
+  int *piv;
+  IRWork w;
+  ZG_TRY(fp64_work(n, &LU, &piv, &w, s));
+  ZG_CUDA(cudaMemcpy2DAsync(LU, sizeof(double) * n, A, sizeof(double) * lda, sizeof(double) * n,
+                            n, cudaMemcpyDeviceToDevice, s));
+  *berr = INFINITY;
+  ZG_TRY(getrf_dev<double>(n, n, LU, n, piv, info, s));
+  if (*info != 0) return 0;
+  ZG_CUDA(cudaMemcpy2DAsync(X, sizeof(double) * ldx, B, sizeof(double) * ldb, sizeof(double) * n,
+                            nrhs, cudaMemcpyDeviceToDevice, s));
+  ZG_TRY(getrs_dev<double>(kNoTrans, n, nrhs, LU, n, piv, X, ldx, s));
+  return berr_cols(n, nrhs, A, lda, B, ldb, X, ldx, w, berr, s);
+}
+
+// The SPD counterpart (posv.zig:15: potrf.zig:17 + potrs.zig:15) on a copy of
+// the `lower` (else upper) triangle of A; the backward error is measured on
+// the full symmetric matrix, which is rebuilt into the Sym slot.
+static int fp64_posv(bool lower, int n, int nrhs, const double *A, long lda, const double *B,
+                     long ldb, double *X, long ldx, double *berr, int *info, cudaStream_t s) {
+  double *F;
+  int *piv;
+  IRWork w;
+  ZG_TRY(fp64_work(n, &F, &piv, &w, s));
+  ZG_CUDA(cudaMemcpy2DAsync(F, sizeof(double) * n, A, sizeof(double) * lda, sizeof(double) * n,
+                            n, cudaMemcpyDeviceToDevice, s));
+  *berr = INFINITY;
+  const int uplo = lower ? kLower : kUpper;
+  ZG_TRY(potrf_dev<double>(uplo, n, F, n, info, s));
+  if (*info != 0) return 0;
+  ZG_CUDA(cudaMemcpy2DAsync(X, sizeof(double) * ldx, B, sizeof(double) * ldb, sizeof(double) * n,
+                            nrhs, cudaMemcpyDeviceToDevice, s));
+  ZG_TRY(potrs_dev<double>(uplo, n, nrhs, F, n, X, ldx, s));
+  void *ws;
+  ZG_TRY(workspace(s, kSlotSym, sizeof(double) * (size_t)n * n, &ws));
+  ZG_LAUNCH(kTagConvert, 0, 16.0 * n * n, s,
+            sym_full_kernel<<<grid1d((long)n * n), 256, 0, s>>>(n, A, lda, lower, (double *)ws));
+  return berr_cols(n, nrhs, (const double *)ws, n, B, ldb, X, ldx, w, berr, s);
+}
+
+static int solve_mpir_dev(bool spd, bool lower, int n, int nrhs, const double *A, long lda,
+                          const double *B, long ldb, double *X, long ldx, const MpirOpts &o,
+                          MpirResult *res, cudaStream_t s) {
+  *res = MpirResult{};
+  if (n <= 0 || nrhs <= 0) return 0;
+  MpirCtx c;
+  ZG_TRY(mpir_factor(spd, lower, n, A, lda, o, &c, res, s));
+  if (res->info == 0) ZG_TRY(mpir_refine(c, o, nrhs, B, ldb, X, ldx, false, res, s));
+  if (!o.fallback || (res->info == 0 && res->converged)) return 0;
+  // the safety net: the low-precision factors could not take the backward
+  // error down to the target, so the FP64 factorization solves the system
+  double berr = INFINITY;
+  int info = 0;
+  if (spd)
+    ZG_TRY(fp64_posv(lower, n, nrhs, A, lda, B, ldb, X, ldx, &berr, &info, s));
+  else
+    ZG_TRY(fp64_solve(n, nrhs, A, lda, B, ldb, X, ldx, &berr, &info, s));
+  res->fp64_fallback = 1;
+  res->info = info;
+  res->berr = berr;
+  // the FP64 factorization's backward error is FP64 accuracy by definition,
+  // even where it lies a little above a tol taken from another FP64 solve
+  const double goal = std::max(o.tol > 0 ? o.tol : 0.0, 64 * 1.1102230246251565e-16);
+  res->converged = info == 0 && std::isfinite(berr) && berr <= goal;
+  return 0;
+}
+
+int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, long ldb,
+                  double *X, long ldx, const MpirOpts &o, MpirResult *res, cudaStream_t s) {
+  return solve_mpir_dev(false, false, n, nrhs, A, lda, B, ldb, X, ldx, o, res, s);
+}
+
+int posv_mpir_dev(bool lower, int n, int nrhs, const double *A, long lda, const double *B,
+                  long ldb, double *X, long ldx, const MpirOpts &o, MpirResult *res,
+                  cudaStream_t s) {
+  return solve_mpir_dev(true, lower, n, nrhs, A, lda, B, ldb, X, ldx, o, res, s);
+}
+
+// ---------------------------------------------------------------------------
+// Precision selection.
 
 void probe_features(const MpirResult &pr, float *f) {
   // log10 of a backward error, clamped to [1e-18, 1e2] (non-finite: 1e2)

@@ -239,7 +239,10 @@ __global__ void __launch_bounds__(kPcThreads, 1)
       if (tid == 0) tc::mbar_expect_tx(&sh.mbar[b], xbytes);
       // the cluster's pivot, identical in every CTA
       const unsigned long long g = warp_max64(lane < nct ? sh.skey[b][lane] : 0ull);
-      const int p = pc_row(g);
+      // a row outside [k, m) only after an exchange timed out (stale words):
+      // row k stands in, so that the slot index and the swaps stay in range
+      int p = pc_row(g);
+      if (p < k || p >= m) p = k;
       const float *prow = sh.slot[b][p / R];
       const float piv = prow[32];
       const bool swap = piv != 0.f && p != k;

@@ -212,13 +212,7 @@ static int qr_panel(int m, int nb, T *A, long lda, T *tau, T *Tout, T *xchg, Con
   nblk = ceil_div(m, R);
   // CTA 0 reuses its shared memory for G and T (2 nb^2) at the end
   const size_t smem = std::max((size_t)R * nb, (size_t)2 * nb * nb) * sizeof(T);
-  static bool attr[2] = {false, false};
-  const int ti = sizeof(T) == 8 ? 0 : 1;
-  if (!attr[ti]) {
-    ZG_CUDA(cudaFuncSetAttribute(qr_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)limit));
-    attr[ti] = true;
-  }
+  ZG_TRY(smem_optin(qr_panel_kernel<T>, (int)limit));
   ZG_CUDA(cudaMemsetAsync(&ctl->barrier[0], 0, 2 * sizeof(unsigned), s));
   void *args[] = {&m, &nb, &A, &lda, &tau, &Tout, &ctl, &R, &xchg};
   ZG_LAUNCH(kTagQR, 4.0 * m * nb * nb, 2.0 * sizeof(T) * m * nb, s,

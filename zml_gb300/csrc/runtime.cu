@@ -42,6 +42,41 @@ int device_info(DeviceInfo *out) {
   return 0;
 }
 
+static std::vector<int (*)(long long)> &spin_setters() {
+  static std::vector<int (*)(long long)> v;  // built during static initialisation
+  return v;
+}
+
+int register_spin_setter(int (*set)(long long)) {
+  spin_setters().push_back(set);
+  return 0;
+}
+
+int set_spin_limit(long long tries) {
+  if (tries <= 0) tries = kSpinLimit;
+  for (auto set : spin_setters()) {
+    if (set(tries) != 0) {
+      set_last_error("set_spin_limit: cudaMemcpyToSymbol failed");
+      return kErrCuda;
+    }
+  }
+  return 0;
+}
+
+static std::map<std::pair<int, const void *>, int> g_smem_optin;
+
+int smem_optin_raw(const void *func, int bytes) {
+  int dev = 0;
+  ZG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_mu);
+  int &have = g_smem_optin[{dev, func}];
+  if (bytes > have) {
+    ZG_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    have = bytes;
+  }
+  return 0;
+}
+
 struct StreamState {
   Workspace ws[kNumSlots];
   Control *ctl = nullptr;

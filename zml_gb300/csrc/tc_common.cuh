@@ -1,6 +1,6 @@
 // tc_common.cuh -- Blackwell (sm_103a) building blocks written as inline PTX:
 // mbarriers, TMA tensor copies, tcgen05 MMA / TMEM and their descriptors.
-// Every wait is bounded (kSpinLimit tries) and reports a status bit.
+// Every wait is bounded (spin_limit() tries) and reports a status bit.
 #pragma once
 #include <cuda.h>
 
@@ -45,7 +45,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 
 // Bounded wait; returns false (and sets the status bit) on timeout.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, unsigned *status) {
-  for (long long i = 0; i < kSpinLimit; ++i)
+  const long long lim = spin_limit();
+  for (long long i = 0; i < lim; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   if (status) atomicOr(status, kStatusMbarTimeout);
   return false;

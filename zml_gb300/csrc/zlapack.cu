@@ -214,12 +214,7 @@ int ztrsm_dev(int side, int uplo, int transa, int diag, int m, int n, const R *a
   const C2 *Ac = (const C2 *)A;
   C2 *Bc = (C2 *)B;
   const size_t smem = sizeof(C2) * kZB * (kZB + 1);
-  static bool attr = false;
-  if (!attr) {
-    ZG_CUDA(cudaFuncSetAttribute(ctrsm_diag_kernel<R, C2>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  ZG_TRY(smem_optin(ctrsm_diag_kernel<R, C2>, (int)smem));
   const int nblk = ceil_div(m, kZB);
   for (int q = 0; q < nblk; ++q) {
     const int b = lower ? q : nblk - 1 - q;
