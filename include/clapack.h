@@ -334,6 +334,19 @@ const char *zml_gpu_last_error(void);
  * index kept in range; the call then returns ZML_GPU_ERR_TIMEOUT.  For tests
  * of that path; no counterpart in the reference. */
 int zml_gpu_set_spin_limit(long long tries);
+/* Pivoting of the mixed-precision LU's panels (zml_*gesv_mpir, the ladder):
+ * 1 tournament pivoting (the default: a communication-avoiding LU whose
+ * 32-column sub-panels need one exchange between the panel's thread blocks
+ * instead of one per column), 0 partial pivoting.  Returns the previous
+ * setting.  No counterpart in the reference (its getrf2 pivots partially). */
+int zml_gpu_mixed_panel(int tournament);
+/* FP32 LU with tournament pivoting on device memory (column-major), the
+ * factorization the mixed solver preconditions with: P A = L U as sgetrf's,
+ * ipiv in LAPACK's form, but each 32-column sub-panel's pivots are chosen
+ * among candidates the panel's thread blocks nominate from their own rows, so
+ * they can differ from partial pivoting's.  info > 0: a zero pivot.  No
+ * counterpart in the reference. */
+int zml_gpu_sgetrf_calu(int m, int n, float *dA, int ldda, int *dipiv, int *info, void *stream);
 /* ABI version of this library. */
 int zml_gpu_version(void);
 

@@ -1205,6 +1205,18 @@ const char *zml_gpu_last_error(void) { return last_error(); }
 
 int zml_gpu_set_spin_limit(long long tries) { return set_spin_limit(tries); }
 
+int zml_gpu_mixed_panel(int tournament) { return set_mixed_tournament(tournament); }
+
+int zml_gpu_sgetrf_calu(int m, int n, float *dA, int ldda, int *dipiv, int *info, void *stream) {
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (ldda < std::max(1, m)) return -4;
+  int inf = 0;
+  ZG_TRY(getrf_dev<float>(m, n, dA, ldda, dipiv, &inf, (cudaStream_t)stream, true));
+  if (info) *info = inf;
+  return 0;
+}
+
 int zml_gpu_version(void) { return 1; }
 
 }  // extern "C"

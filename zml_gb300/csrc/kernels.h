@@ -89,11 +89,16 @@ int panel_lu(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *c
 // leaves it to panel_lu.  The interchanges are also applied to the xl
 // columns at XL and the xr columns at XR (leading dim lda, rows aligned with
 // the panel's), as laswp would.
+// tournament: pivots by tournament (communication-avoiding LU) instead of
+// partial pivoting -- one cluster exchange per 32-column sub-panel instead of
+// one per column; P A = L U still holds, with different pivots.
 int panel_lu_cluster(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base, Control *ctl,
                      int info_base, cudaStream_t s, bool *launched, float *XL = nullptr,
-                     int xl = 0, float *XR = nullptr, int xr = 0);
+                     int xl = 0, float *XR = nullptr, int xr = 0, bool tournament = false);
+// tournament: FP32 panels by tournament pivoting (see panel_lu_cluster).
 template <typename T>
-int getrf_dev(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s);
+int getrf_dev(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s,
+              bool tournament = false);
 template <typename T>
 int getrs_dev(int trans, int n, int nrhs, const T *A, long lda, const int *ipiv, T *B, long ldb,
               cudaStream_t s);

@@ -41,6 +41,9 @@ struct MpirResult {
 };
 
 int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cudaStream_t s);
+// Panels of getrf_lowp: tournament pivoting (on != 0, the default) or partial
+// pivoting; returns the previous setting.
+int set_mixed_tournament(int on);
 // Solves A X = B (device pointers, column-major) to FP64 accuracy: one
 // low-precision factorization, then refinement of each right-hand side.
 int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, long ldb,

@@ -400,17 +400,19 @@ template <typename T> static int lu_block() { return sizeof(T) == 8 ? 64 : 128; 
 // FP32 panels go to the cluster-resident panel where it applies.
 template <typename T>
 static int panel_any(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *ctl,
-                     int info_base, cudaStream_t s) {
+                     int info_base, cudaStream_t s, bool tournament) {
   if constexpr (sizeof(T) == sizeof(float)) {
     bool done = false;
-    ZG_TRY(panel_lu_cluster(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, &done));
+    ZG_TRY(panel_lu_cluster(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, &done, nullptr, 0,
+                            nullptr, 0, tournament));
     if (done) return 0;
   }
   return panel_lu<T>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s);
 }
 
 template <typename T>
-int getrf_dev(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s) {
+int getrf_dev(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s,
+              bool tournament) {
   *info = 0;
   if (m <= 0 || n <= 0) return 0;
   Control *ctl;
@@ -420,7 +422,7 @@ int getrf_dev(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s
   for (int j = 0; j < mn; j += nb) {
     const int jb = min(nb, mn - j);
     T *Ajj = A + j + (long)j * lda;
-    ZG_TRY(panel_any<T>(m - j, jb, Ajj, lda, ipiv + j, j, ctl, j, s));
+    ZG_TRY(panel_any<T>(m - j, jb, Ajj, lda, ipiv + j, j, ctl, j, s, tournament));
     ZG_TRY(laswp_panel<T>(j, std::min(n, j + jb), n, A, lda, j + 1, j + jb, ipiv, s));
     if (j + jb < n) {
       T *Aright = A + (long)(j + jb) * lda;
@@ -760,7 +762,7 @@ int getrs_dev(int trans, int n, int nrhs, const T *A, long lda, const int *ipiv,
   template int laswp_panel<T>(int, int, int, T *, long, int, int, const int *, cudaStream_t);    \
   template int panel_lu<T>(int, int, T *, long, int *, int, Control *, int, cudaStream_t);      \
   template int laswp_dev<T>(int, T *, long, int, int, const int *, int, cudaStream_t);          \
-  template int getrf_dev<T>(int, int, T *, long, int *, int *, cudaStream_t);                   \
+  template int getrf_dev<T>(int, int, T *, long, int *, int *, cudaStream_t, bool);                   \
   template int getrs_dev<T>(int, int, int, const T *, long, const int *, T *, long, cudaStream_t);
 INST(double)
 INST(float)

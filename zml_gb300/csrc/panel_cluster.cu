@@ -34,6 +34,9 @@
 // back) and each CTA updates
 // its own rows of the columns to the right, A22 -= L21 U12, with L21 loaded
 // into registers.
+#include <map>
+#include <mutex>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "tc_common.cuh"
@@ -90,6 +93,15 @@ __device__ __forceinline__ unsigned long long pc_word(float v, int row, int k) {
   const unsigned ord = key == -INFINITY ? 0u : __float_as_uint(key) + 1u;
   return ((unsigned long long)ord << 32) | (unsigned)(0xffffffffu - (unsigned)row);
 }
+// The tournament's word: as pc_word, but a NaN below the diagonal orders just
+// above zero instead of at zero, so that every row still in play remains a
+// candidate and each elimination step always finds a pivot row.
+__device__ __forceinline__ unsigned long long tw_word(float v, int row, int k) {
+  float key = fabsf(v);
+  if (v != v) key = row == k ? INFINITY : -INFINITY;
+  const unsigned ord = key == -INFINITY ? 1u : __float_as_uint(key) + 2u;
+  return ((unsigned long long)ord << 32) | (unsigned)(0xffffffffu - (unsigned)row);
+}
 // Warp maximum of 64-bit words: the high halves first, then the low halves
 // among the lanes that hold the highest one.
 __device__ __forceinline__ unsigned long long warp_max64(unsigned long long w) {
@@ -121,6 +133,15 @@ struct __align__(16) PcShared {
   int piv[32];                             // pivot rows of the sub-panel (panel-relative)
   int mdst[64], msrc[64];                  // the sub-panel's interchanges, composed
   float L11[32][33];                       // unit-lower diagonal block of the sub-panel
+  // tournament pivoting (TOURN): the CTA's local candidates, the cluster's
+  // pivot rows in order, U11 of the sub-panel and 1 / its diagonal, the
+  // argmax words of the final elimination and the exchange's mbarrier
+  int lcand[32];
+  int fpiv[32];
+  float U11[32][33];
+  float rdiag[32];
+  unsigned long long fmax[2];
+  uint64_t tmbar;
   alignas(16) float U[kPcMaxRight][kPcUStride];  // U12 by right column: U[c][k]
 };
 
@@ -134,7 +155,7 @@ __device__ __forceinline__ int pc_trace(int x, int c0, int ws, const int *piv) {
   return x;
 }
 
-template <int RPT, int W>
+template <int RPT, int W, bool TOURN>
 __global__ void __launch_bounds__(kPcThreads, 1)
     panel_cluster_kernel(int m, int nb, float *__restrict__ A, long lda, int *__restrict__ ipiv,
                          int ipiv_base, Control *ctl, int info_base, float *XL, int xl,
@@ -152,11 +173,20 @@ __global__ void __launch_bounds__(kPcThreads, 1)
   // bytes landing in this CTA per column: every CTA's candidate row (two
   // words a lane) and word, and row k from CTA 0
   const unsigned xbytes = nct * (2 * 32 * 4 + 8) + 2 * 32 * 4;
-  if (tid < 2) sh.cmax[tid] = 0;
+  // tournament: every CTA's W candidate rows (W values and the row) and, from
+  // CTA 0, the sub-panel's W top rows land in this CTA's Lsm once per sub-panel
+  const unsigned tbytes = (unsigned)(nct * W * (W + 1) + W * W) * 4u;
+  if (tid < 2) sh.cmax[tid] = sh.fmax[tid] = 0;
   if (tid == 0) {
-    for (int q = 0; q < kPcBuf; ++q) tc::mbar_init(&sh.mbar[q], 1);
-    tc::fence_barrier_init();
-    for (int q = 0; q < kPcBuf; ++q) tc::mbar_expect_tx(&sh.mbar[q], xbytes);
+    if constexpr (TOURN) {
+      tc::mbar_init(&sh.tmbar, 1);
+      tc::fence_barrier_init();
+      tc::mbar_expect_tx(&sh.tmbar, tbytes);
+    } else {
+      for (int q = 0; q < kPcBuf; ++q) tc::mbar_init(&sh.mbar[q], 1);
+      tc::fence_barrier_init();
+      for (int q = 0; q < kPcBuf; ++q) tc::mbar_expect_tx(&sh.mbar[q], xbytes);
+    }
   }
   // every CTA of the cluster runs, and its slots and mbarriers are ready,
   // before any remote write
@@ -173,147 +203,359 @@ __global__ void __launch_bounds__(kPcThreads, 1)
         v[i][c] = (row < m && c < ws) ? __ldcg(A + row + (long)(c0 + c) * lda) : 0.f;
     }
 
-    // B. factor the sub-panel, one exchange per column.  v[i][c] holds
-    // column kk + c of the thread's rows; Lsm holds columns < kk.
+    if constexpr (TOURN) {
+      // B'. Tournament pivoting (communication-avoiding LU, flat tree over the
+      // cluster): the sub-panel's pivots come from one exchange instead of one
+      // per column.
+      //  1. every CTA runs partial-pivot elimination on its own rows only (a
+      //     CTA-wide argmax a column, no cluster traffic) to pick W candidate
+      //     rows;
+      //  2. it pushes their original values (re-read from A, which still holds
+      //     the sub-panel as it entered) into every CTA, and CTA 0 also pushes
+      //     the sub-panel's top W rows;
+      //  3. every CTA eliminates the <= 16 W candidates in the same order and
+      //     so chooses the same W pivot rows, with U11 and the pivot rows'
+      //     multipliers L11;
+      //  4. each row's multipliers are its original values times U11^-1
+      //     (forward substitution), which is what elimination with those
+      //     pivots computes; the results go to Lsm for phase C.
+      float *rcv = Lsm;                          // [nct W][W + 1]: values, then the row
+      float *top = Lsm + (long)nct * W * (W + 1);  // [W][W]: rows c0 .. c0 + W - 1
+      // 1. local selection
+      if (tid < 2) sh.cmax[tid] = sh.fmax[tid] = 0;
+      __syncthreads();
+      unsigned used = 0;  // bit i: the thread's row i is a candidate already
 #pragma unroll 1
-    for (int kk = 0; kk < ws; ++kk) {
-      const int k = c0 + kk, par = k & 1, b = k % kPcBuf;
-      unsigned long long best = 0;
+      for (int kk = 0; kk < ws; ++kk) {
+        const int k = c0 + kk, par = kk & 1;
+        unsigned long long best = 0;
 #pragma unroll
-      for (int i = 0; i < RPT; ++i) {
-        const int row = r0 + tid + i * T;
-        if (row >= k && row < m) best = max(best, pc_word(v[i][0], row, k));
-      }
-      best = warp_max64(best);
-      if (lane == 0 && best != 0) atomicMax(&sh.cmax[par], best);
-      __syncthreads();
-      // every thread has read the previous column's word: clear it for the next
-      if (tid == 0) sh.cmax[par ^ 1] = 0;
-      const unsigned long long cbest = sh.cmax[par];
-      const int wrow = cbest != 0 ? pc_row(cbest) : -1;
-      // owners stage the register part of the CTA's winning row and of row k:
-      // [c] = column kk + 1 + c, [32] = column kk
-#pragma unroll
-      for (int i = 0; i < RPT; ++i) {
-        const int row = r0 + tid + i * T;
-        if (row == wrow || row == k) {
-          float *dst = row == wrow ? sh.cand : sh.krow;
-#pragma unroll
-          for (int c = 0; c + 1 < W; ++c) dst[c] = v[i][c + 1];
-#pragma unroll
-          for (int c = W - 1; c < 32; ++c) dst[c] = 0.f;
-          dst[32] = v[i][0];
-          if (row == wrow && row == k)
-#pragma unroll
-            for (int c = 0; c < 33; ++c) sh.krow[c] = sh.cand[c];
+        for (int i = 0; i < RPT; ++i) {
+          const int row = r0 + tid + i * T;
+          if (!((used >> i) & 1u) && row >= c0 && row < m)
+            best = max(best, tw_word(v[i][0], row, k));
         }
-      }
-      __syncthreads();
-      // warp w pushes to CTAs w, w + nwarps, ...: the candidate, its word,
-      // and (CTA 0) row k
-      if (warp < nct) {
-        float lo = 0.f, hi = 0.f;
-        if (wrow >= 0) {
-          lo = sh.cand[lane];
-          hi = lane == 0 ? sh.cand[32] : (lane - 1 < kk ? Lsm[(lane - 1) * LD + (wrow - r0)] : 0.f);
-        }
-        float klo = 0.f, khi = 0.f;
-        if (rank == 0) {  // row k < nb <= R lies in CTA 0
-          klo = sh.krow[lane];
-          khi = lane == 0 ? sh.krow[32] : (lane - 1 < kk ? Lsm[(lane - 1) * LD + k] : 0.f);
-        }
-        for (int d = warp; d < nct; d += nwarps) {
-          const unsigned mb = remote_addr(&sh.mbar[b], d);
-          st_async(remote_addr(&sh.slot[b][rank][lane], d), lo, mb);
-          st_async(remote_addr(&sh.slot[b][rank][32 + lane], d), hi, mb);
-          if (lane == 0) st_async(remote_addr(&sh.skey[b][rank], d), cbest, mb);
-          if (rank == 0) {
-            st_async(remote_addr(&sh.rowk[b][lane], d), klo, mb);
-            st_async(remote_addr(&sh.rowk[b][32 + lane], d), khi, mb);
+        best = warp_max64(best);
+        if (lane == 0 && best != 0) atomicMax(&sh.cmax[par], best);
+        __syncthreads();
+        if (tid == 0) sh.cmax[par ^ 1] = 0;
+        const unsigned long long cb = sh.cmax[par];
+        const int lrow = cb != 0 ? pc_row(cb) : -1;
+#pragma unroll
+        for (int i = 0; i < RPT; ++i) {
+          const int row = r0 + tid + i * T;
+          if (row == lrow) {
+#pragma unroll
+            for (int c = 0; c + 1 < W; ++c) sh.cand[c] = v[i][c + 1];
+            sh.cand[32] = v[i][0];
+            used |= 1u << i;
           }
         }
-      }
-      // this column's pushes from every CTA have landed; then the buffer is
-      // armed for column k + kPcBuf
-      tc::mbar_wait(&sh.mbar[b], (k / kPcBuf) & 1, &ctl->status);
-      if (tid == 0) tc::mbar_expect_tx(&sh.mbar[b], xbytes);
-      // the cluster's pivot, identical in every CTA
-      const unsigned long long g = warp_max64(lane < nct ? sh.skey[b][lane] : 0ull);
-      // a row outside [k, m) only after an exchange timed out (stale words):
-      // row k stands in, so that the slot index and the swaps stay in range
-      int p = pc_row(g);
-      if (p < k || p >= m) p = k;
-      const float *prow = sh.slot[b][p / R];
-      const float piv = prow[32];
-      const bool swap = piv != 0.f && p != k;
-      if (tid == 0) {
-        sh.piv[kk] = swap ? p : k;
-        if (rank == 0) {
-          ipiv[k] = p + 1 + ipiv_base;
-          if (piv == 0.f) atomicCAS(&ctl->info, 0, k + 1 + info_base);
-        }
-      }
-      if (swap) {  // the finished part of rows k and p, one warp each
-        if (warp == nwarps - 2 && rank == 0 && lane < kk) Lsm[lane * LD + k] = prow[33 + lane];
-        if (warp == nwarps - 1 && p / R == rank && lane < kk)
-          Lsm[lane * LD + (p - r0)] = sh.rowk[b][33 + lane];
-      }
-      const bool recip = fabsf(piv) >= Real<float>::sfmin();
-      const float rp = 1.f / piv;
-      const int live = ws - 1 - kk;  // columns right of kk still to update
-      const float4 *p4 = reinterpret_cast<const float4 *>(prow);
+        if (tid == 0) sh.lcand[kk] = lrow;
+        __syncthreads();
+        const float piv = lrow >= 0 ? sh.cand[32] : 0.f;
+        const bool recip = fabsf(piv) >= Real<float>::sfmin();
+        const float rp = 1.f / piv;
 #pragma unroll
-      for (int i = 0; i < RPT; ++i) {
-        const int row = r0 + tid + i * T, lr = tid + i * T;
-        if (swap && (row == k || row == p)) {
-          const float *src = row == k ? prow : sh.rowk[b];
-          v[i][0] = src[32];
+        for (int i = 0; i < RPT; ++i) {
+          const int row = r0 + tid + i * T;
+          if (!((used >> i) & 1u) && row >= c0 && row < m && lrow >= 0) {
+            float x = v[i][0];
+            if (piv != 0.f) x = recip ? x * rp : x / piv;
 #pragma unroll
-          for (int c = 1; c < W; ++c) v[i][c] = src[c - 1];
-        }
-        float x = v[i][0];
-        const bool below = row > k && row < m;
-        if (below && piv != 0.f) {
-          if (recip) x *= rp;
-          else x = x / piv;
-        }
-        Lsm[kk * LD + lr] = x;
-        // rotate: column kk + 1 + c moves to register c; only the first
-        // `live` positions carry data, the rest are zero.  Rows not below
-        // the pivot move without arithmetic (an inf in the pivot row must
-        // not reach them through 0 * inf).
-        if (below) {
-          if (live > W / 2) {
-#pragma unroll
-            for (int j = 0; j < W / 4; ++j) {
-              const float4 q = p4[j];
-              v[i][4 * j + 0] = fmaf(-x, q.x, v[i][4 * j + 1]);
-              v[i][4 * j + 1] = fmaf(-x, q.y, v[i][4 * j + 2]);
-              v[i][4 * j + 2] = fmaf(-x, q.z, v[i][4 * j + 3]);
-              if (4 * j + 4 < W) v[i][4 * j + 3] = fmaf(-x, q.w, v[i][4 * j + 4]);
-            }
+            for (int c = 0; c + 1 < W; ++c) v[i][c] = fmaf(-x, sh.cand[c], v[i][c + 1]);
           } else {
 #pragma unroll
-            for (int j = 0; j < W / 8; ++j) {
-              const float4 q = p4[j];
-              v[i][4 * j + 0] = fmaf(-x, q.x, v[i][4 * j + 1]);
-              v[i][4 * j + 1] = fmaf(-x, q.y, v[i][4 * j + 2]);
-              v[i][4 * j + 2] = fmaf(-x, q.z, v[i][4 * j + 3]);
-              v[i][4 * j + 3] = fmaf(-x, q.w, v[i][4 * j + 4]);
-            }
+            for (int c = 0; c + 1 < W; ++c) v[i][c] = v[i][c + 1];
           }
+          v[i][W - 1] = 0.f;
+        }
+      }
+      for (int kk = ws + tid; kk < W; kk += T) sh.lcand[kk] = -1;
+      __syncthreads();
+      // 2. the exchange: slot q of CTA `rank` lands in rcv row rank W + q
+      for (int q = warp; q < W; q += nwarps) {
+        const int row = sh.lcand[q];
+        const float val = (row >= 0 && lane < ws) ? __ldcg(A + row + (long)(c0 + lane) * lda) : 0.f;
+        for (int d = 0; d < nct; ++d) {
+          const unsigned mb = remote_addr(&sh.tmbar, d);
+          const unsigned dst = remote_addr(rcv + (long)(rank * W + q) * (W + 1), d);
+          if (lane < W) st_async(dst + 4u * lane, val, mb);
+          if (lane == 0) st_async(dst + 4u * W, __int_as_float(row), mb);
+        }
+      }
+      if (rank == 0)
+        for (int t = warp; t < W; t += nwarps) {
+          const float val =
+              (t < ws && lane < ws) ? __ldcg(A + (c0 + t) + (long)(c0 + lane) * lda) : 0.f;
+          for (int d = 0; d < nct; ++d) {
+            const unsigned mb = remote_addr(&sh.tmbar, d);
+            if (lane < W) st_async(remote_addr(top + t * W + lane, d), val, mb);
+          }
+        }
+      tc::mbar_wait(&sh.tmbar, (c0 / W) & 1, &ctl->status);
+      if (tid == 0) tc::mbar_expect_tx(&sh.tmbar, tbytes);  // armed for the next sub-panel
+      // 3. the final elimination over the candidates, one a thread, the same
+      // in every CTA; a candidate's multipliers are kept in its rcv row
+      const int ncand = nct * W;
+      int cid = -1;
+      float cr[W];
+#pragma unroll
+      for (int c = 0; c < W; ++c) cr[c] = 0.f;
+      if (tid < ncand) {
+        cid = __float_as_int(rcv[tid * (W + 1) + W]);
+        if (cid < c0 || cid >= m) cid = -1;  // an empty slot (or words left by a timeout)
+#pragma unroll
+        for (int c = 0; c < W; ++c) cr[c] = rcv[tid * (W + 1) + c];
+      }
+      bool cdone = cid < 0;
+#pragma unroll 1
+      for (int j = 0; j < ws; ++j) {
+        const int k = c0 + j, par = j & 1;
+        unsigned long long best = cdone ? 0ull : tw_word(cr[0], cid, k);
+        best = warp_max64(best);
+        if (lane == 0 && best != 0) atomicMax(&sh.fmax[par], best);
+        __syncthreads();
+        if (tid == 0) sh.fmax[par ^ 1] = 0;
+        const unsigned long long g = sh.fmax[par];
+        const int prow = g != 0 ? pc_row(g) : -1;
+        if (!cdone && cid == prow) {  // this candidate is pivot j: U11 row j, L11 row j
+#pragma unroll
+          for (int c = 0; c < W; ++c)
+            if (j + c < W) sh.U11[j][j + c] = cr[c];
+          for (int c = 0; c < j; ++c) sh.L11[j][c] = rcv[tid * (W + 1) + c];
+          cdone = true;
+        }
+        if (tid == 0) {
+          sh.fpiv[j] = prow;
+          if (prow < 0) {  // no candidate left (only after a timeout): a zero step
+#pragma unroll 1
+            for (int c = j; c < W; ++c) sh.U11[j][c] = 0.f;
+            for (int c = 0; c < j; ++c) sh.L11[j][c] = 0.f;
+          }
+        }
+        __syncthreads();
+        const float piv = sh.U11[j][j];
+        const bool recip = fabsf(piv) >= Real<float>::sfmin();
+        const float rp = 1.f / piv;
+        if (!cdone) {
+          float x = cr[0];
+          if (piv != 0.f) x = recip ? x * rp : x / piv;
+          rcv[tid * (W + 1) + j] = x;
+#pragma unroll
+          for (int c = 0; c + 1 < W; ++c)
+            cr[c] = j + 1 + c < W ? fmaf(-x, sh.U11[j][min(j + 1 + c, W - 1)], cr[c + 1]) : 0.f;
         } else {
 #pragma unroll
-          for (int c = 0; c + 1 < W; ++c) v[i][c] = v[i][c + 1];
+          for (int c = 0; c + 1 < W; ++c) cr[c] = cr[c + 1];
         }
-        if (live <= W / 2) {
-#pragma unroll
-          for (int c = W / 2; c + 1 < W; ++c) v[i][c] = 0.f;
-        }
-        v[i][W - 1] = 0.f;
+        cr[W - 1] = 0.f;
       }
+      // the interchanges in LAPACK's form: step t swaps row c0 + t with the
+      // row where pivot row fpiv[t] sits after steps 0 .. t-1
+      if (tid == 0) {
+        for (int t = 0; t < ws; ++t) {
+          int pos = sh.fpiv[t];
+          if (pos < c0 || pos >= m) pos = c0 + t;
+          for (int u = 0; u < t; ++u) {
+            if (pos == c0 + u) pos = sh.piv[u];
+            else if (pos == sh.piv[u]) pos = c0 + u;
+          }
+          sh.piv[t] = pos;
+          if (rank == 0) {
+            ipiv[c0 + t] = pos + 1 + ipiv_base;
+            if (sh.U11[t][t] == 0.f) atomicCAS(&ctl->info, 0, c0 + t + 1 + info_base);
+          }
+        }
+      }
+      if (tid < W) {
+        const float u = tid < ws ? sh.U11[tid][tid] : 1.f;
+        sh.rdiag[tid] = 1.f / u;
+      }
+      __syncthreads();
+      // 4. every row of this CTA: its factored sub-panel row into registers
+#pragma unroll
+      for (int i = 0; i < RPT; ++i) {
+        const int lr = tid + i * T, x = r0 + lr;
+        if (x >= m) {
+#pragma unroll
+          for (int c = 0; c < W; ++c) v[i][c] = 0.f;
+        } else if (x < c0) {  // an earlier pivot row: unchanged
+#pragma unroll
+          for (int c = 0; c < W; ++c) v[i][c] = c < ws ? __ldcg(A + x + (long)(c0 + c) * lda) : 0.f;
+        } else if (x < c0 + ws) {  // pivot position: L11 row, then U11 row
+          const int t = x - c0;
+#pragma unroll
+          for (int c = 0; c < W; ++c) v[i][c] = c < ws ? (c < t ? sh.L11[t][c] : sh.U11[t][c]) : 0.f;
+        } else {
+          int src = pc_trace(x, c0, ws, sh.piv);  // x itself, or a displaced top row
+          if (src < c0 || src >= c0 + ws) src = x;
+#pragma unroll
+          for (int c = 0; c < W; ++c) {
+            float a = 0.f;
+            if (c < ws) a = src == x ? __ldcg(A + x + (long)(c0 + c) * lda) : top[(src - c0) * W + c];
+#pragma unroll
+            for (int q = 0; q < c; ++q) a = fmaf(-v[i][q], sh.U11[q][c], a);
+            if (c < ws) {
+              const float u = sh.U11[c][c];
+              if (u != 0.f) a = fabsf(u) >= Real<float>::sfmin() ? a * sh.rdiag[c] : a / u;
+            }
+            v[i][c] = c < ws ? a : 0.f;
+          }
+        }
+      }
+      __syncthreads();  // every read of rcv / top is done: Lsm takes the results
+#pragma unroll
+      for (int i = 0; i < RPT; ++i) {
+        const int lr = tid + i * T;
+#pragma unroll
+        for (int c = 0; c < W; ++c)
+          if (c < ws) Lsm[c * LD + lr] = v[i][c];
+      }
+      __syncthreads();
+    } else {
+      // B. factor the sub-panel, one exchange per column.  v[i][c] holds
+      // column kk + c of the thread's rows; Lsm holds columns < kk.
+  #pragma unroll 1
+      for (int kk = 0; kk < ws; ++kk) {
+        const int k = c0 + kk, par = k & 1, b = k % kPcBuf;
+        unsigned long long best = 0;
+  #pragma unroll
+        for (int i = 0; i < RPT; ++i) {
+          const int row = r0 + tid + i * T;
+          if (row >= k && row < m) best = max(best, pc_word(v[i][0], row, k));
+        }
+        best = warp_max64(best);
+        if (lane == 0 && best != 0) atomicMax(&sh.cmax[par], best);
+        __syncthreads();
+        // every thread has read the previous column's word: clear it for the next
+        if (tid == 0) sh.cmax[par ^ 1] = 0;
+        const unsigned long long cbest = sh.cmax[par];
+        const int wrow = cbest != 0 ? pc_row(cbest) : -1;
+        // owners stage the register part of the CTA's winning row and of row k:
+        // [c] = column kk + 1 + c, [32] = column kk
+  #pragma unroll
+        for (int i = 0; i < RPT; ++i) {
+          const int row = r0 + tid + i * T;
+          if (row == wrow || row == k) {
+            float *dst = row == wrow ? sh.cand : sh.krow;
+  #pragma unroll
+            for (int c = 0; c + 1 < W; ++c) dst[c] = v[i][c + 1];
+  #pragma unroll
+            for (int c = W - 1; c < 32; ++c) dst[c] = 0.f;
+            dst[32] = v[i][0];
+            if (row == wrow && row == k)
+  #pragma unroll
+              for (int c = 0; c < 33; ++c) sh.krow[c] = sh.cand[c];
+          }
+        }
+        __syncthreads();
+        // warp w pushes to CTAs w, w + nwarps, ...: the candidate, its word,
+        // and (CTA 0) row k
+        if (warp < nct) {
+          float lo = 0.f, hi = 0.f;
+          if (wrow >= 0) {
+            lo = sh.cand[lane];
+            hi = lane == 0 ? sh.cand[32] : (lane - 1 < kk ? Lsm[(lane - 1) * LD + (wrow - r0)] : 0.f);
+          }
+          float klo = 0.f, khi = 0.f;
+          if (rank == 0) {  // row k < nb <= R lies in CTA 0
+            klo = sh.krow[lane];
+            khi = lane == 0 ? sh.krow[32] : (lane - 1 < kk ? Lsm[(lane - 1) * LD + k] : 0.f);
+          }
+          for (int d = warp; d < nct; d += nwarps) {
+            const unsigned mb = remote_addr(&sh.mbar[b], d);
+            st_async(remote_addr(&sh.slot[b][rank][lane], d), lo, mb);
+            st_async(remote_addr(&sh.slot[b][rank][32 + lane], d), hi, mb);
+            if (lane == 0) st_async(remote_addr(&sh.skey[b][rank], d), cbest, mb);
+            if (rank == 0) {
+              st_async(remote_addr(&sh.rowk[b][lane], d), klo, mb);
+              st_async(remote_addr(&sh.rowk[b][32 + lane], d), khi, mb);
+            }
+          }
+        }
+        // this column's pushes from every CTA have landed; then the buffer is
+        // armed for column k + kPcBuf
+        tc::mbar_wait(&sh.mbar[b], (k / kPcBuf) & 1, &ctl->status);
+        if (tid == 0) tc::mbar_expect_tx(&sh.mbar[b], xbytes);
+        // the cluster's pivot, identical in every CTA
+        const unsigned long long g = warp_max64(lane < nct ? sh.skey[b][lane] : 0ull);
+        // a row outside [k, m) only after an exchange timed out (stale words):
+        // row k stands in, so that the slot index and the swaps stay in range
+        int p = pc_row(g);
+        if (p < k || p >= m) p = k;
+        const float *prow = sh.slot[b][p / R];
+        const float piv = prow[32];
+        const bool swap = piv != 0.f && p != k;
+        if (tid == 0) {
+          sh.piv[kk] = swap ? p : k;
+          if (rank == 0) {
+            ipiv[k] = p + 1 + ipiv_base;
+            if (piv == 0.f) atomicCAS(&ctl->info, 0, k + 1 + info_base);
+          }
+        }
+        if (swap) {  // the finished part of rows k and p, one warp each
+          if (warp == nwarps - 2 && rank == 0 && lane < kk) Lsm[lane * LD + k] = prow[33 + lane];
+          if (warp == nwarps - 1 && p / R == rank && lane < kk)
+            Lsm[lane * LD + (p - r0)] = sh.rowk[b][33 + lane];
+        }
+        const bool recip = fabsf(piv) >= Real<float>::sfmin();
+        const float rp = 1.f / piv;
+        const int live = ws - 1 - kk;  // columns right of kk still to update
+        const float4 *p4 = reinterpret_cast<const float4 *>(prow);
+  #pragma unroll
+        for (int i = 0; i < RPT; ++i) {
+          const int row = r0 + tid + i * T, lr = tid + i * T;
+          if (swap && (row == k || row == p)) {
+            const float *src = row == k ? prow : sh.rowk[b];
+            v[i][0] = src[32];
+  #pragma unroll
+            for (int c = 1; c < W; ++c) v[i][c] = src[c - 1];
+          }
+          float x = v[i][0];
+          const bool below = row > k && row < m;
+          if (below && piv != 0.f) {
+            if (recip) x *= rp;
+            else x = x / piv;
+          }
+          Lsm[kk * LD + lr] = x;
+          // rotate: column kk + 1 + c moves to register c; only the first
+          // `live` positions carry data, the rest are zero.  Rows not below
+          // the pivot move without arithmetic (an inf in the pivot row must
+          // not reach them through 0 * inf).
+          if (below) {
+            if (live > W / 2) {
+  #pragma unroll
+              for (int j = 0; j < W / 4; ++j) {
+                const float4 q = p4[j];
+                v[i][4 * j + 0] = fmaf(-x, q.x, v[i][4 * j + 1]);
+                v[i][4 * j + 1] = fmaf(-x, q.y, v[i][4 * j + 2]);
+                v[i][4 * j + 2] = fmaf(-x, q.z, v[i][4 * j + 3]);
+                if (4 * j + 4 < W) v[i][4 * j + 3] = fmaf(-x, q.w, v[i][4 * j + 4]);
+              }
+            } else {
+  #pragma unroll
+              for (int j = 0; j < W / 8; ++j) {
+                const float4 q = p4[j];
+                v[i][4 * j + 0] = fmaf(-x, q.x, v[i][4 * j + 1]);
+                v[i][4 * j + 1] = fmaf(-x, q.y, v[i][4 * j + 2]);
+                v[i][4 * j + 2] = fmaf(-x, q.z, v[i][4 * j + 3]);
+                v[i][4 * j + 3] = fmaf(-x, q.w, v[i][4 * j + 4]);
+              }
+            }
+          } else {
+  #pragma unroll
+            for (int c = 0; c + 1 < W; ++c) v[i][c] = v[i][c + 1];
+          }
+          if (live <= W / 2) {
+  #pragma unroll
+            for (int c = W / 2; c + 1 < W; ++c) v[i][c] = 0.f;
+          }
+          v[i][W - 1] = 0.f;
+        }
+      }
+      __syncthreads();
     }
-    __syncthreads();
 
     // C. the factored sub-panel back to the panel; L21 into registers
 #pragma unroll
@@ -482,23 +724,35 @@ __global__ void __launch_bounds__(kPcThreads, 1)
   }
 }
 
+// Occupancy check of a kernel variant on its largest shape, once per device.
 struct PcState {
   bool checked = false, ok = false;
 };
+std::mutex g_pc_mu;
+std::map<std::pair<int, const void *>, PcState> g_pc_state;
 
-template <int RPT, int W>
+template <int RPT, int W, bool TOURN>
 int launch_pc(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base, Control *ctl,
               int info_base, cudaStream_t s, bool *launched, float *XL, int xl, float *XR,
               int xr) {
   // rows spread over up to 16 CTAs; a CTA holds at least nb rows (row k of
-  // every column lies in CTA 0) and at most 512 RPT
+  // every column lies in CTA 0) and at most 512 RPT.  The tournament runs 512
+  // threads, so that its final elimination has a thread for each of the
+  // nct W candidates.
   int T = ceil_div(ceil_div(m, kPcMaxCta * RPT), 32) * 32;
   T = std::max(T, ceil_div(ceil_div(nb, RPT), 32) * 32);
   T = std::max(T, 128);
+  if (TOURN) T = kPcThreads;
   if (T > kPcThreads) return 0;
   const int R = T * RPT, nct = ceil_div(m, R);
   if (nct > kPcMaxCta) return 0;
-  const size_t lsm = sizeof(float) * (R + 1) * W;
+  // Lsm: the finished columns; for the tournament also the candidate exchange
+  auto lsm_floats = [](int rows, int ncta) {
+    const long fin = (long)(rows + 1) * W;
+    const long xch = TOURN ? (long)ncta * W * (W + 1) + (long)W * W : 0;
+    return std::max(fin, xch);
+  };
+  const size_t lsm = sizeof(float) * lsm_floats(R, nct);
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
@@ -511,41 +765,55 @@ int launch_pc(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base, Contr
   cfg.stream = s;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  // one check per variant on its largest shape: 16 CTAs of 512 threads
-  static PcState st;
-  if (!st.checked) {
-    st.checked = true;
-    const size_t lmax = sizeof(float) * (kPcThreads * RPT + 1) * W;
-    ZG_CUDA(cudaFuncSetAttribute(panel_cluster_kernel<RPT, W>,
-                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    ZG_CUDA(cudaFuncSetAttribute(panel_cluster_kernel<RPT, W>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lmax));
-    cudaLaunchConfig_t big = cfg;
-    cudaLaunchAttribute bat[1] = {at[0]};
-    bat[0].val.clusterDim.x = kPcMaxCta;
-    big.gridDim = dim3(kPcMaxCta);
-    big.blockDim = dim3(kPcThreads);
-    big.dynamicSmemBytes = lmax;
-    big.attrs = bat;
-    int nclusters = 0;
-    const cudaError_t e =
-        cudaOccupancyMaxActiveClusters(&nclusters, (void *)panel_cluster_kernel<RPT, W>, &big);
-    if (e != cudaSuccess) (void)cudaGetLastError();
-    st.ok = e == cudaSuccess && nclusters >= 1;
+  // one check per variant and device on its largest shape: 16 CTAs of 512 threads
+  auto *kern = panel_cluster_kernel<RPT, W, TOURN>;
+  int dev = 0;
+  ZG_CUDA(cudaGetDevice(&dev));
+  const size_t lmax = sizeof(float) * lsm_floats(kPcThreads * RPT, kPcMaxCta);
+  {
+    std::lock_guard<std::mutex> lk(g_pc_mu);
+    PcState &st = g_pc_state[{dev, (const void *)kern}];
+    if (!st.checked) {
+      st.checked = true;
+      ZG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+      ZG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lmax));
+      cudaLaunchConfig_t big = cfg;
+      cudaLaunchAttribute bat[1] = {at[0]};
+      bat[0].val.clusterDim.x = kPcMaxCta;
+      big.gridDim = dim3(kPcMaxCta);
+      big.blockDim = dim3(kPcThreads);
+      big.dynamicSmemBytes = lmax;
+      big.attrs = bat;
+      int nclusters = 0;
+      const cudaError_t e = cudaOccupancyMaxActiveClusters(&nclusters, (void *)kern, &big);
+      if (e != cudaSuccess) (void)cudaGetLastError();
+      st.ok = e == cudaSuccess && nclusters >= 1;
+    }
+    if (!st.ok) return 0;
   }
-  if (!st.ok) return 0;
   ZG_LAUNCH(kTagPanel, 1.0 * m * nb * nb, 2.0 * sizeof(float) * m * nb, s,
-            ZG_CUDA(cudaLaunchKernelEx(&cfg, panel_cluster_kernel<RPT, W>, m, nb, A, lda, ipiv,
-                                       ipiv_base, ctl, info_base, XL, xl, XR, xr)));
+            ZG_CUDA(cudaLaunchKernelEx(&cfg, kern, m, nb, A, lda, ipiv, ipiv_base, ctl, info_base,
+                                       XL, xl, XR, xr)));
   *launched = true;
   return 0;
+}
+
+template <int RPT, int W>
+int launch_pc_any(bool tourn, int m, int nb, float *A, long lda, int *ipiv, int ipiv_base,
+                  Control *ctl, int info_base, cudaStream_t s, bool *launched, float *XL, int xl,
+                  float *XR, int xr) {
+  if (tourn)
+    return launch_pc<RPT, W, true>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, launched,
+                                   XL, xl, XR, xr);
+  return launch_pc<RPT, W, false>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, launched, XL,
+                                  xl, XR, xr);
 }
 
 }  // namespace
 
 int panel_lu_cluster(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base, Control *ctl,
                      int info_base, cudaStream_t s, bool *launched, float *XL, int xl, float *XR,
-                     int xr) {
+                     int xr, bool tournament) {
   *launched = false;
   if (m <= 0 || nb <= 0) {
     *launched = true;
@@ -553,14 +821,14 @@ int panel_lu_cluster(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base
   }
   if (nb > kPcMaxNb || m < nb || xl < 0 || xr < 0) return 0;
   if (m <= kPcMaxCta * kPcThreads)
-    return launch_pc<1, 32>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, launched, XL, xl,
-                            XR, xr);
+    return launch_pc_any<1, 32>(tournament, m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s,
+                                launched, XL, xl, XR, xr);
   if (m <= kPcMaxCta * kPcThreads * 2)
-    return launch_pc<2, 32>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, launched, XL, xl,
-                            XR, xr);
+    return launch_pc_any<2, 32>(tournament, m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s,
+                                launched, XL, xl, XR, xr);
   if (m <= kPcMaxCta * kPcThreads * 4)
-    return launch_pc<4, 16>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, launched, XL, xl,
-                            XR, xr);
+    return launch_pc_any<4, 16>(tournament, m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s,
+                                launched, XL, xl, XR, xr);
   return 0;
 }
 
