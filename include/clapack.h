@@ -335,10 +335,11 @@ const char *zml_gpu_last_error(void);
  * of that path; no counterpart in the reference. */
 int zml_gpu_set_spin_limit(long long tries);
 /* Pivoting of the mixed-precision LU's panels (zml_*gesv_mpir, the ladder):
- * 1 tournament pivoting (the default: a communication-avoiding LU whose
- * 32-column sub-panels need one exchange between the panel's thread blocks
- * instead of one per column), 0 partial pivoting.  Returns the previous
- * setting.  No counterpart in the reference (its getrf2 pivots partially). */
+ * 1 tournament pivoting (a communication-avoiding LU whose 32-column
+ * sub-panels need one exchange between the panel's thread blocks instead of
+ * one per column), 0 partial pivoting (the default, faster on GB300).
+ * Returns the previous setting.  No counterpart in the reference (its getrf2
+ * pivots partially). */
 int zml_gpu_mixed_panel(int tournament);
 /* FP32 LU with tournament pivoting on device memory (column-major), the
  * factorization the mixed solver preconditions with: P A = L U as sgetrf's,

@@ -41,7 +41,7 @@ struct MpirResult {
 };
 
 int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cudaStream_t s);
-// Panels of getrf_lowp: tournament pivoting (on != 0, the default) or partial
+// Panels of getrf_lowp: tournament pivoting (on != 0) or partial (the default)
 // pivoting; returns the previous setting.
 int set_mixed_tournament(int on);
 // Solves A X = B (device pointers, column-major) to FP64 accuracy: one

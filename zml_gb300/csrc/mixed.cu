@@ -361,9 +361,11 @@ static int getrf_lowp_blocks(int n, float *A, long lda, int *ipiv, int prec, Con
 
 // Pivoting of the low-precision LU's panels.  The factors only precondition
 // the refinement, so they need not carry partial pivoting's exact pivots:
-// tournament pivoting (one cluster exchange per 32-column sub-panel instead of
-// one per column) is the default, partial pivoting the alternative.
-static std::atomic<int> g_tournament{1};
+// tournament pivoting needs one cluster exchange per 32-column sub-panel
+// instead of one per column, but its two CTA-wide elimination rounds per
+// column measured slower on GB300 (n = 16384: 72.9 against 41.0 ms of panels
+// a solve), so partial pivoting is the default.
+static std::atomic<int> g_tournament{0};
 
 int set_mixed_tournament(int on) { return g_tournament.exchange(on != 0 ? 1 : 0); }
 
