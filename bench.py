@@ -353,6 +353,18 @@ def suite_bench(torch, zg, L, dev, st):
         info = (C.c_int * 1)()
         t, _ = timed(lambda: L.zml_gpu_dgetrf(n, n, F.data_ptr(), n, piv.data_ptr(), info, sh))
         row["getrf_s"], row["getrf_tflops"] = t, (2.0 * n ** 3 / 3) / t / 1e12
+        row["getrf_info"] = info[0]
+        if n == 8192:  # the same LU with every update on the FP64 pipe
+            F2 = S.clone()
+            piv2 = torch.zeros(n, dtype=torch.int32, device=dev)
+            prev = L.zml_gpu_fp64_updates(0)
+            t2, _ = timed(lambda: L.zml_gpu_dgetrf(n, n, F2.data_ptr(), n, piv2.data_ptr(), info,
+                                                   sh))
+            L.zml_gpu_fp64_updates(prev)
+            row["getrf_fp64_pipe_s"] = t2
+            row["getrf_pivots_equal_fp64_pipe"] = bool(torch.equal(piv, piv2))
+            row["getrf_max_rel_diff_fp64_pipe"] = ((F2 - F).abs().max() / F.abs().max()).item()
+            del F2, piv2
         for nrhs in (1, 64):
             Bs = torch.rand(nrhs, n, dtype=torch.float64, device=dev, generator=g) * 2 - 1
             Xs = Bs.clone()
@@ -369,6 +381,15 @@ def suite_bench(torch, zg, L, dev, st):
         F = P.clone()
         t, _ = timed(lambda: L.zml_gpu_dpotrf(b"L", n, F.data_ptr(), n, info, sh))
         row["potrf_s"], row["potrf_tflops"] = t, (n ** 3 / 3.0) / t / 1e12
+        if n == 8192:  # the same Cholesky with every update on the FP64 pipe
+            F2 = P.clone()
+            prev = L.zml_gpu_fp64_updates(0)
+            t2, _ = timed(lambda: L.zml_gpu_dpotrf(b"L", n, F2.data_ptr(), n, info, sh))
+            L.zml_gpu_fp64_updates(prev)
+            row["potrf_fp64_pipe_s"] = t2
+            row["potrf_max_rel_diff_fp64_pipe"] = (
+                (torch.triu(F2) - torch.triu(F)).abs().max() / F.abs().max()).item()  # col-major lower
+            del F2
         row["potrf_info"] = info[0]
         for nrhs in (1, 64):
             Bs = torch.rand(nrhs, n, dtype=torch.float64, device=dev, generator=g) * 2 - 1
@@ -644,18 +665,29 @@ def main():
     # the plain FP64 GPU LU on the same system first: its backward error is the
     # target the mixed solve refines to ("until normwise backward error <= the
     # FP64 LU's"), and its time is the comparator
-    Af = A.clone()
-    bf = b.clone()
     piv = torch.zeros(n, dtype=torch.int32, device=dev)
     info = (C.c_int * 1)()
-    torch.cuda.synchronize()
-    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    f0.record(st)
-    rc1 = L.zml_gpu_dgetrf(n, n, Af.data_ptr(), n, piv.data_ptr(), info, sh)
-    rc2 = L.zml_gpu_dgetrs(b"N", n, 1, Af.data_ptr(), n, piv.data_ptr(), bf.data_ptr(), n, sh)
-    f1.record(st)
-    torch.cuda.synchronize()
-    fp64_s = f0.elapsed_time(f1) / 1e3
+
+    def fp64_lu(mode):
+        # mode 1: trailing updates on the tensor cores by exact slices (the
+        # default); 0: on the FP64 pipe
+        prev = L.zml_gpu_fp64_updates(mode)
+        Af = A.clone()
+        bf = b.clone()
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(st)
+        r1 = L.zml_gpu_dgetrf(n, n, Af.data_ptr(), n, piv.data_ptr(), info, sh)
+        r2 = L.zml_gpu_dgetrs(b"N", n, 1, Af.data_ptr(), n, piv.data_ptr(), bf.data_ptr(), n, sh)
+        f1.record(st)
+        torch.cuda.synchronize()
+        L.zml_gpu_fp64_updates(prev)
+        del Af
+        return f0.elapsed_time(f1) / 1e3, bf, r1, r2
+
+    fp64_lu(1)  # warm: workspaces and modules
+    fp64_s, bf, rc1, rc2 = fp64_lu(1)
+    fp64_pipe_s = fp64_lu(0)[0] if a.suite else None
     r64 = b - Acol @ bf
     berr64 = (r64.abs().max() / (Acol.abs().sum(1).max() * bf.abs().max() + b.abs().max())).item()
     del Af, bf, r64
@@ -782,7 +814,8 @@ def main():
         "berr_history": [last.berr_history[i] for i in range(min(32, last.iters + 1))],
         "ferr": ferr, "outer_iters": last.iters,
         "gmres_iters": last.inner_iters, "factor_ms": last.factor_ms, "converged": bool(last.converged),
-        "fp64_lu": {"time_s": fp64_s, "berr": berr64, "rc": [rc1, rc2, info[0]],
+        "fp64_lu": {"time_s": fp64_s, "updates": "tensor cores, exact 7-bit slices of the FP64 operands",
+                    "time_s_fp64_pipe_updates": fp64_pipe_s, "berr": berr64, "rc": [rc1, rc2, info[0]],
                     "speedup_of_mixed": fp64_s / t_step, "berr_ratio": berr / berr64 if berr64 else None},
         "e2e": {"value": world / t_e2e, "unit": UNIT, "h2d_bytes_per_step": 8 * n * n + 8 * n,
                 "d2h_bytes_per_step": 8 * n, "matches_device_result": e2e_ok},

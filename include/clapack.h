@@ -125,8 +125,11 @@ int zml_gpu_dgetrf(int m, int n, double *dA, int ldda, int *dipiv, int *info, vo
  * hosts whose device memory belongs to another allocator (a caching pool or a
  * fixed arena that a cudaMalloc from the library would fragment or overrun),
  * and loops that must not allocate after start-up.  Same factorization, bit
- * for bit, as zml_gpu_dgetrf.  Its scratch is one static device array of
- * about 273 KB that every GPU loading the library holds until exit; the first
+ * for bit, as zml_gpu_dgetrf with its updates on the FP64 pipe (always below
+ * min(m, n) = 2048, or after zml_gpu_fp64_updates(0)); from 2048 up
+ * zml_gpu_dgetrf's default tensor-core updates agree with it to rounding.  Its
+ * scratch is one static device array of about 273 KB that every GPU loading
+ * the library holds until exit; the first
  * call on a device resolves that array's address (make it before any stream
  * capture).  Every call shares the array: calls that overlap on the GPU race.
  * Limit: m at most what one 64-column panel holds in shared memory (about 446
@@ -341,6 +344,21 @@ int zml_gpu_set_spin_limit(long long tries);
  * Returns the previous setting.  No counterpart in the reference (its getrf2
  * pivots partially). */
 int zml_gpu_mixed_panel(int tournament);
+/* Where the FP64 factorizations (getrf, potrf and what calls them) run their
+ * trailing updates from n = 2048 up: 1 (the default) on the BF16 tensor
+ * cores, each FP64 operand cut into eight exact 7-bit integer slices whose
+ * products are accumulated exactly where it matters (about the accuracy of an
+ * FP64 GEMM); 0 on the FP64 pipe.  Returns the previous mode.  No counterpart
+ * in the reference (an FP64 loop nest). */
+int zml_gpu_fp64_updates(int mode);
+/* The FP64 update those factorizations use, on device memory (column-major):
+ * C (m x n) -= A (m x k) B (k x n) with k <= 256, by exact 7-bit slices of A's
+ * rows and B's columns multiplied on the BF16 tensor cores; lower != 0:
+ * C -= A A^T on C's lower triangle only (m == n, dB unused).  About the
+ * accuracy of an FP64 GEMM (the slices keep 56 bits of each row's / column's
+ * largest entry).  No counterpart in the reference. */
+int zml_gpu_dgemm_slices(int m, int n, int k, const double *dA, int ldda, const double *dB,
+                         int lddb, double *dC, int lddc, int lower, void *stream);
 /* FP32 LU with tournament pivoting on device memory (column-major), the
  * factorization the mixed solver preconditions with: P A = L U as sgetrf's,
  * ipiv in LAPACK's form, but each 32-column sub-panel's pivots are chosen

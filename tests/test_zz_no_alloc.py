@@ -4,8 +4,10 @@ Some hosts own all device memory through their own allocator (a caching pool,
 or an arena reserved at start-up); a cudaMalloc from the library would
 fragment or overrun it.  Some loops must not allocate after initialisation.
 This entry point takes its scratch from a static device array instead.  It
-runs the same panel grid, interchanges, trsm and gemm as zml_gpu_dgetrf, so
-the factors must be identical bit for bit, with identical pivots and info.
+runs the same panel grid, interchanges, trsm and gemm as zml_gpu_dgetrf does
+below min(m, n) = 2048 (where zml_gpu_dgetrf keeps its updates on the FP64
+pipe), so at the sizes here the factors must be identical bit for bit, with
+identical pivots and info.
 That is checked on two calls in a row: the scratch keeps the previous call's
 contents, so the second call shows that everything that must start at zero is
 cleared.  A third check reads the device's free memory around a call: any

@@ -1207,6 +1207,24 @@ int zml_gpu_set_spin_limit(long long tries) { return set_spin_limit(tries); }
 
 int zml_gpu_mixed_panel(int tournament) { return set_mixed_tournament(tournament); }
 
+int zml_gpu_fp64_updates(int mode) { return set_fp64_updates(mode); }
+
+int zml_gpu_dgemm_slices(int m, int n, int k, const double *dA, int ldda, const double *dB,
+                         int lddb, double *dC, int lddc, int lower, void *stream) {
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (k < 0 || k > 256) return -3;
+  if (ldda < std::max(1, m)) return -5;
+  if (!lower && lddb < std::max(1, k)) return -7;
+  if (lddc < std::max(1, m)) return -9;
+  if (lower && m != n) return -10;
+  cudaStream_t s = (cudaStream_t)stream;
+  Control *ctl;
+  ZG_TRY(control(s, &ctl));
+  ZG_TRY(dgemm_oz_sub(m, n, k, dA, ldda, dB, lddb, dC, lddc, lower != 0, &ctl->status, s));
+  return check_status(s, ctl, nullptr);
+}
+
 int zml_gpu_sgetrf_calu(int m, int n, float *dA, int ldda, int *dipiv, int *info, void *stream) {
   if (m < 0) return -1;
   if (n < 0) return -2;

@@ -93,6 +93,12 @@ int potrf_launch(int uplo, int n, T *A, long lda, Control *ctl, int info_base, c
 template <typename T> int potrf_dev(int uplo, int n, T *A, long lda, int *info, cudaStream_t s) {
   *info = 0;
   if (n <= 0) return 0;
+  // from n = 2048 up the FP64 lower Cholesky takes its trailing SYRKs on the
+  // tensor cores (exact slices, ozaki.cu); the upper form and smaller sizes
+  // stay on the FP64 pipe
+  if constexpr (sizeof(T) == sizeof(double))
+    if (uplo == kLower && fp64_updates_on_tensor_cores(n, n))
+      return potrf_oz(n, reinterpret_cast<double *>(A), lda, info, s);
   Control *ctl;
   ZG_TRY(control(s, &ctl));
   ZG_TRY(potrf_launch<T>(uplo, n, A, lda, ctl, 0, s));

@@ -110,7 +110,9 @@ enum Slot : int {
   kSlotZTmp = 23,             // complex herk / syrk: the full product
   kSlotZTr = 24,              // complex trsm: the transposed right-hand side (right side)
   kSlotSytrf = 25,            // Bunch-Kaufman: the step's block size read back by the host
-  kNumSlots = 28
+  kSlotOzA = 26, kSlotOzB = 27,  // FP64-by-slices GEMM: the BF16 slices of A and B, exponents
+  kSlotOzC = 28,              // FP64-by-slices GEMM: the FP32 accumulators
+  kNumSlots = 30
 };
 
 // Returns a device buffer of at least `bytes` bound to `stream` in `slot`.

@@ -96,9 +96,24 @@ int panel_lu_cluster(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base
                      int info_base, cudaStream_t s, bool *launched, float *XL = nullptr,
                      int xl = 0, float *XR = nullptr, int xr = 0, bool tournament = false);
 // tournament: FP32 panels by tournament pivoting (see panel_lu_cluster).
+// FP64 from n = 2048 up: getrf_oz (tensor-core updates), else getrf_simt.
 template <typename T>
 int getrf_dev(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s,
               bool tournament = false);
+// The blocked LU with every update on the FP32 / FP64 pipe (nb 128 / 64).
+template <typename T>
+int getrf_simt(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s,
+               bool tournament = false);
+// ozaki.cu: FP64 C (m x n) -= A (m x k) B (k x n), k <= 256, on the BF16
+// tensor cores through exact integer slices of A and B (syrk: C -= A A^T on
+// C's lower triangle, B unused); getrf with NB 256 and those updates; the
+// switch between FP64-pipe and tensor-core updates.
+int dgemm_oz_sub(int m, int n, int k, const double *A, long lda, const double *B, long ldb,
+                 double *C, long ldc, bool syrk, unsigned *status, cudaStream_t s);
+int getrf_oz(int m, int n, double *A, long lda, int *ipiv, int *info, cudaStream_t s);
+int potrf_oz(int n, double *A, long lda, int *info, cudaStream_t s);  // lower
+int set_fp64_updates(int mode);                    // returns the previous mode
+bool fp64_updates_on_tensor_cores(int m, int n);
 template <typename T>
 int getrs_dev(int trans, int n, int nrhs, const T *A, long lda, const int *ipiv, T *B, long ldb,
               cudaStream_t s);

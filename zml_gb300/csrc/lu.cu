@@ -411,8 +411,8 @@ static int panel_any(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Co
 }
 
 template <typename T>
-int getrf_dev(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s,
-              bool tournament) {
+int getrf_simt(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s,
+               bool tournament) {
   *info = 0;
   if (m <= 0 || n <= 0) return 0;
   Control *ctl;
@@ -434,6 +434,24 @@ int getrf_dev(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s
     }
   }
   return check_status(s, ctl, info);
+}
+
+// FP64 LUs from n = 2048 up take their trailing updates on the tensor cores
+// (getrf_oz, exact slices of the FP64 operands); smaller ones, FP32 and a
+// caller that chose zml_gpu_fp64_updates(0) stay on getrf_simt.
+template <typename T>
+int getrf_dev(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s,
+              bool tournament) {
+  if constexpr (sizeof(T) == sizeof(double)) {
+    if (fp64_updates_on_tensor_cores(m, n)) {
+      if (m <= 0 || n <= 0) {
+        *info = 0;
+        return 0;
+      }
+      return getrf_oz(m, n, reinterpret_cast<double *>(A), lda, ipiv, info, s);
+    }
+  }
+  return getrf_simt<T>(m, n, A, lda, ipiv, info, s, tournament);
 }
 
 // ---------------------------------------------------------------------------
@@ -762,7 +780,8 @@ int getrs_dev(int trans, int n, int nrhs, const T *A, long lda, const int *ipiv,
   template int laswp_panel<T>(int, int, int, T *, long, int, int, const int *, cudaStream_t);    \
   template int panel_lu<T>(int, int, T *, long, int *, int, Control *, int, cudaStream_t);      \
   template int laswp_dev<T>(int, T *, long, int, int, const int *, int, cudaStream_t);          \
-  template int getrf_dev<T>(int, int, T *, long, int *, int *, cudaStream_t, bool);                   \
+  template int getrf_dev<T>(int, int, T *, long, int *, int *, cudaStream_t, bool);          \
+  template int getrf_simt<T>(int, int, T *, long, int *, int *, cudaStream_t, bool);                   \
   template int getrs_dev<T>(int, int, int, const T *, long, const int *, T *, long, cudaStream_t);
 INST(double)
 INST(float)
@@ -876,7 +895,10 @@ int na_laswp(const NaDevice &d, int n, double *A, long lda, int k1, int k2, cons
 using namespace zg;
 
 // FP64 getrf (partial pivoting, 1-based ipiv, LAPACK info) on device memory
-// with no allocation; same factorization, bit for bit, as zml_gpu_dgetrf.
+// with no allocation; same factorization, bit for bit, as zml_gpu_dgetrf with
+// its updates on the FP64 pipe (below min(m, n) = 2048, or after
+// zml_gpu_fp64_updates(0)); above that zml_gpu_dgetrf's default tensor-core
+// updates agree with it to rounding.
 // Returns 0, -(bad argument index), or a library error (ZML_GPU_ERR_INVALID
 // with a message when m exceeds what one panel can hold on this device).
 extern "C" int zml_gpu_dgetrf_noalloc(int m, int n, double *dA, int ldda, int *dipiv, int *info,
