@@ -3,8 +3,10 @@ the FP64 LU built on them.
 
 C -= A B is computed from eight 7-bit integer slices of every row of A and
 column of B, multiplied in BF16 with FP32 accumulation that is exact where it
-matters.  Bar, against numpy's FP64 product: |C - C_ref| <= 16 u (|A| |B| +
-|C|) elementwise (an FP64 GEMM's own error is a few u of |A| |B|); NaN in a row
+matters.  Bar, against numpy's FP64 product: |C - C_ref| <= 32 u (|A| |B| +
+|C|) elementwise -- the slices' own error (about 6 u on N(0,1) data) plus
+numpy's rounding (a few u), at the worst of up to 17 million entries; an FP64
+GEMM's error bound is k u |A| |B| = 256 u.  NaN in a row
 of A reaches that row of C; rows and columns of very different scales keep
 their relative accuracy; the lower form touches only C's lower triangle.
 The LU with these updates (LAPACKE_dgetrf from n = 2048 up) is compared with
@@ -48,7 +50,7 @@ def test_slices_match_fp64(m, n, k):
     a, b, c = rng.standard_normal((m, k)), rng.standard_normal((k, n)), rng.standard_normal((m, n))
     out = slices_sub(a, b, c)
     ref = c - a @ b
-    bound = 16 * U * (np.abs(a) @ np.abs(b) + np.abs(c))
+    bound = 32 * U * (np.abs(a) @ np.abs(b) + np.abs(c))
     assert np.all(np.abs(out - ref) <= bound), np.max(np.abs(out - ref) / bound)
 
 
@@ -62,7 +64,7 @@ def test_slices_scaled_rows_and_columns():
     c = np.zeros((m, n))
     out = slices_sub(a, b, c)
     ref = -(a @ b)
-    bound = 16 * U * (np.abs(a) @ np.abs(b))
+    bound = 32 * U * (np.abs(a) @ np.abs(b))
     assert np.all(np.abs(out - ref) <= bound)
 
 
@@ -86,7 +88,7 @@ def test_slices_lower_form():
     out = slices_sub(a, None, c, lower=True)
     ref = c - a @ a.T
     low = np.tril(np.ones((n, n), bool))
-    bound = 16 * U * (np.abs(a) @ np.abs(a).T + np.abs(c))
+    bound = 32 * U * (np.abs(a) @ np.abs(a).T + np.abs(c))
     assert np.all(np.abs(out - ref)[low] <= bound[low])
     np.testing.assert_array_equal(out[~low], c[~low])
 
