@@ -690,7 +690,7 @@ def main():
     fp64_pipe_s = fp64_lu(0)[0] if a.suite else None
     r64 = b - Acol @ bf
     berr64 = (r64.abs().max() / (Acol.abs().sum(1).max() * bf.abs().max() + b.abs().max())).item()
-    del Af, bf, r64
+    del bf, r64
     tol = berr64 if a.tol == "fp64" else float(a.tol)
 
     def solve():
