@@ -1093,6 +1093,8 @@ static int berr_of(int n, const double *A, long lda, const double *b, const doub
 
 // GMRES on (LU)^-1 A d = (LU)^-1 r with restart m; returns after `inner`
 // iterations or when the preconditioned residual fell by `rtol`.
+constexpr int kGmresStallSteps = 16;
+
 static int gmres_correction(int n, const double *A, long lda, const LowLU &f, IRWork &w, int m,
                             double rtol, int *iters, Control *ctl, cudaStream_t s) {
   const int b1 = ceil_div(n, 256);
@@ -1146,6 +1148,14 @@ static int gmres_correction(int n, const double *A, long lda, const LowLU &f, IR
     for (int i = 0; i <= k; ++i) H[i + k * (m + 1)] = hcol[i];
     ++*iters;
     if (std::fabs(g[k + 1]) <= rtol * beta || !(hk1 > 0)) {
+      ++k;
+      break;
+    }
+    // a cycle that has not halved the preconditioned residual in 16 steps is
+    // stuck on a spread of small eigenvalues (factors too far from A for its
+    // conditioning) that would take O(n) more: stop it, so that refinement
+    // decides early -- a different arithmetic, or the FP64 factorization
+    if (k + 1 >= kGmresStallSteps && std::fabs(g[k + 1]) > 0.5 * beta) {
       ++k;
       break;
     }
