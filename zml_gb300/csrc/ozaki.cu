@@ -50,14 +50,34 @@ __device__ __forceinline__ int oz_exponent(double mx) {
   return e;
 }
 
-// The slices of one value scaled to |v| < 2^7: q_i = rint(v), v = (v - q_i) 2^7.
-__device__ __forceinline__ void oz_slices(double v, float (&q)[kOzS]) {
+// 2^p as a double for the normal range, else 0 (the caller uses ldexp then).
+__device__ __forceinline__ double oz_pow2(int p) {
+  return (p >= -1022 && p <= 1023) ? __longlong_as_double((long long)(p + 1023) << 52) : 0.0;
+}
+
+// The S slices of x, a value of a row (column) whose entries lie below 2^e in
+// magnitude: N = x 2^(56 - e) rounded to an integer (|N| < 2^56; exact unless
+// x lies more than 2^3 below 2^(e - 53)), then N's balanced base-2^7 digits
+// from the top, q_i = round(r / 2^(49 - 7 i)), r -= q_i 2^(49 - 7 i): |q_0| <= 128,
+// |q_i| <= 64, and N = sum q_i 2^(49 - 7 i) exactly.  Integer shifts only, so
+// the FP64 pipe sees one multiply and one conversion per value.  A non-finite
+// row (nan set) gives NaN slices.
+__device__ __forceinline__ void oz_slices(double x, int e, bool nan, float (&q)[kOzS]) {
+  if (nan || !isfinite(x)) {
 #pragma unroll
-  for (int i = 0; i < kOzS; ++i) {
-    const double t = rint(v);
-    q[i] = (float)t;
-    v = (v - t) * 128.0;
+    for (int i = 0; i < kOzS; ++i) q[i] = __int_as_float(0x7fc00000);
+    return;
   }
+  const double p = oz_pow2(56 - e);
+  long long r = __double2ll_rn(p != 0.0 ? x * p : ldexp(x, 56 - e));
+#pragma unroll
+  for (int i = 0; i < kOzS - 1; ++i) {
+    const int sh = 49 - 7 * i;
+    const long long t = (r + (1ll << (sh - 1))) >> sh;
+    r -= t << sh;
+    q[i] = (float)(int)t;
+  }
+  q[kOzS - 1] = (float)(int)r;
 }
 
 // Rows of A (m x k, column-major, k <= 256): per row its exponent and the S
@@ -70,6 +90,7 @@ __global__ void __launch_bounds__(256) oz_split_rows_kernel(int m, int k, const 
                                                             __nv_bfloat16 *rev, int *ex) {
   extern __shared__ double ozt[];  // ozt[r * (kOzMaxK + 1) + c]
   __shared__ int er[kOzRows];
+  __shared__ bool bad[kOzRows];
   constexpr int LD = kOzMaxK + 1;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int r0 = blockIdx.x * kOzRows;
@@ -80,16 +101,19 @@ __global__ void __launch_bounds__(256) oz_split_rows_kernel(int m, int k, const 
   __syncthreads();
   for (int r = warp; r < kOzRows; r += blockDim.x >> 5) {
     double mx = 0;
-    for (int c = lane; c < k; c += 32) mx = fmax(mx, fabs(ozt[r * LD + c]));
-    // a NaN anywhere makes the row's maximum NaN
-    for (int c = lane; c < k; c += 32)
-      if (ozt[r * LD + c] != ozt[r * LD + c]) mx = ozt[r * LD + c];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const double y = __shfl_xor_sync(~0u, mx, o);
-      mx = (y != y || mx != mx) ? (y != y ? y : mx) : fmax(mx, y);
+    bool nonfinite = false;
+    for (int c = lane; c < k; c += 32) {
+      const double v = ozt[r * LD + c];
+      mx = fmax(mx, fabs(v));
+      nonfinite |= !isfinite(v);
     }
-    if (lane == 0) er[r] = oz_exponent(mx);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(~0u, mx, o));
+    nonfinite = __any_sync(~0u, nonfinite);
+    if (lane == 0) {
+      er[r] = oz_exponent(mx);
+      bad[r] = nonfinite;
+    }
   }
   __syncthreads();
   const long ldo = (long)kOzS * kp;
@@ -97,11 +121,10 @@ __global__ void __launch_bounds__(256) oz_split_rows_kernel(int m, int k, const 
   for (int e = tid; e < kOzRows * half; e += blockDim.x) {
     const int r = e / half, c = 2 * (e - r * half);
     if (r0 + r >= m) continue;
-    const int sh = 7 - er[r];
     const double x0 = c < k ? ozt[r * LD + c] : 0.0, x1 = c + 1 < k ? ozt[r * LD + c + 1] : 0.0;
     float q0[kOzS], q1[kOzS];
-    oz_slices(ldexp(x0, sh), q0);
-    oz_slices(ldexp(x1, sh), q1);
+    oz_slices(x0, er[r], bad[r], q0);
+    oz_slices(x1, er[r], bad[r], q1);
     __nv_bfloat16 *fr = fwd ? fwd + (long)(r0 + r) * ldo + c : nullptr;
     __nv_bfloat16 *rr = rev ? rev + (long)(r0 + r) * ldo + c : nullptr;
 #pragma unroll
@@ -125,18 +148,18 @@ __global__ void __launch_bounds__(256) oz_split_cols_kernel(int k, int n, const 
   constexpr int kPer = kOzMaxK / 32;
   double x[kPer];
   double mx = 0;
-  bool nan = false;
+  bool nonfinite = false;
 #pragma unroll
   for (int t = 0; t < kPer; ++t) {
     const int c = lane + 32 * t;
     x[t] = c < k ? B[c + (long)col * ldb] : 0.0;
     mx = fmax(mx, fabs(x[t]));
-    nan |= x[t] != x[t];
+    nonfinite |= !isfinite(x[t]);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(~0u, mx, o));
-  nan = __any_sync(~0u, nan);
-  const int e = oz_exponent(nan ? NAN : mx);
+  nonfinite = __any_sync(~0u, nonfinite);
+  const int e = oz_exponent(mx);
   const long ldo = (long)kOzS * kp;
   __nv_bfloat16 *out = rev + (long)col * ldo;
 #pragma unroll
@@ -144,7 +167,7 @@ __global__ void __launch_bounds__(256) oz_split_cols_kernel(int k, int n, const 
     const int c = lane + 32 * t;
     if (c >= kp) continue;
     float q[kOzS];
-    oz_slices(ldexp(nan && x[t] == x[t] ? NAN : x[t], 7 - e), q);
+    oz_slices(x[t], e, nonfinite, q);
 #pragma unroll
     for (int i = 0; i < kOzS; ++i) out[(long)(kOzS - 1 - i) * kp + c] = __float2bfloat16_rn(q[i]);
   }
@@ -152,31 +175,36 @@ __global__ void __launch_bounds__(256) oz_split_cols_kernel(int k, int n, const 
 }
 
 // C (m x n) -= 2^(er + ec - 14) (C_0 + 2^-7 C_1 + 2^-14 C_2 + 2^-21 C_3 + 2^-28 C_4)
-// with the accumulators W (m x n each, ld ldw, one after the other); lower:
-// only r >= c.
-__global__ void oz_combine_kernel(int m, int n, double *__restrict__ C, long ldc,
-                                  const float *__restrict__ W, long ldw, long wstride,
-                                  const int *__restrict__ er, const int *__restrict__ ec,
-                                  bool lower) {
-  const long total = (long)m * n;
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total;
-       e += (long)gridDim.x * blockDim.x) {
-    const int r = (int)(e % m), c = (int)(e / m);
+// with the accumulators W (m x n each, ld ldw, wstride apart); lower: only
+// r >= c.  C_0 .. C_3 are integers below 2^24 in magnitude, so they fold into
+// one 64-bit integer exactly, I = 2^21 C_0 + 2^14 C_1 + 2^7 C_2 + C_3; the
+// FP64 pipe then sees one conversion, one FMA for C_4 and one FMA into C.
+// Rows run along x, columns along y (no index division).
+__global__ void __launch_bounds__(256) oz_combine_kernel(int m, int n, double *__restrict__ C,
+                                                         long ldc, const float *__restrict__ W,
+                                                         long ldw, long wstride,
+                                                         const int *__restrict__ er,
+                                                         const int *__restrict__ ec, bool lower) {
+  const int c = blockIdx.y;
+  const int ecc = ec[c] - 35;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
     if (lower && r < c) continue;
-    const long w = r + (long)c * ldw;
-    double acc = (double)W[w + 4 * wstride];
-    acc = acc * 0.0078125 + (double)W[w + 3 * wstride];
-    acc = acc * 0.0078125 + (double)W[w + 2 * wstride];
-    acc = acc * 0.0078125 + (double)W[w + wstride];
-    acc = acc * 0.0078125 + (double)W[w];
+    const float *w = W + r + (long)c * ldw;
+    const float w0 = __ldcs(w), w1 = __ldcs(w + wstride), w2 = __ldcs(w + 2 * wstride);
+    const float w3 = __ldcs(w + 3 * wstride), w4 = __ldcs(w + 4 * wstride);
+    double x;
+    if (isfinite(w0) && isfinite(w1) && isfinite(w2) && isfinite(w3)) {
+      const long long I = ((long long)__float2int_rn(w0) << 21) + ((long long)__float2int_rn(w1) << 14) +
+                          ((long long)__float2int_rn(w2) << 7) + (long long)__float2int_rn(w3);
+      x = fma((double)w4, 0.0078125, (double)I);
+    } else {  // a NaN / inf operand reaches C as NaN
+      x = (double)(w0 + w1 + w2 + w3 + w4);
+    }
+    const int p = er[r] + ecc;
+    const double sc = oz_pow2(p);
     double *cp = C + r + (long)c * ldc;
-    *cp -= ldexp(acc, er[r] + ec[c] - 14);
+    *cp = sc != 0.0 ? fma(-x, sc, *cp) : *cp - ldexp(x, p);
   }
-}
-
-__global__ void ipiv_add_kernel(int n, int *ipiv, int add) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) ipiv[i] += add;
 }
 
 std::atomic<int> g_oz_mode{1};  // 1: tensor-core updates above the threshold
@@ -236,8 +264,8 @@ int dgemm_oz_sub(int m, int n, int k, const double *A, long lda, const double *B
                      Br + (long)(kOzS - 1 - d) * kp + (long)c0 * ldo, ldo, beta,
                      W + (size_t)slot * ldw * nc, ldw, 1, status, s, syrk ? 1 : 0));
     }
-    const long total = (long)rows * w;
-    const int grid = (int)std::min<long>((total + 255) / 256, 152L * 8);
+    const double total = (double)rows * w;
+    const dim3 grid(std::min(ceil_div(rows, 256), 64), w);
     ZG_LAUNCH(kTagConvert, 0, (8.0 * 2 + 4.0 * kOzAcc) * total, s,
               oz_combine_kernel<<<grid, 256, 0, s>>>(rows, w, C + r0 + (long)c0 * ldc, ldc, W, ldw,
                                                      (long)ldw * nc, ea + r0, ecol + c0, syrk));
@@ -246,39 +274,58 @@ int dgemm_oz_sub(int m, int n, int k, const double *A, long lda, const double *B
   return 0;
 }
 
-// FP64 LU with partial pivoting, blocked with NB = 256: each 256-column panel
-// is factored by the FP64-pipe getrf (64-column cooperative panels, its own
-// small updates), the interchanges reach the other columns, U12 = L11^-1 A12
-// is a triangular solve, and the trailing update A22 -= L21 U12 -- nearly all
-// of the flops -- runs on the tensor cores through dgemm_oz_sub.  The loop is
-// getrf.zig:52-136's with a wider block.
+// FP64 LU with partial pivoting, blocked with NB = 256 -- the loop of
+// getrf.zig:52-136 with a wider block.  Each 256-column block is factored as
+// two 128-column halves by the cooperative FP64 panel (the pivot search of
+// getrf2.zig:45-89 over the whole column), with the right half's update from
+// the left one between them; the interchanges then reach the other columns,
+// U12 = L11^-1 A12 is a triangular solve, and the trailing update
+// A22 -= L21 U12 -- nearly all of the flops -- runs on the tensor cores
+// through dgemm_oz_sub, as does the half-panel update (k = 128).  Every wait
+// reports into one status word, read once at the end.
 int getrf_oz(int m, int n, double *A, long lda, int *ipiv, int *info, cudaStream_t s) {
   constexpr int NB = 256;
   *info = 0;
   const int mn = std::min(m, n);
+  // half-panel width: 128 columns while one per-SM slab of the tallest panel
+  // fits in shared memory, else 64 (about twice the rows)
+  DeviceInfo di;
+  ZG_TRY(device_info(&di));
+  const long slab = (long)ceil_div(m, di.num_sms) * sizeof(double);
+  const int NBP = slab * 128 <= (long)di.smem_optin - 4096 ? 128 : 64;
   Control *ctl;
   ZG_TRY(control(s, &ctl));
   for (int j = 0; j < mn; j += NB) {
     const int jb = std::min(NB, mn - j);
-    double *Ajj = A + j + (long)j * lda;
-    int iinfo = 0;
-    ZG_TRY(getrf_simt<double>(m - j, jb, Ajj, lda, ipiv + j, &iinfo, s));
-    if (*info == 0 && iinfo > 0) *info = iinfo + j;
-    ZG_LAUNCH(kTagVector, 0, 0, s, ipiv_add_kernel<<<ceil_div(jb, 256), 256, 0, s>>>(jb, ipiv + j, j));
+    double *Ab = A + (long)j * lda;  // the block's columns
+    for (int p = 0; p < jb; p += NBP) {
+      const int r = j + p, pb = std::min(NBP, jb - p), right = jb - p - pb;
+      double *Arr = A + r + (long)r * lda;
+      ZG_TRY(panel_lu<double>(m - r, pb, Arr, lda, ipiv + r, r, ctl, r, s));
+      // the half-panel's interchanges in the block's other columns
+      ZG_TRY(laswp_panel<double>(p, p + pb, jb, Ab, lda, r + 1, r + pb, ipiv, s));
+      if (right > 0) {
+        double *Ar = Arr + (long)pb * lda;  // rows r.., the block's columns right of the half
+        ZG_TRY(trsm_dev<double>(kLeft, kLower, kNoTrans, kUnit, pb, right, 1.0, Arr, lda, Ar, lda,
+                                s));
+        if (r + pb < m)
+          ZG_TRY(dgemm_oz_sub(m - r - pb, right, pb, Arr + pb, lda, Ar, lda, Ar + pb, lda, false,
+                              &ctl->status, s));
+      }
+    }
+    // the block's interchanges in every column outside it
     ZG_TRY(laswp_panel<double>(j, std::min(n, j + jb), n, A, lda, j + 1, j + jb, ipiv, s));
     if (j + jb < n) {
+      double *Ajj = A + j + (long)j * lda;
       double *A12 = A + j + (long)(j + jb) * lda;
       ZG_TRY(trsm_dev<double>(kLeft, kLower, kNoTrans, kUnit, jb, n - j - jb, 1.0, Ajj, lda, A12,
                               lda, s));
-      if (j + jb < m) {
+      if (j + jb < m)
         ZG_TRY(dgemm_oz_sub(m - j - jb, n - j - jb, jb, Ajj + jb, lda, A12, lda, A12 + jb, lda,
                             false, &ctl->status, s));
-        // the next panel's getrf re-arms the stream's status word: read it now
-        ZG_TRY(check_status(s, ctl, nullptr));
-      }
     }
   }
-  return check_status(s, ctl, nullptr);
+  return check_status(s, ctl, info);
 }
 
 // FP64 Cholesky A = L L^T (lower), right-looking with NB = 256: the diagonal
