@@ -227,17 +227,40 @@ def batched_workload(torch, dev, count=20000, nrhs=4, seed=7, rank=0, world=1):
                 A[offs[m]:offs[m + 1]] = flat[j]
     B = torch.rand(int((n.astype(np.int64) * nrhs).sum()), dtype=torch.float64, device=dev,
                    generator=g) * 2 - 1
-    flops = float(sum((k ** 3 / 3.0 if s else 2.0 * k ** 3 / 3) + 2.0 * k * k * nrhs
-                      for k, s in zip(n.astype(np.float64), spd)))
-    nbytes = float(sum(8.0 * (k * (k + 1) if s else 2 * k * k) + 16.0 * k * nrhs + (0 if s else 4 * k)
-                       for k, s in zip(n.astype(np.float64), spd)))
+    flops, nbytes = batched_costs(n, spd, nrhs)
     return n, spd, A, B, flops, nbytes
+
+
+def batched_costs(n, spd, nrhs):
+    """Algorithmic flops and bytes of a batch (SURVEY-style minimum): Cholesky
+    n^3/3, LU 2n^3/3, plus 2n^2 per right-hand side for the two solves; bytes:
+    the stored triangle (Cholesky) or the matrix (LU) read and its factor
+    written, B read and X written, LU's pivots."""
+    nn = n.astype("float64")
+    flops = float(sum((k ** 3 / 3.0 if s else 2.0 * k ** 3 / 3) + 2.0 * k * k * nrhs
+                      for k, s in zip(nn, spd)))
+    nbytes = float(sum(8.0 * (k * (k + 1) if s else 2 * k * k) + 16.0 * k * nrhs + (0 if s else 4 * k)
+                       for k, s in zip(nn, spd)))
+    return flops, nbytes
+
+
+def batched_subset(torch, n, spd, A0, B, nrhs, sel):
+    """The systems `sel` (indices) of a batch as a batch of their own."""
+    import numpy as np
+    offs = np.concatenate([[0], np.cumsum(n.astype(np.int64) ** 2)])
+    boffs = np.concatenate([[0], np.cumsum(n.astype(np.int64) * nrhs)])
+    A = torch.cat([A0[int(offs[i]):int(offs[i + 1])] for i in sel])
+    Bs = torch.cat([B[int(boffs[i]):int(boffs[i + 1])] for i in sel])
+    return n[sel].copy(), spd[sel].copy(), A, Bs
 
 
 def batched_bench(torch, zg, L, dev, st, steps, warmup, hbm, rank=0, world=1, dist=None,
                   total_count=20000, autotune=True):
     """The batched workload, sharded over ranks by n^3-balanced index ranges
-    (strong scaling: the 20000 systems are split); time = max over ranks."""
+    (strong scaling: the 20000 systems are split); time = max over ranks.
+    Beside the whole mixed batch, its Cholesky half and its LU half are timed
+    on their own, each precision against its binding roof."""
+    import numpy as np
     n, spd, A0, B, flops, nbytes = batched_workload(torch, dev, total_count, rank=rank,
                                                     world=world)
     nrhs, count = 4, len(n)
@@ -249,45 +272,56 @@ def batched_bench(torch, zg, L, dev, st, steps, warmup, hbm, rank=0, world=1, di
                        "(getrf+getrs), %d RHS" % (total_count, nrhs), "count": total_count,
            "ranks": world, "scaling": "strong" if world > 1 else None,
            "algorithmic_flops": flops, "algorithmic_bytes": nbytes}
-    # FP64 is the binding roof (about 8 flop per algorithmic byte): its peak
-    # is measured here as cuBLAS DGEMM 8192^3 through torch, best of 3
-    a64 = torch.randn(8192, 8192, dtype=torch.float64, device=dev)
-    torch.matmul(a64, a64)
-    best = 1e30
-    for _ in range(3):
-        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        g0.record(st)
-        torch.matmul(a64, a64)
-        g1.record(st)
-        torch.cuda.synchronize()
-        best = min(best, g0.elapsed_time(g1) / 1e3)
-    del a64
-    fp64_peak = 2.0 * 8192 ** 3 / best / 1e12
+    # compute roofs, measured here: cuBLAS DGEMM and SGEMM (TF32 off) 8192^3
+    # through torch, best of 3 each
+    def gemm_peak(dtype):
+        a = torch.randn(8192, 8192, dtype=dtype, device=dev)
+        torch.matmul(a, a)
+        best = 1e30
+        for _ in range(3):
+            g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            g0.record(st)
+            torch.matmul(a, a)
+            g1.record(st)
+            torch.cuda.synchronize()
+            best = min(best, g0.elapsed_time(g1) / 1e3)
+        return 2.0 * 8192 ** 3 / best / 1e12
+    tf32 = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    fp64_peak, fp32_peak = gemm_peak(torch.float64), gemm_peak(torch.float32)
+    torch.backends.cuda.matmul.allow_tf32 = tf32
     out["fp64_peak_tflops"] = fp64_peak
-    out["fp64_peak_source"] = "measured: cuBLAS DGEMM 8192^3 (torch.matmul), best of 3"
-    for prec, name in ((0, "fp64"), (1, "fp32_factor_fp64_ir")):
+    out["fp32_peak_tflops"] = fp32_peak
+    out["peak_source"] = "measured: cuBLAS DGEMM / SGEMM (TF32 off) 8192^3 (torch.matmul), best of 3"
+
+    chosen_for = {}
+    for prec in (0, 1):
         ncls = L.zml_gpu_batched_schedule(prec, None, None, 0, 0)
         chosen = (C.c_int * ncls)()
         if autotune:
             L.zml_gpu_batched_autotune(prec, nrhs, chosen, None, st.cuda_stream)
         else:
             L.zml_gpu_batched_schedule(prec, chosen, None, ncls, 0)
+        chosen_for[prec] = chosen
+
+    def run(nb, sb, Ab, Bb, prec, total):
+        cnt = len(nb)
         plan = C.c_void_p()
-        rc = L.zml_gpu_batched_plan_create(C.byref(plan), count, n.ctypes.data_as(C.c_void_p),
-                                           spd.ctypes.data_as(C.c_void_p), nrhs, prec, 10)
+        rc = L.zml_gpu_batched_plan_create(C.byref(plan), cnt, nb.ctypes.data_as(C.c_void_p),
+                                           sb.ctypes.data_as(C.c_void_p), nrhs, prec, 10)
         if rc != 0:
             raise RuntimeError("batched plan: %s" % zg.last_error())
-        A = A0.clone()
-        X = torch.zeros_like(B)
-        P = torch.zeros(int(n.sum()), dtype=torch.int32, device=dev)
-        info = torch.zeros(count, dtype=torch.int32, device=dev)
-        iters = torch.zeros(count, dtype=torch.int32, device=dev)
-        args = (plan, A.data_ptr(), B.data_ptr(), X.data_ptr(), P.data_ptr(), info.data_ptr(),
+        A = Ab.clone()
+        X = torch.zeros_like(Bb)
+        P = torch.zeros(int(nb.sum()), dtype=torch.int32, device=dev)
+        info = torch.zeros(cnt, dtype=torch.int32, device=dev)
+        iters = torch.zeros(cnt, dtype=torch.int32, device=dev)
+        args = (plan, A.data_ptr(), Bb.data_ptr(), X.data_ptr(), P.data_ptr(), info.data_ptr(),
                 iters.data_ptr(), st.cuda_stream)
-        total = 0.0
+        tsum = 0.0
         for it in range(max(3, warmup) + steps):
             if prec == 0:
-                A.copy_(A0)  # the FP64 path factors A in place
+                A.copy_(Ab)  # the FP64 path factors A in place
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(st)
             if L.zml_gpu_batched_run_graph(*args) != 0:
@@ -295,10 +329,11 @@ def batched_bench(torch, zg, L, dev, st, steps, warmup, hbm, rank=0, world=1, di
             e1.record(st)
             torch.cuda.synchronize()
             if it >= max(3, warmup):
-                total += e0.elapsed_time(e1) / 1e3
-        t = total / steps
+                tsum += e0.elapsed_time(e1) / 1e3
+        t = tsum / steps
         L.zml_gpu_batched_plan_destroy(plan)
         ok = int((info == 0).sum().item())
+        it_host = iters.cpu().numpy() if prec else np.zeros(cnt, dtype=np.int32)
         if dist:
             tt = torch.tensor([t], dtype=torch.float64, device=dev)
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -306,14 +341,51 @@ def batched_bench(torch, zg, L, dev, st, steps, warmup, hbm, rank=0, world=1, di
             okt = torch.tensor([ok], dtype=torch.int64, device=dev)
             dist.all_reduce(okt)
             ok = int(okt.item())
-        out[name] = {"solves_per_s": total_count / t, "ms_per_batch": 1e3 * t,
-                     "roofline": {"kernel": "batched_kernel", "bound": "fp64",
-                                  "achieved": flops / t / 1e12, "peak": fp64_peak,
-                                  "unit": "TFLOP/s", "frac": flops / t / 1e12 / fp64_peak},
-                     "tflops": flops / t / 1e12, "hbm_gbs": nbytes / t / 1e9,
-                     "hbm_frac": nbytes / t / 1e9 / hbm, "info_ok": ok,
-                     "schedule_warps_per_class": list(chosen),
-                     "max_refinement_steps": int(iters.max().item()) if prec else 0}
+        fl, by = batched_costs(nb, sb, nrhs)
+        if dist:
+            tot = torch.tensor([fl, by], dtype=torch.float64, device=dev)
+            dist.all_reduce(tot)
+            fl, by = tot.tolist()
+        # the binding roof: bytes at HBM speed against the arithmetic at its
+        # pipe's speed; FP32 factors + FP64 refinement: factorization and the
+        # correction solves in FP32, each step's residual (2 n^2 per RHS) in FP64
+        if prec == 0:
+            t_cmp = fl / (fp64_peak * 1e12)
+            arith = "FP64: %.3g flop at %.3g TF/s" % (fl, fp64_peak)
+        else:
+            fact = fl - float(sum(2.0 * k * k * nrhs for k in nb.astype("float64")))
+            steps_ir = it_host.astype("float64")
+            ir64 = float(sum(2.0 * k * k * nrhs * s for k, s in zip(nb.astype("float64"), steps_ir)))
+            ir32 = float(sum(2.0 * k * k * nrhs * (s + 1) for k, s in zip(nb.astype("float64"), steps_ir)))
+            t_cmp = (fact + ir32) / (fp32_peak * 1e12) + ir64 / (fp64_peak * 1e12)
+            arith = ("FP32: %.3g flop at %.3g TF/s, FP64 residuals: %.3g flop at %.3g TF/s"
+                     % (fact + ir32, fp32_peak, ir64, fp64_peak))
+        t_mem = by / (hbm * 1e9)
+        bound = "hbm" if t_mem >= t_cmp else ("fp64" if prec == 0 else "fp32+fp64")
+        roof_t = max(t_mem, t_cmp)
+        return {"solves_per_s": total / t, "ms_per_batch": 1e3 * t, "algorithmic_flops": fl,
+                "algorithmic_bytes": by, "tflops": fl / t / 1e12, "hbm_gbs": by / t / 1e9,
+                "hbm_frac": by / t / 1e9 / hbm, "info_ok": ok,
+                "roofline": {"bound": bound, "roof_ms": 1e3 * roof_t, "frac": roof_t / t,
+                             "hbm_ms": 1e3 * t_mem, "compute_ms": 1e3 * t_cmp,
+                             "arithmetic": arith},
+                "max_refinement_steps": int(it_host.max()) if prec else 0,
+                "mean_refinement_steps": float(it_host.mean()) if prec else 0.0}
+
+    names = {0: "fp64", 1: "fp32_factor_fp64_ir"}
+    for prec in (0, 1):
+        r = run(n, spd, A0, B, prec, total_count)
+        r["roofline"]["kernel"] = "batched_kernel"
+        r["schedule_warps_per_class"] = list(chosen_for[prec])
+        out[names[prec]] = r
+    half = total_count // 2
+    for kind, label in ((1, "cholesky_only"), (0, "lu_only")):
+        sel = np.nonzero(spd == kind)[0]
+        nb, sb, Ab, Bb = batched_subset(torch, n, spd, A0, B, nrhs, sel)
+        out[label] = {"count": half}
+        for prec in (0, 1):
+            out[label][names[prec]] = run(nb, sb, Ab, Bb, prec, half)
+        del Ab, Bb
     return out
 
 
