@@ -96,6 +96,12 @@ int LAPACKE_zposv(int matrix_layout, char uplo, int n, int nrhs, void *a, int ld
                   int ldb);
 int LAPACKE_cposv(int matrix_layout, char uplo, int n, int nrhs, void *a, int lda, void *b,
                   int ldb);
+/* complex QR (lapack.zig:5138 LAPACKE_cgeqrf, :5152 LAPACKE_zgeqrf; kernel
+ * lapack/geqrf.zig:18 over cfloat): R on and above the diagonal, the
+ * Householder vectors below it, tau[min(m,n)] complex; H(i) = I - tau_i v v^H
+ * and A = H(0) ... H(k-1) R. */
+int LAPACKE_zgeqrf(int matrix_layout, int m, int n, void *a, int lda, void *tau);
+int LAPACKE_cgeqrf(int matrix_layout, int m, int n, void *a, int lda, void *tau);
 
 /* replaces zml.linalg.lapack.geqrf (lapack.zig:5060; kernel lapack/geqrf.zig:18):
  * R in the upper triangle, the Householder vectors below it, tau[min(m,n)] */
@@ -118,6 +124,8 @@ int LAPACKE_slaswp(int matrix_layout, int n, float *a, int lda, int k1, int k2, 
 /* ---- GPU extensions: device pointers, column-major, stream ordered ------
  * `stream` is a cudaStream_t (NULL = legacy default stream).  The call
  * returns after the stream has drained (info is a host value). */
+/* device-pointer form of LAPACKE_zgeqrf (interleaved complex, column-major) */
+int zml_gpu_zgeqrf(int m, int n, void *dA, int ldda, void *dtau, void *stream);
 /* device-pointer form of getrf (lapack/getrf.zig:14) */
 int zml_gpu_dgetrf(int m, int n, double *dA, int ldda, int *dipiv, int *info, void *stream);
 /* FP64 getrf on device memory that allocates nothing; no counterpart in the

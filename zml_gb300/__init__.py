@@ -59,6 +59,7 @@ _SIGS.update({
     "zml_gpu_dgetrf_noalloc": (i32, [i32, i32, vp, i32, vp, vp, vp]),
     "zml_gpu_dorgqr": (i32, [i32, i32, i32, vp, i32, vp, vp]),
     "zml_gpu_dgeqrf": (i32, [i32, i32, vp, i32, vp, vp]),
+    "zml_gpu_zgeqrf": (i32, [i32, i32, vp, i32, vp, vp]),
     "zml_gpu_dpotrf": (i32, [ch, i32, vp, i32, vp, vp]),
     "zml_gpu_dpotrs": (i32, [ch, i32, i32, vp, i32, vp, i32, vp]),
     "zml_gpu_dgemm": (i32, [i32, i32, i32, i32, i32, f64, vp, i32, vp, i32, f64, vp, i32, vp]),

@@ -508,6 +508,24 @@ template <typename R> int zgetrf_any(int layout, int m, int n, R *a, int lda, in
 
 int ztrans_code(char t) { return t == 'N' ? kNoTrans : t == 'T' ? kTrans : kConjTrans; }
 
+template <typename R> int zgeqrf_any(int layout, int m, int n, R *a, int lda, R *tau) {
+  using C2 = typename Cx<R>::T;
+  if (!lay_ok(layout)) return -1;
+  if (m < 0) return -2;
+  if (n < 0) return -3;
+  if (lda < std::max(1, layout == kColMajor ? m : n)) return -5;
+  if (m == 0 || n == 0) return 0;
+  cudaStream_t s = lib_stream();
+  ColMajor<C2> A;
+  Buf<C2> Tau;
+  ZG_TRY(A.in(layout, (const C2 *)a, lda, m, n, kSlotA, kSlotAT, true, s));
+  ZG_TRY(Tau.in((C2 *)tau, std::min(m, n), kSlotPiv, false, s));
+  ZG_TRY(zgeqrf_dev<R>(m, n, (R *)A.d, A.ld, (R *)Tau.d, s));
+  ZG_TRY(A.out(s));
+  ZG_TRY(Tau.out(s));
+  return sync(s);
+}
+
 template <typename R>
 int zgetrs_any(int layout, char trans, int n, int nrhs, const R *a, int lda, const int *ipiv,
                R *b, int ldb) {
@@ -842,6 +860,9 @@ CBLAS_ZGEMM(c, float)
   int LAPACKE_##P##posv(int layout, char uplo, int n, int nrhs, void *a, int lda, void *b,       \
                         int ldb) {                                                               \
     return zposv_any<R>(layout, uplo, n, nrhs, (R *)a, lda, (R *)b, ldb);                        \
+  }                                                                                              \
+  int LAPACKE_##P##geqrf(int layout, int m, int n, void *a, int lda, void *tau) {                \
+    return zgeqrf_any<R>(layout, m, n, (R *)a, lda, (R *)tau);                                   \
   }
 int LAPACKE_dsytrf(int layout, char uplo, int n, double *a, int lda, int *ipiv) {
   return sytrf_any<double>(layout, uplo, n, a, lda, ipiv);
@@ -883,6 +904,12 @@ int LAPACKE_dgeqrf(int layout, int m, int n, double *a, int lda, double *tau) {
 }
 int LAPACKE_sgeqrf(int layout, int m, int n, float *a, int lda, float *tau) {
   return geqrf_any<float>(layout, m, n, a, lda, tau);
+}
+int zml_gpu_zgeqrf(int m, int n, void *dA, int ldda, void *dtau, void *stream) {
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (ldda < std::max(1, m)) return -4;
+  return zgeqrf_dev<double>(m, n, (double *)dA, ldda, (double *)dtau, (cudaStream_t)stream);
 }
 int zml_gpu_dgeqrf(int m, int n, double *dA, int ldda, double *dtau, void *stream) {
   if (m < 0) return -1;

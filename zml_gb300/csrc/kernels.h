@@ -49,6 +49,9 @@ template <typename R>
 int zgetrs_dev(int trans, int n, int nrhs, const R *A, long lda, const int *ipiv, R *B, long ldb,
                cudaStream_t s);
 template <typename R> int zpotrf_dev(int uplo, int n, R *A, long lda, int *info, cudaStream_t s);
+// zqr.cu: complex Householder QR (interleaved (re, im) pairs, lda in complex
+// elements), tau[min(m, n)] complex.
+template <typename R> int zgeqrf_dev(int m, int n, R *A, long lda, R *tau, cudaStream_t s);
 template <typename R>
 int zpotrs_dev(int uplo, int n, int nrhs, const R *A, long lda, R *B, long ldb, cudaStream_t s);
 

@@ -1151,11 +1151,15 @@ static int gmres_correction(int n, const double *A, long lda, const LowLU &f, IR
       ++k;
       break;
     }
-    // a cycle that has not halved the preconditioned residual in 16 steps is
-    // stuck on a spread of small eigenvalues (factors too far from A for its
-    // conditioning) that would take O(n) more: stop it, so that refinement
-    // decides early -- a different arithmetic, or the FP64 factorization
-    if (k + 1 >= kGmresStallSteps && std::fabs(g[k + 1]) > 0.5 * beta) {
+    // a cycle whose first 16 steps fell short of the geometric rate that
+    // reaches rtol within the restart (|g| / beta <= rtol^(16 / m)) is stuck
+    // on a spread of small eigenvalues (factors too far from A for its
+    // conditioning) that would take O(n) more steps: it ends here, its partial
+    // correction is applied, and refinement decides early -- another cycle if
+    // the backward error halved, else a different arithmetic or the FP64
+    // factorization
+    if (k + 1 == kGmresStallSteps && m > kGmresStallSteps &&
+        std::fabs(g[k + 1]) > std::pow(rtol, (double)kGmresStallSteps / m) * beta) {
       ++k;
       break;
     }
