@@ -658,6 +658,21 @@ def next_rows_bench(torch, L, dev, g, n=4096):
         t, info = wall(factor)
         return {"s": t, "real_tflops": 4.0 * n ** 3 / 3 / t / 1e12, "info": info}
 
+    def zgeqrf():
+        G = torch.randn(n, n, dtype=torch.complex128, device=dev, generator=g)
+        F = G.clone()
+        tau = torch.zeros(n, dtype=torch.complex128, device=dev)
+
+        def factor():
+            F.copy_(G)
+            return L.LAPACKE_zgeqrf(102, n, n, F.data_ptr(), n, tau.data_ptr())
+        t, rc = wall(factor)
+        # ||A(:, j)|| = ||R(0:j, j)|| (storage is A^T: rows of F are columns)
+        Rn = torch.linalg.norm(torch.triu(F.t()), dim=0)
+        An = torch.linalg.norm(G.t(), dim=0)
+        return {"s": t, "real_tflops": 4.0 * (4.0 * n ** 3 / 3) / t / 1e12, "rc": rc,
+                "max_rel_colnorm_dev": ((Rn - An).abs() / An).max().item()}
+
     def dsytrf():
         G = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
         Sy = (G + G.t()) / 2
@@ -674,6 +689,7 @@ def next_rows_bench(torch, L, dev, g, n=4096):
     guarded("zgemm_n%d" % n, zgemm)
     guarded("zgetrf_n%d" % n, zgetrf)
     guarded("zpotrf_n%d" % n, zpotrf)
+    guarded("zgeqrf_n%d" % n, zgeqrf)
     guarded("dsytrf_n%d" % n, dsytrf)
     torch.cuda.empty_cache()
     return out
