@@ -2,13 +2,16 @@
 // A = U D U^T or L D L^T with 1x1 and 2x2 pivot blocks (LAPACK's dsytf2
 // pivoting, as zml restates it in lapack/sytf2.zig:17-522).
 //
-// One step per pivot block, driven by the host: a single-CTA kernel finds
-// the pivot (|a_kk|, the column maximum, and when needed the maximum of row
-// imax, with zml's iamax semantics: the first maximum wins, a NaN never
-// displaces it, a NaN at the first position blocks the search), decides the
-// 1x1 / 2x2 block, performs the symmetric interchange and writes ipiv / info;
-// the host reads the block size back (one 8-byte copy) and launches the
-// update of the remaining triangle.  Every product and sum of the update is
+// One step per pivot block, driven from device memory: a single-CTA kernel
+// takes the step's column from the previous step (a four-word state: column,
+// block size, skip, done), finds the pivot (|a_kk|, the column maximum, and
+// when needed the maximum of row imax, with zml's iamax semantics: the first
+// maximum wins, a NaN never displaces it, a NaN at the first position blocks
+// the search), decides the 1x1 / 2x2 block, performs the symmetric
+// interchange and writes ipiv / info and the state; the update of the
+// remaining triangle and the block's columns read the state too.  The host
+// only enqueues n steps -- those past the last column find `done` set and
+// return -- so no step waits for a round trip to the host.  Every product and sum of the update is
 // rounded on its own (__dmul_rn / __dadd_rn; the compiler may not contract
 // them into an FMA), in the association sytf2.zig writes, so the result is
 // the restated unblocked algorithm's, bit for bit.  zml's sytrf factors
@@ -85,16 +88,28 @@ __device__ int cta_iamax(int len, F v, T *sv, int *si) {
 // factorization runs from the last column down), as sytf2.zig:67-68 sets it.
 __device__ __forceinline__ void record_first(int *info, int v) { atomicCAS(info, 0, v); }
 
-// Step k (sytf2.zig:30-296 upper, 297-515 lower): pivot choice, interchange,
-// ipiv, info.  out[0] = kstep, out[1] = 1 when the column is zero (or its
-// diagonal NaN) and the step makes no update.
+// The state of the factorization in device memory: st[0] = the current
+// step's column k, st[1] = its block size, st[2] = 1 when the column is zero
+// (or its diagonal NaN) and the step makes no update, st[3] = 1 once every
+// column is done.
+enum : int { kStK = 0, kStStep = 1, kStSkip = 2, kStDone = 3 };
+
+// Step k (sytf2.zig:30-296 upper, 297-515 lower): the column after the
+// previous step's block, pivot choice, interchange, ipiv, info.
 template <typename T>
 __global__ void __launch_bounds__(1024) sytf2_pivot_kernel(int n, T *A, long lda, bool upper,
-                                                           int k, T alpha, int *ipiv, int *out,
+                                                           T alpha, int *ipiv, int *st,
                                                            int *info) {
   __shared__ T sv[32];
   __shared__ int si[32];
   auto a = [&](int i, int j) -> T & { return A[i + (long)j * lda]; };
+  if (st[kStDone]) return;
+  const int k = upper ? st[kStK] - st[kStStep] : st[kStK] + st[kStStep];
+  if (upper ? k < 0 : k >= n) {
+    __syncthreads();  // every thread has read the state
+    if (threadIdx.x == 0) st[kStDone] = 1;
+    return;
+  }
   const T absakk = fabs(a(k, k));
   int imax = 0;
   T colmax = T(0);
@@ -185,8 +200,9 @@ __global__ void __launch_bounds__(1024) sytf2_pivot_kernel(int n, T *A, long lda
       ipiv[k] = -(kp + 1);
       ipiv[upper ? k - 1 : k + 1] = -(kp + 1);
     }
-    out[0] = kstep;
-    out[1] = skip;
+    st[kStK] = k;
+    st[kStStep] = kstep;
+    st[kStSkip] = skip;
   }
 }
 
@@ -198,8 +214,10 @@ __global__ void __launch_bounds__(1024) sytf2_pivot_kernel(int n, T *A, long lda
 // of the block are rewritten afterwards by sytf2_store_kernel.
 template <typename T>
 __global__ void __launch_bounds__(256) sytf2_update_kernel(int n, T *A, long lda, bool upper,
-                                                           int k, int kstep) {
+                                                           const int *st) {
   auto a = [&](int i, int j) -> T & { return A[i + (long)j * lda]; };
+  if (st[kStDone] || st[kStSkip]) return;
+  const int k = st[kStK], kstep = st[kStStep];
   // the triangle to update: upper rows/cols [0, m), lower [k + kstep, n)
   const int m = upper ? k - kstep + 1 : n - k - kstep;
   const int o = upper ? 0 : k + kstep;
@@ -242,9 +260,11 @@ __global__ void __launch_bounds__(256) sytf2_update_kernel(int n, T *A, long lda
 
 // The block's columns after the update: x / d (1x1) or the multipliers (2x2).
 template <typename T>
-__global__ void __launch_bounds__(256) sytf2_store_kernel(int n, T *A, long lda, bool upper, int k,
-                                                          int kstep) {
+__global__ void __launch_bounds__(256) sytf2_store_kernel(int n, T *A, long lda, bool upper,
+                                                          const int *st) {
   auto a = [&](int i, int j) -> T & { return A[i + (long)j * lda]; };
+  if (st[kStDone] || st[kStSkip]) return;
+  const int k = st[kStK], kstep = st[kStStep];
   const int m = upper ? k - kstep + 1 : n - k - kstep;
   const int o = upper ? 0 : k + kstep;
   const int j0 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -280,31 +300,26 @@ int sytrf_dev(int uplo, int n, T *A, long lda, int *ipiv, int *info, cudaStream_
   Control *ctl;
   ZG_TRY(control(s, &ctl));
   void *w;
-  ZG_TRY(workspace(s, kSlotSytrf, sizeof(int) * 2, &w));
-  int *out = (int *)w;
+  ZG_TRY(workspace(s, kSlotSytrf, sizeof(int) * 4, &w));
+  int *st = (int *)w;
   DeviceInfo di;
   ZG_TRY(device_info(&di));
   const bool upper = uplo == kUpper;
   const T alpha = (T(1) + std::sqrt(T(17))) / T(8);
-  int k = upper ? n - 1 : 0;
-  int hout[2];
-  while (upper ? k >= 0 : k < n) {
+  // the first step's column is n - 1 (upper) or 0 (lower)
+  const int st0[4] = {upper ? n : -1, 1, 0, 0};
+  ZG_CUDA(cudaMemcpyAsync(st, st0, sizeof st0, cudaMemcpyHostToDevice, s));
+  const long tot = (long)n * n;
+  const int grid = (int)std::max(1L, std::min((tot + 255) / 256, (long)di.num_sms * 8));
+  // at most n steps (one per column when every block is 1x1)
+  for (int it = 0; it < n; ++it) {
     ZG_LAUNCH(kTagPanel, 0, 0, s,
-              (sytf2_pivot_kernel<T><<<1, 1024, 0, s>>>(n, A, lda, upper, k, alpha, ipiv, out,
+              (sytf2_pivot_kernel<T><<<1, 1024, 0, s>>>(n, A, lda, upper, alpha, ipiv, st,
                                                         &ctl->info)));
-    ZG_CUDA(cudaMemcpyAsync(hout, out, sizeof(hout), cudaMemcpyDeviceToHost, s));
-    ZG_CUDA(cudaStreamSynchronize(s));
-    const int kstep = hout[0];
-    const int m = upper ? k - kstep + 1 : n - k - kstep;
-    if (!hout[1] && m > 0) {
-      const long tot = (long)m * m;
-      const int grid = (int)std::max(1L, std::min((tot + 255) / 256, (long)di.num_sms * 8));
-      ZG_LAUNCH(kTagPotf2, 1.0 * tot, 24.0 * tot / 2, s,
-                (sytf2_update_kernel<T><<<grid, 256, 0, s>>>(n, A, lda, upper, k, kstep)));
-      ZG_LAUNCH(kTagPotf2, 0, 0, s,
-                (sytf2_store_kernel<T><<<ceil_div(m, 256), 256, 0, s>>>(n, A, lda, upper, k, kstep)));
-    }
-    k = upper ? k - kstep : k + kstep;
+    ZG_LAUNCH(kTagPotf2, 0, 0, s,
+              (sytf2_update_kernel<T><<<grid, 256, 0, s>>>(n, A, lda, upper, st)));
+    ZG_LAUNCH(kTagPotf2, 0, 0, s,
+              (sytf2_store_kernel<T><<<ceil_div(n, 256), 256, 0, s>>>(n, A, lda, upper, st)));
   }
   return check_status(s, ctl, info);
 }
