@@ -611,6 +611,7 @@ def next_rows_bench(torch, L, dev, g, n=4096):
     def guarded(name, fn):
         try:
             out[name] = fn()
+            torch.cuda.synchronize()
         except Exception as e:  # noqa: BLE001 - reported in the line
             out[name] = {"error": str(e)[:200]}
 
@@ -691,7 +692,7 @@ def next_rows_bench(torch, L, dev, g, n=4096):
     guarded("zpotrf_n%d" % n, zpotrf)
     guarded("zgeqrf_n%d" % n, zgeqrf)
     guarded("dsytrf_n%d" % n, dsytrf)
-    torch.cuda.empty_cache()
+    guarded("release", lambda: torch.cuda.empty_cache())
     return out
 
 
@@ -855,7 +856,12 @@ def main():
     e2e_ok = bool(torch.allclose(xh.to(dev), X, rtol=0, atol=1e-9))
 
     hbm, bf16, src = peaks()
-    suite = suite_bench(torch, zg, L, dev, st) if (a.suite and rank == 0) else None
+    suite = None
+    if a.suite and rank == 0:
+        try:  # the headline line is printed even if a suite row fails
+            suite = suite_bench(torch, zg, L, dev, st)
+        except Exception as e:  # noqa: BLE001 - reported in the line
+            suite = {"error": str(e)[:300]}
     batched = (batched_bench(torch, zg, L, dev, st, a.steps, a.warmup, hbm, rank, world, dist,
                              a.batched_count, bool(a.batched_autotune)) if a.batched else None)
 

@@ -8,8 +8,10 @@
  * provided.
  *
  * Pointers may be host memory (staged to the GPU and back) or device /
- * managed memory (used in place).  Calls are synchronous.  Invalid arguments
- * return silently, as zml's src/cblas.zig does.
+ * managed memory (used in place).  Calls are synchronous.  Device operands
+ * are read after all work queued earlier on the legacy default stream; a
+ * caller that fills them on another stream synchronizes that stream first.
+ * Invalid arguments return silently, as zml's src/cblas.zig does.
  */
 #ifndef ZML_GB300_CBLAS_H
 #define ZML_GB300_CBLAS_H

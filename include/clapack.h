@@ -15,7 +15,9 @@
  * return codes <= -1000; zml_gpu_last_error() describes them.
  *
  * Pointers may be host memory (staged to the GPU and back) or device /
- * managed memory (used in place).  Calls are synchronous.
+ * managed memory (used in place).  Calls are synchronous.  Device operands
+ * are read after all work queued earlier on the legacy default stream; a
+ * caller that fills them on another stream synchronizes that stream first.
  */
 #ifndef ZML_GB300_CLAPACK_H
 #define ZML_GB300_CLAPACK_H

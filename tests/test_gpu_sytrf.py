@@ -114,3 +114,22 @@ def test_bunchkaufman_facade_reconstructs(uplo, layout):
     perm, t, D = _bk_unpack(L, h, upper, n)
     (L.zml_udut_deinit if upper else L.zml_ldlt_deinit)(h)
     assert np.abs(a[np.ix_(perm, perm)] - t @ D @ t.T).max() <= 1e-10 * np.abs(a).max()
+
+
+@pytest.mark.parametrize("uplo", [b"U", b"L"])
+def test_dsytrf_device_pointers_n1536_bitwise(uplo):
+    """Device operands at n = 1536 (every step enqueued from device state):
+    still the oracle's sytf2 bit for bit."""
+    import torch
+    n = 1536
+    a = sym(n, seed=31 + uplo[0])
+    F = torch.from_numpy(np.ascontiguousarray(a.T)).cuda()  # row-major storage of a^T = a
+    piv = torch.zeros(n, dtype=torch.int32, device="cuda")
+    info = zg.lib().LAPACKE_dsytrf(102, uplo, n, F.data_ptr(), n, piv.data_ptr())
+    ul = 121 if uplo == b"U" else 122
+    fr, ipr, infr = oracle_sytf2(a, ul)
+    assert info == infr == 0
+    np.testing.assert_array_equal(piv.cpu().numpy(), ipr)
+    f = F.cpu().numpy().T  # column-major view
+    tri = np.triu if uplo == b"U" else np.tril
+    np.testing.assert_array_equal(tri(f), tri(fr))

@@ -29,13 +29,18 @@ using namespace zg;
 
 namespace {
 
+// The stream of the synchronous entries.  A blocking stream: its work starts
+// after everything already queued on the legacy default stream (where
+// PyTorch and most CUDA callers fill device buffers), so an operand passed
+// as a device pointer is never read while the caller's copy into it is still
+// running.
 cudaStream_t lib_stream() {
   static thread_local cudaStream_t s = nullptr;
   static thread_local int dev = -1;
   int d = 0;
   cudaGetDevice(&d);
   if (!s || d != dev) {
-    cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    cudaStreamCreateWithFlags(&s, cudaStreamDefault);
     dev = d;
   }
   return s;

@@ -94,6 +94,16 @@ __device__ __forceinline__ void record_first(int *info, int v) { atomicCAS(info,
 // column is done.
 enum : int { kStK = 0, kStStep = 1, kStSkip = 2, kStDone = 3 };
 
+// Thread 0's value of v for the whole CTA.  Every value a branch depends on
+// goes through here, so the control flow around the CTA's barriers is the
+// same in every thread even when the matrix changes under the kernel.
+template <typename T> __device__ __forceinline__ T cta_bcast(T v, T *slot) {
+  __syncthreads();
+  if (threadIdx.x == 0) *slot = v;
+  __syncthreads();
+  return *slot;
+}
+
 // Step k (sytf2.zig:30-296 upper, 297-515 lower): the column after the
 // previous step's block, pivot choice, interchange, ipiv, info.
 template <typename T>
@@ -102,6 +112,7 @@ __global__ void __launch_bounds__(1024) sytf2_pivot_kernel(int n, T *A, long lda
                                                            int *info) {
   __shared__ T sv[32];
   __shared__ int si[32];
+  __shared__ T sb;
   auto a = [&](int i, int j) -> T & { return A[i + (long)j * lda]; };
   if (st[kStDone]) return;
   const int k = upper ? st[kStK] - st[kStStep] : st[kStK] + st[kStStep];
@@ -110,17 +121,17 @@ __global__ void __launch_bounds__(1024) sytf2_pivot_kernel(int n, T *A, long lda
     if (threadIdx.x == 0) st[kStDone] = 1;
     return;
   }
-  const T absakk = fabs(a(k, k));
+  const T absakk = cta_bcast(fabs(a(k, k)), &sb);
   int imax = 0;
   T colmax = T(0);
   if (upper) {
     if (k > 0) {
       imax = cta_iamax<T>(k, [&](int q) { return a(q, k); }, sv, si);
-      colmax = fabs(a(imax, k));
+      colmax = cta_bcast(fabs(a(imax, k)), &sb);
     }
   } else if (k < n - 1) {
     imax = k + 1 + cta_iamax<T>(n - k - 1, [&](int q) { return a(k + 1 + q, k); }, sv, si);
-    colmax = fabs(a(imax, k));
+    colmax = cta_bcast(fabs(a(imax, k)), &sb);
   }
   int kp = k, kstep = 1, skip = 0;
   if (cmax(absakk, colmax) == T(0) || absakk != absakk) {
@@ -129,22 +140,23 @@ __global__ void __launch_bounds__(1024) sytf2_pivot_kernel(int n, T *A, long lda
     T rowmax;
     if (upper) {
       int jmax = imax + 1 + cta_iamax<T>(k - imax, [&](int q) { return a(imax, imax + 1 + q); }, sv, si);
-      rowmax = fabs(a(imax, jmax));
+      rowmax = cta_bcast(fabs(a(imax, jmax)), &sb);
       if (imax > 0) {
         jmax = cta_iamax<T>(imax, [&](int q) { return a(q, imax); }, sv, si);
-        rowmax = cmax(rowmax, fabs(a(jmax, imax)));
+        rowmax = cmax(rowmax, cta_bcast(fabs(a(jmax, imax)), &sb));
       }
     } else {
       int jmax = k + cta_iamax<T>(imax - k, [&](int q) { return a(imax, k + q); }, sv, si);
-      rowmax = fabs(a(imax, jmax));
+      rowmax = cta_bcast(fabs(a(imax, jmax)), &sb);
       if (imax < n - 1) {
         jmax = imax + 1 + cta_iamax<T>(n - imax - 1, [&](int q) { return a(imax + 1 + q, imax); }, sv, si);
-        rowmax = cmax(rowmax, fabs(a(jmax, imax)));
+        rowmax = cmax(rowmax, cta_bcast(fabs(a(jmax, imax)), &sb));
       }
     }
+    const T absimax = cta_bcast(fabs(a(imax, imax)), &sb);
     if (absakk >= Rn<T>::mul(alpha, Rn<T>::mul(colmax, Rn<T>::div(colmax, rowmax)))) {
       kp = k;
-    } else if (fabs(a(imax, imax)) >= Rn<T>::mul(alpha, rowmax)) {
+    } else if (absimax >= Rn<T>::mul(alpha, rowmax)) {
       kp = imax;
     } else {
       kp = imax;
