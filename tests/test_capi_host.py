@@ -20,6 +20,17 @@ def test_library_exports_every_declared_symbol():
     assert L.zml_gpu_version() >= 1
 
 
+def test_every_declared_function_has_a_ctypes_signature():
+    """Without argtypes ctypes passes a Python int as a 32-bit C int, so a
+    device pointer given as tensor.data_ptr() would reach the library cut to
+    its low 32 bits."""
+    missing = [n for n in zg.declared_symbols() if n not in zg._SIGS]
+    assert not missing, missing
+    L = zg.lib()
+    for n in zg.declared_symbols():
+        assert getattr(L, n).argtypes is not None, n
+
+
 @pytest.mark.parametrize("call,expect", [
     (lambda L, a, p: L.LAPACKE_dgetrf(103, 4, 4, a, 4, p), -1),
     (lambda L, a, p: L.LAPACKE_dgetrf(102, -1, 4, a, 4, p), -2),
