@@ -300,9 +300,12 @@ typedef struct zml_auto_result {
   double ms;         /* wall time of the call */
   float features[16]; /* the selector's input features: [0]-[11] as
                          zml_gpu_selector_features; [12] log10 of the first
-                         BF16 backward error, [13]-[14] log10 of the next two
-                         step ratios, [15] 1 if the BF16 LU failed (0.5 if the
-                         solves moved to FP64 arithmetic) */
+                         BF16 backward error, [13] log10 of the first step's
+                         ratio, [14] log10 of a condition estimate,
+                         ||A||inf times ||z||inf after 3 steps of inverse
+                         iteration with the BF16 factors (0 if they failed),
+                         [15] 1 if the BF16 LU failed (0.5 if the solves moved
+                         to FP64 arithmetic) */
   float proba[5];    /* predicted class probabilities */
   int reserved;
 } zml_auto_result;

@@ -193,11 +193,40 @@ def test_selector_gains_over_ladder(torch, sel):
     time than the plain one."""
     dev = torch.device("cuda", 0)
     sel.warm_up(torch, dev, 384)
-    X, y, _ = sel.build_dataset(torch, sel.sample_specs(800, seed=1, nmax=384), dev)
+    X, y, _ = sel.build_dataset(torch, sel.sample_specs(800, seed=1, nmax=384), dev, workers=4)
     assert len(set(y.tolist())) >= 3
     state = sel.train(torch, X, y, dev, epochs=200)
-    rec, s = sel.evaluate(torch, sel.sample_specs(200, seed=2, nmax=384), state, dev)
+    rec, s = sel.evaluate(torch, sel.sample_specs(200, seed=2, nmax=384), state, dev, workers=4,
+                          time_sample=200)
     print(s)
     assert s["converged_guided"] == 1.0 and s["converged_ladder"] == 1.0
     assert s["choice_at_or_above_label"] >= 0.85
     assert s["speedup_vs_ladder"] > 1.0
+
+
+def test_concurrent_labelling_equals_sequential(torch, sel):
+    """Labels and features from several streams in flight are those of one
+    stream: the library's state is per stream and its kernels deterministic."""
+    dev = torch.device("cuda", 0)
+    specs = sel.sample_specs(48, seed=5, nmax=512)
+    X1, y1, _ = sel.build_dataset(torch, specs, dev, workers=1)
+    X4, y4, _ = sel.build_dataset(torch, specs, dev, workers=6)
+    np.testing.assert_array_equal(y1, y4)
+    np.testing.assert_array_equal(X1, X4)
+
+
+def test_condition_estimate_feature_tracks_kappa(torch, sel):
+    """Feature 14, log10 of ||A||inf times ||z||inf after three steps of
+    inverse iteration with the BF16 probe's factors, grows with the
+    matrix's condition number and is close to it when the factors are
+    accurate (kappa_2 = 10: kappa_inf lies within a factor n of it)."""
+    dev = torch.device("cuda", 0)
+    n = 256
+    est = []
+    for kappa in (1e1, 1e4, 1e8):
+        t, m = sel.generate(torch, 0, n, kappa, 77, dev)
+        b = sel.rhs(torch, m, 77)
+        r = sel.solve_auto(torch, t, b, torch.zeros_like(b), n)
+        est.append(float(np.frombuffer(r.features, dtype=np.float32)[14]))
+    assert est[0] < est[1] < est[2], est
+    assert 0.5 <= est[0] <= 1.0 + np.log10(n), est

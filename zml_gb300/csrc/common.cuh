@@ -15,6 +15,7 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <cstdio>
 #include <mutex>
 #include <string>
@@ -202,7 +203,7 @@ enum ProfTag : int {
   kTagGemmTC = 0, kTagGemmSimt, kTagPanel, kTagTrsmDiag, kTagLaswp, kTagTrsv, kTagGemv,
   kTagConvert, kTagPotf2, kTagVector, kTagBatched, kTagQR, kTagMLP, kTagOther, kNumTags
 };
-extern unsigned long long g_launches;
+extern std::atomic<unsigned long long> g_launches;  // calls from several threads / streams
 extern bool g_profiling;
 void prof_record(cudaStream_t s, int tag, double flops, double bytes, cudaEvent_t *begin);
 void prof_end(cudaStream_t s, cudaEvent_t begin, int tag, double flops, double bytes);

@@ -88,7 +88,10 @@ struct AutoResult {
 int gesv_auto_dev(int n, int nrhs, const double *A, long lda, const double *B, long ldb, double *X,
                   long ldx, const float *model, float confidence, int max_iter, AutoResult *r,
                   cudaStream_t s);
-// Features 12..15 from the probe's refinement record.
-void probe_features(const MpirResult &pr, float *f);
+// Features 12..15 from the probe's refinement record and the condition
+// estimate of its factors (0 when they failed).
+void probe_features(const MpirResult &pr, double kappa, float *f);
+// Steps of inverse iteration behind the probe's condition estimate.
+constexpr int kCondSteps = 3;
 
 }  // namespace zg

@@ -1495,7 +1495,43 @@ int posv_mpir_dev(bool lower, int n, int nrhs, const double *A, long lda, const 
 // ---------------------------------------------------------------------------
 // Precision selection.
 
-void probe_features(const MpirResult &pr, float *f) {
+// u_i = (-1)^i (1 + i / n): the start of the inverse iteration, with no
+// structure a test matrix family shares
+__global__ void cond_start_kernel(int n, double *u) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) u[i] = (i & 1 ? -1.0 : 1.0) * (1.0 + (double)i / n);
+}
+// y = x / *den when *den is positive and finite, else y = x
+__global__ void scale_inv_kernel(int n, const double *den, const double *x, double *y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const double d = *den;
+  if (i < n) y[i] = (d > 0 && d <= 1.79e308) ? x[i] / d : x[i];
+}
+
+// A few-step condition estimate from the low-precision factors of c:
+// `steps` steps of inverse iteration z = (LU)^-1 P u, u = z / ||z||_inf,
+// whose last ||z||_inf (with ||u||_inf = 1) is a lower estimate of
+// ||A^-1||_inf; kappa = ||A||_inf times it.  Scratch: the first two Krylov
+// columns of c's work, which no refinement call keeps between calls.
+static int cond_estimate(MpirCtx &c, int steps, double *kappa, cudaStream_t s) {
+  const int n = c.n, b1 = ceil_div(n, 256);
+  double *u = c.w.V, *z = c.w.V + n;
+  ZG_LAUNCH(kTagVector, 0, 0, s, cond_start_kernel<<<b1, 256, 0, s>>>(n, u));
+  ZG_LAUNCH(kTagVector, 0, 0, s, absmax_kernel<<<1, 256, 0, s>>>(n, u, c.w.scal + 2));
+  ZG_LAUNCH(kTagVector, 0, 0, s, scale_inv_kernel<<<b1, 256, 0, s>>>(n, c.w.scal + 2, u, u));
+  for (int it = 0; it < steps; ++it) {
+    ZG_TRY(lu_apply(n, c.f, u, z, c.w.tw, &c.ctl->status, s));
+    ZG_LAUNCH(kTagVector, 0, 0, s, absmax_kernel<<<1, 256, 0, s>>>(n, z, c.w.scal + 2));
+    ZG_LAUNCH(kTagVector, 0, 0, s, scale_inv_kernel<<<b1, 256, 0, s>>>(n, c.w.scal + 2, z, u));
+  }
+  ZG_CUDA(cudaGetLastError());
+  double zn;
+  ZG_TRY(host_scalar(c.w.scal + 2, &zn, s));
+  *kappa = c.anrm * zn;
+  return 0;
+}
+
+void probe_features(const MpirResult &pr, double kappa, float *f) {
   // log10 of a backward error, clamped to [1e-18, 1e2] (non-finite: 1e2)
   auto lg = [](double v) {
     if (!std::isfinite(v)) v = 1e2;
@@ -1508,10 +1544,11 @@ void probe_features(const MpirResult &pr, float *f) {
   }
   const double h0 = pr.berr_history[0];
   const double h1 = pr.iters >= 1 ? pr.berr_history[1] : h0;
-  const double h2 = pr.iters >= 2 ? pr.berr_history[2] : h1;
   f[12] = lg(h0);
   f[13] = lg(h1) - lg(h0);
-  f[14] = lg(h2) - lg(h1);
+  // log10 of the condition estimate, in [0, 20] (non-finite: 20)
+  const double k = std::isfinite(kappa) ? std::min(std::max(kappa, 1.0), 1e20) : 1e20;
+  f[14] = (float)std::log10(k);
   f[15] = pr.switched_f64 ? 0.5f : 0.f;
 }
 
@@ -1552,9 +1589,13 @@ int gesv_auto_dev(int n, int nrhs, const double *A, long lda, const double *B, l
   MpirResult pr;
   ZG_TRY(mpir_factor(false, false, n, A, lda, o, &c, &pr, s));
   r->attempts = 1;
-  if (pr.info == 0) ZG_TRY(mpir_refine(c, o, nrhs, B, ldb, X, ldx, false, &pr, s));
+  double kappa = 0;
+  if (pr.info == 0) {
+    ZG_TRY(mpir_refine(c, o, nrhs, B, ldb, X, ldx, false, &pr, s));
+    ZG_TRY(cond_estimate(c, kCondSteps, &kappa, s));
+  }
   ZG_CUDA(cudaStreamSynchronize(s));
-  probe_features(pr, feat);
+  probe_features(pr, kappa, feat);
   std::copy(feat, feat + kSelFeatures, r->features);
   if (pr.info == 0 && pr.converged) {
     r->used = kClassBF16;

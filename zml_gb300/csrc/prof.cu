@@ -5,7 +5,7 @@
 
 namespace zg {
 
-unsigned long long g_launches = 0;
+std::atomic<unsigned long long> g_launches{0};
 bool g_profiling = false;
 
 namespace {
@@ -100,6 +100,6 @@ int zml_gpu_profile_read(int tag, unsigned long long *launches, double *ms, doub
 }
 
 // Number of kernels this library has launched in this process.
-unsigned long long zml_gpu_launch_count(void) { return g_launches; }
+unsigned long long zml_gpu_launch_count(void) { return g_launches.load(); }
 
 }  // extern "C"

@@ -123,16 +123,51 @@ def fp64_ms(torch, t, b, n):
     return (time.perf_counter() - t0) * 1e3
 
 
-def build_dataset(torch, specs, dev, log=None, rank=0, world=1):
+def _run_workers(torch, dev, idx, workers, fn):
+    """fn(i) for every i of idx on `workers` host threads, each with its own
+    CUDA stream (the library keeps its workspaces per stream, so the solves
+    of different threads share nothing).  Small solves occupy a few SMs, so
+    several in flight raise throughput; the first exception is re-raised."""
+    import threading
+    errors = []
+
+    def body(part):
+        try:
+            torch.cuda.set_device(dev)
+            with torch.cuda.stream(torch.cuda.Stream(device=dev)):
+                for i in part:
+                    if errors:
+                        return
+                    fn(i)
+                torch.cuda.current_stream().synchronize()
+        except Exception as e:  # noqa: BLE001 - re-raised below
+            errors.append(e)
+
+    workers = max(1, min(workers, len(idx)))
+    if workers == 1:
+        body(idx)
+    else:
+        th = [threading.Thread(target=body, args=(idx[w::workers],)) for w in range(workers)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+    if errors:
+        raise errors[0]
+
+
+def build_dataset(torch, specs, dev, log=None, rank=0, world=1, workers=1):
     """Features (float32, len x 16), labels (int32) and the plain ladder's
-    wall time (ms) per matrix.  With world > 1 (an initialised process group)
-    each rank labels its n^3-balanced contiguous share and every rank
-    returns the gathered whole."""
+    wall time (ms; inflated when workers > 1) per matrix.  With world > 1
+    (an initialised process group) each rank labels its n^3-balanced
+    contiguous share and every rank returns the gathered whole."""
     lo, hi = shard.shard([s[1] for s in specs], rank, world)
     X = np.zeros((len(specs), NF), dtype=np.float32)
     y = np.zeros(len(specs), dtype=np.int32)
     ms = np.zeros(len(specs))
-    for i in range(lo, hi):
+    done = [0]
+
+    def label(i):
         kind, n, kappa, seed = specs[i]
         t, m = generate(torch, kind, n, kappa, seed, dev)
         b = rhs(torch, m, seed)
@@ -144,8 +179,11 @@ def build_dataset(torch, specs, dev, log=None, rank=0, world=1):
         X[i] = np.frombuffer(res.features, dtype=np.float32)
         y[i] = res.used
         ms[i] = res.ms
-        if log and (i + 1 - lo) % 500 == 0:
-            log("  %d/%d matrices labelled" % (i + 1 - lo, hi - lo))
+        done[0] += 1
+        if log and done[0] % 2500 == 0:
+            log("  %d/%d matrices labelled" % (done[0], hi - lo))
+
+    _run_workers(torch, dev, list(range(lo, hi)), workers, label)
     if world > 1:
         for plo, phi, pX, py, pms in shard.gather((lo, hi, X[lo:hi], y[lo:hi], ms[lo:hi])):
             X[plo:phi], y[plo:phi], ms[plo:phi] = pX, py, pms
@@ -283,14 +321,20 @@ def warm_up(torch, dev, nmax):
     fp64_ms(torch, t, b, nmax)
 
 
-def evaluate(torch, specs, state, dev, confidence=DEFAULT_CONFIDENCE, log=None, rank=0, world=1):
+def evaluate(torch, specs, state, dev, confidence=DEFAULT_CONFIDENCE, log=None, rank=0, world=1,
+             workers=1, time_sample=0):
     """Solves every held-out matrix with the plain ladder and with the ladder
-    guided by the network (alternating which goes first), plus the FP64 LU.
-    Returns per-matrix records and a summary (sharded like build_dataset)."""
+    guided by the network (on `workers` concurrent streams), recording
+    labels, choices and convergence.  Then `time_sample` of them, spread
+    over the n range, are solved again one at a time -- ladder, guided (in
+    alternating order) and the FP64 LU -- for the time comparison.  Returns
+    per-matrix records and a summary (sharded like build_dataset)."""
     model = model_array(state)
-    rec = []
     lo, hi = shard.shard([s[1] for s in specs], rank, world)
-    for i in range(lo, hi):
+    recs = {}
+    done = [0]
+
+    def solve_both(i, timed=False):
         kind, n, kappa, seed = specs[i]
         t, m = generate(torch, kind, n, kappa, seed, dev)
         b = rhs(torch, m, seed)
@@ -300,27 +344,64 @@ def evaluate(torch, specs, state, dev, confidence=DEFAULT_CONFIDENCE, log=None, 
             runs["guided" if which is not None else "ladder"] = solve_auto(
                 torch, t, b, x, n, which, confidence)
         lad, gui = runs["ladder"], runs["guided"]
-        rec.append({"kind": kind, "n": n, "kappa": kappa, "label": lad.used,
-                    "predicted": gui.predicted, "used": gui.used, "attempts": gui.attempts,
-                    "ladder_attempts": lad.attempts, "converged": bool(gui.converged),
-                    "ladder_converged": bool(lad.converged), "berr": gui.berr,
-                    "ladder_ms": lad.ms, "guided_ms": gui.ms, "fp64_ms": fp64_ms(torch, t, b, n),
-                    "features": list(np.frombuffer(lad.features, dtype=np.float32).tolist())})
-        if log and (i + 1 - lo) % 250 == 0:
-            log("  %d/%d held-out matrices" % (i + 1 - lo, hi - lo))
+        r = {"kind": kind, "n": n, "kappa": kappa, "label": lad.used,
+             "predicted": gui.predicted, "used": gui.used, "attempts": gui.attempts,
+             "ladder_attempts": lad.attempts, "converged": bool(gui.converged),
+             "ladder_converged": bool(lad.converged), "berr": gui.berr,
+             "features": list(np.frombuffer(lad.features, dtype=np.float32).tolist())}
+        if timed:
+            r.update({"ladder_ms": lad.ms, "guided_ms": gui.ms, "fp64_ms": fp64_ms(torch, t, b, n)})
+        return r
+
+    def conv(i):
+        recs[i] = solve_both(i)
+        done[0] += 1
+        if log and done[0] % 1000 == 0:
+            log("  %d/%d held-out matrices" % (done[0], hi - lo))
+
+    _run_workers(torch, dev, list(range(lo, hi)), workers, conv)
+    # the timing sample: every k-th matrix in order of n, one at a time
+    order = sorted(range(lo, hi), key=lambda i: specs[i][1])
+    k = max(1, len(order) // time_sample) if time_sample > 0 else 0
+    for i in (order[::k][:time_sample] if k else []):
+        r = solve_both(i, timed=True)
+        recs[i].update({key: r[key] for key in ("ladder_ms", "guided_ms", "fp64_ms")})
+    rec = [recs[i] for i in range(lo, hi)]
     if world > 1:
         rec = [r for part in shard.gather(rec) for r in part]
     return rec, summarize(rec)
+
+
+BUCKETS = ((64, 128), (128, 256), (256, 512), (512, 1024), (1024, 2049))
 
 
 def summarize(rec):
     lab = np.array([r["label"] for r in rec])
     pred = np.array([r["predicted"] if r["predicted"] >= 0 else r["label"] for r in rec])
     probed = np.array([r["predicted"] >= 0 for r in rec])
-    lad = np.array([r["ladder_ms"] for r in rec])
-    gui = np.array([r["guided_ms"] for r in rec])
-    f64 = np.array([r["fp64_ms"] for r in rec])
-    return {
+    timed = [r for r in rec if "guided_ms" in r]
+    lad = np.array([r["ladder_ms"] for r in timed])
+    gui = np.array([r["guided_ms"] for r in timed])
+    f64 = np.array([r["fp64_ms"] for r in timed])
+    by_n = []
+    for a, b in BUCKETS:
+        sel = [r for r in timed if a <= r["n"] < b]
+        if sel:
+            by_n.append({"n": [a, b - 1], "timed": len(sel),
+                         "ladder_ms_median": float(np.median([r["ladder_ms"] for r in sel])),
+                         "guided_ms_median": float(np.median([r["guided_ms"] for r in sel])),
+                         "fp64_ms_median": float(np.median([r["fp64_ms"] for r in sel])),
+                         "guided_ms_total": float(sum(r["guided_ms"] for r in sel)),
+                         "fp64_ms_total": float(sum(r["fp64_ms"] for r in sel))})
+    conv_by_n = []
+    for a, b in BUCKETS:
+        sel = [r for r in rec if a <= r["n"] < b]
+        if sel:
+            conv_by_n.append({"n": [a, b - 1], "matrices": len(sel),
+                              "converged_guided": float(np.mean([r["converged"] for r in sel])),
+                              "label_counts": np.bincount([r["label"] for r in sel],
+                                                          minlength=NO).tolist()})
+    out = {
         "matrices": len(rec),
         "label_counts": np.bincount(lab, minlength=NO).tolist(),
         "converged_guided": float(np.mean([r["converged"] for r in rec])),
@@ -330,23 +411,34 @@ def summarize(rec):
         "choice_at_or_above_label": float(np.mean(pred[probed] >= lab[probed])) if probed.any() else 1.0,
         "choice_exact": float(np.mean(pred[probed] == lab[probed])) if probed.any() else 1.0,
         "probe_settled": float(np.mean(~probed)),
-        "ladder_ms_total": float(lad.sum()),
-        "guided_ms_total": float(gui.sum()),
-        "fp64_ms_total": float(f64.sum()),
-        "speedup_vs_ladder": float(lad.sum() / gui.sum()),
-        "speedup_vs_fp64": float(f64.sum() / gui.sum()),
         "attempts_ladder": float(np.mean([r["ladder_attempts"] for r in rec])),
         "attempts_guided": float(np.mean([r["attempts"] for r in rec])),
+        "by_n": conv_by_n,
     }
+    if timed:
+        out.update({
+            "timed": len(timed),
+            "ladder_ms_total": float(lad.sum()),
+            "guided_ms_total": float(gui.sum()),
+            "fp64_ms_total": float(f64.sum()),
+            "speedup_vs_ladder": float(lad.sum() / gui.sum()),
+            "speedup_vs_fp64": float(f64.sum() / gui.sum()),
+            "time_by_n": by_n,
+        })
+    return out
 
 
 def main():
     import argparse
     import torch
     ap = argparse.ArgumentParser(description="train and evaluate the precision selector")
-    ap.add_argument("--train", type=int, default=4000)
-    ap.add_argument("--heldout", type=int, default=1000)
-    ap.add_argument("--nmax", type=int, default=1024)
+    ap.add_argument("--train", type=int, default=50000)
+    ap.add_argument("--heldout", type=int, default=5000)
+    ap.add_argument("--nmax", type=int, default=2048)
+    ap.add_argument("--workers", type=int, default=8,
+                    help="concurrent solves (threads, one CUDA stream each)")
+    ap.add_argument("--time-sample", type=int, default=500,
+                    help="held-out matrices timed one at a time for the time comparison")
     ap.add_argument("--epochs", type=int, default=300)
     ap.add_argument("--confidence", type=float, default=DEFAULT_CONFIDENCE)
     ap.add_argument("--checkpoint", default=None)
@@ -373,7 +465,7 @@ def main():
     t0 = time.time()
     warm_up(torch, dev, a.nmax)
     Xtr, ytr, _ = build_dataset(torch, sample_specs(a.train, seed=1, nmax=a.nmax), dev, log,
-                                rank, world)
+                                rank, world, a.workers)
     log("labelled %d training matrices in %.0f s, classes %s" %
         (a.train, time.time() - t0, np.bincount(ytr, minlength=NO).tolist()))
     t1 = time.time()
@@ -383,9 +475,12 @@ def main():
         (a.epochs, time.time() - t1, state["loss_history"][0], state["loss_history"][-1]))
     if a.out and rank == 0:
         save_checkpoint(a.out, state)
+    t2 = time.time()
     rec, summ = evaluate(torch, sample_specs(a.heldout, seed=2, nmax=a.nmax), state, dev,
-                         a.confidence, log, rank, world)
-    summ.update({"train": a.train, "nmax": a.nmax, "epochs": a.epochs,
+                         a.confidence, log, rank, world, a.workers, a.time_sample)
+    log("evaluated %d held-out matrices in %.0f s" % (a.heldout, time.time() - t2))
+    summ.update({"train": a.train, "nmax": a.nmax, "epochs": a.epochs, "workers": a.workers,
+                 "label_seconds": t1 - t0, "train_seconds": t2 - t1,
                  "confidence": a.confidence, "train_label_counts":
                  np.bincount(ytr, minlength=NO).tolist(),
                  "loss_first": float(state["loss_history"][0]),
