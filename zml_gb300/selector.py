@@ -123,7 +123,7 @@ def fp64_ms(torch, t, b, n):
     return (time.perf_counter() - t0) * 1e3
 
 
-def _run_workers(torch, dev, idx, workers, fn):
+def _run_workers(torch, dev, idx, workers, fn, warm=None):
     """fn(i) for every i of idx on `workers` host threads, each with its own
     CUDA stream (the library keeps its workspaces per stream, so the solves
     of different threads share nothing).  Small solves occupy a few SMs, so
@@ -135,6 +135,8 @@ def _run_workers(torch, dev, idx, workers, fn):
         try:
             torch.cuda.set_device(dev)
             with torch.cuda.stream(torch.cuda.Stream(device=dev)):
+                if warm is not None and part:
+                    warm()
                 for i in part:
                     if errors:
                         return
@@ -183,7 +185,9 @@ def build_dataset(torch, specs, dev, log=None, rank=0, world=1, workers=1):
         if log and done[0] % 2500 == 0:
             log("  %d/%d matrices labelled" % (done[0], hi - lo))
 
-    _run_workers(torch, dev, list(range(lo, hi)), workers, label)
+    nmax = max([s[1] for s in specs[lo:hi]], default=0)
+    _run_workers(torch, dev, list(range(lo, hi)), workers, label,
+                 (lambda: warm_up(torch, dev, nmax)) if workers > 1 and nmax else None)
     if world > 1:
         for plo, phi, pX, py, pms in shard.gather((lo, hi, X[lo:hi], y[lo:hi], ms[lo:hi])):
             X[plo:phi], y[plo:phi], ms[plo:phi] = pX, py, pms
@@ -359,7 +363,9 @@ def evaluate(torch, specs, state, dev, confidence=DEFAULT_CONFIDENCE, log=None, 
         if log and done[0] % 1000 == 0:
             log("  %d/%d held-out matrices" % (done[0], hi - lo))
 
-    _run_workers(torch, dev, list(range(lo, hi)), workers, conv)
+    nmax = max([s[1] for s in specs[lo:hi]], default=0)
+    _run_workers(torch, dev, list(range(lo, hi)), workers, conv,
+                 (lambda: warm_up(torch, dev, nmax)) if workers > 1 and nmax else None)
     # the timing sample: every k-th matrix in order of n, one at a time
     order = sorted(range(lo, hi), key=lambda i: specs[i][1])
     k = max(1, len(order) // time_sample) if time_sample > 0 else 0
