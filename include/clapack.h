@@ -364,6 +364,13 @@ int zml_gpu_mixed_panel(int tournament);
  * FP64 GEMM); 0 on the FP64 pipe.  Returns the previous mode.  No counterpart
  * in the reference (an FP64 loop nest). */
 int zml_gpu_fp64_updates(int mode);
+/* Rows per thread block that the cooperative LU panel (the FP64 panel, and
+ * the FP32 one where the cluster panel does not apply) aims for: fewer,
+ * taller blocks make its per-column grid barrier cheaper and its per-column
+ * update longer.  0 spreads the panel over every SM; a negative value
+ * restores the default.  The factorization is the same for every value.
+ * Returns the previous setting.  No counterpart in the reference. */
+int zml_gpu_panel_rows(int rows);
 /* The FP64 update those factorizations use, on device memory (column-major):
  * C (m x n) -= A (m x k) B (k x n) with k <= 256, by exact 7-bit slices of A's
  * rows and B's columns multiplied on the BF16 tensor cores; lower != 0:

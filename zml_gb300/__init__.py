@@ -69,6 +69,7 @@ _SIGS.update({
     "zml_gpu_set_spin_limit": (i32, [C.c_longlong]),
     "zml_gpu_mixed_panel": (i32, [i32]),
     "zml_gpu_fp64_updates": (i32, [i32]),
+    "zml_gpu_panel_rows": (i32, [i32]),
     "zml_gpu_dgemm_slices": (i32, [i32, i32, i32, vp, i32, vp, i32, vp, i32, i32, vp]),
     "zml_gpu_sgetrf_calu": (i32, [i32, i32, vp, i32, vp, vp, vp]),
     "zml_gpu_version": (i32, []),

@@ -1240,6 +1240,7 @@ int zml_gpu_set_spin_limit(long long tries) { return set_spin_limit(tries); }
 int zml_gpu_mixed_panel(int tournament) { return set_mixed_tournament(tournament); }
 
 int zml_gpu_fp64_updates(int mode) { return set_fp64_updates(mode); }
+int zml_gpu_panel_rows(int rows) { return set_panel_rows(rows); }
 
 int zml_gpu_dgemm_slices(int m, int n, int k, const double *dA, int ldda, const double *dB,
                          int lddb, double *dC, int lddc, int lower, void *stream) {

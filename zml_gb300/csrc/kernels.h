@@ -116,6 +116,10 @@ int dgemm_oz_sub(int m, int n, int k, const double *A, long lda, const double *B
 int getrf_oz(int m, int n, double *A, long lda, int *ipiv, int *info, cudaStream_t s);
 int potrf_oz(int n, double *A, long lda, int *info, cudaStream_t s);  // lower
 int set_fp64_updates(int mode);                    // returns the previous mode
+// Rows per CTA targeted by the cooperative FP64 / FP32 panel (0: spread over
+// every SM); returns the previous target; negative restores the default.
+constexpr int kPanelRowsDefault = 0;
+int set_panel_rows(int rows);
 bool fp64_updates_on_tensor_cores(int m, int n);
 template <typename T>
 int getrs_dev(int trans, int n, int nrhs, const T *A, long lda, const int *ipiv, T *B, long ldb,

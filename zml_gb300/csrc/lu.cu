@@ -185,6 +185,11 @@ __global__ void __launch_bounds__(256) panel_lu_kernel(int m, int nb, T *__restr
   }
 }
 
+// Rows per CTA of the cooperative panel (0: spread over every SM, at least
+// 8 rows each).
+static std::atomic<int> g_panel_rows{kPanelRowsDefault};
+int set_panel_rows(int rows) { return g_panel_rows.exchange(rows < 0 ? kPanelRowsDefault : rows); }
+
 template <typename T>
 int panel_lu(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *ctl, int info_base,
              cudaStream_t s) {
@@ -195,14 +200,20 @@ int panel_lu(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *c
   }
   DeviceInfo di;
   ZG_TRY(device_info(&di));
-  // rows per CTA: at least 8, at most what fits in shared memory
+  // rows per CTA: the tuning target (fewer CTAs make the per-column grid
+  // barrier cheaper, taller slabs the per-column update longer), at least
+  // m / SMs (one CTA per SM), at most what fits in shared memory
   const size_t limit = di.smem_optin - 4096;
-  int nblk = min(di.num_sms, ceil_div(m, 8));
-  int R = ceil_div(m, nblk);
-  if ((size_t)R * nb * sizeof(T) > limit) {
+  const int rmax = (int)(limit / ((size_t)nb * sizeof(T)));
+  const int target = g_panel_rows.load();
+  int R = target > 0 ? std::min(rmax, target) : 8;
+  R = std::max(R, ceil_div(m, di.num_sms));
+  if (R > rmax) {
     set_last_error("panel_lu: panel %d x %d too tall for %d SMs", m, nb, di.num_sms);
     return kErrInvalid;
   }
+  int nblk = ceil_div(m, R);
+  R = ceil_div(m, nblk);
   nblk = ceil_div(m, R);
   const size_t smem = (size_t)R * nb * sizeof(T);
   void *xchg;
