@@ -34,6 +34,7 @@ template <int BN, int STAGES> struct TileCfg {
   static constexpr int b_bytes = BN * kBK * 2;
   static constexpr int stage_bytes = a_bytes + b_bytes;
   static constexpr int smem_bytes = STAGES * stage_bytes + 1024 /*align*/ + 256 /*barriers*/;
+  static_assert(2 * STAGES * 8 + 8 + 4 + 3 * 4 <= 256, "barrier area");
   static constexpr uint32_t tmem_cols = BN < 32 ? 32 : BN;
 };
 
@@ -55,12 +56,16 @@ __global__ void __launch_bounds__(256)
   uint64_t *empty = full + kStages;
   uint64_t *done = empty + kStages;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+  // stages the producer issued and the MMA issuer consumed, and whether any
+  // wait of the CTA ran out (then the exit drains what is still in flight)
+  int *issued = reinterpret_cast<int *>(tmem_slot + 1), *consumed = issued + 1, *bad = issued + 2;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
   const int KT = (K + kBK - 1) / kBK;
 
   if (warp == 0 && lane == 0) {
+    *issued = *consumed = *bad = 0;
     tc::prefetch_tmap(&tmA);
     tc::prefetch_tmap(&tmB);
     for (int s = 0; s < kStages; ++s) {
@@ -80,7 +85,8 @@ __global__ void __launch_bounds__(256)
   bool ok = true;
 
   if (warp == 0 && lane == 0) {  // TMA producer
-    for (int kt = 0; kt < KT && ok; ++kt) {
+    int kt = 0;
+    for (; kt < KT && ok; ++kt) {
       const int s = kt % kStages, round = kt / kStages;
       if (round > 0) ok = tc::mbar_wait(&empty[s], (round - 1) & 1, status);
       if (!ok) break;
@@ -90,9 +96,12 @@ __global__ void __launch_bounds__(256)
       tc::tma_load_2d(sa, &tmA, &full[s], kt * kBK, m0);
       tc::tma_load_2d(sb, &tmB, &full[s], kt * kBK, n0);
     }
+    *issued = kt;
+    if (!ok) *bad = 1;
   } else if (warp == 1 && lane == 0) {  // MMA issuer
     const uint32_t idesc = tc::idesc_f16(kBM, BN, ab_type);
-    for (int kt = 0; kt < KT && ok; ++kt) {
+    int kt = 0;
+    for (; kt < KT && ok; ++kt) {
       const int s = kt % kStages, round = kt / kStages;
       ok = tc::mbar_wait(&full[s], round & 1, status);
       if (!ok) break;
@@ -105,6 +114,8 @@ __global__ void __launch_bounds__(256)
         tc::mma_f16(tmem, adesc + 2 * kk, bdesc + 2 * kk, idesc, (kt | kk) != 0);
       tc::mma_commit(&empty[s]);
     }
+    *consumed = kt;
+    if (!ok) *bad = 1;
     tc::mma_commit(done);
   }
   __syncwarp();
@@ -128,6 +139,7 @@ __global__ void __launch_bounds__(256)
     for (int j = 0; j < 32; ++j) old[q][j] = (pre && j < nc) ? __ldcg(base + (long)j * ldc) : 0.f;
   }
   const bool have = tc::mbar_wait(done, 0, status);
+  if (!have) *bad = 1;
   tc::tc_fence_after();
   if (have && K > 0) {
     const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16);
@@ -152,6 +164,15 @@ __global__ void __launch_bounds__(256)
     }
   }
   tc::tc_fence_before();
+  __syncthreads();
+  // after a wait ran out: wait (bounded again) for the TMA copies issued but
+  // never consumed and for the MMAs behind the final commit, so that neither
+  // lands in shared memory or TMEM after the CTA has released them
+  if (*bad && threadIdx.x == 0) {
+    for (int kt = *consumed; kt < *issued; ++kt)
+      tc::mbar_wait(&full[kt % kStages], (kt / kStages) & 1, status);
+    tc::mbar_wait(done, 0, status);
+  }
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, Cfg::tmem_cols);
 }
