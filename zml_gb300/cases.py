@@ -13,7 +13,7 @@ Each run is timed with CUDA events and printed with its return code.
 import argparse
 import ctypes as C
 
-from . import MpirResult, last_error, lib
+from . import MpirResult, last_error, lib, profile_read
 
 
 def main():
@@ -23,6 +23,8 @@ def main():
                                      "dsytrf"])
     ap.add_argument("n", type=int)
     ap.add_argument("--reps", type=int, default=2)
+    ap.add_argument("--profile", action="store_true",
+                    help="one more run with per-launch CUDA events: time per kernel class")
     ap.add_argument("--fp64-updates", type=int, default=1,
                     help="1: FP64 trailing updates by exact slices on the tensor cores "
                          "(above the size threshold), 0: on the FP64 pipe")
@@ -82,6 +84,15 @@ def main():
                                                      "" if rc == 0 else " " + last_error()))
         if rc != 0:
             raise SystemExit(1)
+    if a.profile:
+        L.zml_gpu_profile(1)
+        run()
+        torch.cuda.synchronize()
+        prof = profile_read()
+        L.zml_gpu_profile(0)
+        for name, (cnt, ms, fl, by) in sorted(prof.items(), key=lambda kv: -kv[1][1]):
+            print("  %-10s %6d launches %9.3f ms %8.2f TFLOP/s %8.1f GB/s"
+                  % (name, cnt, ms, fl / ms / 1e9 if ms else 0, by / ms / 1e6 if ms else 0))
 
 
 if __name__ == "__main__":
