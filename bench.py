@@ -186,6 +186,27 @@ def cpu_reference_sample(n, threads):
     return dt, step_flops
 
 
+def cpu_extrapolation_check(n=4096):
+    """The reference arm's extrapolation checked at a size the oracle solves
+    in seconds: the full single-threaded oracle getrf + getrs of an n x n
+    N(0,1) system against the time its first 64-column block step predicts."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib as ol
+    dt, fl = cpu_reference_sample(n, 1)
+    predicted = lu_flops(n) / (fl / dt)
+    a = cpu_matrix(n)
+    b = np.random.default_rng(3).random((n, 1)) * 2 - 1
+    t0 = time.perf_counter()
+    lu, ipiv, info = ol.getrf(a)
+    x = ol.getrs(lu, ipiv, b)
+    measured = time.perf_counter() - t0
+    r = a @ x - b
+    berr = float(np.abs(r).max() / (np.abs(a).sum(1).max() * np.abs(x).max() + np.abs(b).max()))
+    return {"n": n, "threads": 1, "predicted_s": predicted, "measured_s": measured,
+            "measured_over_predicted": measured / predicted, "info": int(info), "berr": berr}
+
+
 def cpu_block(n, threads, label):
     dt, fl = cpu_reference_sample(n, threads)
     rate = fl / dt
@@ -582,6 +603,10 @@ def suite_bench(torch, zg, L, dev, st):
     del S
     torch.cuda.empty_cache()
     out["next"] = next_rows_bench(torch, L, dev, g)
+    try:
+        out["cpu_extrapolation_check"] = cpu_extrapolation_check()
+    except Exception as e:  # noqa: BLE001 - reported in the line
+        out["cpu_extrapolation_check"] = {"error": str(e)[:200]}
     return out
 
 
