@@ -104,6 +104,12 @@ int LAPACKE_cposv(int matrix_layout, char uplo, int n, int nrhs, void *a, int ld
  * and A = H(0) ... H(k-1) R. */
 int LAPACKE_zgeqrf(int matrix_layout, int m, int n, void *a, int lda, void *tau);
 int LAPACKE_cgeqrf(int matrix_layout, int m, int n, void *a, int lda, void *tau);
+/* complex symmetric Bunch-Kaufman (lapack.zig:4430 LAPACKE_zsytrf and its
+ * cfloat twin; kernel lapack/sytrf.zig:17 over cfloat): A = U D U^T or
+ * L D L^T without conjugation, pivot magnitudes |re| + |im|; ipiv and info as
+ * LAPACKE_dsytrf. */
+int LAPACKE_zsytrf(int matrix_layout, char uplo, int n, void *a, int lda, int *ipiv);
+int LAPACKE_csytrf(int matrix_layout, char uplo, int n, void *a, int lda, int *ipiv);
 
 /* replaces zml.linalg.lapack.geqrf (lapack.zig:5060; kernel lapack/geqrf.zig:18):
  * R in the upper triangle, the Householder vectors below it, tau[min(m,n)] */

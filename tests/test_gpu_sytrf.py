@@ -133,3 +133,56 @@ def test_dsytrf_device_pointers_n1536_bitwise(uplo):
     f = F.cpu().numpy().T  # column-major view
     tri = np.triu if uplo == b"U" else np.tril
     np.testing.assert_array_equal(tri(f), tri(fr))
+
+
+def csym(n, seed, dtype=np.complex128):
+    rng = np.random.default_rng(seed)
+    g = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    return np.asfortranarray(((g + g.T) / 2).astype(dtype))  # complex symmetric, not Hermitian
+
+
+def gpu_zsytrf(a, uplo, layout=102):
+    n = a.shape[0]
+    buf = np.array(a, order="F" if layout == 102 else "C", copy=True)
+    ipiv = np.zeros(n, dtype=np.int32)
+    f = zg.lib().LAPACKE_zsytrf if a.dtype == np.complex128 else zg.lib().LAPACKE_csytrf
+    info = f(layout, uplo, n, P(buf), n, P(ipiv))
+    return np.asfortranarray(buf), ipiv, info
+
+
+@pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
+@pytest.mark.parametrize("uplo", [b"U", b"L"])
+@pytest.mark.parametrize("n", [1, 2, 5, 64, 130, 257])
+def test_zsytrf_bitwise_equals_oracle_sytf2(n, uplo, dtype):
+    """Complex symmetric Bunch-Kaufman (no conjugation, |re| + |im| pivots,
+    zml's fused complex products and Smith quotients): the oracle's complex
+    sytf2 bit for bit, the untouched triangle left as it was."""
+    a = csym(n, seed=3 * n + uplo[0], dtype=dtype)
+    f, ipiv, info = gpu_zsytrf(a, uplo)
+    ul = 121 if uplo == b"U" else 122
+    fr, ipr, infr = oracle_sytf2(a, ul)
+    assert info == infr == 0
+    np.testing.assert_array_equal(ipiv, ipr)
+    tri = np.triu if uplo == b"U" else np.tril
+    np.testing.assert_array_equal(tri(f), tri(fr))
+    np.testing.assert_array_equal(f - tri(f), a - tri(a))
+
+
+def test_zsytrf_row_major_zero_column_and_lapack_solve():
+    a = csym(90, seed=8)
+    fc, pc, _ = gpu_zsytrf(a, b"L")
+    fr, pr, _ = gpu_zsytrf(a, b"L", layout=101)
+    np.testing.assert_array_equal(pr, pc)
+    np.testing.assert_array_equal(np.tril(fr), np.tril(fc))
+    x = np.random.default_rng(2).standard_normal((90, 2)) + 0j
+    sol, inf = lap.zsytrs(fc, pc, a @ x, lower=1)
+    assert inf == 0
+    np.testing.assert_allclose(sol, x, rtol=1e-9, atol=1e-9)
+    z = csym(30, seed=6)
+    z[11, :] = 0
+    z[:, 11] = 0
+    for uplo, ul in ((b"U", 121), (b"L", 122)):
+        f, ipiv, info = gpu_zsytrf(z, uplo)
+        fr, ipr, infr = oracle_sytf2(z, ul)
+        assert info == infr > 0
+        np.testing.assert_array_equal(ipiv, ipr)

@@ -868,6 +868,10 @@ CBLAS_ZGEMM(c, float)
   }                                                                                              \
   int LAPACKE_##P##geqrf(int layout, int m, int n, void *a, int lda, void *tau) {                \
     return zgeqrf_any<R>(layout, m, n, (R *)a, lda, (R *)tau);                                   \
+  }                                                                                              \
+  int LAPACKE_##P##sytrf(int layout, char uplo, int n, void *a, int lda, int *ipiv) {            \
+    using C2 = typename Cx<R>::T;                                                                \
+    return sytrf_any<C2>(layout, uplo, n, (C2 *)a, lda, ipiv);                                   \
   }
 int LAPACKE_dsytrf(int layout, char uplo, int n, double *a, int lda, int *ipiv) {
   return sytrf_any<double>(layout, uplo, n, a, lda, ipiv);

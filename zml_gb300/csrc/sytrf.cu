@@ -24,32 +24,84 @@
 
 namespace zg {
 
-template <typename T> struct Rn;
-template <> struct Rn<double> {
-  static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
-  static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
-  static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
-  static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+// Arithmetic of one step, as the restatement performs it.  Real: every
+// product and sum rounded on its own (no FMA contraction).  Complex (double2 /
+// float2 = (re, im)): zml's cfloat -- products re = fma(x.re, y.re,
+// -x.im y.im), im = fma(x.re, y.im, x.im y.re) (operand order matters),
+// component-wise sums, Smith's division with fused updates, 1 / z as
+// (1 + 0i) / z, and pivot magnitudes |re| + |im|.
+template <typename T> struct BkOps;
+template <typename F> struct BkReal {
+  using R = F;
+  static __device__ __forceinline__ F mul(F a, F b) { return BkOps<F>::rmul(a, b); }
+  static __device__ __forceinline__ F add(F a, F b) { return BkOps<F>::radd(a, b); }
+  static __device__ __forceinline__ F sub(F a, F b) { return BkOps<F>::rsub(a, b); }
+  static __device__ __forceinline__ F div(F a, F b) { return BkOps<F>::rdiv(a, b); }
+  static __device__ __forceinline__ F inv(F a) { return F(1) / a; }
+  static __device__ __forceinline__ F sub1(F a) { return sub(a, F(1)); }
+  static __device__ __forceinline__ F neg(F a) { return -a; }
+  static __device__ __forceinline__ F mag(F a) { return fabs(a); }
+  static __device__ __forceinline__ bool is0(F a) { return a == F(0); }
+  static __device__ __forceinline__ bool is1(F a) { return a == F(1); }
 };
-template <> struct Rn<float> {
-  static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
-  static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
-  static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
-  static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+template <> struct BkOps<double> : BkReal<double> {
+  static __device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+  static __device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+  static __device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
+  static __device__ __forceinline__ double rdiv(double a, double b) { return __ddiv_rn(a, b); }
 };
+template <> struct BkOps<float> : BkReal<float> {
+  static __device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+  static __device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+  static __device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+  static __device__ __forceinline__ float rdiv(float a, float b) { return __fdiv_rn(a, b); }
+};
+template <typename C, typename F> struct BkCplx {
+  using R = F;
+  using O = BkOps<F>;
+  static __device__ __forceinline__ C mk(F re, F im) {
+    C z;
+    z.x = re;
+    z.y = im;
+    return z;
+  }
+  static __device__ __forceinline__ C mul(C a, C b) {
+    return mk(fma(a.x, b.x, O::rmul(-a.y, b.y)), fma(a.x, b.y, O::rmul(a.y, b.x)));
+  }
+  static __device__ __forceinline__ C add(C a, C b) { return mk(O::radd(a.x, b.x), O::radd(a.y, b.y)); }
+  static __device__ __forceinline__ C sub(C a, C b) { return mk(O::rsub(a.x, b.x), O::rsub(a.y, b.y)); }
+  static __device__ __forceinline__ C div(C a, C b) {
+    if (fabs(b.y) < fabs(b.x)) {
+      const F t1 = O::rdiv(b.y, b.x);
+      const F t2 = O::rdiv(F(1), fma(t1, b.y, b.x));
+      return mk(O::rmul(fma(a.y, t1, a.x), t2), O::rmul(fma(-a.x, t1, a.y), t2));
+    }
+    const F t1 = O::rdiv(b.x, b.y);
+    const F t2 = O::rdiv(F(1), fma(t1, b.x, b.y));
+    return mk(O::rmul(fma(a.x, t1, a.y), t2), O::rmul(fma(a.y, t1, -a.x), t2));
+  }
+  static __device__ __forceinline__ C inv(C a) { return div(mk(F(1), F(0)), a); }
+  static __device__ __forceinline__ C sub1(C a) { return mk(O::rsub(a.x, F(1)), a.y); }
+  static __device__ __forceinline__ C neg(C a) { return mk(-a.x, -a.y); }
+  static __device__ __forceinline__ F mag(C a) { return O::radd(fabs(a.x), fabs(a.y)); }
+  static __device__ __forceinline__ bool is0(C a) { return a.x == F(0) && a.y == F(0); }
+  static __device__ __forceinline__ bool is1(C a) { return a.x == F(1) && a.y == F(0); }
+};
+template <> struct BkOps<double2> : BkCplx<double2, double> {};
+template <> struct BkOps<float2> : BkCplx<float2, float> {};
 
 // the C macro max of the restatement: (a) > (b) ? (a) : (b)
 template <typename T> __device__ __forceinline__ T cmax(T a, T b) { return a > b ? a : b; }
 
-// zml's iamax over len values v(t), t = 0 .. len-1, by the whole CTA:
-// first maximum of |v|, NaN never chosen, a NaN first blocks (index 0).
+// zml's iamax over len magnitudes v(t), t = 0 .. len-1, by the whole CTA:
+// the first maximum, NaN never chosen, a NaN first blocks (index 0).
 template <typename T, typename F>
 __device__ int cta_iamax(int len, F v, T *sv, int *si) {
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   T best = T(-1);
   int bi = INT_MAX;
   for (int q = t; q < len; q += blockDim.x) {
-    const T a = fabs(v(q));
+    const T a = v(q);
     if (a > best) {
       best = a;
       bi = q;
@@ -75,7 +127,7 @@ __device__ int cta_iamax(int len, F v, T *sv, int *si) {
         best = sv[q];
         bi = si[q];
       }
-    const T a0 = len > 0 ? fabs(v(0)) : T(0);
+    const T a0 = len > 0 ? v(0) : T(0);
     si[0] = (len <= 0 || a0 != a0 || bi == INT_MAX) ? 0 : bi;
   }
   __syncthreads();
@@ -108,11 +160,14 @@ template <typename T> __device__ __forceinline__ T cta_bcast(T v, T *slot) {
 // previous step's block, pivot choice, interchange, ipiv, info.
 template <typename T>
 __global__ void __launch_bounds__(1024) sytf2_pivot_kernel(int n, T *A, long lda, bool upper,
-                                                           T alpha, int *ipiv, int *st,
-                                                           int *info) {
-  __shared__ T sv[32];
+                                                           typename BkOps<T>::R alpha, int *ipiv,
+                                                           int *st, int *info) {
+  using Ops = BkOps<T>;
+  using R = typename Ops::R;
+  using RO = BkOps<R>;
+  __shared__ R sv[32];
   __shared__ int si[32];
-  __shared__ T sb;
+  __shared__ R sb;
   auto a = [&](int i, int j) -> T & { return A[i + (long)j * lda]; };
   if (st[kStDone]) return;
   const int k = upper ? st[kStK] - st[kStStep] : st[kStK] + st[kStStep];
@@ -121,42 +176,44 @@ __global__ void __launch_bounds__(1024) sytf2_pivot_kernel(int n, T *A, long lda
     if (threadIdx.x == 0) st[kStDone] = 1;
     return;
   }
-  const T absakk = cta_bcast(fabs(a(k, k)), &sb);
+  const R absakk = cta_bcast(Ops::mag(a(k, k)), &sb);
   int imax = 0;
-  T colmax = T(0);
+  R colmax = R(0);
   if (upper) {
     if (k > 0) {
-      imax = cta_iamax<T>(k, [&](int q) { return a(q, k); }, sv, si);
-      colmax = cta_bcast(fabs(a(imax, k)), &sb);
+      imax = cta_iamax<R>(k, [&](int q) { return Ops::mag(a(q, k)); }, sv, si);
+      colmax = cta_bcast(Ops::mag(a(imax, k)), &sb);
     }
   } else if (k < n - 1) {
-    imax = k + 1 + cta_iamax<T>(n - k - 1, [&](int q) { return a(k + 1 + q, k); }, sv, si);
-    colmax = cta_bcast(fabs(a(imax, k)), &sb);
+    imax = k + 1 + cta_iamax<R>(n - k - 1, [&](int q) { return Ops::mag(a(k + 1 + q, k)); }, sv, si);
+    colmax = cta_bcast(Ops::mag(a(imax, k)), &sb);
   }
   int kp = k, kstep = 1, skip = 0;
-  if (cmax(absakk, colmax) == T(0) || absakk != absakk) {
+  if (cmax(absakk, colmax) == R(0) || absakk != absakk) {
     skip = 1;
-  } else if (!(absakk >= Rn<T>::mul(alpha, colmax))) {
-    T rowmax;
+  } else if (!(absakk >= RO::mul(alpha, colmax))) {
+    R rowmax;
     if (upper) {
-      int jmax = imax + 1 + cta_iamax<T>(k - imax, [&](int q) { return a(imax, imax + 1 + q); }, sv, si);
-      rowmax = cta_bcast(fabs(a(imax, jmax)), &sb);
+      int jmax = imax + 1 +
+                 cta_iamax<R>(k - imax, [&](int q) { return Ops::mag(a(imax, imax + 1 + q)); }, sv, si);
+      rowmax = cta_bcast(Ops::mag(a(imax, jmax)), &sb);
       if (imax > 0) {
-        jmax = cta_iamax<T>(imax, [&](int q) { return a(q, imax); }, sv, si);
-        rowmax = cmax(rowmax, cta_bcast(fabs(a(jmax, imax)), &sb));
+        jmax = cta_iamax<R>(imax, [&](int q) { return Ops::mag(a(q, imax)); }, sv, si);
+        rowmax = cmax(rowmax, cta_bcast(Ops::mag(a(jmax, imax)), &sb));
       }
     } else {
-      int jmax = k + cta_iamax<T>(imax - k, [&](int q) { return a(imax, k + q); }, sv, si);
-      rowmax = cta_bcast(fabs(a(imax, jmax)), &sb);
+      int jmax = k + cta_iamax<R>(imax - k, [&](int q) { return Ops::mag(a(imax, k + q)); }, sv, si);
+      rowmax = cta_bcast(Ops::mag(a(imax, jmax)), &sb);
       if (imax < n - 1) {
-        jmax = imax + 1 + cta_iamax<T>(n - imax - 1, [&](int q) { return a(imax + 1 + q, imax); }, sv, si);
-        rowmax = cmax(rowmax, cta_bcast(fabs(a(jmax, imax)), &sb));
+        jmax = imax + 1 + cta_iamax<R>(n - imax - 1,
+                                       [&](int q) { return Ops::mag(a(imax + 1 + q, imax)); }, sv, si);
+        rowmax = cmax(rowmax, cta_bcast(Ops::mag(a(jmax, imax)), &sb));
       }
     }
-    const T absimax = cta_bcast(fabs(a(imax, imax)), &sb);
-    if (absakk >= Rn<T>::mul(alpha, Rn<T>::mul(colmax, Rn<T>::div(colmax, rowmax)))) {
+    const R absimax = cta_bcast(Ops::mag(a(imax, imax)), &sb);
+    if (absakk >= RO::mul(alpha, RO::mul(colmax, RO::div(colmax, rowmax)))) {
       kp = k;
-    } else if (absimax >= Rn<T>::mul(alpha, rowmax)) {
+    } else if (absimax >= RO::mul(alpha, rowmax)) {
       kp = imax;
     } else {
       kp = imax;
@@ -227,6 +284,7 @@ __global__ void __launch_bounds__(1024) sytf2_pivot_kernel(int n, T *A, long lda
 template <typename T>
 __global__ void __launch_bounds__(256) sytf2_update_kernel(int n, T *A, long lda, bool upper,
                                                            const int *st) {
+  using Ops = BkOps<T>;
   auto a = [&](int i, int j) -> T & { return A[i + (long)j * lda]; };
   if (st[kStDone] || st[kStSkip]) return;
   const int k = st[kStK], kstep = st[kStStep];
@@ -235,37 +293,37 @@ __global__ void __launch_bounds__(256) sytf2_update_kernel(int n, T *A, long lda
   const int o = upper ? 0 : k + kstep;
   const long tot = (long)m * m;
   if (kstep == 1) {
-    const T r1 = T(1) / a(k, k);
-    const T nr1 = -r1;
+    const T r1 = Ops::inv(a(k, k));
+    const T nr1 = Ops::neg(r1);
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < tot;
          e += (long)gridDim.x * blockDim.x) {
       const int i = o + (int)(e % m), j = o + (int)(e / m);
       if (upper ? i > j : i < j) continue;
       const T xj = a(j, k);
-      if (xj == T(0)) continue;
-      const T temp = Rn<T>::mul(xj, nr1);
-      a(i, j) = Rn<T>::add(a(i, j), Rn<T>::mul(a(i, k), temp));
+      if (Ops::is0(xj)) continue;
+      const T temp = Ops::mul(xj, nr1);
+      a(i, j) = Ops::add(a(i, j), Ops::mul(a(i, k), temp));
     }
   } else {
     const int k2 = upper ? k - 1 : k + 1;  // the block's other column
     T d = a(k2, k);  // d12 (upper) / d21 (lower)
-    const T dkk = Rn<T>::div(a(k2, k2), d);  // d22 (upper) / d11 (lower)
-    const T dk = Rn<T>::div(a(k, k), d);     // d11 (upper) / d22 (lower)
-    const T t = T(1) / Rn<T>::sub(Rn<T>::mul(upper ? dk : dkk, upper ? dkk : dk), T(1));
-    d = Rn<T>::div(t, d);
+    const T dkk = Ops::div(a(k2, k2), d);  // d22 (upper) / d11 (lower)
+    const T dk = Ops::div(a(k, k), d);     // d11 (upper) / d22 (lower)
+    const T t = Ops::inv(Ops::sub1(Ops::mul(upper ? dk : dkk, upper ? dkk : dk)));
+    d = Ops::div(t, d);
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < tot;
          e += (long)gridDim.x * blockDim.x) {
       const int i = o + (int)(e % m), j = o + (int)(e / m);
       if (upper ? i > j : i < j) continue;
       T wk, wo;  // the multipliers of columns k and k2 in column j
       if (upper) {  // wkm1 = d12 (d11 a_j,k-1 - a_jk), wk = d12 (d22 a_jk - a_j,k-1)
-        wo = Rn<T>::mul(d, Rn<T>::sub(Rn<T>::mul(dk, a(j, k2)), a(j, k)));
-        wk = Rn<T>::mul(d, Rn<T>::sub(Rn<T>::mul(dkk, a(j, k)), a(j, k2)));
+        wo = Ops::mul(d, Ops::sub(Ops::mul(dk, a(j, k2)), a(j, k)));
+        wk = Ops::mul(d, Ops::sub(Ops::mul(dkk, a(j, k)), a(j, k2)));
       } else {  // wk = d21 (d11 a_jk - a_j,k+1), wkp1 = d21 (d22 a_j,k+1 - a_jk)
-        wk = Rn<T>::mul(d, Rn<T>::sub(Rn<T>::mul(dkk, a(j, k)), a(j, k2)));
-        wo = Rn<T>::mul(d, Rn<T>::sub(Rn<T>::mul(dk, a(j, k2)), a(j, k)));
+        wk = Ops::mul(d, Ops::sub(Ops::mul(dkk, a(j, k)), a(j, k2)));
+        wo = Ops::mul(d, Ops::sub(Ops::mul(dk, a(j, k2)), a(j, k)));
       }
-      a(i, j) = Rn<T>::sub(a(i, j), Rn<T>::add(Rn<T>::mul(a(i, k), wk), Rn<T>::mul(a(i, k2), wo)));
+      a(i, j) = Ops::sub(a(i, j), Ops::add(Ops::mul(a(i, k), wk), Ops::mul(a(i, k2), wo)));
     }
   }
 }
@@ -274,6 +332,7 @@ __global__ void __launch_bounds__(256) sytf2_update_kernel(int n, T *A, long lda
 template <typename T>
 __global__ void __launch_bounds__(256) sytf2_store_kernel(int n, T *A, long lda, bool upper,
                                                           const int *st) {
+  using Ops = BkOps<T>;
   auto a = [&](int i, int j) -> T & { return A[i + (long)j * lda]; };
   if (st[kStDone] || st[kStSkip]) return;
   const int k = st[kStK], kstep = st[kStStep];
@@ -281,24 +340,25 @@ __global__ void __launch_bounds__(256) sytf2_store_kernel(int n, T *A, long lda,
   const int o = upper ? 0 : k + kstep;
   const int j0 = blockIdx.x * blockDim.x + threadIdx.x;
   if (kstep == 1) {
-    const T r1 = T(1) / a(k, k);
-    for (int j = j0; j < m; j += gridDim.x * blockDim.x) a(o + j, k) = Rn<T>::mul(a(o + j, k), r1);
+    const T r1 = Ops::inv(a(k, k));
+    if (Ops::is1(r1)) return;  // scal returns early for alpha == 1 (scal.zig)
+    for (int j = j0; j < m; j += gridDim.x * blockDim.x) a(o + j, k) = Ops::mul(a(o + j, k), r1);
     return;
   }
   const int k2 = upper ? k - 1 : k + 1;
   T d = a(k2, k);
-  const T dkk = Rn<T>::div(a(k2, k2), d), dk = Rn<T>::div(a(k, k), d);
-  const T t = T(1) / Rn<T>::sub(Rn<T>::mul(upper ? dk : dkk, upper ? dkk : dk), T(1));
-  d = Rn<T>::div(t, d);
+  const T dkk = Ops::div(a(k2, k2), d), dk = Ops::div(a(k, k), d);
+  const T t = Ops::inv(Ops::sub1(Ops::mul(upper ? dk : dkk, upper ? dkk : dk)));
+  d = Ops::div(t, d);
   for (int q = j0; q < m; q += gridDim.x * blockDim.x) {
     const int j = o + q;
     T wk, wo;
     if (upper) {
-      wo = Rn<T>::mul(d, Rn<T>::sub(Rn<T>::mul(dk, a(j, k2)), a(j, k)));
-      wk = Rn<T>::mul(d, Rn<T>::sub(Rn<T>::mul(dkk, a(j, k)), a(j, k2)));
+      wo = Ops::mul(d, Ops::sub(Ops::mul(dk, a(j, k2)), a(j, k)));
+      wk = Ops::mul(d, Ops::sub(Ops::mul(dkk, a(j, k)), a(j, k2)));
     } else {
-      wk = Rn<T>::mul(d, Rn<T>::sub(Rn<T>::mul(dkk, a(j, k)), a(j, k2)));
-      wo = Rn<T>::mul(d, Rn<T>::sub(Rn<T>::mul(dk, a(j, k2)), a(j, k)));
+      wk = Ops::mul(d, Ops::sub(Ops::mul(dkk, a(j, k)), a(j, k2)));
+      wo = Ops::mul(d, Ops::sub(Ops::mul(dk, a(j, k2)), a(j, k)));
     }
     a(j, k) = wk;
     a(j, k2) = wo;
@@ -317,7 +377,8 @@ int sytrf_dev(int uplo, int n, T *A, long lda, int *ipiv, int *info, cudaStream_
   DeviceInfo di;
   ZG_TRY(device_info(&di));
   const bool upper = uplo == kUpper;
-  const T alpha = (T(1) + std::sqrt(T(17))) / T(8);
+  using R = typename BkOps<T>::R;
+  const R alpha = (R(1) + std::sqrt(R(17))) / R(8);
   // the first step's column is n - 1 (upper) or 0 (lower)
   const int st0[4] = {upper ? n : -1, 1, 0, 0};
   ZG_CUDA(cudaMemcpyAsync(st, st0, sizeof st0, cudaMemcpyHostToDevice, s));
@@ -338,5 +399,7 @@ int sytrf_dev(int uplo, int n, T *A, long lda, int *ipiv, int *info, cudaStream_
 
 template int sytrf_dev<double>(int, int, double *, long, int *, int *, cudaStream_t);
 template int sytrf_dev<float>(int, int, float *, long, int *, int *, cudaStream_t);
+template int sytrf_dev<double2>(int, int, double2 *, long, int *, int *, cudaStream_t);
+template int sytrf_dev<float2>(int, int, float2 *, long, int *, int *, cudaStream_t);
 
 }  // namespace zg
