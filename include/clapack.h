@@ -110,6 +110,12 @@ int LAPACKE_cgeqrf(int matrix_layout, int m, int n, void *a, int lda, void *tau)
  * LAPACKE_dsytrf. */
 int LAPACKE_zsytrf(int matrix_layout, char uplo, int n, void *a, int lda, int *ipiv);
 int LAPACKE_csytrf(int matrix_layout, char uplo, int n, void *a, int lda, int *ipiv);
+/* Hermitian Bunch-Kaufman (lapack.zig:4556 LAPACKE_zhetrf and its cfloat
+ * twin; kernel lapack/hetrf.zig:17 with hetf2.zig): A = U D U^H or L D L^H,
+ * D Hermitian with real 1x1 blocks, the diagonal pivot magnitude |re a_kk|;
+ * ipiv and info as LAPACKE_dsytrf. */
+int LAPACKE_zhetrf(int matrix_layout, char uplo, int n, void *a, int lda, int *ipiv);
+int LAPACKE_chetrf(int matrix_layout, char uplo, int n, void *a, int lda, int *ipiv);
 
 /* replaces zml.linalg.lapack.geqrf (lapack.zig:5060; kernel lapack/geqrf.zig:18):
  * R in the upper triangle, the Householder vectors below it, tau[min(m,n)] */

@@ -186,3 +186,65 @@ def test_zsytrf_row_major_zero_column_and_lapack_solve():
         fr, ipr, infr = oracle_sytf2(z, ul)
         assert info == infr > 0
         np.testing.assert_array_equal(ipiv, ipr)
+
+
+def herm(n, seed, dtype=np.complex128):
+    rng = np.random.default_rng(seed)
+    g = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    return np.asfortranarray(((g + g.conj().T) / 2).astype(dtype))
+
+
+def gpu_zhetrf(a, uplo, layout=102):
+    n = a.shape[0]
+    buf = np.array(a, order="F" if layout == 102 else "C", copy=True)
+    ipiv = np.zeros(n, dtype=np.int32)
+    f = zg.lib().LAPACKE_zhetrf if a.dtype == np.complex128 else zg.lib().LAPACKE_chetrf
+    info = f(layout, uplo, n, P(buf), n, P(ipiv))
+    return np.asfortranarray(buf), ipiv, info
+
+
+def oracle_hetf2(a, ul):
+    f = np.asfortranarray(a.copy())
+    ipiv = np.zeros(a.shape[0], dtype=np.int32)
+    info = ol.fn("hetf2", a.dtype)(102, ul, a.shape[0], ol.ptr(f), max(1, a.shape[0]), ol.ptr(ipiv))
+    return f, ipiv, info
+
+
+@pytest.mark.parametrize("dtype,tol", [(np.complex128, 1e-12), (np.complex64, 2e-5)])
+@pytest.mark.parametrize("uplo", [b"U", b"L"])
+@pytest.mark.parametrize("n", [1, 2, 5, 64, 130, 257])
+def test_zhetrf_equals_oracle_hetf2(n, uplo, dtype, tol):
+    """Hermitian Bunch-Kaufman: the oracle's hetf2 pivots exactly and its
+    factors to rounding (the 2x2 step's |a_k',k| is a hypot from another
+    math library), a real diagonal, the other triangle untouched."""
+    a = herm(n, seed=5 * n + uplo[0], dtype=dtype)
+    f, ipiv, info = gpu_zhetrf(a, uplo)
+    ul = 121 if uplo == b"U" else 122
+    fr, ipr, infr = oracle_hetf2(a, ul)
+    assert info == infr == 0
+    np.testing.assert_array_equal(ipiv, ipr)
+    tri = np.triu if uplo == b"U" else np.tril
+    scale = np.abs(tri(fr)).max()
+    assert np.abs(tri(f) - tri(fr)).max() <= tol * scale
+    assert np.all(np.diag(f).imag == 0)
+    np.testing.assert_array_equal(f - tri(f), a - tri(a))
+
+
+def test_zhetrf_row_major_zero_column_and_lapack_solve():
+    a = herm(90, seed=12)
+    fc, pc, _ = gpu_zhetrf(a, b"U")
+    fr, pr, _ = gpu_zhetrf(a, b"U", layout=101)
+    np.testing.assert_array_equal(pr, pc)
+    np.testing.assert_array_equal(np.triu(fr), np.triu(fc))
+    x = np.random.default_rng(4).standard_normal((90, 2)) + 0j
+    sol, inf = lap.zhetrs(fc, pc, a @ x, lower=0)
+    assert inf == 0
+    np.testing.assert_allclose(sol, x, rtol=1e-9, atol=1e-9)
+    z = herm(30, seed=9)
+    z[7, :] = 0
+    z[:, 7] = 0
+    for uplo, ul in ((b"U", 121), (b"L", 122)):
+        _, ipiv, info = gpu_zhetrf(z, uplo)
+        _, ipr, infr = oracle_hetf2(z, ul)
+        assert info == infr > 0
+        np.testing.assert_array_equal(ipiv, ipr)

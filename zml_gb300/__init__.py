@@ -54,6 +54,7 @@ for p, R in (("z", f64), ("c", f32)):  # complex: scalars by pointer, herk's rea
         "LAPACKE_%sposv" % p: (i32, [i32, ch, i32, i32, vp, i32, vp, i32]),
         "LAPACKE_%sgeqrf" % p: (i32, [i32, i32, i32, vp, i32, vp]),
         "LAPACKE_%ssytrf" % p: (i32, [i32, ch, i32, vp, i32, vp]),
+        "LAPACKE_%shetrf" % p: (i32, [i32, ch, i32, vp, i32, vp]),
     })
 _SIGS.update({
     "zml_gpu_dgetrf": (i32, [i32, i32, vp, i32, vp, vp, vp]),

@@ -649,7 +649,8 @@ int zposv_any(int layout, char uplo, int n, int nrhs, R *a, int lda, R *b, int l
 // Bunch-Kaufman (LAPACKE_dsytrf / ssytrf, called from lapack.zig:4400-4409):
 // the uplo triangle of the symmetric n x n matrix is overwritten with the
 // block-diagonal D and the multipliers; ipiv as LAPACK's dsytrf.
-template <typename T> int sytrf_any(int layout, char uplo, int n, T *a, int lda, int *ipiv) {
+template <typename T, bool HERM = false>
+int sytrf_any(int layout, char uplo, int n, T *a, int lda, int *ipiv) {
   if (!lay_ok(layout)) return -1;
   uplo = up(uplo);
   if (uplo != 'U' && uplo != 'L') return -2;
@@ -662,7 +663,10 @@ template <typename T> int sytrf_any(int layout, char uplo, int n, T *a, int lda,
   ZG_TRY(A.in(layout, a, lda, n, n, kSlotA, kSlotAT, true, s));
   ZG_TRY(P.in(ipiv, n, kSlotPiv, false, s));
   int info = 0;
-  ZG_TRY(sytrf_dev<T>(uplo == 'U' ? kUpper : kLower, n, A.d, A.ld, P.d, &info, s));
+  if constexpr (HERM)
+    ZG_TRY(hetrf_dev<T>(uplo == 'U' ? kUpper : kLower, n, A.d, A.ld, P.d, &info, s));
+  else
+    ZG_TRY(sytrf_dev<T>(uplo == 'U' ? kUpper : kLower, n, A.d, A.ld, P.d, &info, s));
   ZG_TRY(A.out(s));
   ZG_TRY(P.out(s));
   ZG_TRY(sync(s));
@@ -872,6 +876,10 @@ CBLAS_ZGEMM(c, float)
   int LAPACKE_##P##sytrf(int layout, char uplo, int n, void *a, int lda, int *ipiv) {            \
     using C2 = typename Cx<R>::T;                                                                \
     return sytrf_any<C2>(layout, uplo, n, (C2 *)a, lda, ipiv);                                   \
+  }                                                                                              \
+  int LAPACKE_##P##hetrf(int layout, char uplo, int n, void *a, int lda, int *ipiv) {            \
+    using C2 = typename Cx<R>::T;                                                                \
+    return sytrf_any<C2, true>(layout, uplo, n, (C2 *)a, lda, ipiv);                             \
   }
 int LAPACKE_dsytrf(int layout, char uplo, int n, double *a, int lda, int *ipiv) {
   return sytrf_any<double>(layout, uplo, n, a, lda, ipiv);

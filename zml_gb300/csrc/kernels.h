@@ -58,6 +58,9 @@ int zpotrs_dev(int uplo, int n, int nrhs, const R *A, long lda, R *B, long ldb, 
 // sytrf.cu -- Bunch-Kaufman A = U D U^T / L D L^T (LAPACK ipiv and info).
 template <typename T>
 int sytrf_dev(int uplo, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s);
+// Hermitian Bunch-Kaufman (hetf2), complex T (double2 / float2)
+template <typename T>
+int hetrf_dev(int uplo, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s);
 
 // qr.cu -- Householder QR (geqrf) with the T factor of each panel.
 template <typename T> int geqrf_dev(int m, int n, T *A, long lda, T *tau, cudaStream_t s);

@@ -156,9 +156,10 @@ template <typename T> __device__ __forceinline__ T cta_bcast(T v, T *slot) {
   return *slot;
 }
 
-// Step k (sytf2.zig:30-296 upper, 297-515 lower): the column after the
-// previous step's block, pivot choice, interchange, ipiv, info.
-template <typename T>
+// Step k (sytf2.zig:30-296 upper, 297-515 lower; HERM: hetf2.zig, the
+// Hermitian form): the column after the previous step's block, pivot choice,
+// interchange, ipiv, info.
+template <typename T, bool HERM>
 __global__ void __launch_bounds__(1024) sytf2_pivot_kernel(int n, T *A, long lda, bool upper,
                                                            typename BkOps<T>::R alpha, int *ipiv,
                                                            int *st, int *info) {
@@ -176,7 +177,10 @@ __global__ void __launch_bounds__(1024) sytf2_pivot_kernel(int n, T *A, long lda
     if (threadIdx.x == 0) st[kStDone] = 1;
     return;
   }
-  const R absakk = cta_bcast(Ops::mag(a(k, k)), &sb);
+  R akk_mag;
+  if constexpr (HERM) akk_mag = fabs(a(k, k).x);  // the diagonal's real part
+  else akk_mag = Ops::mag(a(k, k));
+  const R absakk = cta_bcast(akk_mag, &sb);
   int imax = 0;
   R colmax = R(0);
   if (upper) {
@@ -224,6 +228,11 @@ __global__ void __launch_bounds__(1024) sytf2_pivot_kernel(int n, T *A, long lda
   __syncthreads();  // every thread has read what the decision needs
   if (!skip) {
     const int kk = upper ? k - kstep + 1 : k + kstep - 1;
+    // the entries that cross the diagonal are conjugated in the Hermitian form
+    auto cr = [](T x) -> T {
+      if constexpr (HERM) x.y = -x.y;
+      return x;
+    };
     if (kp != kk) {  // the interchange: disjoint pairs, all at once
       if (upper) {
         for (int i = t; i < kp; i += blockDim.x) {  // columns kk and kp above row kp
@@ -232,8 +241,8 @@ __global__ void __launch_bounds__(1024) sytf2_pivot_kernel(int n, T *A, long lda
           a(i, kp) = x;
         }
         for (int q = t; q < kk - kp - 1; q += blockDim.x) {  // column kk below kp <-> row kp
-          const T x = a(kp + 1 + q, kk);
-          a(kp + 1 + q, kk) = a(kp, kp + 1 + q);
+          const T x = cr(a(kp + 1 + q, kk));
+          a(kp + 1 + q, kk) = cr(a(kp, kp + 1 + q));
           a(kp, kp + 1 + q) = x;
         }
       } else {
@@ -243,20 +252,36 @@ __global__ void __launch_bounds__(1024) sytf2_pivot_kernel(int n, T *A, long lda
           a(kp + 1 + q, kp) = x;
         }
         for (int q = t; q < kp - kk - 1; q += blockDim.x) {  // column kk below kk <-> row kp
-          const T x = a(kk + 1 + q, kk);
-          a(kk + 1 + q, kk) = a(kp, kk + 1 + q);
+          const T x = cr(a(kk + 1 + q, kk));
+          a(kk + 1 + q, kk) = cr(a(kp, kk + 1 + q));
           a(kp, kk + 1 + q) = x;
         }
       }
       if (t == 0) {
-        T x = a(kk, kk);
-        a(kk, kk) = a(kp, kp);
-        a(kp, kp) = x;
+        if constexpr (HERM) {  // hetf2: a(kp, kk) conjugated, the diagonal kept real
+          a(kp, kk) = cr(a(kp, kk));
+          const R r1 = a(kk, kk).x;
+          a(kk, kk) = Ops::mk(a(kp, kp).x, R(0));
+          a(kp, kp) = Ops::mk(r1, R(0));
+          if (kstep == 2) a(k, k).y = R(0);
+        } else {
+          T x = a(kk, kk);
+          a(kk, kk) = a(kp, kp);
+          a(kp, kp) = x;
+        }
         if (kstep == 2) {
           const int r = upper ? k - 1 : k + 1;
-          x = a(r, k);
+          const T x = a(r, k);
           a(r, k) = a(kp, k);
           a(kp, k) = x;
+        }
+      }
+    } else if constexpr (HERM) {
+      if (t == 0) {  // the block's diagonal made real
+        a(k, k).y = R(0);
+        if (kstep == 2) {
+          const int r = upper ? k - 1 : k + 1;
+          a(r, r).y = R(0);
         }
       }
     }
@@ -280,11 +305,54 @@ __global__ void __launch_bounds__(1024) sytf2_pivot_kernel(int n, T *A, long lda
 // column j skipped where x_j == 0 (syr.zig:62, 142).  2x2 (185-236 /
 // 430-482): the multipliers of column j from the original columns k, k-1
 // (upper) or k, k+1 (lower), then a_ij -= a_ik wk + a_ik' wk'.  The columns
-// of the block are rewritten afterwards by sytf2_store_kernel.
+// of the block are rewritten afterwards by sytf2_store_kernel.  HERM
+// (hetf2.zig): her with the real alpha -1/re(d), a_ij += x_i (conj(x_j)
+// alpha), the diagonal kept real; 2x2 with d = |a_k',k| and conjugated
+// multipliers, a_ij -= a_ik conj(wk) + a_ik' conj(wk').
+template <typename T> struct HermScalars {
+  typename BkOps<T>::R d, dk, dother;
+  T dd;
+};
+// hetf2's 2x2 block scalars: d = |a(k2, k)|, dk = re a(k, k) / d, dother =
+// re a(k2, k2) / d, dd = a(k2, k) / d, then d <- (1 / (dk dother - 1)) / d
 template <typename T>
+__device__ __forceinline__ HermScalars<T> herm_scalars(const T &akk, const T &a2k, const T &a22) {
+  using R = typename BkOps<T>::R;
+  using RO = BkOps<R>;
+  HermScalars<T> h;
+  R d = hypot(a2k.x, a2k.y);
+  h.dother = RO::div(a22.x, d);
+  h.dk = RO::div(akk.x, d);
+  const R t = R(1) / RO::sub(RO::mul(h.dk, h.dother), R(1));
+  h.dd = BkOps<T>::mk(RO::div(a2k.x, d), RO::div(a2k.y, d));
+  h.d = RO::div(t, d);
+  return h;
+}
+template <typename T>
+__device__ __forceinline__ T cscale(const T &z, typename BkOps<T>::R s) {
+  using RO = BkOps<typename BkOps<T>::R>;
+  return BkOps<T>::mk(RO::mul(z.x, s), RO::mul(z.y, s));
+}
+template <typename T> __device__ __forceinline__ T cconj(T z) {
+  z.y = -z.y;
+  return z;
+}
+// wk (the multiplier of column k) and wo (of the block's other column) in
+// column j of the Hermitian 2x2 step: wk = d (dother a_jk - dd a_jo),
+// wo = d (dk a_jo - conj(dd) a_jk), in both triangles (hetf2.zig)
+template <typename T>
+__device__ __forceinline__ void herm_mult(const HermScalars<T> &h, const T &ajk, const T &ajo, T &wk,
+                                          T &wo) {
+  using Ops = BkOps<T>;
+  wk = cscale(Ops::sub(cscale(ajk, h.dother), Ops::mul(h.dd, ajo)), h.d);
+  wo = cscale(Ops::sub(cscale(ajo, h.dk), Ops::mul(cconj(h.dd), ajk)), h.d);
+}
+
+template <typename T, bool HERM>
 __global__ void __launch_bounds__(256) sytf2_update_kernel(int n, T *A, long lda, bool upper,
                                                            const int *st) {
   using Ops = BkOps<T>;
+  using R = typename Ops::R;
   auto a = [&](int i, int j) -> T & { return A[i + (long)j * lda]; };
   if (st[kStDone] || st[kStSkip]) return;
   const int k = st[kStK], kstep = st[kStStep];
@@ -293,46 +361,79 @@ __global__ void __launch_bounds__(256) sytf2_update_kernel(int n, T *A, long lda
   const int o = upper ? 0 : k + kstep;
   const long tot = (long)m * m;
   if (kstep == 1) {
-    const T r1 = Ops::inv(a(k, k));
-    const T nr1 = Ops::neg(r1);
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < tot;
-         e += (long)gridDim.x * blockDim.x) {
-      const int i = o + (int)(e % m), j = o + (int)(e / m);
-      if (upper ? i > j : i < j) continue;
-      const T xj = a(j, k);
-      if (Ops::is0(xj)) continue;
-      const T temp = Ops::mul(xj, nr1);
-      a(i, j) = Ops::add(a(i, j), Ops::mul(a(i, k), temp));
+    if constexpr (HERM) {
+      const R alpha = -(R(1) / a(k, k).x);
+      for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < tot;
+           e += (long)gridDim.x * blockDim.x) {
+        const int i = o + (int)(e % m), j = o + (int)(e / m);
+        if (upper ? i > j : i < j) continue;
+        const T xj = a(j, k);
+        if (Ops::is0(xj)) {
+          if (i == j) a(j, j).y = R(0);
+          continue;
+        }
+        const T temp = cscale(cconj(xj), alpha);
+        if (i == j) a(j, j) = Ops::mk(BkOps<R>::add(a(j, j).x, Ops::mul(xj, temp).x), R(0));
+        else a(i, j) = Ops::add(a(i, j), Ops::mul(a(i, k), temp));
+      }
+    } else {
+      const T r1 = Ops::inv(a(k, k));
+      const T nr1 = Ops::neg(r1);
+      for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < tot;
+           e += (long)gridDim.x * blockDim.x) {
+        const int i = o + (int)(e % m), j = o + (int)(e / m);
+        if (upper ? i > j : i < j) continue;
+        const T xj = a(j, k);
+        if (Ops::is0(xj)) continue;
+        const T temp = Ops::mul(xj, nr1);
+        a(i, j) = Ops::add(a(i, j), Ops::mul(a(i, k), temp));
+      }
     }
   } else {
     const int k2 = upper ? k - 1 : k + 1;  // the block's other column
-    T d = a(k2, k);  // d12 (upper) / d21 (lower)
-    const T dkk = Ops::div(a(k2, k2), d);  // d22 (upper) / d11 (lower)
-    const T dk = Ops::div(a(k, k), d);     // d11 (upper) / d22 (lower)
-    const T t = Ops::inv(Ops::sub1(Ops::mul(upper ? dk : dkk, upper ? dkk : dk)));
-    d = Ops::div(t, d);
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < tot;
-         e += (long)gridDim.x * blockDim.x) {
-      const int i = o + (int)(e % m), j = o + (int)(e / m);
-      if (upper ? i > j : i < j) continue;
-      T wk, wo;  // the multipliers of columns k and k2 in column j
-      if (upper) {  // wkm1 = d12 (d11 a_j,k-1 - a_jk), wk = d12 (d22 a_jk - a_j,k-1)
-        wo = Ops::mul(d, Ops::sub(Ops::mul(dk, a(j, k2)), a(j, k)));
-        wk = Ops::mul(d, Ops::sub(Ops::mul(dkk, a(j, k)), a(j, k2)));
-      } else {  // wk = d21 (d11 a_jk - a_j,k+1), wkp1 = d21 (d22 a_j,k+1 - a_jk)
-        wk = Ops::mul(d, Ops::sub(Ops::mul(dkk, a(j, k)), a(j, k2)));
-        wo = Ops::mul(d, Ops::sub(Ops::mul(dk, a(j, k2)), a(j, k)));
+    if constexpr (HERM) {
+      const HermScalars<T> h = herm_scalars(a(k, k), a(k2, k), a(k2, k2));
+      for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < tot;
+           e += (long)gridDim.x * blockDim.x) {
+        const int i = o + (int)(e % m), j = o + (int)(e / m);
+        if (upper ? i > j : i < j) continue;
+        T wk, wo;
+        herm_mult(h, a(j, k), a(j, k2), wk, wo);
+        T v = Ops::sub(a(i, j),
+                       Ops::add(Ops::mul(a(i, k), cconj(wk)), Ops::mul(a(i, k2), cconj(wo))));
+        if (i == j) v.y = R(0);
+        a(i, j) = v;
       }
-      a(i, j) = Ops::sub(a(i, j), Ops::add(Ops::mul(a(i, k), wk), Ops::mul(a(i, k2), wo)));
+    } else {
+      T d = a(k2, k);  // d12 (upper) / d21 (lower)
+      const T dkk = Ops::div(a(k2, k2), d);  // d22 (upper) / d11 (lower)
+      const T dk = Ops::div(a(k, k), d);     // d11 (upper) / d22 (lower)
+      const T t = Ops::inv(Ops::sub1(Ops::mul(upper ? dk : dkk, upper ? dkk : dk)));
+      d = Ops::div(t, d);
+      for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < tot;
+           e += (long)gridDim.x * blockDim.x) {
+        const int i = o + (int)(e % m), j = o + (int)(e / m);
+        if (upper ? i > j : i < j) continue;
+        T wk, wo;  // the multipliers of columns k and k2 in column j
+        if (upper) {  // wkm1 = d12 (d11 a_j,k-1 - a_jk), wk = d12 (d22 a_jk - a_j,k-1)
+          wo = Ops::mul(d, Ops::sub(Ops::mul(dk, a(j, k2)), a(j, k)));
+          wk = Ops::mul(d, Ops::sub(Ops::mul(dkk, a(j, k)), a(j, k2)));
+        } else {  // wk = d21 (d11 a_jk - a_j,k+1), wkp1 = d21 (d22 a_j,k+1 - a_jk)
+          wk = Ops::mul(d, Ops::sub(Ops::mul(dkk, a(j, k)), a(j, k2)));
+          wo = Ops::mul(d, Ops::sub(Ops::mul(dk, a(j, k2)), a(j, k)));
+        }
+        a(i, j) = Ops::sub(a(i, j), Ops::add(Ops::mul(a(i, k), wk), Ops::mul(a(i, k2), wo)));
+      }
     }
   }
 }
 
 // The block's columns after the update: x / d (1x1) or the multipliers (2x2).
-template <typename T>
+template <typename T, bool HERM>
 __global__ void __launch_bounds__(256) sytf2_store_kernel(int n, T *A, long lda, bool upper,
                                                           const int *st) {
   using Ops = BkOps<T>;
+  using R = typename Ops::R;
   auto a = [&](int i, int j) -> T & { return A[i + (long)j * lda]; };
   if (st[kStDone] || st[kStSkip]) return;
   const int k = st[kStK], kstep = st[kStStep];
@@ -340,12 +441,28 @@ __global__ void __launch_bounds__(256) sytf2_store_kernel(int n, T *A, long lda,
   const int o = upper ? 0 : k + kstep;
   const int j0 = blockIdx.x * blockDim.x + threadIdx.x;
   if (kstep == 1) {
-    const T r1 = Ops::inv(a(k, k));
-    if (Ops::is1(r1)) return;  // scal returns early for alpha == 1 (scal.zig)
-    for (int j = j0; j < m; j += gridDim.x * blockDim.x) a(o + j, k) = Ops::mul(a(o + j, k), r1);
+    if constexpr (HERM) {  // x scaled by the real 1 / re(d), no early return
+      const R r1 = R(1) / a(k, k).x;
+      for (int j = j0; j < m; j += gridDim.x * blockDim.x) a(o + j, k) = cscale(a(o + j, k), r1);
+    } else {
+      const T r1 = Ops::inv(a(k, k));
+      if (Ops::is1(r1)) return;  // scal returns early for alpha == 1 (scal.zig)
+      for (int j = j0; j < m; j += gridDim.x * blockDim.x) a(o + j, k) = Ops::mul(a(o + j, k), r1);
+    }
     return;
   }
   const int k2 = upper ? k - 1 : k + 1;
+  if constexpr (HERM) {
+    const HermScalars<T> h = herm_scalars(a(k, k), a(k2, k), a(k2, k2));
+    for (int q = j0; q < m; q += gridDim.x * blockDim.x) {
+      const int j = o + q;
+      T wk, wo;
+      herm_mult(h, a(j, k), a(j, k2), wk, wo);
+      a(j, k) = wk;
+      a(j, k2) = wo;
+    }
+    return;
+  }
   T d = a(k2, k);
   const T dkk = Ops::div(a(k2, k2), d), dk = Ops::div(a(k, k), d);
   const T t = Ops::inv(Ops::sub1(Ops::mul(upper ? dk : dkk, upper ? dkk : dk)));
@@ -365,8 +482,8 @@ __global__ void __launch_bounds__(256) sytf2_store_kernel(int n, T *A, long lda,
   }
 }
 
-template <typename T>
-int sytrf_dev(int uplo, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s) {
+template <typename T, bool HERM>
+static int bk_dev(int uplo, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s) {
   *info = 0;
   if (n <= 0) return 0;
   Control *ctl;
@@ -387,19 +504,30 @@ int sytrf_dev(int uplo, int n, T *A, long lda, int *ipiv, int *info, cudaStream_
   // at most n steps (one per column when every block is 1x1)
   for (int it = 0; it < n; ++it) {
     ZG_LAUNCH(kTagPanel, 0, 0, s,
-              (sytf2_pivot_kernel<T><<<1, 1024, 0, s>>>(n, A, lda, upper, alpha, ipiv, st,
+              (sytf2_pivot_kernel<T, HERM><<<1, 1024, 0, s>>>(n, A, lda, upper, alpha, ipiv, st,
                                                         &ctl->info)));
     ZG_LAUNCH(kTagPotf2, 0, 0, s,
-              (sytf2_update_kernel<T><<<grid, 256, 0, s>>>(n, A, lda, upper, st)));
+              (sytf2_update_kernel<T, HERM><<<grid, 256, 0, s>>>(n, A, lda, upper, st)));
     ZG_LAUNCH(kTagPotf2, 0, 0, s,
-              (sytf2_store_kernel<T><<<ceil_div(n, 256), 256, 0, s>>>(n, A, lda, upper, st)));
+              (sytf2_store_kernel<T, HERM><<<ceil_div(n, 256), 256, 0, s>>>(n, A, lda, upper, st)));
   }
   return check_status(s, ctl, info);
+}
+
+template <typename T>
+int sytrf_dev(int uplo, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s) {
+  return bk_dev<T, false>(uplo, n, A, lda, ipiv, info, s);
+}
+template <typename T>
+int hetrf_dev(int uplo, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s) {
+  return bk_dev<T, true>(uplo, n, A, lda, ipiv, info, s);
 }
 
 template int sytrf_dev<double>(int, int, double *, long, int *, int *, cudaStream_t);
 template int sytrf_dev<float>(int, int, float *, long, int *, int *, cudaStream_t);
 template int sytrf_dev<double2>(int, int, double2 *, long, int *, int *, cudaStream_t);
 template int sytrf_dev<float2>(int, int, float2 *, long, int *, int *, cudaStream_t);
+template int hetrf_dev<double2>(int, int, double2 *, long, int *, int *, cudaStream_t);
+template int hetrf_dev<float2>(int, int, float2 *, long, int *, int *, cudaStream_t);
 
 }  // namespace zg
