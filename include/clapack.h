@@ -152,8 +152,8 @@ int zml_gpu_dgetrf(int m, int n, double *dA, int ldda, int *dipiv, int *info, vo
  * zml_gpu_dgetrf's default tensor-core updates agree with it to rounding.  Its
  * scratch is one static device array of about 273 KB that every GPU loading
  * the library holds until exit; the first
- * call on a device resolves that array's address (make it before any stream
- * capture).  Every call shares the array: calls that overlap on the GPU race.
+ * call on a device resolves that array's address, once, under a lock.  Every
+ * call shares the array: calls that overlap on the GPU race.
  * Limit: m at most what one 64-column panel holds in shared memory (about 446
  * rows per SM), on devices of at most 256 SMs; larger sizes return
  * ZML_GPU_ERR_INVALID with a message in zml_gpu_last_error(). */
