@@ -582,6 +582,9 @@ __global__ void gemv_partial_kernel(int n, int ncols, const double *__restrict__
   double acc0 = 0, acc1 = 0;
   const double *a = A + i + (long)c0 * lda;
   int c = c0;
+  // unrolled so that several columns' loads are in flight per thread (the
+  // two accumulators keep their summation order)
+#pragma unroll 8
   for (; c + 1 < c1; c += 2, a += 2 * lda) {
     acc0 = fma(a[0], xs[c - c0], acc0);
     acc1 = fma(a[lda], xs[c + 1 - c0], acc1);
