@@ -230,3 +230,22 @@ def test_condition_estimate_feature_tracks_kappa(torch, sel):
         est.append(float(np.frombuffer(r.features, dtype=np.float32)[14]))
     assert est[0] < est[1] < est[2], est
     assert 0.5 <= est[0] <= 1.0 + np.log10(n), est
+
+
+def test_shipped_model_guides_heldout_solves(torch, sel):
+    """The network shipped with the package (trained on 50000 matrices up to
+    n = 2048) on held-out seeds: every solve converges, and where the probe
+    did not settle the matrix the network's class is used."""
+    dev = torch.device("cuda", 0)
+    model = sel.trained_model()
+    specs = sel.sample_specs(40, seed=2, nmax=512)
+    consulted = 0
+    for kind, n, kappa, seed in specs:
+        t, m = sel.generate(torch, kind, n, kappa, seed, dev)
+        b = sel.rhs(torch, m, seed)
+        r = sel.solve_auto(torch, t, b, torch.zeros_like(b), n, model)
+        assert r.converged
+        if r.predicted >= 0:
+            consulted += 1
+            assert r.used >= r.predicted
+    assert consulted >= 5

@@ -285,6 +285,15 @@ def train(torch, X, y, dev, epochs=300, batch=256, lr=3e-3, weight_decay=1e-5, s
     return state(epochs)
 
 
+def trained_model():
+    """The network trained at the selector workload's scale (50000 matrices,
+    n log-uniform in [64, 2048], 300 epochs), as the flat array
+    zml_gpu_dgesv_auto takes: parameters, feature means, feature scales."""
+    path = os.path.join(os.path.dirname(__file__), "data", "selector_model.npz")
+    with np.load(path) as d:
+        return model_array({"params": d["params"], "mu": d["mu"], "sd": d["sd"]})
+
+
 def model_array(state):
     """The flat model zml_gpu_dgesv_auto takes: parameters, means, scales."""
     a = np.concatenate([np.asarray(state["params"], np.float32), np.asarray(state["mu"], np.float32),
