@@ -101,6 +101,10 @@ int panel_lu(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *c
 int panel_lu_cluster(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base, Control *ctl,
                      int info_base, cudaStream_t s, bool *launched, float *XL = nullptr,
                      int xl = 0, float *XR = nullptr, int xr = 0, bool tournament = false);
+// The same for an FP64 panel (partial pivoting only).
+int panel_lu_cluster(int m, int nb, double *A, long lda, int *ipiv, int ipiv_base, Control *ctl,
+                     int info_base, cudaStream_t s, bool *launched, double *XL = nullptr,
+                     int xl = 0, double *XR = nullptr, int xr = 0);
 // tournament: FP32 panels by tournament pivoting (see panel_lu_cluster).
 // FP64 from n = 2048 up: getrf_oz (tensor-core updates), else getrf_simt.
 template <typename T>

@@ -412,12 +412,13 @@ template <typename T> static int lu_block() { return sizeof(T) == 8 ? 64 : 128; 
 template <typename T>
 static int panel_any(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *ctl,
                      int info_base, cudaStream_t s, bool tournament) {
-  if constexpr (sizeof(T) == sizeof(float)) {
-    bool done = false;
+  bool done = false;
+  if constexpr (sizeof(T) == sizeof(float))
     ZG_TRY(panel_lu_cluster(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, &done, nullptr, 0,
                             nullptr, 0, tournament));
-    if (done) return 0;
-  }
+  else
+    ZG_TRY(panel_lu_cluster(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, &done));
+  if (done) return 0;
   return panel_lu<T>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s);
 }
 

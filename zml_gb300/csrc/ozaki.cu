@@ -301,9 +301,15 @@ int getrf_oz(int m, int n, double *A, long lda, int *ipiv, int *info, cudaStream
     for (int p = 0; p < jb; p += NBP) {
       const int r = j + p, pb = std::min(NBP, jb - p), right = jb - p - pb;
       double *Arr = A + r + (long)r * lda;
-      ZG_TRY(panel_lu<double>(m - r, pb, Arr, lda, ipiv + r, r, ctl, r, s));
-      // the half-panel's interchanges in the block's other columns
-      ZG_TRY(laswp_panel<double>(p, p + pb, jb, Ab, lda, r + 1, r + pb, ipiv, s));
+      // the half-panel on one thread-block cluster, its interchanges applied
+      // to the block's other columns inside it; else the cooperative panel
+      bool done = false;
+      ZG_TRY(panel_lu_cluster(m - r, pb, Arr, lda, ipiv + r, r, ctl, r, s, &done, Ab + r, p,
+                              Arr + (long)pb * lda, right));
+      if (!done) {
+        ZG_TRY(panel_lu<double>(m - r, pb, Arr, lda, ipiv + r, r, ctl, r, s));
+        ZG_TRY(laswp_panel<double>(p, p + pb, jb, Ab, lda, r + 1, r + pb, ipiv, s));
+      }
       if (right > 0) {
         double *Ar = Arr + (long)pb * lda;  // rows r.., the block's columns right of the half
         ZG_TRY(trsm_dev<double>(kLeft, kLower, kNoTrans, kUnit, pb, right, 1.0, Arr, lda, Ar, lda,

@@ -48,7 +48,7 @@ constexpr int kPcThreads = 512;
 constexpr int kPcMaxCta = 16;
 constexpr int kPcMaxNb = 128;
 constexpr int kPcSlot = 64;          // row values; entries W..63 stay zero
-constexpr int kPcMaxRight = kPcMaxNb - 16;
+constexpr int kPcMaxRight = kPcMaxNb - 8;  // right of the first sub-panel (W >= 8)
 constexpr int kPcUStride = 36;       // U12 tile row stride (16-byte aligned rows)
 
 __device__ __forceinline__ unsigned cl_rank() {
@@ -82,6 +82,60 @@ __device__ __forceinline__ void st_async(unsigned addr, unsigned long long v, un
                    addr),
                "l"(v), "r"(mbar)
                : "memory");
+}
+
+__device__ __forceinline__ void st_async(unsigned addr, double v, unsigned mbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(
+                   addr),
+               "l"(__double_as_longlong(v)), "r"(mbar)
+               : "memory");
+}
+__device__ __forceinline__ void st_async(unsigned addr, int v, unsigned mbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(
+                   addr),
+               "r"(v), "r"(mbar)
+               : "memory");
+}
+__device__ __forceinline__ float fmae(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fmae(double a, double b, double c) { return fma(a, b, c); }
+// four consecutive elements of a 16-byte aligned shared-memory row
+__device__ __forceinline__ void load4(const float *p, float &a, float &b, float &c, float &d) {
+  const float4 q = *reinterpret_cast<const float4 *>(p);
+  a = q.x;
+  b = q.y;
+  c = q.z;
+  d = q.w;
+}
+__device__ __forceinline__ void load4(const double *p, double &a, double &b, double &c,
+                                      double &d) {
+  const double2 q0 = reinterpret_cast<const double2 *>(p)[0];
+  const double2 q1 = reinterpret_cast<const double2 *>(p)[1];
+  a = q0.x;
+  b = q0.y;
+  c = q1.x;
+  d = q1.y;
+}
+
+// binary64 candidate key of row `row` with value v for pivot column k: the
+// bits of |v| + 1 (positive doubles order as integers), a NaN counting as
+// +inf on the diagonal and as "no candidate" (0) below it.  Ties of the key
+// go to the lower row, so (key, row) orders exactly as the restatement's
+// first-maximum search.
+__device__ __forceinline__ unsigned long long pd_key(double v, int row, int k) {
+  double key = fabs(v);
+  if (v != v) key = row == k ? INFINITY : -INFINITY;
+  return key == -INFINITY ? 0ull : (unsigned long long)__double_as_longlong(key) + 1ull;
+}
+// The warp's largest (key, row): the largest key, then the lowest row among
+// the lanes that hold it; every lane receives it.
+__device__ __forceinline__ void warp_lexmax(unsigned long long &key, int &row) {
+  const unsigned hi = (unsigned)(key >> 32), lo = (unsigned)key;
+  const unsigned mh = __reduce_max_sync(~0u, hi);
+  const unsigned ml = __reduce_max_sync(~0u, hi == mh ? lo : 0u);
+  const unsigned long long mk = ((unsigned long long)mh << 32) | ml;
+  const int r = (int)__reduce_min_sync(~0u, key == mk ? (unsigned)row : 0xffffffffu);
+  key = mk;
+  row = r;
 }
 
 // Candidate word of row `row` with value v for pivot column k: a NaN counts
@@ -119,31 +173,41 @@ __device__ __forceinline__ int pc_row(unsigned long long w) {
 // k + 2, by which time every thread here is done with column k's rows.
 constexpr int kPcBuf = 3;
 
-struct __align__(16) PcShared {
+template <typename E> struct __align__(16) PcShared {
   // Exchanged rows at column kk, 64 words: [c] = column kk + 1 + c (zero
   // past the register window), [32] = column kk, [33 + c] = finished column
   // c < kk.
-  float slot[kPcBuf][kPcMaxCta][kPcSlot];  // candidate rows pushed by every CTA
-  float rowk[kPcBuf][kPcSlot];             // row k before the interchange, pushed by CTA 0
-  float cand[33];                          // this CTA's winning row (register part), staged
-  float krow[33];                          // row k (register part), staged by its owner
+  E slot[kPcBuf][kPcMaxCta][kPcSlot];      // candidate rows pushed by every CTA
+  E rowk[kPcBuf][kPcSlot];                 // row k before the interchange, pushed by CTA 0
+  E cand[33];                              // this CTA's winning row (register part), staged
+  E krow[33];                              // row k (register part), staged by its owner
   unsigned long long cmax[2];              // this CTA's best candidate word (atomicMax)
   unsigned long long skey[kPcBuf][kPcMaxCta];  // every CTA's best word, pushed by that CTA
+  // binary64: each warp's best (key, row) and every CTA's best row beside its key
+  unsigned long long wkey[2][kPcThreads / 32];
+  int wrow[2][kPcThreads / 32];
+  int srow[kPcBuf][kPcMaxCta];
   uint64_t mbar[kPcBuf];                   // completes when a column's pushes have all landed
   int piv[32];                             // pivot rows of the sub-panel (panel-relative)
   int mdst[64], msrc[64];                  // the sub-panel's interchanges, composed
-  float L11[32][33];                       // unit-lower diagonal block of the sub-panel
+  E L11[32][33];                           // unit-lower diagonal block of the sub-panel
   // tournament pivoting (TOURN): the CTA's local candidates, the cluster's
   // pivot rows in order, U11 of the sub-panel and 1 / its diagonal, the
   // argmax words of the final elimination and the exchange's mbarrier
   int lcand[32];
   int fpiv[32];
-  float U11[32][33];
-  float rdiag[32];
+  E U11[32][33];
+  E rdiag[32];
   unsigned long long fmax[2];
   uint64_t tmbar;
-  alignas(16) float U[kPcMaxRight][kPcUStride];  // U12 by right column: U[c][k]
+  alignas(16) E U[kPcMaxRight][kPcUStride];  // U12 by right column: U[c][k]
 };
+
+// Bytes of the exchange state at the start of the dynamic shared memory
+// (16-byte aligned, so the finished columns after it are too).
+template <typename E> __host__ __device__ constexpr int pc_state_bytes() {
+  return (int)((sizeof(PcShared<E>) + 15) / 16 * 16);
+}
 
 // Row whose old content ends in row x after the swaps (c0 + t, piv[t]), t < ws.
 __device__ __forceinline__ int pc_trace(int x, int c0, int ws, const int *piv) {
@@ -155,24 +219,27 @@ __device__ __forceinline__ int pc_trace(int x, int c0, int ws, const int *piv) {
   return x;
 }
 
-template <int RPT, int W, bool TOURN>
+template <typename E, int RPT, int W, bool TOURN>
 __global__ void __launch_bounds__(kPcThreads, 1)
-    panel_cluster_kernel(int m, int nb, float *__restrict__ A, long lda, int *__restrict__ ipiv,
-                         int ipiv_base, Control *ctl, int info_base, float *XL, int xl,
-                         float *XR, int xr) {
-  static_assert(W <= 32 && W % 4 == 0 && RPT * W <= 64, "sub-panel shape");
-  __shared__ PcShared sh;
-  extern __shared__ __align__(16) float Lsm[];  // finished columns: Lsm[c LD + local row]
+    panel_cluster_kernel(int m, int nb, E *__restrict__ A, long lda, int *__restrict__ ipiv,
+                         int ipiv_base, Control *ctl, int info_base, E *XL, int xl, E *XR,
+                         int xr) {
+  static_assert(W >= 8 && W <= 32 && W % 4 == 0 && RPT * W <= 64, "sub-panel shape");
+  // the exchange state, then the finished columns: Lsm[c LD + local row]
+  extern __shared__ __align__(16) unsigned char pc_smem[];
+  PcShared<E> &sh = *reinterpret_cast<PcShared<E> *>(pc_smem);
+  E *Lsm = reinterpret_cast<E *>(pc_smem + pc_state_bytes<E>());
   const int rank = (int)cl_rank(), nct = (int)cl_size();
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int T = blockDim.x, nwarps = T >> 5, R = T * RPT;
   const int LD = R + 1;  // Lsm column stride, odd: a row's finished columns hit distinct banks
   const int r0 = rank * R;
-  float v[RPT][W];
-  for (int e = tid; e < kPcBuf * kPcMaxCta * kPcSlot; e += T) (&sh.slot[0][0][0])[e] = 0.f;
+  E v[RPT][W];
+  constexpr bool kF64 = sizeof(E) == 8;
+  for (int e = tid; e < kPcBuf * kPcMaxCta * kPcSlot; e += T) (&sh.slot[0][0][0])[e] = E(0);
   // bytes landing in this CTA per column: every CTA's candidate row (two
-  // words a lane) and word, and row k from CTA 0
-  const unsigned xbytes = nct * (2 * 32 * 4 + 8) + 2 * 32 * 4;
+  // values a lane) and word (binary64: key and row), and row k from CTA 0
+  const unsigned xbytes = nct * (2 * 32 * sizeof(E) + 8 + (kF64 ? 4 : 0)) + 2 * 32 * sizeof(E);
   // tournament: every CTA's W candidate rows (W values and the row) and, from
   // CTA 0, the sub-panel's W top rows land in this CTA's Lsm once per sub-panel
   const unsigned tbytes = (unsigned)(nct * W * (W + 1) + W * W) * 4u;
@@ -200,7 +267,7 @@ __global__ void __launch_bounds__(kPcThreads, 1)
       const int row = r0 + tid + i * T;
 #pragma unroll
       for (int c = 0; c < W; ++c)
-        v[i][c] = (row < m && c < ws) ? __ldcg(A + row + (long)(c0 + c) * lda) : 0.f;
+        v[i][c] = (row < m && c < ws) ? __ldcg(A + row + (long)(c0 + c) * lda) : E(0);
     }
 
     if constexpr (TOURN) {
@@ -419,30 +486,61 @@ __global__ void __launch_bounds__(kPcThreads, 1)
   #pragma unroll 1
       for (int kk = 0; kk < ws; ++kk) {
         const int k = c0 + kk, par = k & 1, b = k % kPcBuf;
-        unsigned long long best = 0;
+        unsigned long long cbest;  // the CTA's candidate word (binary64: its key)
+        int wrow;                  // its row, -1 when the CTA has none
+        if constexpr (!kF64) {
+          unsigned long long best = 0;
   #pragma unroll
-        for (int i = 0; i < RPT; ++i) {
-          const int row = r0 + tid + i * T;
-          if (row >= k && row < m) best = max(best, pc_word(v[i][0], row, k));
+          for (int i = 0; i < RPT; ++i) {
+            const int row = r0 + tid + i * T;
+            if (row >= k && row < m) best = max(best, pc_word(v[i][0], row, k));
+          }
+          best = warp_max64(best);
+          if (lane == 0 && best != 0) atomicMax(&sh.cmax[par], best);
+          __syncthreads();
+          // every thread has read the previous column's word: clear it for the next
+          if (tid == 0) sh.cmax[par ^ 1] = 0;
+          cbest = sh.cmax[par];
+          wrow = cbest != 0 ? pc_row(cbest) : -1;
+        } else {
+          // binary64 keys need the whole 64 bits: (key, row) pairs reduced
+          // per warp, then over the CTA's warps (by every warp alike)
+          unsigned long long key = 0;
+          int krow_ = 0x7fffffff;
+  #pragma unroll
+          for (int i = 0; i < RPT; ++i) {
+            const int row = r0 + tid + i * T;
+            if (row >= k && row < m) {
+              const unsigned long long w = pd_key(v[i][0], row, k);
+              if (w > key) {  // rows of a thread ascend: the first maximum stays
+                key = w;
+                krow_ = row;
+              }
+            }
+          }
+          warp_lexmax(key, krow_);
+          if (lane == 0) {
+            sh.wkey[par][warp] = key;
+            sh.wrow[par][warp] = krow_;
+          }
+          __syncthreads();
+          key = lane < nwarps ? sh.wkey[par][lane] : 0ull;
+          krow_ = lane < nwarps ? sh.wrow[par][lane] : 0x7fffffff;
+          warp_lexmax(key, krow_);
+          cbest = key;
+          wrow = key != 0 ? krow_ : -1;
         }
-        best = warp_max64(best);
-        if (lane == 0 && best != 0) atomicMax(&sh.cmax[par], best);
-        __syncthreads();
-        // every thread has read the previous column's word: clear it for the next
-        if (tid == 0) sh.cmax[par ^ 1] = 0;
-        const unsigned long long cbest = sh.cmax[par];
-        const int wrow = cbest != 0 ? pc_row(cbest) : -1;
         // owners stage the register part of the CTA's winning row and of row k:
         // [c] = column kk + 1 + c, [32] = column kk
   #pragma unroll
         for (int i = 0; i < RPT; ++i) {
           const int row = r0 + tid + i * T;
           if (row == wrow || row == k) {
-            float *dst = row == wrow ? sh.cand : sh.krow;
+            E *dst = row == wrow ? sh.cand : sh.krow;
   #pragma unroll
             for (int c = 0; c + 1 < W; ++c) dst[c] = v[i][c + 1];
   #pragma unroll
-            for (int c = W - 1; c < 32; ++c) dst[c] = 0.f;
+            for (int c = W - 1; c < 32; ++c) dst[c] = E(0);
             dst[32] = v[i][0];
             if (row == wrow && row == k)
   #pragma unroll
@@ -453,21 +551,22 @@ __global__ void __launch_bounds__(kPcThreads, 1)
         // warp w pushes to CTAs w, w + nwarps, ...: the candidate, its word,
         // and (CTA 0) row k
         if (warp < nct) {
-          float lo = 0.f, hi = 0.f;
+          E lo = E(0), hi = E(0);
           if (wrow >= 0) {
             lo = sh.cand[lane];
-            hi = lane == 0 ? sh.cand[32] : (lane - 1 < kk ? Lsm[(lane - 1) * LD + (wrow - r0)] : 0.f);
+            hi = lane == 0 ? sh.cand[32] : (lane - 1 < kk ? Lsm[(lane - 1) * LD + (wrow - r0)] : E(0));
           }
-          float klo = 0.f, khi = 0.f;
+          E klo = E(0), khi = E(0);
           if (rank == 0) {  // row k < nb <= R lies in CTA 0
             klo = sh.krow[lane];
-            khi = lane == 0 ? sh.krow[32] : (lane - 1 < kk ? Lsm[(lane - 1) * LD + k] : 0.f);
+            khi = lane == 0 ? sh.krow[32] : (lane - 1 < kk ? Lsm[(lane - 1) * LD + k] : E(0));
           }
           for (int d = warp; d < nct; d += nwarps) {
             const unsigned mb = remote_addr(&sh.mbar[b], d);
             st_async(remote_addr(&sh.slot[b][rank][lane], d), lo, mb);
             st_async(remote_addr(&sh.slot[b][rank][32 + lane], d), hi, mb);
             if (lane == 0) st_async(remote_addr(&sh.skey[b][rank], d), cbest, mb);
+            if (kF64 && lane == 1) st_async(remote_addr(&sh.srow[b][rank], d), wrow, mb);
             if (rank == 0) {
               st_async(remote_addr(&sh.rowk[b][lane], d), klo, mb);
               st_async(remote_addr(&sh.rowk[b][32 + lane], d), khi, mb);
@@ -479,19 +578,26 @@ __global__ void __launch_bounds__(kPcThreads, 1)
         tc::mbar_wait(&sh.mbar[b], (k / kPcBuf) & 1, &ctl->status);
         if (tid == 0) tc::mbar_expect_tx(&sh.mbar[b], xbytes);
         // the cluster's pivot, identical in every CTA
-        const unsigned long long g = warp_max64(lane < nct ? sh.skey[b][lane] : 0ull);
+        int p;
+        if constexpr (!kF64) {
+          p = pc_row(warp_max64(lane < nct ? sh.skey[b][lane] : 0ull));
+        } else {
+          unsigned long long gk = lane < nct ? sh.skey[b][lane] : 0ull;
+          int gr = lane < nct && gk != 0 ? sh.srow[b][lane] : 0x7fffffff;
+          warp_lexmax(gk, gr);
+          p = gr;
+        }
         // a row outside [k, m) only after an exchange timed out (stale words):
         // row k stands in, so that the slot index and the swaps stay in range
-        int p = pc_row(g);
         if (p < k || p >= m) p = k;
-        const float *prow = sh.slot[b][p / R];
-        const float piv = prow[32];
-        const bool swap = piv != 0.f && p != k;
+        const E *prow = sh.slot[b][p / R];
+        const E piv = prow[32];
+        const bool swap = piv != E(0) && p != k;
         if (tid == 0) {
           sh.piv[kk] = swap ? p : k;
           if (rank == 0) {
             ipiv[k] = p + 1 + ipiv_base;
-            if (piv == 0.f) atomicCAS(&ctl->info, 0, k + 1 + info_base);
+            if (piv == E(0)) atomicCAS(&ctl->info, 0, k + 1 + info_base);
           }
         }
         if (swap) {  // the finished part of rows k and p, one warp each
@@ -499,22 +605,21 @@ __global__ void __launch_bounds__(kPcThreads, 1)
           if (warp == nwarps - 1 && p / R == rank && lane < kk)
             Lsm[lane * LD + (p - r0)] = sh.rowk[b][33 + lane];
         }
-        const bool recip = fabsf(piv) >= Real<float>::sfmin();
-        const float rp = 1.f / piv;
+        const bool recip = fabs(piv) >= Real<E>::sfmin();
+        const E rp = E(1) / piv;
         const int live = ws - 1 - kk;  // columns right of kk still to update
-        const float4 *p4 = reinterpret_cast<const float4 *>(prow);
   #pragma unroll
         for (int i = 0; i < RPT; ++i) {
           const int row = r0 + tid + i * T, lr = tid + i * T;
           if (swap && (row == k || row == p)) {
-            const float *src = row == k ? prow : sh.rowk[b];
+            const E *src = row == k ? prow : sh.rowk[b];
             v[i][0] = src[32];
   #pragma unroll
             for (int c = 1; c < W; ++c) v[i][c] = src[c - 1];
           }
-          float x = v[i][0];
+          E x = v[i][0];
           const bool below = row > k && row < m;
-          if (below && piv != 0.f) {
+          if (below && piv != E(0)) {
             if (recip) x *= rp;
             else x = x / piv;
           }
@@ -527,20 +632,22 @@ __global__ void __launch_bounds__(kPcThreads, 1)
             if (live > W / 2) {
   #pragma unroll
               for (int j = 0; j < W / 4; ++j) {
-                const float4 q = p4[j];
-                v[i][4 * j + 0] = fmaf(-x, q.x, v[i][4 * j + 1]);
-                v[i][4 * j + 1] = fmaf(-x, q.y, v[i][4 * j + 2]);
-                v[i][4 * j + 2] = fmaf(-x, q.z, v[i][4 * j + 3]);
-                if (4 * j + 4 < W) v[i][4 * j + 3] = fmaf(-x, q.w, v[i][4 * j + 4]);
+                E q0, q1, q2, q3;
+                load4(prow + 4 * j, q0, q1, q2, q3);
+                v[i][4 * j + 0] = fmae(-x, q0, v[i][4 * j + 1]);
+                v[i][4 * j + 1] = fmae(-x, q1, v[i][4 * j + 2]);
+                v[i][4 * j + 2] = fmae(-x, q2, v[i][4 * j + 3]);
+                if (4 * j + 4 < W) v[i][4 * j + 3] = fmae(-x, q3, v[i][4 * j + 4]);
               }
             } else {
   #pragma unroll
               for (int j = 0; j < W / 8; ++j) {
-                const float4 q = p4[j];
-                v[i][4 * j + 0] = fmaf(-x, q.x, v[i][4 * j + 1]);
-                v[i][4 * j + 1] = fmaf(-x, q.y, v[i][4 * j + 2]);
-                v[i][4 * j + 2] = fmaf(-x, q.z, v[i][4 * j + 3]);
-                v[i][4 * j + 3] = fmaf(-x, q.w, v[i][4 * j + 4]);
+                E q0, q1, q2, q3;
+                load4(prow + 4 * j, q0, q1, q2, q3);
+                v[i][4 * j + 0] = fmae(-x, q0, v[i][4 * j + 1]);
+                v[i][4 * j + 1] = fmae(-x, q1, v[i][4 * j + 2]);
+                v[i][4 * j + 2] = fmae(-x, q2, v[i][4 * j + 3]);
+                v[i][4 * j + 3] = fmae(-x, q3, v[i][4 * j + 4]);
               }
             }
           } else {
@@ -549,9 +656,9 @@ __global__ void __launch_bounds__(kPcThreads, 1)
           }
           if (live <= W / 2) {
   #pragma unroll
-            for (int c = W / 2; c + 1 < W; ++c) v[i][c] = 0.f;
+            for (int c = W / 2; c + 1 < W; ++c) v[i][c] = E(0);
           }
-          v[i][W - 1] = 0.f;
+          v[i][W - 1] = E(0);
         }
       }
       __syncthreads();
@@ -563,7 +670,7 @@ __global__ void __launch_bounds__(kPcThreads, 1)
       const int row = r0 + tid + i * T, lr = tid + i * T;
 #pragma unroll
       for (int c = 0; c < W; ++c) {
-        v[i][c] = c < ws ? Lsm[c * LD + lr] : 0.f;
+        v[i][c] = c < ws ? Lsm[c * LD + lr] : E(0);
         if (row < m && c < ws) A[row + (long)(c0 + c) * lda] = v[i][c];
       }
     }
@@ -608,11 +715,11 @@ __global__ void __launch_bounds__(kPcThreads, 1)
       constexpr int kRounds = 16;
       const bool part = tid < kCpr * kEnt && dst >= 0;
       for (int base = 0; base < mine; base += kRounds * kCpr) {
-        float val[kRounds];
+        E val[kRounds];
 #pragma unroll
         for (int u = 0; u < kRounds; ++u) {
           const int jl = base + u * kCpr + tid / kEnt;
-          val[u] = (part && jl < mine) ? __ldcg(column(jl) + src) : 0.f;
+          val[u] = (part && jl < mine) ? __ldcg(column(jl) + src) : E(0);
         }
         __syncthreads();
 #pragma unroll
@@ -630,11 +737,11 @@ __global__ void __launch_bounds__(kPcThreads, 1)
     if (nr > 0) {
       // lanes over rows (contiguous), warps over columns, several loads in flight
       {
-        float t[8];
+        E t[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
           const int c = warp + nwarps * u;
-          t[u] = (lane < ws && c < ws) ? __ldcg(A + (c0 + lane) + (long)(c0 + c) * lda) : 0.f;
+          t[u] = (lane < ws && c < ws) ? __ldcg(A + (c0 + lane) + (long)(c0 + c) * lda) : E(0);
         }
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
@@ -646,7 +753,7 @@ __global__ void __launch_bounds__(kPcThreads, 1)
           for (int u = 0; u < 8; ++u) {
             const int c = cb + warp + nwarps * u;
             t[u] = (lane < ws && c < nr) ? __ldcg(A + (c0 + lane) + (long)(c0 + ws + c) * lda)
-                                         : 0.f;
+                                         : E(0);
           }
 #pragma unroll
           for (int u = 0; u < 8; ++u) {
@@ -657,15 +764,15 @@ __global__ void __launch_bounds__(kPcThreads, 1)
       }
       __syncthreads();
       if (tid < nr) {
-        float u[W];
+        E u[W];
 #pragma unroll
-        for (int r = 0; r < W; ++r) u[r] = r < ws ? sh.U[tid][r] : 0.f;
+        for (int r = 0; r < W; ++r) u[r] = r < ws ? sh.U[tid][r] : E(0);
 #pragma unroll
         for (int q = 0; q + 1 < W; ++q)
 #pragma unroll
-          for (int r = q + 1; r < W; ++r) u[r] = fmaf(-sh.L11[r][q], u[q], u[r]);
+          for (int r = q + 1; r < W; ++r) u[r] = fmae(-sh.L11[r][q], u[q], u[r]);
 #pragma unroll
-        for (int r = 0; r < W; ++r) sh.U[tid][r] = r < ws ? u[r] : 0.f;
+        for (int r = 0; r < W; ++r) sh.U[tid][r] = r < ws ? u[r] : E(0);
       }
       __syncthreads();
       if (rank == 0)
@@ -677,13 +784,13 @@ __global__ void __launch_bounds__(kPcThreads, 1)
       const int rs = c0 + ws;
       // four columns a step; the next step's loads are issued before this
       // step's arithmetic so their latency overlaps it
-      float a[4][RPT], an[4][RPT];
+      E a[4][RPT], an[4][RPT];
 #pragma unroll
       for (int q = 0; q < 4; ++q)
 #pragma unroll
         for (int i = 0; i < RPT; ++i) {
           const int row = r0 + tid + i * T;
-          a[q][i] = (q < nr && row >= rs && row < m) ? __ldcg(A + row + (long)(rs + q) * lda) : 0.f;
+          a[q][i] = (q < nr && row >= rs && row < m) ? __ldcg(A + row + (long)(rs + q) * lda) : E(0);
         }
       for (int cb = 0; cb < nr; cb += 4) {
 #pragma unroll
@@ -693,20 +800,21 @@ __global__ void __launch_bounds__(kPcThreads, 1)
             const int row = r0 + tid + i * T, col = cb + 4 + q;
             an[q][i] = (col < nr && row >= rs && row < m)
                            ? __ldcg(A + row + (long)(rs + col) * lda)
-                           : 0.f;
+                           : E(0);
           }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          const float *u = sh.U[min(cb + q, nr - 1)];
+          const E *u = sh.U[min(cb + q, nr - 1)];
 #pragma unroll
           for (int k4 = 0; k4 < W / 4; ++k4) {
-            const float4 uu = *reinterpret_cast<const float4 *>(u + 4 * k4);
+            E u0, u1, u2, u3;
+            load4(u + 4 * k4, u0, u1, u2, u3);
 #pragma unroll
             for (int i = 0; i < RPT; ++i) {
-              a[q][i] = fmaf(-v[i][4 * k4 + 0], uu.x, a[q][i]);
-              a[q][i] = fmaf(-v[i][4 * k4 + 1], uu.y, a[q][i]);
-              a[q][i] = fmaf(-v[i][4 * k4 + 2], uu.z, a[q][i]);
-              a[q][i] = fmaf(-v[i][4 * k4 + 3], uu.w, a[q][i]);
+              a[q][i] = fmae(-v[i][4 * k4 + 0], u0, a[q][i]);
+              a[q][i] = fmae(-v[i][4 * k4 + 1], u1, a[q][i]);
+              a[q][i] = fmae(-v[i][4 * k4 + 2], u2, a[q][i]);
+              a[q][i] = fmae(-v[i][4 * k4 + 3], u3, a[q][i]);
             }
           }
         }
@@ -731,10 +839,9 @@ struct PcState {
 std::mutex g_pc_mu;
 std::map<std::pair<int, const void *>, PcState> g_pc_state;
 
-template <int RPT, int W, bool TOURN>
-int launch_pc(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base, Control *ctl,
-              int info_base, cudaStream_t s, bool *launched, float *XL, int xl, float *XR,
-              int xr) {
+template <typename E, int RPT, int W, bool TOURN>
+int launch_pc(int m, int nb, E *A, long lda, int *ipiv, int ipiv_base, Control *ctl,
+              int info_base, cudaStream_t s, bool *launched, E *XL, int xl, E *XR, int xr) {
   // rows spread over up to 16 CTAs; a CTA holds at least nb rows (row k of
   // every column lies in CTA 0) and at most 512 RPT.  The tournament runs 512
   // threads, so that its final elimination has a thread for each of the
@@ -746,13 +853,14 @@ int launch_pc(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base, Contr
   if (T > kPcThreads) return 0;
   const int R = T * RPT, nct = ceil_div(m, R);
   if (nct > kPcMaxCta) return 0;
-  // Lsm: the finished columns; for the tournament also the candidate exchange
-  auto lsm_floats = [](int rows, int ncta) {
+  // dynamic shared memory: the exchange state, then the finished columns
+  // (for the tournament also the candidate exchange)
+  auto smem_bytes = [](int rows, int ncta) {
     const long fin = (long)(rows + 1) * W;
     const long xch = TOURN ? (long)ncta * W * (W + 1) + (long)W * W : 0;
-    return std::max(fin, xch);
+    return (size_t)pc_state_bytes<E>() + sizeof(E) * (size_t)std::max(fin, xch);
   };
-  const size_t lsm = sizeof(float) * lsm_floats(R, nct);
+  const size_t lsm = smem_bytes(R, nct);
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
@@ -766,15 +874,18 @@ int launch_pc(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base, Contr
   cfg.attrs = at;
   cfg.numAttrs = 1;
   // one check per variant and device on its largest shape: 16 CTAs of 512 threads
-  auto *kern = panel_cluster_kernel<RPT, W, TOURN>;
+  auto *kern = panel_cluster_kernel<E, RPT, W, TOURN>;
   int dev = 0;
   ZG_CUDA(cudaGetDevice(&dev));
-  const size_t lmax = sizeof(float) * lsm_floats(kPcThreads * RPT, kPcMaxCta);
+  const size_t lmax = smem_bytes(kPcThreads * RPT, kPcMaxCta);
   {
     std::lock_guard<std::mutex> lk(g_pc_mu);
     PcState &st = g_pc_state[{dev, (const void *)kern}];
     if (!st.checked) {
       st.checked = true;
+      DeviceInfo di;
+      ZG_TRY(device_info(&di));
+      if (lmax > di.smem_optin) return 0;  // st.ok stays false
       ZG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
       ZG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lmax));
       cudaLaunchConfig_t big = cfg;
@@ -791,7 +902,7 @@ int launch_pc(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base, Contr
     }
     if (!st.ok) return 0;
   }
-  ZG_LAUNCH(kTagPanel, 1.0 * m * nb * nb, 2.0 * sizeof(float) * m * nb, s,
+  ZG_LAUNCH(kTagPanel, 1.0 * m * nb * nb, 2.0 * sizeof(E) * m * nb, s,
             ZG_CUDA(cudaLaunchKernelEx(&cfg, kern, m, nb, A, lda, ipiv, ipiv_base, ctl, info_base,
                                        XL, xl, XR, xr)));
   *launched = true;
@@ -803,10 +914,10 @@ int launch_pc_any(bool tourn, int m, int nb, float *A, long lda, int *ipiv, int 
                   Control *ctl, int info_base, cudaStream_t s, bool *launched, float *XL, int xl,
                   float *XR, int xr) {
   if (tourn)
-    return launch_pc<RPT, W, true>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, launched,
-                                   XL, xl, XR, xr);
-  return launch_pc<RPT, W, false>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s, launched, XL,
-                                  xl, XR, xr);
+    return launch_pc<float, RPT, W, true>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s,
+                                          launched, XL, xl, XR, xr);
+  return launch_pc<float, RPT, W, false>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s,
+                                         launched, XL, xl, XR, xr);
 }
 
 }  // namespace
@@ -829,6 +940,30 @@ int panel_lu_cluster(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base
   if (m <= kPcMaxCta * kPcThreads * 4)
     return launch_pc_any<4, 16>(tournament, m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s,
                                 launched, XL, xl, XR, xr);
+  return 0;
+}
+
+// The FP64 panel on one cluster: exact (key, row) pivot selection, sub-panels
+// of 32 / 16 / 8 columns so that the finished columns fit beside the exchange
+// state (about 78 KB + 131 KB of shared memory a CTA).
+int panel_lu_cluster(int m, int nb, double *A, long lda, int *ipiv, int ipiv_base, Control *ctl,
+                     int info_base, cudaStream_t s, bool *launched, double *XL, int xl,
+                     double *XR, int xr) {
+  *launched = false;
+  if (m <= 0 || nb <= 0) {
+    *launched = true;
+    return 0;
+  }
+  if (nb > kPcMaxNb || m < nb || xl < 0 || xr < 0) return 0;
+  if (m <= kPcMaxCta * kPcThreads)
+    return launch_pc<double, 1, 32, false>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s,
+                                           launched, XL, xl, XR, xr);
+  if (m <= kPcMaxCta * kPcThreads * 2)
+    return launch_pc<double, 2, 16, false>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s,
+                                           launched, XL, xl, XR, xr);
+  if (m <= kPcMaxCta * kPcThreads * 4)
+    return launch_pc<double, 4, 8, false>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s,
+                                          launched, XL, xl, XR, xr);
   return 0;
 }
 
