@@ -37,6 +37,10 @@ def dev(a):
 
 
 def test_panel_grid_barrier_timeout_then_recovers(lib):
+    """The cooperative FP64 panel's grid barrier (the no-allocation LU keeps
+    that panel; zml_gpu_dgetrf takes panels of up to 8192 rows on one
+    thread-block cluster, whose mbarrier waits suspend in hardware and do not
+    run out at one try)."""
     import torch
     n = 1024
     a = gaussian(n, seed=41)
@@ -44,8 +48,8 @@ def test_panel_grid_barrier_timeout_then_recovers(lib):
     piv = torch.zeros(n, dtype=torch.int32, device="cuda")
     da = dev(a)
     assert lib.zml_gpu_set_spin_limit(1) == 0
-    rc = lib.zml_gpu_dgetrf(n, n, da.data_ptr(), n, piv.data_ptr(),
-                            info.ctypes.data_as(C.c_void_p), None)
+    rc = lib.zml_gpu_dgetrf_noalloc(n, n, da.data_ptr(), n, piv.data_ptr(),
+                                    info.ctypes.data_as(C.c_void_p), None)
     assert rc == ERR_TIMEOUT, (rc, zg.last_error())
     assert "timed out" in zg.last_error()
     ipiv = piv.cpu().numpy()

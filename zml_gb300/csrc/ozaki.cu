@@ -179,31 +179,63 @@ __global__ void __launch_bounds__(256) oz_split_cols_kernel(int k, int n, const 
 // r >= c.  C_0 .. C_3 are integers below 2^24 in magnitude, so they fold into
 // one 64-bit integer exactly, I = 2^21 C_0 + 2^14 C_1 + 2^7 C_2 + C_3; the
 // FP64 pipe then sees one conversion, one FMA for C_4 and one FMA into C.
-// Rows run along x, columns along y (no index division).
+// A thread takes kOzCR rows (256 apart) of kOzCC columns, so that a block
+// moves enough bytes to be worth its launch and a thread has its loads of
+// several elements in flight.
+constexpr int kOzCR = 4, kOzCC = 4;
+// Exact conversions that keep GB300's narrow FP64 pipe to one add: an integer
+// |I| < 2^51 placed in the mantissa of 2^52 + 2^51 and that constant taken
+// off again; a normal float's sign, exponent and mantissa moved into a
+// double's fields with integer operations (zero, subnormal, inf and NaN take
+// the hardware conversion).
+__device__ __forceinline__ double oz_ll2d(long long I) {
+  return __longlong_as_double(I + 0x4338000000000000ll) - 6755399441055744.0;
+}
+__device__ __forceinline__ double oz_f2d(float f) {
+  const unsigned u = __float_as_uint(f), e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)f;
+  return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) |
+                                          ((unsigned long long)(e + 896u) << 52) |
+                                          ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+__device__ __forceinline__ double oz_fold(float w0, float w1, float w2, float w3, float w4) {
+  if (isfinite(w0) && isfinite(w1) && isfinite(w2) && isfinite(w3)) {
+    const long long I = ((long long)__float2int_rn(w0) << 21) + ((long long)__float2int_rn(w1) << 14) +
+                        ((long long)__float2int_rn(w2) << 7) + (long long)__float2int_rn(w3);
+    return fma(oz_f2d(w4), 0.0078125, oz_ll2d(I));  // |I| < 2^46
+  }
+  return (double)(w0 + w1 + w2 + w3 + w4);  // a NaN / inf operand reaches C as NaN
+}
 __global__ void __launch_bounds__(256) oz_combine_kernel(int m, int n, double *__restrict__ C,
                                                          long ldc, const float *__restrict__ W,
                                                          long ldw, long wstride,
                                                          const int *__restrict__ er,
                                                          const int *__restrict__ ec, bool lower) {
-  const int c = blockIdx.y;
-  const int ecc = ec[c] - 35;
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
-    if (lower && r < c) continue;
-    const float *w = W + r + (long)c * ldw;
-    const float w0 = __ldcs(w), w1 = __ldcs(w + wstride), w2 = __ldcs(w + 2 * wstride);
-    const float w3 = __ldcs(w + 3 * wstride), w4 = __ldcs(w + 4 * wstride);
-    double x;
-    if (isfinite(w0) && isfinite(w1) && isfinite(w2) && isfinite(w3)) {
-      const long long I = ((long long)__float2int_rn(w0) << 21) + ((long long)__float2int_rn(w1) << 14) +
-                          ((long long)__float2int_rn(w2) << 7) + (long long)__float2int_rn(w3);
-      x = fma((double)w4, 0.0078125, (double)I);
-    } else {  // a NaN / inf operand reaches C as NaN
-      x = (double)(w0 + w1 + w2 + w3 + w4);
+  const int r0 = blockIdx.x * (256 * kOzCR) + threadIdx.x, c0 = blockIdx.y * kOzCC;
+#pragma unroll
+  for (int cc = 0; cc < kOzCC; ++cc) {
+    const int c = c0 + cc;
+    if (c >= n) break;
+    const int ecc = ec[c] - 35;
+    float w[kOzCR][kOzAcc];
+#pragma unroll
+    for (int q = 0; q < kOzCR; ++q) {
+      const int r = r0 + 256 * q;
+      const float *wp = W + r + (long)c * ldw;
+      const bool in = r < m && !(lower && r < c);
+#pragma unroll
+      for (int a = 0; a < kOzAcc; ++a) w[q][a] = in ? __ldcs(wp + a * wstride) : 0.f;
     }
-    const int p = er[r] + ecc;
-    const double sc = oz_pow2(p);
-    double *cp = C + r + (long)c * ldc;
-    *cp = sc != 0.0 ? fma(-x, sc, *cp) : *cp - ldexp(x, p);
+#pragma unroll
+    for (int q = 0; q < kOzCR; ++q) {
+      const int r = r0 + 256 * q;
+      if (r >= m || (lower && r < c)) continue;
+      const double x = oz_fold(w[q][0], w[q][1], w[q][2], w[q][3], w[q][4]);
+      const int p = er[r] + ecc;
+      const double sc = oz_pow2(p);
+      double *cp = C + r + (long)c * ldc;
+      *cp = sc != 0.0 ? fma(-x, sc, *cp) : *cp - ldexp(x, p);
+    }
   }
 }
 
@@ -265,7 +297,7 @@ int dgemm_oz_sub(int m, int n, int k, const double *A, long lda, const double *B
                      W + (size_t)slot * ldw * nc, ldw, 1, status, s, syrk ? 1 : 0));
     }
     const double total = (double)rows * w;
-    const dim3 grid(std::min(ceil_div(rows, 256), 64), w);
+    const dim3 grid(ceil_div(rows, 256 * kOzCR), ceil_div(w, kOzCC));
     ZG_LAUNCH(kTagConvert, 0, (8.0 * 2 + 4.0 * kOzAcc) * total, s,
               oz_combine_kernel<<<grid, 256, 0, s>>>(rows, w, C + r0 + (long)c0 * ldc, ldc, W, ldw,
                                                      (long)ldw * nc, ea + r0, ecol + c0, syrk));
@@ -287,12 +319,10 @@ int getrf_oz(int m, int n, double *A, long lda, int *ipiv, int *info, cudaStream
   constexpr int NB = 256;
   *info = 0;
   const int mn = std::min(m, n);
-  // half-panel width: 128 columns while one per-SM slab of the tallest panel
-  // fits in shared memory, else 64 (about twice the rows)
-  DeviceInfo di;
-  ZG_TRY(device_info(&di));
-  const long slab = (long)ceil_div(m, di.num_sms) * sizeof(double);
-  const int NBP = slab * 128 <= (long)di.smem_optin - 4096 ? 128 : 64;
+  // sub-panel width: 64 columns.  On GB300 a panel's FP64 arithmetic runs on
+  // the few SMs of its cluster at the FP64 pipe's rate, so narrower panels,
+  // with the slice update between them on the tensor cores, cost less
+  const int NBP = 64;
   Control *ctl;
   ZG_TRY(control(s, &ctl));
   for (int j = 0; j < mn; j += NB) {

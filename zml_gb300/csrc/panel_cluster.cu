@@ -943,9 +943,12 @@ int panel_lu_cluster(int m, int nb, float *A, long lda, int *ipiv, int ipiv_base
   return 0;
 }
 
-// The FP64 panel on one cluster: exact (key, row) pivot selection, sub-panels
-// of 32 / 16 / 8 columns so that the finished columns fit beside the exchange
-// state (about 78 KB + 131 KB of shared memory a CTA).
+// The FP64 panel on one cluster: exact (key, row) pivot selection, 32-column
+// sub-panels, one row a thread (the finished columns, 131 KB, fit beside the
+// exchange state, about 80 KB).  Taller panels (more than 8192 rows) return
+// unlaunched: with two or four rows a thread the finished columns allow only
+// 16- or 8-column sub-panels, whose transitions made the panel slower than
+// the cooperative one (n = 16384 FP64 LU: 207 against 130 ms of panels).
 int panel_lu_cluster(int m, int nb, double *A, long lda, int *ipiv, int ipiv_base, Control *ctl,
                      int info_base, cudaStream_t s, bool *launched, double *XL, int xl,
                      double *XR, int xr) {
@@ -958,12 +961,6 @@ int panel_lu_cluster(int m, int nb, double *A, long lda, int *ipiv, int ipiv_bas
   if (m <= kPcMaxCta * kPcThreads)
     return launch_pc<double, 1, 32, false>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s,
                                            launched, XL, xl, XR, xr);
-  if (m <= kPcMaxCta * kPcThreads * 2)
-    return launch_pc<double, 2, 16, false>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s,
-                                           launched, XL, xl, XR, xr);
-  if (m <= kPcMaxCta * kPcThreads * 4)
-    return launch_pc<double, 4, 8, false>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s,
-                                          launched, XL, xl, XR, xr);
   return 0;
 }
 
