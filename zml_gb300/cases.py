@@ -5,7 +5,8 @@ profiler captures (ncu -k <kernel> -c <launches> python -m zml_gb300.cases ...).
 
 Cases (seeded N(0,1) inputs; SPD inputs G G^T / n + I):
   dgetrf, dpotrf        FP64 LU / Cholesky (zml_gpu_dgetrf, zml_gpu_dpotrf)
-  dgemm_slices          one n x n x n FP64 product by the exact-slice GEMM
+  dgemm_slices          C (n x n) -= A (n x 256) B (256 x n) in FP64 by the exact-slice
+                        GEMM (the LU's trailing update)
   mixed                 n x n Ax=b, BF16x3 LU + GMRES-IR (zml_gpu_dgesv_mpir)
   zgeqrf, dsytrf        complex QR, Bunch-Kaufman (device pointers, C entries)
 Each run is timed with CUDA events and printed with its return code.
@@ -51,7 +52,7 @@ def main():
     if a.case == "dsytrf":
         S = (S + S.t()) / 2
     if a.case == "dgemm_slices":
-        B2 = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
+        B2 = torch.randn(n, 256, dtype=torch.float64, device=dev, generator=g)  # storage of B^T
         C2 = torch.zeros(n, n, dtype=torch.float64, device=dev)
 
     def run():
@@ -62,7 +63,7 @@ def main():
             F.copy_(S)
             return L.zml_gpu_dpotrf(b"L", n, F.data_ptr(), n, C.byref(info), st)
         if a.case == "dgemm_slices":
-            return L.zml_gpu_dgemm_slices(n, n, n, S.data_ptr(), n, B2.data_ptr(), n,
+            return L.zml_gpu_dgemm_slices(n, n, 256, S.data_ptr(), n, B2.data_ptr(), 256,
                                           C2.data_ptr(), n, 0, st)
         if a.case == "mixed":
             return L.zml_gpu_dgesv_mpir(n, 1, S.data_ptr(), n, b.data_ptr(), n, x.data_ptr(), n,

@@ -42,12 +42,21 @@ constexpr int kOzAcc = 5;      // FP32 accumulators: d = 0, 1, 2, 3 and 4..7
 constexpr int kOzRows = 32;    // rows of A a block splits
 constexpr int kOzMinN = 2048;  // smaller LUs keep their updates on the FP64 pipe
 
-// Exponent e with max|row| < 2^e (0 for a zero row).
-__device__ __forceinline__ int oz_exponent(double mx) {
-  if (!(mx > 0) || !isfinite(mx)) return 0;
-  int e;
-  (void)frexp(mx, &e);
-  return e;
+// Bits of |x| (sign cleared): for finite x they order as |x| does, and a
+// NaN or inf has every exponent bit set.
+__device__ __forceinline__ unsigned long long oz_abits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+constexpr unsigned long long kOzInfBits = 0x7ff0000000000000ull;
+
+// Exponent e with max|row| < 2^e (0 for a zero or non-finite row), from the
+// bits of the row's largest |x|: frexp's exponent, taken from the exponent
+// field (normal) or the leading-zero count of the fraction (subnormal).
+__device__ __forceinline__ int oz_exponent_bits(unsigned long long b) {
+  if (b == 0 || b >= kOzInfBits) return 0;
+  const int ex = (int)(b >> 52);
+  if (ex != 0) return ex - 1022;
+  return -1010 - __clzll((long long)b);  // b < 2^52: 2^(-1074) b in [2^(e-1), 2^e)
 }
 
 // 2^p as a double for the normal range, else 0 (the caller uses ldexp then).
@@ -59,23 +68,41 @@ __device__ __forceinline__ double oz_pow2(int p) {
 // magnitude: N = x 2^(56 - e) rounded to an integer (|N| < 2^56; exact unless
 // x lies more than 2^3 below 2^(e - 53)), then N's balanced base-2^7 digits
 // from the top, q_i = round(r / 2^(49 - 7 i)), r -= q_i 2^(49 - 7 i): |q_0| <= 128,
-// |q_i| <= 64, and N = sum q_i 2^(49 - 7 i) exactly.  Integer shifts only, so
-// the FP64 pipe sees one multiply and one conversion per value.  A non-finite
-// row (nan set) gives NaN slices.
+// |q_i| <= 64, and N = sum q_i 2^(49 - 7 i) exactly.  N is formed from x's
+// fraction and exponent by shifts with round-half-even -- the value the
+// scaling x 2^(56 - e) (exact) rounded by __double2ll_rn gives -- so the whole
+// split runs on the integer pipes.  A non-finite row (nan set) gives NaN
+// slices.
 __device__ __forceinline__ void oz_slices(double x, int e, bool nan, float (&q)[kOzS]) {
-  if (nan || !isfinite(x)) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  int ex = (int)((bits >> 52) & 0x7ff);
+  if (nan || ex == 0x7ff) {
 #pragma unroll
     for (int i = 0; i < kOzS; ++i) q[i] = __int_as_float(0x7fc00000);
     return;
   }
-  const double p = oz_pow2(56 - e);
-  long long r = __double2ll_rn(p != 0.0 ? x * p : ldexp(x, 56 - e));
+  unsigned long long mant = bits & 0xfffffffffffffull;
+  if (ex != 0) mant |= 1ull << 52;
+  else ex = 1;  // subnormal: 2^(1 - 1075) times the fraction
+  const int t = ex - 1019 - e;  // |x| 2^(56 - e) = mant 2^t, t <= 3
+  unsigned long long a;
+  if (t >= 0) {
+    a = mant << t;
+  } else if (t < -63) {
+    a = 0;
+  } else {
+    const int k = -t;
+    a = mant >> k;
+    const unsigned long long rem = mant & ((1ull << k) - 1), half = 1ull << (k - 1);
+    if (rem > half || (rem == half && (a & 1))) ++a;
+  }
+  long long r = (bits >> 63) ? -(long long)a : (long long)a;
 #pragma unroll
   for (int i = 0; i < kOzS - 1; ++i) {
     const int sh = 49 - 7 * i;
-    const long long t = (r + (1ll << (sh - 1))) >> sh;
-    r -= t << sh;
-    q[i] = (float)(int)t;
+    const long long t2 = (r + (1ll << (sh - 1))) >> sh;
+    r -= t2 << sh;
+    q[i] = (float)(int)t2;
   }
   q[kOzS - 1] = (float)(int)r;
 }
@@ -100,19 +127,13 @@ __global__ void __launch_bounds__(256) oz_split_rows_kernel(int m, int k, const 
   }
   __syncthreads();
   for (int r = warp; r < kOzRows; r += blockDim.x >> 5) {
-    double mx = 0;
-    bool nonfinite = false;
-    for (int c = lane; c < k; c += 32) {
-      const double v = ozt[r * LD + c];
-      mx = fmax(mx, fabs(v));
-      nonfinite |= !isfinite(v);
-    }
+    unsigned long long mx = 0;  // the bits of the largest |x| (integers order them)
+    for (int c = lane; c < k; c += 32) mx = max(mx, oz_abits(ozt[r * LD + c]));
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(~0u, mx, o));
-    nonfinite = __any_sync(~0u, nonfinite);
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(~0u, mx, o));
     if (lane == 0) {
-      er[r] = oz_exponent(mx);
-      bad[r] = nonfinite;
+      er[r] = oz_exponent_bits(mx);
+      bad[r] = mx >= kOzInfBits;
     }
   }
   __syncthreads();
@@ -147,19 +168,17 @@ __global__ void __launch_bounds__(256) oz_split_cols_kernel(int k, int n, const 
   if (col >= n) return;
   constexpr int kPer = kOzMaxK / 32;
   double x[kPer];
-  double mx = 0;
-  bool nonfinite = false;
+  unsigned long long mx = 0;
 #pragma unroll
   for (int t = 0; t < kPer; ++t) {
     const int c = lane + 32 * t;
     x[t] = c < k ? B[c + (long)col * ldb] : 0.0;
-    mx = fmax(mx, fabs(x[t]));
-    nonfinite |= !isfinite(x[t]);
+    mx = max(mx, oz_abits(x[t]));
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(~0u, mx, o));
-  nonfinite = __any_sync(~0u, nonfinite);
-  const int e = oz_exponent(mx);
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(~0u, mx, o));
+  const bool nonfinite = mx >= kOzInfBits;
+  const int e = oz_exponent_bits(mx);
   const long ldo = (long)kOzS * kp;
   __nv_bfloat16 *out = rev + (long)col * ldo;
 #pragma unroll
@@ -183,13 +202,19 @@ __global__ void __launch_bounds__(256) oz_split_cols_kernel(int k, int n, const 
 // moves enough bytes to be worth its launch and a thread has its loads of
 // several elements in flight.
 constexpr int kOzCR = 4, kOzCC = 4;
-// Exact conversions that keep GB300's narrow FP64 pipe to one add: an integer
-// |I| < 2^51 placed in the mantissa of 2^52 + 2^51 and that constant taken
-// off again; a normal float's sign, exponent and mantissa moved into a
-// double's fields with integer operations (zero, subnormal, inf and NaN take
-// the hardware conversion).
+// Exact conversions on the integer pipes, which keep GB300's narrow FP64
+// pipe (under one instruction a clock per SM) for the two FMAs that round:
+// an integer |I| < 2^53 normalised by its leading-zero count into a double's
+// exponent and fraction; a normal float's sign, exponent and mantissa moved
+// into a double's fields (zero, subnormal, inf and NaN take the hardware
+// conversion).
 __device__ __forceinline__ double oz_ll2d(long long I) {
-  return __longlong_as_double(I + 0x4338000000000000ll) - 6755399441055744.0;
+  if (I == 0) return 0.0;
+  const unsigned long long a = I < 0 ? 0ull - (unsigned long long)I : (unsigned long long)I;
+  const int lz = __clzll((long long)a);  // >= 11
+  const unsigned long long frac = (a << (lz + 1)) >> 12;  // the bits below the leading one
+  return __longlong_as_double((long long)((I < 0 ? 1ull << 63 : 0ull) |
+                                          ((unsigned long long)(1086 - lz) << 52) | frac));
 }
 __device__ __forceinline__ double oz_f2d(float f) {
   const unsigned u = __float_as_uint(f), e = (u >> 23) & 0xffu;
@@ -232,9 +257,9 @@ __global__ void __launch_bounds__(256) oz_combine_kernel(int m, int n, double *_
       if (r >= m || (lower && r < c)) continue;
       const double x = oz_fold(w[q][0], w[q][1], w[q][2], w[q][3], w[q][4]);
       const int p = er[r] + ecc;
-      const double sc = oz_pow2(p);
       double *cp = C + r + (long)c * ldc;
-      *cp = sc != 0.0 ? fma(-x, sc, *cp) : *cp - ldexp(x, p);
+      // the scale 2^p as a normal double when p is in range (an integer test)
+      *cp = (p >= -1022 && p <= 1023) ? fma(-x, oz_pow2(p), *cp) : *cp - ldexp(x, p);
     }
   }
 }
