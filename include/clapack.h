@@ -217,7 +217,11 @@ typedef struct zml_mpir_result {
  * modified.  tol = 0 refines until the backward error stops improving.  When
  * the low-precision LU fails or refinement stops short (of tol, or of 64 u
  * with tol = 0), the system is solved again by the FP64 LU (fp64_fallback).
- * Host or device pointers. */
+ * Host or device pointers.  A column-major A in page-locked host memory
+ * (cudaHostAlloc / cudaHostRegister) with n >= 4096 and ZML_PREC_BF16X3 is
+ * copied in column chunks while the LU factors the chunks already copied;
+ * the result is bit for bit the device-pointer call's, and res->factor_ms
+ * then includes the copy. */
 int zml_dgesv_mpir(int matrix_layout, int n, int nrhs, const double *a, int lda, const double *b,
                    int ldb, double *x, int ldx, int prec, int mode, double tol, int max_iter,
                    zml_mpir_result *res);

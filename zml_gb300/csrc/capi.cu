@@ -56,6 +56,18 @@ bool is_device_ptr(const void *p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// Page-locked host memory (cudaHostAlloc / cudaHostRegister): copies from it
+// are asynchronous, so they can run beside kernels.
+bool is_pinned_host(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
 // A column-major rows x cols operand that lives on the device for the call.
 template <typename T> struct Staged {
   T *d = nullptr;
@@ -743,10 +755,17 @@ int mpir_any(int layout, int n, int nrhs, const double *a, int lda, const double
   if (n == 0 || nrhs == 0) return 0;
   cudaStream_t s = lib_stream();
   ColMajor<double> A, B, X;
-  ZG_TRY(A.in(layout, a, lda, n, n, kSlotA, kSlotAT, true, s));
   ZG_TRY(B.in(layout, b, ldb, n, nrhs, kSlotB, kSlotBT, true, s));
   ZG_TRY(X.in(layout, x, ldx, n, nrhs, kSlotX, kSlotXT, false, s));
-  ZG_TRY(gesv_mpir_dev(n, nrhs, A.d, A.ld, B.d, B.ld, X.d, X.ld, o, res, s));
+  if (layout == kColMajor && mixed_streams_host(n, o) && is_pinned_host(a)) {
+    // A from page-locked memory: its copy overlaps the factorization
+    void *w;
+    ZG_TRY(workspace(s, kSlotA, sizeof(double) * (size_t)n * n, &w));
+    ZG_TRY(gesv_mpir_host(n, nrhs, a, lda, (double *)w, B.d, B.ld, X.d, X.ld, o, res, s));
+  } else {
+    ZG_TRY(A.in(layout, a, lda, n, n, kSlotA, kSlotAT, true, s));
+    ZG_TRY(gesv_mpir_dev(n, nrhs, A.d, A.ld, B.d, B.ld, X.d, X.ld, o, res, s));
+  }
   ZG_TRY(X.out(s));
   return sync(s);
 }

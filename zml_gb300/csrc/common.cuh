@@ -113,6 +113,7 @@ enum Slot : int {
   kSlotSytrf = 25,            // Bunch-Kaufman: the step's block size read back by the host
   kSlotOzA = 26, kSlotOzB = 27,  // FP64-by-slices GEMM: the BF16 slices of A and B, exponents
   kSlotOzC = 28,              // FP64-by-slices GEMM: the FP32 accumulators
+  kSlotChunk = 29,            // mixed LU of a host A: the replayed blocks' 16-bit operands
   kNumSlots = 30
 };
 

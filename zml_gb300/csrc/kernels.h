@@ -79,6 +79,9 @@ int transpose_dev(int rows, int cols, const T *src, long lds, T *dst, long ldd, 
 // lu.cu
 template <typename T>
 int laswp_dev(int n, T *A, long lda, int k1, int k2, const int *ipiv, int incx, cudaStream_t s);
+// Sizes the interchange workspace of stream s now (laswp_dev then allocates
+// nothing on s).
+int laswp_reserve(cudaStream_t s);
 // One panel's interchanges (rows k1..k2, forward, 1-based) on the column
 // ranges [0, c_left) and [c_right, n), composed once.
 template <typename T>

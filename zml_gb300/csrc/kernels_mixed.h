@@ -48,6 +48,16 @@ int set_mixed_tournament(int on);
 // low-precision factorization, then refinement of each right-hand side.
 int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, long ldb,
                   double *X, long ldx, const MpirOpts &o, MpirResult *res, cudaStream_t s);
+// The same solve with A in pinned host memory (column-major, ld ldh): A is
+// copied into Ad (device, n x n, ld n) in column chunks while the
+// factorization already runs on the chunks that have arrived; the factors
+// and the solution equal gesv_mpir_dev's on the same A.  Only where
+// mixed_streams_host(n, o) holds: n >= kChunkMinN and BF16x3 updates.
+constexpr int kChunkMinN = 4096;
+bool mixed_streams_host(int n, const MpirOpts &o);
+int gesv_mpir_host(int n, int nrhs, const double *Ah, long ldh, double *Ad, const double *B,
+                   long ldb, double *X, long ldx, const MpirOpts &o, MpirResult *res,
+                   cudaStream_t s);
 // SPD form: low-precision Cholesky (only the `lower` / upper triangle of A is
 // read) and the same refinement.
 int posv_mpir_dev(bool lower, int n, int nrhs, const double *A, long lda, const double *B,

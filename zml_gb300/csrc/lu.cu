@@ -369,6 +369,11 @@ static int laswp_apply(int n, T *A, long lda, const SwapPlan &plan, cudaStream_t
   return 0;
 }
 
+int laswp_reserve(cudaStream_t s) {
+  void *w;
+  return workspace(s, kSlotSwap, sizeof(int) * (4 * kSwapMax + 8), &w);
+}
+
 template <typename T>
 int laswp_dev(int n, T *A, long lda, int k1, int k2, const int *ipiv, int incx, cudaStream_t s) {
   if (n <= 0 || k2 < k1) return 0;

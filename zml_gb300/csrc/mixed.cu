@@ -354,10 +354,84 @@ int lookahead(cudaStream_t s, Lookahead **out) {
   *out = &l;
   return 0;
 }
+
+// A factored while it arrives from pinned host memory: its columns come in
+// chunks on a copy stream, each chunk is converted to FP32 on its own stream
+// and there receives, in order, the updates of the blocks factored before
+// it joins the main loop (replayed from their saved 16-bit operands); from
+// its join block on, the main loop updates it like any other column.
+struct ChunkStreams {
+  static constexpr int kMax = 8;
+  cudaStream_t copy = nullptr, ck[kMax] = {};
+  cudaEvent_t copied[kMax] = {}, caught[kMax] = {};
+  std::vector<cudaEvent_t> ops;  // block b's saved operands and pivots are final
+};
+std::map<std::pair<int, cudaStream_t>, ChunkStreams> g_cs;
+
+int chunk_streams(cudaStream_t s, int nblocks, ChunkStreams **out) {
+  int dev = 0;
+  ZG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_la_mu);
+  ChunkStreams &c = g_cs[{dev, s}];
+  const unsigned fl = cudaEventDisableTiming;
+  if (!c.copy) {
+    int least = 0, greatest = 0;
+    ZG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    ZG_CUDA(cudaStreamCreateWithFlags(&c.copy, cudaStreamNonBlocking));
+    for (int q = 0; q < ChunkStreams::kMax; ++q) {
+      ZG_CUDA(cudaStreamCreateWithPriority(&c.ck[q], cudaStreamNonBlocking, least));
+      ZG_CUDA(cudaEventCreateWithFlags(&c.copied[q], fl));
+      ZG_CUDA(cudaEventCreateWithFlags(&c.caught[q], fl));
+    }
+  }
+  while ((int)c.ops.size() < nblocks) {
+    cudaEvent_t e;
+    ZG_CUDA(cudaEventCreateWithFlags(&e, fl));
+    c.ops.push_back(e);
+  }
+  *out = &c;
+  return 0;
+}
+
+// The geometry of one streamed factorization (BF16x3 updates, NB = 256).
+struct ChunkPlan {
+  int w = 0, nck = 0;                  // chunk width (a multiple of 512 columns), chunk count
+  int join[ChunkStreams::kMax] = {};   // block before whose interchanges chunk c joins
+  int bmax = 0;                        // blocks 0 .. bmax-1 keep their operands for replays
+  uint16_t *savedL = nullptr;          // their L21 operands, one after the other
+  uint16_t *savedLi = nullptr;         // their L11^-1 operands, NB x ldo each
+  std::vector<size_t> offL;            // element offset of block b's L21 operand in savedL
+  ChunkStreams *cs = nullptr;
+};
+
+// Block b's update of chunk c on the chunk's stream, as the main loop makes
+// it on joined columns: the block's interchanges, U12 = L11^-1 A12 on the
+// tensor cores, then A22 -= L21 U12.  The arithmetic per element is the
+// main loop's (same operands, same K order), so the factors do not depend
+// on when a chunk arrived.
+static int replay_block(const ChunkPlan &cp, int c, int b, int n, float *A, long lda,
+                        const int *ipiv, unsigned *status) {
+  constexpr int NB = 256, ldk = NB;
+  constexpr long ldo = 3L * ldk;
+  const int j = b * NB, c0 = c * cp.w, wc = std::min(cp.w, n - c0);
+  const cudaStream_t st = cp.cs->ck[c];
+  ZG_CUDA(cudaStreamWaitEvent(st, cp.cs->ops[b], 0));
+  float *Ac = A + (long)c0 * lda;
+  ZG_TRY(laswp_dev<float>(wc, Ac, lda, j + 1, j + NB, ipiv, 1, st));
+  void *wu;
+  ZG_TRY(workspace(st, kSlotU16, sizeof(uint16_t) * (size_t)wc * ldo, &wu));
+  ZG_TRY(to_kmajor_n(kPrecBF16x3, NB, wc, Ac + j, lda, wu, ldk, st));
+  ZG_TRY(gemm_tc(NB, wc, (int)ldo, 1.f, cp.savedLi + (size_t)b * NB * ldo, ldo, wu, ldo, 0.f,
+                 Ac + j, lda, 1, status, st));
+  ZG_TRY(to_kmajor_n(kPrecBF16x3, NB, wc, Ac + j, lda, wu, ldk, st));
+  ZG_TRY(gemm_tc(n - j - NB, wc, (int)ldo, -1.f, cp.savedL + cp.offL[b], ldo, wu, ldo, 1.f,
+                 Ac + j + NB, lda, 1, status, st));
+  return 0;
+}
 }  // namespace
 
 static int getrf_lowp_blocks(int n, float *A, long lda, int *ipiv, int prec, Control *ctl,
-                             cudaStream_t s, Lookahead &la);
+                             cudaStream_t s, Lookahead &la, ChunkPlan *cp = nullptr);
 
 // Pivoting of the low-precision LU's panels.  The factors only precondition
 // the refinement, so they need not carry partial pivoting's exact pivots:
@@ -393,7 +467,7 @@ int getrf_lowp(int n, float *A, long lda, int *ipiv, int prec, Control *ctl, cud
 }
 
 static int getrf_lowp_blocks(int n, float *A, long lda, int *ipiv, int prec, Control *ctl,
-                             cudaStream_t s, Lookahead &la) {
+                             cudaStream_t s, Lookahead &la, ChunkPlan *cp) {
   constexpr int NB = 256, NBP = 128;
   const int segs = prec == kPrecBF16x3 ? 3 : 1;
   const size_t nop = (size_t)n * NB * segs;  // 16-bit elements of one operand buffer
@@ -411,9 +485,17 @@ static int getrf_lowp_blocks(int n, float *A, long lda, int *ipiv, int prec, Con
   void *wli = Tb + ntb;
   const cudaStream_t sp = la.panel, sb = la.bulk;
   constexpr int R = Lookahead::kRing;
+  // columns the main loop updates: all n, or the chunks joined so far
+  int lim = n, joined = 0;
+  if (cp) {
+    lim = 0;
+    ZG_CUDA(cudaStreamWaitEvent(sp, cp->cs->caught[0], 0));  // block 0's panel reads chunk 0
+  }
   for (int j = 0, b = 0; j < n; j += NB, ++b) {
     const int jb = std::min(NB, n - j);
-    uint16_t *wl = (uint16_t *)wl0 + (b & 1) * nop, *wu = (uint16_t *)wu0 + (b & 1) * nop;
+    const bool keep = cp && b < cp->bmax;  // a later chunk replays this block
+    uint16_t *wl = keep ? cp->savedL + cp->offL[b] : (uint16_t *)wl0 + (b & 1) * nop;
+    uint16_t *wu = (uint16_t *)wu0 + (b & 1) * nop;
     // this block's columns were last updated by block b-2's bulk update
     if (b >= 2) ZG_CUDA(cudaStreamWaitEvent(sp, la.bulk_done[(b - 2) % R], 0));
     ZG_CUDA(cudaMemsetAsync(Linv, 0, sizeof(float) * NB * NB, sp));
@@ -463,9 +545,16 @@ static int getrf_lowp_blocks(int n, float *A, long lda, int *ipiv, int prec, Con
     }
     // the interchanges reach every other column: wait for block b-1's bulk update
     if (b >= 1) ZG_CUDA(cudaStreamWaitEvent(sp, la.bulk_done[(b - 1) % R], 0));
-    ZG_TRY(laswp_panel<float>(j, j + jb, n, A, lda, j + 1, j + jb, ipiv, sp));
-    const int rest = n - j - jb;
+    // chunks due now join, caught up through block b-1
+    while (cp && joined < cp->nck && cp->join[joined] <= b) {
+      ZG_CUDA(cudaStreamWaitEvent(sp, cp->cs->caught[joined], 0));
+      lim = std::min(n, (joined + 1) * cp->w);
+      ++joined;
+    }
+    ZG_TRY(laswp_panel<float>(j, j + jb, lim, A, lda, j + 1, j + jb, ipiv, sp));
+    const int rest = n - j - jb;   // rows below the block
     if (rest <= 0) break;
+    const int rc = lim - j - jb;   // columns right of the block that the main loop updates
     float *A12 = A + j + (long)(j + jb) * lda;
     // U12 = L11^-1 A12.  BF16x3 (about 16 bits, the precision of its trailing
     // updates): on the tensor cores, A12 read through its 16-bit copy and U12
@@ -473,27 +562,35 @@ static int getrf_lowp_blocks(int n, float *A, long lda, int *ipiv, int prec, Con
     // 11 bits, so there the product is an FP32 GEMM.
     const int ldk = ((jb + 7) / 8) * 8;
     const long ldo = (long)ldk * segs;
+    void *wlib = keep ? (void *)(cp->savedLi + (size_t)b * NB * ldo) : wli;
     if (prec == kPrecBF16x3) {
-      ZG_TRY(to_kmajor_t(prec, jb, jb, Linv, NB, wli, ldk, sp));
-      ZG_TRY(to_kmajor_n(prec, jb, rest, A12, lda, wu, ldk, sp));
-      ZG_TRY(gemm_tc(jb, rest, (int)ldo, 1.f, wli, ldo, wu, ldo, 0.f, A12, lda, 1, &ctl->status,
+      ZG_TRY(to_kmajor_t(prec, jb, jb, Linv, NB, wlib, ldk, sp));
+      ZG_TRY(to_kmajor_n(prec, jb, rc, A12, lda, wu, ldk, sp));
+      ZG_TRY(gemm_tc(jb, rc, (int)ldo, 1.f, wlib, ldo, wu, ldo, 0.f, A12, lda, 1, &ctl->status,
                      sp));
     } else {
-      ZG_TRY(apply_inverse(jb, rest, Linv, NB, A12, lda, Tb, sp));
+      ZG_TRY(apply_inverse(jb, rc, Linv, NB, A12, lda, Tb, sp));
     }
-    // 16-bit operands: L21 (rest x jb) and U12^T (rest x jb), K-major
+    // 16-bit operands: L21 (rest x jb) and U12^T (rc x jb), K-major
     ZG_TRY(to_kmajor_t(prec, rest, jb, A + (j + jb) + (long)j * lda, lda, wl, ldk, sp));
-    ZG_TRY(to_kmajor_n(prec, jb, rest, A12, lda, wu, ldk, sp));
+    if (keep) {  // the chunks not yet joined replay this block on their own streams
+      ZG_CUDA(cudaEventRecord(cp->cs->ops[b], sp));
+      for (int c = joined; c < cp->nck; ++c) {
+        ZG_TRY(replay_block(*cp, c, b, n, A, lda, ipiv, &ctl->status));
+        if (cp->join[c] == b + 1) ZG_CUDA(cudaEventRecord(cp->cs->caught[c], cp->cs->ck[c]));
+      }
+    }
+    ZG_TRY(to_kmajor_n(prec, jb, rc, A12, lda, wu, ldk, sp));
     const int abt = prec == kPrecFP16 ? 0 : 1;  // 16-bit operand type: FP16 0, BF16 1
     // the next block's columns now, on the panel stream ...
-    const int near = std::min(NB, rest);
+    const int near = std::min(NB, rc);
     ZG_TRY(gemm_tc(rest, near, (int)ldo, -1.f, wl, ldo, wu, ldo, 1.f, A12 + jb, lda, abt,
                    &ctl->status, sp));
     // ... the rest on the bulk stream, beside the next block's panel
-    if (rest > near) {
+    if (rc > near) {
       ZG_CUDA(cudaEventRecord(la.upd[b % R], sp));
       ZG_CUDA(cudaStreamWaitEvent(sb, la.upd[b % R], 0));
-      ZG_TRY(gemm_tc(rest, rest - near, (int)ldo, -1.f, wl, ldo, wu + (long)near * ldo, ldo, 1.f,
+      ZG_TRY(gemm_tc(rest, rc - near, (int)ldo, -1.f, wl, ldo, wu + (long)near * ldo, ldo, 1.f,
                      A12 + jb + (long)near * lda, lda, abt, &ctl->status, sb));
     }
     ZG_CUDA(cudaEventRecord(la.bulk_done[b % R], sb));
@@ -954,11 +1051,13 @@ __global__ void absmax_kernel(int n, const double *x, double *out) {
 // One pass over the FP64 matrix: B = fp32(A), and the row sums of |A| for
 // ||A||_inf, as FP32 partial sums over 512-column chunks (positive terms, at
 // most 512 a chunk: relative error below 1e-4, ample for a norm that only
-// scales the backward error) that a second kernel adds in FP64.
-__global__ void __launch_bounds__(kGemvRows) d2s_rowabs_kernel(int n, const double *A, long lda,
-                                                                float *B, long ldb, float *part) {
+// scales the backward error) that a second kernel adds in FP64.  n rows;
+// ncols columns (all n, or one column chunk starting on a 512-column group).
+__global__ void __launch_bounds__(kGemvRows) d2s_rowabs_kernel(int n, int ncols, const double *A,
+                                                                long lda, float *B, long ldb,
+                                                                float *part) {
   const int i = blockIdx.x * kGemvRows + threadIdx.x;
-  const int c0 = blockIdx.y * kGemvCols, c1 = min(n, c0 + kGemvCols);
+  const int c0 = blockIdx.y * kGemvCols, c1 = min(ncols, c0 + kGemvCols);
   if (i >= n) return;
   float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
   int j = c0;
@@ -1194,11 +1293,96 @@ struct MpirCtx {
   IRWork w{};
 };
 
+// BF16x3 LU of an n x n A that arrives from pinned host memory (column-major,
+// ld ldh): its FP64 copy lands in Ad (ld n) and its FP32 copy in LU (ld n),
+// with the row sums of |A| as 512-column partials in rpart, chunk by chunk,
+// while the factorization runs on the chunks already there.  The factors
+// equal those of getrf_lowp on the whole FP32 copy.
+static int getrf_lowp_host(int n, const double *Ah, long ldh, double *Ad, float *LU, int *ipiv,
+                           float *rpart, Control *ctl, cudaStream_t s) {
+  constexpr int NB = 256;
+  constexpr long ldo = 3L * NB;
+  Lookahead *la;
+  ZG_TRY(lookahead(s, &la));
+  ChunkStreams *cs;
+  ZG_TRY(chunk_streams(s, ceil_div(n, NB), &cs));
+  ChunkPlan cp;
+  cp.cs = cs;
+  cp.w = ceil_div(ceil_div(n, ChunkStreams::kMax), kGemvCols) * kGemvCols;
+  cp.nck = ceil_div(n, cp.w);
+  // a chunk joins one chunk width before its first block, so its replays run
+  // beside the factorization of the chunk before it
+  const int lag = cp.w / NB;
+  for (int c = 0; c < cp.nck; ++c) cp.join[c] = std::max(0, c * cp.w / NB - lag);
+  cp.bmax = cp.join[cp.nck - 1];
+  cp.offL.resize(cp.bmax + 1);
+  size_t tot = 0;
+  for (int b = 0; b < cp.bmax; ++b) {
+    cp.offL[b] = tot;
+    tot += (size_t)(n - (b + 1) * NB) * ldo;
+  }
+  void *w;
+  ZG_TRY(workspace(s, kSlotChunk, sizeof(uint16_t) * (tot + (size_t)cp.bmax * NB * ldo), &w));
+  cp.savedL = (uint16_t *)w;
+  cp.savedLi = cp.savedL + tot;
+  // the chunk streams' buffers, sized before anything is queued: no
+  // allocation (nor its synchronisation) between the queued copies
+  for (int c = 0; c < cp.nck; ++c) {
+    void *t;
+    ZG_TRY(workspace(cs->ck[c], kSlotU16, sizeof(uint16_t) * (size_t)cp.w * ldo, &t));
+    ZG_TRY(laswp_reserve(cs->ck[c]));
+  }
+  // everything after the caller's earlier work, which may still read Ad, LU
+  // or rpart
+  ZG_CUDA(cudaEventRecord(la->first, s));
+  ZG_CUDA(cudaStreamWaitEvent(cs->copy, la->first, 0));
+  ZG_CUDA(cudaStreamWaitEvent(la->panel, la->first, 0));
+  ZG_CUDA(cudaStreamWaitEvent(la->bulk, la->first, 0));
+  for (int c = 0; c < cp.nck; ++c) {
+    const long c0 = (long)c * cp.w;
+    const int wc = std::min<long>(cp.w, n - c0);
+    ZG_CUDA(cudaMemcpy2DAsync(Ad + c0 * n, sizeof(double) * n, Ah + c0 * ldh,
+                              sizeof(double) * ldh, sizeof(double) * n, wc,
+                              cudaMemcpyHostToDevice, cs->copy));
+    ZG_CUDA(cudaEventRecord(cs->copied[c], cs->copy));
+  }
+  for (int c = 0; c < cp.nck; ++c) {
+    const long c0 = (long)c * cp.w;
+    const int wc = std::min<long>(cp.w, n - c0);
+    const cudaStream_t st = cs->ck[c];
+    ZG_CUDA(cudaStreamWaitEvent(st, cs->copied[c], 0));
+    ZG_LAUNCH(kTagConvert, 0, 12.0 * n * wc, st,
+              d2s_rowabs_kernel<<<dim3(ceil_div(n, kGemvRows), ceil_div(wc, kGemvCols)),
+                                  kGemvRows, 0, st>>>(n, wc, Ad + c0 * n, n, LU + c0 * n, n,
+                                                      rpart + (c0 / kGemvCols) * n));
+    if (cp.join[c] == 0) ZG_CUDA(cudaEventRecord(cs->caught[c], st));
+  }
+  const int rc = getrf_lowp_blocks(n, LU, n, ipiv, kPrecBF16x3, ctl, s, *la, &cp);
+  // the caller's stream resumes after every internal stream (also when the
+  // loop stopped early and left chunks unjoined)
+  ZG_CUDA(cudaEventRecord(la->end_panel, la->panel));
+  ZG_CUDA(cudaEventRecord(la->end_bulk, la->bulk));
+  ZG_CUDA(cudaStreamWaitEvent(s, la->end_panel, 0));
+  ZG_CUDA(cudaStreamWaitEvent(s, la->end_bulk, 0));
+  for (int c = 0; c < cp.nck; ++c) {
+    ZG_CUDA(cudaEventRecord(cs->caught[c], cs->ck[c]));
+    ZG_CUDA(cudaStreamWaitEvent(s, cs->caught[c], 0));
+  }
+  return rc;
+}
+
+bool mixed_streams_host(int n, const MpirOpts &o) {
+  return n >= kChunkMinN && o.prec == kPrecBF16x3;
+}
+
 // Factor phase.  spd: A symmetric positive definite, only its `lower` (else
 // upper) triangle is read; factored by the low-precision Cholesky.
 // Otherwise general, LU.  res->info receives the factorization's info.
+// Ah (general A, BF16x3, n >= kChunkMinN only): A is copied from this pinned
+// host matrix (ld ldh) into A (ld n) during the factorization.
 static int mpir_factor(bool spd, bool lower, int n, const double *A, long lda, const MpirOpts &o,
-                       MpirCtx *c, MpirResult *res, cudaStream_t s) {
+                       MpirCtx *c, MpirResult *res, cudaStream_t s, const double *Ah = nullptr,
+                       long ldh = 0) {
   *res = MpirResult{};
   Control *ctl;
   ZG_TRY(control(s, &ctl));
@@ -1241,31 +1425,40 @@ static int mpir_factor(bool spd, bool lower, int n, const double *A, long lda, c
   w.tw = (unsigned *)p;
 
   // the FP32 working copy of A and ||A||_inf, in one pass over A
-  {
-    float *rpart = reinterpret_cast<float *>(w.part);  // n x nparts floats fit in w.part
+  float *rpart = reinterpret_cast<float *>(w.part);  // n x nparts floats fit in w.part
+  double anrm = 0;
+  if (!Ah) {
     ZG_LAUNCH(kTagConvert, 0, 12.0 * n * n, s,
               d2s_rowabs_kernel<<<dim3(ceil_div(n, kGemvRows), nparts), kGemvRows, 0, s>>>(
-                  n, A, lda, LU, n, rpart));
+                  n, n, A, lda, LU, n, rpart));
     ZG_LAUNCH(kTagVector, 0, 0, s,
               rowabs_finish_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, nparts, rpart, w.r));
+    ZG_LAUNCH(kTagVector, 0, 0, s, absmax_kernel<<<1, 256, 0, s>>>(n, w.r, w.scal));
+    ZG_CUDA(cudaGetLastError());
+    ZG_TRY(host_scalar(w.scal, &anrm, s));
   }
-  ZG_LAUNCH(kTagVector, 0, 0, s, absmax_kernel<<<1, 256, 0, s>>>(n, w.r, w.scal));
-  ZG_CUDA(cudaGetLastError());
-  double anrm;
-  ZG_TRY(host_scalar(w.scal, &anrm, s));
 
-  // factor in low precision
+  // factor in low precision (with A's arrival, for a host A)
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, s);
-  if (spd)
+  if (Ah)
+    ZG_TRY(getrf_lowp_host(n, Ah, ldh, const_cast<double *>(A), LU, ipiv, rpart, ctl, s));
+  else if (spd)
     ZG_TRY(potrf_lowp(n, LU, n, o.prec, ctl, s));
   else
     ZG_TRY(getrf_lowp(n, LU, n, ipiv, o.prec, ctl, s));
   cudaEventRecord(e1, s);
+  if (Ah) {
+    ZG_LAUNCH(kTagVector, 0, 0, s,
+              rowabs_finish_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, nparts, rpart, w.r));
+    ZG_LAUNCH(kTagVector, 0, 0, s, absmax_kernel<<<1, 256, 0, s>>>(n, w.r, w.scal));
+    ZG_CUDA(cudaGetLastError());
+  }
   int info = 0;
   ZG_TRY(check_status(s, ctl, &info));
+  if (Ah) ZG_TRY(host_scalar(w.scal, &anrm, s));
   float ms = 0;
   cudaEventElapsedTime(&ms, e0, e1);
   res->factor_ms = ms;
@@ -1459,11 +1652,12 @@ static int fp64_posv(bool lower, int n, int nrhs, const double *A, long lda, con
 
 static int solve_mpir_dev(bool spd, bool lower, int n, int nrhs, const double *A, long lda,
                           const double *B, long ldb, double *X, long ldx, const MpirOpts &o,
-                          MpirResult *res, cudaStream_t s) {
+                          MpirResult *res, cudaStream_t s, const double *Ah = nullptr,
+                          long ldh = 0) {
   *res = MpirResult{};
   if (n <= 0 || nrhs <= 0) return 0;
   MpirCtx c;
-  ZG_TRY(mpir_factor(spd, lower, n, A, lda, o, &c, res, s));
+  ZG_TRY(mpir_factor(spd, lower, n, A, lda, o, &c, res, s, Ah, ldh));
   if (res->info == 0) ZG_TRY(mpir_refine(c, o, nrhs, B, ldb, X, ldx, false, res, s));
   if (!o.fallback || (res->info == 0 && res->converged)) return 0;
   // the safety net: the low-precision factors could not take the backward
@@ -1487,6 +1681,16 @@ static int solve_mpir_dev(bool spd, bool lower, int n, int nrhs, const double *A
 int gesv_mpir_dev(int n, int nrhs, const double *A, long lda, const double *B, long ldb,
                   double *X, long ldx, const MpirOpts &o, MpirResult *res, cudaStream_t s) {
   return solve_mpir_dev(false, false, n, nrhs, A, lda, B, ldb, X, ldx, o, res, s);
+}
+
+int gesv_mpir_host(int n, int nrhs, const double *Ah, long ldh, double *Ad, const double *B,
+                   long ldb, double *X, long ldx, const MpirOpts &o, MpirResult *res,
+                   cudaStream_t s) {
+  if (!mixed_streams_host(n, o)) {
+    set_last_error("gesv_mpir_host: needs n >= %d and BF16x3 updates", kChunkMinN);
+    return kErrInvalid;
+  }
+  return solve_mpir_dev(false, false, n, nrhs, Ad, n, B, ldb, X, ldx, o, res, s, Ah, ldh);
 }
 
 int posv_mpir_dev(bool lower, int n, int nrhs, const double *A, long lda, const double *B,
