@@ -88,3 +88,31 @@ def test_streamed_host_solve_repeats_and_interleaves():
     r = b.cuda() - A1d @ x2.cuda()
     scale = A1d.abs().sum(1).max() * x2.cuda().abs().max() + b.cuda().abs().max()
     assert float(r.abs().max() / scale) <= 1e-13
+
+
+def test_streamed_host_solve_repeats_bitwise_at_n32768():
+    """The streamed path at n = 32768 keeps about nine streams busy beside the
+    factorization, so the thread-block-cluster panel's CTAs share SMs with
+    other kernels and drift apart in time.  Repeated solves must stay bit for
+    bit those of the device-pointer solve: this caught a missing cluster
+    barrier in the panel (a late CTA read rows of A12 that CTA 0 had already
+    replaced by U12), which changed pivots in about four solves of ten."""
+    import torch
+    L = zg.lib()
+    n = 32768
+    g = torch.Generator(device="cuda").manual_seed(1)
+    Ad = torch.randn(n, n, dtype=torch.float64, device="cuda", generator=g)
+    bd = torch.rand(n, 1, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+    Ah = torch.empty(n, n, dtype=torch.float64).pin_memory()
+    Ah.copy_(Ad)
+    bh = bd.cpu().pin_memory()
+    xd = torch.zeros(n, 1, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    rd = _solve(L, n, n, Ad.data_ptr(), bd.data_ptr(), xd.data_ptr())
+    assert rd.converged == 1 and rd.fp64_fallback == 0
+    x_ref = xd.cpu()
+    xh = torch.zeros(n, 1, dtype=torch.float64).pin_memory()
+    for _ in range(6):
+        rh = _solve(L, n, n, Ah.data_ptr(), bh.data_ptr(), xh.data_ptr())
+        assert rh.fp64_fallback == 0 and rh.iters == rd.iters
+        assert torch.equal(xh, x_ref)

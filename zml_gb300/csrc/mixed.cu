@@ -395,7 +395,9 @@ int chunk_streams(cudaStream_t s, int nblocks, ChunkStreams **out) {
 
 // The geometry of one streamed factorization (BF16x3 updates, NB = 256).
 struct ChunkPlan {
-  int w = 0, nck = 0;                  // chunk width (a multiple of 512 columns), chunk count
+  int nck = 0;                         // chunk count
+  int c0[ChunkStreams::kMax + 1] = {}; // chunk c: columns c0[c] .. c0[c+1]-1 (512-multiples)
+  int wmax = 0;                        // widest chunk
   int join[ChunkStreams::kMax] = {};   // block before whose interchanges chunk c joins
   int bmax = 0;                        // blocks 0 .. bmax-1 keep their operands for replays
   uint16_t *savedL = nullptr;          // their L21 operands, one after the other
@@ -413,7 +415,7 @@ static int replay_block(const ChunkPlan &cp, int c, int b, int n, float *A, long
                         const int *ipiv, unsigned *status) {
   constexpr int NB = 256, ldk = NB;
   constexpr long ldo = 3L * ldk;
-  const int j = b * NB, c0 = c * cp.w, wc = std::min(cp.w, n - c0);
+  const int j = b * NB, c0 = cp.c0[c], wc = cp.c0[c + 1] - c0;
   const cudaStream_t st = cp.cs->ck[c];
   ZG_CUDA(cudaStreamWaitEvent(st, cp.cs->ops[b], 0));
   float *Ac = A + (long)c0 * lda;
@@ -548,7 +550,7 @@ static int getrf_lowp_blocks(int n, float *A, long lda, int *ipiv, int prec, Con
     // chunks due now join, caught up through block b-1
     while (cp && joined < cp->nck && cp->join[joined] <= b) {
       ZG_CUDA(cudaStreamWaitEvent(sp, cp->cs->caught[joined], 0));
-      lim = std::min(n, (joined + 1) * cp->w);
+      lim = cp->c0[joined + 1];
       ++joined;
     }
     ZG_TRY(laswp_panel<float>(j, j + jb, lim, A, lda, j + 1, j + jb, ipiv, sp));
@@ -1308,12 +1310,23 @@ static int getrf_lowp_host(int n, const double *Ah, long ldh, double *Ad, float 
   ZG_TRY(chunk_streams(s, ceil_div(n, NB), &cs));
   ChunkPlan cp;
   cp.cs = cs;
-  cp.w = ceil_div(ceil_div(n, ChunkStreams::kMax), kGemvCols) * kGemvCols;
-  cp.nck = ceil_div(n, cp.w);
-  // a chunk joins one chunk width before its first block, so its replays run
-  // beside the factorization of the chunk before it
-  const int lag = cp.w / NB;
-  for (int c = 0; c < cp.nck; ++c) cp.join[c] = std::max(0, c * cp.w / NB - lag);
+  // a 512-column first chunk (the first panel waits only for it), the rest
+  // in equal chunks of whole 512-column groups
+  const int rest = ceil_div(ceil_div(n - kGemvCols, ChunkStreams::kMax - 1), kGemvCols) *
+                   kGemvCols;
+  cp.c0[0] = 0;
+  cp.c0[1] = kGemvCols;
+  cp.nck = 1;
+  while (cp.c0[cp.nck] < n) {
+    cp.c0[cp.nck + 1] = std::min(n, cp.c0[cp.nck] + rest);
+    ++cp.nck;
+  }
+  // a chunk joins at the first block of the chunk before it, so its replays
+  // run beside the factorization of that chunk
+  for (int c = 0; c < cp.nck; ++c) {
+    cp.join[c] = c == 0 ? 0 : cp.c0[c - 1] / NB;
+    cp.wmax = std::max(cp.wmax, cp.c0[c + 1] - cp.c0[c]);
+  }
   cp.bmax = cp.join[cp.nck - 1];
   cp.offL.resize(cp.bmax + 1);
   size_t tot = 0;
@@ -1329,7 +1342,7 @@ static int getrf_lowp_host(int n, const double *Ah, long ldh, double *Ad, float 
   // allocation (nor its synchronisation) between the queued copies
   for (int c = 0; c < cp.nck; ++c) {
     void *t;
-    ZG_TRY(workspace(cs->ck[c], kSlotU16, sizeof(uint16_t) * (size_t)cp.w * ldo, &t));
+    ZG_TRY(workspace(cs->ck[c], kSlotU16, sizeof(uint16_t) * (size_t)cp.wmax * ldo, &t));
     ZG_TRY(laswp_reserve(cs->ck[c]));
   }
   // everything after the caller's earlier work, which may still read Ad, LU
@@ -1339,16 +1352,16 @@ static int getrf_lowp_host(int n, const double *Ah, long ldh, double *Ad, float 
   ZG_CUDA(cudaStreamWaitEvent(la->panel, la->first, 0));
   ZG_CUDA(cudaStreamWaitEvent(la->bulk, la->first, 0));
   for (int c = 0; c < cp.nck; ++c) {
-    const long c0 = (long)c * cp.w;
-    const int wc = std::min<long>(cp.w, n - c0);
+    const long c0 = cp.c0[c];
+    const int wc = cp.c0[c + 1] - cp.c0[c];
     ZG_CUDA(cudaMemcpy2DAsync(Ad + c0 * n, sizeof(double) * n, Ah + c0 * ldh,
                               sizeof(double) * ldh, sizeof(double) * n, wc,
                               cudaMemcpyHostToDevice, cs->copy));
     ZG_CUDA(cudaEventRecord(cs->copied[c], cs->copy));
   }
   for (int c = 0; c < cp.nck; ++c) {
-    const long c0 = (long)c * cp.w;
-    const int wc = std::min<long>(cp.w, n - c0);
+    const long c0 = cp.c0[c];
+    const int wc = cp.c0[c + 1] - cp.c0[c];
     const cudaStream_t st = cs->ck[c];
     ZG_CUDA(cudaStreamWaitEvent(st, cs->copied[c], 0));
     ZG_LAUNCH(kTagConvert, 0, 12.0 * n * wc, st,

@@ -763,6 +763,10 @@ __global__ void __launch_bounds__(kPcThreads, 1)
         }
       }
       __syncthreads();
+      // every CTA holds its copy of A12 before CTA 0 overwrites those rows
+      // with U12 below: without this barrier a CTA slowed by other work on
+      // its SM could load rows already solved and solve them a second time
+      cl_sync();
       if (tid < nr) {
         E u[W];
 #pragma unroll
