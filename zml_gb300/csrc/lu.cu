@@ -235,71 +235,59 @@ int panel_lu(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Control *c
 }
 
 // Row interchanges (laswp.zig:12-96).  The sequence of swaps k1..k2 (1-based,
-// forward for incx > 0, backward otherwise) is first composed by one warp
-// into a list of (destination row, source row) pairs -- at most 2 (k2-k1+1)
-// rows move -- and then every column gathers its moved rows and scatters
-// them in parallel, so no column walks a chain of dependent swaps.
+// forward for incx > 0, backward otherwise) is first composed into a list of
+// (destination row, source row) pairs -- at most 2 (k2-k1+1) rows move -- and
+// then every column gathers its moved rows and scatters them in parallel, so
+// no column walks a chain of dependent swaps.
 constexpr int kSwapMax = 256;  // pivots per composed chunk
 
+// The composition, one thread per row that can move: the rows k1-1 .. k2-1
+// and every row outside them that a pivot names (at its first occurrence).
+// Each traces back through the swaps to the row whose content it ends with;
+// the traces are independent, so the block's cost is one pass over the
+// pivots instead of a chain of dependent swaps in shared memory.  A row that
+// keeps its content emits no pair; the pairs' order does not matter (the
+// apply kernel loads every source before it stores).
 __global__ void __launch_bounds__(256) laswp_prep_kernel(int k1, int k2,
                                                          const int *__restrict__ ipiv, int incx,
                                                          int *pairs, int *npairs) {
-  __shared__ int seg[kSwapMax];    // content of rows base .. base+len-1
-  __shared__ int piv[kSwapMax];    // the chunk's pivots (0-based target rows)
-  __shared__ int first[kSwapMax];  // for an outside target: index of its first occurrence
-  __shared__ int ocont[kSwapMax];  // content of the outside row first named at that index
+  __shared__ int piv[kSwapMax];  // the chunk's pivots (0-based target rows)
   __shared__ int np;
   const int t = threadIdx.x;
   const int base = k1 - 1, len = k2 - k1 + 1;
   if (t == 0) np = 0;
-  for (int i = t; i < len; i += blockDim.x) {
-    seg[i] = base + i;
-    piv[i] = ipiv[base + i] - 1;
-  }
+  for (int i = t; i < len; i += blockDim.x) piv[i] = ipiv[base + i] - 1;
   __syncthreads();
-  // outside targets: the first index naming the same row owns its slot
-  for (int i = t; i < len; i += blockDim.x) {
-    const int p = piv[i];
-    int f = -1;
-    if (p < base || p >= base + len) {
-      f = i;
-      for (int j = 0; j < i; ++j)
-        if (piv[j] == p) { f = j; break; }
-      if (f == i) ocont[i] = p;
+  for (int e = t; e < 2 * len; e += blockDim.x) {
+    int x;  // a destination row
+    if (e < len) {
+      x = base + e;
+    } else {
+      const int i = e - len, p = piv[i];
+      if (p >= base && p < base + len) continue;
+      bool first = true;
+      for (int j = 0; j < i && first; ++j) first = piv[j] != p;
+      if (!first) continue;
+      x = p;
     }
-    first[i] = f;
-  }
-  __syncthreads();
-  // the interchanges in application order, shared memory only
-  if (t == 0) {
-    for (int st = 0; st < len; ++st) {
-      const int i = incx > 0 ? st : len - 1 - st;
-      const int p = piv[i];
-      if (p == base + i) continue;
-      const int f = first[i];
-      if (f < 0) {
-        const int q = p - base, tmp = seg[i];
-        seg[i] = seg[q];
-        seg[q] = tmp;
-      } else {
-        const int tmp = seg[i];
-        seg[i] = ocont[f];
-        ocont[f] = tmp;
+    // content of x after the swaps = content of y before them: x taken back
+    // through the swaps in reverse order of application
+    int y = x;
+    if (incx > 0) {
+      for (int q = len - 1; q >= 0; --q) {
+        const int k = base + q, p = piv[q];
+        y = y == k ? p : (y == p ? k : y);
+      }
+    } else {
+      for (int q = 0; q < len; ++q) {
+        const int k = base + q, p = piv[q];
+        y = y == k ? p : (y == p ? k : y);
       }
     }
-  }
-  __syncthreads();
-  // every row whose content changed is one (destination, source) pair
-  for (int i = t; i < len; i += blockDim.x) {
-    if (seg[i] != base + i) {
-      const int k = atomicAdd(&np, 1);
-      pairs[2 * k] = base + i;
-      pairs[2 * k + 1] = seg[i];
-    }
-    if (first[i] == i && ocont[i] != piv[i]) {
-      const int k = atomicAdd(&np, 1);
-      pairs[2 * k] = piv[i];
-      pairs[2 * k + 1] = ocont[i];
+    if (y != x) {
+      const int c = atomicAdd(&np, 1);
+      pairs[2 * c] = x;
+      pairs[2 * c + 1] = y;
     }
   }
   __syncthreads();
