@@ -116,3 +116,31 @@ def test_streamed_host_solve_repeats_bitwise_at_n32768():
         rh = _solve(L, n, n, Ah.data_ptr(), bh.data_ptr(), xh.data_ptr())
         assert rh.fp64_fallback == 0 and rh.iters == rd.iters
         assert torch.equal(xh, x_ref)
+
+
+@pytest.mark.parametrize("n,prec", [(1000, BF16X3), (4096, 2)])
+def test_pinned_host_below_streaming_scope_equals_device(n, prec):
+    """Page-locked A outside the streamed path's scope (n < 4096, or factors
+    other than BF16x3) is staged whole first and gives the device solve."""
+    import torch
+    L = zg.lib()
+    g = torch.Generator().manual_seed(n + prec)
+    A = torch.randn(n, n, dtype=torch.float64, generator=g)
+    b = torch.rand(n, 1, dtype=torch.float64, generator=g) * 2 - 1
+
+    def solve(a, bb, xx):
+        res = zg.MpirResult()
+        rc = L.zml_dgesv_mpir(102, n, 1, a, n, bb, n, xx, n, prec, GMRES, 64 * 2.0 ** -53, 30,
+                              C.byref(res))
+        assert rc == 0, zg.last_error()
+        return res
+
+    Ad, bd = A.cuda(), b.cuda()
+    xd = torch.zeros(n, 1, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    rd = solve(Ad.data_ptr(), bd.data_ptr(), xd.data_ptr())
+    Ah, bh = A.pin_memory(), b.pin_memory()
+    xh = torch.zeros(n, 1, dtype=torch.float64).pin_memory()
+    rh = solve(Ah.data_ptr(), bh.data_ptr(), xh.data_ptr())
+    assert rd.converged == 1 and rh.iters == rd.iters and rh.berr == rd.berr
+    assert torch.equal(xh, xd.cpu())

@@ -363,7 +363,7 @@ int lookahead(cudaStream_t s, Lookahead **out) {
 struct ChunkStreams {
   static constexpr int kMax = 8;
   cudaStream_t copy = nullptr, ck[kMax] = {};
-  cudaEvent_t copied[kMax] = {}, caught[kMax] = {};
+  cudaEvent_t copied[kMax] = {}, caught[kMax] = {}, copy_end = nullptr;
   std::vector<cudaEvent_t> ops;  // block b's saved operands and pivots are final
 };
 std::map<std::pair<int, cudaStream_t>, ChunkStreams> g_cs;
@@ -378,6 +378,7 @@ int chunk_streams(cudaStream_t s, int nblocks, ChunkStreams **out) {
     int least = 0, greatest = 0;
     ZG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
     ZG_CUDA(cudaStreamCreateWithFlags(&c.copy, cudaStreamNonBlocking));
+    ZG_CUDA(cudaEventCreateWithFlags(&c.copy_end, fl));
     for (int q = 0; q < ChunkStreams::kMax; ++q) {
       ZG_CUDA(cudaStreamCreateWithPriority(&c.ck[q], cudaStreamNonBlocking, least));
       ZG_CUDA(cudaEventCreateWithFlags(&c.copied[q], fl));
@@ -1295,6 +1296,34 @@ struct MpirCtx {
   IRWork w{};
 };
 
+// The queued part of getrf_lowp_host: the chunk copies, the conversions and
+// the factorization with its replays (the caller joins every stream after it).
+static int chunked_factor(int n, const double *Ah, long ldh, double *Ad, float *LU, int *ipiv,
+                          float *rpart, Control *ctl, cudaStream_t s, Lookahead &la,
+                          ChunkPlan &cp) {
+  ChunkStreams *cs = cp.cs;
+  for (int c = 0; c < cp.nck; ++c) {
+    const long c0 = cp.c0[c];
+    const int wc = cp.c0[c + 1] - cp.c0[c];
+    ZG_CUDA(cudaMemcpy2DAsync(Ad + c0 * n, sizeof(double) * n, Ah + c0 * ldh,
+                              sizeof(double) * ldh, sizeof(double) * n, wc,
+                              cudaMemcpyHostToDevice, cs->copy));
+    ZG_CUDA(cudaEventRecord(cs->copied[c], cs->copy));
+  }
+  for (int c = 0; c < cp.nck; ++c) {
+    const long c0 = cp.c0[c];
+    const int wc = cp.c0[c + 1] - cp.c0[c];
+    const cudaStream_t st = cs->ck[c];
+    ZG_CUDA(cudaStreamWaitEvent(st, cs->copied[c], 0));
+    ZG_LAUNCH(kTagConvert, 0, 12.0 * n * wc, st,
+              d2s_rowabs_kernel<<<dim3(ceil_div(n, kGemvRows), ceil_div(wc, kGemvCols)),
+                                  kGemvRows, 0, st>>>(n, wc, Ad + c0 * n, n, LU + c0 * n, n,
+                                                      rpart + (c0 / kGemvCols) * n));
+    if (cp.join[c] == 0) ZG_CUDA(cudaEventRecord(cs->caught[c], st));
+  }
+  return getrf_lowp_blocks(n, LU, n, ipiv, kPrecBF16x3, ctl, s, la, &cp);
+}
+
 // BF16x3 LU of an n x n A that arrives from pinned host memory (column-major,
 // ld ldh): its FP64 copy lands in Ad (ld n) and its FP32 copy in LU (ld n),
 // with the row sums of |A| as 512-column partials in rpart, chunk by chunk,
@@ -1351,37 +1380,20 @@ static int getrf_lowp_host(int n, const double *Ah, long ldh, double *Ad, float 
   ZG_CUDA(cudaStreamWaitEvent(cs->copy, la->first, 0));
   ZG_CUDA(cudaStreamWaitEvent(la->panel, la->first, 0));
   ZG_CUDA(cudaStreamWaitEvent(la->bulk, la->first, 0));
-  for (int c = 0; c < cp.nck; ++c) {
-    const long c0 = cp.c0[c];
-    const int wc = cp.c0[c + 1] - cp.c0[c];
-    ZG_CUDA(cudaMemcpy2DAsync(Ad + c0 * n, sizeof(double) * n, Ah + c0 * ldh,
-                              sizeof(double) * ldh, sizeof(double) * n, wc,
-                              cudaMemcpyHostToDevice, cs->copy));
-    ZG_CUDA(cudaEventRecord(cs->copied[c], cs->copy));
-  }
-  for (int c = 0; c < cp.nck; ++c) {
-    const long c0 = cp.c0[c];
-    const int wc = cp.c0[c + 1] - cp.c0[c];
-    const cudaStream_t st = cs->ck[c];
-    ZG_CUDA(cudaStreamWaitEvent(st, cs->copied[c], 0));
-    ZG_LAUNCH(kTagConvert, 0, 12.0 * n * wc, st,
-              d2s_rowabs_kernel<<<dim3(ceil_div(n, kGemvRows), ceil_div(wc, kGemvCols)),
-                                  kGemvRows, 0, st>>>(n, wc, Ad + c0 * n, n, LU + c0 * n, n,
-                                                      rpart + (c0 / kGemvCols) * n));
-    if (cp.join[c] == 0) ZG_CUDA(cudaEventRecord(cs->caught[c], st));
-  }
-  const int rc = getrf_lowp_blocks(n, LU, n, ipiv, kPrecBF16x3, ctl, s, *la, &cp);
-  // the caller's stream resumes after every internal stream (also when the
-  // loop stopped early and left chunks unjoined)
-  ZG_CUDA(cudaEventRecord(la->end_panel, la->panel));
-  ZG_CUDA(cudaEventRecord(la->end_bulk, la->bulk));
-  ZG_CUDA(cudaStreamWaitEvent(s, la->end_panel, 0));
-  ZG_CUDA(cudaStreamWaitEvent(s, la->end_bulk, 0));
-  for (int c = 0; c < cp.nck; ++c) {
-    ZG_CUDA(cudaEventRecord(cs->caught[c], cs->ck[c]));
-    ZG_CUDA(cudaStreamWaitEvent(s, cs->caught[c], 0));
-  }
-  return rc;
+  const int rc = chunked_factor(n, Ah, ldh, Ad, LU, ipiv, rpart, ctl, s, *la, cp);
+  // the caller's stream resumes after every internal stream, also after a
+  // failure part way (no copy from the caller's buffer may outlive the call)
+  int jrc = 0;
+  auto join = [&](cudaEvent_t e, cudaStream_t from) {
+    if (cudaEventRecord(e, from) != cudaSuccess || cudaStreamWaitEvent(s, e, 0) != cudaSuccess)
+      jrc = kErrCuda;
+  };
+  join(cs->copy_end, cs->copy);
+  join(la->end_panel, la->panel);
+  join(la->end_bulk, la->bulk);
+  for (int c = 0; c < cp.nck; ++c) join(cs->caught[c], cs->ck[c]);
+  if (jrc != 0) set_last_error("getrf_lowp_host: joining the internal streams failed");
+  return rc != 0 ? rc : jrc;
 }
 
 bool mixed_streams_host(int n, const MpirOpts &o) {
