@@ -27,6 +27,8 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <map>
+#include <mutex>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -340,19 +342,89 @@ int dgemm_oz_sub(int m, int n, int k, const double *A, long lda, const double *B
 // A22 -= L21 U12 -- nearly all of the flops -- runs on the tensor cores
 // through dgemm_oz_sub, as does the half-panel update (k = 128).  Every wait
 // reports into one status word, read once at the end.
+namespace {
+// Lookahead streams of the slice LU, one set per (device, caller stream),
+// created on first use and kept: a high-priority panel stream and a
+// low-priority bulk stream, with the events that order them.
+struct OzLookahead {
+  static constexpr int kRing = 4;
+  cudaStream_t panel = nullptr, bulk = nullptr;
+  cudaEvent_t first = nullptr, upd[kRing] = {}, bulk_done[kRing] = {}, end_panel = nullptr,
+              end_bulk = nullptr;
+};
+std::mutex g_ozla_mu;
+std::map<std::pair<int, cudaStream_t>, OzLookahead> g_ozla;
+
+int oz_lookahead(cudaStream_t s, OzLookahead **out) {
+  int dev = 0;
+  ZG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_ozla_mu);
+  OzLookahead &l = g_ozla[{dev, s}];
+  if (!l.panel) {
+    int least = 0, greatest = 0;
+    ZG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    ZG_CUDA(cudaStreamCreateWithPriority(&l.panel, cudaStreamNonBlocking, greatest));
+    ZG_CUDA(cudaStreamCreateWithPriority(&l.bulk, cudaStreamNonBlocking, least));
+    const unsigned fl = cudaEventDisableTiming;
+    ZG_CUDA(cudaEventCreateWithFlags(&l.first, fl));
+    ZG_CUDA(cudaEventCreateWithFlags(&l.end_panel, fl));
+    ZG_CUDA(cudaEventCreateWithFlags(&l.end_bulk, fl));
+    for (int q = 0; q < OzLookahead::kRing; ++q) {
+      ZG_CUDA(cudaEventCreateWithFlags(&l.upd[q], fl));
+      ZG_CUDA(cudaEventCreateWithFlags(&l.bulk_done[q], fl));
+    }
+  }
+  *out = &l;
+  return 0;
+}
+}  // namespace
+
+static int getrf_oz_blocks(int m, int n, double *A, long lda, int *ipiv, Control *ctl,
+                           OzLookahead &la);
+
 int getrf_oz(int m, int n, double *A, long lda, int *ipiv, int *info, cudaStream_t s) {
-  constexpr int NB = 256;
   *info = 0;
+  Control *ctl;
+  ZG_TRY(control(s, &ctl));
+  OzLookahead *la;
+  ZG_TRY(oz_lookahead(s, &la));
+  // both internal streams start after the caller's earlier work, and the
+  // caller's stream resumes after both (also after a failure part way)
+  ZG_CUDA(cudaEventRecord(la->first, s));
+  ZG_CUDA(cudaStreamWaitEvent(la->panel, la->first, 0));
+  ZG_CUDA(cudaStreamWaitEvent(la->bulk, la->first, 0));
+  const int rc = getrf_oz_blocks(m, n, A, lda, ipiv, ctl, *la);
+  ZG_CUDA(cudaEventRecord(la->end_panel, la->panel));
+  ZG_CUDA(cudaEventRecord(la->end_bulk, la->bulk));
+  ZG_CUDA(cudaStreamWaitEvent(s, la->end_panel, 0));
+  ZG_CUDA(cudaStreamWaitEvent(s, la->end_bulk, 0));
+  if (rc != 0) return rc;
+  return check_status(s, ctl, info);
+}
+
+// The blocks of getrf_oz.  Lookahead: a block's trailing update is split into
+// the next block's columns (triangular solve and slice GEMM on the panel
+// stream) and the rest (on the bulk stream), so the bulk of the update runs
+// beside the next block's panels.  Block b's panels wait for the bulk update
+// of block b-2, the last to touch their columns; block b's full-width
+// interchanges for that of block b-1, which still reads block b-1's L21.
+// Splitting the columns changes no element's arithmetic: the slices scale
+// by rows of L21 and by columns of U12, and each column of the triangular
+// solve is independent.
+static int getrf_oz_blocks(int m, int n, double *A, long lda, int *ipiv, Control *ctl,
+                           OzLookahead &la) {
+  constexpr int NB = 256;
+  constexpr int R = OzLookahead::kRing;
+  const cudaStream_t s = la.panel, sb = la.bulk;
   const int mn = std::min(m, n);
   // sub-panel width: 64 columns.  On GB300 a panel's FP64 arithmetic runs on
   // the few SMs of its cluster at the FP64 pipe's rate, so narrower panels,
   // with the slice update between them on the tensor cores, cost less
   const int NBP = 64;
-  Control *ctl;
-  ZG_TRY(control(s, &ctl));
-  for (int j = 0; j < mn; j += NB) {
+  for (int j = 0, b = 0; j < mn; j += NB, ++b) {
     const int jb = std::min(NB, mn - j);
     double *Ab = A + (long)j * lda;  // the block's columns
+    if (b >= 2) ZG_CUDA(cudaStreamWaitEvent(s, la.bulk_done[(b - 2) % R], 0));
     for (int p = 0; p < jb; p += NBP) {
       const int r = j + p, pb = std::min(NBP, jb - p), right = jb - p - pb;
       double *Arr = A + r + (long)r * lda;
@@ -375,18 +447,34 @@ int getrf_oz(int m, int n, double *A, long lda, int *ipiv, int *info, cudaStream
       }
     }
     // the block's interchanges in every column outside it
+    if (b >= 1) ZG_CUDA(cudaStreamWaitEvent(s, la.bulk_done[(b - 1) % R], 0));
     ZG_TRY(laswp_panel<double>(j, std::min(n, j + jb), n, A, lda, j + 1, j + jb, ipiv, s));
-    if (j + jb < n) {
+    const int rest = n - j - jb;
+    if (rest > 0) {
       double *Ajj = A + j + (long)j * lda;
       double *A12 = A + j + (long)(j + jb) * lda;
-      ZG_TRY(trsm_dev<double>(kLeft, kLower, kNoTrans, kUnit, jb, n - j - jb, 1.0, Ajj, lda, A12,
-                              lda, s));
+      // the next block's columns now, on the panel stream ...
+      const int near = std::min(NB, rest);
+      ZG_TRY(trsm_dev<double>(kLeft, kLower, kNoTrans, kUnit, jb, near, 1.0, Ajj, lda, A12, lda,
+                              s));
       if (j + jb < m)
-        ZG_TRY(dgemm_oz_sub(m - j - jb, n - j - jb, jb, Ajj + jb, lda, A12, lda, A12 + jb, lda,
-                            false, &ctl->status, s));
+        ZG_TRY(dgemm_oz_sub(m - j - jb, near, jb, Ajj + jb, lda, A12, lda, A12 + jb, lda, false,
+                            &ctl->status, s));
+      // ... the rest on the bulk stream, beside the next block's panels
+      if (rest > near) {
+        ZG_CUDA(cudaEventRecord(la.upd[b % R], s));
+        ZG_CUDA(cudaStreamWaitEvent(sb, la.upd[b % R], 0));
+        double *A12f = A12 + (long)near * lda;
+        ZG_TRY(trsm_dev<double>(kLeft, kLower, kNoTrans, kUnit, jb, rest - near, 1.0, Ajj, lda,
+                                A12f, lda, sb));
+        if (j + jb < m)
+          ZG_TRY(dgemm_oz_sub(m - j - jb, rest - near, jb, Ajj + jb, lda, A12f, lda, A12f + jb,
+                              lda, false, &ctl->status, sb));
+      }
     }
+    ZG_CUDA(cudaEventRecord(la.bulk_done[b % R], sb));
   }
-  return check_status(s, ctl, info);
+  return 0;
 }
 
 // FP64 Cholesky A = L L^T (lower), right-looking with NB = 256: the diagonal
