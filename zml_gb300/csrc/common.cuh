@@ -114,7 +114,8 @@ enum Slot : int {
   kSlotOzA = 26, kSlotOzB = 27,  // FP64-by-slices GEMM: the BF16 slices of A and B, exponents
   kSlotOzC = 28,              // FP64-by-slices GEMM: the FP32 accumulators
   kSlotChunk = 29,            // mixed LU of a host A: the replayed blocks' 16-bit operands
-  kNumSlots = 30
+  kSlotOzT = 30,              // FP64 slice Cholesky: the next block's L21 rows, transposed
+  kNumSlots = 31
 };
 
 // Returns a device buffer of at least `bytes` bound to `stream` in `slot`.

@@ -481,24 +481,69 @@ static int getrf_oz_blocks(int m, int n, double *A, long lda, int *ipiv, Control
 // block by the FP64-pipe potrf (64-wide steps), the block column by a
 // triangular solve, and the trailing SYRK A22 -= L21 L21^T on the tensor cores
 // through dgemm_oz_sub's lower form.  The first non-positive pivot lands in
-// info (1-based), as potrf2.zig:37-47 reports it.
-int potrf_oz(int n, double *A, long lda, int *info, cudaStream_t s) {
+// info (1-based), as potrf2.zig:37-47 reports it.  Lookahead as in getrf_oz:
+// the next block's columns (its diagonal block by the lower SYRK, the rows
+// below it by a GEMM against its rows of L21 transposed) on the panel stream,
+// the rest of the SYRK on the bulk stream.  Block b's diagonal block and
+// triangular solve wait for block b-2's bulk update, the last to touch their
+// columns; block b's near update waits for block b-1's, which updates the same
+// columns.  The strictly upper triangle is never written.
+static int potrf_oz_blocks(int n, double *A, long lda, Control *ctl, OzLookahead &la) {
   constexpr int NB = 256;
+  constexpr int R = OzLookahead::kRing;
+  const cudaStream_t sp = la.panel, sb = la.bulk;
+  void *wt;
+  ZG_TRY(workspace(sp, kSlotOzT, sizeof(double) * NB * NB, &wt));
+  double *T = (double *)wt;
+  for (int j = 0, b = 0; j < n; j += NB, ++b) {
+    const int jb = std::min(NB, n - j);
+    double *Ajj = A + j + (long)j * lda;
+    if (b >= 2) ZG_CUDA(cudaStreamWaitEvent(sp, la.bulk_done[(b - 2) % R], 0));
+    ZG_TRY(potrf_launch<double>(kLower, jb, Ajj, lda, ctl, j, sp));
+    const int rest = n - j - jb;
+    if (rest > 0) {
+      double *A21 = Ajj + jb;
+      ZG_TRY(trsm_dev<double>(kRight, kLower, kTrans, kNonUnit, rest, jb, 1.0, Ajj, lda, A21, lda,
+                              sp));
+      // the next block's columns now, on the panel stream, once block b-1's
+      // bulk update (which also updates them) is done ...
+      if (b >= 1) ZG_CUDA(cudaStreamWaitEvent(sp, la.bulk_done[(b - 1) % R], 0));
+      const int near = std::min(NB, rest);
+      ZG_TRY(dgemm_oz_sub(near, near, jb, A21, lda, nullptr, 0, A21 + (long)jb * lda, lda, true,
+                          &ctl->status, sp));
+      if (rest > near) {
+        ZG_TRY(transpose_dev<double>(near, jb, A21, lda, T, jb, sp));
+        ZG_TRY(dgemm_oz_sub(rest - near, near, jb, A21 + near, lda, T, jb,
+                            A21 + near + (long)jb * lda, lda, false, &ctl->status, sp));
+        // ... the rest on the bulk stream, beside the next block's diagonal
+        // block and triangular solve
+        ZG_CUDA(cudaEventRecord(la.upd[b % R], sp));
+        ZG_CUDA(cudaStreamWaitEvent(sb, la.upd[b % R], 0));
+        ZG_TRY(dgemm_oz_sub(rest - near, rest - near, jb, A21 + near, lda, nullptr, 0,
+                            A21 + near + (long)(jb + near) * lda, lda, true, &ctl->status, sb));
+      }
+    }
+    ZG_CUDA(cudaEventRecord(la.bulk_done[b % R], sb));
+  }
+  return 0;
+}
+
+int potrf_oz(int n, double *A, long lda, int *info, cudaStream_t s) {
   *info = 0;
   if (n <= 0) return 0;
   Control *ctl;
   ZG_TRY(control(s, &ctl));
-  for (int j = 0; j < n; j += NB) {
-    const int jb = std::min(NB, n - j);
-    double *Ajj = A + j + (long)j * lda;
-    ZG_TRY(potrf_launch<double>(kLower, jb, Ajj, lda, ctl, j, s));
-    const int rest = n - j - jb;
-    if (rest <= 0) break;
-    double *A21 = Ajj + jb;
-    ZG_TRY(trsm_dev<double>(kRight, kLower, kTrans, kNonUnit, rest, jb, 1.0, Ajj, lda, A21, lda, s));
-    ZG_TRY(dgemm_oz_sub(rest, rest, jb, A21, lda, nullptr, 0, A21 + (long)jb * lda, lda, true,
-                        &ctl->status, s));
-  }
+  OzLookahead *la;
+  ZG_TRY(oz_lookahead(s, &la));
+  ZG_CUDA(cudaEventRecord(la->first, s));
+  ZG_CUDA(cudaStreamWaitEvent(la->panel, la->first, 0));
+  ZG_CUDA(cudaStreamWaitEvent(la->bulk, la->first, 0));
+  const int rc = potrf_oz_blocks(n, A, lda, ctl, *la);
+  ZG_CUDA(cudaEventRecord(la->end_panel, la->panel));
+  ZG_CUDA(cudaEventRecord(la->end_bulk, la->bulk));
+  ZG_CUDA(cudaStreamWaitEvent(s, la->end_panel, 0));
+  ZG_CUDA(cudaStreamWaitEvent(s, la->end_bulk, 0));
+  if (rc != 0) return rc;
   return check_status(s, ctl, info);
 }
 
