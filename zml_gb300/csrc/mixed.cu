@@ -603,31 +603,76 @@ static int getrf_lowp_blocks(int n, float *A, long lda, int *ipiv, int prec, Con
 // Low-precision Cholesky (lower) of an n x n SPD FP32 matrix: FP32 64-wide
 // diagonal blocks, FP32 block-column TRSM, trailing SYRK on the tensor cores
 // (lower 128 x 128 tiles only), NB = 256.  The first non-positive pivot lands
-// in ctl->info.
-int potrf_lowp(int n, float *A, long lda, int prec, Control *ctl, cudaStream_t s) {
-  if (n <= 0) return 0;
+// in ctl->info.  Lookahead as in getrf_lowp: the next block's columns (its
+// diagonal tiles and the rows below them) on the panel stream, the rest of
+// the SYRK on the bulk stream.  Block b's diagonal block waits for block b-2's
+// bulk update, the last to touch its columns; block b's near update for block
+// b-1's, which updates the same columns; the 16-bit operand buffers alternate
+// by block parity.  The tiles computed and every tile's arithmetic are those
+// of one SYRK over the whole trailing matrix.
+static int potrf_lowp_blocks(int n, float *A, long lda, int prec, Control *ctl, cudaStream_t s,
+                             Lookahead &la) {
   constexpr int NB = 256;
-  if (prec == kPrecFP32) return potrf_launch<float>(kLower, n, A, lda, ctl, 0, s);
+  constexpr int R = Lookahead::kRing;
+  const cudaStream_t sp = la.panel, sb = la.bulk;
   const int segs = prec == kPrecBF16x3 ? 3 : 1;
-  void *wl, *wu;
-  ZG_TRY(workspace(s, kSlotL16, sizeof(uint16_t) * (size_t)n * NB * segs, &wl));
-  ZG_TRY(workspace(s, kSlotU16, sizeof(uint16_t) * (size_t)n * NB * segs, &wu));
-  for (int j = 0; j < n; j += NB) {
+  const size_t nop = (size_t)n * NB * segs;
+  void *wl0, *wu0;
+  ZG_TRY(workspace(s, kSlotL16, sizeof(uint16_t) * 2 * nop, &wl0));
+  ZG_TRY(workspace(s, kSlotU16, sizeof(uint16_t) * 2 * nop, &wu0));
+  const int abt = prec == kPrecFP16 ? 0 : 1;
+  for (int j = 0, b = 0; j < n; j += NB, ++b) {
     const int jb = std::min(NB, n - j);
     float *Ajj = A + j + (long)j * lda;
-    ZG_TRY(potrf_launch<float>(kLower, jb, Ajj, lda, ctl, j, s));
+    uint16_t *wl = (uint16_t *)wl0 + (b & 1) * nop, *wu = (uint16_t *)wu0 + (b & 1) * nop;
+    if (b >= 2) ZG_CUDA(cudaStreamWaitEvent(sp, la.bulk_done[(b - 2) % R], 0));
+    ZG_TRY(potrf_launch<float>(kLower, jb, Ajj, lda, ctl, j, sp));
     const int rest = n - j - jb;
-    if (rest <= 0) break;
-    float *A21 = Ajj + jb;
-    ZG_TRY(trsm_dev<float>(kRight, kLower, kTrans, kNonUnit, rest, jb, 1.f, Ajj, lda, A21, lda, s));
-    const int ldk = ((jb + 7) / 8) * 8;
-    ZG_TRY(to_kmajor_t(prec, rest, jb, A21, lda, wl, ldk, s, false));
-    ZG_TRY(to_kmajor_t(prec, rest, jb, A21, lda, wu, ldk, s, true));
-    const long ldo = (long)ldk * segs;
-    ZG_TRY(gemm_tc(rest, rest, (int)ldo, -1.f, wl, ldo, wu, ldo, 1.f, A21 + (long)jb * lda, lda,
-                   prec == kPrecFP16 ? 0 : 1, &ctl->status, s, /*tri=*/1));
+    if (rest > 0) {
+      float *A21 = Ajj + jb;
+      ZG_TRY(trsm_dev<float>(kRight, kLower, kTrans, kNonUnit, rest, jb, 1.f, Ajj, lda, A21, lda,
+                             sp));
+      const int ldk = ((jb + 7) / 8) * 8;
+      ZG_TRY(to_kmajor_t(prec, rest, jb, A21, lda, wl, ldk, sp, false));
+      ZG_TRY(to_kmajor_t(prec, rest, jb, A21, lda, wu, ldk, sp, true));
+      const long ldo = (long)ldk * segs;
+      // the next block's columns now, once block b-1's bulk update is done ...
+      if (b >= 1) ZG_CUDA(cudaStreamWaitEvent(sp, la.bulk_done[(b - 1) % R], 0));
+      const int near = std::min(NB, rest);
+      float *C = A21 + (long)jb * lda;  // the trailing matrix
+      ZG_TRY(gemm_tc(near, near, (int)ldo, -1.f, wl, ldo, wu, ldo, 1.f, C, lda, abt,
+                     &ctl->status, sp, /*tri=*/1));
+      if (rest > near) {
+        ZG_TRY(gemm_tc(rest - near, near, (int)ldo, -1.f, wl + (long)near * ldo, ldo, wu, ldo,
+                       1.f, C + near, lda, abt, &ctl->status, sp));
+        // ... the rest on the bulk stream, beside the next block's diagonal
+        // block and triangular solve
+        ZG_CUDA(cudaEventRecord(la.upd[b % R], sp));
+        ZG_CUDA(cudaStreamWaitEvent(sb, la.upd[b % R], 0));
+        ZG_TRY(gemm_tc(rest - near, rest - near, (int)ldo, -1.f, wl + (long)near * ldo, ldo,
+                       wu + (long)near * ldo, ldo, 1.f, C + near + (long)near * lda, lda, abt,
+                       &ctl->status, sb, /*tri=*/1));
+      }
+    }
+    ZG_CUDA(cudaEventRecord(la.bulk_done[b % R], sb));
   }
   return 0;
+}
+
+int potrf_lowp(int n, float *A, long lda, int prec, Control *ctl, cudaStream_t s) {
+  if (n <= 0) return 0;
+  if (prec == kPrecFP32) return potrf_launch<float>(kLower, n, A, lda, ctl, 0, s);
+  Lookahead *la;
+  ZG_TRY(lookahead(s, &la));
+  ZG_CUDA(cudaEventRecord(la->first, s));
+  ZG_CUDA(cudaStreamWaitEvent(la->panel, la->first, 0));
+  ZG_CUDA(cudaStreamWaitEvent(la->bulk, la->first, 0));
+  const int rc = potrf_lowp_blocks(n, A, lda, prec, ctl, s, *la);
+  ZG_CUDA(cudaEventRecord(la->end_panel, la->panel));
+  ZG_CUDA(cudaEventRecord(la->end_bulk, la->bulk));
+  ZG_CUDA(cudaStreamWaitEvent(s, la->end_panel, 0));
+  ZG_CUDA(cudaStreamWaitEvent(s, la->end_bulk, 0));
+  return rc;
 }
 
 // The strict lower triangle mirrored into the upper one (A(j,i) = A(i,j)),
