@@ -121,6 +121,20 @@ enum Slot : int {
 // Returns a device buffer of at least `bytes` bound to `stream` in `slot`.
 int workspace(cudaStream_t stream, int slot, size_t bytes, void **out);
 
+// Streams and events of a blocked factorization's lookahead, one set per
+// (device, caller stream), created on first use and kept: a high-priority
+// panel stream for the critical chain of panels and next-block updates, a
+// low-priority bulk stream for the rest of each trailing update, and the
+// events that order them (kRing in flight).  The LU and Cholesky drivers that
+// use it never run inside one another on the same caller stream.
+struct Lookahead {
+  static constexpr int kRing = 4;
+  cudaStream_t panel = nullptr, bulk = nullptr;
+  cudaEvent_t first = nullptr, upd[kRing] = {}, bulk_done[kRing] = {}, end_panel = nullptr,
+              end_bulk = nullptr;
+};
+int lookahead(cudaStream_t s, Lookahead **out);
+
 // Small per-stream control block: grid-barrier counters and a status word.
 struct Control {
   unsigned int barrier[2];   // arrive counter, generation

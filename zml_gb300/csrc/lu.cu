@@ -415,6 +415,56 @@ static int panel_any(int m, int nb, T *A, long lda, int *ipiv, int ipiv_base, Co
   return panel_lu<T>(m, nb, A, lda, ipiv, ipiv_base, ctl, info_base, s);
 }
 
+// The blocks of getrf_simt.  Lookahead: a block's trailing update is split
+// into the next block's columns (triangular solve and GEMM on the panel
+// stream) and the rest (on the bulk stream), so the bulk of the update runs
+// beside the next block's panel.  Block b's panel waits for block b-2's bulk
+// update, the last to touch its columns; block b's full-width interchanges
+// for block b-1's, which still reads block b-1's L21.  Each element's
+// arithmetic is that of one update over all the columns (the GEMM's tiles and
+// K order do not depend on N; every column of the triangular solve is
+// independent).
+template <typename T>
+static int getrf_simt_blocks(int m, int n, T *A, long lda, int *ipiv, Control *ctl,
+                             Lookahead &la, bool tournament) {
+  constexpr int R = Lookahead::kRing;
+  const cudaStream_t s = la.panel, sb = la.bulk;
+  const int nb = lu_block<T>();
+  const int mn = min(m, n);
+  for (int j = 0, b = 0; j < mn; j += nb, ++b) {
+    const int jb = min(nb, mn - j);
+    T *Ajj = A + j + (long)j * lda;
+    if (b >= 2) ZG_CUDA(cudaStreamWaitEvent(s, la.bulk_done[(b - 2) % R], 0));
+    ZG_TRY(panel_any<T>(m - j, jb, Ajj, lda, ipiv + j, j, ctl, j, s, tournament));
+    if (b >= 1) ZG_CUDA(cudaStreamWaitEvent(s, la.bulk_done[(b - 1) % R], 0));
+    ZG_TRY(laswp_panel<T>(j, std::min(n, j + jb), n, A, lda, j + 1, j + jb, ipiv, s));
+    const int rest = n - j - jb;
+    if (rest > 0) {
+      T *Aright = A + (long)(j + jb) * lda;
+      // the next block's columns now, on the panel stream ...
+      const int near = min(nb, rest);
+      ZG_TRY(trsm_dev<T>(kLeft, kLower, kNoTrans, kUnit, jb, near, T(1), Ajj, lda, Aright + j,
+                         lda, s));
+      if (j + jb < m)
+        ZG_TRY(gemm_simt<T>(kNoTrans, kNoTrans, m - j - jb, near, jb, T(-1), Ajj + jb, lda,
+                            Aright + j, lda, T(1), Aright + j + jb, lda, 0, s));
+      // ... the rest on the bulk stream, beside the next block's panel
+      if (rest > near) {
+        ZG_CUDA(cudaEventRecord(la.upd[b % R], s));
+        ZG_CUDA(cudaStreamWaitEvent(sb, la.upd[b % R], 0));
+        T *Af = Aright + (long)near * lda;
+        ZG_TRY(trsm_dev<T>(kLeft, kLower, kNoTrans, kUnit, jb, rest - near, T(1), Ajj, lda,
+                           Af + j, lda, sb));
+        if (j + jb < m)
+          ZG_TRY(gemm_simt<T>(kNoTrans, kNoTrans, m - j - jb, rest - near, jb, T(-1), Ajj + jb,
+                              lda, Af + j, lda, T(1), Af + j + jb, lda, 0, sb));
+      }
+    }
+    ZG_CUDA(cudaEventRecord(la.bulk_done[b % R], sb));
+  }
+  return 0;
+}
+
 template <typename T>
 int getrf_simt(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t s,
                bool tournament) {
@@ -422,22 +472,19 @@ int getrf_simt(int m, int n, T *A, long lda, int *ipiv, int *info, cudaStream_t 
   if (m <= 0 || n <= 0) return 0;
   Control *ctl;
   ZG_TRY(control(s, &ctl));
-  const int nb = lu_block<T>();
-  const int mn = min(m, n);
-  for (int j = 0; j < mn; j += nb) {
-    const int jb = min(nb, mn - j);
-    T *Ajj = A + j + (long)j * lda;
-    ZG_TRY(panel_any<T>(m - j, jb, Ajj, lda, ipiv + j, j, ctl, j, s, tournament));
-    ZG_TRY(laswp_panel<T>(j, std::min(n, j + jb), n, A, lda, j + 1, j + jb, ipiv, s));
-    if (j + jb < n) {
-      T *Aright = A + (long)(j + jb) * lda;
-      ZG_TRY(trsm_dev<T>(kLeft, kLower, kNoTrans, kUnit, jb, n - j - jb, T(1), Ajj, lda,
-                         Aright + j, lda, s));
-      if (j + jb < m)
-        ZG_TRY(gemm_simt<T>(kNoTrans, kNoTrans, m - j - jb, n - j - jb, jb, T(-1), Ajj + jb, lda,
-                            Aright + j, lda, T(1), Aright + j + jb, lda, 0, s));
-    }
-  }
+  Lookahead *la;
+  ZG_TRY(lookahead(s, &la));
+  // both internal streams start after the caller's earlier work, and the
+  // caller's stream resumes after both (also after a failure part way)
+  ZG_CUDA(cudaEventRecord(la->first, s));
+  ZG_CUDA(cudaStreamWaitEvent(la->panel, la->first, 0));
+  ZG_CUDA(cudaStreamWaitEvent(la->bulk, la->first, 0));
+  const int rc = getrf_simt_blocks<T>(m, n, A, lda, ipiv, ctl, *la, tournament);
+  ZG_CUDA(cudaEventRecord(la->end_panel, la->panel));
+  ZG_CUDA(cudaEventRecord(la->end_bulk, la->bulk));
+  ZG_CUDA(cudaStreamWaitEvent(s, la->end_panel, 0));
+  ZG_CUDA(cudaStreamWaitEvent(s, la->end_bulk, 0));
+  if (rc != 0) return rc;
   return check_status(s, ctl, info);
 }
 

@@ -321,40 +321,6 @@ static int apply_inverse(int k, int cols, const float *Linv, long ldi, float *B,
 // that of block b-1.  The 16-bit operand buffers alternate by block parity.
 
 namespace {
-// Streams and events of the lookahead, one set per (device, caller stream),
-// created on first use and kept.
-struct Lookahead {
-  static constexpr int kRing = 4;
-  cudaStream_t panel = nullptr, bulk = nullptr;
-  cudaEvent_t first = nullptr, upd[kRing] = {}, bulk_done[kRing] = {}, end_panel = nullptr,
-              end_bulk = nullptr;
-};
-std::mutex g_la_mu;
-std::map<std::pair<int, cudaStream_t>, Lookahead> g_la;
-
-int lookahead(cudaStream_t s, Lookahead **out) {
-  int dev = 0;
-  ZG_CUDA(cudaGetDevice(&dev));
-  std::lock_guard<std::mutex> lk(g_la_mu);
-  Lookahead &l = g_la[{dev, s}];
-  if (!l.panel) {
-    int least = 0, greatest = 0;
-    ZG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-    ZG_CUDA(cudaStreamCreateWithPriority(&l.panel, cudaStreamNonBlocking, greatest));
-    ZG_CUDA(cudaStreamCreateWithPriority(&l.bulk, cudaStreamNonBlocking, least));
-    const unsigned fl = cudaEventDisableTiming;
-    ZG_CUDA(cudaEventCreateWithFlags(&l.first, fl));
-    ZG_CUDA(cudaEventCreateWithFlags(&l.end_panel, fl));
-    ZG_CUDA(cudaEventCreateWithFlags(&l.end_bulk, fl));
-    for (int q = 0; q < Lookahead::kRing; ++q) {
-      ZG_CUDA(cudaEventCreateWithFlags(&l.upd[q], fl));
-      ZG_CUDA(cudaEventCreateWithFlags(&l.bulk_done[q], fl));
-    }
-  }
-  *out = &l;
-  return 0;
-}
-
 // A factored while it arrives from pinned host memory: its columns come in
 // chunks on a copy stream, each chunk is converted to FP32 on its own stream
 // and there receives, in order, the updates of the blocks factored before
@@ -366,12 +332,13 @@ struct ChunkStreams {
   cudaEvent_t copied[kMax] = {}, caught[kMax] = {}, copy_end = nullptr;
   std::vector<cudaEvent_t> ops;  // block b's saved operands and pivots are final
 };
+std::mutex g_cs_mu;
 std::map<std::pair<int, cudaStream_t>, ChunkStreams> g_cs;
 
 int chunk_streams(cudaStream_t s, int nblocks, ChunkStreams **out) {
   int dev = 0;
   ZG_CUDA(cudaGetDevice(&dev));
-  std::lock_guard<std::mutex> lk(g_la_mu);
+  std::lock_guard<std::mutex> lk(g_cs_mu);
   ChunkStreams &c = g_cs[{dev, s}];
   const unsigned fl = cudaEventDisableTiming;
   if (!c.copy) {

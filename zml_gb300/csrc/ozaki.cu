@@ -342,52 +342,15 @@ int dgemm_oz_sub(int m, int n, int k, const double *A, long lda, const double *B
 // A22 -= L21 U12 -- nearly all of the flops -- runs on the tensor cores
 // through dgemm_oz_sub, as does the half-panel update (k = 128).  Every wait
 // reports into one status word, read once at the end.
-namespace {
-// Lookahead streams of the slice LU, one set per (device, caller stream),
-// created on first use and kept: a high-priority panel stream and a
-// low-priority bulk stream, with the events that order them.
-struct OzLookahead {
-  static constexpr int kRing = 4;
-  cudaStream_t panel = nullptr, bulk = nullptr;
-  cudaEvent_t first = nullptr, upd[kRing] = {}, bulk_done[kRing] = {}, end_panel = nullptr,
-              end_bulk = nullptr;
-};
-std::mutex g_ozla_mu;
-std::map<std::pair<int, cudaStream_t>, OzLookahead> g_ozla;
-
-int oz_lookahead(cudaStream_t s, OzLookahead **out) {
-  int dev = 0;
-  ZG_CUDA(cudaGetDevice(&dev));
-  std::lock_guard<std::mutex> lk(g_ozla_mu);
-  OzLookahead &l = g_ozla[{dev, s}];
-  if (!l.panel) {
-    int least = 0, greatest = 0;
-    ZG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-    ZG_CUDA(cudaStreamCreateWithPriority(&l.panel, cudaStreamNonBlocking, greatest));
-    ZG_CUDA(cudaStreamCreateWithPriority(&l.bulk, cudaStreamNonBlocking, least));
-    const unsigned fl = cudaEventDisableTiming;
-    ZG_CUDA(cudaEventCreateWithFlags(&l.first, fl));
-    ZG_CUDA(cudaEventCreateWithFlags(&l.end_panel, fl));
-    ZG_CUDA(cudaEventCreateWithFlags(&l.end_bulk, fl));
-    for (int q = 0; q < OzLookahead::kRing; ++q) {
-      ZG_CUDA(cudaEventCreateWithFlags(&l.upd[q], fl));
-      ZG_CUDA(cudaEventCreateWithFlags(&l.bulk_done[q], fl));
-    }
-  }
-  *out = &l;
-  return 0;
-}
-}  // namespace
-
 static int getrf_oz_blocks(int m, int n, double *A, long lda, int *ipiv, Control *ctl,
-                           OzLookahead &la);
+                           Lookahead &la);
 
 int getrf_oz(int m, int n, double *A, long lda, int *ipiv, int *info, cudaStream_t s) {
   *info = 0;
   Control *ctl;
   ZG_TRY(control(s, &ctl));
-  OzLookahead *la;
-  ZG_TRY(oz_lookahead(s, &la));
+  Lookahead *la;
+  ZG_TRY(lookahead(s, &la));
   // both internal streams start after the caller's earlier work, and the
   // caller's stream resumes after both (also after a failure part way)
   ZG_CUDA(cudaEventRecord(la->first, s));
@@ -412,9 +375,9 @@ int getrf_oz(int m, int n, double *A, long lda, int *ipiv, int *info, cudaStream
 // by rows of L21 and by columns of U12, and each column of the triangular
 // solve is independent.
 static int getrf_oz_blocks(int m, int n, double *A, long lda, int *ipiv, Control *ctl,
-                           OzLookahead &la) {
+                           Lookahead &la) {
   constexpr int NB = 256;
-  constexpr int R = OzLookahead::kRing;
+  constexpr int R = Lookahead::kRing;
   const cudaStream_t s = la.panel, sb = la.bulk;
   const int mn = std::min(m, n);
   // sub-panel width: 64 columns.  On GB300 a panel's FP64 arithmetic runs on
@@ -488,9 +451,9 @@ static int getrf_oz_blocks(int m, int n, double *A, long lda, int *ipiv, Control
 // triangular solve wait for block b-2's bulk update, the last to touch their
 // columns; block b's near update waits for block b-1's, which updates the same
 // columns.  The strictly upper triangle is never written.
-static int potrf_oz_blocks(int n, double *A, long lda, Control *ctl, OzLookahead &la) {
+static int potrf_oz_blocks(int n, double *A, long lda, Control *ctl, Lookahead &la) {
   constexpr int NB = 256;
-  constexpr int R = OzLookahead::kRing;
+  constexpr int R = Lookahead::kRing;
   const cudaStream_t sp = la.panel, sb = la.bulk;
   void *wt;
   ZG_TRY(workspace(sp, kSlotOzT, sizeof(double) * NB * NB, &wt));
@@ -533,8 +496,8 @@ int potrf_oz(int n, double *A, long lda, int *info, cudaStream_t s) {
   if (n <= 0) return 0;
   Control *ctl;
   ZG_TRY(control(s, &ctl));
-  OzLookahead *la;
-  ZG_TRY(oz_lookahead(s, &la));
+  Lookahead *la;
+  ZG_TRY(lookahead(s, &la));
   ZG_CUDA(cudaEventRecord(la->first, s));
   ZG_CUDA(cudaStreamWaitEvent(la->panel, la->first, 0));
   ZG_CUDA(cudaStreamWaitEvent(la->bulk, la->first, 0));

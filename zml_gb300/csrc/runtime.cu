@@ -123,6 +123,32 @@ int workspace(cudaStream_t stream, int slot, size_t bytes, void **out) {
   return 0;
 }
 
+static std::mutex g_la_mu;
+static std::map<std::pair<int, cudaStream_t>, Lookahead> g_la;
+
+int lookahead(cudaStream_t s, Lookahead **out) {
+  int dev = 0;
+  ZG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_la_mu);
+  Lookahead &l = g_la[{dev, s}];
+  if (!l.panel) {
+    int least = 0, greatest = 0;
+    ZG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    ZG_CUDA(cudaStreamCreateWithPriority(&l.panel, cudaStreamNonBlocking, greatest));
+    ZG_CUDA(cudaStreamCreateWithPriority(&l.bulk, cudaStreamNonBlocking, least));
+    const unsigned fl = cudaEventDisableTiming;
+    ZG_CUDA(cudaEventCreateWithFlags(&l.first, fl));
+    ZG_CUDA(cudaEventCreateWithFlags(&l.end_panel, fl));
+    ZG_CUDA(cudaEventCreateWithFlags(&l.end_bulk, fl));
+    for (int q = 0; q < Lookahead::kRing; ++q) {
+      ZG_CUDA(cudaEventCreateWithFlags(&l.upd[q], fl));
+      ZG_CUDA(cudaEventCreateWithFlags(&l.bulk_done[q], fl));
+    }
+  }
+  *out = &l;
+  return 0;
+}
+
 int control(cudaStream_t stream, Control **out) {
   std::lock_guard<std::mutex> lk(g_mu);
   int err;
