@@ -62,6 +62,17 @@ def test_dgetrf_rectangular(m, n):
     check_lu(a, lu, ipiv, info)
 
 
+@pytest.mark.parametrize("m,n", [(2600, 2100), (2100, 2600)])
+def test_dgetrf_rectangular_slice_path(m, n):
+    """Rectangular, with a ragged last block, at sizes where the trailing
+    updates run as exact slices on the tensor cores (min(m, n) >= 2048) and
+    the lookahead splits each update into the next block's columns and the
+    rest on two streams."""
+    a = gaussian(m, n, seed=m + n)
+    lu, ipiv, info = gpu_getrf(a)
+    check_lu(a, lu, ipiv, info)
+
+
 def test_dgetrf_padded_lda_and_row_major():
     a = gaussian(150, seed=9)
     lu, ipiv, info = gpu_getrf(a, lda=173)
