@@ -179,7 +179,7 @@ def test_dgetrf_2048_vs_oracle():
 
 
 @pytest.mark.parametrize("uplo", [b"L", b"U"])
-@pytest.mark.parametrize("n", [1, 7, 64, 65, 200, 700])
+@pytest.mark.parametrize("n", [1, 7, 64, 65, 200, 700, 2600])  # 2600: slice updates, ragged
 def test_dpotrf_vs_oracle(uplo, n):
     a = spd(n, seed=n)
     f = a.copy(order="F")
