@@ -144,3 +144,34 @@ def test_pinned_host_below_streaming_scope_equals_device(n, prec):
     rh = solve(Ah.data_ptr(), bh.data_ptr(), xh.data_ptr())
     assert rd.converged == 1 and rh.iters == rd.iters and rh.berr == rd.berr
     assert torch.equal(xh, xd.cpu())
+
+
+def test_streamed_host_solve_singular_matches_device():
+    """A zero column in page-locked A: the streamed factorization records the
+    zero pivot like the device path, refinement is skipped, the FP64 fallback
+    finds the matrix singular too, and both calls report the same."""
+    import torch
+    L = zg.lib()
+    n = 4096
+    g = torch.Generator().manual_seed(7)
+    A = torch.randn(n, n, dtype=torch.float64, generator=g)
+    A[1000, :] = 0.0  # storage row 1000 = column 1000 of the column-major matrix
+    b = torch.rand(n, 1, dtype=torch.float64, generator=g) * 2 - 1
+
+    def solve(a, bb, xx):
+        res = zg.MpirResult()
+        rc = L.zml_dgesv_mpir(102, n, 1, a, n, bb, n, xx, n, BF16X3, GMRES, 64 * 2.0 ** -53, 30,
+                              C.byref(res))
+        return rc, res
+
+    Ad, bd = A.cuda(), b.cuda()
+    xd = torch.zeros(n, 1, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    rcd, rd = solve(Ad.data_ptr(), bd.data_ptr(), xd.data_ptr())
+    Ah, bh = A.pin_memory(), b.pin_memory()
+    xh = torch.zeros(n, 1, dtype=torch.float64).pin_memory()
+    rch, rh = solve(Ah.data_ptr(), bh.data_ptr(), xh.data_ptr())
+    assert rch == rcd
+    assert rh.info == rd.info and rh.info > 0
+    assert rh.fp64_fallback == rd.fp64_fallback
+    assert rh.converged == rd.converged == 0
