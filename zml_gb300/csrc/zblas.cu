@@ -147,13 +147,18 @@ int zgemm_dev(int ta, int tb, int m, int n, int k, const R *alpha, const R *A, l
   const bool notb = tb == kNoTrans || tb == kConjNoTrans;
   const bool cja = ta == kConjNoTrans || ta == kConjTrans;
   const bool cjb = tb == kConjNoTrans || tb == kConjTrans;
+  // FP64 products as exact slices on the tensor cores (as the FP64 LU's
+  // updates), where they apply; they subtract, so the expansion carries -alpha
+  bool slices = false;
+  if constexpr (sizeof(R) == sizeof(double)) slices = fp64_updates_on_tensor_cores(2 * m, n);
+  const R ar = slices ? -alpha[0] : alpha[0], ai = slices ? -alpha[1] : alpha[1];
   void *we;
   ZG_TRY(workspace(s, kSlotZExp, sizeof(R) * 4 * (size_t)m * k, &we));
   R *E = (R *)we;
   const long tot = (long)m * k;
   ZG_LAUNCH(kTagConvert, 0, 2.0 * sizeof(R) * tot + 4.0 * sizeof(R) * tot, s,
             (cexpand_kernel<R, C2><<<grid_for(tot), 256, 0, s>>>(
-                m, k, alpha[0], alpha[1], reinterpret_cast<const C2 *>(A), lda, nota, cja, E)));
+                m, k, ar, ai, reinterpret_cast<const C2 *>(A), lda, nota, cja, E)));
   const R *Bh = B;
   long ldbh = 2 * ldb;
   if (!(notb && !cjb)) {  // op(B) materialized, k x n
@@ -165,6 +170,18 @@ int zgemm_dev(int ta, int tb, int m, int n, int k, const R *alpha, const R *A, l
                   k, n, reinterpret_cast<const C2 *>(B), ldb, notb, cjb, (C2 *)wb)));
     Bh = (const R *)wb;
     ldbh = 2L * k;
+  }
+  if constexpr (sizeof(R) == sizeof(double)) {
+    if (slices) {  // C (2m x n real) -= (-E) op(B), K in chunks of the slices' 256
+      Control *ctl;
+      ZG_TRY(control(s, &ctl));
+      for (int kk = 0; kk < 2 * k; kk += 256) {
+        const int kc = std::min(256, 2 * k - kk);
+        ZG_TRY(dgemm_oz_sub(2 * m, n, kc, E + (long)kk * 2 * m, 2L * m, Bh + kk, ldbh, C, 2 * ldc,
+                            false, &ctl->status, s));
+      }
+      return 0;
+    }
   }
   return gemm_simt<R>(kNoTrans, kNoTrans, 2 * m, n, 2 * k, R(1), E, 2L * m, Bh, ldbh, R(1), C,
                       2 * ldc, 0, s);
