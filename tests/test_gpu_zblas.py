@@ -183,3 +183,31 @@ def test_zgemm_device_pointers():
     zg.lib().cblas_zgemm(102, 111, 111, m, n, k, P(scal(1 + 0j)), dA.data_ptr(), m, dB.data_ptr(),
                          k, P(scal(0j)), dC.data_ptr(), m)
     np.testing.assert_allclose(dC.cpu().numpy().T, A @ B, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("ta,tb", [(111, 111), (113, 112)])
+def test_zgemm_exact_slices_path(ta, tb):
+    """FP64 complex GEMM large enough (min(2m, n) >= 2048) to run as exact
+    slices on the tensor cores, with K = 2 x 300 split into 256, 256 and 88,
+    complex alpha and beta, and transposed / conjugated operands: within the
+    error of an FP64 product of that depth."""
+    import torch
+    m, n, k = 1100, 2100, 300
+    rng = np.random.default_rng(21)
+    opA = cmat((m, k), rng)
+    opB = cmat((k, n), rng)
+    A = opA if ta == 111 else (opA.T if ta == 112 else opA.conj().T)  # stored op^-1(opA)
+    B = opB if tb == 111 else (opB.T if tb == 112 else opB.conj().T)
+    C0 = cmat((m, n), rng)
+    alpha, beta = 0.75 - 0.5j, -0.25 + 1.5j
+    dA = torch.from_numpy(np.ascontiguousarray(A.T)).cuda()  # column-major storage
+    dB = torch.from_numpy(np.ascontiguousarray(B.T)).cuda()
+    dC = torch.from_numpy(np.ascontiguousarray(C0.T)).cuda()
+    torch.cuda.synchronize()
+    zg.lib().cblas_zgemm(102, ta, tb, m, n, k, P(scal(alpha)), dA.data_ptr(), A.shape[0],
+                         dB.data_ptr(), B.shape[0], P(scal(beta)), dC.data_ptr(), m)
+    torch.cuda.synchronize()
+    ref = alpha * (opA @ opB) + beta * C0
+    got = dC.cpu().numpy().T
+    scale = np.abs(alpha) * (np.abs(opA) @ np.abs(opB)) + np.abs(beta) * np.abs(C0)
+    assert (np.abs(got - ref) / scale).max() <= 64 * 2.0 ** -53
